@@ -1,0 +1,291 @@
+/*
+ * yelmo_gpu.h -- C ABI of the GB300 (sm_103a) SSA/DIVA ice-velocity solver.
+ *
+ * Drop-in for Yelmo's velocity-solver entry points:
+ *   calc_velocity_ssa   (src/physics/velocity_ssa.f90:60, called from src/yelmo_dynamics.f90:504)
+ *   calc_velocity_diva  (src/physics/velocity_diva.f90:59, called from src/yelmo_dynamics.f90:630)
+ * and the lower linear-solver seam
+ *   linear_solver_matrix_solve (src/physics/solver_linear.F90:151).
+ *
+ * Conventions (those of Yelmo's own C API, docs/c-api.md:28-36):
+ *   - every array is caller owned, Fortran column-major: 2D fields (nx,ny) with x
+ *     fastest, 3D fields (nx,ny,nz) with k=1 at the ice base;
+ *   - staggered fields share the cell shape: ux(i,j) lives on the right face of
+ *     cell (i,j) (acx), uy(i,j) on its top face (acy), corner (i,j) is top-right;
+ *   - reals are double precision (Fortran real(c_double)), masks are C int;
+ *   - functions return an int status: 0 OK, 2 linear-solve breakdown, 4 linear
+ *     solve hit its iteration limit (the LIS codes of solver_linear.F90:36-39),
+ *     negative values for errors (see YGPU_ERR_*). Nothing here calls exit().
+ */
+#ifndef YELMO_GPU_H
+#define YELMO_GPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define YGPU_OK               0
+#define YGPU_BREAKDOWN        2   /* LGS_BREAKDOWN, solver_linear.F90:38            */
+#define YGPU_MAXITER          4   /* LGS_MAXITER,   solver_linear.F90:39            */
+#define YGPU_ERR_NONFINITE   -1   /* velocity not finite (velocity_general.f90:2114) */
+#define YGPU_ERR_BAD_ARG     -2   /* bad size / option / method code               */
+#define YGPU_ERR_CUDA        -3   /* CUDA runtime error (message: ygpu_last_error)  */
+#define YGPU_ERR_TIMEOUT     -4   /* a device-side wait hit its iteration limit     */
+#define YGPU_ERR_ADMISSION   -5   /* serving: request rejected by the HBM budget    */
+#define YGPU_ERR_NOMEM       -6   /* device allocation failed                       */
+#define YGPU_ERR_BUSY        -7   /* serving: no free slot, try again               */
+
+/* ---- boundary codes: yelmo_tools.f90:14-20 (BND_*), boundary_code() :248 ---- */
+#define YGPU_BND_ZEROS        0
+#define YGPU_BND_INFINITE     1   /* also "mask" */
+#define YGPU_BND_MISMIP3D     2
+#define YGPU_BND_TROUGH       3
+#define YGPU_BND_PERIODIC     4
+#define YGPU_BND_PERIODIC_X   5
+#define YGPU_BND_PERIODIC_Y   6
+
+/* ---- ydyn.ssa_solver ("residual" | "energy"), velocity_ssa.f90:25 ---- */
+#define YGPU_SSA_RESIDUAL     0
+#define YGPU_SSA_ENERGY       1
+
+/* ---- ydyn.ssa_vel_lim_method ("clip" | "drag") ---- */
+#define YGPU_VEL_LIM_CLIP     0
+#define YGPU_VEL_LIM_DRAG     1
+
+/* ---- ydyn.ssa_lat_bc for set_ssa_masks (solver_ssa_ac.f90:985-994) ---- */
+#define YGPU_LATBC_NONE       0
+#define YGPU_LATBC_FLOATING   1
+#define YGPU_LATBC_MARINE     2
+#define YGPU_LATBC_ALL        3
+
+/* ---- LIS option string "-i ... -p ..." (input/yelmo_defaults.nml:160-161) ---- */
+#define YGPU_LIN_CG           0
+#define YGPU_LIN_BICGSTAB     1
+#define YGPU_LIN_MINRES       2
+#define YGPU_PRE_NONE         0
+#define YGPU_PRE_JACOBI       1
+#define YGPU_PRE_ILU0         2   /* GPU: block-ILU(0) on C-grid tiles */
+
+/* ---- arithmetic of the GPU solve ---- */
+#define YGPU_PREC_FP64        0   /* plain FP64 solve: the drop-in                         */
+#define YGPU_PREC_MIXED       1   /* FP32 viscosity/operator/preconditioner/Krylov inside an
+                                     FP64 defect-correction loop                             */
+
+/*
+ * Parameters of one velocity solve. Mirrors ssa_param_class
+ * (velocity_ssa.f90:23-52) and diva_param_class (velocity_diva.f90:22-51), with
+ * the character fields replaced by the codes above and ssa_lis_opt parsed into
+ * the lin_* fields (ygpu_parse_lis_opt).
+ */
+typedef struct ygpu_dyn_par {
+    int    ssa_solver;          /* YGPU_SSA_*                                   */
+    int    boundaries;          /* YGPU_BND_*                                   */
+    int    no_slip;             /* DIVA only: solver = "diva-noslip"            */
+    int    visc_method;         /* 0 const, 1 quadrature nodes, 2 aa-nodes      */
+    double visc_const;          /* [Pa a]                                       */
+    int    beta_method;         /* -1 imposed, 0 const, 1 linear, 2 power, 3 reg. Coulomb, 4/5 centred */
+    double beta_const;          /* [Pa a m-1]                                   */
+    double beta_q;
+    double beta_u0;             /* [m a-1]                                      */
+    int    beta_gl_scale;       /* 0 fraction, 1 H_grnd, 2 zstar, 3 f_grnd      */
+    int    beta_gl_stag;        /* -1 imposed, 0 mean, 1 upstream, 2 downstream, 3 subgrid, 4 flux */
+    double beta_gl_f;
+    double H_grnd_lim;          /* [m]                                          */
+    double beta_min;            /* [Pa a m-1]                                   */
+    double eps_0;               /* [a-1]                                        */
+    int    ssa_vel_lim_method;  /* YGPU_VEL_LIM_*                               */
+    double ssa_vel_lim_tau;     /* [Pa]                                         */
+    double ssa_vel_max;         /* [m a-1]                                      */
+    int    ssa_iter_max;
+    double ssa_iter_rel;
+    double ssa_iter_conv;
+    int    ssa_write_log;       /* print the per-iteration "ssa:" line          */
+    double rho_ice;
+    double rho_sw;
+    double g;
+    /* parsed ssa_lis_opt */
+    int    lin_solver;          /* YGPU_LIN_*                                   */
+    int    lin_precond;         /* YGPU_PRE_*                                   */
+    int    lin_maxiter;
+    double lin_tol;             /* relative residual ||b-Ax||/||b||             */
+    int    lin_initx_zeros;     /* 1: start the Krylov solve from x=0           */
+    /* GPU solve only */
+    int    precision;           /* YGPU_PREC_*                                  */
+    int    inner_maxiter;       /* mixed: FP32 iterations per defect-correction step (0: default) */
+    double inner_tol;           /* mixed: FP32 relative tolerance per step (0: default)          */
+} ygpu_dyn_par;
+
+/* Iteration counters of one solve (ydyn%par%ssa_iter_now etc., yelmo_defs.f90:483-486) */
+typedef struct ygpu_stats {
+    int    ssa_iter_now;        /* Picard iterations done                       */
+    int    ssa_lin_iter;        /* linear iterations, summed over Picard        */
+    int    ssa_lin_fail;        /* linear solves that ended at breakdown/maxiter */
+    int    ssa_lim_n;           /* faces at the velocity limit (count_vel_lim_faces) */
+    double ssa_resid;           /* last Picard L2 relative change               */
+    double lin_resid;           /* last linear relative residual                */
+    int    outer_iter;          /* mixed: defect-correction steps, summed       */
+    int    status;              /* YGPU_* of the solve                          */
+    double device_ms;           /* device time of the solve (CUDA events)       */
+} ygpu_stats;
+
+/* ---- parameter helpers -------------------------------------------------- */
+/* Defaults of input/yelmo_defaults.nml &ydyn (:140-172) and &Earth constants. */
+void ygpu_dyn_par_defaults(ygpu_dyn_par* par);
+/* Parse a LIS option string such as "-i cg -p jacobi -maxiter 200 -tol 1.0e-2
+   -initx_zeros false" into par->lin_*. Returns YGPU_OK or YGPU_ERR_BAD_ARG. */
+int  ygpu_parse_lis_opt(const char* opts, ygpu_dyn_par* par);
+/* boundary_code() of yelmo_tools.f90:248; -1 if not recognised. */
+int  ygpu_boundary_code(const char* boundaries);
+/* Message of the last error on this thread (empty string if none). */
+const char* ygpu_last_error(void);
+/* Library version string. */
+const char* ygpu_version(void);
+
+/*
+ * ygpu_calc_velocity_ssa -- GPU replacement of calc_velocity_ssa
+ * (src/physics/velocity_ssa.f90:60-357). Same arguments in the same order,
+ * with the array extents appended (Fortran assumed shape). Host pointers; the
+ * call copies inputs to the device, runs the whole Picard loop there and copies
+ * the INOUT/OUT fields back. ssa_mask_acx/acy are read (as set by set_ssa_masks).
+ * Returns the status of the last linear solve (0/2/4) or a negative error.
+ */
+int ygpu_calc_velocity_ssa(
+    double* ux_b, double* uy_b, double* taub_acx, double* taub_acy,
+    double* visc_eff, double* visc_eff_int, int* ssa_mask_acx, int* ssa_mask_acy,
+    double* ssa_err_acx, double* ssa_err_acy,
+    int* ssa_iter_now, int* ssa_lin_iter, int* ssa_lin_fail, int* ssa_lim_n,
+    double* beta, double* beta_acx, double* beta_acy,
+    const double* c_bed, const double* f_slide,
+    const double* taud_acx, const double* taud_acy,
+    const double* taul_int_acx, const double* taul_int_acy,
+    const double* H_ice, const double* f_ice, const double* H_grnd, const double* f_grnd,
+    const double* f_grnd_acx, const double* f_grnd_acy,
+    const double* ATT, const double* zeta_aa,
+    const double* z_sl, const double* z_bed, const double* z_srf,
+    double dx, double dy, double n_glen,
+    int nx, int ny, int nz, const ygpu_dyn_par* par);
+
+/*
+ * ygpu_calc_velocity_diva -- GPU replacement of calc_velocity_diva
+ * (src/physics/velocity_diva.f90:59-429), without the optional neff_hook.
+ * Same arguments in the same order, extents appended. c_bed is read only.
+ */
+int ygpu_calc_velocity_diva(
+    double* ux, double* uy, double* ux_bar, double* uy_bar,
+    double* ux_b, double* uy_b, double* ux_i, double* uy_i,
+    double* taub_acx, double* taub_acy,
+    double* beta, double* beta_acx, double* beta_acy, double* beta_eff,
+    double* visc_eff, double* visc_eff_int, double* duxdz, double* duydz,
+    int* ssa_mask_acx, int* ssa_mask_acy, double* ssa_err_acx, double* ssa_err_acy,
+    int* ssa_iter_now, int* ssa_lin_iter, int* ssa_lin_fail, int* ssa_lim_n,
+    const double* c_bed, const double* f_slide,
+    const double* taud_acx, const double* taud_acy,
+    const double* taul_int_acx, const double* taul_int_acy,
+    const double* H_ice, const double* f_ice, const double* H_grnd, const double* f_grnd,
+    const double* f_grnd_acx, const double* f_grnd_acy,
+    const double* ATT, const double* zeta_aa,
+    const double* z_sl, const double* z_bed, const double* z_srf,
+    double dx, double dy, double n_glen,
+    int nx, int ny, int nz, const ygpu_dyn_par* par);
+
+/*
+ * ygpu_set_ssa_masks -- set_ssa_masks (src/physics/solver_ssa_ac.f90:851-943)
+ * on the GPU; integer result, bit-exact. lateral_bc is YGPU_LATBC_*.
+ */
+int ygpu_set_ssa_masks(int* ssa_mask_acx, int* ssa_mask_acy, const int* mask_frnt,
+                       const double* f_ice, const double* f_grnd,
+                       int lateral_bc, int boundaries, int nx, int ny);
+
+/*
+ * ygpu_calc_dyn_inputs -- the fields calc_ydyn builds before the solve, on the
+ * GPU, from H_ice, z_bed, z_sl with a binary ice mask (front_subgrid = "none",
+ * gl_sep = 1):
+ *   f_ice = 1 where H_ice > 0                      (yelmo_topography.f90:1348)
+ *   H_grnd                                         calc_H_grnd, topography.f90:876 (use_f_ice=.FALSE.)
+ *   z_srf                                          calc_z_srf_max, topography.f90:820
+ *   f_grnd, f_grnd_acx, f_grnd_acy                 calc_f_grnd_subgrid_linear, topography.f90:977
+ *   mask_frnt                                      calc_ice_front, topography.f90:724
+ *   dzsdx, dzsdy                                   calc_gradient_acx/acy, yelmo_tools.f90:341,405
+ *   taud_acx, taud_acy                             calc_driving_stress, velocity_general.f90:1118
+ *   taul_int_acx, taul_int_acy                     calc_lateral_bc_stress_2D, velocity_general.f90:1453
+ * The flotation test and every mask are computed in FP64 without contraction
+ * (bit-exact with a CPU evaluation of the same expressions).
+ */
+int ygpu_calc_dyn_inputs(const double* H_ice, const double* z_bed, const double* z_sl,
+                         double* f_ice, double* H_grnd, double* z_srf,
+                         double* f_grnd, double* f_grnd_acx, double* f_grnd_acy,
+                         int* mask_frnt, double* dzsdx, double* dzsdy,
+                         double* taud_acx, double* taud_acy,
+                         double* taul_int_acx, double* taul_int_acy,
+                         double dx, double grad_lim, double taud_lim,
+                         double rho_ice, double rho_sw, double g,
+                         int boundaries, int nx, int ny);
+
+/*
+ * ygpu_linear_solver_matrix_solve -- GPU Krylov solve of a CSR system, the
+ * drop-in for linear_solver_matrix_solve (solver_linear.F90:151-190) with the
+ * linear_solver_class arrays (1-based a_ptr/a_index as Fortran holds them).
+ * x_value is the start vector on entry (unless -initx_zeros true) and the
+ * solution on return. b == 0 gives x = 0 without iterating (:162-174).
+ */
+int ygpu_linear_solver_matrix_solve(int nmax, const int* a_ptr, const int* a_index,
+                                    const double* a_value, const double* b_value,
+                                    double* x_value, const char* lis_opt,
+                                    int* lin_iter, int* status, double* L2_rel_norm);
+
+/* ======================================================================== */
+/* Device-resident API: the solve on fields already in GPU memory.           */
+/* ======================================================================== */
+
+/* Device pointers of one instance (all FP64, same layout as above). Fields the
+   solver kind does not use may be NULL (ux,uy,ux_i,uy_i,duxdz,duydz,beta_eff for
+   SSA). */
+typedef struct ygpu_fields {
+    int nx, ny, nz;
+    double dx, dy, n_glen;
+    /* in/out state */
+    double *ux, *uy, *ux_bar, *uy_bar, *ux_b, *uy_b, *ux_i, *uy_i;
+    double *taub_acx, *taub_acy, *beta, *beta_acx, *beta_acy, *beta_eff;
+    double *visc_eff, *visc_eff_int, *duxdz, *duydz;
+    double *ssa_err_acx, *ssa_err_acy;
+    int    *ssa_mask_acx, *ssa_mask_acy;
+    /* inputs */
+    const double *c_bed, *f_slide, *taud_acx, *taud_acy, *taul_int_acx, *taul_int_acy;
+    const double *H_ice, *f_ice, *H_grnd, *f_grnd, *f_grnd_acx, *f_grnd_acy;
+    const double *ATT, *zeta_aa, *z_sl, *z_bed, *z_srf;
+} ygpu_fields;
+
+typedef struct ygpu_ctx ygpu_ctx;
+
+/* A context owns one CUDA stream and the scratch of its solves. */
+ygpu_ctx* ygpu_ctx_create(int device);
+void      ygpu_ctx_destroy(ygpu_ctx* ctx);
+/* The context's stream, as a cudaStream_t cast to void*. */
+void*     ygpu_ctx_stream(ygpu_ctx* ctx);
+
+/* kind: 0 = SSA (calc_velocity_ssa), 1 = DIVA (calc_velocity_diva). */
+#define YGPU_KIND_SSA   0
+#define YGPU_KIND_DIVA  1
+
+/* One solve on device-resident fields; enqueued on the context stream and
+   synchronised before return (stats filled). */
+int ygpu_solve_device(ygpu_ctx* ctx, int kind, const ygpu_dyn_par* par,
+                      const ygpu_fields* f, ygpu_stats* stats);
+
+/*
+ * Batched solve: n_inst independent instances of uneven size in one persistent
+ * launch. Each instance is solved by a team of CTAs that takes instances from
+ * a device work queue until the queue is empty. stats may be NULL or an array
+ * of n_inst entries.
+ */
+int ygpu_solve_batch_device(ygpu_ctx* ctx, int kind, const ygpu_dyn_par* par,
+                            int n_inst, const ygpu_fields* inst, ygpu_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YELMO_GPU_H */

@@ -1,0 +1,129 @@
+"""Python binding of the CPU oracle (oracle/yelmo_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the yelmo_gb300 package. The oracle is
+an FP64 restatement of the reference solve; see yelmo_oracle.h for what pins it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from yelmo_gb300 import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so with the Makefile beside this file."""
+    if force or not os.path.exists(LIB_PATH) or \
+            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "yelmo_oracle.c")):
+        subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        abi.declare_velocity(L.orc_calc_velocity_ssa, abi.SSA_ARGS)
+        abi.declare_velocity(L.orc_calc_velocity_diva, abi.DIVA_ARGS)
+        abi.declare_inputs(L.orc_calc_dyn_inputs)
+        abi.declare_masks(L.orc_set_ssa_masks)
+        dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
+        L.orc_assemble_csr.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int] + \
+            [dp] * 4 + [dp, ip, ip] + [dp] * 8 + [C.c_int, ip, ip, dp, dp, dp, ip]
+        L.orc_assemble_csr.restype = C.c_int
+        L.orc_linear_solve.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_int, C.c_int, C.c_int,
+                                       C.c_double, C.c_int, ip, dp]
+        L.orc_linear_solve.restype = C.c_int
+        L.orc_set_threads.argtypes = [C.c_int]
+        _lib = L
+    return _lib
+
+
+def set_threads(n: int):
+    lib().orc_set_threads(int(n))
+
+
+def calc_dyn_inputs(inst) -> dict:
+    """Oracle restatement of the fields calc_ydyn builds before the solve."""
+    d = inst.input_buffers()
+    p = inst.par
+    st = abi.call_inputs(lib().orc_calc_dyn_inputs, d, inst.dx, p.grad_lim, p.taud_lim,
+                         p.rho_ice, p.rho_sw, p.g, abi.BOUNDARY_CODES[p.boundaries])
+    assert st == 0
+    return d
+
+
+def set_ssa_masks(mask_frnt, f_ice, f_grnd, lateral_bc: str, boundaries: str):
+    nx, ny = f_ice.shape
+    mx = np.zeros((nx, ny), dtype=np.int32, order="F")
+    my = np.zeros((nx, ny), dtype=np.int32, order="F")
+    lib().orc_set_ssa_masks(abi.ptr(mx, "i"), abi.ptr(my, "i"), abi.ptr(mask_frnt, "i"),
+                            abi.ptr(f_ice, "d"), abi.ptr(f_grnd, "d"),
+                            abi.LATBC_CODES[lateral_bc], abi.BOUNDARY_CODES[boundaries], nx, ny)
+    return mx, my
+
+
+def prepare(inst) -> dict:
+    """Cold-start state of one solve with the oracle's prologue and masks."""
+    inputs = calc_dyn_inputs(inst)
+    f = inst.state(inputs)
+    f["ssa_mask_acx"], f["ssa_mask_acy"] = set_ssa_masks(
+        inputs["mask_frnt"], inputs["f_ice"], inputs["f_grnd"], inst.par.ssa_lat_bc, inst.par.boundaries)
+    return f
+
+
+def calc_velocity(fields: dict, inst, par=None) -> dict:
+    """Run orc_calc_velocity_ssa / _diva on ``fields`` (updated in place)."""
+    par = par or inst.par
+    cpar = par.to_c()
+    if par.solver == "ssa":
+        return abi.call_velocity(lib().orc_calc_velocity_ssa, abi.SSA_ARGS, fields, inst.dx, inst.dx,
+                                 inst.n_glen, cpar)
+    return abi.call_velocity(lib().orc_calc_velocity_diva, abi.DIVA_ARGS, fields, inst.dx, inst.dx,
+                             inst.n_glen, cpar)
+
+
+def assemble_csr(energy: bool, f: dict, dx: float, dy: float, boundaries: str, N_aa=None,
+                 beta_acx=None, beta_acy=None, ux=None, uy=None):
+    """CSR (0-based) of the residual or energy assembler on the given fields."""
+    nx, ny = f["H_ice"].shape
+    n = 2 * nx * ny
+    cap = 64 * n
+    ptr_ = np.zeros(n + 1, dtype=np.int32)
+    idx = np.zeros(cap, dtype=np.int32)
+    val = np.zeros(cap)
+    b = np.zeros(n)
+    x = np.zeros(n)
+    cf = np.zeros(n, dtype=np.int32)
+    g = lambda k: abi.ptr(f[k], "d")
+    nnz = lib().orc_assemble_csr(
+        int(energy), nx, ny, dx, dy, abi.BOUNDARY_CODES[boundaries],
+        abi.ptr(ux if ux is not None else f["ux"], "d"), abi.ptr(uy if uy is not None else f["uy"], "d"),
+        abi.ptr(beta_acx if beta_acx is not None else f["beta_acx"], "d"),
+        abi.ptr(beta_acy if beta_acy is not None else f["beta_acy"], "d"),
+        abi.ptr(N_aa if N_aa is not None else f["N_aa"], "d"),
+        abi.ptr(f["ssa_mask_acx"], "i"), abi.ptr(f["ssa_mask_acy"], "i"),
+        g("H_ice"), g("f_ice"), g("z_bed"), g("z_sl"), g("taud_acx"), g("taud_acy"),
+        g("taul_int_acx"), g("taul_int_acy"), cap, abi.ptr(ptr_, "i"), abi.ptr(idx, "i"),
+        abi.ptr(val, "d"), abi.ptr(b, "d"), abi.ptr(x, "d"), abi.ptr(cf, "i"))
+    if nnz < 0:
+        raise RuntimeError(f"orc_assemble_csr failed ({nnz})")
+    return ptr_, idx[:nnz].copy(), val[:nnz].copy(), b, x, cf
+
+
+def linear_solve(ptr_, idx, val, b, x, method, precond, maxiter, tol, initx_zeros=False):
+    it = C.c_int(0)
+    rr = C.c_double(0.0)
+    st = lib().orc_linear_solve(len(b), abi.ptr(ptr_, "i"), abi.ptr(idx, "i"), abi.ptr(val, "d"),
+                                abi.ptr(b, "d"), abi.ptr(x, "d"), method, precond, maxiter, tol,
+                                int(initx_zeros), C.byref(it), C.byref(rr))
+    return st, it.value, rr.value

@@ -1,0 +1,177 @@
+"""ctypes mirror of ``include/yelmo_gpu.h`` (structs, codes, prototypes).
+
+The C header is the interface; this module only restates its layouts so that
+Python hosts (and the tests) can call the shared library with plain pointers.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+# status codes (yelmo_gpu.h; 0/2/4 are the LIS codes of solver_linear.F90:36-39)
+OK, BREAKDOWN, MAXITER = 0, 2, 4
+ERR_NONFINITE, ERR_BAD_ARG, ERR_CUDA, ERR_TIMEOUT = -1, -2, -3, -4
+ERR_ADMISSION, ERR_NOMEM, ERR_BUSY = -5, -6, -7
+
+STATUS_NAMES = {
+    OK: "ok", BREAKDOWN: "BREAKDOWN", MAXITER: "MAXITER", ERR_NONFINITE: "NONFINITE",
+    ERR_BAD_ARG: "BAD_ARG", ERR_CUDA: "CUDA_ERROR", ERR_TIMEOUT: "TIMEOUT",
+    ERR_ADMISSION: "ADMISSION_REJECTED", ERR_NOMEM: "NOMEM", ERR_BUSY: "BUSY",
+}
+
+# boundary codes, yelmo_tools.f90:14-20 and boundary_code() :248-271
+BOUNDARY_CODES = {
+    "zeros": 0, "infinite": 1, "mask": 1, "MISMIP3D": 2, "TROUGH": 3,
+    "periodic": 4, "periodic-x": 5, "periodic-y": 6,
+}
+LATBC_CODES = {"none": 0, "floating": 1, "float": 1, "marine": 2, "all": 3}
+SSA_SOLVER_CODES = {"residual": 0, "energy": 1}
+VEL_LIM_CODES = {"clip": 0, "drag": 1}
+LIN_CG, LIN_BICGSTAB, LIN_MINRES = 0, 1, 2
+PRE_NONE, PRE_JACOBI, PRE_ILU0 = 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
+KIND_SSA, KIND_DIVA = 0, 1
+
+
+class DynPar(C.Structure):
+    """ygpu_dyn_par: ssa_param_class / diva_param_class + parsed ssa_lis_opt."""
+    _fields_ = [
+        ("ssa_solver", C.c_int), ("boundaries", C.c_int), ("no_slip", C.c_int),
+        ("visc_method", C.c_int), ("visc_const", C.c_double),
+        ("beta_method", C.c_int), ("beta_const", C.c_double), ("beta_q", C.c_double),
+        ("beta_u0", C.c_double), ("beta_gl_scale", C.c_int), ("beta_gl_stag", C.c_int),
+        ("beta_gl_f", C.c_double), ("H_grnd_lim", C.c_double), ("beta_min", C.c_double),
+        ("eps_0", C.c_double), ("ssa_vel_lim_method", C.c_int), ("ssa_vel_lim_tau", C.c_double),
+        ("ssa_vel_max", C.c_double), ("ssa_iter_max", C.c_int), ("ssa_iter_rel", C.c_double),
+        ("ssa_iter_conv", C.c_double), ("ssa_write_log", C.c_int),
+        ("rho_ice", C.c_double), ("rho_sw", C.c_double), ("g", C.c_double),
+        ("lin_solver", C.c_int), ("lin_precond", C.c_int), ("lin_maxiter", C.c_int),
+        ("lin_tol", C.c_double), ("lin_initx_zeros", C.c_int),
+        ("precision", C.c_int), ("inner_maxiter", C.c_int), ("inner_tol", C.c_double),
+    ]
+
+
+class Stats(C.Structure):
+    """ygpu_stats."""
+    _fields_ = [
+        ("ssa_iter_now", C.c_int), ("ssa_lin_iter", C.c_int), ("ssa_lin_fail", C.c_int),
+        ("ssa_lim_n", C.c_int), ("ssa_resid", C.c_double), ("lin_resid", C.c_double),
+        ("outer_iter", C.c_int), ("status", C.c_int), ("device_ms", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class Fields(C.Structure):
+    """ygpu_fields: device pointers of one instance."""
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("dx", C.c_double), ("dy", C.c_double), ("n_glen", C.c_double),
+    ] + [(n, C.c_void_p) for n in (
+        "ux", "uy", "ux_bar", "uy_bar", "ux_b", "uy_b", "ux_i", "uy_i",
+        "taub_acx", "taub_acy", "beta", "beta_acx", "beta_acy", "beta_eff",
+        "visc_eff", "visc_eff_int", "duxdz", "duydz", "ssa_err_acx", "ssa_err_acy",
+        "ssa_mask_acx", "ssa_mask_acy",
+        "c_bed", "f_slide", "taud_acx", "taud_acy", "taul_int_acx", "taul_int_acy",
+        "H_ice", "f_ice", "H_grnd", "f_grnd", "f_grnd_acx", "f_grnd_acy",
+        "ATT", "zeta_aa", "z_sl", "z_bed", "z_srf")]
+
+
+# Argument names of calc_velocity_ssa (velocity_ssa.f90:60) and
+# calc_velocity_diva (velocity_diva.f90:59), in order, with their C type.
+SSA_ARGS = [
+    ("ux_b", "d"), ("uy_b", "d"), ("taub_acx", "d"), ("taub_acy", "d"),
+    ("visc_eff", "d"), ("visc_eff_int", "d"), ("ssa_mask_acx", "i"), ("ssa_mask_acy", "i"),
+    ("ssa_err_acx", "d"), ("ssa_err_acy", "d"),
+    ("ssa_iter_now", "s"), ("ssa_lin_iter", "s"), ("ssa_lin_fail", "s"), ("ssa_lim_n", "s"),
+    ("beta", "d"), ("beta_acx", "d"), ("beta_acy", "d"), ("c_bed", "d"), ("f_slide", "d"),
+    ("taud_acx", "d"), ("taud_acy", "d"), ("taul_int_acx", "d"), ("taul_int_acy", "d"),
+    ("H_ice", "d"), ("f_ice", "d"), ("H_grnd", "d"), ("f_grnd", "d"),
+    ("f_grnd_acx", "d"), ("f_grnd_acy", "d"), ("ATT", "d"), ("zeta_aa", "d"),
+    ("z_sl", "d"), ("z_bed", "d"), ("z_srf", "d"),
+]
+DIVA_ARGS = [
+    ("ux", "d"), ("uy", "d"), ("ux_bar", "d"), ("uy_bar", "d"),
+    ("ux_b", "d"), ("uy_b", "d"), ("ux_i", "d"), ("uy_i", "d"),
+    ("taub_acx", "d"), ("taub_acy", "d"),
+    ("beta", "d"), ("beta_acx", "d"), ("beta_acy", "d"), ("beta_eff", "d"),
+    ("visc_eff", "d"), ("visc_eff_int", "d"), ("duxdz", "d"), ("duydz", "d"),
+    ("ssa_mask_acx", "i"), ("ssa_mask_acy", "i"), ("ssa_err_acx", "d"), ("ssa_err_acy", "d"),
+    ("ssa_iter_now", "s"), ("ssa_lin_iter", "s"), ("ssa_lin_fail", "s"), ("ssa_lim_n", "s"),
+    ("c_bed", "d"), ("f_slide", "d"),
+    ("taud_acx", "d"), ("taud_acy", "d"), ("taul_int_acx", "d"), ("taul_int_acy", "d"),
+    ("H_ice", "d"), ("f_ice", "d"), ("H_grnd", "d"), ("f_grnd", "d"),
+    ("f_grnd_acx", "d"), ("f_grnd_acy", "d"), ("ATT", "d"), ("zeta_aa", "d"),
+    ("z_sl", "d"), ("z_bed", "d"), ("z_srf", "d"),
+]
+INPUT_ARGS = [
+    ("H_ice", "d"), ("z_bed", "d"), ("z_sl", "d"),
+    ("f_ice", "d"), ("H_grnd", "d"), ("z_srf", "d"), ("f_grnd", "d"), ("f_grnd_acx", "d"),
+    ("f_grnd_acy", "d"), ("mask_frnt", "i"), ("dzsdx", "d"), ("dzsdy", "d"),
+    ("taud_acx", "d"), ("taud_acy", "d"), ("taul_int_acx", "d"), ("taul_int_acy", "d"),
+]
+
+
+def _ctype(t):
+    return {"d": _dp, "i": _ip, "s": _ip}[t]
+
+
+def declare_velocity(fn, args):
+    fn.argtypes = [_ctype(t) for _, t in args] + [
+        C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.POINTER(DynPar)]
+    fn.restype = C.c_int
+
+
+def declare_inputs(fn):
+    fn.argtypes = [_ctype(t) for _, t in INPUT_ARGS] + [C.c_double] * 6 + [C.c_int] * 3
+    fn.restype = C.c_int
+
+
+def declare_masks(fn):
+    fn.argtypes = [_ip, _ip, _ip, _dp, _dp, C.c_int, C.c_int, C.c_int, C.c_int]
+    fn.restype = C.c_int
+
+
+def ptr(a: np.ndarray, kind: str):
+    """Pointer to a Fortran-ordered array (checked dtype and contiguity)."""
+    want = np.float64 if kind == "d" else np.int32
+    if a.dtype != want:
+        raise TypeError(f"array of dtype {a.dtype}, expected {want}")
+    if not (a.flags.f_contiguous or a.ndim <= 1):
+        raise TypeError("arrays must be Fortran-contiguous (column-major, x fastest)")
+    return a.ctypes.data_as(_dp if kind == "d" else _ip)
+
+
+def call_velocity(fn, args, fields: dict, dx, dy, n_glen, par: DynPar):
+    """Call a calc_velocity_* style entry with a dict of named numpy arrays.
+
+    Scalars ssa_iter_now etc. are returned in a dict; arrays are updated in place.
+    """
+    nx, ny = fields["H_ice"].shape
+    nz = fields["zeta_aa"].shape[0]
+    scal = {n: C.c_int(0) for n, t in args if t == "s"}
+    cargs = []
+    for n, t in args:
+        if t == "s":
+            cargs.append(C.pointer(scal[n]))
+        else:
+            cargs.append(ptr(fields[n], t))
+    st = fn(*cargs, C.c_double(dx), C.c_double(dy), C.c_double(n_glen),
+            C.c_int(nx), C.c_int(ny), C.c_int(nz), C.byref(par))
+    out = {n: v.value for n, v in scal.items()}
+    out["status"] = int(st)
+    return out
+
+
+def call_inputs(fn, fields: dict, dx, grad_lim, taud_lim, rho_ice, rho_sw, g, bc):
+    nx, ny = fields["H_ice"].shape
+    cargs = [ptr(fields[n], t) for n, t in INPUT_ARGS]
+    return int(fn(*cargs, C.c_double(dx), C.c_double(grad_lim), C.c_double(taud_lim),
+                  C.c_double(rho_ice), C.c_double(rho_sw), C.c_double(g),
+                  C.c_int(bc), C.c_int(nx), C.c_int(ny)))

@@ -1,0 +1,294 @@
+"""Synthetic velocity-solve workloads (seeded, platform independent).
+
+Each builder returns an ``Instance``: the raw fields a Yelmo run would hold
+before calc_ydyn (ice thickness, bed, sea level, rate factor, friction inputs,
+sigma grid) plus the solver parameters. ``Instance.state()`` allocates the
+INOUT fields of calc_velocity_ssa / calc_velocity_diva at their cold-start
+values (ydyn_alloc, src/yelmo_dynamics.f90:1165: visc_eff = 1e3, velocities 0).
+The fields that calc_ydyn derives before the solve (masks, flotation,
+driving and lateral stress) come from ``ygpu_calc_dyn_inputs`` (GPU) or the
+oracle's restatement of it.
+
+Workloads (sizes as the benchmark definitions):
+  dome_ssa        81x81, dx 16 km, grounded dome, imposed beta     (SSA, residual, BiCGSTAB+ILU0)
+  marine_diva     161x161, dx 8 km, nz 10, marine dome with rough bed (DIVA)
+  ensemble_member side n in {41,81,121,161}, 1280 km domain          (batched SSA)
+  continent_diva  801x801, dx 4 km, nz 20, spectral bed, power-law friction (DIVA)
+Any builder takes ``n`` to scale the grid for tests.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .params import YdynParams
+
+T0 = 273.15
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def splitmix64(seed: int, n: int) -> np.ndarray:
+    """n outputs of the splitmix64 generator started at ``seed`` (uint64)."""
+    with np.errstate(over="ignore"):
+        s = np.uint64(seed) + np.uint64(0x9E3779B97F4A7C15) * np.arange(1, n + 1, dtype=np.uint64)
+        z = s
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def uniform01(seed: int, n: int) -> np.ndarray:
+    """Uniform doubles in (0, 1) from the top 53 bits of splitmix64."""
+    return ((splitmix64(seed, n) >> np.uint64(11)).astype(np.float64) + 0.5) * (1.0 / 2.0**53)
+
+
+def normal(seed: int, n: int) -> np.ndarray:
+    """Standard normal deviates (Box-Muller on splitmix64 uniforms)."""
+    m = (n + 1) // 2
+    u = uniform01(seed, 2 * m)
+    r = np.sqrt(-2.0 * np.log(u[:m]))
+    t = 2.0 * np.pi * u[m:]
+    return np.concatenate([r * np.cos(t), r * np.sin(t)])[:n]
+
+
+def gaussian_field(nx, ny, dx, sigma, ell, seed):
+    """Gaussian-correlated noise: white noise filtered with exp(-(r/ell)^2), std sigma."""
+    w = normal(seed, nx * ny).reshape((nx, ny), order="F")
+    kx = np.fft.fftfreq(nx, d=dx) * 2.0 * np.pi
+    ky = np.fft.fftfreq(ny, d=dx) * 2.0 * np.pi
+    k2 = kx[:, None] ** 2 + ky[None, :] ** 2
+    f = np.real(np.fft.ifft2(np.fft.fft2(w) * np.exp(-k2 * ell * ell / 4.0)))
+    f = f - f.mean()
+    sd = f.std()
+    return np.asfortranarray(f * (sigma / sd if sd > 0 else 0.0))
+
+
+def spectral_field(nx, ny, dx, rms, mean, seed, slope=-2.0):
+    """Noise with power spectrum ~ k^slope, given rms and mean."""
+    w = normal(seed, nx * ny).reshape((nx, ny), order="F")
+    kx = np.fft.fftfreq(nx, d=dx)
+    ky = np.fft.fftfreq(ny, d=dx)
+    k = np.sqrt(kx[:, None] ** 2 + ky[None, :] ** 2)
+    k[0, 0] = np.inf
+    f = np.real(np.fft.ifft2(np.fft.fft2(w) * k ** (slope / 2.0)))
+    f = f - f.mean()
+    return np.asfortranarray(mean + f * (rms / f.std()))
+
+
+def calc_zeta(nz: int, scale: str = "exp", zeta_exp: float = 2.0) -> np.ndarray:
+    """zeta_aa of calc_zeta (yelmo_grid.f90:41-121)."""
+    z = np.array([k / (nz - 1) for k in range(nz)], dtype=np.float64)
+    if scale == "exp":
+        z = z ** zeta_exp
+    elif scale == "exp-inv":
+        z = (1.0 - z ** zeta_exp)[::-1].copy()
+    elif scale == "tanh":
+        z = np.tanh(np.pi * (z - 0.5))
+        z = z - z.min()
+        z = z / z.max()
+    return z
+
+
+def rate_factor(T_ice, T_pmp, enh=1.0):
+    """calc_rate_factor (deformation.f90:305-341), Kelvin, n = 3."""
+    Tp = np.clip(T_ice - T_pmp + T0, 220.0, T0)
+    A1 = enh * 1.25671e-05 * np.exp(-60.0e3 / (8.314 * Tp))
+    A2 = enh * 6.0422976e10 * np.exp(-139.0e3 / (8.314 * Tp))
+    return np.where(Tp <= 263.15, A1, A2)
+
+
+def _F(a):
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+@dataclass
+class Instance:
+    """Raw fields of one velocity solve (Fortran-ordered numpy arrays)."""
+    name: str
+    par: YdynParams
+    dx: float
+    H_ice: np.ndarray
+    z_bed: np.ndarray
+    z_sl: np.ndarray
+    ATT: np.ndarray
+    zeta_aa: np.ndarray
+    beta: np.ndarray          # imposed beta on aa-nodes (beta_method = -1), else zeros
+    c_bed: np.ndarray
+    f_slide: np.ndarray
+    n_glen: float = 3.0
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def nx(self):
+        return self.H_ice.shape[0]
+
+    @property
+    def ny(self):
+        return self.H_ice.shape[1]
+
+    @property
+    def nz(self):
+        return self.zeta_aa.shape[0]
+
+    def input_buffers(self) -> dict:
+        """Empty output buffers of ygpu_calc_dyn_inputs, plus the three inputs."""
+        s2 = (self.nx, self.ny)
+        d = {k: np.zeros(s2, order="F") for k in (
+            "f_ice", "H_grnd", "z_srf", "f_grnd", "f_grnd_acx", "f_grnd_acy", "dzsdx", "dzsdy",
+            "taud_acx", "taud_acy", "taul_int_acx", "taul_int_acy")}
+        d["mask_frnt"] = np.zeros(s2, dtype=np.int32, order="F")
+        d["H_ice"], d["z_bed"], d["z_sl"] = self.H_ice, self.z_bed, self.z_sl
+        return d
+
+    def state(self, inputs: dict) -> dict:
+        """All arrays of one calc_velocity_* call, cold start, given the prologue fields."""
+        s2, s3 = (self.nx, self.ny), (self.nx, self.ny, self.nz)
+        f = {}
+        for k in ("ux_b", "uy_b", "ux_bar", "uy_bar", "taub_acx", "taub_acy", "visc_eff_int",
+                  "ssa_err_acx", "ssa_err_acy", "beta_acx", "beta_acy", "beta_eff"):
+            f[k] = np.zeros(s2, order="F")
+        for k in ("ux", "uy", "ux_i", "uy_i", "duxdz", "duydz"):
+            f[k] = np.zeros(s3, order="F")
+        f["visc_eff"] = np.full(s3, 1e3, order="F")
+        f["beta"] = _F(self.beta.copy())
+        f["ssa_mask_acx"] = np.zeros(s2, dtype=np.int32, order="F")
+        f["ssa_mask_acy"] = np.zeros(s2, dtype=np.int32, order="F")
+        for k in ("c_bed", "f_slide", "H_ice", "z_bed", "z_sl", "ATT", "zeta_aa"):
+            f[k] = getattr(self, k)
+        for k in ("taud_acx", "taud_acy", "taul_int_acx", "taul_int_acy", "f_ice", "H_grnd",
+                  "f_grnd", "f_grnd_acx", "f_grnd_acy", "z_srf", "mask_frnt"):
+            f[k] = inputs[k]
+        return f
+
+
+def _lin(lo, hi, n):
+    return np.array([lo + (hi - lo) * i / (n - 1) for i in range(n)])
+
+
+def dome_ssa(n: int = 81, seed: int = 1234, nz: int = 10) -> Instance:
+    """Plain single SSA solve: grounded dome on a flat bed, imposed beta."""
+    dx = 16e3 * 80.0 / (n - 1)
+    x = (np.arange(n) - (n - 1) / 2.0) * dx
+    r = np.sqrt(x[:, None] ** 2 + x[None, :] ** 2)
+    H = 3000.0 * np.sqrt(np.maximum(0.0, 1.0 - (r / 600e3) ** 2))
+    u = uniform01(seed, n * n).reshape((n, n), order="F")
+    beta = 10.0 ** (2.0 + 2.0 * u)            # log-uniform in [1e2, 1e4]
+    zeta = calc_zeta(nz)
+    par = YdynParams(
+        solver="ssa", ssa_solver="residual", visc_method=1, beta_method=-1, beta_gl_stag=1,
+        ssa_iter_max=50, ssa_iter_conv=1e-4,
+        ssa_lis_opt_residual="-i bicgstab -p ilu -maxiter 1000 -tol 1.0e-8 -initx_zeros false",
+        boundaries="zeros")
+    return Instance("dome_ssa", par, dx, _F(H), _F(np.zeros((n, n))), _F(np.zeros((n, n))),
+                    _F(np.full((n, n, nz), 1e-16)), zeta, _F(beta), _F(np.zeros((n, n))),
+                    _F(np.ones((n, n))))
+
+
+def _marine_geometry(n, dx, seed):
+    x = (np.arange(n) - (n - 1) / 2.0) * dx
+    r = np.sqrt(x[:, None] ** 2 + x[None, :] ** 2)
+    L = (n - 1) * dx
+    bed = 200.0 - 1000.0 * (x[:, None] - x[0]) / L + np.zeros((1, n))
+    bed = bed + gaussian_field(n, n, dx, 100.0, 40e3, seed)
+    H = 3500.0 * np.sqrt(np.maximum(0.0, 1.0 - (r / 700e3) ** 2))
+    H = np.where(r > 600e3, 0.0, H)
+    return _F(H), _F(bed)
+
+
+def _temperature_att(H, zeta, Ts=-30.0, Tb=-2.0):
+    """A(T) with T linear in depth from Ts (surface) to Tb (base), homologous."""
+    T = Tb + (Ts - Tb) * zeta[None, None, :] + 0.0 * H[:, :, None]
+    return _F(rate_factor(T0 + T, T0))
+
+
+def marine_diva(n: int = 161, seed: int = 2024, nz: int = 10) -> Instance:
+    """Marine single DIVA solve: dome over a seaward-deepening rough bed."""
+    dx = 8e3 * 160.0 / (n - 1)
+    H, bed = _marine_geometry(n, dx, seed)
+    zeta = calc_zeta(nz)
+    ATT = _temperature_att(H, zeta)
+    u = uniform01(seed + 7, n * n).reshape((n, n), order="F")
+    beta = 10.0 ** (2.0 + 2.0 * u)
+    floating = H < -(1028.0 / 910.0) * bed
+    beta = np.where(floating, 0.0, beta)
+    par = YdynParams(solver="diva", ssa_solver="energy", beta_method=-1, beta_gl_stag=1)
+    return Instance("marine_diva", par, dx, H, bed, _F(np.zeros((n, n))), ATT, zeta, _F(beta),
+                    _F(np.zeros((n, n))), _F(np.ones((n, n))))
+
+
+def ensemble_member(i: int, seed: int = 77, nz: int = 10, sides=(41, 81, 121, 161)) -> Instance:
+    """Member i of the batched ensemble: side drawn from ``sides``, 1280 km domain, SSA."""
+    side = int(sides[int(uniform01(seed + i, 1)[0] * len(sides)) % len(sides)])
+    dx = 1280e3 / (side - 1)
+    H, bed = _marine_geometry(side, dx, seed + i)
+    zeta = calc_zeta(nz)
+    ATT = _temperature_att(H, zeta)
+    u = uniform01(seed + 1000 + i, side * side).reshape((side, side), order="F")
+    beta = np.where(H < -(1028.0 / 910.0) * bed, 0.0, 10.0 ** (2.0 + 2.0 * u))
+    par = YdynParams(solver="ssa", ssa_solver="energy", beta_method=-1, beta_gl_stag=1)
+    return Instance(f"ensemble_{i}", par, dx, H, bed, _F(np.zeros((side, side))), ATT, zeta,
+                    _F(beta), _F(np.zeros((side, side))), _F(np.ones((side, side))))
+
+
+def continent_diva(n: int = 801, seed: int = 4242, nz: int = 20) -> Instance:
+    """Large DIVA solve: spectral bed (~30 % floating), random domes, power-law friction."""
+    dx = 4e3 * 800.0 / (n - 1)
+    bed = spectral_field(n, n, dx, 600.0, -200.0, seed)
+    x = (np.arange(n) - (n - 1) / 2.0) * dx
+    H = np.zeros((n, n))
+    cen = uniform01(seed + 1, 24).reshape(12, 2)
+    rad = uniform01(seed + 2, 12)
+    L = (n - 1) * dx
+    for (cx, cy), rr in zip(cen, rad):
+        x0, y0, R = (cx - 0.5) * 0.6 * L, (cy - 0.5) * 0.6 * L, (0.15 + 0.2 * rr) * L
+        d = np.sqrt((x[:, None] - x0) ** 2 + (x[None, :] - y0) ** 2)
+        H = H + 3000.0 * np.sqrt(np.maximum(0.0, 1.0 - (d / R) ** 2))
+    H = np.minimum(H, 4000.0)
+    zeta = calc_zeta(nz)
+    ATT = _temperature_att(H, zeta, Ts=-25.0, Tb=-1.0)
+    cb = 1e4 * 10.0 ** (uniform01(seed + 3, n * n).reshape((n, n), order="F") - 0.5)
+    par = YdynParams(solver="diva", ssa_solver="energy", beta_method=2, beta_q=1.0 / 3.0,
+                     beta_u0=100.0, beta_gl_stag=1)
+    return Instance("continent_diva", par, dx, _F(H), _F(bed), _F(np.zeros((n, n))), ATT, zeta,
+                    _F(np.zeros((n, n))), _F(cb), _F(np.ones((n, n))))
+
+
+BUILDERS = {
+    "dome_ssa": dome_ssa,
+    "marine_diva": marine_diva,
+    "continent_diva": continent_diva,
+}
+
+
+def radial_shelf(dx_km: float = 10.0, H: float = 400.0, R_s: float = 300e3, L: float = 400e3,
+                 A: float = 1e-18, beta_reg: float = 1e-3, z_bed: float = -2000.0,
+                 nz: int = 10) -> Instance:
+    """A2 radial floating shelf (docs/dev/benchmark-protocol, tests/bench/src/shelf.jl):
+    constant thickness H inside r < R_s on [-L, L]^2, uniform imposed friction beta_reg,
+    par/yelmo_bench_SHELF-R.nml settings (beta_method = beta_gl_stag = -1, lat bc "marine").
+    Exact solution: u = e x, v = e y, e = A S^n 3^(-(n+1)/2), S = rho_i g H (1 - rho_i/rho_w)/2."""
+    dx = dx_km * 1e3
+    n = int(round(2 * L / dx))
+    xc = -L + dx / 2 + dx * np.arange(n)
+    r = np.sqrt(xc[:, None] ** 2 + xc[None, :] ** 2)
+    Hf = np.where(r < R_s, H, 0.0)
+    zeta = calc_zeta(nz)
+    par = YdynParams(solver="diva", ssa_solver="energy", beta_method=-1, beta_gl_stag=-1,
+                     ssa_lat_bc="marine")
+    inst = Instance("radial_shelf", par, dx, _F(Hf), _F(np.full((n, n), z_bed)), _F(np.zeros((n, n))),
+                    _F(np.full((n, n, nz), A)), zeta, _F(np.full((n, n), beta_reg)),
+                    _F(np.zeros((n, n))), _F(np.ones((n, n))))
+    S = 0.5 * par.rho_ice * par.g * H * (1.0 - par.rho_ice / par.rho_sw)
+    inst.extra = {"xc": xc, "strain_rate": A * S ** 3 * 3.0 ** (-2.0), "beta_reg": beta_reg}
+    return inst
+
+
+def shelf_state(inst: Instance, inputs: dict) -> dict:
+    """Cold state of the A2 shelf with the imposed staggered friction (beta_gl_stag = -1)."""
+    f = inst.state(inputs)
+    f["beta_acx"][:] = inst.extra["beta_reg"]
+    f["beta_acy"][:] = inst.extra["beta_reg"]
+    return f
