@@ -1526,6 +1526,11 @@ static int pc_setup(precond_t* P, int n, const int* ptr, const int* idx, const d
             if (P->diag[r] < 0) return YGPU_BREAKDOWN;
         }
         /* ILU(0), IKJ variant (Saad 10.3.2) */
+        /* A pivot that cancels to zero (possible with uniform coefficients and
+           the mixed-sign rows of the residual form) is replaced by the row's
+           original diagonal entry, so the factorization always exists. */
+        double* d0 = malloc((size_t)n * sizeof(double));
+        for (int r = 0; r < n; r++) d0[r] = P->lval[P->diag[r]];
         int* pos = malloc((size_t)n * sizeof(int));
         for (int r = 0; r < n; r++) pos[r] = -1;
         int bad = 0;
@@ -1535,7 +1540,6 @@ static int pc_setup(precond_t* P, int n, const int* ptr, const int* idx, const d
                 int c = P->lidx[k];
                 if (c >= i) break;
                 double piv = P->lval[P->diag[c]];
-                if (piv == 0.0) { bad = 1; break; }
                 double lik = P->lval[k] / piv;
                 P->lval[k] = lik;
                 for (int m = P->diag[c] + 1; m < P->lptr[c + 1]; m++) {
@@ -1544,9 +1548,11 @@ static int pc_setup(precond_t* P, int n, const int* ptr, const int* idx, const d
                 }
             }
             for (int k = P->lptr[i]; k < P->lptr[i + 1]; k++) pos[P->lidx[k]] = -1;
+            if (fabs(P->lval[P->diag[i]]) <= 1e-14 * fabs(d0[i])) P->lval[P->diag[i]] = d0[i];
             if (P->lval[P->diag[i]] == 0.0) bad = 1;
         }
         free(pos);
+        free(d0);
         if (bad) return YGPU_BREAKDOWN;
     }
     return 0;

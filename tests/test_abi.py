@@ -1,0 +1,70 @@
+"""C-ABI checks that need no GPU: the library builds and loads, exports every
+function include/yelmo_gpu.h declares, and its host-side parameter logic
+agrees with the Python mirror and the oracle."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from yelmo_gb300 import abi, gpu
+from yelmo_gb300.params import YdynParams, parse_lis_opt
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    txt = open(os.path.join(ROOT, "include", "yelmo_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(ygpu_\w+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_function():
+    L = gpu.lib()
+    names = header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(L, n), n
+    for n in gpu.EXPORTS:
+        assert n in names
+
+
+def test_version_and_boundary_codes():
+    L = gpu.lib()
+    assert b"sm_103a" in L.ygpu_version()
+    for name, code in abi.BOUNDARY_CODES.items():
+        assert L.ygpu_boundary_code(name.encode()) == code
+    assert L.ygpu_boundary_code(b"nonsense") == -1
+
+
+@pytest.mark.parametrize("opt", [
+    "-i cg -p jacobi -maxiter 200 -tol 1.0e-2 -initx_zeros false",
+    "-i minres -p jacobi -maxiter 100 -tol 1.0e-2 -initx_zeros false",
+    "-i bicgstab -p ilu -maxiter 1000 -tol 1.0e-8 -initx_zeros true",
+    "-i cg -p none -maxiter 5 -tol 1e-12",
+])
+def test_lis_option_parsing_matches_python(opt):
+    L = gpu.lib()
+    p = abi.DynPar()
+    L.ygpu_dyn_par_defaults(C.byref(p))
+    assert L.ygpu_parse_lis_opt(opt.encode(), C.byref(p)) == 0
+    for k, v in parse_lis_opt(opt).items():
+        assert getattr(p, k) == v, k
+
+
+def test_bad_lis_option_rejected():
+    L = gpu.lib()
+    p = abi.DynPar()
+    assert L.ygpu_parse_lis_opt(b"-i gmres -p jacobi", C.byref(p)) == abi.ERR_BAD_ARG
+    assert L.ygpu_parse_lis_opt(b"-i cg -p", C.byref(p)) == abi.ERR_BAD_ARG
+
+
+def test_defaults_match_namelist():
+    L = gpu.lib()
+    p = abi.DynPar()
+    L.ygpu_dyn_par_defaults(C.byref(p))
+    q = YdynParams().to_c()
+    for k, _ in abi.DynPar._fields_:
+        if k in ("no_slip",):
+            continue
+        assert getattr(p, k) == getattr(q, k), k

@@ -1,0 +1,739 @@
+// ygpu_api.cu -- C ABI of libyelmo_gpu.so: parameter helpers, contexts,
+// device-resident solves, and the host-pointer drop-ins for
+// calc_velocity_ssa / calc_velocity_diva / set_ssa_masks / the calc_ydyn
+// prologue / linear_solver_matrix_solve.
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ygpu_common.cuh"
+#include "ygpu_host.h"
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string t_err;
+
+void ygpu_set_error(const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_err = buf;
+}
+
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            ygpu_set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+            return YGPU_ERR_CUDA;                                                        \
+        }                                                                                \
+    } while (0)
+
+extern "C" const char* ygpu_last_error(void) { return t_err.c_str(); }
+extern "C" const char* ygpu_version(void) { return "yelmo_gb300 0.1 (sm_103a)"; }
+
+// ---------------------------------------------------------------------------
+// parameters
+// ---------------------------------------------------------------------------
+extern "C" void ygpu_dyn_par_defaults(ygpu_dyn_par* p) {
+    memset(p, 0, sizeof(*p));
+    p->ssa_solver = YGPU_SSA_ENERGY;
+    p->boundaries = YGPU_BND_ZEROS;
+    p->visc_method = 1;
+    p->visc_const = 1e7;
+    p->beta_method = 1;
+    p->beta_const = 1e3;
+    p->beta_q = 1.0;
+    p->beta_u0 = 100.0;
+    p->beta_gl_scale = 0;
+    p->beta_gl_stag = 1;
+    p->beta_gl_f = 1.0;
+    p->H_grnd_lim = 500.0;
+    p->beta_min = 100.0;
+    p->eps_0 = 1e-6;
+    p->ssa_vel_lim_method = YGPU_VEL_LIM_DRAG;
+    p->ssa_vel_max = 10000.0;
+    p->ssa_vel_lim_tau = 1e5;
+    p->ssa_iter_max = 20;
+    p->ssa_iter_rel = 0.7;
+    p->ssa_iter_conv = 1e-2;
+    p->rho_ice = 910.0;
+    p->rho_sw = 1028.0;
+    p->g = 9.81;
+    p->lin_solver = YGPU_LIN_CG;
+    p->lin_precond = YGPU_PRE_JACOBI;
+    p->lin_maxiter = 200;
+    p->lin_tol = 1e-2;
+    p->lin_initx_zeros = 0;
+    p->precision = YGPU_PREC_FP64;
+}
+
+extern "C" int ygpu_parse_lis_opt(const char* opts, ygpu_dyn_par* p) {
+    if (!opts || !p) return YGPU_ERR_BAD_ARG;
+    std::vector<std::string> tok;
+    const char* s = opts;
+    while (*s) {
+        while (*s == ' ' || *s == '\t') s++;
+        const char* e = s;
+        while (*e && *e != ' ' && *e != '\t') e++;
+        if (e > s) tok.emplace_back(s, e - s);
+        s = e;
+    }
+    if (tok.size() % 2) {
+        ygpu_set_error("LIS option string has an option without value: %s", opts);
+        return YGPU_ERR_BAD_ARG;
+    }
+    for (size_t k = 0; k < tok.size(); k += 2) {
+        const std::string& key = tok[k];
+        const std::string& v = tok[k + 1];
+        if (key == "-i") {
+            if (v == "cg" || v == "1") p->lin_solver = YGPU_LIN_CG;
+            else if (v == "bicgstab" || v == "3") p->lin_solver = YGPU_LIN_BICGSTAB;
+            else if (v == "minres" || v == "5") p->lin_solver = YGPU_LIN_MINRES;
+            else { ygpu_set_error("LIS solver not supported: %s", v.c_str()); return YGPU_ERR_BAD_ARG; }
+        } else if (key == "-p") {
+            if (v == "none" || v == "0") p->lin_precond = YGPU_PRE_NONE;
+            else if (v == "jacobi" || v == "1") p->lin_precond = YGPU_PRE_JACOBI;
+            else if (v == "ilu" || v == "2") p->lin_precond = YGPU_PRE_ILU0;
+            else { ygpu_set_error("LIS preconditioner not supported: %s", v.c_str()); return YGPU_ERR_BAD_ARG; }
+        } else if (key == "-maxiter") {
+            p->lin_maxiter = atoi(v.c_str());
+        } else if (key == "-tol") {
+            p->lin_tol = atof(v.c_str());
+        } else if (key == "-initx_zeros") {
+            p->lin_initx_zeros = (v == "true" || v == "1");
+        }
+    }
+    return YGPU_OK;
+}
+
+extern "C" int ygpu_boundary_code(const char* b) {
+    if (!b) return -1;
+    if (!strcmp(b, "zeros")) return YGPU_BND_ZEROS;
+    if (!strcmp(b, "infinite") || !strcmp(b, "mask")) return YGPU_BND_INFINITE;
+    if (!strcmp(b, "MISMIP3D")) return YGPU_BND_MISMIP3D;
+    if (!strcmp(b, "TROUGH")) return YGPU_BND_TROUGH;
+    if (!strcmp(b, "periodic")) return YGPU_BND_PERIODIC;
+    if (!strcmp(b, "periodic-x")) return YGPU_BND_PERIODIC_X;
+    if (!strcmp(b, "periodic-y")) return YGPU_BND_PERIODIC_Y;
+    return -1;
+}
+
+static int check_par(const ygpu_dyn_par* p) {
+    if (!p) { ygpu_set_error("par is NULL"); return YGPU_ERR_BAD_ARG; }
+    if (p->boundaries < 0 || p->boundaries > 6) { ygpu_set_error("bad boundary code %d", p->boundaries); return YGPU_ERR_BAD_ARG; }
+    if (p->visc_method < 0 || p->visc_method > 2) { ygpu_set_error("visc_method not recognized: %d", p->visc_method); return YGPU_ERR_BAD_ARG; }
+    if (p->beta_method < -1 || p->beta_method > 5) { ygpu_set_error("beta_method not recognized: %d", p->beta_method); return YGPU_ERR_BAD_ARG; }
+    if (p->beta_gl_stag < -1 || p->beta_gl_stag > 4) { ygpu_set_error("beta_gl_stag not recognized: %d", p->beta_gl_stag); return YGPU_ERR_BAD_ARG; }
+    if (p->beta_gl_scale < 0 || p->beta_gl_scale > 3) { ygpu_set_error("beta_gl_scale not recognized: %d", p->beta_gl_scale); return YGPU_ERR_BAD_ARG; }
+    if (p->beta_gl_scale == 0 && (p->beta_gl_f < 0.0 || p->beta_gl_f > 1.0)) { ygpu_set_error("beta_gl_f must be between 0 and 1"); return YGPU_ERR_BAD_ARG; }
+    if (p->beta_gl_scale == 1 && p->H_grnd_lim <= 0.0) { ygpu_set_error("H_grnd_lim must be positive"); return YGPU_ERR_BAD_ARG; }
+    if (p->ssa_solver != YGPU_SSA_RESIDUAL && p->ssa_solver != YGPU_SSA_ENERGY) { ygpu_set_error("bad ssa_solver"); return YGPU_ERR_BAD_ARG; }
+    if (p->ssa_iter_max < 0 || p->lin_maxiter < 0) { ygpu_set_error("negative iteration limit"); return YGPU_ERR_BAD_ARG; }
+    if (!(p->ssa_vel_max > 0.0)) { ygpu_set_error("ssa_vel_max must be positive"); return YGPU_ERR_BAD_ARG; }
+    return YGPU_OK;
+}
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct ygpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    char* arena = nullptr;          // per-instance scratch
+    size_t arena_cap = 0;
+    char* fbuf = nullptr;           // fields of host-pointer calls
+    size_t fbuf_cap = 0;
+    Inst* d_insts = nullptr;
+    int insts_cap = 0;
+    InstOut* d_out = nullptr;
+    int out_cap = 0;
+    TeamCtl* d_ctl = nullptr;
+    int ctl_cap = 0;
+    int* d_misc = nullptr;          // [0] queue, [1] abort, [2..3] csr out
+    double* d_miscd = nullptr;
+    int max_ctas = 0;
+    int csr_max_ctas = 0;
+    int sms = 0;
+    std::vector<Inst> h_insts;
+    std::vector<InstOut> h_out;
+};
+
+static int grow(char** p, size_t* cap, size_t need) {
+    if (*cap >= need) return YGPU_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    if (cudaMalloc((void**)p, need) != cudaSuccess) {
+        cudaGetLastError();
+        ygpu_set_error("device allocation of %zu bytes failed", need);
+        return YGPU_ERR_NOMEM;
+    }
+    *cap = need;
+    return YGPU_OK;
+}
+
+extern "C" ygpu_ctx* ygpu_ctx_create(int device) {
+    ygpu_ctx* c = new ygpu_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&c->e0) != cudaSuccess || cudaEventCreate(&c->e1) != cudaSuccess ||
+        cudaMalloc((void**)&c->d_misc, 64) != cudaSuccess || cudaMalloc((void**)&c->d_miscd, 64) != cudaSuccess) {
+        ygpu_set_error("context creation on device %d failed: %s", device, cudaGetErrorString(cudaGetLastError()));
+        delete c;
+        return nullptr;
+    }
+    // the solver kernel's non-inlined phases need more than the default 1 KB of stack per thread
+    size_t stack = 0;
+    cudaDeviceGetLimit(&stack, cudaLimitStackSize);
+    if (stack < 4096) cudaDeviceSetLimit(cudaLimitStackSize, 4096);
+    c->max_ctas = ygpu_solver_max_ctas(device);
+    c->csr_max_ctas = ygpu_csr_max_ctas(device);
+    c->sms = ygpu_sm_count(device);
+    return c;
+}
+
+extern "C" void ygpu_ctx_destroy(ygpu_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->arena);
+    cudaFree(c->fbuf);
+    cudaFree(c->d_insts);
+    cudaFree(c->d_out);
+    cudaFree(c->d_ctl);
+    cudaFree(c->d_misc);
+    cudaFree(c->d_miscd);
+    if (c->e0) cudaEventDestroy(c->e0);
+    if (c->e1) cudaEventDestroy(c->e1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+extern "C" void* ygpu_ctx_stream(ygpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+// default context of the calling thread (host-pointer entry points)
+static thread_local ygpu_ctx* t_ctx = nullptr;
+static ygpu_ctx* default_ctx() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (t_ctx && t_ctx->device != dev) {
+        ygpu_ctx_destroy(t_ctx);
+        t_ctx = nullptr;
+    }
+    if (!t_ctx) t_ctx = ygpu_ctx_create(dev);
+    return t_ctx;
+}
+
+// ---------------------------------------------------------------------------
+// scratch layout of one instance
+// ---------------------------------------------------------------------------
+static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static size_t inst_scratch_bytes(int nx, int ny, int nz, bool mixed) {
+    size_t n2 = (size_t)nx * ny, nu = 2 * n2, n3 = n2 * nz;
+    size_t b = al(n3 * 8);               // visc_alt
+    b += 16 * al(n2 * 8);                // 2D scratch
+    b += 14 * al(nu * 8);                // linear system
+    b += 6 * al(nu * 4);                 // ukind, emap, mem(3), rpart
+    if (mixed) b += 4 * al(n2 * 4) + 12 * al(nu * 4);
+    return b;
+}
+
+static void inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed) {
+    size_t n2 = (size_t)nx * ny, nu = 2 * n2, n3 = n2 * nz;
+    char* p = base;
+    auto D = [&](size_t n) { double* r = (double*)p; p += al(n * 8); return r; };
+    auto Iv = [&](size_t n) { int* r = (int*)p; p += al(n * 4); return r; };
+    auto Fv = [&](size_t n) { float* r = (float*)p; p += al(n * 4); return r; };
+    I.visc_alt = D(n3);
+    I.ux_nm1 = D(n2); I.uy_nm1 = D(n2); I.bm_x = D(n2); I.bm_y = D(n2);
+    I.lk_x = D(n2); I.lk_y = D(n2); I.lr_x = D(n2); I.lr_y = D(n2);
+    I.F2 = D(n2); I.F2x = D(n2); I.F2y = D(n2); I.Nab = D(n2);
+    I.tbp_x = D(n2); I.tbp_y = D(n2); I.drag_x = D(n2); I.drag_y = D(n2);
+    I.x = D(nu); I.b = D(nu); I.r = D(nu); I.p = D(nu); I.q = D(nu); I.z = D(nu); I.dinv = D(nu);
+    I.rt = D(nu); I.v = D(nu); I.s = D(nu); I.t = D(nu); I.ph = D(nu); I.sh = D(nu); I.dval = D(nu);
+    I.ukind = Iv(nu); I.emap = Iv(nu); I.mem = Iv(3 * nu); I.rpart = Iv(nu);
+    if (mixed) {
+        I.fN = Fv(n2); I.fNab = Fv(n2); I.fdrag_x = Fv(n2); I.fdrag_y = Fv(n2);
+        I.fdinv = Fv(nu); I.fx = Fv(nu); I.fr = Fv(nu); I.fp = Fv(nu); I.fq = Fv(nu); I.fz = Fv(nu);
+        I.frt = Fv(nu); I.fv = Fv(nu); I.fs = Fv(nu); I.ft = Fv(nu); I.fph = Fv(nu); I.fsh = Fv(nu);
+    } else {
+        I.fN = I.fNab = I.fdrag_x = I.fdrag_y = I.fdinv = nullptr;
+        I.fx = I.fr = I.fp = I.fq = I.fz = I.frt = I.fv = I.fs = I.ft = I.fph = I.fsh = nullptr;
+    }
+}
+
+static int fields_check(int kind, const ygpu_fields* f) {
+    if (!f) { ygpu_set_error("fields is NULL"); return YGPU_ERR_BAD_ARG; }
+    if (f->nx < 3 || f->ny < 3 || f->nz < 2) {
+        ygpu_set_error("grid too small: nx=%d ny=%d nz=%d (need nx,ny >= 3, nz >= 2)", f->nx, f->ny, f->nz);
+        return YGPU_ERR_BAD_ARG;
+    }
+    if ((size_t)f->nx * f->ny > (size_t)(1 << 29)) { ygpu_set_error("grid too large"); return YGPU_ERR_BAD_ARG; }
+    if (!(f->dx > 0.0) || !(f->dy > 0.0) || !(f->n_glen > 0.0)) { ygpu_set_error("dx, dy and n_glen must be positive"); return YGPU_ERR_BAD_ARG; }
+    const void* need[] = {f->taub_acx, f->taub_acy, f->beta, f->beta_acx, f->beta_acy, f->visc_eff, f->visc_eff_int,
+                          f->ssa_err_acx, f->ssa_err_acy, f->ssa_mask_acx, f->ssa_mask_acy, f->c_bed, f->f_slide,
+                          f->taud_acx, f->taud_acy, f->taul_int_acx, f->taul_int_acy, f->H_ice, f->f_ice, f->H_grnd,
+                          f->f_grnd, f->f_grnd_acx, f->f_grnd_acy, f->ATT, f->zeta_aa, f->z_sl, f->z_bed,
+                          f->ux_b, f->uy_b};
+    for (const void* q : need)
+        if (!q) { ygpu_set_error("a required field pointer is NULL"); return YGPU_ERR_BAD_ARG; }
+    if (kind == YGPU_KIND_DIVA) {
+        const void* nd[] = {f->ux, f->uy, f->ux_bar, f->uy_bar, f->ux_i, f->uy_i, f->beta_eff, f->duxdz, f->duydz};
+        for (const void* q : nd)
+            if (!q) { ygpu_set_error("a DIVA field pointer is NULL"); return YGPU_ERR_BAD_ARG; }
+    }
+    return YGPU_OK;
+}
+
+static void fill_inst(Inst& I, int kind, const ygpu_fields* f) {
+    memset(&I, 0, sizeof(I));
+    I.nx = f->nx; I.ny = f->ny; I.nz = f->nz; I.n2 = f->nx * f->ny; I.nu = 2 * I.n2;
+    I.kind = kind;
+    I.dx = f->dx; I.dy = f->dy; I.n_glen = f->n_glen;
+    if (kind == YGPU_KIND_DIVA) {
+        I.u_x = f->ux_bar; I.u_y = f->uy_bar;
+        I.ux3 = f->ux; I.uy3 = f->uy; I.ux_i = f->ux_i; I.uy_i = f->uy_i;
+        I.duxdz = f->duxdz; I.duydz = f->duydz; I.beta_eff = f->beta_eff;
+    } else {
+        I.u_x = f->ux_b; I.u_y = f->uy_b;
+    }
+    I.ux_b = f->ux_b; I.uy_b = f->uy_b;
+    I.taub_x = f->taub_acx; I.taub_y = f->taub_acy;
+    I.beta = f->beta; I.beta_x = f->beta_acx; I.beta_y = f->beta_acy;
+    I.visc = f->visc_eff; I.visc_int = f->visc_eff_int;
+    I.err_x = f->ssa_err_acx; I.err_y = f->ssa_err_acy;
+    I.mask_x = f->ssa_mask_acx; I.mask_y = f->ssa_mask_acy;
+    I.c_bed = f->c_bed; I.f_slide = f->f_slide;
+    I.taud_x = f->taud_acx; I.taud_y = f->taud_acy; I.taul_x = f->taul_int_acx; I.taul_y = f->taul_int_acy;
+    I.H = f->H_ice; I.f_ice = f->f_ice; I.H_grnd = f->H_grnd; I.f_grnd = f->f_grnd;
+    I.fg_x = f->f_grnd_acx; I.fg_y = f->f_grnd_acy; I.ATT = f->ATT; I.zeta = f->zeta_aa;
+    I.z_sl = f->z_sl; I.z_bed = f->z_bed;
+}
+
+static int env_int(const char* name, int dflt) {
+    const char* v = getenv(name);
+    return (v && *v) ? atoi(v) : dflt;
+}
+
+// Launch shape of a batch: (n_teams, team_ctas).
+static void choose_teams(const ygpu_ctx* c, int n_inst, size_t max_nu, int* n_teams, int* team_ctas) {
+    int maxc = c->max_ctas > 0 ? c->max_ctas : 1;
+    if (n_inst == 1) {
+        // one team over the GPU, sized to the instance
+        int want = (int)((max_nu + 2 * YG_BLOCK - 1) / (2 * YG_BLOCK));
+        int tc = env_int("YGPU_TEAM_CTAS", want);
+        if (tc < 1) tc = 1;
+        if (tc > maxc) tc = maxc;
+        if (tc > YG_MAX_TEAM_CTAS) tc = YG_MAX_TEAM_CTAS;
+        *team_ctas = tc;
+        *n_teams = 1;
+        return;
+    }
+    int tc = env_int("YGPU_BATCH_TEAM_CTAS", 1);
+    if (tc < 1) tc = 1;
+    if (tc > maxc) tc = maxc;
+    int nt = maxc / tc;
+    if (nt > n_inst) nt = n_inst;
+    if (nt < 1) nt = 1;
+    *team_ctas = tc;
+    *n_teams = nt;
+}
+
+static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, const ygpu_fields* inst,
+                       ygpu_stats* stats) {
+    int st = check_par(par);
+    if (st) return st;
+    if (kind != YGPU_KIND_SSA && kind != YGPU_KIND_DIVA) { ygpu_set_error("bad solver kind %d", kind); return YGPU_ERR_BAD_ARG; }
+    if (n < 1) { ygpu_set_error("no instances"); return YGPU_ERR_BAD_ARG; }
+    for (int k = 0; k < n; k++)
+        if ((st = fields_check(kind, &inst[k]))) return st;
+    CK(cudaSetDevice(c->device));
+    const bool mixed = (par->precision == YGPU_PREC_MIXED);
+    std::vector<size_t> off(n);
+    size_t total = 0, max_nu = 0;
+    for (int k = 0; k < n; k++) {
+        off[k] = total;
+        total += al(inst_scratch_bytes(inst[k].nx, inst[k].ny, inst[k].nz, mixed));
+        max_nu = std::max(max_nu, (size_t)2 * inst[k].nx * inst[k].ny);
+    }
+    if ((st = grow(&c->arena, &c->arena_cap, total))) return st;
+    if (c->insts_cap < n) {
+        cudaFree(c->d_insts);
+        cudaFree(c->d_out);
+        c->d_insts = nullptr;
+        c->d_out = nullptr;
+        CK(cudaMalloc((void**)&c->d_insts, sizeof(Inst) * (size_t)n));
+        CK(cudaMalloc((void**)&c->d_out, sizeof(InstOut) * (size_t)n));
+        c->insts_cap = n;
+    }
+    int n_teams, team_ctas;
+    choose_teams(c, n, max_nu, &n_teams, &team_ctas);
+    if (c->ctl_cap < n_teams) {
+        cudaFree(c->d_ctl);
+        c->d_ctl = nullptr;
+        CK(cudaMalloc((void**)&c->d_ctl, sizeof(TeamCtl) * (size_t)n_teams));
+        c->ctl_cap = n_teams;
+    }
+    c->h_insts.resize(n);
+    for (int k = 0; k < n; k++) {
+        Inst& I = c->h_insts[k];
+        fill_inst(I, kind, &inst[k]);
+        inst_scratch_carve(I, c->arena + off[k], inst[k].nx, inst[k].ny, inst[k].nz, mixed);
+        I.out = c->d_out + k;
+    }
+    CK(cudaMemcpyAsync(c->d_insts, c->h_insts.data(), sizeof(Inst) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->d_out, 0, sizeof(InstOut) * (size_t)n, c->stream));
+    CK(cudaEventRecord(c->e0, c->stream));
+    st = ygpu_launch_solver(c->device, c->stream, c->d_insts, n, *par, c->d_ctl, n_teams, team_ctas, c->d_misc,
+                            c->d_misc + 1);
+    if (st) return st;
+    CK(cudaEventRecord(c->e1, c->stream));
+    c->h_out.resize(n);
+    CK(cudaMemcpyAsync(c->h_out.data(), c->d_out, sizeof(InstOut) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    int abort_flag = 0;
+    CK(cudaMemcpyAsync(&abort_flag, c->d_misc + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->e0, c->e1);
+    int worst = YGPU_OK;
+    for (int k = 0; k < n; k++) {
+        const InstOut& o = c->h_out[k];
+        int s_k = abort_flag ? YGPU_ERR_TIMEOUT : o.status;
+        if (stats) {
+            ygpu_stats& S = stats[k];
+            S.ssa_iter_now = o.iter_now;
+            S.ssa_lin_iter = o.lin_iter;
+            S.ssa_lin_fail = o.lin_fail;
+            S.ssa_lim_n = o.lim_n;
+            S.ssa_resid = o.resid;
+            S.lin_resid = o.lin_resid;
+            S.outer_iter = o.outer_iter;
+            S.status = s_k;
+            S.device_ms = ms;
+        }
+        if (s_k < 0 && (worst >= 0 || s_k < worst)) worst = s_k;
+        else if (worst >= 0 && s_k > worst) worst = s_k;
+    }
+    if (abort_flag) ygpu_set_error("a device-side wait hit its iteration limit (team barrier timeout)");
+    return worst;
+}
+
+extern "C" int ygpu_solve_device(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, const ygpu_fields* f,
+                                 ygpu_stats* stats) {
+    if (!c) { ygpu_set_error("context is NULL"); return YGPU_ERR_BAD_ARG; }
+    return solve_batch(c, kind, par, 1, f, stats);
+}
+
+extern "C" int ygpu_solve_batch_device(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n_inst,
+                                       const ygpu_fields* inst, ygpu_stats* stats) {
+    if (!c) { ygpu_set_error("context is NULL"); return YGPU_ERR_BAD_ARG; }
+    return solve_batch(c, kind, par, n_inst, inst, stats);
+}
+
+// ---------------------------------------------------------------------------
+// host-pointer drop-ins
+// ---------------------------------------------------------------------------
+namespace {
+struct HostArg {
+    void* host;          // host pointer
+    size_t bytes;
+    bool in, out;
+    void* dev;
+};
+
+struct Staging {
+    std::vector<HostArg> args;
+    size_t add(void* h, size_t bytes, bool in, bool out) {
+        args.push_back({h, bytes, in, out, nullptr});
+        return args.size() - 1;
+    }
+    int upload(ygpu_ctx* c) {
+        size_t tot = 0;
+        for (auto& a : args) tot += al(a.bytes);
+        int st = grow(&c->fbuf, &c->fbuf_cap, tot);
+        if (st) return st;
+        char* p = c->fbuf;
+        for (auto& a : args) {
+            a.dev = p;
+            p += al(a.bytes);
+            if (a.in) CK(cudaMemcpyAsync(a.dev, a.host, a.bytes, cudaMemcpyHostToDevice, c->stream));
+        }
+        return YGPU_OK;
+    }
+    int download(ygpu_ctx* c) {
+        for (auto& a : args)
+            if (a.out) CK(cudaMemcpyAsync(a.host, a.dev, a.bytes, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        return YGPU_OK;
+    }
+};
+}  // namespace
+
+static bool any_null(std::initializer_list<const void*> ps) {
+    for (const void* p : ps)
+        if (!p) return true;
+    return false;
+}
+
+extern "C" int ygpu_calc_velocity_ssa(double* ux_b, double* uy_b, double* taub_acx, double* taub_acy,
+                                      double* visc_eff, double* visc_eff_int, int* ssa_mask_acx, int* ssa_mask_acy,
+                                      double* ssa_err_acx, double* ssa_err_acy, int* ssa_iter_now, int* ssa_lin_iter,
+                                      int* ssa_lin_fail, int* ssa_lim_n, double* beta, double* beta_acx,
+                                      double* beta_acy, const double* c_bed, const double* f_slide,
+                                      const double* taud_acx, const double* taud_acy, const double* taul_int_acx,
+                                      const double* taul_int_acy, const double* H_ice, const double* f_ice,
+                                      const double* H_grnd, const double* f_grnd, const double* f_grnd_acx,
+                                      const double* f_grnd_acy, const double* ATT, const double* zeta_aa,
+                                      const double* z_sl, const double* z_bed, const double* z_srf, double dx,
+                                      double dy, double n_glen, int nx, int ny, int nz, const ygpu_dyn_par* par) {
+    if (nx < 3 || ny < 3 || nz < 2) { ygpu_set_error("grid too small: nx=%d ny=%d nz=%d", nx, ny, nz); return YGPU_ERR_BAD_ARG; }
+    if (any_null({ux_b, uy_b, taub_acx, taub_acy, visc_eff, visc_eff_int, ssa_mask_acx, ssa_mask_acy, ssa_err_acx,
+                  ssa_err_acy, ssa_iter_now, ssa_lin_iter, ssa_lin_fail, ssa_lim_n, beta, beta_acx, beta_acy, c_bed,
+                  f_slide, taud_acx, taud_acy, taul_int_acx, taul_int_acy, H_ice, f_ice, H_grnd, f_grnd, f_grnd_acx,
+                  f_grnd_acy, ATT, zeta_aa, z_sl, z_bed, z_srf})) {
+        ygpu_set_error("NULL argument");
+        return YGPU_ERR_BAD_ARG;
+    }
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const size_t b2 = (size_t)nx * ny * 8, b3 = b2 * nz, i2 = (size_t)nx * ny * 4;
+    Staging S;
+    size_t a_uxb = S.add(ux_b, b2, 1, 1), a_uyb = S.add(uy_b, b2, 1, 1);
+    size_t a_tbx = S.add(taub_acx, b2, 1, 1), a_tby = S.add(taub_acy, b2, 1, 1);
+    size_t a_v = S.add(visc_eff, b3, 1, 1), a_vi = S.add(visc_eff_int, b2, 0, 1);
+    size_t a_mx = S.add(ssa_mask_acx, i2, 1, 0), a_my = S.add(ssa_mask_acy, i2, 1, 0);
+    size_t a_ex = S.add(ssa_err_acx, b2, 0, 1), a_ey = S.add(ssa_err_acy, b2, 0, 1);
+    size_t a_b = S.add(beta, b2, 1, 1), a_bx = S.add(beta_acx, b2, 1, 1), a_by = S.add(beta_acy, b2, 1, 1);
+    size_t a_cb = S.add((void*)c_bed, b2, 1, 0), a_fs = S.add((void*)f_slide, b2, 1, 0);
+    size_t a_tdx = S.add((void*)taud_acx, b2, 1, 0), a_tdy = S.add((void*)taud_acy, b2, 1, 0);
+    size_t a_tlx = S.add((void*)taul_int_acx, b2, 1, 0), a_tly = S.add((void*)taul_int_acy, b2, 1, 0);
+    size_t a_H = S.add((void*)H_ice, b2, 1, 0), a_fi = S.add((void*)f_ice, b2, 1, 0);
+    size_t a_hg = S.add((void*)H_grnd, b2, 1, 0), a_fg = S.add((void*)f_grnd, b2, 1, 0);
+    size_t a_fgx = S.add((void*)f_grnd_acx, b2, 1, 0), a_fgy = S.add((void*)f_grnd_acy, b2, 1, 0);
+    size_t a_att = S.add((void*)ATT, b3, 1, 0), a_z = S.add((void*)zeta_aa, (size_t)nz * 8, 1, 0);
+    size_t a_zsl = S.add((void*)z_sl, b2, 1, 0), a_zb = S.add((void*)z_bed, b2, 1, 0);
+    size_t a_zs = S.add((void*)z_srf, b2, 1, 0);
+    int st = S.upload(c);
+    if (st) return st;
+    auto d = [&](size_t k) { return (double*)S.args[k].dev; };
+    ygpu_fields f;
+    memset(&f, 0, sizeof(f));
+    f.nx = nx; f.ny = ny; f.nz = nz; f.dx = dx; f.dy = dy; f.n_glen = n_glen;
+    f.ux_b = d(a_uxb); f.uy_b = d(a_uyb); f.taub_acx = d(a_tbx); f.taub_acy = d(a_tby);
+    f.visc_eff = d(a_v); f.visc_eff_int = d(a_vi);
+    f.ssa_mask_acx = (int*)S.args[a_mx].dev; f.ssa_mask_acy = (int*)S.args[a_my].dev;
+    f.ssa_err_acx = d(a_ex); f.ssa_err_acy = d(a_ey);
+    f.beta = d(a_b); f.beta_acx = d(a_bx); f.beta_acy = d(a_by);
+    f.c_bed = d(a_cb); f.f_slide = d(a_fs); f.taud_acx = d(a_tdx); f.taud_acy = d(a_tdy);
+    f.taul_int_acx = d(a_tlx); f.taul_int_acy = d(a_tly); f.H_ice = d(a_H); f.f_ice = d(a_fi);
+    f.H_grnd = d(a_hg); f.f_grnd = d(a_fg); f.f_grnd_acx = d(a_fgx); f.f_grnd_acy = d(a_fgy);
+    f.ATT = d(a_att); f.zeta_aa = d(a_z); f.z_sl = d(a_zsl); f.z_bed = d(a_zb); f.z_srf = d(a_zs);
+    ygpu_stats sts;
+    memset(&sts, 0, sizeof(sts));
+    st = solve_batch(c, YGPU_KIND_SSA, par, 1, &f, &sts);
+    if (st == YGPU_ERR_CUDA || st == YGPU_ERR_NOMEM || st == YGPU_ERR_BAD_ARG) return st;
+    int st2 = S.download(c);
+    if (st2) return st2;
+    *ssa_iter_now = sts.ssa_iter_now;
+    *ssa_lin_iter = sts.ssa_lin_iter;
+    *ssa_lin_fail = sts.ssa_lin_fail;
+    *ssa_lim_n = sts.ssa_lim_n;
+    return st;
+}
+
+extern "C" int ygpu_calc_velocity_diva(double* ux, double* uy, double* ux_bar, double* uy_bar, double* ux_b,
+                                       double* uy_b, double* ux_i, double* uy_i, double* taub_acx, double* taub_acy,
+                                       double* beta, double* beta_acx, double* beta_acy, double* beta_eff,
+                                       double* visc_eff, double* visc_eff_int, double* duxdz, double* duydz,
+                                       int* ssa_mask_acx, int* ssa_mask_acy, double* ssa_err_acx,
+                                       double* ssa_err_acy, int* ssa_iter_now, int* ssa_lin_iter, int* ssa_lin_fail,
+                                       int* ssa_lim_n, const double* c_bed, const double* f_slide,
+                                       const double* taud_acx, const double* taud_acy, const double* taul_int_acx,
+                                       const double* taul_int_acy, const double* H_ice, const double* f_ice,
+                                       const double* H_grnd, const double* f_grnd, const double* f_grnd_acx,
+                                       const double* f_grnd_acy, const double* ATT, const double* zeta_aa,
+                                       const double* z_sl, const double* z_bed, const double* z_srf, double dx,
+                                       double dy, double n_glen, int nx, int ny, int nz, const ygpu_dyn_par* par) {
+    if (nx < 3 || ny < 3 || nz < 2) { ygpu_set_error("grid too small: nx=%d ny=%d nz=%d", nx, ny, nz); return YGPU_ERR_BAD_ARG; }
+    if (any_null({ux, uy, ux_bar, uy_bar, ux_b, uy_b, ux_i, uy_i, taub_acx, taub_acy, beta, beta_acx, beta_acy,
+                  beta_eff, visc_eff, visc_eff_int, duxdz, duydz, ssa_mask_acx, ssa_mask_acy, ssa_err_acx,
+                  ssa_err_acy, ssa_iter_now, ssa_lin_iter, ssa_lin_fail, ssa_lim_n, c_bed, f_slide, taud_acx,
+                  taud_acy, taul_int_acx, taul_int_acy, H_ice, f_ice, H_grnd, f_grnd, f_grnd_acx, f_grnd_acy, ATT,
+                  zeta_aa, z_sl, z_bed, z_srf})) {
+        ygpu_set_error("NULL argument");
+        return YGPU_ERR_BAD_ARG;
+    }
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const size_t b2 = (size_t)nx * ny * 8, b3 = b2 * nz, i2 = (size_t)nx * ny * 4;
+    Staging S;
+    size_t a_ux = S.add(ux, b3, 0, 1), a_uy = S.add(uy, b3, 0, 1);
+    size_t a_uxbar = S.add(ux_bar, b2, 1, 1), a_uybar = S.add(uy_bar, b2, 1, 1);
+    size_t a_uxb = S.add(ux_b, b2, 1, 1), a_uyb = S.add(uy_b, b2, 1, 1);
+    size_t a_uxi = S.add(ux_i, b3, 0, 1), a_uyi = S.add(uy_i, b3, 0, 1);
+    size_t a_tbx = S.add(taub_acx, b2, 1, 1), a_tby = S.add(taub_acy, b2, 1, 1);
+    size_t a_b = S.add(beta, b2, 1, 1), a_bx = S.add(beta_acx, b2, 1, 1), a_by = S.add(beta_acy, b2, 1, 1);
+    size_t a_be = S.add(beta_eff, b2, 0, 1);
+    size_t a_v = S.add(visc_eff, b3, 1, 1), a_vi = S.add(visc_eff_int, b2, 0, 1);
+    size_t a_dx = S.add(duxdz, b3, 0, 1), a_dy = S.add(duydz, b3, 0, 1);
+    size_t a_mx = S.add(ssa_mask_acx, i2, 1, 0), a_my = S.add(ssa_mask_acy, i2, 1, 0);
+    size_t a_ex = S.add(ssa_err_acx, b2, 0, 1), a_ey = S.add(ssa_err_acy, b2, 0, 1);
+    size_t a_cb = S.add((void*)c_bed, b2, 1, 0), a_fs = S.add((void*)f_slide, b2, 1, 0);
+    size_t a_tdx = S.add((void*)taud_acx, b2, 1, 0), a_tdy = S.add((void*)taud_acy, b2, 1, 0);
+    size_t a_tlx = S.add((void*)taul_int_acx, b2, 1, 0), a_tly = S.add((void*)taul_int_acy, b2, 1, 0);
+    size_t a_H = S.add((void*)H_ice, b2, 1, 0), a_fi = S.add((void*)f_ice, b2, 1, 0);
+    size_t a_hg = S.add((void*)H_grnd, b2, 1, 0), a_fg = S.add((void*)f_grnd, b2, 1, 0);
+    size_t a_fgx = S.add((void*)f_grnd_acx, b2, 1, 0), a_fgy = S.add((void*)f_grnd_acy, b2, 1, 0);
+    size_t a_att = S.add((void*)ATT, b3, 1, 0), a_z = S.add((void*)zeta_aa, (size_t)nz * 8, 1, 0);
+    size_t a_zsl = S.add((void*)z_sl, b2, 1, 0), a_zb = S.add((void*)z_bed, b2, 1, 0);
+    size_t a_zs = S.add((void*)z_srf, b2, 1, 0);
+    int st = S.upload(c);
+    if (st) return st;
+    auto d = [&](size_t k) { return (double*)S.args[k].dev; };
+    ygpu_fields f;
+    memset(&f, 0, sizeof(f));
+    f.nx = nx; f.ny = ny; f.nz = nz; f.dx = dx; f.dy = dy; f.n_glen = n_glen;
+    f.ux = d(a_ux); f.uy = d(a_uy); f.ux_bar = d(a_uxbar); f.uy_bar = d(a_uybar);
+    f.ux_b = d(a_uxb); f.uy_b = d(a_uyb); f.ux_i = d(a_uxi); f.uy_i = d(a_uyi);
+    f.taub_acx = d(a_tbx); f.taub_acy = d(a_tby); f.beta = d(a_b); f.beta_acx = d(a_bx); f.beta_acy = d(a_by);
+    f.beta_eff = d(a_be); f.visc_eff = d(a_v); f.visc_eff_int = d(a_vi); f.duxdz = d(a_dx); f.duydz = d(a_dy);
+    f.ssa_mask_acx = (int*)S.args[a_mx].dev; f.ssa_mask_acy = (int*)S.args[a_my].dev;
+    f.ssa_err_acx = d(a_ex); f.ssa_err_acy = d(a_ey);
+    f.c_bed = d(a_cb); f.f_slide = d(a_fs); f.taud_acx = d(a_tdx); f.taud_acy = d(a_tdy);
+    f.taul_int_acx = d(a_tlx); f.taul_int_acy = d(a_tly); f.H_ice = d(a_H); f.f_ice = d(a_fi);
+    f.H_grnd = d(a_hg); f.f_grnd = d(a_fg); f.f_grnd_acx = d(a_fgx); f.f_grnd_acy = d(a_fgy);
+    f.ATT = d(a_att); f.zeta_aa = d(a_z); f.z_sl = d(a_zsl); f.z_bed = d(a_zb); f.z_srf = d(a_zs);
+    ygpu_stats sts;
+    memset(&sts, 0, sizeof(sts));
+    st = solve_batch(c, YGPU_KIND_DIVA, par, 1, &f, &sts);
+    if (st == YGPU_ERR_CUDA || st == YGPU_ERR_NOMEM || st == YGPU_ERR_BAD_ARG) return st;
+    int st2 = S.download(c);
+    if (st2) return st2;
+    *ssa_iter_now = sts.ssa_iter_now;
+    *ssa_lin_iter = sts.ssa_lin_iter;
+    *ssa_lin_fail = sts.ssa_lin_fail;
+    *ssa_lim_n = sts.ssa_lim_n;
+    return st;
+}
+
+extern "C" int ygpu_set_ssa_masks(int* mx, int* my, const int* mf, const double* f_ice, const double* f_grnd,
+                                  int lateral_bc, int boundaries, int nx, int ny) {
+    if (nx < 2 || ny < 2 || any_null({mx, my, mf, f_ice, f_grnd})) { ygpu_set_error("bad arguments"); return YGPU_ERR_BAD_ARG; }
+    if (boundaries < 0 || boundaries > 6 || lateral_bc < 0 || lateral_bc > 3) { ygpu_set_error("bad code"); return YGPU_ERR_BAD_ARG; }
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const size_t b2 = (size_t)nx * ny * 8, i2 = (size_t)nx * ny * 4;
+    Staging S;
+    size_t a_mx = S.add(mx, i2, 0, 1), a_my = S.add(my, i2, 0, 1), a_mf = S.add((void*)mf, i2, 1, 0);
+    size_t a_fi = S.add((void*)f_ice, b2, 1, 0), a_fg = S.add((void*)f_grnd, b2, 1, 0);
+    int st = S.upload(c);
+    if (st) return st;
+    st = ygpu_ssa_masks_device(c->stream, (int*)S.args[a_mx].dev, (int*)S.args[a_my].dev, (const int*)S.args[a_mf].dev,
+                               (const double*)S.args[a_fi].dev, (const double*)S.args[a_fg].dev, lateral_bc,
+                               boundaries, nx, ny);
+    if (st) return st;
+    return S.download(c);
+}
+
+extern "C" int ygpu_calc_dyn_inputs(const double* H_ice, const double* z_bed, const double* z_sl, double* f_ice,
+                                    double* H_grnd, double* z_srf, double* f_grnd, double* f_grnd_acx,
+                                    double* f_grnd_acy, int* mask_frnt, double* dzsdx, double* dzsdy,
+                                    double* taud_acx, double* taud_acy, double* taul_int_acx, double* taul_int_acy,
+                                    double dx, double grad_lim, double taud_lim, double rho_ice, double rho_sw,
+                                    double g, int boundaries, int nx, int ny) {
+    if (nx < 3 || ny < 3 || !(dx > 0.0) || boundaries < 0 || boundaries > 6 ||
+        any_null({H_ice, z_bed, z_sl, f_ice, H_grnd, z_srf, f_grnd, f_grnd_acx, f_grnd_acy, mask_frnt, dzsdx, dzsdy,
+                  taud_acx, taud_acy, taul_int_acx, taul_int_acy})) {
+        ygpu_set_error("bad arguments");
+        return YGPU_ERR_BAD_ARG;
+    }
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const size_t b2 = (size_t)nx * ny * 8, i2 = (size_t)nx * ny * 4;
+    Staging S;
+    size_t a_H = S.add((void*)H_ice, b2, 1, 0), a_zb = S.add((void*)z_bed, b2, 1, 0), a_zl = S.add((void*)z_sl, b2, 1, 0);
+    size_t a_fi = S.add(f_ice, b2, 0, 1), a_hg = S.add(H_grnd, b2, 0, 1), a_zs = S.add(z_srf, b2, 0, 1);
+    size_t a_fg = S.add(f_grnd, b2, 0, 1), a_fx = S.add(f_grnd_acx, b2, 0, 1), a_fy = S.add(f_grnd_acy, b2, 0, 1);
+    size_t a_mf = S.add(mask_frnt, i2, 0, 1), a_dx = S.add(dzsdx, b2, 0, 1), a_dy = S.add(dzsdy, b2, 0, 1);
+    size_t a_tx = S.add(taud_acx, b2, 0, 1), a_ty = S.add(taud_acy, b2, 0, 1);
+    size_t a_lx = S.add(taul_int_acx, b2, 0, 1), a_ly = S.add(taul_int_acy, b2, 0, 1);
+    int st = S.upload(c);
+    if (st) return st;
+    auto d = [&](size_t k) { return (double*)S.args[k].dev; };
+    st = ygpu_dyn_inputs_device(c->stream, d(a_H), d(a_zb), d(a_zl), d(a_fi), d(a_hg), d(a_zs), d(a_fg), d(a_fx),
+                                d(a_fy), (int*)S.args[a_mf].dev, d(a_dx), d(a_dy), d(a_tx), d(a_ty), d(a_lx), d(a_ly),
+                                dx, grad_lim, taud_lim, rho_ice, rho_sw, g, boundaries, nx, ny);
+    if (st) return st;
+    return S.download(c);
+}
+
+extern "C" int ygpu_linear_solver_matrix_solve(int nmax, const int* a_ptr, const int* a_index, const double* a_value,
+                                               const double* b_value, double* x_value, const char* lis_opt,
+                                               int* lin_iter, int* status, double* L2_rel_norm) {
+    if (nmax < 1 || any_null({a_ptr, a_index, a_value, b_value, x_value, lin_iter, status, L2_rel_norm})) {
+        ygpu_set_error("bad arguments");
+        return YGPU_ERR_BAD_ARG;
+    }
+    ygpu_dyn_par p;
+    ygpu_dyn_par_defaults(&p);
+    int st = ygpu_parse_lis_opt(lis_opt ? lis_opt : "", &p);
+    if (st) return st;
+    int nnz = a_ptr[nmax] - 1;
+    if (nnz < 0 || a_ptr[0] != 1) { ygpu_set_error("a_ptr must be 1-based CSR"); return YGPU_ERR_BAD_ARG; }
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    // 0-based copies on the host (the Fortran arrays are 1-based)
+    std::vector<int> ptr0(nmax + 1), idx0(nnz);
+    for (int k = 0; k <= nmax; k++) ptr0[k] = a_ptr[k] - 1;
+    for (int k = 0; k < nnz; k++) {
+        idx0[k] = a_index[k] - 1;
+        if (idx0[k] < 0 || idx0[k] >= nmax) { ygpu_set_error("column index out of range at %d", k); return YGPU_ERR_BAD_ARG; }
+    }
+    Staging S;
+    size_t a_p = S.add(ptr0.data(), (size_t)(nmax + 1) * 4, 1, 0), a_i = S.add(idx0.data(), (size_t)nnz * 4, 1, 0);
+    size_t a_v = S.add((void*)a_value, (size_t)nnz * 8, 1, 0), a_b = S.add((void*)b_value, (size_t)nmax * 8, 1, 0);
+    size_t a_x = S.add(x_value, (size_t)nmax * 8, 1, 1);
+    std::vector<double> dummy(1);
+    size_t a_w = S.add(nullptr, (size_t)nmax * 8 * 12, 0, 0);
+    if (c->ctl_cap < 1) {
+        CK(cudaMalloc((void**)&c->d_ctl, sizeof(TeamCtl)));
+        c->ctl_cap = 1;
+    }
+    st = S.upload(c);
+    if (st) return st;
+    int nct = (nmax + 2 * YG_BLOCK - 1) / (2 * YG_BLOCK);
+    if (nct > c->csr_max_ctas) nct = c->csr_max_ctas;
+    if (nct > YG_MAX_TEAM_CTAS) nct = YG_MAX_TEAM_CTAS;
+    if (nct < 1) nct = 1;
+    int method = p.lin_solver == YGPU_LIN_BICGSTAB ? YGPU_LIN_BICGSTAB : YGPU_LIN_CG;
+    st = ygpu_launch_csr(c->stream, nmax, (const int*)S.args[a_p].dev, (const int*)S.args[a_i].dev,
+                         (const double*)S.args[a_v].dev, (const double*)S.args[a_b].dev, (double*)S.args[a_x].dev,
+                         (double*)S.args[a_w].dev, method, p.lin_precond, p.lin_maxiter, p.lin_tol,
+                         p.lin_initx_zeros, c->d_misc + 2, c->d_miscd, c->d_ctl, c->d_misc + 1, nct);
+    if (st) return st;
+    int outi[2];
+    double outd;
+    CK(cudaMemcpyAsync(outi, c->d_misc + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&outd, c->d_miscd, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    st = S.download(c);
+    if (st) return st;
+    *lin_iter = outi[0];
+    *status = outi[1];
+    *L2_rel_norm = outd;
+    return outi[1];
+}

@@ -1,0 +1,252 @@
+// ygpu_common.cuh -- device helpers shared by the sm_103a kernels:
+// C-grid neighbour indexing with Yelmo's boundary codes, the instance
+// descriptor the persistent solver works on, and the team barrier with a
+// fused, deterministic all-reduce.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/yelmo_gpu.h"
+
+#define YG_DEV __device__ __forceinline__
+
+// ---------------------------------------------------------------------------
+// Grid indexing (0-based, column-major: c = i + nx*j; 3D: c + n2*k)
+// ---------------------------------------------------------------------------
+
+// get_neighbor_indices_bc_codes, yelmo_tools.f90:118-201
+YG_DEV void nbr_bc(int i, int j, int nx, int ny, int bc, int& im1, int& ip1, int& jm1, int& jp1) {
+    const bool wx = (bc == YGPU_BND_PERIODIC || bc == YGPU_BND_PERIODIC_X);
+    const bool wy = (bc == YGPU_BND_PERIODIC || bc == YGPU_BND_PERIODIC_Y || bc == YGPU_BND_MISMIP3D ||
+                     bc == YGPU_BND_TROUGH);
+    if (wx) {
+        im1 = (i == 0) ? nx - 1 : i - 1;
+        ip1 = (i == nx - 1) ? 0 : i + 1;
+    } else {
+        im1 = (i > 0) ? i - 1 : 0;
+        ip1 = (i < nx - 1) ? i + 1 : nx - 1;
+    }
+    if (wy) {
+        jm1 = (j == 0) ? ny - 1 : j - 1;
+        jp1 = (j == ny - 1) ? 0 : j + 1;
+    } else {
+        jm1 = (j > 0) ? j - 1 : 0;
+        jp1 = (j < ny - 1) ? j + 1 : ny - 1;
+    }
+}
+
+YG_DEV void periodic_dirs(int bc, bool& px, bool& py) {
+    px = (bc == YGPU_BND_PERIODIC || bc == YGPU_BND_PERIODIC_X);
+    py = (bc == YGPU_BND_PERIODIC || bc == YGPU_BND_PERIODIC_Y || bc == YGPU_BND_MISMIP3D ||
+          bc == YGPU_BND_TROUGH);
+}
+
+// Border kinds of the assemblers (solver_ssa_ac.f90:149-210), index 0..3 =
+// bcs(1..4) = right, upper, left, lower. Returns bits: periodic (1<<k), free (1<<(4+k)).
+YG_DEV unsigned border_bits(int bc) {
+    // 0 no-slip, 1 free-slip, 2 periodic
+    int t0, t1, t2, t3;
+    switch (bc) {
+        case YGPU_BND_MISMIP3D:
+        case YGPU_BND_TROUGH: t0 = 1; t1 = 2; t2 = 0; t3 = 2; break;
+        case YGPU_BND_PERIODIC: t0 = t1 = t2 = t3 = 2; break;
+        case YGPU_BND_PERIODIC_X: t0 = 2; t1 = 1; t2 = 2; t3 = 1; break;
+        case YGPU_BND_PERIODIC_Y: t0 = 1; t1 = 2; t2 = 1; t3 = 2; break;
+        case YGPU_BND_INFINITE: t0 = t1 = t2 = t3 = 1; break;
+        default: t0 = t1 = t2 = t3 = 0; break;
+    }
+    unsigned b = 0;
+    int t[4] = {t0, t1, t2, t3};
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        if (t[k] == 2) b |= 1u << k;
+        if (t[k] == 1) b |= 1u << (4 + k);
+    }
+    return b;
+}
+YG_DEV bool bper(unsigned b, int k) { return (b >> k) & 1u; }
+YG_DEV bool bfree(unsigned b, int k) { return (b >> (4 + k)) & 1u; }
+
+// calc_staggered_margin, velocity_diva.f90:1052-1082
+template <typename T>
+YG_DEV T stag_margin(T v0, T v1, double f0, double f1) {
+    if (f0 == 1.0 && f1 < 1.0) return v0;
+    if (f0 < 1.0 && f1 == 1.0) return v1;
+    return T(0.5) * (v0 + v1);
+}
+
+// ---------------------------------------------------------------------------
+// Unknown numbering inside the GPU solver: two planes, ux then uy
+//   u = c (ux at cell c) or n2 + c (uy at cell c)
+// ---------------------------------------------------------------------------
+enum { DOF_FREE = 0, DOF_DIR = 1, DOF_TIED = 2 };
+// residual-form row kinds
+enum { RROW_ID = 0, RROW_FREESLIP = 1, RROW_FRONT = 2, RROW_INNER = 3 };
+
+// Outputs of one instance's solve (device memory, copied back by the host).
+struct InstOut {
+    int iter_now;
+    int lin_iter;
+    int lin_fail;
+    int lim_n;
+    double resid;
+    double lin_resid;
+    int status;        // YGPU_* of the solve
+    int lin_status;    // status of the last linear solve
+    int outer_iter;    // mixed: defect-correction steps
+    int converged;
+};
+
+// Descriptor of one instance (device memory). Field pointers follow
+// ygpu_fields; the rest is scratch owned by the host driver.
+struct Inst {
+    int nx, ny, nz, n2, nu;
+    int kind;                      // YGPU_KIND_*
+    double dx, dy, n_glen;
+    // solve velocity (SSA: ux_b/uy_b, DIVA: ux_bar/uy_bar)
+    double *u_x, *u_y;
+    // DIVA outputs
+    double *ux3, *uy3, *ux_b, *uy_b, *ux_i, *uy_i, *duxdz, *duydz, *beta_eff;
+    double *taub_x, *taub_y, *beta, *beta_x, *beta_y;
+    double *visc, *visc_int, *err_x, *err_y;
+    const int *mask_x, *mask_y;
+    const double *c_bed, *f_slide, *taud_x, *taud_y, *taul_x, *taul_y;
+    const double *H, *f_ice, *H_grnd, *f_grnd, *fg_x, *fg_y, *ATT, *zeta, *z_sl, *z_bed;
+    // scratch, 3D
+    double* visc_alt;
+    // scratch, 2D
+    double *ux_nm1, *uy_nm1, *bm_x, *bm_y, *lk_x, *lk_y, *lr_x, *lr_y, *F2, *F2x, *F2y, *Nab;
+    double *tbp_x, *tbp_y, *drag_x, *drag_y;
+    // linear system (nu entries each)
+    double *x, *b, *r, *p, *q, *z, *dinv, *rt, *v, *s, *t, *ph, *sh, *dval;
+    int *ukind, *emap, *mem, *rpart;
+    // mixed precision scratch (nu entries; coefficient copies n2)
+    float *fN, *fNab, *fdrag_x, *fdrag_y, *fdinv;
+    float *fx, *fr, *fp, *fq, *fz, *frt, *fv, *fs, *ft, *fph, *fsh;
+    InstOut* out;
+    int visc_final_in_alt;         // set by the kernel: final visc is in visc_alt
+};
+
+// ---------------------------------------------------------------------------
+// Team of CTAs: barrier and fused all-reduce (bounded waits)
+// ---------------------------------------------------------------------------
+#define YG_MAX_TEAM_CTAS 1024
+#define YG_RED_MAX 4
+
+struct TeamCtl {
+    unsigned int count;
+    unsigned int gen;
+    int abort;
+    int inst;                      // instance the team works on (work queue)
+    double slots[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
+};
+
+struct Team {
+    int cta, ncta;                 // rank of this CTA in the team, CTAs in the team
+    int tid, nthr;                 // thread rank in the team, threads in the team
+    int parity;                    // reduction slot buffer in use
+    TeamCtl* ctl;
+    int* abort_all;                // whole-launch abort flag (timeout anywhere)
+};
+
+YG_DEV unsigned ld_acquire_u32(const unsigned int* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+YG_DEV int ld_acquire_s32(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Spin budget of one barrier wait: ~2^22 polls of >= 256 ns (about a second
+// or more). A wait that runs out sets the abort flags; every later wait of the
+// launch returns at once, and the kernel reports YGPU_ERR_TIMEOUT.
+#define YG_SPIN_LIMIT (1u << 22)
+
+// Returns false if the launch is aborting.
+YG_DEV bool team_barrier(Team& T) {
+    __syncthreads();
+    __shared__ int s_ok;
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        if (T.ncta > 1) {
+            unsigned gen = ld_acquire_u32(&T.ctl->gen);
+            __threadfence();
+            unsigned arrived = atomicAdd(&T.ctl->count, 1u);
+            if (arrived == (unsigned)T.ncta - 1u) {
+                T.ctl->count = 0u;
+                __threadfence();
+                atomicAdd(&T.ctl->gen, 1u);
+            } else {
+                unsigned n = 0;
+                while (ld_acquire_u32(&T.ctl->gen) == gen) {
+                    if (ld_acquire_s32(T.abort_all)) { ok = 0; break; }
+                    if (++n > YG_SPIN_LIMIT) {
+                        atomicExch(T.abort_all, 1);
+                        atomicExch(&T.ctl->abort, 1);
+                        ok = 0;
+                        break;
+                    }
+                    __nanosleep(256);
+                }
+            }
+            __threadfence();
+        }
+        if (ld_acquire_s32(T.abort_all)) ok = 0;
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+YG_DEV double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// All-reduce (sum) of nv <= YG_RED_MAX values over the team, deterministic
+// for a fixed launch shape. Every thread passes its partials; every thread
+// gets the totals. Also acts as a team barrier.
+YG_DEV bool team_allreduce(Team& T, double* vals, int nv) {
+    __shared__ double s_red[32][YG_RED_MAX];
+    __shared__ double s_tot[YG_RED_MAX];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int k = 0; k < nv; k++) {
+        double w = warp_sum(vals[k]);
+        if (lane == 0) s_red[wid][k] = w;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        for (int k = 0; k < nv; k++) {
+            double w = (lane < nw) ? s_red[lane][k] : 0.0;
+            w = warp_sum(w);
+            if (lane == 0) {
+                if (T.ncta > 1) T.ctl->slots[T.parity][T.cta][k] = w;
+                else s_tot[k] = w;
+            }
+        }
+    }
+    if (T.ncta > 1) {
+        if (!team_barrier(T)) return false;
+        if (wid == 0) {
+            for (int k = 0; k < nv; k++) {
+                double w = 0.0;
+                for (int c = lane; c < T.ncta; c += 32) w += __ldcg(&T.ctl->slots[T.parity][c][k]);
+                w = warp_sum(w);
+                if (lane == 0) s_tot[k] = w;
+            }
+        }
+        T.parity ^= 1;
+    }
+    __syncthreads();
+    for (int k = 0; k < nv; k++) vals[k] = s_tot[k];
+    __syncthreads();
+    return true;
+}
+
+// Integer all-reduce helpers via the double path (exact for |v| < 2^53).
+YG_DEV bool team_allreduce_or_max(Team& T, double* vals, int nv) { return team_allreduce(T, vals, nv); }

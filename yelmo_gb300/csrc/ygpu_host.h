@@ -1,0 +1,35 @@
+// ygpu_host.h -- host-side declarations shared by the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/yelmo_gpu.h"
+
+#ifndef YG_BLOCK
+#define YG_BLOCK 256
+#endif
+
+struct Inst;
+struct TeamCtl;
+
+// error message of the calling thread (ygpu_last_error)
+void ygpu_set_error(const char* fmt, ...);
+
+// ygpu_solver.cu
+int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
+                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_queue, int* d_abort);
+int ygpu_solver_max_ctas(int device);
+int ygpu_sm_count(int device);
+size_t ygpu_teamctl_bytes();
+size_t ygpu_inst_bytes();
+int ygpu_launch_csr(cudaStream_t stream, int n, const int* ptr, const int* idx, const double* val, const double* b,
+                    double* x, double* work, int method, int precond, int maxiter, double tol, int initx_zeros,
+                    int* d_out_i, double* d_out_d, TeamCtl* d_ctl, int* d_abort, int n_ctas);
+int ygpu_csr_max_ctas(int device);
+int ygpu_dyn_inputs_device(cudaStream_t s, const double* H, const double* zb, const double* zsl, double* f_ice,
+                           double* H_grnd, double* z_srf, double* f_grnd, double* fgx, double* fgy, int* mf,
+                           double* dzsdx, double* dzsdy, double* tdx, double* tdy, double* tlx, double* tly,
+                           double dx, double grad_lim, double taud_lim, double rho_ice, double rho_sw, double g,
+                           int bc, int nx, int ny);
+int ygpu_ssa_masks_device(cudaStream_t s, int* mx, int* my, const int* mf, const double* f_ice, const double* f_grnd,
+                          int lat, int bc, int nx, int ny);

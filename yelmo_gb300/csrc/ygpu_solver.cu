@@ -1,0 +1,1760 @@
+// ygpu_solver.cu -- the persistent SSA/DIVA Picard solver for sm_103a.
+//
+// One cooperative launch solves a batch of instances. The launch is split
+// into teams of CTAs; a team takes an instance from a device work queue and
+// runs its whole Picard loop (calc_velocity_ssa, velocity_ssa.f90:60-357, and
+// calc_velocity_diva, velocity_diva.f90:59-429) without returning to the
+// host, then takes the next instance. Phases inside a team are separated by
+// team barriers (bounded spin waits); dot products and norms are deterministic
+// team all-reduces. A single large instance is one team spanning the grid.
+//
+// Phases of one Picard iteration:
+//   strain      horizontal strain rates on the faces (calc_strain_rate_horizontal_2D)
+//   column      3D viscosity (nodes/aa), log relaxation, depth integrals visc_eff_int
+//               and F2, basal friction beta on aa-nodes, all in one pass over each column
+//   faces       staggered F2 and beta, beta_eff, beta_min, speed-limit drag, N_ab,
+//               operator drag coefficients
+//   system      right-hand side, start vector and Jacobi diagonal of the
+//               matrix-free residual or energy operator
+//   krylov      CG / BiCGSTAB, FP64, or FP32 inside FP64 defect correction
+//   epilogue    velocity extraction, clip, relaxation, L2 convergence norm,
+//               error matrix, basal stress and basal velocity
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdio.h>
+
+#include "ygpu_common.cuh"
+#include "ygpu_host.h"
+
+// 2x2 Gauss-Legendre weights of the bilinear corner interpolation, node q
+// (SW, SE, NE, NW) from corner c (same order); set by the host.
+__constant__ double c_gqw[4][4];
+
+static const double TOL_UNDERFLOW = 1e-15;
+#define VISC_MIN 1e5
+
+// ---------------------------------------------------------------------------
+// Per-solve constants derived once from the instance and the parameters
+// ---------------------------------------------------------------------------
+struct Geo {
+    int nx, ny, nz, n2, nu, bc;
+    unsigned bb;                   // border_bits
+    bool per_x, per_y;             // energy assembler periodicity (both sides)
+    double dx, dy, dxdy, dyodx, dxody;
+};
+
+YG_DEV Geo make_geo(const Inst& I, const ygpu_dyn_par& P) {
+    Geo G;
+    G.nx = I.nx; G.ny = I.ny; G.nz = I.nz; G.n2 = I.n2; G.nu = I.nu; G.bc = P.boundaries;
+    G.bb = border_bits(P.boundaries);
+    G.per_x = bper(G.bb, 0) && bper(G.bb, 2);
+    G.per_y = bper(G.bb, 1) && bper(G.bb, 3);
+    G.dx = I.dx; G.dy = I.dy; G.dxdy = I.dx * I.dy; G.dyodx = I.dy / I.dx; G.dxody = I.dx / I.dy;
+    return G;
+}
+
+// ---------------------------------------------------------------------------
+// Quadrature helpers (restated gq2D_to_nodes_*, see the oracle for the rule)
+// ---------------------------------------------------------------------------
+YG_DEV void gq_nodes(const double c[4], double v[4]) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        double s = c_gqw[q][0] * c[0];
+        s = s + c_gqw[q][1] * c[1];
+        s = s + c_gqw[q][2] * c[2];
+        s = s + c_gqw[q][3] * c[3];
+        v[q] = s;
+    }
+}
+YG_DEV double gq_mean(const double v[4]) { return (((v[0] + v[1]) + v[2]) + v[3]) / 4.0; }
+
+YG_DEV double mean2_act(double a, double b, bool aa, bool ab) {
+    int n = (int)aa + (int)ab;
+    if (n == 0) return 0.0;
+    return ((aa ? a : 0.0) + (ab ? b : 0.0)) / (double)n;
+}
+YG_DEV double mean4_act(double a, double b, double c, double d, bool aa, bool ab, bool ac, bool ad) {
+    int n = (int)aa + (int)ab + (int)ac + (int)ad;
+    if (n == 0) return 0.0;
+    double s = (aa ? a : 0.0) + (ab ? b : 0.0);
+    s = s + (ac ? c : 0.0);
+    s = s + (ad ? d : 0.0);
+    return s / (double)n;
+}
+
+// neighbourhood of a cell: index of (im1|i|ip1, jm1|j|jp1)
+struct Nb {
+    int i, j, im1, ip1, jm1, jp1;
+};
+YG_DEV Nb make_nb(const Geo& G, int c) {
+    Nb n;
+    n.i = c % G.nx;
+    n.j = c / G.nx;
+    nbr_bc(n.i, n.j, G.nx, G.ny, G.bc, n.im1, n.ip1, n.jm1, n.jp1);
+    return n;
+}
+#define CI(ii, jj) ((ii) + G.nx * (jj))
+
+// active faces (calc_active_faces, deformation.f90:1316-1344)
+YG_DEV bool act_x(const Geo& G, const double* f_ice, int i, int j) {
+    int im1, ip1, jm1, jp1;
+    nbr_bc(i, j, G.nx, G.ny, G.bc, im1, ip1, jm1, jp1);
+    return f_ice[CI(i, j)] == 1.0 || f_ice[CI(ip1, j)] == 1.0;
+}
+YG_DEV bool act_y(const Geo& G, const double* f_ice, int i, int j) {
+    int im1, ip1, jm1, jp1;
+    nbr_bc(i, j, G.nx, G.ny, G.bc, im1, ip1, jm1, jp1);
+    return f_ice[CI(i, j)] == 1.0 || f_ice[CI(i, jp1)] == 1.0;
+}
+
+// acx-field to quadrature nodes of cell nb (corner = mean of the acx faces above/below)
+template <typename F>
+YG_DEV void nodes_acx(const Geo& G, const Nb& n, F val, const bool* ax, double v[4]) {
+    // ax: active flags of faces [im1,jm1],[im1,j],[im1,jp1],[i,jm1],[i,j],[i,jp1]
+    double c[4];
+    double a_im1_jm1 = val(n.im1, n.jm1), a_im1_j = val(n.im1, n.j), a_im1_jp1 = val(n.im1, n.jp1);
+    double a_i_jm1 = val(n.i, n.jm1), a_i_j = val(n.i, n.j), a_i_jp1 = val(n.i, n.jp1);
+    if (ax) {
+        c[0] = mean2_act(a_im1_jm1, a_im1_j, ax[0], ax[1]);
+        c[1] = mean2_act(a_i_jm1, a_i_j, ax[3], ax[4]);
+        c[2] = mean2_act(a_i_j, a_i_jp1, ax[4], ax[5]);
+        c[3] = mean2_act(a_im1_j, a_im1_jp1, ax[1], ax[2]);
+    } else {
+        c[0] = 0.5 * (a_im1_jm1 + a_im1_j);
+        c[1] = 0.5 * (a_i_jm1 + a_i_j);
+        c[2] = 0.5 * (a_i_j + a_i_jp1);
+        c[3] = 0.5 * (a_im1_j + a_im1_jp1);
+    }
+    gq_nodes(c, v);
+}
+// acy-field to nodes (corner = mean of the acy faces left/right)
+template <typename F>
+YG_DEV void nodes_acy(const Geo& G, const Nb& n, F val, const bool* ay, double v[4]) {
+    // ay: active flags of faces [im1,jm1],[i,jm1],[ip1,jm1],[im1,j],[i,j],[ip1,j]
+    double c[4];
+    double a_im1_jm1 = val(n.im1, n.jm1), a_i_jm1 = val(n.i, n.jm1), a_ip1_jm1 = val(n.ip1, n.jm1);
+    double a_im1_j = val(n.im1, n.j), a_i_j = val(n.i, n.j), a_ip1_j = val(n.ip1, n.j);
+    if (ay) {
+        c[0] = mean2_act(a_im1_jm1, a_i_jm1, ay[0], ay[1]);
+        c[1] = mean2_act(a_i_jm1, a_ip1_jm1, ay[1], ay[2]);
+        c[2] = mean2_act(a_i_j, a_ip1_j, ay[4], ay[5]);
+        c[3] = mean2_act(a_im1_j, a_i_j, ay[3], ay[4]);
+    } else {
+        c[0] = 0.5 * (a_im1_jm1 + a_i_jm1);
+        c[1] = 0.5 * (a_i_jm1 + a_ip1_jm1);
+        c[2] = 0.5 * (a_i_j + a_ip1_j);
+        c[3] = 0.5 * (a_im1_j + a_i_j);
+    }
+    gq_nodes(c, v);
+}
+// aa-field to nodes (corner = mean of the 4 cells around it; act: active cells only)
+template <typename F, typename A>
+YG_DEV void nodes_aa(const Geo& G, const Nb& n, F val, A act, bool use_act, double v[4]) {
+    const int ii[4][4] = {{n.im1, n.i, n.im1, n.i}, {n.i, n.ip1, n.i, n.ip1}, {n.i, n.ip1, n.i, n.ip1}, {n.im1, n.i, n.im1, n.i}};
+    const int jj[4][4] = {{n.jm1, n.jm1, n.j, n.j}, {n.jm1, n.jm1, n.j, n.j}, {n.j, n.j, n.jp1, n.jp1}, {n.j, n.j, n.jp1, n.jp1}};
+    double c[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        double a0 = val(ii[q][0], jj[q][0]), a1 = val(ii[q][1], jj[q][1]);
+        double a2 = val(ii[q][2], jj[q][2]), a3 = val(ii[q][3], jj[q][3]);
+        if (use_act) {
+            c[q] = mean4_act(a0, a1, a2, a3, act(ii[q][0], jj[q][0]), act(ii[q][1], jj[q][1]),
+                             act(ii[q][2], jj[q][2]), act(ii[q][3], jj[q][3]));
+        } else {
+            double s = a0 + a1;
+            s = s + a2;
+            s = s + a3;
+            c[q] = 0.25 * s;
+        }
+    }
+    gq_nodes(c, v);
+}
+
+// ---------------------------------------------------------------------------
+// Phase: horizontal strain rates at the faces of every cell
+// (calc_strain_rate_horizontal_2D, deformation.f90:1393-1507)
+// ---------------------------------------------------------------------------
+YG_DEV double deriv_active(double vm, double v0, double vp, bool am, bool ap, double h) {
+    if (am && ap) return (vp - vm) / (2.0 * h);
+    if (ap) return (vp - v0) / h;
+    if (am) return (v0 - vm) / h;
+    return 0.0;
+}
+
+__device__ __noinline__ void phase_strain(const Inst& I, const Geo& G, Team& T, const double* ux, const double* uy, double* sdudx,
+                         double* sdudy, double* sdvdx, double* sdvdy) {
+    const double* f = I.f_ice;
+    const double dx = G.dx, dy = G.dy;
+    for (int c = T.tid; c < G.n2; c += T.nthr) {
+        Nb n = make_nb(G, c);
+        const int i = n.i, j = n.j;
+        double dudx = (ux[CI(n.ip1, j)] - ux[CI(n.im1, j)]) / (2.0 * dx);
+        double dudy = deriv_active(ux[CI(i, n.jm1)], ux[c], ux[CI(i, n.jp1)], act_x(G, f, i, n.jm1), act_x(G, f, i, n.jp1), dy);
+        double dvdx = deriv_active(uy[CI(n.im1, j)], uy[c], uy[CI(n.ip1, j)], act_y(G, f, n.im1, j), act_y(G, f, n.ip1, j), dx);
+        double dvdy = (uy[CI(i, n.jp1)] - uy[CI(i, n.jm1)]) / (2.0 * dy);
+        int d1, d2, d3;
+        if (f[c] == 1.0 && f[CI(n.ip1, j)] < 1.0) {
+            int im2;
+            nbr_bc(n.im1, j, G.nx, G.ny, G.bc, im2, d1, d2, d3);
+            if (f[CI(n.im1, j)] == 1.0 && im2 != n.im1)
+                dudx = (1.0 * ux[CI(im2, j)] - 4.0 * ux[CI(n.im1, j)] + 3.0 * ux[c]) / (2.0 * dx);
+            else
+                dudx = (ux[c] - ux[CI(n.im1, j)]) / dx;
+        } else if (f[c] < 1.0 && f[CI(n.ip1, j)] == 1.0) {
+            int ip2;
+            nbr_bc(n.ip1, j, G.nx, G.ny, G.bc, d1, ip2, d2, d3);
+            if (ip2 != n.ip1 && f[CI(ip2, j)] == 1.0)
+                dudx = -(1.0 * ux[CI(ip2, j)] - 4.0 * ux[CI(n.ip1, j)] + 3.0 * ux[c]) / (2.0 * dx);
+            else
+                dudx = (ux[CI(n.ip1, j)] - ux[c]) / dx;
+        }
+        if (f[c] == 1.0 && f[CI(i, n.jp1)] < 1.0) {
+            int jm2;
+            nbr_bc(i, n.jm1, G.nx, G.ny, G.bc, d1, d2, jm2, d3);
+            if (f[CI(i, n.jm1)] == 1.0 && jm2 != n.jm1)
+                dvdy = (1.0 * uy[CI(i, jm2)] - 4.0 * uy[CI(i, n.jm1)] + 3.0 * uy[c]) / (2.0 * dy);
+            else
+                dvdy = (uy[c] - uy[CI(i, n.jm1)]) / dy;
+        } else if (f[c] < 1.0 && f[CI(i, n.jp1)] == 1.0) {
+            int jp2;
+            nbr_bc(i, n.jp1, G.nx, G.ny, G.bc, d1, d2, d3, jp2);
+            if (jp2 != n.jp1 && f[CI(i, jp2)] == 1.0)
+                dvdy = -(1.0 * uy[CI(i, jp2)] - 4.0 * uy[CI(i, n.jp1)] + 3.0 * uy[c]) / (2.0 * dy);
+            else
+                dvdy = (uy[CI(i, n.jp1)] - uy[c]) / dy;
+        }
+        sdudx[c] = dudx;
+        sdudy[c] = dudy;
+        sdvdx[c] = dvdx;
+        sdvdy[c] = dvdy;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Basal friction on aa-nodes (calc_beta, basal_dragging.f90:384-579)
+// ---------------------------------------------------------------------------
+YG_DEV double beta_raw(const Inst& I, const ygpu_dyn_par& P, const Geo& G, int i, int j, const double* ux_b,
+                       const double* uy_b) {
+    const int m = P.beta_method;
+    const int c = CI(i, j);
+    double beta;
+    if (m == 0) {
+        beta = P.beta_const;
+    } else {
+        const double q = (m == 1) ? 1.0 : P.beta_q;
+        const double u0 = P.beta_u0;
+        const bool coulomb = (m == 3 || m == 5);
+        const bool simple = (m == 4 || m == 5);
+        const double ub_min = 1e-3, ub_sq_min = ub_min * ub_min;
+        if (I.f_ice[c] == 1.0) {
+            Nb n = make_nb(G, c);
+            double cbn[4], uxn[4], uyn[4], bn[4];
+            if (simple) {
+                double ucx = 0.5 * (ux_b[c] + ux_b[CI(n.im1, j)]);
+                double ucy = 0.5 * (uy_b[c] + uy_b[CI(i, n.jm1)]);
+#pragma unroll
+                for (int k = 0; k < 4; k++) { cbn[k] = I.c_bed[c]; uxn[k] = ucx; uyn[k] = ucy; }
+            } else {
+                auto cb = [&](int a, int b) { return I.c_bed[CI(a, b)]; };
+                auto aa = [&](int a, int b) { return I.f_ice[CI(a, b)] == 1.0 && I.f_grnd[CI(a, b)] > 0.0; };
+                nodes_aa(G, n, cb, aa, true, cbn);
+                bool ax[6] = {act_x(G, I.f_ice, n.im1, n.jm1), act_x(G, I.f_ice, n.im1, n.j), act_x(G, I.f_ice, n.im1, n.jp1),
+                              act_x(G, I.f_ice, n.i, n.jm1), act_x(G, I.f_ice, n.i, n.j), act_x(G, I.f_ice, n.i, n.jp1)};
+                bool ay[6] = {act_y(G, I.f_ice, n.im1, n.jm1), act_y(G, I.f_ice, n.i, n.jm1), act_y(G, I.f_ice, n.ip1, n.jm1),
+                              act_y(G, I.f_ice, n.im1, n.j), act_y(G, I.f_ice, n.i, n.j), act_y(G, I.f_ice, n.ip1, n.j)};
+                auto vx = [&](int a, int b) { return ux_b[CI(a, b)]; };
+                auto vy = [&](int a, int b) { return uy_b[CI(a, b)]; };
+                nodes_acx(G, n, vx, ax, uxn);
+                nodes_acy(G, n, vy, ay, uyn);
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                double s = uxn[k] * uxn[k] + uyn[k] * uyn[k];
+                double uxy = sqrt(s + ub_sq_min);
+                double fac = coulomb ? pow(uxy / (uxy + u0), q) : pow(uxy / u0, q);
+                bn[k] = cbn[k] * fac * (1.0 / uxy);
+            }
+            beta = gq_mean(bn);
+        } else {
+            double uxy = ub_min;
+            double fac = coulomb ? pow(uxy / (uxy + u0), q) : pow(uxy / u0, q);
+            beta = I.c_bed[c] * fac * (1.0 / uxy);
+        }
+    }
+    const double q_frz = (m == 0 || m == 1) ? 1.0 : P.beta_q;
+    beta = beta * pow(I.f_slide[c], -q_frz);
+    switch (P.beta_gl_scale) {
+        case 0: {
+            int im1, ip1, jm1, jp1;
+            nbr_bc(i, j, G.nx, G.ny, G.bc, im1, ip1, jm1, jp1);
+            const double* fg = I.f_grnd;
+            if (fg[c] > 0.0 && (fg[CI(im1, j)] == 0.0 || fg[CI(ip1, j)] == 0.0 || fg[CI(i, jm1)] == 0.0 || fg[CI(i, jp1)] == 0.0))
+                beta = beta * P.beta_gl_f;
+        } break;
+        case 1: {
+            double hg = I.H_grnd[c] < P.H_grnd_lim ? I.H_grnd[c] : P.H_grnd_lim;
+            double f = hg / P.H_grnd_lim;
+            if (f < 0.0) f = 0.0;
+            beta = beta * f;
+        } break;
+        case 2: {
+            if (I.f_ice[c] > 0.0) {
+                double Heff = I.H[c] / I.f_ice[c];
+                if (I.f_ice[c] < 1.0) Heff = 0.0;
+                double f;
+                if (I.z_bed[c] > I.z_sl[c]) f = Heff;
+                else {
+                    f = Heff - (I.z_sl[c] - I.z_bed[c]) * (P.rho_sw / P.rho_ice);
+                    if (f < 0.0) f = 0.0;
+                }
+                if (Heff > 0.0) f = f / Heff;
+                beta = beta * f;
+            }
+        } break;
+        case 3: beta = I.f_grnd[c] * beta; break;
+        default: break;
+    }
+    if (I.f_grnd[c] == 0.0) beta = 0.0;
+    return beta;
+}
+
+YG_DEV double beta_aa(const Inst& I, const ygpu_dyn_par& P, const Geo& G, int i, int j, const double* ux_b,
+                      const double* uy_b) {
+    // edge copies of calc_beta (MISMIP3D: left column; infinite/mask: all edges), then beta_min
+    int si = i, sj = j;
+    if (G.bc == YGPU_BND_MISMIP3D) {
+        if (i == 0) si = 1;
+    } else if (G.bc == YGPU_BND_INFINITE) {
+        if (i == 0) si = 1;
+        if (i == G.nx - 1) si = G.nx - 2;
+        if (j == 0) sj = 1;
+        if (j == G.ny - 1) sj = G.ny - 2;
+    }
+    double b = beta_raw(I, P, G, si, sj, ux_b, uy_b);
+    if (b > 0.0 && b < P.beta_min) b = P.beta_min;
+    return b;
+}
+
+// ---------------------------------------------------------------------------
+// Phase: column pass -- viscosity, relaxation, depth integrals, beta (aa)
+// ---------------------------------------------------------------------------
+__device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, const double* vcur,
+                         double* vnew, const double* sdudx, const double* sdudy, const double* sdvdx,
+                         const double* sdvdy, bool relax, bool diva, bool first_copy, bool visc_only = false) {
+    const int nz = G.nz, n2 = G.n2;
+    const double p1 = (1.0 - I.n_glen) / (2.0 * I.n_glen);
+    const double p2 = -1.0 / I.n_glen;
+    const bool glen3 = (I.n_glen == 3.0);
+    const double eps0sq = P.eps_0 * P.eps_0;
+    const double rel = P.ssa_iter_rel;
+    const double* zeta = I.zeta;
+    const double* f = I.f_ice;
+    const int vm = P.visc_method;
+    for (int c = T.tid; c < n2; c += T.nthr) {
+        Nb n = make_nb(G, c);
+        if (first_copy) {
+            I.ux_nm1[c] = I.u_x[c];
+            I.uy_nm1[c] = I.u_y[c];
+            if (diva) {
+                I.tbp_x[c] = I.taub_x[c];
+                I.tbp_y[c] = I.taub_y[c];
+            }
+        }
+        const bool ice = (f[c] == 1.0);
+        const double Hc = I.H[c];
+        // quadrature-node horizontal strain rates (independent of k)
+        double dudxn[4], dudyn[4], dvdxn[4], dvdyn[4];
+        bool ax[6], ay[6];
+        double e_aa = 0.0;
+        if (ice && vm == 1) {
+            ax[0] = act_x(G, f, n.im1, n.jm1); ax[1] = act_x(G, f, n.im1, n.j); ax[2] = act_x(G, f, n.im1, n.jp1);
+            ax[3] = act_x(G, f, n.i, n.jm1); ax[4] = act_x(G, f, n.i, n.j); ax[5] = act_x(G, f, n.i, n.jp1);
+            ay[0] = act_y(G, f, n.im1, n.jm1); ay[1] = act_y(G, f, n.i, n.jm1); ay[2] = act_y(G, f, n.ip1, n.jm1);
+            ay[3] = act_y(G, f, n.im1, n.j); ay[4] = act_y(G, f, n.i, n.j); ay[5] = act_y(G, f, n.ip1, n.j);
+            nodes_acx(G, n, [&](int a, int b) { return sdudx[CI(a, b)]; }, ax, dudxn);
+            nodes_acx(G, n, [&](int a, int b) { return sdudy[CI(a, b)]; }, ax, dudyn);
+            nodes_acy(G, n, [&](int a, int b) { return sdvdx[CI(a, b)]; }, ay, dvdxn);
+            nodes_acy(G, n, [&](int a, int b) { return sdvdy[CI(a, b)]; }, ay, dvdyn);
+        } else if (ice && vm == 2) {
+            const double* ux = I.u_x;
+            const double* uy = I.u_y;
+            const int i = n.i, j = n.j;
+            double dudx = (ux[c] - ux[CI(n.im1, j)]) / G.dx;
+            double dvdy = (uy[c] - uy[CI(i, n.jm1)]) / G.dy;
+            double dudy1 = (ux[CI(i, n.jp1)] - ux[CI(i, n.jm1)]) / (2.0 * G.dy);
+            double dudy2 = (ux[CI(n.im1, n.jp1)] - ux[CI(n.im1, n.jm1)]) / (2.0 * G.dy);
+            double dudy = 0.5 * (dudy1 + dudy2);
+            double dvdx1 = (uy[CI(n.ip1, j)] - uy[CI(n.im1, j)]) / (2.0 * G.dx);
+            double dvdx2 = (uy[CI(n.ip1, n.jm1)] - uy[CI(n.im1, n.jm1)]) / (2.0 * G.dx);
+            double dvdx = 0.5 * (dvdx1 + dvdx2);
+            double sh = dudy + dvdx;
+            e_aa = dudx * dudx + dvdy * dvdy;
+            e_aa = e_aa + dudx * dvdy;
+            e_aa = e_aa + 0.25 * (sh * sh);
+        }
+        double vint = 0.0, f2 = 0.0, vprev = 0.0, gprev = 0.0;
+        for (int k = 0; k < nz; k++) {
+            const size_t ck = (size_t)k * n2 + c;
+            double v;
+            if (vm == 0) {
+                v = P.visc_const;
+            } else if (!ice) {
+                v = VISC_MIN;
+            } else {
+                const double omz = 1.0 - zeta[k];
+                // vertical shear of the iterate (calc_vertical_shear_3D, velocity_diva.f90:510-571)
+                auto shx = [&](int a, int b) {
+                    int am1, ap1, bm1, bp1;
+                    nbr_bc(a, b, G.nx, G.ny, G.bc, am1, ap1, bm1, bp1);
+                    double va = stag_margin(vcur[(size_t)k * n2 + CI(a, b)], vcur[(size_t)k * n2 + CI(ap1, b)],
+                                            f[CI(a, b)], f[CI(ap1, b)]);
+                    return (va != 0.0) ? (I.taub_x[CI(a, b)] / va) * omz : 0.0;
+                };
+                auto shy = [&](int a, int b) {
+                    int am1, ap1, bm1, bp1;
+                    nbr_bc(a, b, G.nx, G.ny, G.bc, am1, ap1, bm1, bp1);
+                    double va = stag_margin(vcur[(size_t)k * n2 + CI(a, b)], vcur[(size_t)k * n2 + CI(a, bp1)],
+                                            f[CI(a, b)], f[CI(a, bp1)]);
+                    return (va != 0.0) ? (I.taub_y[CI(a, b)] / va) * omz : 0.0;
+                };
+                if (vm == 1) {
+                    double dudzn[4], dvdzn[4], attn[4], vn[4];
+                    if (diva) {
+                        nodes_acx(G, n, shx, ax, dudzn);
+                        nodes_acy(G, n, shy, ay, dvdzn);
+                    }
+                    auto att = [&](int a, int b) { return I.ATT[(size_t)k * n2 + CI(a, b)]; };
+                    nodes_aa(G, n, att, [](int, int) { return true; }, false, attn);
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        double sh = dudyn[q] + dvdxn[q];
+                        double e = dudxn[q] * dudxn[q] + dvdyn[q] * dvdyn[q];
+                        e = e + dudxn[q] * dvdyn[q];
+                        e = e + 0.25 * (sh * sh);
+                        if (diva) {
+                            e = e + 0.25 * (dudzn[q] * dudzn[q]);
+                            e = e + 0.25 * (dvdzn[q] * dvdzn[q]);
+                        }
+                        e = e + eps0sq;
+                        double ep = glen3 ? rcbrt(e) : pow(e, p1);
+                        double ap = glen3 ? rcbrt(attn[q]) : pow(attn[q], p2);
+                        vn[q] = 0.5 * ep * ap;
+                    }
+                    v = gq_mean(vn);
+                } else {
+                    double e = e_aa;
+                    if (diva) {
+                        double dzx = 0.5 * (shx(n.i, n.j) + shx(n.im1, n.j));
+                        double dzy = 0.5 * (shy(n.i, n.j) + shy(n.i, n.jm1));
+                        e = e + 0.25 * (dzx * dzx);
+                        e = e + 0.25 * (dzy * dzy);
+                    }
+                    e = e + eps0sq;
+                    double a = I.ATT[ck];
+                    double ep = glen3 ? rcbrt(e) : pow(e, p1);
+                    double ap = glen3 ? rcbrt(a) : pow(a, p2);
+                    v = 0.5 * ep * ap;
+                }
+            }
+            if (relax) v = exp((1.0 - rel) * log(vcur[ck]) + rel * log(v));
+            vnew[ck] = v;
+            // trapezoid integrals (integrate_trapezoid1D_pt, yelmo_tools.f90:1092-1122)
+            const double omz = 1.0 - zeta[k];
+            const double g = (Hc / v) * (omz * omz);
+            if (k > 0) {
+                const double dz = zeta[k] - zeta[k - 1];
+                vint = vint + 0.5 * (v + vprev) * dz;
+                f2 = f2 + 0.5 * (g + gprev) * dz;
+            }
+            vprev = v;
+            gprev = g;
+        }
+        if (visc_only) continue;
+        // calc_visc_eff_int, velocity_general.f90:2215-2261
+        double vi = ice ? vint * Hc : VISC_MIN;
+        if (vi < VISC_MIN) vi = VISC_MIN;
+        I.visc_int[c] = vi;
+        // calc_F_integral (n = 2), velocity_diva.f90:824-869
+        if (diva) I.F2[c] = ice ? f2 : 0.0;
+        // calc_beta: SSA uses the iterate, DIVA the basal velocity
+        if (P.beta_method != -1) {
+            const double* ubx = diva ? I.ux_b : I.u_x;
+            const double* uby = diva ? I.uy_b : I.u_y;
+            I.beta[c] = beta_aa(I, P, G, n.i, n.j, ubx, uby);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Phase: faces -- staggering, beta_eff, beta_min, drag, N_ab, drag coefficients
+// ---------------------------------------------------------------------------
+YG_DEV double gl_flux_weight(double beta_a, double ux_a, double ux_b, double H_a, double H_b, double f_ac) {
+    // calc_beta_gl_flux_weight, basal_dragging.f90:1760-1845
+    double q_a = ux_a * H_a, q_b = ux_b * H_b, ug = 0.0, ut = 0.0;
+    for (int n = 1; n <= 100; n++) {
+        double lam = ((double)n - 0.5) / 100.0;
+        double Hn = H_a * lam + H_b * (1.0 - lam);
+        double qn = q_a * lam + q_b * (1.0 - lam);
+        double un = (Hn > 0.0) ? qn / Hn : 0.0;
+        ut = ut + fabs(un);
+        if (lam > (1.0 - f_ac)) ug = ug + fabs(un);
+    }
+    double w = (ut > 0.0) ? ug / ut : 0.0;
+    return beta_a * w;
+}
+
+// stagger_beta for one face (basal_dragging.f90:581-704 and :1360-1758), before the limit
+YG_DEV double stagger_beta_face(const Inst& I, const ygpu_dyn_par& P, const Geo& G, int i, int j, bool xdir) {
+    int im1, ip1, jm1, jp1;
+    nbr_bc(i, j, G.nx, G.ny, G.bc, im1, ip1, jm1, jp1);
+    const int c = CI(i, j), cn = xdir ? CI(ip1, j) : CI(i, jp1);
+    const double* fi = I.f_ice;
+    const double* fg = I.f_grnd;
+    const double* be = I.beta;
+    double b;
+    if (fg[c] == 0.0 && fg[cn] == 0.0) b = 0.0;
+    else if (fi[c] == 1.0 && fi[cn] < 1.0) b = be[c];
+    else if (fi[c] < 1.0 && fi[cn] == 1.0) b = be[cn];
+    else b = 0.5 * (be[c] + be[cn]);
+    const int gs = P.beta_gl_stag;
+    if (gs >= 1 && gs <= 4 && fi[c] == 1.0 && fi[cn] == 1.0) {
+        const bool gl_r = (fg[c] > 0.0 && fg[cn] == 0.0);
+        const bool gl_l = (fg[c] == 0.0 && fg[cn] > 0.0);
+        if (gs == 1) {
+            if (gl_r) b = be[c]; else if (gl_l) b = be[cn];
+        } else if (gs == 2) {
+            if (gl_r) b = be[cn]; else if (gl_l) b = be[c];
+        } else if (gs == 3) {
+            double fgf = xdir ? I.fg_x[c] : I.fg_y[c];
+            double wt = fgf * fgf;
+            if (gl_r) b = wt * be[c] + (1.0 - wt) * be[cn];
+            else if (gl_l) b = (1.0 - wt) * be[c] + wt * be[cn];
+        } else {
+            const double* u = xdir ? I.u_x : I.u_y;
+            const int cm = xdir ? CI(im1, j) : CI(i, jm1);
+            double fgf = xdir ? I.fg_x[c] : I.fg_y[c];
+            if (gl_r) {
+                double ua = 0.5 * (u[cm] + u[c]), ub = 0.5 * (u[cn] + u[c]);
+                b = gl_flux_weight(be[c], ua, ub, I.H[c], I.H[cn], fgf);
+            } else if (gl_l) {
+                double ua = 0.5 * (u[cn] + u[c]), ub = 0.5 * (u[cm] + u[c]);
+                b = gl_flux_weight(be[cn], ua, ub, I.H[cn], I.H[c], fgf);
+            }
+        }
+    }
+    return b;
+}
+
+YG_DEV void lim_face(double& k, double& r, double u, double uc, int mask, double s0, double inv_du, double tau_c) {
+    // calc_vel_lim_drag / lim_drag_face, solver_ssa_ac.f90:1095-1199
+    k = 0.0;
+    r = 0.0;
+    if (mask < 1) return;
+    double s = sqrt(u * u + uc * uc);
+    if (s <= s0) return;
+    double x = (s - s0) * inv_du;
+    double tau = tau_c * x * x;
+    double dtds = 2.0 * tau_c * x * inv_du;
+    double b = tau / s;
+    double w = (u / s) * (u / s);
+    k = b * (1.0 - w) + dtds * w;
+    r = (k - b) * u;
+}
+
+__device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, bool diva) {
+    const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
+    const bool drag = (P.ssa_vel_lim_method == YGPU_VEL_LIM_DRAG);
+    const bool limit = (P.beta_method != -1 && P.beta_gl_stag != -1);
+    const double s0 = 0.8 * P.ssa_vel_max;
+    const double inv_du = 1.0 / (P.ssa_vel_max - s0);
+    const int nx = G.nx, ny = G.ny;
+    for (int c = T.tid; c < G.n2; c += T.nthr) {
+        Nb n = make_nb(G, c);
+        const int i = n.i, j = n.j;
+        // staggered F2 (stagger_F_integral, velocity_diva.f90:871-910)
+        double F2x = 0.0, F2y = 0.0;
+        if (diva) {
+            F2x = stag_margin(I.F2[c], I.F2[CI(n.ip1, j)], I.f_ice[c], I.f_ice[CI(n.ip1, j)]);
+            F2y = stag_margin(I.F2[c], I.F2[CI(i, n.jp1)], I.f_ice[c], I.f_ice[CI(i, n.jp1)]);
+            I.F2x[c] = F2x;
+            I.F2y[c] = F2y;
+        }
+        // stagger_beta with the border copies of infinite/MISMIP3D/mask
+        double bx = I.beta_x[c], by = I.beta_y[c];
+        if (P.beta_gl_stag != -1) {
+            int sxi = i, sxj = j, syi = i, syj = j;
+            if (G.bc == YGPU_BND_INFINITE || G.bc == YGPU_BND_MISMIP3D) {
+                if (i == 0) sxi = 1;
+                else if (i == nx - 2 || i == nx - 1) sxi = nx - 3;
+                if (i == 0) syi = 1;
+                else if (i == nx - 1) syi = nx - 2;
+            }
+            if (G.bc == YGPU_BND_INFINITE) {
+                if (j == 0) sxj = 1;
+                else if (j == ny - 1) sxj = ny - 2;
+                if (j == 0) syj = 1;
+                else if (j == ny - 2 || j == ny - 1) syj = ny - 3;
+            }
+            bx = stagger_beta_face(I, P, G, sxi, sxj, true);
+            by = stagger_beta_face(I, P, G, syi, syj, false);
+        }
+        if (limit) {
+            if (bx > 0.0 && bx < P.beta_min) bx = P.beta_min;
+            if (by > 0.0 && by < P.beta_min) by = P.beta_min;
+        }
+        I.beta_x[c] = bx;
+        I.beta_y[c] = by;
+        // friction used by the matrix
+        double mx_b = bx, my_b = by;
+        if (diva) {
+            // calc_beta_eff, velocity_diva.f90:912-958
+            if (P.no_slip) {
+                mx_b = (F2x > 0.0) ? 1.0 / F2x : 0.0;
+                my_b = (F2y > 0.0) ? 1.0 / F2y : 0.0;
+                I.beta_eff[c] = (I.F2[c] > 0.0) ? 1.0 / I.F2[c] : 0.0;
+            } else {
+                mx_b = bx / (1.0 + bx * F2x);
+                my_b = by / (1.0 + by * F2y);
+                I.beta_eff[c] = I.beta[c] / (1.0 + I.beta[c] * I.F2[c]);
+            }
+        }
+        // set_beta_min_grounded, basal_dragging.f90:706-780
+        const int mx = I.mask_x[c], my = I.mask_y[c];
+        if (mx == 1 && mx_b == 0.0) mx_b = P.beta_min;
+        if (my == 1 && my_b == 0.0) my_b = P.beta_min;
+        I.bm_x[c] = mx_b;
+        I.bm_y[c] = my_b;
+        // speed-limit drag around the iterate
+        double kx = 0.0, ky = 0.0, rx = 0.0, ry = 0.0;
+        if (drag) {
+            const double* ux = I.u_x;
+            const double* uy = I.u_y;
+            double uc = 0.25 * (uy[c] + uy[CI(n.ip1, j)] + uy[CI(i, n.jm1)] + uy[CI(n.ip1, n.jm1)]);
+            lim_face(kx, rx, ux[c], uc, mx, s0, inv_du, P.ssa_vel_lim_tau);
+            uc = 0.25 * (ux[c] + ux[CI(n.im1, j)] + ux[CI(i, n.jp1)] + ux[CI(n.im1, n.jp1)]);
+            lim_face(ky, ry, uy[c], uc, my, s0, inv_du, P.ssa_vel_lim_tau);
+        }
+        I.lk_x[c] = kx; I.lk_y[c] = ky; I.lr_x[c] = rx; I.lr_y[c] = ry;
+        // operator drag coefficients: w*(beta + k) (* dx*dy for the energy form)
+        double wx, wy;
+        if (energy) {
+            wx = (mx == 3 || mx == 4) ? 0.5 : 1.0;
+            wy = (my == 3 || my == 4) ? 0.5 : 1.0;
+            I.drag_x[c] = wx * (mx_b + kx) * G.dxdy;
+            I.drag_y[c] = wy * (my_b + ky) * G.dxdy;
+        } else {
+            wx = (mx == 4) ? 0.5 : 1.0;
+            wy = (my == 4) ? 0.5 : 1.0;
+            I.drag_x[c] = wx * mx_b + wx * kx;
+            I.drag_y[c] = wy * my_b + wy * ky;
+        }
+        // stagger_visc_aa_ab, solver_ssa_ac.f90:1000-1067
+        {
+            const int cc[4] = {c, CI(n.ip1, j), CI(i, n.jp1), CI(n.ip1, n.jp1)};
+            int nice = 0;
+            bool anyocn = false;
+            double v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                bool ice = (I.f_ice[cc[q]] == 1.0);
+                bool ocn = (!ice) && (I.z_bed[cc[q]] < I.z_sl[cc[q]]);
+                nice += ice;
+                anyocn = anyocn || ocn;
+                v[q] = ice ? I.visc_int[cc[q]] : 0.0;
+            }
+            I.Nab[c] = (anyocn || nice == 0) ? 0.0 : ((v[0] + v[1]) + (v[2] + v[3])) / (double)nice;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Energy operator (solver_ssa_ac_energy.f90:70-708, matrix-free)
+// ---------------------------------------------------------------------------
+YG_DEV bool wrap_index(int& k, int nk, bool periodic, bool free_lo, bool free_hi) {
+    if (k < 0) {
+        if (periodic) k += nk;
+        else if (free_lo) k = 0;
+        else return false;
+    } else if (k > nk - 1) {
+        if (periodic) k -= nk;
+        else if (free_hi) k = nk - 1;
+        else return false;
+    }
+    return true;
+}
+YG_DEV bool elem_index(int& k, int nk, bool periodic) {
+    if (k < 0 || k > nk - 1) {
+        if (!periodic) return false;
+        k = ((k % nk) + nk) % nk;
+    }
+    return true;
+}
+// unknown of ux(ii,jj) / uy(ii,jj) one beyond the domain allowed; -1 = zero ghost
+YG_DEV int dof_u(const Geo& G, int ii, int jj, int plane) {
+    if (!wrap_index(ii, G.nx, G.per_x, bfree(G.bb, 2), bfree(G.bb, 0))) return -1;
+    if (!wrap_index(jj, G.ny, G.per_y, bfree(G.bb, 3), bfree(G.bb, 1))) return -1;
+    return ii + G.nx * jj + plane * G.n2;
+}
+
+// Contribution of member unknown mm (plane pl, cell (i,j)) of the elements
+// around it: sum over the slots holding mm of H(l,:) . val(dofs). val(d) must
+// return 0 for d < 0.
+template <typename T, typename CT, typename V>
+YG_DEV T member_elems(const Geo& G, const CT* N, const CT* Nab, int mm, V val) {
+    const int pl = (mm >= G.n2) ? 1 : 0;
+    const int c = mm - pl * G.n2;
+    const int i = c % G.nx, j = c / G.nx;
+    const T dyodx = (T)G.dyodx, dxody = (T)G.dxody;
+    T acc = T(0);
+    // cells: ux -> (i,j),(i+1,j); uy -> (i,j),(i,j+1)
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+        int ci = (pl == 0) ? i + e : i, cj = (pl == 0) ? j : j + e;
+        if (!elem_index(ci, G.nx, G.per_x) || !elem_index(cj, G.ny, G.per_y)) continue;
+        int d0 = dof_u(G, ci - 1, cj, 0), d1 = dof_u(G, ci, cj, 0);
+        int d2 = dof_u(G, ci, cj - 1, 1), d3 = dof_u(G, ci, cj, 1);
+        if (d0 != mm && d1 != mm && d2 != mm && d3 != mm) continue;
+        T Nc = (T)N[ci + G.nx * cj];
+        T hx = T(4) * Nc * dyodx, hy = T(4) * Nc * dxody, hc = T(2) * Nc;
+        T ex = val(d1) - val(d0), ey = val(d3) - val(d2);
+        T Fx = hx * ex + hc * ey, Fy = hc * ex + hy * ey;
+        if (d0 == mm) acc -= Fx;
+        if (d1 == mm) acc += Fx;
+        if (d2 == mm) acc -= Fy;
+        if (d3 == mm) acc += Fy;
+    }
+    // corners: ux -> (i,j),(i,j-1); uy -> (i,j),(i-1,j)
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+        int ci = (pl == 0) ? i : i - e, cj = (pl == 0) ? j - e : j;
+        if (!elem_index(ci, G.nx, G.per_x) || !elem_index(cj, G.ny, G.per_y)) continue;
+        int d0 = dof_u(G, ci, cj, 0), d1 = dof_u(G, ci, cj + 1, 0);
+        int d2 = dof_u(G, ci, cj, 1), d3 = dof_u(G, ci + 1, cj, 1);
+        if (d0 != mm && d1 != mm && d2 != mm && d3 != mm) continue;
+        T Nc = (T)Nab[ci + G.nx * cj];
+        T sx = val(d1) - val(d0), sy = val(d3) - val(d2);
+        T G1 = Nc * (dxody * sx + sy), G2 = Nc * (sx + dyodx * sy);
+        if (d0 == mm) acc -= G1;
+        if (d1 == mm) acc += G1;
+        if (d2 == mm) acc -= G2;
+        if (d3 == mm) acc += G2;
+    }
+    return acc;
+}
+
+// y = K v for the rows [tid.. nu) of the team (identity on Dirichlet/tied rows)
+template <typename T, typename CT>
+__device__ __noinline__ void energy_apply(const Inst& I, const Geo& G, Team& Tm, const CT* N, const CT* Nab, const CT* dgx,
+                         const CT* dgy, const T* v, T* y) {
+    const int* emap = I.emap;
+    auto val = [&](int d) -> T {
+        if (d < 0) return T(0);
+        int e = emap[d];
+        return (e >= 0) ? v[e] : T(0);
+    };
+    for (int u = Tm.tid; u < G.nu; u += Tm.nthr) {
+        if (I.ukind[u] != DOF_FREE) {
+            y[u] = v[u];
+            continue;
+        }
+        const T vr = v[u];
+        T acc = ((u < G.n2) ? (T)dgx[u] : (T)dgy[u - G.n2]) * vr;
+        acc += member_elems<T>(G, N, Nab, u, val);
+        const int* mem = I.mem + 3 * u;
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+            int mm = mem[m];
+            if (mm < 0) break;
+            acc += ((mm < G.n2) ? (T)dgx[mm] : (T)dgy[mm - G.n2]) * vr;
+            acc += member_elems<T>(G, N, Nab, mm, val);
+        }
+        y[u] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Residual operator (solver_ssa_ac.f90:73-848, matrix-free)
+// ---------------------------------------------------------------------------
+template <typename T, typename CT>
+YG_DEV T residual_row(const Inst& I, const Geo& G, const CT* N, const CT* Nab, const CT* dgx, const CT* dgy,
+                      const T* v, int u, T* diag_out) {
+    const int rk = I.ukind[u];
+    if (rk == RROW_ID) {
+        if (diag_out) *diag_out = T(1);
+        return v[u];
+    }
+    if (rk == RROW_FREESLIP) {
+        if (diag_out) *diag_out = T(1);
+        return v[u] - v[I.rpart[u]];
+    }
+    const int nx = G.nx, ny = G.ny, n2 = G.n2;
+    const int pl = (u >= n2) ? 1 : 0;
+    const int c = u - pl * n2;
+    const int i = c % nx, j = c / nx;
+    const int im1 = (i == 0) ? nx - 1 : i - 1, ip1 = (i == nx - 1) ? 0 : i + 1;
+    const int jm1 = (j == 0) ? ny - 1 : j - 1, jp1 = (j == ny - 1) ? 0 : j + 1;
+    const T inv_dx = T(1.0 / G.dx), inv_dy = T(1.0 / G.dy);
+    const T inv_dxdx = T(1.0 / (G.dx * G.dx)), inv_dydy = T(1.0 / (G.dy * G.dy)), inv_dxdy = T(1.0 / (G.dx * G.dy));
+#define VX(a, b) v[(a) + nx * (b)]
+#define VY(a, b) v[n2 + (a) + nx * (b)]
+#define NN(a, b) ((T)N[(a) + nx * (b)])
+#define NB(a, b) ((T)Nab[(a) + nx * (b)])
+    if (rk == RROW_FRONT) {
+        if (pl == 0) {
+            if (I.f_ice[c] == 1.0 && I.f_ice[ip1 + nx * j] < 1.0) {
+                T Nn = NN(i, j);
+                if (diag_out) *diag_out = T(4) * inv_dx * Nn;
+                return -T(4) * inv_dx * Nn * VX(im1, j) - T(2) * inv_dy * Nn * VY(i, jm1) + T(4) * inv_dx * Nn * VX(i, j) +
+                       T(2) * inv_dy * Nn * VY(i, j);
+            }
+            T Nn = NN(ip1, j);
+            if (diag_out) *diag_out = -T(4) * inv_dx * Nn;
+            return -T(4) * inv_dx * Nn * VX(i, j) - T(2) * inv_dy * Nn * VY(ip1, jm1) + T(4) * inv_dx * Nn * VX(ip1, j) +
+                   T(2) * inv_dy * Nn * VY(ip1, j);
+        } else {
+            if (I.f_ice[c] == 1.0 && I.f_ice[i + nx * jp1] < 1.0) {
+                T Nn = NN(i, j);
+                if (diag_out) *diag_out = T(4) * inv_dy * Nn;
+                return -T(2) * inv_dx * Nn * VX(im1, j) - T(4) * inv_dy * Nn * VY(i, jm1) + T(2) * inv_dx * Nn * VX(i, j) +
+                       T(4) * inv_dy * Nn * VY(i, j);
+            }
+            T Nn = NN(i, jp1);
+            if (diag_out) *diag_out = -T(4) * inv_dy * Nn;
+            return -T(2) * inv_dx * Nn * VX(im1, jp1) - T(4) * inv_dy * Nn * VY(i, j) + T(2) * inv_dx * Nn * VX(i, jp1) +
+                   T(4) * inv_dy * Nn * VY(i, jp1);
+        }
+    }
+    // inner SSA rows
+    if (pl == 0) {
+        T d = -T(4) * inv_dxdx * (NN(ip1, j) + NN(i, j)) - T(1) * inv_dydy * (NB(i, j) + NB(i, jm1)) - (T)dgx[c];
+        if (diag_out) *diag_out = d;
+        T s = d * VX(i, j);
+        s += T(4) * inv_dxdx * NN(ip1, j) * VX(ip1, j);
+        s += T(4) * inv_dxdx * NN(i, j) * VX(im1, j);
+        s += T(1) * inv_dydy * NB(i, j) * VX(i, jp1);
+        s += T(1) * inv_dydy * NB(i, jm1) * VX(i, jm1);
+        s += (-T(2) * inv_dxdy * NN(i, j) - T(1) * inv_dxdy * NB(i, j)) * VY(i, j);
+        s += (T(2) * inv_dxdy * NN(ip1, j) + T(1) * inv_dxdy * NB(i, j)) * VY(ip1, j);
+        s += (-T(2) * inv_dxdy * NN(ip1, j) - T(1) * inv_dxdy * NB(i, jm1)) * VY(ip1, jm1);
+        s += (T(2) * inv_dxdy * NN(i, j) + T(1) * inv_dxdy * NB(i, jm1)) * VY(i, jm1);
+        return s;
+    } else {
+        T d = -T(4) * inv_dydy * (NN(i, jp1) + NN(i, j)) - T(1) * inv_dxdx * (NB(i, j) + NB(im1, j)) - (T)dgy[c];
+        if (diag_out) *diag_out = d;
+        T s = d * VY(i, j);
+        s += T(4) * inv_dydy * NN(i, jp1) * VY(i, jp1);
+        s += T(4) * inv_dydy * NN(i, j) * VY(i, jm1);
+        s += T(1) * inv_dxdx * NB(i, j) * VY(ip1, j);
+        s += T(1) * inv_dxdx * NB(im1, j) * VY(im1, j);
+        s += (-T(2) * inv_dxdy * NN(i, j) - T(1) * inv_dxdy * NB(i, j)) * VX(i, j);
+        s += (T(2) * inv_dxdy * NN(i, jp1) + T(1) * inv_dxdy * NB(i, j)) * VX(i, jp1);
+        s += (-T(2) * inv_dxdy * NN(i, jp1) - T(1) * inv_dxdy * NB(im1, j)) * VX(im1, jp1);
+        s += (T(2) * inv_dxdy * NN(i, j) + T(1) * inv_dxdy * NB(im1, j)) * VX(im1, j);
+        return s;
+    }
+#undef VX
+#undef VY
+#undef NN
+#undef NB
+}
+
+template <typename T, typename CT>
+YG_DEV void operator_apply(const Inst& I, const Geo& G, Team& Tm, bool energy, const CT* N, const CT* Nab,
+                           const CT* dgx, const CT* dgy, const T* v, T* y) {
+    if (energy) {
+        energy_apply<T, CT>(I, G, Tm, N, Nab, dgx, dgy, v, y);
+    } else {
+        for (int u = Tm.tid; u < G.nu; u += Tm.nthr) y[u] = residual_row<T, CT>(I, G, N, Nab, dgx, dgy, v, u, nullptr);
+    }
+}
+
+// Operator functors for the Krylov solvers
+template <typename T, typename CT>
+struct StencilOp {
+    const Inst* I;
+    const Geo* G;
+    bool energy;
+    const CT *N, *Nab, *dgx, *dgy;
+    YG_DEV void operator()(Team& Tm, const T* v, T* y) const {
+        operator_apply<T, CT>(*I, *G, Tm, energy, N, Nab, dgx, dgy, v, y);
+    }
+};
+
+// CSR matrix (0-based), the lower seam linear_solver_matrix_solve
+struct CsrOp {
+    int n;
+    const int* ptr;
+    const int* idx;
+    const double* val;
+    YG_DEV void operator()(Team& Tm, const double* v, double* y) const {
+        for (int r = Tm.tid; r < n; r += Tm.nthr) {
+            double s = 0.0;
+            for (int k = ptr[r]; k < ptr[r + 1]; k++) s += val[k] * v[idx[k]];
+            y[r] = s;
+        }
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Solve setup: unknown classification (energy) or row kinds (residual)
+// ---------------------------------------------------------------------------
+__device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T) {
+    const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
+    const int nx = G.nx, ny = G.ny, n2 = G.n2;
+    const unsigned bb = G.bb;
+    // pass 1: kind and partner
+    for (int u = T.tid; u < G.nu; u += T.nthr) {
+        const int pl = (u >= n2) ? 1 : 0, c = u - pl * n2, i = c % nx, j = c / nx;
+        const int mask = pl ? I.mask_y[c] : I.mask_x[c];
+        const double uval = pl ? I.u_y[c] : I.u_x[c];
+        int kind, part = -1;
+        double dv = 0.0;
+        if (energy) {
+            kind = DOF_FREE;
+            auto edge = [&](bool fr, int inner) {
+                if (fr) { kind = DOF_TIED; part = inner; } else { kind = DOF_DIR; part = -1; }
+            };
+            if (mask == 0) kind = DOF_DIR;
+            else if (mask == -1) { kind = DOF_DIR; dv = uval; }
+            else if (pl == 0) {
+                if (i == 0 && !bper(bb, 2)) edge(bfree(bb, 2), 1 + nx * j);
+                else if (i == nx - 1 && !bper(bb, 0)) edge(bfree(bb, 0), nx - 2 + nx * j);
+                else if (j == 0 && !bper(bb, 3)) edge(bfree(bb, 3), i + nx * 1);
+                else if (j == ny - 1 && !bper(bb, 1)) edge(bfree(bb, 1), i + nx * (ny - 2));
+            } else {
+                if (j == 0 && !bper(bb, 3)) edge(bfree(bb, 3), n2 + i + nx * 1);
+                else if (j == ny - 1 && !bper(bb, 1)) edge(bfree(bb, 1), n2 + i + nx * (ny - 2));
+                else if (i == 0 && !bper(bb, 2)) edge(bfree(bb, 2), n2 + 1 + nx * j);
+                else if (i == nx - 1 && !bper(bb, 0)) edge(bfree(bb, 0), n2 + nx - 2 + nx * j);
+            }
+            I.ukind[u] = kind;
+            I.rpart[u] = part;
+            I.dval[u] = dv;
+        } else {
+            int rk = RROW_INNER;
+            if (mask == 0) rk = RROW_ID;
+            else if (mask == -1) rk = RROW_ID;
+            else {
+                // border order: ux left, right, lower, upper; uy lower, upper, left, right
+                int side[4], partner[4];
+                if (pl == 0) {
+                    side[0] = 2; partner[0] = 1 + nx * j;
+                    side[1] = 0; partner[1] = nx - 2 + nx * j;
+                    side[2] = 3; partner[2] = i + nx * 1;
+                    side[3] = 1; partner[3] = i + nx * (ny - 2);
+                } else {
+                    side[0] = 3; partner[0] = n2 + i + nx * 1;
+                    side[1] = 1; partner[1] = n2 + i + nx * (ny - 2);
+                    side[2] = 2; partner[2] = n2 + 1 + nx * j;
+                    side[3] = 0; partner[3] = n2 + nx - 2 + nx * j;
+                }
+                bool at[4];
+                if (pl == 0) { at[0] = (i == 0); at[1] = (i == nx - 1); at[2] = (j == 0); at[3] = (j == ny - 1); }
+                else { at[0] = (j == 0); at[1] = (j == ny - 1); at[2] = (i == 0); at[3] = (i == nx - 1); }
+                bool done = false;
+                for (int s = 0; s < 4 && !done; s++) {
+                    if (at[s] && !bper(bb, side[s])) {
+                        done = true;
+                        if (bfree(bb, side[s])) { rk = RROW_FREESLIP; part = partner[s]; }
+                        else rk = RROW_ID;
+                    }
+                }
+                if (!done && mask == 3) rk = RROW_FRONT;
+            }
+            I.ukind[u] = rk;
+            I.rpart[u] = part;
+            I.emap[u] = u;
+        }
+    }
+    if (!energy) return team_barrier(T);
+    if (!team_barrier(T)) return false;
+    // pass 2: resolve tied chains to their free root (depth <= 8)
+    double bad = 0.0;
+    for (int u = T.tid; u < G.nu; u += T.nthr) {
+        int m = u, depth = 0;
+        while (I.ukind[m] == DOF_TIED) {
+            m = I.rpart[m];
+            if (++depth > 8) { bad = 1.0; break; }
+        }
+        I.emap[u] = m;     // root for now
+    }
+    if (!team_allreduce(T, &bad, 1)) return false;
+    if (bad > 0.0) return false;
+    // pass 3: a tied unknown whose root is Dirichlet is Dirichlet (value of the root)
+    for (int u = T.tid; u < G.nu; u += T.nthr) {
+        int k = I.ukind[u];
+        if (k == DOF_TIED) {
+            int r = I.emap[u];
+            if (I.ukind[r] == DOF_DIR) {
+                I.dval[u] = I.dval[r];
+                I.rpart[u] = -2;     // mark: becomes Dirichlet
+            }
+        }
+    }
+    if (!team_barrier(T)) return false;
+    for (int u = T.tid; u < G.nu; u += T.nthr) {
+        if (I.rpart[u] == -2) {
+            I.ukind[u] = DOF_DIR;
+            I.rpart[u] = -1;
+        }
+    }
+    if (!team_barrier(T)) return false;
+    // pass 4: column map (free: self, tied: root, Dirichlet: -1) and member lists
+    for (int u = T.tid; u < G.nu; u += T.nthr) {
+        int k = I.ukind[u];
+        int r = I.emap[u];
+        if (k == DOF_DIR) I.emap[u] = -1;
+        else if (k == DOF_FREE) I.emap[u] = u;
+        else I.emap[u] = r;
+        (void)r;
+    }
+    if (!team_barrier(T)) return false;
+    for (int u = T.tid; u < G.nu; u += T.nthr) {
+        int* mem = I.mem + 3 * u;
+        mem[0] = mem[1] = mem[2] = -1;
+        if (I.ukind[u] != DOF_FREE) continue;
+        const int pl = (u >= n2) ? 1 : 0, c = u - pl * n2, i = c % nx, j = c / nx;
+        int nm = 0;
+        // tied unknowns of the same plane within one cell of the root, in unknown order
+        for (int dj = -1; dj <= 1; dj++)
+            for (int di = -1; di <= 1; di++) {
+                int a = i + di, b = j + dj;
+                if (a < 0 || a >= nx || b < 0 || b >= ny || (di == 0 && dj == 0)) continue;
+                int t = pl * n2 + a + nx * b;
+                if (I.ukind[t] == DOF_TIED && I.emap[t] == u && nm < 3) mem[nm++] = t;
+            }
+    }
+    return team_barrier(T);
+}
+
+// ---------------------------------------------------------------------------
+// Phase: linear system -- rhs, start vector, Jacobi diagonal (FP64)
+// ---------------------------------------------------------------------------
+__device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, double& bnorm2) {
+    const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
+    const bool drag = (P.ssa_vel_lim_method == YGPU_VEL_LIM_DRAG);
+    const int n2 = G.n2, nx = G.nx, ny = G.ny;
+    const double* N = I.visc_int;
+    double bn2 = 0.0;
+    for (int u = T.tid; u < G.nu; u += T.nthr) {
+        const int pl = (u >= n2) ? 1 : 0, c = u - pl * n2;
+        const double uval = pl ? I.u_y[c] : I.u_x[c];
+        double b, x0, d = 1.0;
+        if (energy) {
+            const int k = I.ukind[u];
+            if (k == DOF_DIR) { b = I.dval[u]; x0 = I.dval[u]; }
+            else if (k == DOF_TIED) { b = 0.0; x0 = 0.0; }
+            else {
+                // forcing of the root and its members, minus the lifted Dirichlet columns
+                b = 0.0;
+                d = 0.0;
+                const int* mem = I.mem + 3 * u;
+                for (int m = -1; m < 3; m++) {
+                    int mm = (m < 0) ? u : mem[m];
+                    if (mm < 0) break;
+                    const int mpl = (mm >= n2) ? 1 : 0, mc = mm - mpl * n2, mi = mc % nx, mj = mc / nx;
+                    const int mask = mpl ? I.mask_y[mc] : I.mask_x[mc];
+                    const double w = (mask == 3 || mask == 4) ? 0.5 : 1.0;
+                    if (drag) b = b + w * (mpl ? I.lr_y[mc] : I.lr_x[mc]) * G.dxdy;
+                    if (mask == 3) {
+                        int ipj = mpl ? mi + nx * ((mj == ny - 1) ? 0 : mj + 1) : ((mi == nx - 1) ? 0 : mi + 1) + nx * mj;
+                        double tl = mpl ? I.taul_y[mc] : I.taul_x[mc];
+                        double dl = mpl ? G.dx : G.dy;
+                        if (I.f_ice[mc] == 1.0 && I.f_ice[ipj] < 1.0) b = b + tl * dl;
+                        else b = b - tl * dl;
+                    } else {
+                        b = b - (mpl ? I.taud_y[mc] : I.taud_x[mc]) * G.dxdy;
+                    }
+                    auto lift = [&](int dd) -> double {
+                        if (dd < 0) return 0.0;
+                        return (I.ukind[dd] == DOF_DIR) ? I.dval[dd] : 0.0;
+                    };
+                    b = b - member_elems<double>(G, N, I.Nab, mm, lift);
+                    auto unit = [&](int dd) -> double {
+                        if (dd < 0) return 0.0;
+                        return (I.emap[dd] == u) ? 1.0 : 0.0;
+                    };
+                    d = d + (mpl ? I.drag_y[mc] : I.drag_x[mc]) + member_elems<double>(G, N, I.Nab, mm, unit);
+                }
+                x0 = uval;
+            }
+        } else {
+            const int rk = I.ukind[u];
+            const int mask = pl ? I.mask_y[c] : I.mask_x[c];
+            if (rk == RROW_ID) {
+                b = (mask == -1) ? uval : 0.0;
+                x0 = (mask == -1) ? uval : 0.0;
+            } else if (rk == RROW_FREESLIP) {
+                b = 0.0;
+                x0 = uval;
+            } else if (rk == RROW_FRONT) {
+                b = pl ? I.taul_y[c] : I.taul_x[c];
+                x0 = uval;
+                residual_row<double, double>(I, G, N, I.Nab, I.drag_x, I.drag_y, I.x, u, &d);
+            } else {
+                const double w = (mask == 4) ? 0.5 : 1.0;
+                double lr = drag ? w * (pl ? I.lr_y[c] : I.lr_x[c]) : 0.0;
+                b = (pl ? I.taud_y[c] : I.taud_x[c]) - lr;
+                x0 = uval;
+                residual_row<double, double>(I, G, N, I.Nab, I.drag_x, I.drag_y, I.x, u, &d);
+            }
+        }
+        if (P.lin_initx_zeros) x0 = 0.0;
+        I.b[u] = b;
+        I.x[u] = x0;
+        I.dinv[u] = (d != 0.0) ? 1.0 / d : 1.0;
+        bn2 += b * b;
+    }
+    bnorm2 = bn2;
+}
+
+// ---------------------------------------------------------------------------
+// Krylov solvers (team-parallel, deterministic reductions)
+// ---------------------------------------------------------------------------
+// CG with Jacobi (x updated in place). Returns LIS status; iters/relres out.
+template <typename T, typename Op, typename CT>
+__device__ __noinline__ int krylov_cg(Team& Tm, int nu, const Op& A, const CT* dinv, T* x, const T* b, T* r, T* p, T* q, T* z,
+                     int maxiter, double tol, double bnrm, bool precond, int& iters, double& relres, bool& ok) {
+    ok = true;
+    iters = 0;
+    // r = b - A x
+    A(Tm, x, q);
+    double red[2] = {0.0, 0.0};
+    for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+        T ru = b[u] - q[u];
+        r[u] = ru;
+        T zu = precond ? (T)dinv[u] * ru : ru;
+        z[u] = zu;
+        p[u] = zu;
+        red[0] += (double)ru * (double)ru;
+        red[1] += (double)ru * (double)zu;
+    }
+    if (!(ok = team_allreduce(Tm, red, 2))) return YGPU_ERR_TIMEOUT;
+    relres = sqrt(red[0]) / bnrm;
+    if (relres <= tol) return YGPU_OK;
+    double rz = red[1];
+    for (int it = 1; it <= maxiter; it++) {
+        A(Tm, p, q);
+        double pq = 0.0;
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) pq += (double)p[u] * (double)q[u];
+        if (!(ok = team_allreduce(Tm, &pq, 1))) return YGPU_ERR_TIMEOUT;
+        iters = it;
+        if (pq == 0.0 || !isfinite(pq)) return YGPU_BREAKDOWN;
+        const double alpha = rz / pq;
+        double rr[2] = {0.0, 0.0};
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+            x[u] = x[u] + (T)alpha * p[u];
+            T ru = r[u] - (T)alpha * q[u];
+            r[u] = ru;
+            T zu = precond ? (T)dinv[u] * ru : ru;
+            z[u] = zu;
+            rr[0] += (double)ru * (double)ru;
+            rr[1] += (double)ru * (double)zu;
+        }
+        if (!(ok = team_allreduce(Tm, rr, 2))) return YGPU_ERR_TIMEOUT;
+        relres = sqrt(rr[0]) / bnrm;
+        if (relres <= tol) return YGPU_OK;
+        const double beta = rr[1] / rz;
+        rz = rr[1];
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) p[u] = z[u] + (T)beta * p[u];
+        if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
+    }
+    return YGPU_MAXITER;
+}
+
+// BiCGSTAB with Jacobi (van der Vorst 1992, as in the oracle)
+template <typename T, typename Op, typename CT>
+__device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const CT* dinv, T* x, const T* b, T* r, T* rt, T* p, T* v,
+                           T* s, T* t, T* ph, T* sh, int maxiter, double tol, double bnrm, bool precond, int& iters,
+                           double& relres, bool& ok) {
+    ok = true;
+    iters = 0;
+    A(Tm, x, v);
+    double red[2] = {0.0, 0.0};
+    for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+        T ru = b[u] - v[u];
+        r[u] = ru;
+        rt[u] = ru;
+        p[u] = T(0);
+        red[0] += (double)ru * (double)ru;
+    }
+    if (!(ok = team_allreduce(Tm, red, 1))) return YGPU_ERR_TIMEOUT;
+    relres = sqrt(red[0]) / bnrm;
+    if (relres <= tol) return YGPU_OK;
+    double rho = red[0];     // (rt, r) with rt = r
+    double rho_old = 1.0, alpha = 1.0, omega = 1.0;
+    for (int it = 1; it <= maxiter; it++) {
+        iters = it;
+        if (rho == 0.0 || !isfinite(rho)) return YGPU_BREAKDOWN;
+        const double beta = (it == 1) ? 0.0 : (rho / rho_old) * (alpha / omega);
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+            T pu = (it == 1) ? r[u] : r[u] + (T)beta * (p[u] - (T)omega * v[u]);
+            p[u] = pu;
+            ph[u] = precond ? (T)dinv[u] * pu : pu;
+        }
+        if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
+        A(Tm, ph, v);
+        double tv = 0.0;
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) tv += (double)rt[u] * (double)v[u];
+        if (!(ok = team_allreduce(Tm, &tv, 1))) return YGPU_ERR_TIMEOUT;
+        if (tv == 0.0 || !isfinite(tv)) return YGPU_BREAKDOWN;
+        alpha = rho / tv;
+        double ss = 0.0;
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+            T su = r[u] - (T)alpha * v[u];
+            s[u] = su;
+            sh[u] = precond ? (T)dinv[u] * su : su;
+            ss += (double)su * (double)su;
+        }
+        if (!(ok = team_allreduce(Tm, &ss, 1))) return YGPU_ERR_TIMEOUT;
+        if (sqrt(ss) / bnrm <= tol) {
+            for (int u = Tm.tid; u < nu; u += Tm.nthr) x[u] = x[u] + (T)alpha * ph[u];
+            relres = sqrt(ss) / bnrm;
+            if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
+            return YGPU_OK;
+        }
+        A(Tm, sh, t);
+        double ts[2] = {0.0, 0.0};
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+            ts[0] += (double)t[u] * (double)s[u];
+            ts[1] += (double)t[u] * (double)t[u];
+        }
+        if (!(ok = team_allreduce(Tm, ts, 2))) return YGPU_ERR_TIMEOUT;
+        if (ts[1] == 0.0 || !isfinite(ts[1])) return YGPU_BREAKDOWN;
+        omega = ts[0] / ts[1];
+        double rr[2] = {0.0, 0.0};
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+            x[u] = x[u] + (T)alpha * ph[u] + (T)omega * sh[u];
+            T ru = s[u] - (T)omega * t[u];
+            r[u] = ru;
+            rr[0] += (double)ru * (double)ru;
+            rr[1] += (double)rt[u] * (double)ru;
+        }
+        if (!(ok = team_allreduce(Tm, rr, 2))) return YGPU_ERR_TIMEOUT;
+        relres = sqrt(rr[0]) / bnrm;
+        if (relres <= tol) return YGPU_OK;
+        if (omega == 0.0) return YGPU_BREAKDOWN;
+        rho_old = rho;
+        rho = rr[1];
+    }
+    return YGPU_MAXITER;
+}
+
+// ---------------------------------------------------------------------------
+// Linear solve of one Picard iteration: FP64, or FP32 inside FP64 defect correction
+// ---------------------------------------------------------------------------
+__device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, double bnrm, int& iters,
+                        double& relres, int& outer, bool& ok) {
+    const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
+    const bool pre = (P.lin_precond != YGPU_PRE_NONE);
+    // MINRES requests run CG on the symmetric energy system, BiCGSTAB on the residual one
+    const bool use_cg = energy ? (P.lin_solver != YGPU_LIN_BICGSTAB) : false;
+    outer = 0;
+    const StencilOp<double, double> A64{&I, &G, energy, I.visc_int, I.Nab, I.drag_x, I.drag_y};
+    if (P.precision != YGPU_PREC_MIXED) {
+        if (use_cg)
+            return krylov_cg<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.p, I.q, I.z, P.lin_maxiter, P.lin_tol, bnrm,
+                                     pre, iters, relres, ok);
+        return krylov_bicgstab<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.rt, I.p, I.v, I.s, I.t, I.ph, I.sh,
+                                       P.lin_maxiter, P.lin_tol, bnrm, pre, iters, relres, ok);
+    }
+    const StencilOp<float, float> A32{&I, &G, energy, I.fN, I.fNab, I.fdrag_x, I.fdrag_y};
+    // ---- mixed: FP32 coefficients, FP32 inner Krylov, FP64 outer residual ----
+    for (int c = T.tid; c < G.n2; c += T.nthr) {
+        I.fN[c] = (float)I.visc_int[c];
+        I.fNab[c] = (float)I.Nab[c];
+        I.fdrag_x[c] = (float)I.drag_x[c];
+        I.fdrag_y[c] = (float)I.drag_y[c];
+    }
+    for (int u = T.tid; u < G.nu; u += T.nthr) I.fdinv[u] = (float)I.dinv[u];
+    if (!(ok = team_barrier(T))) return YGPU_ERR_TIMEOUT;
+    const double inner_tol = (P.inner_tol > 0.0) ? P.inner_tol : 1e-3;
+    const int inner_max = (P.inner_maxiter > 0) ? P.inner_maxiter : P.lin_maxiter;
+    int total = 0;
+    int status = YGPU_MAXITER;
+    const int max_outer = 60;
+    for (int o = 0; o < max_outer; o++) {
+        // r64 = b - A64 x (FP64 residual of the outer iterate)
+        A64(T, I.x, I.q);
+        double rr = 0.0;
+        for (int u = T.tid; u < G.nu; u += T.nthr) {
+            double ru = I.b[u] - I.q[u];
+            I.r[u] = ru;
+            rr += ru * ru;
+        }
+        if (!(ok = team_allreduce(T, &rr, 1))) return YGPU_ERR_TIMEOUT;
+        relres = sqrt(rr) / bnrm;
+        if (relres <= P.lin_tol) { status = YGPU_OK; break; }
+        if (total >= P.lin_maxiter) { status = YGPU_MAXITER; break; }
+        // inner FP32 solve of A d = r, d0 = 0, scaled by ||r||
+        const double sc = 1.0 / sqrt(rr);
+        for (int u = T.tid; u < G.nu; u += T.nthr) {
+            I.fr[u] = (float)(I.r[u] * sc);
+            I.fx[u] = 0.0f;
+        }
+        if (!(ok = team_barrier(T))) return YGPU_ERR_TIMEOUT;
+        int it = 0;
+        double rel_in = 0.0;
+        int st;
+        if (use_cg)
+            st = krylov_cg<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.fz, I.fp, I.fq, I.fs, inner_max, inner_tol, 1.0,
+                                  pre, it, rel_in, ok);
+        else
+            st = krylov_bicgstab<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.fz, I.frt, I.fp, I.fv, I.fs, I.ft, I.fph,
+                                        I.fsh, inner_max, inner_tol, 1.0, pre, it, rel_in, ok);
+        if (!ok) return YGPU_ERR_TIMEOUT;
+        total += it;
+        outer++;
+        // x += d (FP64 accumulation)
+        for (int u = T.tid; u < G.nu; u += T.nthr) I.x[u] = I.x[u] + (double)I.fx[u] / sc;
+        if (!(ok = team_barrier(T))) return YGPU_ERR_TIMEOUT;
+        if (st == YGPU_BREAKDOWN && it <= 1) { status = YGPU_BREAKDOWN; break; }
+    }
+    iters = total;
+    return status;
+}
+
+// ---------------------------------------------------------------------------
+// Phase: epilogue of one Picard iteration
+// ---------------------------------------------------------------------------
+__device__ __noinline__ void phase_epilogue(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, bool diva, double red[4]) {
+    const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
+    const double lim = P.ssa_vel_max, rel = P.ssa_iter_rel;
+    const double vel_tol = 1e-5;
+    double r1 = 0.0, r2 = 0.0, nchk = 0.0, nbad = 0.0;
+    for (int c = T.tid; c < G.n2; c += T.nthr) {
+        double uv[2];
+#pragma unroll
+        for (int pl = 0; pl < 2; pl++) {
+            const int u = pl * G.n2 + c;
+            int src = u;
+            if (energy) {
+                int e = I.emap[u];
+                if (e >= 0) src = e;
+            }
+            double val = I.x[src];
+            // linear_solver_save_velocity: underflow flush
+            if (fabs(val) < TOL_UNDERFLOW) val = 0.0;
+            // ssa_vel_clip (NaN passes through)
+            if (val > lim) val = lim;
+            if (val < -lim) val = -lim;
+            // picard_relax_vel
+            const double up = pl ? I.uy_nm1[c] : I.ux_nm1[c];
+            val = up + rel * (val - up);
+            uv[pl] = val;
+            // picard_calc_convergence_l2 contributions
+            const int mask = pl ? I.mask_y[c] : I.mask_x[c];
+            if (fabs(val) > vel_tol && mask > 0) {
+                nchk += 1.0;
+                double t = val - up;
+                if (fabs(t) < TOL_UNDERFLOW) t = 0.0;
+                r1 += t * t;
+                t = up;
+                if (fabs(t) < TOL_UNDERFLOW) t = 0.0;
+                r2 += t * t;
+            }
+            if (mask > 0 && !isfinite(val)) nbad += 1.0;
+            // picard_calc_convergence_l1rel_matrix
+            double err = (fabs(val) > 1e-2) ? 2.0 * fabs(val - up) / fabs(val + up + 1e-5) : 0.0;
+            if (pl) I.err_y[c] = err; else I.err_x[c] = err;
+        }
+        I.u_x[c] = uv[0];
+        I.u_y[c] = uv[1];
+        if (diva) {
+            // calc_basal_stress (velocity_diva.f90:1011-1050) and calc_vel_basal (:960-1009)
+            double tx = I.bm_x[c] * uv[0];
+            if (fabs(tx) < TOL_UNDERFLOW) tx = 0.0;
+            double ty = I.bm_y[c] * uv[1];
+            if (fabs(ty) < TOL_UNDERFLOW) ty = 0.0;
+            I.taub_x[c] = tx;
+            I.taub_y[c] = ty;
+            if (P.no_slip) {
+                I.ux_b[c] = 0.0;
+                I.uy_b[c] = 0.0;
+            } else {
+                I.ux_b[c] = uv[0] - tx * I.F2x[c];
+                I.uy_b[c] = uv[1] - ty * I.F2y[c];
+            }
+        }
+    }
+    red[0] = r1;
+    red[1] = r2;
+    red[2] = nchk;
+    red[3] = nbad;
+}
+
+// ---------------------------------------------------------------------------
+// Final passes after the Picard loop
+// ---------------------------------------------------------------------------
+__device__ __noinline__ double count_lim_part(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T) {
+    const bool drag = (P.ssa_vel_lim_method == YGPU_VEL_LIM_DRAG);
+    const double s0 = 0.8 * P.ssa_vel_max, umax = P.ssa_vel_max;
+    const double* ux = I.u_x;
+    const double* uy = I.u_y;
+    double n = 0.0;
+    for (int c = T.tid; c < G.n2; c += T.nthr) {
+        Nb b = make_nb(G, c);
+        const int i = b.i, j = b.j;
+        if (I.mask_x[c] >= 1) {
+            if (drag) {
+                double uc = 0.25 * (uy[c] + uy[CI(b.ip1, j)] + uy[CI(i, b.jm1)] + uy[CI(b.ip1, b.jm1)]);
+                if (ux[c] * ux[c] + uc * uc > s0 * s0) n += 1.0;
+            } else if (fabs(ux[c]) >= umax) n += 1.0;
+        }
+        if (I.mask_y[c] >= 1) {
+            if (drag) {
+                double uc = 0.25 * (ux[c] + ux[CI(b.im1, j)] + ux[CI(i, b.jp1)] + ux[CI(b.im1, b.jp1)]);
+                if (uy[c] * uy[c] + uc * uc > s0 * s0) n += 1.0;
+            } else if (fabs(uy[c]) >= umax) n += 1.0;
+        }
+    }
+    return n;
+}
+
+// DIVA: final vertical shear (from the state at the start of the last
+// iteration) and the 3D velocity (calc_vel_horizontal_3D, velocity_diva.f90:431-508)
+__device__ __noinline__ void phase_diva_final(const Inst& I, const Geo& G, Team& T, const double* vlast_cur, const double* vfinal) {
+    const int n2 = G.n2, nz = G.nz;
+    const double* f = I.f_ice;
+    const double* zeta = I.zeta;
+    for (int c = T.tid; c < n2; c += T.nthr) {
+        Nb n = make_nb(G, c);
+        const int cx = CI(n.ip1, n.j), cy = CI(n.i, n.jp1);
+        double F1c = 0.0, F1x = 0.0, F1y = 0.0;
+        double gc = 0.0, gx = 0.0, gy = 0.0;
+        const bool ic = (f[c] == 1.0), ix = (f[cx] == 1.0), iy = (f[cy] == 1.0);
+        for (int k = 0; k < nz; k++) {
+            const size_t o = (size_t)k * n2;
+            const double omz = 1.0 - zeta[k];
+            // shear at the start of the last iteration
+            double va = stag_margin(vlast_cur[o + c], vlast_cur[o + cx], f[c], f[cx]);
+            I.duxdz[o + c] = (va != 0.0) ? (I.tbp_x[c] / va) * omz : 0.0;
+            va = stag_margin(vlast_cur[o + c], vlast_cur[o + cy], f[c], f[cy]);
+            I.duydz[o + c] = (va != 0.0) ? (I.tbp_y[c] / va) * omz : 0.0;
+            // F1 up to level k at this cell and its +x / +y neighbours
+            double g0 = ic ? (I.H[c] / vfinal[o + c]) * omz : 0.0;
+            double g1 = ix ? (I.H[cx] / vfinal[o + cx]) * omz : 0.0;
+            double g2 = iy ? (I.H[cy] / vfinal[o + cy]) * omz : 0.0;
+            if (k > 0) {
+                const double dz = zeta[k] - zeta[k - 1];
+                F1c = F1c + 0.5 * (g0 + gc) * dz;
+                F1x = F1x + 0.5 * (g1 + gx) * dz;
+                F1y = F1y + 0.5 * (g2 + gy) * dz;
+            }
+            gc = g0; gx = g1; gy = g2;
+            double fa = stag_margin(ic ? F1c : 0.0, ix ? F1x : 0.0, f[c], f[cx]);
+            double ux = I.ux_b[c] + I.taub_x[c] * fa;
+            fa = stag_margin(ic ? F1c : 0.0, iy ? F1y : 0.0, f[c], f[cy]);
+            double uy = I.uy_b[c] + I.taub_y[c] * fa;
+            I.ux3[o + c] = ux;
+            I.uy3[o + c] = uy;
+            I.ux_i[o + c] = ux - I.ux_b[c];
+            I.uy_i[o + c] = uy - I.uy_b[c];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The Picard loop of one instance, run by one team
+// ---------------------------------------------------------------------------
+__device__ __noinline__ void solve_instance(const Inst& I, const ygpu_dyn_par& P, Team& T) {
+    const bool diva = (I.kind == YGPU_KIND_DIVA);
+    const Geo G = make_geo(I, P);
+    InstOut* out = I.out;
+    const bool lead = (T.cta == 0 && threadIdx.x == 0);
+    int status = YGPU_OK, lin_status = YGPU_OK;
+    int iter_now = 0, lin_iter = 0, lin_fail = 0, outer_total = 0;
+    double resid = 0.0, lin_resid = 0.0;
+    bool ok = true;
+    // scratch for the strain rates (the drag arrays are free until the faces phase)
+    double* sdudx = I.lk_x;
+    double* sdudy = I.lk_y;
+    double* sdvdx = I.lr_x;
+    double* sdvdy = I.lr_y;
+    // ---- setup ----
+    for (int c = T.tid; c < G.n2; c += T.nthr) {
+        I.err_x[c] = 1.0;
+        I.err_y[c] = 1.0;
+        if (!diva) {
+            // set_inactive_margins (velocity_general.f90:1687-1750), SSA only
+            Nb n = make_nb(G, c);
+            const double fa = I.f_ice[c];
+            double fb = I.f_ice[CI(n.ip1, n.j)];
+            if ((fb == 0.0 && fa < 1.0) || (fa == 0.0 && fb < 1.0)) I.u_x[c] = 0.0;
+            fb = I.f_ice[CI(n.i, n.jp1)];
+            if ((fb == 0.0 && fa < 1.0) || (fa == 0.0 && fb < 1.0)) I.u_y[c] = 0.0;
+        }
+    }
+    if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+    if (!phase_classify(I, P, G, T)) { status = ld_acquire_s32(T.abort_all) ? YGPU_ERR_TIMEOUT : YGPU_ERR_BAD_ARG; goto finish; }
+
+    {
+        double* vcur = I.visc;
+        double* vnew = I.visc_alt;
+        int in_alt = 0;            // the current visc lives in visc_alt
+        double* last_cur = vcur;
+        for (int iter = 1; iter <= P.ssa_iter_max; iter++) {
+            const bool relax = diva ? true : (P.visc_method != 0);
+            if (P.visc_method == 1) {
+                phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
+                if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            }
+            phase_column(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true);
+            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            last_cur = vcur;
+            { double* tmp = vcur; vcur = vnew; vnew = tmp; in_alt ^= 1; }
+            phase_faces(I, P, G, T, diva);
+            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            double bn2 = 0.0;
+            phase_system(I, P, G, T, bn2);
+            if (!team_allreduce(T, &bn2, 1)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            int it = 0, outer = 0;
+            double rr = 0.0;
+            int st;
+            if (bn2 == 0.0) {
+                // homogeneous system: x = 0 (solver_linear.F90:162-174)
+                for (int u = T.tid; u < G.nu; u += T.nthr) I.x[u] = 0.0;
+                st = YGPU_OK;
+            } else {
+                st = linear_solve(I, P, G, T, sqrt(bn2), it, rr, outer, ok);
+                if (!ok) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            }
+            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            lin_iter += it;
+            outer_total += outer;
+            if (st != YGPU_OK) lin_fail++;
+            lin_status = st;
+            lin_resid = rr;
+            double red[4];
+            phase_epilogue(I, P, G, T, diva, red);
+            if (!team_allreduce(T, red, 4)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            resid = (red[2] > 0.0) ? sqrt(red[0]) / (sqrt(red[1]) + 1e-10) : 0.0;
+            iter_now = iter;
+            if (P.ssa_write_log && lead)
+                printf("ssa: %s %4d %12.4g | lin %6d %d\n", (resid < P.ssa_iter_conv) ? "C" : "", iter, resid, it, st);
+            if (red[3] > 0.0 || !isfinite(resid)) { status = YGPU_ERR_NONFINITE; break; }
+            if (resid < P.ssa_iter_conv || iter == P.ssa_iter_max) break;
+        }
+        if (status != YGPU_OK) goto finish;
+        // ---- after the loop ----
+        double nlim = count_lim_part(I, P, G, T);
+        if (diva) {
+            phase_diva_final(I, G, T, last_cur, vcur);
+        } else {
+            for (int c = T.tid; c < G.n2; c += T.nthr) {
+                // calc_basal_stress, velocity_ssa.f90:588-617
+                double tx = I.bm_x[c] * I.u_x[c], ty = I.bm_y[c] * I.u_y[c];
+                I.taub_x[c] = (fabs(tx) < 1e-5) ? 0.0 : tx;
+                I.taub_y[c] = (fabs(ty) < 1e-5) ? 0.0 : ty;
+            }
+        }
+        if (!team_allreduce(T, &nlim, 1)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+        if (!diva && P.visc_method == 0) {
+            // diagnose the viscosity of the solution (not used prognostically)
+            phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
+            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            ygpu_dyn_par P1 = P;
+            P1.visc_method = 1;
+            phase_column(I, P1, G, T, vcur, vcur, sdudx, sdudy, sdvdx, sdvdy, false, false, false, true);
+            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+        }
+        // the caller's visc_eff must hold the final viscosity
+        if (in_alt) {
+            for (size_t k = T.tid; k < (size_t)G.n2 * G.nz; k += T.nthr) I.visc[k] = I.visc_alt[k];
+        }
+        if (lead) out->lim_n = (int)nlim;
+    }
+finish:
+    if (lead) {
+        out->iter_now = iter_now;
+        out->lin_iter = lin_iter;
+        out->lin_fail = lin_fail;
+        out->resid = resid;
+        out->lin_resid = lin_resid;
+        out->outer_iter = outer_total;
+        out->lin_status = lin_status;
+        out->status = (status != YGPU_OK) ? status : lin_status;
+        out->converged = (status == YGPU_OK);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// The persistent kernel: teams take instances from the queue
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(YG_BLOCK, 2) ygpu_solve_kernel(const Inst* __restrict__ insts, int n_inst,
+                                                              ygpu_dyn_par P, TeamCtl* ctls, int team_ctas,
+                                                              int* queue, int* abort_all) {
+    __shared__ Inst sI;
+    __shared__ int s_inst;
+    Team T;
+    T.ncta = team_ctas;
+    T.cta = blockIdx.x % team_ctas;
+    T.tid = T.cta * blockDim.x + threadIdx.x;
+    T.nthr = team_ctas * blockDim.x;
+    T.ctl = ctls + blockIdx.x / team_ctas;
+    T.parity = 0;
+    T.abort_all = abort_all;
+    for (;;) {
+        if (T.cta == 0 && threadIdx.x == 0) {
+            int k = atomicAdd(queue, 1);
+            if (team_ctas == 1) s_inst = k;
+            else atomicExch(&T.ctl->inst, k);
+        }
+        if (!team_barrier(T)) return;
+        if (threadIdx.x == 0 && team_ctas > 1) s_inst = ld_acquire_s32(&T.ctl->inst);
+        __syncthreads();
+        const int k = s_inst;
+        if (k >= n_inst) return;
+        if (threadIdx.x == 0) sI = insts[k];
+        __syncthreads();
+        solve_instance(sI, P, T);
+        if (!team_barrier(T)) return;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// CSR seam: one team (the grid) solves A x = b with the LIS option semantics
+// ---------------------------------------------------------------------------
+struct CsrJob {
+    int n, method, precond, maxiter, initx_zeros;
+    double tol;
+    const int *ptr, *idx;
+    const double *val, *b;
+    double *x, *dinv, *r, *rt, *p, *q, *v, *s, *t, *ph, *sh, *z;
+    int* out_iters;
+    int* out_status;
+    double* out_relres;
+};
+
+__global__ void __launch_bounds__(YG_BLOCK) ygpu_csr_kernel(CsrJob J, TeamCtl* ctl, int* abort_all) {
+    Team T;
+    T.ncta = gridDim.x;
+    T.cta = blockIdx.x;
+    T.tid = blockIdx.x * blockDim.x + threadIdx.x;
+    T.nthr = gridDim.x * blockDim.x;
+    T.ctl = ctl;
+    T.parity = 0;
+    T.abort_all = abort_all;
+    const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+    // Jacobi diagonal and ||b||
+    double bn = 0.0;
+    for (int r = T.tid; r < J.n; r += T.nthr) {
+        double d = 0.0;
+        for (int k = J.ptr[r]; k < J.ptr[r + 1]; k++)
+            if (J.idx[k] == r) d += J.val[k];
+        if (J.method == YGPU_LIN_MINRES) d = fabs(d);
+        J.dinv[r] = (d != 0.0) ? 1.0 / d : 1.0;
+        if (J.initx_zeros) J.x[r] = 0.0;
+        bn += J.b[r] * J.b[r];
+    }
+    if (!team_allreduce(T, &bn, 1)) {
+        if (lead) *J.out_status = YGPU_ERR_TIMEOUT;
+        return;
+    }
+    int iters = 0, st;
+    double rel = 0.0;
+    bool ok = true;
+    if (bn == 0.0) {
+        for (int r = T.tid; r < J.n; r += T.nthr) J.x[r] = 0.0;
+        st = YGPU_OK;
+    } else {
+        const CsrOp A{J.n, J.ptr, J.idx, J.val};
+        const bool pre = (J.precond != YGPU_PRE_NONE);
+        if (J.method == YGPU_LIN_BICGSTAB)
+            st = krylov_bicgstab<double>(T, J.n, A, J.dinv, J.x, J.b, J.r, J.rt, J.p, J.v, J.s, J.t, J.ph, J.sh,
+                                         J.maxiter, J.tol, sqrt(bn), pre, iters, rel, ok);
+        else
+            st = krylov_cg<double>(T, J.n, A, J.dinv, J.x, J.b, J.r, J.p, J.q, J.z, J.maxiter, J.tol, sqrt(bn), pre,
+                                   iters, rel, ok);
+        if (!ok) st = YGPU_ERR_TIMEOUT;
+    }
+    if (lead) {
+        *J.out_iters = iters;
+        *J.out_status = st;
+        *J.out_relres = rel;
+    }
+}
+
+int ygpu_launch_csr(cudaStream_t stream, int n, const int* ptr, const int* idx, const double* val, const double* b,
+                    double* x, double* work, int method, int precond, int maxiter, double tol, int initx_zeros,
+                    int* d_out_i, double* d_out_d, TeamCtl* d_ctl, int* d_abort, int n_ctas) {
+    CsrJob J;
+    J.n = n; J.method = method; J.precond = precond; J.maxiter = maxiter; J.initx_zeros = initx_zeros; J.tol = tol;
+    J.ptr = ptr; J.idx = idx; J.val = val; J.b = b; J.x = x;
+    double* w[12];
+    for (int k = 0; k < 12; k++) w[k] = work + (size_t)k * n;
+    J.dinv = w[0]; J.r = w[1]; J.rt = w[2]; J.p = w[3]; J.q = w[4]; J.v = w[5]; J.s = w[6]; J.t = w[7];
+    J.ph = w[8]; J.sh = w[9]; J.z = w[10];
+    J.out_iters = d_out_i;
+    J.out_status = d_out_i + 1;
+    J.out_relres = d_out_d;
+    if (cudaMemsetAsync(d_abort, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    if (cudaMemsetAsync(d_ctl, 0, sizeof(TeamCtl), stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    void* args[] = {(void*)&J, (void*)&d_ctl, (void*)&d_abort};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)ygpu_csr_kernel, dim3(n_ctas), dim3(YG_BLOCK), args, 0,
+                                                stream);
+    if (e != cudaSuccess) {
+        ygpu_set_error("cooperative launch of the CSR solve failed: %s", cudaGetErrorString(e));
+        return YGPU_ERR_CUDA;
+    }
+    return YGPU_OK;
+}
+
+int ygpu_csr_max_ctas(int device) {
+    int nsm = 0, bps = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ygpu_csr_kernel, YG_BLOCK, 0);
+    return nsm * bps;
+}
+
+// ---------------------------------------------------------------------------
+// Host side: launch
+// ---------------------------------------------------------------------------
+static bool g_gqw_set[64] = {false};
+
+int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
+                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_queue, int* d_abort) {
+    if (device >= 0 && device < 64 && !g_gqw_set[device]) {
+        double w[4][4];
+        const int sx[4] = {-1, 1, 1, -1}, sy[4] = {-1, -1, 1, 1};
+        const double g = 1.0 / sqrt(3.0);
+        for (int q = 0; q < 4; q++)
+            for (int c = 0; c < 4; c++) {
+                volatile double ax = 1.0 + (double)(sx[q] * sx[c]) * g;
+                volatile double ay = 1.0 + (double)(sy[q] * sy[c]) * g;
+                volatile double pr = ax * ay;
+                w[q][c] = pr * 0.25;
+            }
+        if (cudaMemcpyToSymbol(c_gqw, w, sizeof(w)) != cudaSuccess) return YGPU_ERR_CUDA;
+        g_gqw_set[device] = true;
+    }
+    if (cudaMemsetAsync(d_queue, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    if (cudaMemsetAsync(d_abort, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    if (cudaMemsetAsync(d_ctls, 0, sizeof(TeamCtl) * (size_t)n_teams, stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    void* args[] = {(void*)&d_insts, (void*)&n_inst, (void*)&P, (void*)&d_ctls, (void*)&team_ctas, (void*)&d_queue,
+                    (void*)&d_abort};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)ygpu_solve_kernel, dim3(n_teams * team_ctas),
+                                                dim3(YG_BLOCK), args, 0, stream);
+    if (e != cudaSuccess) {
+        ygpu_set_error("cooperative launch of the solver failed: %s", cudaGetErrorString(e));
+        return YGPU_ERR_CUDA;
+    }
+    return YGPU_OK;
+}
+
+int ygpu_solver_max_ctas(int device) {
+    int nsm = 0, bps = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ygpu_solve_kernel, YG_BLOCK, 0);
+    return nsm * bps;
+}
+
+int ygpu_sm_count(int device) {
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    return nsm;
+}
+
+size_t ygpu_teamctl_bytes() { return sizeof(TeamCtl); }
+size_t ygpu_inst_bytes() { return sizeof(Inst); }

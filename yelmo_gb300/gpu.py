@@ -1,0 +1,210 @@
+"""Python host binding of libyelmo_gpu.so (the sm_103a solver).
+
+Mirrors the reference's solver interface for Python hosts:
+
+* ``calc_velocity(fields, dx, n_glen, par)`` -- calc_velocity_ssa /
+  calc_velocity_diva (velocity_ssa.f90:60, velocity_diva.f90:59) on a dict of
+  Fortran-ordered numpy arrays named as in the reference; INOUT arrays are
+  updated in place, the integer counters are returned.
+* ``calc_dyn_inputs(inst)`` / ``set_ssa_masks(...)`` / ``prepare(inst)`` -- the
+  fields calc_ydyn derives before the solve and set_ssa_masks, on the GPU.
+* ``linear_solver_matrix_solve(...)`` -- the CSR seam of solver_linear.F90:151.
+* ``DeviceSolver`` -- solves on device-resident fields (no host copies).
+
+There is no CPU fallback: if the library cannot be loaded, or no CUDA device is
+present, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .params import YdynParams
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libyelmo_gpu.so")
+_lib = None
+
+EXPORTS = [
+    "ygpu_dyn_par_defaults", "ygpu_parse_lis_opt", "ygpu_boundary_code", "ygpu_last_error", "ygpu_version",
+    "ygpu_calc_velocity_ssa", "ygpu_calc_velocity_diva", "ygpu_set_ssa_masks", "ygpu_calc_dyn_inputs",
+    "ygpu_linear_solver_matrix_solve", "ygpu_ctx_create", "ygpu_ctx_destroy", "ygpu_ctx_stream",
+    "ygpu_solve_device", "ygpu_solve_batch_device",
+]
+
+
+class YgpuError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {msg}")
+
+
+def lib(build_if_missing: bool = True):
+    """Load libyelmo_gpu.so (building it with nvcc if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH) and build_if_missing:
+        from . import build
+        build.build()
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: run python -m yelmo_gb300.build")
+    L = C.CDLL(LIB_PATH)
+    abi.declare_velocity(L.ygpu_calc_velocity_ssa, abi.SSA_ARGS)
+    abi.declare_velocity(L.ygpu_calc_velocity_diva, abi.DIVA_ARGS)
+    abi.declare_inputs(L.ygpu_calc_dyn_inputs)
+    abi.declare_masks(L.ygpu_set_ssa_masks)
+    L.ygpu_last_error.restype = C.c_char_p
+    L.ygpu_version.restype = C.c_char_p
+    L.ygpu_boundary_code.argtypes = [C.c_char_p]
+    L.ygpu_parse_lis_opt.argtypes = [C.c_char_p, C.POINTER(abi.DynPar)]
+    L.ygpu_dyn_par_defaults.argtypes = [C.POINTER(abi.DynPar)]
+    L.ygpu_ctx_create.restype = C.c_void_p
+    L.ygpu_ctx_create.argtypes = [C.c_int]
+    L.ygpu_ctx_destroy.argtypes = [C.c_void_p]
+    L.ygpu_ctx_stream.restype = C.c_void_p
+    L.ygpu_ctx_stream.argtypes = [C.c_void_p]
+    L.ygpu_solve_device.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.DynPar), C.POINTER(abi.Fields),
+                                    C.POINTER(abi.Stats)]
+    L.ygpu_solve_batch_device.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.DynPar), C.c_int,
+                                          C.POINTER(abi.Fields), C.POINTER(abi.Stats)]
+    ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+    L.ygpu_linear_solver_matrix_solve.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_char_p, ip, ip, dp]
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return lib().ygpu_last_error().decode()
+
+
+def _check(st, allow_linear=True):
+    if st < 0 or (not allow_linear and st != 0):
+        raise YgpuError(st, last_error())
+    return st
+
+
+def calc_velocity(fields: dict, dx: float, n_glen: float, par: YdynParams, dy: float | None = None) -> dict:
+    """calc_velocity_ssa / calc_velocity_diva on the GPU (host arrays, updated in place)."""
+    L = lib()
+    cpar = par.to_c()
+    dy = dx if dy is None else dy
+    if par.solver == "ssa":
+        out = abi.call_velocity(L.ygpu_calc_velocity_ssa, abi.SSA_ARGS, fields, dx, dy, n_glen, cpar)
+    else:
+        out = abi.call_velocity(L.ygpu_calc_velocity_diva, abi.DIVA_ARGS, fields, dx, dy, n_glen, cpar)
+    _check(out["status"])
+    return out
+
+
+def calc_dyn_inputs(inst) -> dict:
+    d = inst.input_buffers()
+    p = inst.par
+    _check(abi.call_inputs(lib().ygpu_calc_dyn_inputs, d, inst.dx, p.grad_lim, p.taud_lim, p.rho_ice,
+                           p.rho_sw, p.g, abi.BOUNDARY_CODES[p.boundaries]))
+    return d
+
+
+def set_ssa_masks(mask_frnt, f_ice, f_grnd, lateral_bc: str, boundaries: str):
+    nx, ny = f_ice.shape
+    mx = np.zeros((nx, ny), dtype=np.int32, order="F")
+    my = np.zeros((nx, ny), dtype=np.int32, order="F")
+    _check(lib().ygpu_set_ssa_masks(abi.ptr(mx, "i"), abi.ptr(my, "i"), abi.ptr(mask_frnt, "i"),
+                                    abi.ptr(f_ice, "d"), abi.ptr(f_grnd, "d"), abi.LATBC_CODES[lateral_bc],
+                                    abi.BOUNDARY_CODES[boundaries], nx, ny))
+    return mx, my
+
+
+def prepare(inst) -> dict:
+    """Cold-start state of one solve with the GPU prologue and masks."""
+    inputs = calc_dyn_inputs(inst)
+    f = inst.state(inputs)
+    f["ssa_mask_acx"], f["ssa_mask_acy"] = set_ssa_masks(
+        inputs["mask_frnt"], inputs["f_ice"], inputs["f_grnd"], inst.par.ssa_lat_bc, inst.par.boundaries)
+    return f
+
+
+def linear_solver_matrix_solve(a_ptr1, a_index1, a_value, b_value, x_value, lis_opt: str):
+    """GPU solve of a 1-based CSR system (linear_solver_class arrays); x updated in place."""
+    it, st, rr = C.c_int(0), C.c_int(0), C.c_double(0.0)
+    ret = lib().ygpu_linear_solver_matrix_solve(
+        len(b_value), abi.ptr(a_ptr1, "i"), abi.ptr(a_index1, "i"), abi.ptr(a_value, "d"),
+        abi.ptr(b_value, "d"), abi.ptr(x_value, "d"), lis_opt.encode(), C.byref(it), C.byref(st), C.byref(rr))
+    _check(ret)
+    return st.value, it.value, rr.value
+
+
+# ---------------------------------------------------------------------------
+# device-resident solves (torch tensors as device memory)
+# ---------------------------------------------------------------------------
+FIELD_NAMES_2D = ["ux_bar", "uy_bar", "ux_b", "uy_b", "taub_acx", "taub_acy", "beta", "beta_acx", "beta_acy",
+                  "beta_eff", "visc_eff_int", "ssa_err_acx", "ssa_err_acy", "c_bed", "f_slide", "taud_acx",
+                  "taud_acy", "taul_int_acx", "taul_int_acy", "H_ice", "f_ice", "H_grnd", "f_grnd",
+                  "f_grnd_acx", "f_grnd_acy", "z_sl", "z_bed", "z_srf"]
+FIELD_NAMES_3D = ["ux", "uy", "ux_i", "uy_i", "visc_eff", "duxdz", "duydz", "ATT"]
+INT_NAMES = ["ssa_mask_acx", "ssa_mask_acy"]
+STATE_NAMES = ["ux_bar", "uy_bar", "ux_b", "uy_b", "taub_acx", "taub_acy", "beta", "beta_acx", "beta_acy",
+               "visc_eff"]
+
+
+def to_device(fields: dict, device: str = "cuda"):
+    """Copy a field dict to torch device tensors (same memory layout as the Fortran arrays)."""
+    import torch
+    out = {}
+    for k, a in fields.items():
+        if not isinstance(a, np.ndarray):
+            continue
+        flat = np.ravel(a, order="F")
+        out[k] = torch.from_numpy(np.ascontiguousarray(flat)).to(device)
+    return out
+
+
+def make_fields(dev: dict, nx, ny, nz, dx, dy, n_glen) -> abi.Fields:
+    f = abi.Fields()
+    f.nx, f.ny, f.nz, f.dx, f.dy, f.n_glen = nx, ny, nz, dx, dy, n_glen
+    for name, _ in abi.Fields._fields_[6:]:
+        t = dev.get(name)
+        setattr(f, name, t.data_ptr() if t is not None else None)
+    return f
+
+
+class DeviceSolver:
+    """A solver context (one CUDA stream) for device-resident solves."""
+
+    def __init__(self, device: int = 0):
+        self.L = lib()
+        self.ctx = self.L.ygpu_ctx_create(device)
+        if not self.ctx:
+            raise YgpuError(abi.ERR_CUDA, last_error())
+
+    def close(self):
+        if self.ctx:
+            self.L.ygpu_ctx_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, kind: int, par: YdynParams, fields: abi.Fields) -> dict:
+        st = abi.Stats()
+        cpar = par.to_c()
+        r = self.L.ygpu_solve_device(self.ctx, kind, C.byref(cpar), C.byref(fields), C.byref(st))
+        _check(r)
+        out = st.as_dict()
+        out["return"] = r
+        return out
+
+    def solve_batch(self, kind: int, par: YdynParams, fields: list) -> list:
+        n = len(fields)
+        arr = (abi.Fields * n)(*fields)
+        sts = (abi.Stats * n)()
+        cpar = par.to_c()
+        r = self.L.ygpu_solve_batch_device(self.ctx, kind, C.byref(cpar), n, arr, sts)
+        _check(r)
+        return [s.as_dict() for s in sts]
