@@ -29,7 +29,11 @@ def case(name):
     if name == "marine_diva":
         return _tight(configs.marine_diva(n=33, nz=6))
     if name == "marine_diva_residual":
-        return _tight(configs.marine_diva(n=33, nz=6), ssa_solver="residual")
+        # With ~150 faces at the velocity limit this residual-form problem has
+        # fixed points that depend on the preconditioner (the oracle's ILU(0)
+        # and Jacobi answers differ by 16 %), so both sides use Jacobi here.
+        return _tight(configs.marine_diva(n=33, nz=6), ssa_solver="residual",
+                      ssa_lis_opt_residual="-i bicgstab -p jacobi -maxiter 20000 -tol 1.0e-11")
     # power-law friction with q = 1/3 ends in a Picard 2-cycle (beta toggles at
     # the beta_min floor), so the tight cases use q = 0.5 and Coulomb q = 1
     if name == "continent_diva":
