@@ -129,6 +129,10 @@ typedef struct ygpu_stats {
     int    outer_iter;          /* mixed: defect-correction steps, summed       */
     int    status;              /* YGPU_* of the solve                          */
     double device_ms;           /* device time of the solve (CUDA events)       */
+    double phase_ms[10];        /* device time per phase of the solve: setup, strain rates,
+                                   column (viscosity, integrals, beta), faces, linear system,
+                                   Krylov, epilogue, final passes; then the time spent in
+                                   team all-reduces over the solve and within the Krylov phase */
 } ygpu_stats;
 
 /* ---- parameter helpers -------------------------------------------------- */

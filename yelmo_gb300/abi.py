@@ -58,10 +58,16 @@ class Stats(C.Structure):
         ("ssa_iter_now", C.c_int), ("ssa_lin_iter", C.c_int), ("ssa_lin_fail", C.c_int),
         ("ssa_lim_n", C.c_int), ("ssa_resid", C.c_double), ("lin_resid", C.c_double),
         ("outer_iter", C.c_int), ("status", C.c_int), ("device_ms", C.c_double),
+        ("phase_ms", C.c_double * 10),
     ]
 
+    PHASES = ("setup", "strain", "column", "faces", "system", "krylov", "epilogue", "final", "sync_all",
+              "sync_krylov")
+
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "phase_ms"}
+        d["phase_ms"] = {n: float(self.phase_ms[i]) for i, n in enumerate(self.PHASES)}
+        return d
 
 
 _dp = C.POINTER(C.c_double)

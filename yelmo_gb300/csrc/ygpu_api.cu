@@ -246,10 +246,11 @@ static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
 static size_t inst_scratch_bytes(int nx, int ny, int nz, bool mixed) {
     size_t n2 = (size_t)nx * ny, nu = 2 * n2, n3 = n2 * nz;
     size_t b = al(n3 * 8);               // visc_alt
+    b += al(4 * n3 * 8) + al(n3 * 8);    // attp, lvis
     b += 16 * al(n2 * 8);                // 2D scratch
-    b += 14 * al(nu * 8);                // linear system
+    b += 15 * al(nu * 8);                // linear system
     b += 6 * al(nu * 4);                 // ukind, emap, mem(3), rpart
-    if (mixed) b += 4 * al(n2 * 4) + 12 * al(nu * 4);
+    if (mixed) b += 4 * al(n2 * 4) + 13 * al(nu * 4);
     return b;
 }
 
@@ -260,20 +261,24 @@ static void inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool
     auto Iv = [&](size_t n) { int* r = (int*)p; p += al(n * 4); return r; };
     auto Fv = [&](size_t n) { float* r = (float*)p; p += al(n * 4); return r; };
     I.visc_alt = D(n3);
+    I.attp = D(4 * n3);
+    I.lvis = D(n3);
     I.ux_nm1 = D(n2); I.uy_nm1 = D(n2); I.bm_x = D(n2); I.bm_y = D(n2);
     I.lk_x = D(n2); I.lk_y = D(n2); I.lr_x = D(n2); I.lr_y = D(n2);
     I.F2 = D(n2); I.F2x = D(n2); I.F2y = D(n2); I.Nab = D(n2);
     I.tbp_x = D(n2); I.tbp_y = D(n2); I.drag_x = D(n2); I.drag_y = D(n2);
     I.x = D(nu); I.b = D(nu); I.r = D(nu); I.p = D(nu); I.q = D(nu); I.z = D(nu); I.dinv = D(nu);
     I.rt = D(nu); I.v = D(nu); I.s = D(nu); I.t = D(nu); I.ph = D(nu); I.sh = D(nu); I.dval = D(nu);
+    I.m2 = D(nu);
     I.ukind = Iv(nu); I.emap = Iv(nu); I.mem = Iv(3 * nu); I.rpart = Iv(nu);
     if (mixed) {
         I.fN = Fv(n2); I.fNab = Fv(n2); I.fdrag_x = Fv(n2); I.fdrag_y = Fv(n2);
         I.fdinv = Fv(nu); I.fx = Fv(nu); I.fr = Fv(nu); I.fp = Fv(nu); I.fq = Fv(nu); I.fz = Fv(nu);
         I.frt = Fv(nu); I.fv = Fv(nu); I.fs = Fv(nu); I.ft = Fv(nu); I.fph = Fv(nu); I.fsh = Fv(nu);
+        I.fm2 = Fv(nu);
     } else {
         I.fN = I.fNab = I.fdrag_x = I.fdrag_y = I.fdinv = nullptr;
-        I.fx = I.fr = I.fp = I.fq = I.fz = I.frt = I.fv = I.fs = I.ft = I.fph = I.fsh = nullptr;
+        I.fx = I.fr = I.fp = I.fq = I.fz = I.frt = I.fv = I.fs = I.ft = I.fph = I.fsh = I.fm2 = nullptr;
     }
 }
 
@@ -425,6 +430,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
             S.outer_iter = o.outer_iter;
             S.status = s_k;
             S.device_ms = ms;
+            for (int q = 0; q < 10; q++) S.phase_ms[q] = o.phase_ns[q] * 1e-6;
         }
         if (s_k < 0 && (worst >= 0 || s_k < worst)) worst = s_k;
         else if (worst >= 0 && s_k > worst) worst = s_k;

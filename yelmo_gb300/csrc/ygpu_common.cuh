@@ -96,7 +96,15 @@ struct InstOut {
     int lin_status;    // status of the last linear solve
     int outer_iter;    // mixed: defect-correction steps
     int converged;
+    double phase_ns[10];   // device time per phase: setup, strain, column, faces, system, krylov, epilogue,
+                           // final, and the all-reduce share of the solve and of the Krylov phase
 };
+
+YG_DEV unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Descriptor of one instance (device memory). Field pointers follow
 // ygpu_fields; the rest is scratch owned by the host driver.
@@ -115,15 +123,17 @@ struct Inst {
     const double *H, *f_ice, *H_grnd, *f_grnd, *fg_x, *fg_y, *ATT, *zeta, *z_sl, *z_bed;
     // scratch, 3D
     double* visc_alt;
+    double* attp;                  // A^(-1/n) at the quadrature nodes (4 x nz x n2), constant in a solve
+    double* lvis;                  // log of the current viscosity (nz x n2)
     // scratch, 2D
     double *ux_nm1, *uy_nm1, *bm_x, *bm_y, *lk_x, *lk_y, *lr_x, *lr_y, *F2, *F2x, *F2y, *Nab;
     double *tbp_x, *tbp_y, *drag_x, *drag_y;
     // linear system (nu entries each)
-    double *x, *b, *r, *p, *q, *z, *dinv, *rt, *v, *s, *t, *ph, *sh, *dval;
+    double *x, *b, *r, *p, *q, *z, *dinv, *rt, *v, *s, *t, *ph, *sh, *dval, *m2;
     int *ukind, *emap, *mem, *rpart;
     // mixed precision scratch (nu entries; coefficient copies n2)
     float *fN, *fNab, *fdrag_x, *fdrag_y, *fdinv;
-    float *fx, *fr, *fp, *fq, *fz, *frt, *fv, *fs, *ft, *fph, *fsh;
+    float *fx, *fr, *fp, *fq, *fz, *frt, *fv, *fs, *ft, *fph, *fsh, *fm2;
     InstOut* out;
     int visc_final_in_alt;         // set by the kernel: final visc is in visc_alt
 };
@@ -148,6 +158,8 @@ struct Team {
     int parity;                    // reduction slot buffer in use
     TeamCtl* ctl;
     int* abort_all;                // whole-launch abort flag (timeout anywhere)
+    double sync_ns;                // time CTA 0 / thread 0 spent in team all-reduces
+    unsigned gen;                  // thread 0: generation of the team barrier (mirrors ctl->gen)
 };
 
 YG_DEV unsigned ld_acquire_u32(const unsigned int* p) {
@@ -161,41 +173,49 @@ YG_DEV int ld_acquire_s32(const int* p) {
     return v;
 }
 
-// Spin budget of one barrier wait: ~2^22 polls of >= 256 ns (about a second
-// or more). A wait that runs out sets the abort flags; every later wait of the
+// Spin budget of one barrier wait: 2^22 acquire polls of the L2 (about a
+// second or more). A wait that runs out sets the abort flags; every later wait of the
 // launch returns at once, and the kernel reports YGPU_ERR_TIMEOUT.
 #define YG_SPIN_LIMIT (1u << 22)
 
-// Returns false if the launch is aborting.
+YG_DEV unsigned atom_add_acqrel_u32(unsigned int* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+
+// Returns false if the launch is aborting. Arrival: fence + acq_rel atomic on
+// the team counter; the last CTA resets it and bumps the generation; the
+// others poll the generation with acquire loads (no sleep: one thread per CTA).
 YG_DEV bool team_barrier(Team& T) {
     __syncthreads();
     __shared__ int s_ok;
     if (threadIdx.x == 0) {
         int ok = 1;
         if (T.ncta > 1) {
-            unsigned gen = ld_acquire_u32(&T.ctl->gen);
+            const unsigned gen = T.gen;
             __threadfence();
-            unsigned arrived = atomicAdd(&T.ctl->count, 1u);
+            unsigned arrived = atom_add_acqrel_u32(&T.ctl->count, 1u);
             if (arrived == (unsigned)T.ncta - 1u) {
                 T.ctl->count = 0u;
-                __threadfence();
-                atomicAdd(&T.ctl->gen, 1u);
+                atom_add_acqrel_u32(&T.ctl->gen, 1u);
             } else {
                 unsigned n = 0;
                 while (ld_acquire_u32(&T.ctl->gen) == gen) {
-                    if (ld_acquire_s32(T.abort_all)) { ok = 0; break; }
-                    if (++n > YG_SPIN_LIMIT) {
-                        atomicExch(T.abort_all, 1);
-                        atomicExch(&T.ctl->abort, 1);
-                        ok = 0;
-                        break;
+                    if ((++n & 1023u) == 0u) {
+                        if (ld_acquire_s32(T.abort_all)) { ok = 0; break; }
+                        if (n > YG_SPIN_LIMIT) {
+                            atomicExch(T.abort_all, 1);
+                            atomicExch(&T.ctl->abort, 1);
+                            ok = 0;
+                            break;
+                        }
                     }
-                    __nanosleep(256);
                 }
             }
-            __threadfence();
+            T.gen = gen + 1u;
         }
-        if (ld_acquire_s32(T.abort_all)) ok = 0;
+        if (ok && ld_acquire_s32(T.abort_all)) ok = 0;
         s_ok = ok;
     }
     __syncthreads();
@@ -211,7 +231,14 @@ YG_DEV double warp_sum(double v) {
 // All-reduce (sum) of nv <= YG_RED_MAX values over the team, deterministic
 // for a fixed launch shape. Every thread passes its partials; every thread
 // gets the totals. Also acts as a team barrier.
+YG_DEV bool team_allreduce_impl(Team& T, double* vals, int nv);
 YG_DEV bool team_allreduce(Team& T, double* vals, int nv) {
+    unsigned long long t0 = global_ns();
+    bool ok = team_allreduce_impl(T, vals, nv);
+    T.sync_ns += (double)(global_ns() - t0);
+    return ok;
+}
+YG_DEV bool team_allreduce_impl(Team& T, double* vals, int nv) {
     __shared__ double s_red[32][YG_RED_MAX];
     __shared__ double s_tot[YG_RED_MAX];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;

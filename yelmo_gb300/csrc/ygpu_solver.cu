@@ -337,17 +337,68 @@ YG_DEV double beta_aa(const Inst& I, const ygpu_dyn_par& P, const Geo& G, int i,
 }
 
 // ---------------------------------------------------------------------------
-// Phase: column pass -- viscosity, relaxation, depth integrals, beta (aa)
+// Phase: A^(-1/n) at the quadrature nodes (once per solve; ATT is constant)
 // ---------------------------------------------------------------------------
-__device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, const double* vcur,
-                         double* vnew, const double* sdudx, const double* sdudy, const double* sdvdx,
-                         const double* sdvdy, bool relax, bool diva, bool first_copy, bool visc_only = false) {
+__device__ __noinline__ void phase_att_powers(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T) {
     const int nz = G.nz, n2 = G.n2;
-    const double p1 = (1.0 - I.n_glen) / (2.0 * I.n_glen);
     const double p2 = -1.0 / I.n_glen;
     const bool glen3 = (I.n_glen == 3.0);
-    const double eps0sq = P.eps_0 * P.eps_0;
-    const double rel = P.ssa_iter_rel;
+    for (int c = T.tid; c < n2; c += T.nthr) {
+        Nb n = make_nb(G, c);
+        for (int k = 0; k < nz; k++) {
+            if (P.visc_method == 1) {
+                double attn[4];
+                auto att = [&](int a, int b) { return I.ATT[(size_t)k * n2 + CI(a, b)]; };
+                nodes_aa(G, n, att, [](int, int) { return true; }, false, attn);
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    I.attp[((size_t)q * nz + k) * n2 + c] = glen3 ? rcbrt(attn[q]) : pow(attn[q], p2);
+            } else {
+                const double a = I.ATT[(size_t)k * n2 + c];
+                I.attp[(size_t)k * n2 + c] = glen3 ? rcbrt(a) : pow(a, p2);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Phase: vertical shear of the iterate on the faces (DIVA), from the basal
+// stress and the viscosity at the start of the iteration
+// (calc_vertical_shear_3D, velocity_diva.f90:510-571)
+// ---------------------------------------------------------------------------
+__device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, const double* vcur) {
+    const int nz = G.nz, n2 = G.n2;
+    const double* f = I.f_ice;
+    for (int c = T.tid; c < n2; c += T.nthr) {
+        Nb n = make_nb(G, c);
+        const int cx = CI(n.ip1, n.j), cy = CI(n.i, n.jp1);
+        const double tx = I.taub_x[c], ty = I.taub_y[c];
+        const double fc = f[c], fx = f[cx], fy = f[cy];
+        for (int k = 0; k < nz; k++) {
+            const size_t o = (size_t)k * n2;
+            const double omz = 1.0 - I.zeta[k];
+            double va = stag_margin(vcur[o + c], vcur[o + cx], fc, fx);
+            I.duxdz[o + c] = (va != 0.0) ? (tx / va) * omz : 0.0;
+            va = stag_margin(vcur[o + c], vcur[o + cy], fc, fy);
+            I.duydz[o + c] = (va != 0.0) ? (ty / va) * omz : 0.0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Phase: column pass -- viscosity, relaxation, depth integrals, beta (aa)
+// R is the arithmetic of the viscosity (double: FP64 solve; float: mixed)
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T,
+                                          const double* vcur, double* vnew, const double* sdudx,
+                                          const double* sdudy, const double* sdvdx, const double* sdvdy, bool relax,
+                                          bool diva, bool first_copy, bool have_log, bool visc_only = false) {
+    const int nz = G.nz, n2 = G.n2;
+    const R p1 = (R)((1.0 - I.n_glen) / (2.0 * I.n_glen));
+    const bool glen3 = (I.n_glen == 3.0);
+    const R eps0sq = (R)(P.eps_0 * P.eps_0);
+    const R rel = (R)P.ssa_iter_rel;
     const double* zeta = I.zeta;
     const double* f = I.f_ice;
     const int vm = P.visc_method;
@@ -364,18 +415,23 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
         const bool ice = (f[c] == 1.0);
         const double Hc = I.H[c];
         // quadrature-node horizontal strain rates (independent of k)
-        double dudxn[4], dudyn[4], dvdxn[4], dvdyn[4];
+        R dudxn[4], dudyn[4], dvdxn[4], dvdyn[4];
         bool ax[6], ay[6];
-        double e_aa = 0.0;
+        R e_aa = R(0);
         if (ice && vm == 1) {
             ax[0] = act_x(G, f, n.im1, n.jm1); ax[1] = act_x(G, f, n.im1, n.j); ax[2] = act_x(G, f, n.im1, n.jp1);
             ax[3] = act_x(G, f, n.i, n.jm1); ax[4] = act_x(G, f, n.i, n.j); ax[5] = act_x(G, f, n.i, n.jp1);
             ay[0] = act_y(G, f, n.im1, n.jm1); ay[1] = act_y(G, f, n.i, n.jm1); ay[2] = act_y(G, f, n.ip1, n.jm1);
             ay[3] = act_y(G, f, n.im1, n.j); ay[4] = act_y(G, f, n.i, n.j); ay[5] = act_y(G, f, n.ip1, n.j);
-            nodes_acx(G, n, [&](int a, int b) { return sdudx[CI(a, b)]; }, ax, dudxn);
-            nodes_acx(G, n, [&](int a, int b) { return sdudy[CI(a, b)]; }, ax, dudyn);
-            nodes_acy(G, n, [&](int a, int b) { return sdvdx[CI(a, b)]; }, ay, dvdxn);
-            nodes_acy(G, n, [&](int a, int b) { return sdvdy[CI(a, b)]; }, ay, dvdyn);
+            double t4[4];
+            nodes_acx(G, n, [&](int a, int b) { return sdudx[CI(a, b)]; }, ax, t4);
+            for (int q = 0; q < 4; q++) dudxn[q] = (R)t4[q];
+            nodes_acx(G, n, [&](int a, int b) { return sdudy[CI(a, b)]; }, ax, t4);
+            for (int q = 0; q < 4; q++) dudyn[q] = (R)t4[q];
+            nodes_acy(G, n, [&](int a, int b) { return sdvdx[CI(a, b)]; }, ay, t4);
+            for (int q = 0; q < 4; q++) dvdxn[q] = (R)t4[q];
+            nodes_acy(G, n, [&](int a, int b) { return sdvdy[CI(a, b)]; }, ay, t4);
+            for (int q = 0; q < 4; q++) dvdyn[q] = (R)t4[q];
         } else if (ice && vm == 2) {
             const double* ux = I.u_x;
             const double* uy = I.u_y;
@@ -389,85 +445,80 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
             double dvdx2 = (uy[CI(n.ip1, n.jm1)] - uy[CI(n.im1, n.jm1)]) / (2.0 * G.dx);
             double dvdx = 0.5 * (dvdx1 + dvdx2);
             double sh = dudy + dvdx;
-            e_aa = dudx * dudx + dvdy * dvdy;
-            e_aa = e_aa + dudx * dvdy;
-            e_aa = e_aa + 0.25 * (sh * sh);
+            double e = dudx * dudx + dvdy * dvdy;
+            e = e + dudx * dvdy;
+            e = e + 0.25 * (sh * sh);
+            e_aa = (R)e;
         }
         double vint = 0.0, f2 = 0.0, vprev = 0.0, gprev = 0.0;
         for (int k = 0; k < nz; k++) {
             const size_t ck = (size_t)k * n2 + c;
-            double v;
+            R v;
             if (vm == 0) {
-                v = P.visc_const;
+                v = (R)P.visc_const;
             } else if (!ice) {
-                v = VISC_MIN;
-            } else {
-                const double omz = 1.0 - zeta[k];
-                // vertical shear of the iterate (calc_vertical_shear_3D, velocity_diva.f90:510-571)
-                auto shx = [&](int a, int b) {
-                    int am1, ap1, bm1, bp1;
-                    nbr_bc(a, b, G.nx, G.ny, G.bc, am1, ap1, bm1, bp1);
-                    double va = stag_margin(vcur[(size_t)k * n2 + CI(a, b)], vcur[(size_t)k * n2 + CI(ap1, b)],
-                                            f[CI(a, b)], f[CI(ap1, b)]);
-                    return (va != 0.0) ? (I.taub_x[CI(a, b)] / va) * omz : 0.0;
-                };
-                auto shy = [&](int a, int b) {
-                    int am1, ap1, bm1, bp1;
-                    nbr_bc(a, b, G.nx, G.ny, G.bc, am1, ap1, bm1, bp1);
-                    double va = stag_margin(vcur[(size_t)k * n2 + CI(a, b)], vcur[(size_t)k * n2 + CI(a, bp1)],
-                                            f[CI(a, b)], f[CI(a, bp1)]);
-                    return (va != 0.0) ? (I.taub_y[CI(a, b)] / va) * omz : 0.0;
-                };
-                if (vm == 1) {
-                    double dudzn[4], dvdzn[4], attn[4], vn[4];
-                    if (diva) {
-                        nodes_acx(G, n, shx, ax, dudzn);
-                        nodes_acy(G, n, shy, ay, dvdzn);
-                    }
-                    auto att = [&](int a, int b) { return I.ATT[(size_t)k * n2 + CI(a, b)]; };
-                    nodes_aa(G, n, att, [](int, int) { return true; }, false, attn);
+                v = (R)VISC_MIN;
+            } else if (vm == 1) {
+                R dudzn[4], dvdzn[4], vn[4];
+                if (diva) {
+                    double t4[4];
+                    const double* dz = I.duxdz + (size_t)k * n2;
+                    nodes_acx(G, n, [&](int a, int b) { return dz[CI(a, b)]; }, ax, t4);
+                    for (int q = 0; q < 4; q++) dudzn[q] = (R)t4[q];
+                    const double* dzy = I.duydz + (size_t)k * n2;
+                    nodes_acy(G, n, [&](int a, int b) { return dzy[CI(a, b)]; }, ay, t4);
+                    for (int q = 0; q < 4; q++) dvdzn[q] = (R)t4[q];
+                }
 #pragma unroll
-                    for (int q = 0; q < 4; q++) {
-                        double sh = dudyn[q] + dvdxn[q];
-                        double e = dudxn[q] * dudxn[q] + dvdyn[q] * dvdyn[q];
-                        e = e + dudxn[q] * dvdyn[q];
-                        e = e + 0.25 * (sh * sh);
-                        if (diva) {
-                            e = e + 0.25 * (dudzn[q] * dudzn[q]);
-                            e = e + 0.25 * (dvdzn[q] * dvdzn[q]);
-                        }
-                        e = e + eps0sq;
-                        double ep = glen3 ? rcbrt(e) : pow(e, p1);
-                        double ap = glen3 ? rcbrt(attn[q]) : pow(attn[q], p2);
-                        vn[q] = 0.5 * ep * ap;
-                    }
-                    v = gq_mean(vn);
-                } else {
-                    double e = e_aa;
+                for (int q = 0; q < 4; q++) {
+                    R sh = dudyn[q] + dvdxn[q];
+                    R e = dudxn[q] * dudxn[q] + dvdyn[q] * dvdyn[q];
+                    e = e + dudxn[q] * dvdyn[q];
+                    e = e + R(0.25) * (sh * sh);
                     if (diva) {
-                        double dzx = 0.5 * (shx(n.i, n.j) + shx(n.im1, n.j));
-                        double dzy = 0.5 * (shy(n.i, n.j) + shy(n.i, n.jm1));
-                        e = e + 0.25 * (dzx * dzx);
-                        e = e + 0.25 * (dzy * dzy);
+                        e = e + R(0.25) * (dudzn[q] * dudzn[q]);
+                        e = e + R(0.25) * (dvdzn[q] * dvdzn[q]);
                     }
                     e = e + eps0sq;
-                    double a = I.ATT[ck];
-                    double ep = glen3 ? rcbrt(e) : pow(e, p1);
-                    double ap = glen3 ? rcbrt(a) : pow(a, p2);
-                    v = 0.5 * ep * ap;
+                    R ep = glen3 ? rcbrt(e) : pow(e, p1);
+                    vn[q] = R(0.5) * ep * (R)I.attp[((size_t)q * nz + k) * n2 + c];
                 }
+                v = (((vn[0] + vn[1]) + vn[2]) + vn[3]) / R(4);
+            } else {
+                R e = e_aa;
+                if (diva) {
+                    const double* dz = I.duxdz + (size_t)k * n2;
+                    const double* dzy = I.duydz + (size_t)k * n2;
+                    R dzx = (R)(0.5 * (dz[c] + dz[CI(n.im1, n.j)]));
+                    R dzyv = (R)(0.5 * (dzy[c] + dzy[CI(n.i, n.jm1)]));
+                    e = e + R(0.25) * (dzx * dzx);
+                    e = e + R(0.25) * (dzyv * dzyv);
+                }
+                e = e + eps0sq;
+                R ep = glen3 ? rcbrt(e) : pow(e, p1);
+                v = R(0.5) * ep * (R)I.attp[ck];
             }
-            if (relax) v = exp((1.0 - rel) * log(vcur[ck]) + rel * log(v));
-            vnew[ck] = v;
+            double vd;
+            if (relax) {
+                // picard_relax_visc in log space; log of the current viscosity carried between iterations
+                const R lc = have_log ? (R)I.lvis[ck] : (R)log(vcur[ck]);
+                const R L = (R(1) - rel) * lc + rel * log(v);
+                vd = (double)exp(L);
+                I.lvis[ck] = (double)L;
+            } else {
+                vd = (double)v;
+                if (!visc_only) I.lvis[ck] = log(vd);
+            }
+            vnew[ck] = vd;
             // trapezoid integrals (integrate_trapezoid1D_pt, yelmo_tools.f90:1092-1122)
             const double omz = 1.0 - zeta[k];
-            const double g = (Hc / v) * (omz * omz);
+            const double g = (Hc / vd) * (omz * omz);
             if (k > 0) {
-                const double dz = zeta[k] - zeta[k - 1];
-                vint = vint + 0.5 * (v + vprev) * dz;
-                f2 = f2 + 0.5 * (g + gprev) * dz;
+                const double dzt = zeta[k] - zeta[k - 1];
+                vint = vint + 0.5 * (vd + vprev) * dzt;
+                f2 = f2 + 0.5 * (g + gprev) * dzt;
             }
-            vprev = v;
+            vprev = vd;
             gprev = g;
         }
         if (visc_only) continue;
@@ -743,34 +794,72 @@ YG_DEV T member_elems(const Geo& G, const CT* N, const CT* Nab, int mm, V val) {
     return acc;
 }
 
-// y = K v for the rows [tid.. nu) of the team (identity on Dirichlet/tied rows)
+// Interior fast path: a free row whose 4 elements hold only free, self-mapped
+// unknowns (no Dirichlet, tied or ghost columns) is the 9-point stencil
+// K = -A_residual * dx*dy (the identity the reference's test_ssa_energy pins).
 template <typename T, typename CT>
-__device__ __noinline__ void energy_apply(const Inst& I, const Geo& G, Team& Tm, const CT* N, const CT* Nab, const CT* dgx,
-                         const CT* dgy, const T* v, T* y) {
+YG_DEV T energy_row_fast(const Geo& G, const CT* N, const CT* Nab, const CT* dgx, const CT* dgy, const T* v, int u) {
+    const int nx = G.nx, ny = G.ny, n2 = G.n2;
+    const int pl = (u >= n2) ? 1 : 0;
+    const int c = u - pl * n2;
+    const int i = c % nx, j = c / nx;
+    const int im1 = (i == 0) ? nx - 1 : i - 1, ip1 = (i == nx - 1) ? 0 : i + 1;
+    const int jm1 = (j == 0) ? ny - 1 : j - 1, jp1 = (j == ny - 1) ? 0 : j + 1;
+    const T dyodx = (T)G.dyodx, dxody = (T)G.dxody;
+    const T* U = v;
+    const T* V = v + n2;
+    if (pl == 0) {
+        const T Ni = (T)N[c], Np = (T)N[ip1 + nx * j];
+        const T Bc = (T)Nab[c], Bm = (T)Nab[i + nx * jm1];
+        T y = (T(4) * dyodx * (Np + Ni) + dxody * (Bc + Bm) + (T)dgx[c]) * U[c];
+        y -= T(4) * dyodx * Np * U[ip1 + nx * j];
+        y -= T(4) * dyodx * Ni * U[im1 + nx * j];
+        y -= dxody * Bc * U[i + nx * jp1];
+        y -= dxody * Bm * U[i + nx * jm1];
+        y += (T(2) * Ni + Bc) * V[c];
+        y -= (T(2) * Np + Bc) * V[ip1 + nx * j];
+        y += (T(2) * Np + Bm) * V[ip1 + nx * jm1];
+        y -= (T(2) * Ni + Bm) * V[i + nx * jm1];
+        return y;
+    } else {
+        const T Ni = (T)N[c], Np = (T)N[i + nx * jp1];
+        const T Bc = (T)Nab[c], Bm = (T)Nab[im1 + nx * j];
+        T y = (T(4) * dxody * (Np + Ni) + dyodx * (Bc + Bm) + (T)dgy[c]) * V[c];
+        y -= T(4) * dxody * Np * V[i + nx * jp1];
+        y -= T(4) * dxody * Ni * V[i + nx * jm1];
+        y -= dyodx * Bc * V[ip1 + nx * j];
+        y -= dyodx * Bm * V[im1 + nx * j];
+        y += (T(2) * Ni + Bc) * U[c];
+        y -= (T(2) * Np + Bc) * U[i + nx * jp1];
+        y += (T(2) * Np + Bm) * U[im1 + nx * jp1];
+        y -= (T(2) * Ni + Bm) * U[im1 + nx * j];
+        return y;
+    }
+}
+
+// Row u of K v (identity on Dirichlet and tied rows)
+template <typename T, typename CT>
+YG_DEV T energy_row(const Inst& I, const Geo& G, const CT* N, const CT* Nab, const CT* dgx, const CT* dgy,
+                    const T* v, int u) {
+    if (I.rpart[u] == 1) return energy_row_fast<T, CT>(G, N, Nab, dgx, dgy, v, u);
+    if (I.ukind[u] != DOF_FREE) return v[u];
     const int* emap = I.emap;
     auto val = [&](int d) -> T {
         if (d < 0) return T(0);
         int e = emap[d];
         return (e >= 0) ? v[e] : T(0);
     };
-    for (int u = Tm.tid; u < G.nu; u += Tm.nthr) {
-        if (I.ukind[u] != DOF_FREE) {
-            y[u] = v[u];
-            continue;
-        }
-        const T vr = v[u];
-        T acc = ((u < G.n2) ? (T)dgx[u] : (T)dgy[u - G.n2]) * vr;
-        acc += member_elems<T>(G, N, Nab, u, val);
-        const int* mem = I.mem + 3 * u;
-#pragma unroll
-        for (int m = 0; m < 3; m++) {
-            int mm = mem[m];
-            if (mm < 0) break;
-            acc += ((mm < G.n2) ? (T)dgx[mm] : (T)dgy[mm - G.n2]) * vr;
-            acc += member_elems<T>(G, N, Nab, mm, val);
-        }
-        y[u] = acc;
+    const T vr = v[u];
+    T acc = ((u < G.n2) ? (T)dgx[u] : (T)dgy[u - G.n2]) * vr;
+    acc += member_elems<T>(G, N, Nab, u, val);
+    const int* mem = I.mem + 3 * u;
+    for (int m = 0; m < 3; m++) {
+        int mm = mem[m];
+        if (mm < 0) break;
+        acc += ((mm < G.n2) ? (T)dgx[mm] : (T)dgy[mm - G.n2]) * vr;
+        acc += member_elems<T>(G, N, Nab, mm, val);
     }
+    return acc;
 }
 
 // ---------------------------------------------------------------------------
@@ -860,24 +949,22 @@ YG_DEV T residual_row(const Inst& I, const Geo& G, const CT* N, const CT* Nab, c
 }
 
 template <typename T, typename CT>
-YG_DEV void operator_apply(const Inst& I, const Geo& G, Team& Tm, bool energy, const CT* N, const CT* Nab,
-                           const CT* dgx, const CT* dgy, const T* v, T* y) {
-    if (energy) {
-        energy_apply<T, CT>(I, G, Tm, N, Nab, dgx, dgy, v, y);
-    } else {
-        for (int u = Tm.tid; u < G.nu; u += Tm.nthr) y[u] = residual_row<T, CT>(I, G, N, Nab, dgx, dgy, v, u, nullptr);
-    }
+YG_DEV T operator_row(const Inst& I, const Geo& G, bool energy, const CT* N, const CT* Nab, const CT* dgx,
+                      const CT* dgy, const T* v, int u) {
+    if (energy) return energy_row<T, CT>(I, G, N, Nab, dgx, dgy, v, u);
+    return residual_row<T, CT>(I, G, N, Nab, dgx, dgy, v, u, nullptr);
 }
 
-// Operator functors for the Krylov solvers
+// Operator functors for the Krylov solvers: row(u, v) = (A v)_u
 template <typename T, typename CT>
 struct StencilOp {
     const Inst* I;
     const Geo* G;
     bool energy;
     const CT *N, *Nab, *dgx, *dgy;
+    YG_DEV T row(int u, const T* v) const { return operator_row<T, CT>(*I, *G, energy, N, Nab, dgx, dgy, v, u); }
     YG_DEV void operator()(Team& Tm, const T* v, T* y) const {
-        operator_apply<T, CT>(*I, *G, Tm, energy, N, Nab, dgx, dgy, v, y);
+        for (int u = Tm.tid; u < G->nu; u += Tm.nthr) y[u] = row(u, v);
     }
 };
 
@@ -887,12 +974,13 @@ struct CsrOp {
     const int* ptr;
     const int* idx;
     const double* val;
+    YG_DEV double row(int r, const double* v) const {
+        double s = 0.0;
+        for (int k = ptr[r]; k < ptr[r + 1]; k++) s += val[k] * v[idx[k]];
+        return s;
+    }
     YG_DEV void operator()(Team& Tm, const double* v, double* y) const {
-        for (int r = Tm.tid; r < n; r += Tm.nthr) {
-            double s = 0.0;
-            for (int k = ptr[r]; k < ptr[r + 1]; k++) s += val[k] * v[idx[k]];
-            y[r] = s;
-        }
+        for (int r = Tm.tid; r < n; r += Tm.nthr) y[r] = row(r, v);
     }
 };
 
@@ -1024,6 +1112,42 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
                 int t = pl * n2 + a + nx * b;
                 if (I.ukind[t] == DOF_TIED && I.emap[t] == u && nm < 3) mem[nm++] = t;
             }
+    }
+    if (!team_barrier(T)) return false;
+    // pass 5: interior fast-path flag (rpart = 1): a free row without members
+    // whose four elements exist and hold only free, self-mapped unknowns
+    for (int u = T.tid; u < G.nu; u += T.nthr) {
+        int fast = 0;
+        if (I.ukind[u] == DOF_FREE && I.mem[3 * u] < 0) {
+            const int pl = (u >= n2) ? 1 : 0, c = u - pl * n2, i = c % nx, j = c / nx;
+            fast = 1;
+            for (int e = 0; e < 4 && fast; e++) {
+                int ci, cj, d[4];
+                if (e < 2) {            // cells
+                    ci = (pl == 0) ? i + e : i;
+                    cj = (pl == 0) ? j : j + e;
+                    if (!elem_index(ci, nx, G.per_x) || !elem_index(cj, ny, G.per_y)) { fast = 0; break; }
+                    d[0] = dof_u(G, ci - 1, cj, 0); d[1] = dof_u(G, ci, cj, 0);
+                    d[2] = dof_u(G, ci, cj - 1, 1); d[3] = dof_u(G, ci, cj, 1);
+                } else {                // corners
+                    ci = (pl == 0) ? i : i - (e - 2);
+                    cj = (pl == 0) ? j - (e - 2) : j;
+                    if (!elem_index(ci, nx, G.per_x) || !elem_index(cj, ny, G.per_y)) { fast = 0; break; }
+                    d[0] = dof_u(G, ci, cj, 0); d[1] = dof_u(G, ci, cj + 1, 0);
+                    d[2] = dof_u(G, ci, cj, 1); d[3] = dof_u(G, ci + 1, cj, 1);
+                }
+                // a column may be a free unknown or a Dirichlet unknown of value 0:
+                // Krylov vectors and the iterate are exactly 0 on those rows
+                for (int q = 0; q < 4; q++) {
+                    const int dq = d[q];
+                    if (dq < 0) { fast = 0; break; }
+                    const bool self = (I.emap[dq] == dq);
+                    const bool zero_dir = (I.ukind[dq] == DOF_DIR && I.dval[dq] == 0.0);
+                    if (!self && !zero_dir) { fast = 0; break; }
+                }
+            }
+        }
+        I.rpart[u] = fast;
     }
     return team_barrier(T);
 }
@@ -1163,6 +1287,105 @@ __device__ __noinline__ int krylov_cg(Team& Tm, int nu, const Op& A, const CT* d
     return YGPU_MAXITER;
 }
 
+// Pipelined preconditioned CG (Ghysels and Vanroose 2014): one team
+// all-reduce per iteration. The three dot products of an iteration are reduced
+// together, and the operator apply, preconditioner and eight vector updates of
+// a row are fused into one pass. The operator input m ping-pongs between two
+// buffers because rows read it at their neighbours while it is being renewed.
+// The recursively updated residual is checked against b - A x when it reaches
+// the tolerance; if the true residual is above it, the recursion restarts from
+// the true residual.
+template <typename T, typename Op, typename CT>
+__device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const CT* dinv, T* x, const T* b, T* r,
+                                            T* u, T* w, T* m0, T* m1, T* z, T* q, T* s, T* p, int maxiter,
+                                            double tol, double bnrm, bool precond, int& iters, double& relres,
+                                            bool& ok) {
+    ok = true;
+    iters = 0;
+    auto Mi = [&](int k) -> T { return precond ? (T)dinv[k] : T(1); };
+    int it = 0;
+    for (int restart = 0; restart < 8; restart++) {
+        // r = b - A x, u = M r
+        for (int k = Tm.tid; k < nu; k += Tm.nthr) {
+            T rk = b[k] - A.row(k, x);
+            r[k] = rk;
+            u[k] = Mi(k) * rk;
+        }
+        if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
+        // w = A u; partial dots; m = M w
+        double red[3] = {0.0, 0.0, 0.0};
+        for (int k = Tm.tid; k < nu; k += Tm.nthr) {
+            T wk = A.row(k, u);
+            w[k] = wk;
+            const T mk = Mi(k) * wk;
+            m0[k] = mk;
+            z[k] = T(0); q[k] = T(0); s[k] = T(0); p[k] = T(0);
+            red[0] += (double)r[k] * (double)u[k];
+            red[1] += (double)wk * (double)u[k];
+            red[2] += (double)r[k] * (double)r[k];
+        }
+        if (!(ok = team_allreduce(Tm, red, 3))) return YGPU_ERR_TIMEOUT;
+        relres = sqrt(red[2]) / bnrm;
+        if (relres <= tol) { iters = it; return YGPU_OK; }
+        double gam_old = 1.0, alpha_old = 1.0;
+        T* mc = m0;
+        T* mn = m1;
+        bool first = true;
+        bool recheck = false;
+        while (it < maxiter) {
+            const double gam = red[0], del = red[1];
+            double beta, alpha;
+            if (first) { beta = 0.0; alpha = gam / del; }
+            else {
+                beta = gam / gam_old;
+                alpha = gam / (del - beta * gam / alpha_old);
+            }
+            if (!isfinite(alpha) || !isfinite(beta) || del == 0.0) { iters = it; return YGPU_BREAKDOWN; }
+            first = false;
+            gam_old = gam;
+            alpha_old = alpha;
+            const T a = (T)alpha, bt = (T)beta;
+            red[0] = red[1] = red[2] = 0.0;
+            for (int k = Tm.tid; k < nu; k += Tm.nthr) {
+                const T nk = A.row(k, mc);
+                const T zk = nk + bt * z[k];
+                const T qk = mc[k] + bt * q[k];
+                const T sk = w[k] + bt * s[k];
+                const T pk = u[k] + bt * p[k];
+                z[k] = zk; q[k] = qk; s[k] = sk; p[k] = pk;
+                x[k] = x[k] + a * pk;
+                const T rk = r[k] - a * sk;
+                const T uk = u[k] - a * qk;
+                const T wk = w[k] - a * zk;
+                r[k] = rk; u[k] = uk; w[k] = wk;
+                mn[k] = Mi(k) * wk;
+                red[0] += (double)rk * (double)uk;
+                red[1] += (double)wk * (double)uk;
+                red[2] += (double)rk * (double)rk;
+            }
+            it++;
+            if (!(ok = team_allreduce(Tm, red, 3))) return YGPU_ERR_TIMEOUT;
+            { T* t = mc; mc = mn; mn = t; }
+            relres = sqrt(red[2]) / bnrm;
+            if (!isfinite(relres)) { iters = it; return YGPU_BREAKDOWN; }
+            if (relres <= tol) { recheck = true; break; }
+        }
+        iters = it;
+        if (!recheck) return YGPU_MAXITER;
+        // true residual check
+        double tr = 0.0;
+        for (int k = Tm.tid; k < nu; k += Tm.nthr) {
+            const double rk = (double)b[k] - (double)A.row(k, x);
+            tr += rk * rk;
+        }
+        if (!(ok = team_allreduce(Tm, &tr, 1))) return YGPU_ERR_TIMEOUT;
+        relres = sqrt(tr) / bnrm;
+        if (relres <= tol) return YGPU_OK;
+        if (it >= maxiter) return YGPU_MAXITER;
+    }
+    return YGPU_MAXITER;
+}
+
 // BiCGSTAB with Jacobi (van der Vorst 1992, as in the oracle)
 template <typename T, typename Op, typename CT>
 __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const CT* dinv, T* x, const T* b, T* r, T* rt, T* p, T* v,
@@ -1254,8 +1477,8 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
     const StencilOp<double, double> A64{&I, &G, energy, I.visc_int, I.Nab, I.drag_x, I.drag_y};
     if (P.precision != YGPU_PREC_MIXED) {
         if (use_cg)
-            return krylov_cg<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.p, I.q, I.z, P.lin_maxiter, P.lin_tol, bnrm,
-                                     pre, iters, relres, ok);
+            return krylov_pcg_pipe<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.rt, I.v, I.ph, I.m2, I.z, I.q, I.s,
+                                           I.p, P.lin_maxiter, P.lin_tol, bnrm, pre, iters, relres, ok);
         return krylov_bicgstab<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.rt, I.p, I.v, I.s, I.t, I.ph, I.sh,
                                        P.lin_maxiter, P.lin_tol, bnrm, pre, iters, relres, ok);
     }
@@ -1298,8 +1521,8 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         double rel_in = 0.0;
         int st;
         if (use_cg)
-            st = krylov_cg<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.fz, I.fp, I.fq, I.fs, inner_max, inner_tol, 1.0,
-                                  pre, it, rel_in, ok);
+            st = krylov_pcg_pipe<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.frt, I.fv, I.ft, I.fph, I.fm2, I.fz,
+                                        I.fq, I.fs, I.fp, inner_max, inner_tol, 1.0, pre, it, rel_in, ok);
         else
             st = krylov_bicgstab<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.fz, I.frt, I.fp, I.fv, I.fs, I.ft, I.fph,
                                         I.fsh, inner_max, inner_tol, 1.0, pre, it, rel_in, ok);
@@ -1427,11 +1650,6 @@ __device__ __noinline__ void phase_diva_final(const Inst& I, const Geo& G, Team&
         for (int k = 0; k < nz; k++) {
             const size_t o = (size_t)k * n2;
             const double omz = 1.0 - zeta[k];
-            // shear at the start of the last iteration
-            double va = stag_margin(vlast_cur[o + c], vlast_cur[o + cx], f[c], f[cx]);
-            I.duxdz[o + c] = (va != 0.0) ? (I.tbp_x[c] / va) * omz : 0.0;
-            va = stag_margin(vlast_cur[o + c], vlast_cur[o + cy], f[c], f[cy]);
-            I.duydz[o + c] = (va != 0.0) ? (I.tbp_y[c] / va) * omz : 0.0;
             // F1 up to level k at this cell and its +x / +y neighbours
             double g0 = ic ? (I.H[c] / vfinal[o + c]) * omz : 0.0;
             double g1 = ix ? (I.H[cx] / vfinal[o + cx]) * omz : 0.0;
@@ -1472,6 +1690,14 @@ __device__ __noinline__ void solve_instance(const Inst& I, const ygpu_dyn_par& P
     double* sdudy = I.lk_y;
     double* sdvdx = I.lr_x;
     double* sdvdy = I.lr_y;
+    double tph[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double sync_before_krylov = 0.0;
+    unsigned long long t_last = global_ns();
+    auto tick = [&](int k) {
+        unsigned long long t = global_ns();
+        tph[k] += (double)(t - t_last);
+        t_last = t;
+    };
     // ---- setup ----
     for (int c = T.tid; c < G.n2; c += T.nthr) {
         I.err_x[c] = 1.0;
@@ -1488,6 +1714,9 @@ __device__ __noinline__ void solve_instance(const Inst& I, const ygpu_dyn_par& P
     }
     if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
     if (!phase_classify(I, P, G, T)) { status = ld_acquire_s32(T.abort_all) ? YGPU_ERR_TIMEOUT : YGPU_ERR_BAD_ARG; goto finish; }
+    if (P.visc_method != 0) phase_att_powers(I, P, G, T);
+    if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+    tick(0);
 
     {
         double* vcur = I.visc;
@@ -1496,19 +1725,28 @@ __device__ __noinline__ void solve_instance(const Inst& I, const ygpu_dyn_par& P
         double* last_cur = vcur;
         for (int iter = 1; iter <= P.ssa_iter_max; iter++) {
             const bool relax = diva ? true : (P.visc_method != 0);
-            if (P.visc_method == 1) {
-                phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
+            if (P.visc_method == 1 || diva) {
+                if (P.visc_method == 1) phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
+                if (diva) phase_shear(I, G, T, vcur);
                 if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
             }
-            phase_column(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true);
+            tick(1);
+            if (P.precision == YGPU_PREC_MIXED)
+                phase_column<float>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
+            else
+                phase_column<double>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
             if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            tick(2);
             last_cur = vcur;
             { double* tmp = vcur; vcur = vnew; vnew = tmp; in_alt ^= 1; }
             phase_faces(I, P, G, T, diva);
             if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            tick(3);
             double bn2 = 0.0;
             phase_system(I, P, G, T, bn2);
             if (!team_allreduce(T, &bn2, 1)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            tick(4);
+            sync_before_krylov = T.sync_ns;
             int it = 0, outer = 0;
             double rr = 0.0;
             int st;
@@ -1521,6 +1759,8 @@ __device__ __noinline__ void solve_instance(const Inst& I, const ygpu_dyn_par& P
                 if (!ok) { status = YGPU_ERR_TIMEOUT; goto finish; }
             }
             if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            tick(5);
+            tph[9] += T.sync_ns - sync_before_krylov;
             lin_iter += it;
             outer_total += outer;
             if (st != YGPU_OK) lin_fail++;
@@ -1529,6 +1769,7 @@ __device__ __noinline__ void solve_instance(const Inst& I, const ygpu_dyn_par& P
             double red[4];
             phase_epilogue(I, P, G, T, diva, red);
             if (!team_allreduce(T, red, 4)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            tick(6);
             resid = (red[2] > 0.0) ? sqrt(red[0]) / (sqrt(red[1]) + 1e-10) : 0.0;
             iter_now = iter;
             if (P.ssa_write_log && lead)
@@ -1556,7 +1797,9 @@ __device__ __noinline__ void solve_instance(const Inst& I, const ygpu_dyn_par& P
             if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
             ygpu_dyn_par P1 = P;
             P1.visc_method = 1;
-            phase_column(I, P1, G, T, vcur, vcur, sdudx, sdudy, sdvdx, sdvdy, false, false, false, true);
+            phase_att_powers(I, P1, G, T);
+            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
+            phase_column<double>(I, P1, G, T, vcur, vcur, sdudx, sdudy, sdvdx, sdvdy, false, false, false, false, true);
             if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
         }
         // the caller's visc_eff must hold the final viscosity
@@ -1566,7 +1809,10 @@ __device__ __noinline__ void solve_instance(const Inst& I, const ygpu_dyn_par& P
         if (lead) out->lim_n = (int)nlim;
     }
 finish:
+    tick(7);
     if (lead) {
+        tph[8] = T.sync_ns;
+        for (int k = 0; k < 10; k++) out->phase_ns[k] = tph[k];
         out->iter_now = iter_now;
         out->lin_iter = lin_iter;
         out->lin_fail = lin_fail;
@@ -1582,7 +1828,7 @@ finish:
 // ---------------------------------------------------------------------------
 // The persistent kernel: teams take instances from the queue
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(YG_BLOCK, 2) ygpu_solve_kernel(const Inst* __restrict__ insts, int n_inst,
+__global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_solve_kernel(const Inst* __restrict__ insts, int n_inst,
                                                               ygpu_dyn_par P, TeamCtl* ctls, int team_ctas,
                                                               int* queue, int* abort_all) {
     __shared__ Inst sI;
@@ -1595,6 +1841,8 @@ __global__ void __launch_bounds__(YG_BLOCK, 2) ygpu_solve_kernel(const Inst* __r
     T.ctl = ctls + blockIdx.x / team_ctas;
     T.parity = 0;
     T.abort_all = abort_all;
+    T.sync_ns = 0.0;
+    T.gen = 0u;
     for (;;) {
         if (T.cta == 0 && threadIdx.x == 0) {
             int k = atomicAdd(queue, 1);
@@ -1608,6 +1856,7 @@ __global__ void __launch_bounds__(YG_BLOCK, 2) ygpu_solve_kernel(const Inst* __r
         if (k >= n_inst) return;
         if (threadIdx.x == 0) sI = insts[k];
         __syncthreads();
+        T.sync_ns = 0.0;
         solve_instance(sI, P, T);
         if (!team_barrier(T)) return;
     }
@@ -1636,6 +1885,8 @@ __global__ void __launch_bounds__(YG_BLOCK) ygpu_csr_kernel(CsrJob J, TeamCtl* c
     T.ctl = ctl;
     T.parity = 0;
     T.abort_all = abort_all;
+    T.sync_ns = 0.0;
+    T.gen = 0u;
     const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
     // Jacobi diagonal and ||b||
     double bn = 0.0;

@@ -208,3 +208,47 @@ class DeviceSolver:
         r = self.L.ygpu_solve_batch_device(self.ctx, kind, C.byref(cpar), n, arr, sts)
         _check(r)
         return [s.as_dict() for s in sts]
+
+
+def host_io_bytes(kind: int, nx: int, ny: int, nz: int):
+    """Bytes the host-pointer drop-in copies in and out (ygpu_calc_velocity_* staging)."""
+    b2, b3, i2, bz = 8 * nx * ny, 8 * nx * ny * nz, 4 * nx * ny, 8 * nz
+    inputs_common = 13 * b2 + b3 + bz + 2 * i2       # c_bed..z_srf (13 2D), ATT, zeta, masks
+    if kind == abi.KIND_SSA:
+        h2d = 7 * b2 + b3 + inputs_common             # ux_b, uy_b, taub x2, beta x3, visc
+        d2h = 10 * b2 + b3                            # ux_b, uy_b, taub x2, visc_int, err x2, beta x3, visc
+    else:
+        h2d = 9 * b2 + b3 + inputs_common             # ux_bar, uy_bar, ux_b, uy_b, taub x2, beta x3, visc
+        d2h = 13 * b2 + 7 * b3                        # 2D: ux_bar..uy_b(4), taub(2), beta(3), beta_eff, visc_int, err(2)
+    return h2d, d2h
+
+
+def algorithmic_bytes(stats: dict, kind: int, nx: int, ny: int, nz: int, mixed: bool, energy: bool = True,
+                      cg: bool = True) -> float:
+    """Algorithmic HBM bytes of one solve: each distinct array read once and
+    written once per phase, with the per-cell counts of the hot-path scope
+    (column pass (3nz+14)w DIVA / (3nz+10)w SSA, matrix-free operator 8w+2,
+    Krylov vector passes) times the phase counts the solve reports."""
+    n2 = nx * ny
+    w = 8
+    picard = stats["ssa_iter_now"]
+    lin = stats["ssa_lin_iter"]
+    col = (3 * nz + (14 if kind == abi.KIND_DIVA else 10)) * w
+    strain = 7 * w
+    faces = 20 * w + 8
+    system = 16 * w + 8
+    epilogue = 16 * w + 8
+    per_picard = strain + col + faces + system + epilogue
+    if not mixed:
+        op = 8 * w + 2
+        vec = (28 if cg else 44) * w               # CG: 14 distinct 2-component array passes; BiCGSTAB: 22
+        krylov = lin * ((1 if cg else 2) * op + vec)
+    else:
+        wf = 4
+        op = 8 * wf + 2
+        vec = (28 if cg else 44) * wf
+        krylov = lin * ((1 if cg else 2) * op + vec)
+        outer = stats.get("outer_iter", 0)
+        krylov += outer * ((8 * w + 2) + 6 * w + 8 * wf)   # FP64 residual + conversions
+        krylov += picard * (4 * wf + 2 * 2 * wf + 2 * 2 * w)  # FP32 coefficient copies
+    return float(n2) * (picard * per_picard + krylov)
