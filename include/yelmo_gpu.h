@@ -288,6 +288,26 @@ int ygpu_solve_device(ygpu_ctx* ctx, int kind, const ygpu_dyn_par* par,
 int ygpu_solve_batch_device(ygpu_ctx* ctx, int kind, const ygpu_dyn_par* par,
                             int n_inst, const ygpu_fields* inst, ygpu_stats* stats);
 
+/*
+ * ygpu_solve_device_noalloc -- no counterpart in the reference.
+ * One solve on device-resident fields, like ygpu_solve_device, for callers that
+ * cannot allocate device memory: a host capturing its work into a CUDA graph,
+ * a host whose device memory belongs to another runtime or pool, a server that
+ * must not grow after start-up. The call allocates nothing: its scratch is a
+ * fixed array of YGPU_NOALLOC_SCRATCH_BYTES inside the library, held by every
+ * GPU that loads the library until the process exits. Instances whose scratch
+ * does not fit are rejected with YGPU_ERR_BAD_ARG (a 161x161x10 FP64 solve needs
+ * about 24 MB). The first call on a device looks up the array's device address;
+ * make that first call before any stream capture. All calls share the array and
+ * it keeps the last call's contents: calls that overlap on the GPU race, so
+ * serialise them. stream is a cudaStream_t (NULL: the legacy default stream);
+ * the call returns after that stream has finished the solve. stats->device_ms
+ * is 0 (no events are created).
+ */
+#define YGPU_NOALLOC_SCRATCH_BYTES (64u << 20)
+int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, const ygpu_fields* f,
+                              ygpu_stats* stats, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

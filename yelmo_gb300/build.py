@@ -22,6 +22,7 @@ UNITS = {
     "ygpu_solver.cu": [],
     "ygpu_api.cu": [],
     "ygpu_inputs.cu": ["-fmad=false"],
+    "ygpu_noalloc.cu": [],
 }
 
 

@@ -131,7 +131,7 @@ extern "C" int ygpu_boundary_code(const char* b) {
     return -1;
 }
 
-static int check_par(const ygpu_dyn_par* p) {
+int ygpu_check_par(const ygpu_dyn_par* p) {
     if (!p) { ygpu_set_error("par is NULL"); return YGPU_ERR_BAD_ARG; }
     if (p->boundaries < 0 || p->boundaries > 6) { ygpu_set_error("bad boundary code %d", p->boundaries); return YGPU_ERR_BAD_ARG; }
     if (p->visc_method < 0 || p->visc_method > 2) { ygpu_set_error("visc_method not recognized: %d", p->visc_method); return YGPU_ERR_BAD_ARG; }
@@ -241,9 +241,10 @@ static ygpu_ctx* default_ctx() {
 // ---------------------------------------------------------------------------
 // scratch layout of one instance
 // ---------------------------------------------------------------------------
-static size_t al(size_t b) { return (b + 255) & ~(size_t)255; }
+size_t ygpu_align256(size_t b) { return (b + 255) & ~(size_t)255; }
+static size_t al(size_t b) { return ygpu_align256(b); }
 
-static size_t inst_scratch_bytes(int nx, int ny, int nz, bool mixed) {
+size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed) {
     size_t n2 = (size_t)nx * ny, nu = 2 * n2, n3 = n2 * nz;
     size_t b = al(n3 * 8);               // visc_alt
     b += al(4 * n3 * 8) + al(n3 * 8);    // attp, lvis
@@ -254,7 +255,7 @@ static size_t inst_scratch_bytes(int nx, int ny, int nz, bool mixed) {
     return b;
 }
 
-static void inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed) {
+void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed) {
     size_t n2 = (size_t)nx * ny, nu = 2 * n2, n3 = n2 * nz;
     char* p = base;
     auto D = [&](size_t n) { double* r = (double*)p; p += al(n * 8); return r; };
@@ -282,7 +283,7 @@ static void inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool
     }
 }
 
-static int fields_check(int kind, const ygpu_fields* f) {
+int ygpu_fields_check(int kind, const ygpu_fields* f) {
     if (!f) { ygpu_set_error("fields is NULL"); return YGPU_ERR_BAD_ARG; }
     if (f->nx < 3 || f->ny < 3 || f->nz < 2) {
         ygpu_set_error("grid too small: nx=%d ny=%d nz=%d (need nx,ny >= 3, nz >= 2)", f->nx, f->ny, f->nz);
@@ -305,7 +306,7 @@ static int fields_check(int kind, const ygpu_fields* f) {
     return YGPU_OK;
 }
 
-static void fill_inst(Inst& I, int kind, const ygpu_fields* f) {
+void ygpu_fill_inst(Inst& I, int kind, const ygpu_fields* f) {
     memset(&I, 0, sizeof(I));
     I.nx = f->nx; I.ny = f->ny; I.nz = f->nz; I.n2 = f->nx * f->ny; I.nu = 2 * I.n2;
     I.kind = kind;
@@ -330,6 +331,16 @@ static void fill_inst(Inst& I, int kind, const ygpu_fields* f) {
     I.z_sl = f->z_sl; I.z_bed = f->z_bed;
 }
 
+int ygpu_single_team_ctas(int max_ctas, size_t nu) {
+    int want = (int)((nu + 2 * YG_BLOCK - 1) / (2 * YG_BLOCK));
+    const char* v = getenv("YGPU_TEAM_CTAS");
+    int tc = (v && *v) ? atoi(v) : want;
+    if (tc < 1) tc = 1;
+    if (tc > max_ctas) tc = max_ctas;
+    if (tc > YG_MAX_TEAM_CTAS) tc = YG_MAX_TEAM_CTAS;
+    return tc;
+}
+
 static int env_int(const char* name, int dflt) {
     const char* v = getenv(name);
     return (v && *v) ? atoi(v) : dflt;
@@ -340,12 +351,7 @@ static void choose_teams(const ygpu_ctx* c, int n_inst, size_t max_nu, int* n_te
     int maxc = c->max_ctas > 0 ? c->max_ctas : 1;
     if (n_inst == 1) {
         // one team over the GPU, sized to the instance
-        int want = (int)((max_nu + 2 * YG_BLOCK - 1) / (2 * YG_BLOCK));
-        int tc = env_int("YGPU_TEAM_CTAS", want);
-        if (tc < 1) tc = 1;
-        if (tc > maxc) tc = maxc;
-        if (tc > YG_MAX_TEAM_CTAS) tc = YG_MAX_TEAM_CTAS;
-        *team_ctas = tc;
+        *team_ctas = ygpu_single_team_ctas(maxc, max_nu);
         *n_teams = 1;
         return;
     }
@@ -361,19 +367,19 @@ static void choose_teams(const ygpu_ctx* c, int n_inst, size_t max_nu, int* n_te
 
 static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, const ygpu_fields* inst,
                        ygpu_stats* stats) {
-    int st = check_par(par);
+    int st = ygpu_check_par(par);
     if (st) return st;
     if (kind != YGPU_KIND_SSA && kind != YGPU_KIND_DIVA) { ygpu_set_error("bad solver kind %d", kind); return YGPU_ERR_BAD_ARG; }
     if (n < 1) { ygpu_set_error("no instances"); return YGPU_ERR_BAD_ARG; }
     for (int k = 0; k < n; k++)
-        if ((st = fields_check(kind, &inst[k]))) return st;
+        if ((st = ygpu_fields_check(kind, &inst[k]))) return st;
     CK(cudaSetDevice(c->device));
     const bool mixed = (par->precision == YGPU_PREC_MIXED);
     std::vector<size_t> off(n);
     size_t total = 0, max_nu = 0;
     for (int k = 0; k < n; k++) {
         off[k] = total;
-        total += al(inst_scratch_bytes(inst[k].nx, inst[k].ny, inst[k].nz, mixed));
+        total += al(ygpu_inst_scratch_bytes(inst[k].nx, inst[k].ny, inst[k].nz, mixed));
         max_nu = std::max(max_nu, (size_t)2 * inst[k].nx * inst[k].ny);
     }
     if ((st = grow(&c->arena, &c->arena_cap, total))) return st;
@@ -397,8 +403,8 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     c->h_insts.resize(n);
     for (int k = 0; k < n; k++) {
         Inst& I = c->h_insts[k];
-        fill_inst(I, kind, &inst[k]);
-        inst_scratch_carve(I, c->arena + off[k], inst[k].nx, inst[k].ny, inst[k].nz, mixed);
+        ygpu_fill_inst(I, kind, &inst[k]);
+        ygpu_inst_scratch_carve(I, c->arena + off[k], inst[k].nx, inst[k].ny, inst[k].nz, mixed);
         I.out = c->d_out + k;
     }
     CK(cudaMemcpyAsync(c->d_insts, c->h_insts.data(), sizeof(Inst) * (size_t)n, cudaMemcpyHostToDevice, c->stream));

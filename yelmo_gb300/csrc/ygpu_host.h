@@ -33,3 +33,13 @@ int ygpu_dyn_inputs_device(cudaStream_t s, const double* H, const double* zb, co
                            int bc, int nx, int ny);
 int ygpu_ssa_masks_device(cudaStream_t s, int* mx, int* my, const int* mf, const double* f_ice, const double* f_grnd,
                           int lat, int bc, int nx, int ny);
+
+// ygpu_api.cu internals shared with the other translation units
+struct ygpu_fields;
+int ygpu_check_par(const ygpu_dyn_par* p);
+int ygpu_fields_check(int kind, const ygpu_fields* f);
+void ygpu_fill_inst(Inst& I, int kind, const ygpu_fields* f);
+size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed);
+void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed);
+size_t ygpu_align256(size_t b);
+int ygpu_single_team_ctas(int max_ctas, size_t nu);

@@ -32,7 +32,7 @@ EXPORTS = [
     "ygpu_dyn_par_defaults", "ygpu_parse_lis_opt", "ygpu_boundary_code", "ygpu_last_error", "ygpu_version",
     "ygpu_calc_velocity_ssa", "ygpu_calc_velocity_diva", "ygpu_set_ssa_masks", "ygpu_calc_dyn_inputs",
     "ygpu_linear_solver_matrix_solve", "ygpu_ctx_create", "ygpu_ctx_destroy", "ygpu_ctx_stream",
-    "ygpu_solve_device", "ygpu_solve_batch_device",
+    "ygpu_solve_device", "ygpu_solve_batch_device", "ygpu_solve_device_noalloc",
 ]
 
 
@@ -71,6 +71,8 @@ def lib(build_if_missing: bool = True):
                                     C.POINTER(abi.Stats)]
     L.ygpu_solve_batch_device.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.DynPar), C.c_int,
                                           C.POINTER(abi.Fields), C.POINTER(abi.Stats)]
+    L.ygpu_solve_device_noalloc.argtypes = [C.c_int, C.POINTER(abi.DynPar), C.POINTER(abi.Fields),
+                                            C.POINTER(abi.Stats), C.c_void_p]
     ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
     L.ygpu_linear_solver_matrix_solve.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_char_p, ip, ip, dp]
     _lib = L
@@ -169,6 +171,19 @@ def make_fields(dev: dict, nx, ny, nz, dx, dy, n_glen) -> abi.Fields:
         t = dev.get(name)
         setattr(f, name, t.data_ptr() if t is not None else None)
     return f
+
+
+def solve_device_noalloc(kind: int, par: YdynParams, fields: abi.Fields, stream: int = 0) -> dict:
+    """ygpu_solve_device_noalloc: the solve with the library's fixed scratch array
+    (no device allocation); ``stream`` is a cudaStream_t handle (0: default stream)."""
+    st = abi.Stats()
+    cpar = par.to_c()
+    r = lib().ygpu_solve_device_noalloc(kind, C.byref(cpar), C.byref(fields), C.byref(st),
+                                        C.c_void_p(stream) if stream else None)
+    _check(r)
+    out = st.as_dict()
+    out["return"] = r
+    return out
 
 
 class DeviceSolver:
