@@ -1,17 +1,28 @@
 #!/usr/bin/env python
 """Benchmark: SSA/DIVA velocity solves per second on GB300.
 
-Workload (default): the marine single DIVA solve, 161 x 161, dx 8 km, 10 sigma
-layers, cold start, converged to Picard change < 1e-7 and linear relative
-residual < 1e-9 so that the velocity is within 1e-6 (relative L2) of the FP64
-oracle converged to 1e-10. One step = one full solve. ``value`` is the
-mixed-precision (FP32 Krylov inside FP64 defect correction) solves/s with the
-fields resident in HBM; the plain FP64 solve is reported beside it. ``e2e`` is
-the same solve through the C ABI drop-in (ygpu_calc_velocity_diva) from host
-buffers, host-device copies included.
+Default workload: the marine single DIVA solve, 161 x 161 cells, dx 8 km, 10 sigma
+layers. Each solve is a cold start, converged to a Picard change < 1e-7 and a linear
+relative residual < 1e-9. That puts the velocity within 1e-6 (relative L2) of the FP64
+oracle converged to 1e-10.
 
-Multi-GPU: replicas only (instances are independent, no collective); each rank
-solves K instances on its own GPU and ``value`` sums over ranks.
+Modes:
+- A *batched* step solves B independent instances of the workload in one persistent
+  launch. The instances differ in the seed of the bed roughness and the friction field;
+  teams of CTAs take them from a device queue.
+- ``value`` is the mixed-precision throughput: B solves per step, with the fields
+  resident in HBM. The mixed precision is FP32 viscosity and Krylov inside FP64 defect
+  correction.
+- The plain FP64 throughput, and single-solve latency p50/p99 for both precisions, are
+  reported beside it.
+- ``e2e`` times the C-ABI drop-in ``ygpu_calc_velocity_diva`` on host buffers, with the
+  host-device copies inside the timed region.
+
+``--workload ensemble`` runs the batched uneven ensemble instead: 256 SSA instances with
+sides in {41, 81, 121, 161}.
+
+Multi-GPU: replicas only. Instances are independent, so there is no collective. Each
+rank runs the same job on its own GPU and ``value`` sums over ranks.
 """
 from __future__ import annotations
 
@@ -31,23 +42,33 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "SSA/DIVA solves/s, p50/p99 latency; mixed-FP32 vs FP64 on GPU at 1e-6 rel err"
+BENCH_TOL = dict(ssa_iter_max=300, ssa_iter_conv=1e-7,
+                 ssa_lis_opt_energy="-i cg -p jacobi -maxiter 5000 -tol 1.0e-9 -initx_zeros false",
+                 ssa_lis_opt_residual="-i bicgstab -p jacobi -maxiter 5000 -tol 1.0e-9 -initx_zeros false")
 
 
-def bench_instance(name: str):
+def make_instances(workload: str, batch: int):
     from yelmo_gb300 import configs
-    if name == "marine_diva":
-        inst = configs.marine_diva()
-    elif name == "dome_ssa":
-        inst = configs.dome_ssa()
-    elif name == "continent_diva":
-        inst = configs.continent_diva()
+    if workload == "marine_diva":
+        insts = [configs.marine_diva(seed=2024 + b) for b in range(batch)]
+    elif workload == "dome_ssa":
+        insts = [configs.dome_ssa(seed=1234 + b) for b in range(batch)]
+    elif workload == "continent_diva":
+        insts = [configs.continent_diva(seed=4242 + b) for b in range(batch)]
+    elif workload == "ensemble":
+        insts = [configs.ensemble_member(i) for i in range(batch)]
     else:
-        raise SystemExit(f"unknown workload {name}")
-    inst.par = inst.par.with_(
-        ssa_iter_max=300, ssa_iter_conv=1e-7,
-        ssa_lis_opt_energy="-i cg -p jacobi -maxiter 5000 -tol 1.0e-9 -initx_zeros false",
-        ssa_lis_opt_residual="-i bicgstab -p jacobi -maxiter 5000 -tol 1.0e-9 -initx_zeros false")
-    return inst
+        raise SystemExit(f"unknown workload {workload}")
+    for inst in insts:
+        inst.par = inst.par.with_(**BENCH_TOL)
+    return insts
+
+
+def describe(inst, batch):
+    kind = "SSA" if inst.par.solver == "ssa" else "DIVA"
+    if inst.name.startswith("ensemble"):
+        return f"ensemble of {batch} {kind} instances, sides 41-161, 1280 km domain, cold solves"
+    return f"{inst.name} {inst.nx}x{inst.ny}x{inst.nz} dx={inst.dx/1e3:g}km cold {kind} solve"
 
 
 def rel_l2(a, b):
@@ -62,17 +83,14 @@ class ClockSampler:
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index=0):
-        self.index = index
-        self.proc = None
-        self.lines = []
+        self.index, self.proc, self.lines = index, None, []
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.t = threading.Thread(target=self._read, daemon=True)
-            self.t.start()
+            threading.Thread(target=self._read, daemon=True).start()
         except Exception:
             self.proc = None
 
@@ -106,43 +124,45 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def run_reference(args, inst, rank, world):
+def _copy(f):
+    return {k: (v.copy(order="F") if isinstance(v, np.ndarray) else v) for k, v in f.items()}
+
+
+def run_reference(args, insts, rank, world):
     """CPU reference arm: the oracle (FP64 restatement of the reference path) on all host cores."""
     if rank != 0:
         return None
     import oracle
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
+    inst = insts[0]
     f0 = oracle.prepare(inst)
-    times = []
+    times, out = [], None
     for s in range(args.warmup + args.steps):
-        f = {k: (v.copy(order="F") if isinstance(v, np.ndarray) else v) for k, v in f0.items()}
+        f = _copy(f0)
         t = time.perf_counter()
         out = oracle.calc_velocity(f, inst)
         dt = time.perf_counter() - t
         if s >= args.warmup:
             times.append(dt)
-    tot = sum(times)
-    value = len(times) / tot
-    line = {
+    value = len(times) / sum(times)
+    return {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded marine dome over a rough, seaward-deepening bed)",
-        "config": {"workload": f"{inst.name} {inst.nx}x{inst.ny}x{inst.nz} dx={inst.dx/1e3:g}km cold DIVA solve",
-                   "picard_tol": inst.par.ssa_iter_conv, "lin": inst.par.lis_opt},
+        "data": "synthetic (seeded)",
+        "config": {"workload": describe(inst, 1), "picard_tol": inst.par.ssa_iter_conv, "lin": inst.par.lis_opt},
         "latency_ms": {"p50": 1e3 * float(np.percentile(times, 50)), "p99": 1e3 * float(np.percentile(times, 99))},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": f"{len(times)} full solves of the workload (oracle: C FP64 restatement, OpenMP)"},
+                         "sample": f"{len(times)} full solves (oracle: C FP64 restatement, OpenMP, {cores} threads)"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "picard_iters": out["ssa_iter_now"], "lin_iters": out["ssa_lin_iter"],
     }
-    return line
 
 
 def cpu_baseline_leg(inst, budget_s=20.0):
     """Oracle timed on the host cores (bounded sample), and its tightly converged
-    solution as the checker of the GPU results."""
+    solution, the checker of the GPU results."""
     import oracle
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
@@ -150,41 +170,43 @@ def cpu_baseline_leg(inst, budget_s=20.0):
     times = []
     t_all = time.perf_counter()
     while True:
-        f = {k: (v.copy(order="F") if isinstance(v, np.ndarray) else v) for k, v in f0.items()}
+        f = _copy(f0)
         t = time.perf_counter()
         oracle.calc_velocity(f, inst)
         times.append(time.perf_counter() - t)
         if time.perf_counter() - t_all > budget_s or len(times) >= 5:
             break
-    tight = {k: (v.copy(order="F") if isinstance(v, np.ndarray) else v) for k, v in f0.items()}
-    par_t = inst.par.with_(ssa_iter_max=600, ssa_iter_conv=1e-10,
+    tight = _copy(f0)
+    par_t = inst.par.with_(ssa_iter_max=800, ssa_iter_conv=1e-10,
                            ssa_lis_opt_energy="-i cg -p jacobi -maxiter 20000 -tol 1.0e-12",
                            ssa_lis_opt_residual="-i bicgstab -p jacobi -maxiter 20000 -tol 1.0e-12")
     oracle.calc_velocity(tight, inst, par_t)
     base = {"value": len(times) / sum(times), "unit": "solves/s", "cores": cores, "kind": "port",
             "sample": f"{len(times)} full solves of the same workload (oracle: C FP64 restatement, "
                       f"OpenMP, {cores} threads)"}
-    return base, tight, f0
+    return base, tight
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="marine_diva")
+    ap.add_argument("--batch", type=int, default=0, help="instances per batched step (default 16; ensemble 256)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    batch = args.batch or (256 if args.workload == "ensemble" else 16)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    inst = bench_instance(args.workload)
+    insts = make_instances(args.workload, batch)
 
     if args.impl == "reference":
-        line = run_reference(args, inst, rank, world)
+        line = run_reference(args, insts, rank, world)
         if line is not None:
             print(json.dumps(line))
         return
@@ -196,123 +218,135 @@ def main():
     dist = None
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        dist.init_process_group("nccl")
 
-    cpu_base, tight, f_host = (None, None, None)
-    if rank == 0 and not args.no_cpu:
-        cpu_base, tight, f_host = cpu_baseline_leg(inst)
-    if f_host is None:
-        f_host = gpu.prepare(inst)
-    nx, ny, nz = inst.nx, inst.ny, inst.nz
-    kind = inst.par.kind
+    ensemble = args.workload == "ensemble"
+    cpu_base, tight = (None, None)
+    if rank == 0 and not args.no_cpu and not ensemble:
+        cpu_base, tight = cpu_baseline_leg(insts[0])
 
-    dev = gpu.to_device(f_host, f"cuda:{local}")
-    pristine = {k: dev[k].clone() for k in gpu.STATE_NAMES}
-    fields = gpu.make_fields(dev, nx, ny, nz, inst.dx, inst.dx, inst.n_glen)
+    kind = insts[0].par.kind
+    hosts = [gpu.prepare(inst) for inst in insts]
+    devs = [gpu.to_device(f, f"cuda:{local}") for f in hosts]
+    pristine = [{k: d[k].clone() for k in gpu.STATE_NAMES} for d in devs]
+    fields = [gpu.make_fields(d, i.nx, i.ny, i.nz, i.dx, i.dx, i.n_glen) for d, i in zip(devs, insts)]
     solver = gpu.DeviceSolver(local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
-    def reset():
-        for k in gpu.STATE_NAMES:
-            dev[k].copy_(pristine[k])
-        for k in ("ux", "uy", "ux_i", "uy_i", "duxdz", "duydz"):
-            dev[k].zero_()
+    def reset(idx):
+        for b in idx:
+            for k in gpu.STATE_NAMES:
+                devs[b][k].copy_(pristine[b][k])
+        flush.zero_()               # L2 flush between timed steps
+        torch.cuda.synchronize()
 
-    def run(par, steps, warmup):
-        res = []
-        for s in range(warmup + steps):
-            reset()
-            flush.zero_()             # L2 flush between timed solves
-            torch.cuda.synchronize()
-            st = solver.solve(kind, par, fields)
-            if s >= warmup:
-                res.append(st)
-        return res
-
-    results = {}
-    for prec in ("fp64", "mixed"):
-        par = inst.par.with_(precision=prec)
+    def barrier():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
+
+    res = {}
+    clocks = None
+    for prec in ("fp64", "mixed"):
+        par = insts[0].par.with_(precision=prec)
+        # single-solve latency (instance 0)
+        lat, st1 = [], None
+        n_single = 0 if ensemble else args.warmup + args.steps
+        for s in range(n_single):
+            reset([0])
+            st1 = solver.solve(kind, par, fields[0])
+            if s >= args.warmup:
+                lat.append(st1["device_ms"])
+        u_single = None if ensemble else devs[0]["ux_bar" if kind == abi.KIND_DIVA else "ux_b"].cpu().numpy().reshape(
+            (insts[0].nx, insts[0].ny), order="F")
+        # batched throughput
+        barrier()
         clk = ClockSampler(local)
         if prec == "mixed":
             clk.start()
-        t0 = time.perf_counter()
-        sts = run(par, args.steps, args.warmup)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
-        clocks = clk.stop() if prec == "mixed" else None
-        ms = [s["device_ms"] for s in sts]
-        u = {k: dev[k].cpu().numpy().reshape((nx, ny), order="F") for k in ("ux_bar", "uy_bar")}
-        err = None
-        if tight is not None:
-            err = max(rel_l2(u["ux_bar"], tight["ux_bar"]), rel_l2(u["uy_bar"], tight["uy_bar"]))
-        tot_ms = sum(ms)
+        step_ms, sts = [], None
+        for s in range(args.warmup + args.steps):
+            reset(range(batch))
+            sts = solver.solve_batch(kind, par, fields)
+            if s >= args.warmup:
+                step_ms.append(sts[0]["device_ms"])
+        barrier()
+        if prec == "mixed":
+            clocks = clk.stop()
+        vel = "ux_bar" if kind == abi.KIND_DIVA else "ux_b"
+        u_batch = [d[vel].cpu().numpy().reshape((i.nx, i.ny), order="F") for d, i in zip(devs, insts)]
+        tot_ms = sum(step_ms)
         if dist is not None:
             t = torch.tensor([tot_ms], device=f"cuda:{local}")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             tot_ms = float(t.item())
-        results[prec] = {"ms": ms, "tot_ms": tot_ms, "stats": sts[-1], "err": err, "clocks": clocks,
-                         "wall": wall}
+        res[prec] = {"lat": lat, "st1": st1, "step_ms": step_ms, "tot_ms": tot_ms, "sts": sts,
+                     "u_single": u_single, "u_batch": u_batch}
 
-    # e2e: the C-ABI drop-in from host buffers (copies inside the timed region)
+    # e2e: the C-ABI drop-in on host buffers (host-device copies inside the timed region)
     e2e_times = []
-    par_m = inst.par.with_(precision="mixed")
-    for s in range(args.warmup + max(3, args.steps // 2)):
-        f = {k: (v.copy(order="F") if isinstance(v, np.ndarray) else v) for k, v in f_host.items()}
-        t = time.perf_counter()
-        gpu.calc_velocity(f, inst.dx, inst.n_glen, par_m)
-        dt = time.perf_counter() - t
-        if s >= args.warmup:
-            e2e_times.append(dt)
-    h2d, d2h = gpu.host_io_bytes(kind, nx, ny, nz)
+    if not ensemble:
+        par_m = insts[0].par.with_(precision="mixed")
+        for s in range(args.warmup + max(3, args.steps // 2)):
+            f = _copy(hosts[0])
+            t = time.perf_counter()
+            gpu.calc_velocity(f, insts[0].dx, insts[0].n_glen, par_m)
+            dt = time.perf_counter() - t
+            if s >= args.warmup:
+                e2e_times.append(dt)
+    i0 = insts[0]
+    h2d, d2h = gpu.host_io_bytes(kind, i0.nx, i0.ny, i0.nz)
 
     if rank != 0:
         if dist is not None:
             dist.destroy_process_group()
         return
-    mixed, fp64 = results["mixed"], results["fp64"]
-    K = len(mixed["ms"])
-    value = world * K / (mixed["tot_ms"] / 1e3)
-    st = mixed["stats"]
-    alg = gpu.algorithmic_bytes(st, kind, nx, ny, nz, mixed=True, energy=inst.par.ssa_solver == "energy")
-    avg_ms = statistics.mean(mixed["ms"])
+    mixed, fp64 = res["mixed"], res["fp64"]
+    K = len(mixed["step_ms"])
+    value = world * batch * K / (mixed["tot_ms"] / 1e3)
+    value64 = world * batch * K / (fp64["tot_ms"] / 1e3)
+    # error of the mixed batch against the FP64 batch, per instance
+    err_mixed_vs_fp64 = max(rel_l2(a, b) for a, b in zip(mixed["u_batch"], fp64["u_batch"]))
+    err_vs_oracle = None
+    if tight is not None:
+        vel = "ux_bar" if kind == abi.KIND_DIVA else "ux_b"
+        err_vs_oracle = {"mixed": rel_l2(mixed["u_single"], tight[vel]), "fp64": rel_l2(fp64["u_single"], tight[vel])}
+    # roofline of the solver kernel over the batched step
+    alg = sum(gpu.algorithmic_bytes(st, kind, i.nx, i.ny, i.nz, mixed=True)
+              for st, i in zip(mixed["sts"], insts))
+    avg_ms = statistics.mean(mixed["step_ms"])
     achieved = alg / (avg_ms / 1e3) / 1e9
-    peaks = {}
     try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        peak_src = "measured"
     except Exception:
-        pass
-    peak = float(peaks.get("hbm_gbs", 6800.0))
-    alg64 = gpu.algorithmic_bytes(fp64["stats"], kind, nx, ny, nz, mixed=False)
+        peak, peak_src = 6800.0, "fallback"
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": avg_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32/f64 (FP32 Krylov, FP64 defect correction)",
-        "data": "synthetic (seeded marine dome over a rough, seaward-deepening bed)",
-        "config": {"workload": f"{inst.name} {nx}x{ny}x{nz} dx={inst.dx/1e3:g}km cold DIVA solve",
-                   "picard_tol": inst.par.ssa_iter_conv, "lin": inst.par.lis_opt,
-                   "l2": "flushed (256 MB write) between timed solves", "parallelism": f"replicas x{world}"},
-        "latency_ms": {"p50": float(np.percentile(mixed["ms"], 50)), "p99": float(np.percentile(mixed["ms"], 99))},
-        "fp64": {"value": world * len(fp64["ms"]) / (fp64["tot_ms"] / 1e3), "unit": "solves/s",
-                 "ms_per_step": statistics.mean(fp64["ms"]),
-                 "latency_ms": {"p50": float(np.percentile(fp64["ms"], 50)),
-                                "p99": float(np.percentile(fp64["ms"], 99))},
-                 "rel_err_vs_oracle": fp64["err"], "picard_iters": fp64["stats"]["ssa_iter_now"],
-                 "lin_iters": fp64["stats"]["ssa_lin_iter"],
-                 "achieved_gbs": alg64 / (statistics.mean(fp64["ms"]) / 1e3) / 1e9},
-        "mixed_over_fp64": (statistics.mean(fp64["ms"]) / avg_ms),
-        "rel_err_vs_oracle": mixed["err"],
-        "picard_iters": st["ssa_iter_now"], "lin_iters": st["ssa_lin_iter"], "outer_iters": st["outer_iter"],
+        "vs_baseline": None, "dtype": "f32/f64 (FP32 viscosity and Krylov, FP64 defect correction)",
+        "data": "synthetic (seeded beds, geometry and friction)",
+        "config": {"workload": describe(i0, batch), "batch": batch, "picard_tol": i0.par.ssa_iter_conv,
+                   "lin": i0.par.lis_opt, "l2": "flushed (256 MB write) between timed steps",
+                   "parallelism": f"replicas x{world}"},
+        "latency_ms": ({"p50": float(np.percentile(mixed["lat"], 50)), "p99": float(np.percentile(mixed["lat"], 99))}
+                       if mixed["lat"] else None),
+        "fp64": {"value": value64, "unit": "solves/s", "ms_per_step": statistics.mean(fp64["step_ms"]),
+                 "latency_ms": ({"p50": float(np.percentile(fp64["lat"], 50)),
+                                 "p99": float(np.percentile(fp64["lat"], 99))} if fp64["lat"] else None)},
+        "mixed_over_fp64": value / value64,
+        "rel_err_vs_oracle": err_vs_oracle,
+        "rel_err_mixed_vs_fp64_max": err_mixed_vs_fp64,
+        "picard_iters": [s["ssa_iter_now"] for s in mixed["sts"][:4]],
         "gpu_launches": K,
-        "e2e": {"value": 1.0 / statistics.mean(e2e_times), "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "path": "ygpu_calc_velocity_diva (host buffers)"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "kernel": "ygpu_solve_kernel (whole Picard solve, one launch)",
-                     "note": "peak = measured copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"},
-        "clocks": mixed["clocks"],
+        "e2e": ({"value": 1.0 / statistics.mean(e2e_times), "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                 "d2h_bytes_per_step": d2h, "path": "ygpu_calc_velocity_diva on host buffers, one solve per step"}
+                if e2e_times else None),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "ygpu_solve_kernel (batched step, one launch)",
+                     "peak_source": peak_src},
+        "phase_ms_single": mixed["st1"]["phase_ms"] if mixed["st1"] else None,
+        "clocks": clocks,
         "cpu_baseline": cpu_base,
     }
     print(json.dumps(line))

@@ -355,9 +355,16 @@ static void choose_teams(const ygpu_ctx* c, int n_inst, size_t max_nu, int* n_te
         *n_teams = 1;
         return;
     }
-    int tc = env_int("YGPU_BATCH_TEAM_CTAS", 1);
+    // teams share the GPU: as many CTAs per team as the batch leaves, but no more
+    // than one CTA per ~4096 unknowns of the largest instance
+    int auto_tc = maxc / n_inst;
+    int by_size = (int)(max_nu / 4096);
+    if (auto_tc > by_size) auto_tc = by_size;
+    if (auto_tc < 1) auto_tc = 1;
+    int tc = env_int("YGPU_BATCH_TEAM_CTAS", auto_tc);
     if (tc < 1) tc = 1;
     if (tc > maxc) tc = maxc;
+    if (tc > YG_MAX_TEAM_CTAS) tc = YG_MAX_TEAM_CTAS;
     int nt = maxc / tc;
     if (nt > n_inst) nt = n_inst;
     if (nt < 1) nt = 1;
@@ -400,12 +407,19 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
         CK(cudaMalloc((void**)&c->d_ctl, sizeof(TeamCtl) * (size_t)n_teams));
         c->ctl_cap = n_teams;
     }
+    // queue order: largest instance first (longest-processing-time first)
+    std::vector<int> order(n);
+    for (int k = 0; k < n; k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (size_t)inst[a].nx * inst[a].ny * inst[a].nz > (size_t)inst[b].nx * inst[b].ny * inst[b].nz;
+    });
     c->h_insts.resize(n);
-    for (int k = 0; k < n; k++) {
-        Inst& I = c->h_insts[k];
+    for (int q = 0; q < n; q++) {
+        const int k = order[q];
+        Inst& I = c->h_insts[q];
         ygpu_fill_inst(I, kind, &inst[k]);
         ygpu_inst_scratch_carve(I, c->arena + off[k], inst[k].nx, inst[k].ny, inst[k].nz, mixed);
-        I.out = c->d_out + k;
+        I.out = c->d_out + k;      // outputs stay in caller order
     }
     CK(cudaMemcpyAsync(c->d_insts, c->h_insts.data(), sizeof(Inst) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->d_out, 0, sizeof(InstOut) * (size_t)n, c->stream));

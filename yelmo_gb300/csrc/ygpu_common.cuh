@@ -96,6 +96,14 @@ struct InstOut {
     int lin_status;    // status of the last linear solve
     int outer_iter;    // mixed: defect-correction steps
     int converged;
+    // state carried between the step kernels of the Picard loop
+    int done;          // solve finished (converged, iteration limit or error)
+    int in_alt;        // the current viscosity lives in visc_alt
+    double bn2;        // ||b||^2 of this iteration's linear system
+    int lin_it;        // last linear solve: iterations, status, outer steps, residual
+    int lin_st;
+    int lin_outer;
+    double lin_rr;
     double phase_ns[10];   // device time per phase: setup, strain, column, faces, system, krylov, epilogue,
                            // final, and the all-reduce share of the solve and of the Krylov phase
 };

@@ -17,7 +17,7 @@ void ygpu_set_error(const char* fmt, ...);
 
 // ygpu_solver.cu
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
-                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_queue, int* d_abort);
+                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort);
 int ygpu_solver_max_ctas(int device);
 int ygpu_sm_count(int device);
 size_t ygpu_teamctl_bytes();

@@ -20,6 +20,7 @@
 //   epilogue    velocity extraction, clip, relaxation, L2 convergence norm,
 //               error matrix, basal stress and basal velocity
 #include <cuda_runtime.h>
+#include <stdlib.h>
 
 #include <math.h>
 #include <stdio.h>
@@ -1674,31 +1675,30 @@ __device__ __noinline__ void phase_diva_final(const Inst& I, const Geo& G, Team&
 }
 
 // ---------------------------------------------------------------------------
-// The Picard loop of one instance, run by one team
+// The Picard loop as steps: setup / pre (strain, shear, column, faces,
+// system) / krylov / post (epilogue, convergence, final passes). Each step
+// is a cooperative kernel over teams of CTAs; the state between steps lives
+// in the instance's InstOut. The heavy steps and the lean Krylov kernel have
+// their own register budgets and block sizes.
 // ---------------------------------------------------------------------------
-__device__ __noinline__ void solve_instance(const Inst& I, const ygpu_dyn_par& P, Team& T) {
+struct PhaseClock {
+    unsigned long long t0;
+    YG_DEV void start() { t0 = global_ns(); }
+    YG_DEV double lap() {
+        unsigned long long t = global_ns();
+        double d = (double)(t - t0);
+        t0 = t;
+        return d;
+    }
+};
+
+__device__ __noinline__ void step_setup(const Inst& I, const ygpu_dyn_par& P, Team& T, int* done_count) {
     const bool diva = (I.kind == YGPU_KIND_DIVA);
     const Geo G = make_geo(I, P);
     InstOut* out = I.out;
     const bool lead = (T.cta == 0 && threadIdx.x == 0);
-    int status = YGPU_OK, lin_status = YGPU_OK;
-    int iter_now = 0, lin_iter = 0, lin_fail = 0, outer_total = 0;
-    double resid = 0.0, lin_resid = 0.0;
-    bool ok = true;
-    // scratch for the strain rates (the drag arrays are free until the faces phase)
-    double* sdudx = I.lk_x;
-    double* sdudy = I.lk_y;
-    double* sdvdx = I.lr_x;
-    double* sdvdy = I.lr_y;
-    double tph[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    double sync_before_krylov = 0.0;
-    unsigned long long t_last = global_ns();
-    auto tick = [&](int k) {
-        unsigned long long t = global_ns();
-        tph[k] += (double)(t - t_last);
-        t_last = t;
-    };
-    // ---- setup ----
+    PhaseClock clk;
+    clk.start();
     for (int c = T.tid; c < G.n2; c += T.nthr) {
         I.err_x[c] = 1.0;
         I.err_y[c] = 1.0;
@@ -1712,154 +1712,257 @@ __device__ __noinline__ void solve_instance(const Inst& I, const ygpu_dyn_par& P
             if ((fb == 0.0 && fa < 1.0) || (fa == 0.0 && fb < 1.0)) I.u_y[c] = 0.0;
         }
     }
-    if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-    if (!phase_classify(I, P, G, T)) { status = ld_acquire_s32(T.abort_all) ? YGPU_ERR_TIMEOUT : YGPU_ERR_BAD_ARG; goto finish; }
-    if (P.visc_method != 0) phase_att_powers(I, P, G, T);
-    if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-    tick(0);
-
-    {
-        double* vcur = I.visc;
-        double* vnew = I.visc_alt;
-        int in_alt = 0;            // the current visc lives in visc_alt
-        double* last_cur = vcur;
-        for (int iter = 1; iter <= P.ssa_iter_max; iter++) {
-            const bool relax = diva ? true : (P.visc_method != 0);
-            if (P.visc_method == 1 || diva) {
-                if (P.visc_method == 1) phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
-                if (diva) phase_shear(I, G, T, vcur);
-                if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-            }
-            tick(1);
-            if (P.precision == YGPU_PREC_MIXED)
-                phase_column<float>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
-            else
-                phase_column<double>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
-            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-            tick(2);
-            last_cur = vcur;
-            { double* tmp = vcur; vcur = vnew; vnew = tmp; in_alt ^= 1; }
-            phase_faces(I, P, G, T, diva);
-            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-            tick(3);
-            double bn2 = 0.0;
-            phase_system(I, P, G, T, bn2);
-            if (!team_allreduce(T, &bn2, 1)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-            tick(4);
-            sync_before_krylov = T.sync_ns;
-            int it = 0, outer = 0;
-            double rr = 0.0;
-            int st;
-            if (bn2 == 0.0) {
-                // homogeneous system: x = 0 (solver_linear.F90:162-174)
-                for (int u = T.tid; u < G.nu; u += T.nthr) I.x[u] = 0.0;
-                st = YGPU_OK;
-            } else {
-                st = linear_solve(I, P, G, T, sqrt(bn2), it, rr, outer, ok);
-                if (!ok) { status = YGPU_ERR_TIMEOUT; goto finish; }
-            }
-            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-            tick(5);
-            tph[9] += T.sync_ns - sync_before_krylov;
-            lin_iter += it;
-            outer_total += outer;
-            if (st != YGPU_OK) lin_fail++;
-            lin_status = st;
-            lin_resid = rr;
-            double red[4];
-            phase_epilogue(I, P, G, T, diva, red);
-            if (!team_allreduce(T, red, 4)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-            tick(6);
-            resid = (red[2] > 0.0) ? sqrt(red[0]) / (sqrt(red[1]) + 1e-10) : 0.0;
-            iter_now = iter;
-            if (P.ssa_write_log && lead)
-                printf("ssa: %s %4d %12.4g | lin %6d %d\n", (resid < P.ssa_iter_conv) ? "C" : "", iter, resid, it, st);
-            if (red[3] > 0.0 || !isfinite(resid)) { status = YGPU_ERR_NONFINITE; break; }
-            if (resid < P.ssa_iter_conv || iter == P.ssa_iter_max) break;
-        }
-        if (status != YGPU_OK) goto finish;
-        // ---- after the loop ----
-        double nlim = count_lim_part(I, P, G, T);
-        if (diva) {
-            phase_diva_final(I, G, T, last_cur, vcur);
-        } else {
-            for (int c = T.tid; c < G.n2; c += T.nthr) {
-                // calc_basal_stress, velocity_ssa.f90:588-617
-                double tx = I.bm_x[c] * I.u_x[c], ty = I.bm_y[c] * I.u_y[c];
-                I.taub_x[c] = (fabs(tx) < 1e-5) ? 0.0 : tx;
-                I.taub_y[c] = (fabs(ty) < 1e-5) ? 0.0 : ty;
-            }
-        }
-        if (!team_allreduce(T, &nlim, 1)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-        if (!diva && P.visc_method == 0) {
-            // diagnose the viscosity of the solution (not used prognostically)
-            phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
-            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-            ygpu_dyn_par P1 = P;
-            P1.visc_method = 1;
-            phase_att_powers(I, P1, G, T);
-            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-            phase_column<double>(I, P1, G, T, vcur, vcur, sdudx, sdudy, sdvdx, sdvdy, false, false, false, false, true);
-            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto finish; }
-        }
-        // the caller's visc_eff must hold the final viscosity
-        if (in_alt) {
-            for (size_t k = T.tid; k < (size_t)G.n2 * G.nz; k += T.nthr) I.visc[k] = I.visc_alt[k];
-        }
-        if (lead) out->lim_n = (int)nlim;
+    int status = YGPU_OK;
+    if (!team_barrier(T)) status = YGPU_ERR_TIMEOUT;
+    else if (!phase_classify(I, P, G, T)) status = ld_acquire_s32(T.abort_all) ? YGPU_ERR_TIMEOUT : YGPU_ERR_BAD_ARG;
+    else {
+        if (P.visc_method != 0) phase_att_powers(I, P, G, T);
+        if (!team_barrier(T)) status = YGPU_ERR_TIMEOUT;
     }
-finish:
-    tick(7);
     if (lead) {
-        tph[8] = T.sync_ns;
-        for (int k = 0; k < 10; k++) out->phase_ns[k] = tph[k];
-        out->iter_now = iter_now;
-        out->lin_iter = lin_iter;
-        out->lin_fail = lin_fail;
-        out->resid = resid;
-        out->lin_resid = lin_resid;
-        out->outer_iter = outer_total;
-        out->lin_status = lin_status;
-        out->status = (status != YGPU_OK) ? status : lin_status;
-        out->converged = (status == YGPU_OK);
+        out->phase_ns[0] += clk.lap();
+        out->status = status;
+        out->done = (status != YGPU_OK);
+        if (status != YGPU_OK) atomicAdd(done_count, 1);
+    }
+}
+
+__device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team& T, int* done_count) {
+    const bool diva = (I.kind == YGPU_KIND_DIVA);
+    const Geo G = make_geo(I, P);
+    InstOut* out = I.out;
+    const bool lead = (T.cta == 0 && threadIdx.x == 0);
+    double* sdudx = I.lk_x;
+    double* sdudy = I.lk_y;
+    double* sdvdx = I.lr_x;
+    double* sdvdy = I.lr_y;
+    const int iter = out->iter_now + 1;
+    const int in_alt = out->in_alt;
+    double* vcur = in_alt ? I.visc_alt : I.visc;
+    double* vnew = in_alt ? I.visc : I.visc_alt;
+    const bool relax = diva ? true : (P.visc_method != 0);
+    PhaseClock clk;
+    clk.start();
+    double t1 = 0, t2 = 0, t3 = 0, t4 = 0;
+    int status = YGPU_OK;
+    double bn2 = 0.0;
+    if (P.visc_method == 1 || diva) {
+        if (P.visc_method == 1) phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
+        if (diva) phase_shear(I, G, T, vcur);
+        if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
+    }
+    t1 = clk.lap();
+    if (P.precision == YGPU_PREC_MIXED)
+        phase_column<float>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
+    else
+        phase_column<double>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
+    if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
+    t2 = clk.lap();
+    phase_faces(I, P, G, T, diva);
+    if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
+    t3 = clk.lap();
+    phase_system(I, P, G, T, bn2);
+    if (!team_allreduce(T, &bn2, 1)) { status = YGPU_ERR_TIMEOUT; goto out_; }
+    t4 = clk.lap();
+out_:
+    if (lead) {
+        out->phase_ns[1] += t1;
+        out->phase_ns[2] += t2;
+        out->phase_ns[3] += t3;
+        out->phase_ns[4] += t4;
+        out->iter_now = iter;
+        out->in_alt = in_alt ^ 1;
+        out->bn2 = bn2;
+        if (status != YGPU_OK) {
+            out->status = status;
+            out->done = 1;
+            atomicAdd(done_count, 1);
+        }
+    }
+}
+
+__device__ __noinline__ void step_krylov(const Inst& I, const ygpu_dyn_par& P, Team& T, int* done_count) {
+    const Geo G = make_geo(I, P);
+    InstOut* out = I.out;
+    const bool lead = (T.cta == 0 && threadIdx.x == 0);
+    PhaseClock clk;
+    clk.start();
+    const double s0 = T.sync_ns;
+    const double bn2 = out->bn2;
+    int it = 0, outer = 0, st;
+    double rr = 0.0;
+    bool ok = true;
+    if (bn2 == 0.0) {
+        // homogeneous system: x = 0 (solver_linear.F90:162-174)
+        for (int u = T.tid; u < G.nu; u += T.nthr) I.x[u] = 0.0;
+        st = YGPU_OK;
+    } else {
+        st = linear_solve(I, P, G, T, sqrt(bn2), it, rr, outer, ok);
+    }
+    if (ok) ok = team_barrier(T);
+    if (lead) {
+        out->phase_ns[5] += clk.lap();
+        out->phase_ns[9] += T.sync_ns - s0;
+        out->lin_it = it;
+        out->lin_st = st;
+        out->lin_outer = outer;
+        out->lin_rr = rr;
+        if (!ok) {
+            out->status = YGPU_ERR_TIMEOUT;
+            out->done = 1;
+            atomicAdd(done_count, 1);
+        }
+    }
+}
+
+// passes after the Picard loop (also for ssa_iter_max = 0)
+__device__ __noinline__ bool final_passes(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, bool diva,
+                                          int in_alt, bool looped) {
+    double* vcur = in_alt ? I.visc_alt : I.visc;
+    // viscosity of the last linear system (before the last update)
+    const double* vlast = looped ? (in_alt ? I.visc : I.visc_alt) : vcur;
+    double* sdudx = I.lk_x;
+    double* sdudy = I.lk_y;
+    double* sdvdx = I.lr_x;
+    double* sdvdy = I.lr_y;
+    double nlim = count_lim_part(I, P, G, T);
+    if (diva) {
+        phase_diva_final(I, G, T, vlast, vcur);
+    } else {
+        for (int c = T.tid; c < G.n2; c += T.nthr) {
+            // calc_basal_stress, velocity_ssa.f90:588-617
+            double tx = I.bm_x[c] * I.u_x[c], ty = I.bm_y[c] * I.u_y[c];
+            I.taub_x[c] = (fabs(tx) < 1e-5) ? 0.0 : tx;
+            I.taub_y[c] = (fabs(ty) < 1e-5) ? 0.0 : ty;
+        }
+    }
+    if (!team_allreduce(T, &nlim, 1)) return false;
+    if (!diva && P.visc_method == 0) {
+        // diagnose the viscosity of the solution (not used prognostically)
+        phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
+        if (!team_barrier(T)) return false;
+        ygpu_dyn_par P1 = P;
+        P1.visc_method = 1;
+        phase_att_powers(I, P1, G, T);
+        if (!team_barrier(T)) return false;
+        phase_column<double>(I, P1, G, T, vcur, vcur, sdudx, sdudy, sdvdx, sdvdy, false, false, false, false, true);
+        if (!team_barrier(T)) return false;
+    }
+    // the caller's visc_eff must hold the final viscosity
+    if (in_alt) {
+        for (size_t k = T.tid; k < (size_t)G.n2 * G.nz; k += T.nthr) I.visc[k] = I.visc_alt[k];
+    }
+    if (T.cta == 0 && threadIdx.x == 0) I.out->lim_n = (int)nlim;
+    return team_barrier(T);
+}
+
+__device__ __noinline__ void step_post(const Inst& I, const ygpu_dyn_par& P, Team& T, int* done_count, bool final_only) {
+    const bool diva = (I.kind == YGPU_KIND_DIVA);
+    const Geo G = make_geo(I, P);
+    InstOut* out = I.out;
+    const bool lead = (T.cta == 0 && threadIdx.x == 0);
+    PhaseClock clk;
+    clk.start();
+    int status = YGPU_OK;
+    bool finish = final_only;
+    double resid = out->resid;
+    if (!final_only) {
+        double red[4];
+        phase_epilogue(I, P, G, T, diva, red);
+        if (!team_allreduce(T, red, 4)) status = YGPU_ERR_TIMEOUT;
+        resid = (red[2] > 0.0) ? sqrt(red[0]) / (sqrt(red[1]) + 1e-10) : 0.0;
+        if (P.ssa_write_log && lead)
+            printf("ssa: %s %4d %12.4g | lin %6d %d\n", (resid < P.ssa_iter_conv) ? "C" : "", out->iter_now, resid,
+                   out->lin_it, out->lin_st);
+        if (status == YGPU_OK && (red[3] > 0.0 || !isfinite(resid))) status = YGPU_ERR_NONFINITE;
+        finish = (status != YGPU_OK) || resid < P.ssa_iter_conv || out->iter_now >= P.ssa_iter_max;
+    }
+    const double t6 = clk.lap();
+    if (finish && status == YGPU_OK) {
+        if (!final_passes(I, P, G, T, diva, out->in_alt, out->iter_now > 0)) status = YGPU_ERR_TIMEOUT;
+    }
+    const double t7 = clk.lap();
+    if (lead) {
+        if (!final_only) {
+            out->lin_iter += out->lin_it;
+            out->outer_iter += out->lin_outer;
+            if (out->lin_st != YGPU_OK) out->lin_fail++;
+            out->lin_status = out->lin_st;
+            out->lin_resid = out->lin_rr;
+            out->resid = resid;
+        }
+        out->phase_ns[6] += t6;
+        out->phase_ns[7] += t7;
+        if (finish) {
+            out->status = (status != YGPU_OK) ? status : out->lin_status;
+            out->converged = (status == YGPU_OK);
+            out->done = 1;
+            atomicAdd(done_count, 1);
+        }
     }
 }
 
 // ---------------------------------------------------------------------------
-// The persistent kernel: teams take instances from the queue
+// Step kernels: teams of CTAs, instances assigned round-robin in queue order
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_solve_kernel(const Inst* __restrict__ insts, int n_inst,
-                                                              ygpu_dyn_par P, TeamCtl* ctls, int team_ctas,
-                                                              int* queue, int* abort_all) {
+enum { STEP_SETUP = 0, STEP_PRE = 1, STEP_KRYLOV = 2, STEP_POST = 3, STEP_FINAL = 4 };
+
+template <int STEP>
+YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamCtl* ctls, int team_ctas,
+                     int* abort_all, int* done_count) {
     __shared__ Inst sI;
-    __shared__ int s_inst;
+    __shared__ int s_skip;
     Team T;
     T.ncta = team_ctas;
     T.cta = blockIdx.x % team_ctas;
     T.tid = T.cta * blockDim.x + threadIdx.x;
     T.nthr = team_ctas * blockDim.x;
-    T.ctl = ctls + blockIdx.x / team_ctas;
+    const int team = blockIdx.x / team_ctas, n_teams = gridDim.x / team_ctas;
+    T.ctl = ctls + team;
     T.parity = 0;
     T.abort_all = abort_all;
     T.sync_ns = 0.0;
-    T.gen = 0u;
-    for (;;) {
-        if (T.cta == 0 && threadIdx.x == 0) {
-            int k = atomicAdd(queue, 1);
-            if (team_ctas == 1) s_inst = k;
-            else atomicExch(&T.ctl->inst, k);
+    T.gen = (threadIdx.x == 0) ? ld_acquire_u32(&T.ctl->gen) : 0u;
+    for (int q = team; q < n_inst; q += n_teams) {
+        if (threadIdx.x == 0) {
+            sI = insts[q];
+            const int d = sI.out->done;
+            s_skip = (STEP == STEP_SETUP) ? 0 : (d || ld_acquire_s32(abort_all));
         }
-        if (!team_barrier(T)) return;
-        if (threadIdx.x == 0 && team_ctas > 1) s_inst = ld_acquire_s32(&T.ctl->inst);
         __syncthreads();
-        const int k = s_inst;
-        if (k >= n_inst) return;
-        if (threadIdx.x == 0) sI = insts[k];
+        if (!s_skip) {
+            if (STEP == STEP_SETUP) step_setup(sI, P, T, done_count);
+            else if (STEP == STEP_PRE) step_pre(sI, P, T, done_count);
+            else if (STEP == STEP_KRYLOV) step_krylov(sI, P, T, done_count);
+            else step_post(sI, P, T, done_count, STEP == STEP_FINAL);
+            if (T.cta == 0 && threadIdx.x == 0) sI.out->phase_ns[8] += T.sync_ns;
+            T.sync_ns = 0.0;
+        }
         __syncthreads();
-        T.sync_ns = 0.0;
-        solve_instance(sI, P, T);
-        if (!team_barrier(T)) return;
     }
+}
+
+#define YG_KBLOCK 512
+
+__global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_setup(const Inst* insts, int n_inst, ygpu_dyn_par P,
+                                                            TeamCtl* ctls, int tc, int* ab, int* dc) {
+    run_step<STEP_SETUP>(insts, n_inst, P, ctls, tc, ab, dc);
+}
+__global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_pre(const Inst* insts, int n_inst, ygpu_dyn_par P,
+                                                          TeamCtl* ctls, int tc, int* ab, int* dc) {
+    run_step<STEP_PRE>(insts, n_inst, P, ctls, tc, ab, dc);
+}
+__global__ void __launch_bounds__(YG_KBLOCK, 1) ygpu_k_krylov(const Inst* insts, int n_inst, ygpu_dyn_par P,
+                                                              TeamCtl* ctls, int tc, int* ab, int* dc) {
+    run_step<STEP_KRYLOV>(insts, n_inst, P, ctls, tc, ab, dc);
+}
+__global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_post(const Inst* insts, int n_inst, ygpu_dyn_par P,
+                                                           TeamCtl* ctls, int tc, int* ab, int* dc) {
+    run_step<STEP_POST>(insts, n_inst, P, ctls, tc, ab, dc);
+}
+__global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_final(const Inst* insts, int n_inst, ygpu_dyn_par P,
+                                                            TeamCtl* ctls, int tc, int* ab, int* dc) {
+    run_step<STEP_FINAL>(insts, n_inst, P, ctls, tc, ab, dc);
 }
 
 // ---------------------------------------------------------------------------
@@ -1964,8 +2067,28 @@ int ygpu_csr_max_ctas(int device) {
 // ---------------------------------------------------------------------------
 static bool g_gqw_set[64] = {false};
 
+static int max_ctas_of(const void* kern, int block) {
+    int dev = 0, nsm = 0, bps = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, block, 0);
+    return nsm * bps;
+}
+
+static int coop(const void* kern, int grid, int block, cudaStream_t s, const Inst* insts, int n_inst,
+                const ygpu_dyn_par& P, TeamCtl* ctls, int tc, int* ab, int* dc) {
+    void* args[] = {(void*)&insts, (void*)&n_inst, (void*)&P, (void*)&ctls, (void*)&tc, (void*)&ab, (void*)&dc};
+    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), args, 0, s);
+    if (e != cudaSuccess) {
+        ygpu_set_error("cooperative launch of a solver step failed: %s", cudaGetErrorString(e));
+        return YGPU_ERR_CUDA;
+    }
+    return YGPU_OK;
+}
+
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
-                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_queue, int* d_abort) {
+                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_misc, int* d_abort) {
+    // d_misc[0]: count of finished instances; d_abort: launch-wide abort flag
     if (device >= 0 && device < 64 && !g_gqw_set[device]) {
         double w[4][4];
         const int sx[4] = {-1, 1, 1, -1}, sy[4] = {-1, -1, 1, 1};
@@ -1980,24 +2103,69 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
         if (cudaMemcpyToSymbol(c_gqw, w, sizeof(w)) != cudaSuccess) return YGPU_ERR_CUDA;
         g_gqw_set[device] = true;
     }
-    if (cudaMemsetAsync(d_queue, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    if (cudaMemsetAsync(d_misc, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
     if (cudaMemsetAsync(d_abort, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
     if (cudaMemsetAsync(d_ctls, 0, sizeof(TeamCtl) * (size_t)n_teams, stream) != cudaSuccess) return YGPU_ERR_CUDA;
-    void* args[] = {(void*)&d_insts, (void*)&n_inst, (void*)&P, (void*)&d_ctls, (void*)&team_ctas, (void*)&d_queue,
-                    (void*)&d_abort};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)ygpu_solve_kernel, dim3(n_teams * team_ctas),
-                                                dim3(YG_BLOCK), args, 0, stream);
-    if (e != cudaSuccess) {
-        ygpu_set_error("cooperative launch of the solver failed: %s", cudaGetErrorString(e));
+    int* dc = d_misc;
+    // Krylov launch shape: the lean kernel, sized to the largest instance, within
+    // the team control blocks the caller provides (n_teams)
+    static int kmax_dev[64];
+    const int dslot = (device >= 0 && device < 64) ? device : 0;
+    if (kmax_dev[dslot] == 0) kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK);
+    const int kmax = kmax_dev[dslot];
+    if (kmax < 1) {
+        ygpu_set_error("Krylov kernel cannot be resident on device %d", device);
         return YGPU_ERR_CUDA;
     }
+    // Krylov teams: as many CTAs as the heavy teams (each CTA twice the threads),
+    // fewer teams if the lean kernel has fewer resident CTAs
+    int ktc = team_ctas;
+    if (const char* e = getenv("YGPU_KRYLOV_CTAS")) {
+        const int v = atoi(e);
+        if (v > 0) ktc = v;
+    }
+    if (ktc < 1) ktc = 1;
+    if (ktc > kmax) ktc = kmax;
+    int knt = kmax / ktc;
+    if (knt > n_teams) knt = n_teams;
+    const int grid = n_teams * team_ctas;
+    int st;
+    if ((st = coop((const void*)ygpu_k_setup, grid, YG_BLOCK, stream, d_insts, n_inst, P, d_ctls, team_ctas, d_abort, dc)))
+        return st;
+    const int check = 4;
+    for (int it = 0; it < P.ssa_iter_max; it++) {
+        if ((st = coop((const void*)ygpu_k_pre, grid, YG_BLOCK, stream, d_insts, n_inst, P, d_ctls, team_ctas, d_abort, dc)))
+            return st;
+        if ((st = coop((const void*)ygpu_k_krylov, knt * ktc, YG_KBLOCK, stream, d_insts, n_inst, P, d_ctls, ktc,
+                       d_abort, dc)))
+            return st;
+        if ((st = coop((const void*)ygpu_k_post, grid, YG_BLOCK, stream, d_insts, n_inst, P, d_ctls, team_ctas, d_abort, dc)))
+            return st;
+        if ((it + 1) % check == 0 || it + 1 == P.ssa_iter_max) {
+            int h[2] = {0, 0};
+            if (cudaMemcpyAsync(&h[0], dc, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+                cudaMemcpyAsync(&h[1], d_abort, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+                cudaStreamSynchronize(stream) != cudaSuccess) {
+                ygpu_set_error("solver step failed: %s", cudaGetErrorString(cudaGetLastError()));
+                return YGPU_ERR_CUDA;
+            }
+            if (h[0] >= n_inst || h[1]) break;
+        }
+    }
+    // instances not finished by the loop (ssa_iter_max = 0) get their final passes
+    if ((st = coop((const void*)ygpu_k_final, grid, YG_BLOCK, stream, d_insts, n_inst, P, d_ctls, team_ctas, d_abort, dc)))
+        return st;
     return YGPU_OK;
 }
 
 int ygpu_solver_max_ctas(int device) {
-    int nsm = 0, bps = 0;
+    int nsm = 0, bps = 0, b2 = 0, b3 = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ygpu_solve_kernel, YG_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ygpu_k_pre, YG_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, ygpu_k_post, YG_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, ygpu_k_setup, YG_BLOCK, 0);
+    if (b2 < bps) bps = b2;
+    if (b3 < bps) bps = b3;
     return nsm * bps;
 }
 
