@@ -31,6 +31,7 @@
 // 2x2 Gauss-Legendre weights of the bilinear corner interpolation, node q
 // (SW, SE, NE, NW) from corner c (same order); set by the host.
 __constant__ double c_gqw[4][4];
+__constant__ float c_gqwf[4][4];   // the same weights rounded to FP32
 
 static const double TOL_UNDERFLOW = 1e-15;
 #define VISC_MIN 1e5
@@ -58,30 +59,44 @@ YG_DEV Geo make_geo(const Inst& I, const ygpu_dyn_par& P) {
 // ---------------------------------------------------------------------------
 // Quadrature helpers (restated gq2D_to_nodes_*, see the oracle for the rule)
 // ---------------------------------------------------------------------------
-YG_DEV void gq_nodes(const double c[4], double v[4]) {
+template <typename V>
+YG_DEV V gq_weight(int q, int c);
+template <>
+YG_DEV double gq_weight<double>(int q, int c) { return c_gqw[q][c]; }
+template <>
+YG_DEV float gq_weight<float>(int q, int c) { return c_gqwf[q][c]; }
+
+template <typename V>
+YG_DEV void gq_nodes(const V c[4], V v[4]) {
 #pragma unroll
     for (int q = 0; q < 4; q++) {
-        double s = c_gqw[q][0] * c[0];
-        s = s + c_gqw[q][1] * c[1];
-        s = s + c_gqw[q][2] * c[2];
-        s = s + c_gqw[q][3] * c[3];
+        V s = gq_weight<V>(q, 0) * c[0];
+        s = s + gq_weight<V>(q, 1) * c[1];
+        s = s + gq_weight<V>(q, 2) * c[2];
+        s = s + gq_weight<V>(q, 3) * c[3];
         v[q] = s;
     }
 }
 YG_DEV double gq_mean(const double v[4]) { return (((v[0] + v[1]) + v[2]) + v[3]) / 4.0; }
 
-YG_DEV double mean2_act(double a, double b, bool aa, bool ab) {
-    int n = (int)aa + (int)ab;
-    if (n == 0) return 0.0;
-    return ((aa ? a : 0.0) + (ab ? b : 0.0)) / (double)n;
+// Means over the active values. Division by the count 1, 2 or 4 is written as
+// an exact scaling (same result, no division); only a count of 3 divides.
+template <typename V>
+YG_DEV V mean2_act(V a, V b, bool aa, bool ab) {
+    const V s = (aa ? a : V(0)) + (ab ? b : V(0));
+    return (aa && ab) ? s * V(0.5) : s;
 }
-YG_DEV double mean4_act(double a, double b, double c, double d, bool aa, bool ab, bool ac, bool ad) {
+template <typename V>
+YG_DEV V mean4_act(V a, V b, V c, V d, bool aa, bool ab, bool ac, bool ad) {
     int n = (int)aa + (int)ab + (int)ac + (int)ad;
-    if (n == 0) return 0.0;
-    double s = (aa ? a : 0.0) + (ab ? b : 0.0);
-    s = s + (ac ? c : 0.0);
-    s = s + (ad ? d : 0.0);
-    return s / (double)n;
+    if (n == 0) return V(0);
+    V s = (aa ? a : V(0)) + (ab ? b : V(0));
+    s = s + (ac ? c : V(0));
+    s = s + (ad ? d : V(0));
+    if (n == 4) return s * V(0.25);
+    if (n == 2) return s * V(0.5);
+    if (n == 1) return s;
+    return s / V(3);
 }
 
 // neighbourhood of a cell: index of (im1|i|ip1, jm1|j|jp1)
@@ -110,42 +125,42 @@ YG_DEV bool act_y(const Geo& G, const double* f_ice, int i, int j) {
 }
 
 // acx-field to quadrature nodes of cell nb (corner = mean of the acx faces above/below)
-template <typename F>
-YG_DEV void nodes_acx(const Geo& G, const Nb& n, F val, const bool* ax, double v[4]) {
+template <typename F, typename V>
+YG_DEV void nodes_acx(const Geo& G, const Nb& n, F val, const bool* ax, V v[4]) {
     // ax: active flags of faces [im1,jm1],[im1,j],[im1,jp1],[i,jm1],[i,j],[i,jp1]
-    double c[4];
-    double a_im1_jm1 = val(n.im1, n.jm1), a_im1_j = val(n.im1, n.j), a_im1_jp1 = val(n.im1, n.jp1);
-    double a_i_jm1 = val(n.i, n.jm1), a_i_j = val(n.i, n.j), a_i_jp1 = val(n.i, n.jp1);
+    V c[4];
+    V a_im1_jm1 = (V)val(n.im1, n.jm1), a_im1_j = (V)val(n.im1, n.j), a_im1_jp1 = (V)val(n.im1, n.jp1);
+    V a_i_jm1 = (V)val(n.i, n.jm1), a_i_j = (V)val(n.i, n.j), a_i_jp1 = (V)val(n.i, n.jp1);
     if (ax) {
         c[0] = mean2_act(a_im1_jm1, a_im1_j, ax[0], ax[1]);
         c[1] = mean2_act(a_i_jm1, a_i_j, ax[3], ax[4]);
         c[2] = mean2_act(a_i_j, a_i_jp1, ax[4], ax[5]);
         c[3] = mean2_act(a_im1_j, a_im1_jp1, ax[1], ax[2]);
     } else {
-        c[0] = 0.5 * (a_im1_jm1 + a_im1_j);
-        c[1] = 0.5 * (a_i_jm1 + a_i_j);
-        c[2] = 0.5 * (a_i_j + a_i_jp1);
-        c[3] = 0.5 * (a_im1_j + a_im1_jp1);
+        c[0] = V(0.5) * (a_im1_jm1 + a_im1_j);
+        c[1] = V(0.5) * (a_i_jm1 + a_i_j);
+        c[2] = V(0.5) * (a_i_j + a_i_jp1);
+        c[3] = V(0.5) * (a_im1_j + a_im1_jp1);
     }
     gq_nodes(c, v);
 }
 // acy-field to nodes (corner = mean of the acy faces left/right)
-template <typename F>
-YG_DEV void nodes_acy(const Geo& G, const Nb& n, F val, const bool* ay, double v[4]) {
+template <typename F, typename V>
+YG_DEV void nodes_acy(const Geo& G, const Nb& n, F val, const bool* ay, V v[4]) {
     // ay: active flags of faces [im1,jm1],[i,jm1],[ip1,jm1],[im1,j],[i,j],[ip1,j]
-    double c[4];
-    double a_im1_jm1 = val(n.im1, n.jm1), a_i_jm1 = val(n.i, n.jm1), a_ip1_jm1 = val(n.ip1, n.jm1);
-    double a_im1_j = val(n.im1, n.j), a_i_j = val(n.i, n.j), a_ip1_j = val(n.ip1, n.j);
+    V c[4];
+    V a_im1_jm1 = (V)val(n.im1, n.jm1), a_i_jm1 = (V)val(n.i, n.jm1), a_ip1_jm1 = (V)val(n.ip1, n.jm1);
+    V a_im1_j = (V)val(n.im1, n.j), a_i_j = (V)val(n.i, n.j), a_ip1_j = (V)val(n.ip1, n.j);
     if (ay) {
         c[0] = mean2_act(a_im1_jm1, a_i_jm1, ay[0], ay[1]);
         c[1] = mean2_act(a_i_jm1, a_ip1_jm1, ay[1], ay[2]);
         c[2] = mean2_act(a_i_j, a_ip1_j, ay[4], ay[5]);
         c[3] = mean2_act(a_im1_j, a_i_j, ay[3], ay[4]);
     } else {
-        c[0] = 0.5 * (a_im1_jm1 + a_i_jm1);
-        c[1] = 0.5 * (a_i_jm1 + a_ip1_jm1);
-        c[2] = 0.5 * (a_i_j + a_ip1_j);
-        c[3] = 0.5 * (a_im1_j + a_i_j);
+        c[0] = V(0.5) * (a_im1_jm1 + a_i_jm1);
+        c[1] = V(0.5) * (a_i_jm1 + a_ip1_jm1);
+        c[2] = V(0.5) * (a_i_j + a_ip1_j);
+        c[3] = V(0.5) * (a_im1_j + a_i_j);
     }
     gq_nodes(c, v);
 }
@@ -340,10 +355,14 @@ YG_DEV double beta_aa(const Inst& I, const ygpu_dyn_par& P, const Geo& G, int i,
 // ---------------------------------------------------------------------------
 // Phase: A^(-1/n) at the quadrature nodes (once per solve; ATT is constant)
 // ---------------------------------------------------------------------------
+// In the mixed mode the powers are stored as FP32 (attp read as float*); the
+// upper half of the array then holds the FP32 shear copies (shear_f32).
 __device__ __noinline__ void phase_att_powers(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T) {
     const int nz = G.nz, n2 = G.n2;
     const double p2 = -1.0 / I.n_glen;
     const bool glen3 = (I.n_glen == 3.0);
+    const bool f32 = (P.precision == YGPU_PREC_MIXED);
+    float* af = (float*)I.attp;
     for (int c = T.tid; c < n2; c += T.nthr) {
         Nb n = make_nb(G, c);
         for (int k = 0; k < nz; k++) {
@@ -352,11 +371,17 @@ __device__ __noinline__ void phase_att_powers(const Inst& I, const ygpu_dyn_par&
                 auto att = [&](int a, int b) { return I.ATT[(size_t)k * n2 + CI(a, b)]; };
                 nodes_aa(G, n, att, [](int, int) { return true; }, false, attn);
 #pragma unroll
-                for (int q = 0; q < 4; q++)
-                    I.attp[((size_t)q * nz + k) * n2 + c] = glen3 ? rcbrt(attn[q]) : pow(attn[q], p2);
+                for (int q = 0; q < 4; q++) {
+                    const double v = glen3 ? rcbrt(attn[q]) : pow(attn[q], p2);
+                    const size_t o = ((size_t)q * nz + k) * n2 + c;
+                    if (f32) af[o] = (float)v;
+                    else I.attp[o] = v;
+                }
             } else {
                 const double a = I.ATT[(size_t)k * n2 + c];
-                I.attp[(size_t)k * n2 + c] = glen3 ? rcbrt(a) : pow(a, p2);
+                const double v = glen3 ? rcbrt(a) : pow(a, p2);
+                if (f32) af[(size_t)k * n2 + c] = (float)v;
+                else I.attp[(size_t)k * n2 + c] = v;
             }
         }
     }
@@ -367,21 +392,39 @@ __device__ __noinline__ void phase_att_powers(const Inst& I, const ygpu_dyn_par&
 // stress and the viscosity at the start of the iteration
 // (calc_vertical_shear_3D, velocity_diva.f90:510-571)
 // ---------------------------------------------------------------------------
+// FP32 copies of the shear (mixed mode): the upper half of the attp array
+YG_DEV float* shear_f32(const Inst& I, int axis) {
+    const size_t n3 = (size_t)I.nz * I.n2;
+    return (float*)I.attp + (4 + axis) * n3;
+}
+
+// R = float (mixed mode): FP32 arithmetic, the FP64 output plus an FP32 copy
+// that the column pass reads
+template <typename R>
 __device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, const double* vcur) {
     const int nz = G.nz, n2 = G.n2;
     const double* f = I.f_ice;
+    float* sx32 = shear_f32(I, 0);
+    float* sy32 = shear_f32(I, 1);
     for (int c = T.tid; c < n2; c += T.nthr) {
         Nb n = make_nb(G, c);
         const int cx = CI(n.ip1, n.j), cy = CI(n.i, n.jp1);
-        const double tx = I.taub_x[c], ty = I.taub_y[c];
+        const R tx = (R)I.taub_x[c], ty = (R)I.taub_y[c];
         const double fc = f[c], fx = f[cx], fy = f[cy];
         for (int k = 0; k < nz; k++) {
             const size_t o = (size_t)k * n2;
-            const double omz = 1.0 - I.zeta[k];
-            double va = stag_margin(vcur[o + c], vcur[o + cx], fc, fx);
-            I.duxdz[o + c] = (va != 0.0) ? (tx / va) * omz : 0.0;
-            va = stag_margin(vcur[o + c], vcur[o + cy], fc, fy);
-            I.duydz[o + c] = (va != 0.0) ? (ty / va) * omz : 0.0;
+            const R omz = (R)(1.0 - I.zeta[k]);
+            const R vc = (R)vcur[o + c];
+            R va = stag_margin<R>(vc, (R)vcur[o + cx], fc, fx);
+            const R gx = (va != R(0)) ? (tx / va) * omz : R(0);
+            va = stag_margin<R>(vc, (R)vcur[o + cy], fc, fy);
+            const R gy = (va != R(0)) ? (ty / va) * omz : R(0);
+            I.duxdz[o + c] = (double)gx;
+            I.duydz[o + c] = (double)gy;
+            if (sizeof(R) == sizeof(float)) {
+                sx32[o + c] = (float)gx;
+                sy32[o + c] = (float)gy;
+            }
         }
     }
 }
@@ -403,6 +446,8 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
     const double* zeta = I.zeta;
     const double* f = I.f_ice;
     const int vm = P.visc_method;
+    // A^(-1/n) at the nodes: FP32 storage in the mixed mode
+    const R* attp_r = (const R*)I.attp;
     for (int c = T.tid; c < n2; c += T.nthr) {
         Nb n = make_nb(G, c);
         if (first_copy) {
@@ -424,15 +469,10 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
             ax[3] = act_x(G, f, n.i, n.jm1); ax[4] = act_x(G, f, n.i, n.j); ax[5] = act_x(G, f, n.i, n.jp1);
             ay[0] = act_y(G, f, n.im1, n.jm1); ay[1] = act_y(G, f, n.i, n.jm1); ay[2] = act_y(G, f, n.ip1, n.jm1);
             ay[3] = act_y(G, f, n.im1, n.j); ay[4] = act_y(G, f, n.i, n.j); ay[5] = act_y(G, f, n.ip1, n.j);
-            double t4[4];
-            nodes_acx(G, n, [&](int a, int b) { return sdudx[CI(a, b)]; }, ax, t4);
-            for (int q = 0; q < 4; q++) dudxn[q] = (R)t4[q];
-            nodes_acx(G, n, [&](int a, int b) { return sdudy[CI(a, b)]; }, ax, t4);
-            for (int q = 0; q < 4; q++) dudyn[q] = (R)t4[q];
-            nodes_acy(G, n, [&](int a, int b) { return sdvdx[CI(a, b)]; }, ay, t4);
-            for (int q = 0; q < 4; q++) dvdxn[q] = (R)t4[q];
-            nodes_acy(G, n, [&](int a, int b) { return sdvdy[CI(a, b)]; }, ay, t4);
-            for (int q = 0; q < 4; q++) dvdyn[q] = (R)t4[q];
+            nodes_acx(G, n, [&](int a, int b) { return sdudx[CI(a, b)]; }, ax, dudxn);
+            nodes_acx(G, n, [&](int a, int b) { return sdudy[CI(a, b)]; }, ax, dudyn);
+            nodes_acy(G, n, [&](int a, int b) { return sdvdx[CI(a, b)]; }, ay, dvdxn);
+            nodes_acy(G, n, [&](int a, int b) { return sdvdy[CI(a, b)]; }, ay, dvdyn);
         } else if (ice && vm == 2) {
             const double* ux = I.u_x;
             const double* uy = I.u_y;
@@ -451,7 +491,8 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
             e = e + 0.25 * (sh * sh);
             e_aa = (R)e;
         }
-        double vint = 0.0, f2 = 0.0, vprev = 0.0, gprev = 0.0;
+        R vint = R(0), f2 = R(0), vprev = R(0), gprev = R(0);
+        const R Hr = (R)Hc;
         for (int k = 0; k < nz; k++) {
             const size_t ck = (size_t)k * n2 + c;
             R v;
@@ -462,13 +503,13 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
             } else if (vm == 1) {
                 R dudzn[4], dvdzn[4], vn[4];
                 if (diva) {
-                    double t4[4];
-                    const double* dz = I.duxdz + (size_t)k * n2;
-                    nodes_acx(G, n, [&](int a, int b) { return dz[CI(a, b)]; }, ax, t4);
-                    for (int q = 0; q < 4; q++) dudzn[q] = (R)t4[q];
-                    const double* dzy = I.duydz + (size_t)k * n2;
-                    nodes_acy(G, n, [&](int a, int b) { return dzy[CI(a, b)]; }, ay, t4);
-                    for (int q = 0; q < 4; q++) dvdzn[q] = (R)t4[q];
+                    // FP64 mode: the FP64 shear; mixed mode: its FP32 copy
+                    const R* dz = (sizeof(R) == sizeof(float)) ? (const R*)shear_f32(I, 0) : (const R*)I.duxdz;
+                    const R* dzy = (sizeof(R) == sizeof(float)) ? (const R*)shear_f32(I, 1) : (const R*)I.duydz;
+                    dz += (size_t)k * n2;
+                    dzy += (size_t)k * n2;
+                    nodes_acx(G, n, [&](int a, int b) { return dz[CI(a, b)]; }, ax, dudzn);
+                    nodes_acy(G, n, [&](int a, int b) { return dzy[CI(a, b)]; }, ay, dvdzn);
                 }
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
@@ -482,7 +523,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                     }
                     e = e + eps0sq;
                     R ep = glen3 ? rcbrt(e) : pow(e, p1);
-                    vn[q] = R(0.5) * ep * (R)I.attp[((size_t)q * nz + k) * n2 + c];
+                    vn[q] = R(0.5) * ep * attp_r[((size_t)q * nz + k) * n2 + c];
                 }
                 v = (((vn[0] + vn[1]) + vn[2]) + vn[3]) / R(4);
             } else {
@@ -497,12 +538,12 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                 }
                 e = e + eps0sq;
                 R ep = glen3 ? rcbrt(e) : pow(e, p1);
-                v = R(0.5) * ep * (R)I.attp[ck];
+                v = R(0.5) * ep * attp_r[ck];
             }
             double vd;
             if (relax) {
                 // picard_relax_visc in log space; log of the current viscosity carried between iterations
-                const R lc = have_log ? (R)I.lvis[ck] : (R)log(vcur[ck]);
+                const R lc = have_log ? (R)I.lvis[ck] : log((R)vcur[ck]);
                 const R L = (R(1) - rel) * lc + rel * log(v);
                 vd = (double)exp(L);
                 I.lvis[ck] = (double)L;
@@ -511,24 +552,26 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                 if (!visc_only) I.lvis[ck] = log(vd);
             }
             vnew[ck] = vd;
-            // trapezoid integrals (integrate_trapezoid1D_pt, yelmo_tools.f90:1092-1122)
-            const double omz = 1.0 - zeta[k];
-            const double g = (Hc / vd) * (omz * omz);
+            // trapezoid integrals (integrate_trapezoid1D_pt, yelmo_tools.f90:1092-1122),
+            // in the viscosity arithmetic R
+            const R vr = (R)vd;
+            const R omz = (R)(1.0 - zeta[k]);
+            const R g = (Hr / vr) * (omz * omz);
             if (k > 0) {
-                const double dzt = zeta[k] - zeta[k - 1];
-                vint = vint + 0.5 * (vd + vprev) * dzt;
-                f2 = f2 + 0.5 * (g + gprev) * dzt;
+                const R dzt = (R)(zeta[k] - zeta[k - 1]);
+                vint = vint + R(0.5) * (vr + vprev) * dzt;
+                f2 = f2 + R(0.5) * (g + gprev) * dzt;
             }
-            vprev = vd;
+            vprev = vr;
             gprev = g;
         }
         if (visc_only) continue;
         // calc_visc_eff_int, velocity_general.f90:2215-2261
-        double vi = ice ? vint * Hc : VISC_MIN;
+        double vi = ice ? (double)vint * Hc : VISC_MIN;
         if (vi < VISC_MIN) vi = VISC_MIN;
         I.visc_int[c] = vi;
         // calc_F_integral (n = 2), velocity_diva.f90:824-869
-        if (diva) I.F2[c] = ice ? f2 : 0.0;
+        if (diva) I.F2[c] = ice ? (double)f2 : 0.0;
         // calc_beta: SSA uses the iterate, DIVA the basal velocity
         if (P.beta_method != -1) {
             const double* ubx = diva ? I.ux_b : I.u_x;
@@ -842,7 +885,10 @@ YG_DEV T energy_row_fast(const Geo& G, const CT* N, const CT* Nab, const CT* dgx
 template <typename T, typename CT>
 YG_DEV T energy_row(const Inst& I, const Geo& G, const CT* N, const CT* Nab, const CT* dgx, const CT* dgy,
                     const T* v, int u) {
-    if (I.rpart[u] == 1) return energy_row_fast<T, CT>(G, N, Nab, dgx, dgy, v, u);
+    // the interior stencil is evaluated for every row (its neighbour indices are
+    // always in range), so its loads do not wait on the row-kind load
+    const T yf = energy_row_fast<T, CT>(G, N, Nab, dgx, dgy, v, u);
+    if (I.rpart[u] == 1) return yf;
     if (I.ukind[u] != DOF_FREE) return v[u];
     const int* emap = I.emap;
     auto val = [&](int d) -> T {
@@ -964,8 +1010,21 @@ struct StencilOp {
     bool energy;
     const CT *N, *Nab, *dgx, *dgy;
     YG_DEV T row(int u, const T* v) const { return operator_row<T, CT>(*I, *G, energy, N, Nab, dgx, dgy, v, u); }
+    // FP32: two rows per thread and trip, both rows' loads issued before either store
     YG_DEV void operator()(Team& Tm, const T* v, T* y) const {
-        for (int u = Tm.tid; u < G->nu; u += Tm.nthr) y[u] = row(u, v);
+        const int nu = G->nu;
+        if (sizeof(T) != sizeof(float)) {
+            for (int k = Tm.tid; k < nu; k += Tm.nthr) y[k] = row(k, v);
+            return;
+        }
+        for (int k0 = Tm.tid; k0 < nu; k0 += 2 * Tm.nthr) {
+            const int k1 = k0 + Tm.nthr;
+            const bool h1 = k1 < nu;
+            const T y0 = row(k0, v);
+            const T y1 = row(h1 ? k1 : k0, v);
+            y[k0] = y0;
+            if (h1) y[k1] = y1;
+        }
     }
 };
 
@@ -1297,10 +1356,18 @@ __device__ __noinline__ int krylov_cg(Team& Tm, int nu, const Op& A, const CT* d
 // the tolerance; if the true residual is above it, the recursion restarts from
 // the true residual.
 template <typename T, typename Op, typename CT>
-__device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const CT* dinv, T* x, const T* b, T* r,
-                                            T* u, T* w, T* m0, T* m1, T* z, T* q, T* s, T* p, int maxiter,
+__device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const CT* __restrict__ dinv,
+                                            T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
+                                            T* __restrict__ u, T* __restrict__ w, T* m0, T* m1, T* __restrict__ z,
+                                            T* __restrict__ q, T* __restrict__ s, T* __restrict__ p, int maxiter,
                                             double tol, double bnrm, bool precond, int& iters, double& relres,
                                             bool& ok) {
+    // Scalar recurrences run on one thread per CTA and are broadcast through
+    // shared memory: FP64 division and square root are slow on this part, and
+    // every thread of the team would otherwise repeat them.
+    __shared__ double s_ab[3];     // alpha, beta, relres
+    __shared__ int s_flag;         // 0 continue, 1 converged, 2 breakdown
+    const bool lead = (threadIdx.x == 0);
     ok = true;
     iters = 0;
     auto Mi = [&](int k) -> T { return precond ? (T)dinv[k] : T(1); };
@@ -1313,63 +1380,126 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             u[k] = Mi(k) * rk;
         }
         if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
-        // w = A u; partial dots; m = M w
-        double red[3] = {0.0, 0.0, 0.0};
+        // w = A u; partial dots; m = M w. Per-thread partial sums in the working
+        // precision (FP32 accumulation in the inner solve of the mixed mode),
+        // combined across the team in FP64.
+        T a0 = T(0), a1 = T(0), a2 = T(0);
         for (int k = Tm.tid; k < nu; k += Tm.nthr) {
             T wk = A.row(k, u);
             w[k] = wk;
             const T mk = Mi(k) * wk;
             m0[k] = mk;
             z[k] = T(0); q[k] = T(0); s[k] = T(0); p[k] = T(0);
-            red[0] += (double)r[k] * (double)u[k];
-            red[1] += (double)wk * (double)u[k];
-            red[2] += (double)r[k] * (double)r[k];
+            const T rk = r[k], uk = u[k];
+            a0 += rk * uk;
+            a1 += wk * uk;
+            a2 += rk * rk;
         }
+        double red[3] = {(double)a0, (double)a1, (double)a2};
         if (!(ok = team_allreduce(Tm, red, 3))) return YGPU_ERR_TIMEOUT;
-        relres = sqrt(red[2]) / bnrm;
-        if (relres <= tol) { iters = it; return YGPU_OK; }
+        // lead thread: gam_old / alpha_old of the recurrence
         double gam_old = 1.0, alpha_old = 1.0;
+        if (lead) {
+            const double rel = sqrt(red[2]) / bnrm;
+            s_ab[2] = rel;
+            if (rel <= tol) s_flag = 1;
+            else {
+                const double gam = red[0], del = red[1];
+                const double alpha = gam / del;
+                if (!isfinite(alpha) || del == 0.0) s_flag = 2;
+                else {
+                    s_flag = 0;
+                    s_ab[0] = alpha;
+                    s_ab[1] = 0.0;
+                    gam_old = gam;
+                    alpha_old = alpha;
+                }
+            }
+        }
+        __syncthreads();
+        relres = s_ab[2];
+        if (s_flag == 1) { iters = it; return YGPU_OK; }
+        if (s_flag == 2) { iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
         T* mc = m0;
         T* mn = m1;
-        bool first = true;
         bool recheck = false;
         while (it < maxiter) {
-            const double gam = red[0], del = red[1];
-            double beta, alpha;
-            if (first) { beta = 0.0; alpha = gam / del; }
-            else {
-                beta = gam / gam_old;
-                alpha = gam / (del - beta * gam / alpha_old);
-            }
-            if (!isfinite(alpha) || !isfinite(beta) || del == 0.0) { iters = it; return YGPU_BREAKDOWN; }
-            first = false;
-            gam_old = gam;
-            alpha_old = alpha;
-            const T a = (T)alpha, bt = (T)beta;
-            red[0] = red[1] = red[2] = 0.0;
-            for (int k = Tm.tid; k < nu; k += Tm.nthr) {
-                const T nk = A.row(k, mc);
-                const T zk = nk + bt * z[k];
-                const T qk = mc[k] + bt * q[k];
-                const T sk = w[k] + bt * s[k];
-                const T pk = u[k] + bt * p[k];
+            const T a = (T)s_ab[0], bt = (T)s_ab[1];
+            a0 = a1 = a2 = T(0);
+            // one row's loads (operator row, nine vectors, preconditioner)
+            struct RowIn { T n, m, z, q, s, p, x, r, u, w, mi; };
+            auto load = [&](int k) {
+                RowIn R;
+                R.n = A.row(k, mc);
+                R.m = mc[k]; R.z = z[k]; R.q = q[k]; R.s = s[k]; R.p = p[k];
+                R.x = x[k]; R.r = r[k]; R.u = u[k]; R.w = w[k]; R.mi = Mi(k);
+                return R;
+            };
+            auto update = [&](int k, const RowIn& R) {
+                const T zk = R.n + bt * R.z;
+                const T qk = R.m + bt * R.q;
+                const T sk = R.w + bt * R.s;
+                const T pk = R.u + bt * R.p;
                 z[k] = zk; q[k] = qk; s[k] = sk; p[k] = pk;
-                x[k] = x[k] + a * pk;
-                const T rk = r[k] - a * sk;
-                const T uk = u[k] - a * qk;
-                const T wk = w[k] - a * zk;
+                x[k] = R.x + a * pk;
+                const T rk = R.r - a * sk;
+                const T uk = R.u - a * qk;
+                const T wk = R.w - a * zk;
                 r[k] = rk; u[k] = uk; w[k] = wk;
-                mn[k] = Mi(k) * wk;
-                red[0] += (double)rk * (double)uk;
-                red[1] += (double)wk * (double)uk;
-                red[2] += (double)rk * (double)rk;
+                mn[k] = R.mi * wk;
+                a0 += rk * uk;
+                a1 += wk * uk;
+                a2 += rk * rk;
+            };
+            if (sizeof(T) == sizeof(float)) {
+                // FP32: two rows per thread and trip, both rows' loads before
+                // either row's stores (FP64 keeps one row: register budget)
+                for (int k0 = Tm.tid; k0 < nu; k0 += 2 * Tm.nthr) {
+                    const int k1 = k0 + Tm.nthr;
+                    const bool h1 = k1 < nu;
+                    const RowIn R0 = load(k0);
+                    const RowIn R1 = load(h1 ? k1 : k0);
+                    update(k0, R0);
+                    if (h1) update(k1, R1);
+                }
+            } else {
+                for (int k = Tm.tid; k < nu; k += Tm.nthr) update(k, load(k));
             }
             it++;
+            red[0] = (double)a0; red[1] = (double)a1; red[2] = (double)a2;
             if (!(ok = team_allreduce(Tm, red, 3))) return YGPU_ERR_TIMEOUT;
             { T* t = mc; mc = mn; mn = t; }
-            relres = sqrt(red[2]) / bnrm;
-            if (!isfinite(relres)) { iters = it; return YGPU_BREAKDOWN; }
-            if (relres <= tol) { recheck = true; break; }
+            if (lead) {
+                const double rel = sqrt(red[2]) / bnrm;
+                s_ab[2] = rel;
+                if (!isfinite(rel)) s_flag = 2;
+                else if (rel <= tol) s_flag = 1;
+                else {
+                    const double gam = red[0], del = red[1];
+                    const double beta = gam / gam_old;
+                    const double alpha = gam / (del - beta * gam / alpha_old);
+                    if (!isfinite(alpha) || !isfinite(beta) || del == 0.0) s_flag = 3;
+                    else {
+                        s_flag = 0;
+                        s_ab[0] = alpha;
+                        s_ab[1] = beta;
+                        gam_old = gam;
+                        alpha_old = alpha;
+                    }
+                }
+            }
+            __syncthreads();
+            // s_flag / s_ab are rewritten only after the next all-reduce's first
+            // __syncthreads, so every thread has read them by then
+            const int flag = s_flag;
+            relres = s_ab[2];
+            if (flag == 2) { iters = it; return YGPU_BREAKDOWN; }
+            if (flag == 1) { recheck = true; break; }
+            if (flag == 3) {
+                // the next iteration's coefficients broke down
+                if (it < maxiter) { iters = it; return YGPU_BREAKDOWN; }
+                break;
+            }
         }
         iters = it;
         if (!recheck) return YGPU_MAXITER;
@@ -1387,80 +1517,135 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
     return YGPU_MAXITER;
 }
 
-// BiCGSTAB with Jacobi (van der Vorst 1992, as in the oracle)
+// BiCGSTAB with Jacobi (van der Vorst 1992, as in the oracle). The scalar
+// recurrences run on one thread per CTA and are broadcast through shared
+// memory (see krylov_pcg_pipe).
 template <typename T, typename Op, typename CT>
-__device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const CT* dinv, T* x, const T* b, T* r, T* rt, T* p, T* v,
-                           T* s, T* t, T* ph, T* sh, int maxiter, double tol, double bnrm, bool precond, int& iters,
-                           double& relres, bool& ok) {
+__device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const CT* __restrict__ dinv,
+                                            T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
+                                            T* __restrict__ rt, T* __restrict__ p, T* v, T* __restrict__ s, T* t,
+                                            T* ph, T* sh, int maxiter, double tol, double bnrm, bool precond,
+                                            int& iters, double& relres, bool& ok) {
+    __shared__ double s_sc[4];     // alpha, omega, beta, relres
+    __shared__ int s_flag;         // 0 continue, 1 converged, 2 breakdown
+    const bool lead = (threadIdx.x == 0);
     ok = true;
     iters = 0;
     A(Tm, x, v);
-    double red[2] = {0.0, 0.0};
+    T a0 = T(0);
     for (int u = Tm.tid; u < nu; u += Tm.nthr) {
         T ru = b[u] - v[u];
         r[u] = ru;
         rt[u] = ru;
         p[u] = T(0);
-        red[0] += (double)ru * (double)ru;
+        a0 += ru * ru;
     }
+    double red[2] = {(double)a0, 0.0};
     if (!(ok = team_allreduce(Tm, red, 1))) return YGPU_ERR_TIMEOUT;
-    relres = sqrt(red[0]) / bnrm;
-    if (relres <= tol) return YGPU_OK;
-    double rho = red[0];     // (rt, r) with rt = r
-    double rho_old = 1.0, alpha = 1.0, omega = 1.0;
+    // lead-thread state of the recurrence
+    double rho = red[0], rho_old = 1.0, alpha = 1.0, omega = 1.0;     // (rt, r) with rt = r
+    if (lead) {
+        s_sc[3] = sqrt(red[0]) / bnrm;
+        s_flag = (s_sc[3] <= tol) ? 1 : 0;
+    }
+    __syncthreads();
+    relres = s_sc[3];
+    if (s_flag == 1) return YGPU_OK;
     for (int it = 1; it <= maxiter; it++) {
         iters = it;
-        if (rho == 0.0 || !isfinite(rho)) return YGPU_BREAKDOWN;
-        const double beta = (it == 1) ? 0.0 : (rho / rho_old) * (alpha / omega);
-        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
-            T pu = (it == 1) ? r[u] : r[u] + (T)beta * (p[u] - (T)omega * v[u]);
-            p[u] = pu;
-            ph[u] = precond ? (T)dinv[u] * pu : pu;
+        __syncthreads();           // every thread has read the previous s_flag / s_sc[3]
+        if (lead) {
+            s_flag = (rho == 0.0 || !isfinite(rho)) ? 2 : 0;
+            s_sc[2] = (it == 1) ? 0.0 : (rho / rho_old) * (alpha / omega);
+            s_sc[1] = omega;
+        }
+        __syncthreads();
+        if (s_flag == 2) return YGPU_BREAKDOWN;
+        {
+            const T beta = (T)s_sc[2], om = (T)s_sc[1];
+            for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+                T pu = (it == 1) ? r[u] : r[u] + beta * (p[u] - om * v[u]);
+                p[u] = pu;
+                ph[u] = precond ? (T)dinv[u] * pu : pu;
+            }
         }
         if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
         A(Tm, ph, v);
-        double tv = 0.0;
-        for (int u = Tm.tid; u < nu; u += Tm.nthr) tv += (double)rt[u] * (double)v[u];
+        T tvp = T(0);
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) tvp += rt[u] * v[u];
+        double tv = (double)tvp;
         if (!(ok = team_allreduce(Tm, &tv, 1))) return YGPU_ERR_TIMEOUT;
-        if (tv == 0.0 || !isfinite(tv)) return YGPU_BREAKDOWN;
-        alpha = rho / tv;
-        double ss = 0.0;
+        if (lead) {
+            if (tv == 0.0 || !isfinite(tv)) s_flag = 2;
+            else {
+                alpha = rho / tv;
+                s_sc[0] = alpha;
+                s_flag = 0;
+            }
+        }
+        __syncthreads();
+        if (s_flag == 2) return YGPU_BREAKDOWN;
+        const T al = (T)s_sc[0];
+        T ssp = T(0);
         for (int u = Tm.tid; u < nu; u += Tm.nthr) {
-            T su = r[u] - (T)alpha * v[u];
+            T su = r[u] - al * v[u];
             s[u] = su;
             sh[u] = precond ? (T)dinv[u] * su : su;
-            ss += (double)su * (double)su;
+            ssp += su * su;
         }
+        double ss = (double)ssp;
         if (!(ok = team_allreduce(Tm, &ss, 1))) return YGPU_ERR_TIMEOUT;
-        if (sqrt(ss) / bnrm <= tol) {
-            for (int u = Tm.tid; u < nu; u += Tm.nthr) x[u] = x[u] + (T)alpha * ph[u];
-            relres = sqrt(ss) / bnrm;
+        if (lead) {
+            s_sc[3] = sqrt(ss) / bnrm;
+            s_flag = (s_sc[3] <= tol) ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_flag == 1) {
+            relres = s_sc[3];
+            for (int u = Tm.tid; u < nu; u += Tm.nthr) x[u] = x[u] + al * ph[u];
             if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
             return YGPU_OK;
         }
         A(Tm, sh, t);
-        double ts[2] = {0.0, 0.0};
+        T ts0 = T(0), ts1 = T(0);
         for (int u = Tm.tid; u < nu; u += Tm.nthr) {
-            ts[0] += (double)t[u] * (double)s[u];
-            ts[1] += (double)t[u] * (double)t[u];
+            const T tu = t[u];
+            ts0 += tu * s[u];
+            ts1 += tu * tu;
         }
+        double ts[2] = {(double)ts0, (double)ts1};
         if (!(ok = team_allreduce(Tm, ts, 2))) return YGPU_ERR_TIMEOUT;
-        if (ts[1] == 0.0 || !isfinite(ts[1])) return YGPU_BREAKDOWN;
-        omega = ts[0] / ts[1];
-        double rr[2] = {0.0, 0.0};
-        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
-            x[u] = x[u] + (T)alpha * ph[u] + (T)omega * sh[u];
-            T ru = s[u] - (T)omega * t[u];
-            r[u] = ru;
-            rr[0] += (double)ru * (double)ru;
-            rr[1] += (double)rt[u] * (double)ru;
+        if (lead) {
+            if (ts[1] == 0.0 || !isfinite(ts[1])) s_flag = 2;
+            else {
+                omega = ts[0] / ts[1];
+                s_sc[1] = omega;
+                s_flag = 0;
+            }
         }
+        __syncthreads();
+        if (s_flag == 2) return YGPU_BREAKDOWN;
+        const T om = (T)s_sc[1];
+        T rr0 = T(0), rr1 = T(0);
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+            x[u] = x[u] + al * ph[u] + om * sh[u];
+            T ru = s[u] - om * t[u];
+            r[u] = ru;
+            rr0 += ru * ru;
+            rr1 += rt[u] * ru;
+        }
+        double rr[2] = {(double)rr0, (double)rr1};
         if (!(ok = team_allreduce(Tm, rr, 2))) return YGPU_ERR_TIMEOUT;
-        relres = sqrt(rr[0]) / bnrm;
-        if (relres <= tol) return YGPU_OK;
-        if (omega == 0.0) return YGPU_BREAKDOWN;
-        rho_old = rho;
-        rho = rr[1];
+        if (lead) {
+            s_sc[3] = sqrt(rr[0]) / bnrm;
+            s_flag = (s_sc[3] <= tol) ? 1 : ((omega == 0.0) ? 2 : 0);
+            rho_old = rho;
+            rho = rr[1];
+        }
+        __syncthreads();
+        relres = s_sc[3];
+        if (s_flag == 1) return YGPU_OK;
+        if (s_flag == 2) return YGPU_BREAKDOWN;
     }
     return YGPU_MAXITER;
 }
@@ -1512,7 +1697,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         if (relres <= P.lin_tol) { status = YGPU_OK; break; }
         if (total >= P.lin_maxiter) { status = YGPU_MAXITER; break; }
         // inner FP32 solve of A d = r, d0 = 0, scaled by ||r||
-        const double sc = 1.0 / sqrt(rr);
+        const double nr = sqrt(rr), sc = 1.0 / nr;
         for (int u = T.tid; u < G.nu; u += T.nthr) {
             I.fr[u] = (float)(I.r[u] * sc);
             I.fx[u] = 0.0f;
@@ -1531,7 +1716,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         total += it;
         outer++;
         // x += d (FP64 accumulation)
-        for (int u = T.tid; u < G.nu; u += T.nthr) I.x[u] = I.x[u] + (double)I.fx[u] / sc;
+        for (int u = T.tid; u < G.nu; u += T.nthr) I.x[u] = I.x[u] + (double)I.fx[u] * nr;
         if (!(ok = team_barrier(T))) return YGPU_ERR_TIMEOUT;
         if (st == YGPU_BREAKDOWN && it <= 1) { status = YGPU_BREAKDOWN; break; }
     }
@@ -1748,7 +1933,10 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
     double bn2 = 0.0;
     if (P.visc_method == 1 || diva) {
         if (P.visc_method == 1) phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
-        if (diva) phase_shear(I, G, T, vcur);
+        if (diva) {
+            if (P.precision == YGPU_PREC_MIXED) phase_shear<float>(I, G, T, vcur);
+            else phase_shear<double>(I, G, T, vcur);
+        }
         if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
     }
     t1 = clk.lap();
@@ -1843,6 +2031,7 @@ __device__ __noinline__ bool final_passes(const Inst& I, const ygpu_dyn_par& P, 
         if (!team_barrier(T)) return false;
         ygpu_dyn_par P1 = P;
         P1.visc_method = 1;
+        P1.precision = YGPU_PREC_FP64;     // the diagnostic pass reads FP64 powers
         phase_att_powers(I, P1, G, T);
         if (!team_barrier(T)) return false;
         phase_column<double>(I, P1, G, T, vcur, vcur, sdudx, sdudy, sdvdx, sdvdy, false, false, false, false, true);
@@ -2100,7 +2289,11 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
                 volatile double pr = ax * ay;
                 w[q][c] = pr * 0.25;
             }
+        float wf[4][4];
+        for (int q = 0; q < 4; q++)
+            for (int c = 0; c < 4; c++) wf[q][c] = (float)w[q][c];
         if (cudaMemcpyToSymbol(c_gqw, w, sizeof(w)) != cudaSuccess) return YGPU_ERR_CUDA;
+        if (cudaMemcpyToSymbol(c_gqwf, wf, sizeof(wf)) != cudaSuccess) return YGPU_ERR_CUDA;
         g_gqw_set[device] = true;
     }
     if (cudaMemsetAsync(d_misc, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
