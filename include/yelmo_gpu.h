@@ -308,6 +308,83 @@ int ygpu_solve_batch_device(ygpu_ctx* ctx, int kind, const ygpu_dyn_par* par,
 int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, const ygpu_fields* f,
                               ygpu_stats* stats, void* stream);
 
+/* ======================================================================== */
+/* Serving: velocity-solve requests from many ensemble members.              */
+/* ======================================================================== */
+/*
+ * No counterpart in the reference, which solves one domain per call
+ * (calc_ydyn -> calc_velocity_*, src/yelmo_dynamics.f90:415,544). A server
+ * keeps the state of every registered member on the device (thickness, bed,
+ * friction, rate factor, viscosity and the previous velocity) and solves the
+ * requests it is sent with continuous batching: a loop on a host thread runs
+ * one Picard iteration of every solve on the GPU per tick (the pre / Krylov /
+ * post step kernels over all of them), retires the solves that converged and
+ * admits waiting requests into the freed slots between ticks, so requests that
+ * arrive while others are on the GPU join them at the next tick.
+ *
+ * A request advances its member by one step: H_ice += dH where H_ice > 0
+ * (dH ~ N(0, dH_sigma^2) per cell, drawn from (seed, member, step) with a
+ * counter-based generator and clamped at 0), rebuilds the inputs of the solve
+ * on the device (ygpu_calc_dyn_inputs, ygpu_set_ssa_masks) and solves warm
+ * from the member's previous velocity and viscosity. Requests of one member
+ * run in submission order, one at a time.
+ *
+ * Admission by device memory: the server never holds more than hbm_budget
+ * bytes. A member that does not fit is refused (YGPU_ERR_ADMISSION); a request
+ * waits until a slot (the scratch of one solve, sized for the largest member)
+ * is free or can be allocated within the budget.
+ */
+typedef struct ygpu_server ygpu_server;
+
+typedef struct ygpu_server_cfg {
+    int    device;              /* CUDA device                                   */
+    int    kind;                /* YGPU_KIND_SSA or YGPU_KIND_DIVA               */
+    ygpu_dyn_par par;           /* solver parameters of every request            */
+    double grad_lim;            /* surface-gradient limit (ytopo grad_lim)       */
+    double taud_lim;            /* driving-stress clamp (Pa)                     */
+    int    lateral_bc;          /* YGPU_LATBC_*                                  */
+    double dH_sigma;            /* standard deviation of the per-step dH (m)     */
+    unsigned long long hbm_budget; /* device bytes the server may hold         */
+    int    max_slots;           /* solves on the GPU at once (0: one per SM)     */
+} ygpu_server_cfg;
+
+typedef struct ygpu_server_info {
+    int    members, slots, active, pending;
+    long long ticks, completed;
+    unsigned long long bytes_held;
+} ygpu_server_info;
+
+/* fields for ygpu_server_fetch */
+#define YGPU_SRV_UX    0        /* solve velocity x: ux_bar (DIVA) / ux_b (SSA)  */
+#define YGPU_SRV_UY    1
+#define YGPU_SRV_VISC  2        /* visc_eff, nx*ny*nz                            */
+#define YGPU_SRV_H     3        /* H_ice                                         */
+#define YGPU_SRV_UXB   4        /* ux_b                                          */
+#define YGPU_SRV_UYB   5
+
+/* NULL on error (ygpu_last_error). Starts the serving thread. */
+ygpu_server* ygpu_server_create(const ygpu_server_cfg* cfg);
+/* Stops the thread after the solves on the GPU finish; frees everything. */
+void ygpu_server_destroy(ygpu_server* srv);
+/*
+ * Registers a member from HOST arrays laid out like ygpu_fields (nx, ny, nz,
+ * dx, dy, n_glen set). Read: H_ice, z_bed, z_sl, c_bed, f_slide, ATT, zeta_aa,
+ * and where not NULL the initial beta, visc_eff (else 1e5 Pa a), velocities and
+ * basal stress (else 0). The other inputs are built on the device per request.
+ */
+int ygpu_server_add_member(ygpu_server* srv, const ygpu_fields* host, int* member_id);
+/* Queues one step of a member; thread-safe. */
+int ygpu_server_submit(ygpu_server* srv, int member, unsigned long long seed, int* request_id);
+/* 1 when the request has finished, 0 while it waits or runs, <0 on a bad id. */
+int ygpu_server_poll(ygpu_server* srv, int request_id);
+/* Waits up to timeout_s (<0: no limit); returns the solve status, or
+   YGPU_ERR_BUSY on timeout. latency_ms: submit to completion. */
+int ygpu_server_wait(ygpu_server* srv, int request_id, double timeout_s, ygpu_stats* stats,
+                     double* latency_ms);
+/* Copies a member field to a host buffer; YGPU_ERR_BUSY while it is solving. */
+int ygpu_server_fetch(ygpu_server* srv, int member, int field, double* host);
+int ygpu_server_get_info(ygpu_server* srv, ygpu_server_info* info);
+
 #ifdef __cplusplus
 }
 #endif

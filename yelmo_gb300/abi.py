@@ -89,6 +89,26 @@ class Fields(C.Structure):
         "ATT", "zeta_aa", "z_sl", "z_bed", "z_srf")]
 
 
+class ServerCfg(C.Structure):
+    """ygpu_server_cfg."""
+    _fields_ = [
+        ("device", C.c_int), ("kind", C.c_int), ("par", DynPar),
+        ("grad_lim", C.c_double), ("taud_lim", C.c_double), ("lateral_bc", C.c_int),
+        ("dH_sigma", C.c_double), ("hbm_budget", C.c_ulonglong), ("max_slots", C.c_int),
+    ]
+
+
+class ServerInfo(C.Structure):
+    """ygpu_server_info."""
+    _fields_ = [
+        ("members", C.c_int), ("slots", C.c_int), ("active", C.c_int), ("pending", C.c_int),
+        ("ticks", C.c_longlong), ("completed", C.c_longlong), ("bytes_held", C.c_ulonglong),
+    ]
+
+
+SRV_UX, SRV_UY, SRV_VISC, SRV_H, SRV_UXB, SRV_UYB = 0, 1, 2, 3, 4, 5
+
+
 # Argument names of calc_velocity_ssa (velocity_ssa.f90:60) and
 # calc_velocity_diva (velocity_diva.f90:59), in order, with their C type.
 SSA_ARGS = [

@@ -23,6 +23,7 @@ UNITS = {
     "ygpu_api.cu": [],
     "ygpu_inputs.cu": ["-fmad=false"],
     "ygpu_noalloc.cu": [],
+    "ygpu_serve.cu": [],
 }
 
 

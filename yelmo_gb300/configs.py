@@ -233,6 +233,22 @@ def ensemble_member(i: int, seed: int = 77, nz: int = 10, sides=(41, 81, 121, 16
                     _F(beta), _F(np.zeros((side, side))), _F(np.ones((side, side))))
 
 
+def served_member(i: int, seed: int = 99, nz: int = 10, lo: int = 64, hi: int = 321) -> Instance:
+    """Member i of the served ensemble stream: side uniform in [lo, hi], 1280 km
+    domain, geometry, roughness and friction as the batched ensemble, SSA."""
+    side = lo + int(uniform01(seed + i, 1)[0] * (hi - lo + 1))
+    side = min(max(side, lo), hi)
+    dx = 1280e3 / (side - 1)
+    H, bed = _marine_geometry(side, dx, seed + i)
+    zeta = calc_zeta(nz)
+    ATT = _temperature_att(H, zeta)
+    u = uniform01(seed + 1000 + i, side * side).reshape((side, side), order="F")
+    beta = np.where(H < -(1028.0 / 910.0) * bed, 0.0, 10.0 ** (2.0 + 2.0 * u))
+    par = YdynParams(solver="ssa", ssa_solver="energy", beta_method=-1, beta_gl_stag=1)
+    return Instance(f"served_{i}", par, dx, H, bed, _F(np.zeros((side, side))), ATT, zeta,
+                    _F(beta), _F(np.zeros((side, side))), _F(np.ones((side, side))))
+
+
 def continent_diva(n: int = 801, seed: int = 4242, nz: int = 20) -> Instance:
     """Large DIVA solve: spectral bed (~30 % floating), random domes, power-law friction."""
     dx = 4e3 * 800.0 / (n - 1)

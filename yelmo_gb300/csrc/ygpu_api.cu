@@ -347,8 +347,8 @@ static int env_int(const char* name, int dflt) {
 }
 
 // Launch shape of a batch: (n_teams, team_ctas).
-static void choose_teams(const ygpu_ctx* c, int n_inst, size_t max_nu, int* n_teams, int* team_ctas) {
-    int maxc = c->max_ctas > 0 ? c->max_ctas : 1;
+void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, int* team_ctas) {
+    int maxc = max_ctas > 0 ? max_ctas : 1;
     if (n_inst == 1) {
         // one team over the GPU, sized to the instance
         *team_ctas = ygpu_single_team_ctas(maxc, max_nu);
@@ -400,7 +400,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
         c->insts_cap = n;
     }
     int n_teams, team_ctas;
-    choose_teams(c, n, max_nu, &n_teams, &team_ctas);
+    ygpu_choose_teams(c->max_ctas, n, max_nu, &n_teams, &team_ctas);
     if (c->ctl_cap < n_teams) {
         cudaFree(c->d_ctl);
         c->d_ctl = nullptr;

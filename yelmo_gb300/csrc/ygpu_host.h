@@ -19,6 +19,17 @@ void ygpu_set_error(const char* fmt, ...);
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
                        TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort);
 int ygpu_solver_max_ctas(int device);
+
+// Step kernels of the Picard loop (one cooperative launch each)
+enum { YG_STEP_SETUP = 0, YG_STEP_PRE = 1, YG_STEP_KRYLOV = 2, YG_STEP_POST = 3, YG_STEP_FINAL = 4 };
+struct StepShape {
+    int grid, team_ctas;           // heavy steps: CTAs, CTAs per team
+    int kgrid, ktc;                // Krylov step: CTAs, CTAs per team
+};
+int ygpu_init_constants(int device);
+int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh);
+int ygpu_launch_step(int step, cudaStream_t s, const StepShape& sh, const Inst* d_insts, int n_inst,
+                     const ygpu_dyn_par& P, TeamCtl* ctls, int* d_done, int* d_abort);
 int ygpu_sm_count(int device);
 size_t ygpu_teamctl_bytes();
 size_t ygpu_inst_bytes();
@@ -43,3 +54,4 @@ size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed);
 void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed);
 size_t ygpu_align256(size_t b);
 int ygpu_single_team_ctas(int max_ctas, size_t nu);
+void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, int* team_ctas);

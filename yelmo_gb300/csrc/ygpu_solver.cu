@@ -2094,7 +2094,6 @@ __device__ __noinline__ void step_post(const Inst& I, const ygpu_dyn_par& P, Tea
 // ---------------------------------------------------------------------------
 // Step kernels: teams of CTAs, instances assigned round-robin in queue order
 // ---------------------------------------------------------------------------
-enum { STEP_SETUP = 0, STEP_PRE = 1, STEP_KRYLOV = 2, STEP_POST = 3, STEP_FINAL = 4 };
 
 template <int STEP>
 YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamCtl* ctls, int team_ctas,
@@ -2116,14 +2115,14 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
         if (threadIdx.x == 0) {
             sI = insts[q];
             const int d = sI.out->done;
-            s_skip = (STEP == STEP_SETUP) ? 0 : (d || ld_acquire_s32(abort_all));
+            s_skip = (STEP == YG_STEP_SETUP) ? 0 : (d || ld_acquire_s32(abort_all));
         }
         __syncthreads();
         if (!s_skip) {
-            if (STEP == STEP_SETUP) step_setup(sI, P, T, done_count);
-            else if (STEP == STEP_PRE) step_pre(sI, P, T, done_count);
-            else if (STEP == STEP_KRYLOV) step_krylov(sI, P, T, done_count);
-            else step_post(sI, P, T, done_count, STEP == STEP_FINAL);
+            if (STEP == YG_STEP_SETUP) step_setup(sI, P, T, done_count);
+            else if (STEP == YG_STEP_PRE) step_pre(sI, P, T, done_count);
+            else if (STEP == YG_STEP_KRYLOV) step_krylov(sI, P, T, done_count);
+            else step_post(sI, P, T, done_count, STEP == YG_STEP_FINAL);
             if (T.cta == 0 && threadIdx.x == 0) sI.out->phase_ns[8] += T.sync_ns;
             T.sync_ns = 0.0;
         }
@@ -2135,23 +2134,23 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
 
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_setup(const Inst* insts, int n_inst, ygpu_dyn_par P,
                                                             TeamCtl* ctls, int tc, int* ab, int* dc) {
-    run_step<STEP_SETUP>(insts, n_inst, P, ctls, tc, ab, dc);
+    run_step<YG_STEP_SETUP>(insts, n_inst, P, ctls, tc, ab, dc);
 }
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_pre(const Inst* insts, int n_inst, ygpu_dyn_par P,
                                                           TeamCtl* ctls, int tc, int* ab, int* dc) {
-    run_step<STEP_PRE>(insts, n_inst, P, ctls, tc, ab, dc);
+    run_step<YG_STEP_PRE>(insts, n_inst, P, ctls, tc, ab, dc);
 }
 __global__ void __launch_bounds__(YG_KBLOCK, 1) ygpu_k_krylov(const Inst* insts, int n_inst, ygpu_dyn_par P,
                                                               TeamCtl* ctls, int tc, int* ab, int* dc) {
-    run_step<STEP_KRYLOV>(insts, n_inst, P, ctls, tc, ab, dc);
+    run_step<YG_STEP_KRYLOV>(insts, n_inst, P, ctls, tc, ab, dc);
 }
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_post(const Inst* insts, int n_inst, ygpu_dyn_par P,
                                                            TeamCtl* ctls, int tc, int* ab, int* dc) {
-    run_step<STEP_POST>(insts, n_inst, P, ctls, tc, ab, dc);
+    run_step<YG_STEP_POST>(insts, n_inst, P, ctls, tc, ab, dc);
 }
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_final(const Inst* insts, int n_inst, ygpu_dyn_par P,
                                                             TeamCtl* ctls, int tc, int* ab, int* dc) {
-    run_step<STEP_FINAL>(insts, n_inst, P, ctls, tc, ab, dc);
+    run_step<YG_STEP_FINAL>(insts, n_inst, P, ctls, tc, ab, dc);
 }
 
 // ---------------------------------------------------------------------------
@@ -2275,33 +2274,31 @@ static int coop(const void* kern, int grid, int block, cudaStream_t s, const Ins
     return YGPU_OK;
 }
 
-int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
-                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_misc, int* d_abort) {
-    // d_misc[0]: count of finished instances; d_abort: launch-wide abort flag
-    if (device >= 0 && device < 64 && !g_gqw_set[device]) {
-        double w[4][4];
-        const int sx[4] = {-1, 1, 1, -1}, sy[4] = {-1, -1, 1, 1};
-        const double g = 1.0 / sqrt(3.0);
-        for (int q = 0; q < 4; q++)
-            for (int c = 0; c < 4; c++) {
-                volatile double ax = 1.0 + (double)(sx[q] * sx[c]) * g;
-                volatile double ay = 1.0 + (double)(sy[q] * sy[c]) * g;
-                volatile double pr = ax * ay;
-                w[q][c] = pr * 0.25;
-            }
-        float wf[4][4];
-        for (int q = 0; q < 4; q++)
-            for (int c = 0; c < 4; c++) wf[q][c] = (float)w[q][c];
-        if (cudaMemcpyToSymbol(c_gqw, w, sizeof(w)) != cudaSuccess) return YGPU_ERR_CUDA;
-        if (cudaMemcpyToSymbol(c_gqwf, wf, sizeof(wf)) != cudaSuccess) return YGPU_ERR_CUDA;
-        g_gqw_set[device] = true;
-    }
-    if (cudaMemsetAsync(d_misc, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
-    if (cudaMemsetAsync(d_abort, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
-    if (cudaMemsetAsync(d_ctls, 0, sizeof(TeamCtl) * (size_t)n_teams, stream) != cudaSuccess) return YGPU_ERR_CUDA;
-    int* dc = d_misc;
-    // Krylov launch shape: the lean kernel, sized to the largest instance, within
-    // the team control blocks the caller provides (n_teams)
+int ygpu_init_constants(int device) {
+    if (device < 0 || device >= 64) return YGPU_OK;
+    if (g_gqw_set[device]) return YGPU_OK;
+    double w[4][4];
+    const int sx[4] = {-1, 1, 1, -1}, sy[4] = {-1, -1, 1, 1};
+    const double g = 1.0 / sqrt(3.0);
+    for (int q = 0; q < 4; q++)
+        for (int c = 0; c < 4; c++) {
+            volatile double ax = 1.0 + (double)(sx[q] * sx[c]) * g;
+            volatile double ay = 1.0 + (double)(sy[q] * sy[c]) * g;
+            volatile double pr = ax * ay;
+            w[q][c] = pr * 0.25;
+        }
+    float wf[4][4];
+    for (int q = 0; q < 4; q++)
+        for (int c = 0; c < 4; c++) wf[q][c] = (float)w[q][c];
+    if (cudaMemcpyToSymbol(c_gqw, w, sizeof(w)) != cudaSuccess) return YGPU_ERR_CUDA;
+    if (cudaMemcpyToSymbol(c_gqwf, wf, sizeof(wf)) != cudaSuccess) return YGPU_ERR_CUDA;
+    g_gqw_set[device] = true;
+    return YGPU_OK;
+}
+
+int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh) {
+    // Krylov launch shape: the lean kernel; teams of as many CTAs as the heavy
+    // teams (each CTA twice the threads), fewer teams if fewer CTAs are resident
     static int kmax_dev[64];
     const int dslot = (device >= 0 && device < 64) ? device : 0;
     if (kmax_dev[dslot] == 0) kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK);
@@ -2310,8 +2307,6 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
         ygpu_set_error("Krylov kernel cannot be resident on device %d", device);
         return YGPU_ERR_CUDA;
     }
-    // Krylov teams: as many CTAs as the heavy teams (each CTA twice the threads),
-    // fewer teams if the lean kernel has fewer resident CTAs
     int ktc = team_ctas;
     if (const char* e = getenv("YGPU_KRYLOV_CTAS")) {
         const int v = atoi(e);
@@ -2321,22 +2316,52 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
     if (ktc > kmax) ktc = kmax;
     int knt = kmax / ktc;
     if (knt > n_teams) knt = n_teams;
-    const int grid = n_teams * team_ctas;
+    sh->team_ctas = team_ctas;
+    sh->grid = n_teams * team_ctas;
+    sh->ktc = ktc;
+    sh->kgrid = knt * ktc;
+    return YGPU_OK;
+}
+
+int ygpu_launch_step(int step, cudaStream_t s, const StepShape& sh, const Inst* d_insts, int n_inst,
+                     const ygpu_dyn_par& P, TeamCtl* ctls, int* d_done, int* d_abort) {
+    switch (step) {
+        case YG_STEP_SETUP:
+            return coop((const void*)ygpu_k_setup, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done);
+        case YG_STEP_PRE:
+            return coop((const void*)ygpu_k_pre, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done);
+        case YG_STEP_KRYLOV:
+            return coop((const void*)ygpu_k_krylov, sh.kgrid, YG_KBLOCK, s, d_insts, n_inst, P, ctls, sh.ktc, d_abort, d_done);
+        case YG_STEP_POST:
+            return coop((const void*)ygpu_k_post, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done);
+        case YG_STEP_FINAL:
+            return coop((const void*)ygpu_k_final, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done);
+        default:
+            ygpu_set_error("bad solver step %d", step);
+            return YGPU_ERR_BAD_ARG;
+    }
+}
+
+int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
+                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort) {
+    // d_done: count of finished instances; d_abort: launch-wide abort flag
     int st;
-    if ((st = coop((const void*)ygpu_k_setup, grid, YG_BLOCK, stream, d_insts, n_inst, P, d_ctls, team_ctas, d_abort, dc)))
-        return st;
+    if ((st = ygpu_init_constants(device))) return st;
+    if (cudaMemsetAsync(d_done, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    if (cudaMemsetAsync(d_abort, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    if (cudaMemsetAsync(d_ctls, 0, sizeof(TeamCtl) * (size_t)n_teams, stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    StepShape sh;
+    if ((st = ygpu_step_shape(device, n_teams, team_ctas, &sh))) return st;
+    if ((st = ygpu_launch_step(YG_STEP_SETUP, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort))) return st;
+    // Picard iterations: one pre / Krylov / post launch each; the host reads the
+    // count of finished instances every few iterations
     const int check = 4;
     for (int it = 0; it < P.ssa_iter_max; it++) {
-        if ((st = coop((const void*)ygpu_k_pre, grid, YG_BLOCK, stream, d_insts, n_inst, P, d_ctls, team_ctas, d_abort, dc)))
-            return st;
-        if ((st = coop((const void*)ygpu_k_krylov, knt * ktc, YG_KBLOCK, stream, d_insts, n_inst, P, d_ctls, ktc,
-                       d_abort, dc)))
-            return st;
-        if ((st = coop((const void*)ygpu_k_post, grid, YG_BLOCK, stream, d_insts, n_inst, P, d_ctls, team_ctas, d_abort, dc)))
-            return st;
+        for (int step : {YG_STEP_PRE, YG_STEP_KRYLOV, YG_STEP_POST})
+            if ((st = ygpu_launch_step(step, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort))) return st;
         if ((it + 1) % check == 0 || it + 1 == P.ssa_iter_max) {
             int h[2] = {0, 0};
-            if (cudaMemcpyAsync(&h[0], dc, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+            if (cudaMemcpyAsync(&h[0], d_done, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
                 cudaMemcpyAsync(&h[1], d_abort, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
                 cudaStreamSynchronize(stream) != cudaSuccess) {
                 ygpu_set_error("solver step failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -2346,9 +2371,7 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
         }
     }
     // instances not finished by the loop (ssa_iter_max = 0) get their final passes
-    if ((st = coop((const void*)ygpu_k_final, grid, YG_BLOCK, stream, d_insts, n_inst, P, d_ctls, team_ctas, d_abort, dc)))
-        return st;
-    return YGPU_OK;
+    return ygpu_launch_step(YG_STEP_FINAL, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort);
 }
 
 int ygpu_solver_max_ctas(int device) {

@@ -33,6 +33,8 @@ EXPORTS = [
     "ygpu_calc_velocity_ssa", "ygpu_calc_velocity_diva", "ygpu_set_ssa_masks", "ygpu_calc_dyn_inputs",
     "ygpu_linear_solver_matrix_solve", "ygpu_ctx_create", "ygpu_ctx_destroy", "ygpu_ctx_stream",
     "ygpu_solve_device", "ygpu_solve_batch_device", "ygpu_solve_device_noalloc",
+    "ygpu_server_create", "ygpu_server_destroy", "ygpu_server_add_member", "ygpu_server_submit",
+    "ygpu_server_poll", "ygpu_server_wait", "ygpu_server_fetch", "ygpu_server_get_info",
 ]
 
 
@@ -75,6 +77,15 @@ def lib(build_if_missing: bool = True):
                                             C.POINTER(abi.Stats), C.c_void_p]
     ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
     L.ygpu_linear_solver_matrix_solve.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_char_p, ip, ip, dp]
+    L.ygpu_server_create.restype = C.c_void_p
+    L.ygpu_server_create.argtypes = [C.POINTER(abi.ServerCfg)]
+    L.ygpu_server_destroy.argtypes = [C.c_void_p]
+    L.ygpu_server_add_member.argtypes = [C.c_void_p, C.POINTER(abi.Fields), ip]
+    L.ygpu_server_submit.argtypes = [C.c_void_p, C.c_int, C.c_ulonglong, ip]
+    L.ygpu_server_poll.argtypes = [C.c_void_p, C.c_int]
+    L.ygpu_server_wait.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(abi.Stats), dp]
+    L.ygpu_server_fetch.argtypes = [C.c_void_p, C.c_int, C.c_int, dp]
+    L.ygpu_server_get_info.argtypes = [C.c_void_p, C.POINTER(abi.ServerInfo)]
     _lib = L
     return L
 
