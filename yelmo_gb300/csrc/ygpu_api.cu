@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <mutex>
 #include <string>
+#include <queue>
 #include <vector>
 
 #include "ygpu_common.cuh"
@@ -163,6 +164,8 @@ struct ygpu_ctx {
     int out_cap = 0;
     TeamCtl* d_ctl = nullptr;
     int ctl_cap = 0;
+    int* d_map = nullptr;           // team plan of a batch (ygpu_plan_teams)
+    int map_cap = 0;
     int* d_misc = nullptr;          // [0] queue, [1] abort, [2..3] csr out
     double* d_miscd = nullptr;
     int max_ctas = 0;
@@ -215,6 +218,7 @@ extern "C" void ygpu_ctx_destroy(ygpu_ctx* c) {
     cudaFree(c->d_insts);
     cudaFree(c->d_out);
     cudaFree(c->d_ctl);
+    cudaFree(c->d_map);
     cudaFree(c->d_misc);
     cudaFree(c->d_miscd);
     if (c->e0) cudaEventDestroy(c->e0);
@@ -372,6 +376,38 @@ void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, in
     *n_teams = nt;
 }
 
+bool ygpu_plan_teams(int max_ctas, int n, const size_t* nu, std::vector<int>& map, int* grid) {
+    if (n < 1 || n > max_ctas) return false;
+    if (const char* v = getenv("YGPU_UNIFORM_TEAMS"))
+        if (*v && atoi(v) != 0) return false;
+    std::vector<int> cnt(n, 1), cap(n);
+    for (int q = 0; q < n; q++) cap[q] = ygpu_single_team_ctas(max_ctas, nu[q]);
+    // greedy: the next CTA goes to the instance with the most unknowns per CTA
+    std::priority_queue<std::pair<double, int>> pq;
+    for (int q = 0; q < n; q++)
+        if (cnt[q] < cap[q]) pq.push({(double)nu[q] / cnt[q], q});
+    int left = max_ctas - n;
+    while (left > 0 && !pq.empty()) {
+        const int q = pq.top().second;
+        pq.pop();
+        cnt[q]++;
+        left--;
+        if (cnt[q] < cap[q]) pq.push({(double)nu[q] / cnt[q], q});
+    }
+    int g = 0;
+    for (int q = 0; q < n; q++) g += cnt[q];
+    map.assign((size_t)g + 2 * (size_t)n, -1);
+    int first = 0;
+    for (int q = 0; q < n; q++) {
+        for (int k = 0; k < cnt[q]; k++) map[first + k] = q;
+        map[g + 2 * q] = first;
+        map[g + 2 * q + 1] = cnt[q];
+        first += cnt[q];
+    }
+    *grid = g;
+    return true;
+}
+
 static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, const ygpu_fields* inst,
                        ygpu_stats* stats) {
     int st = ygpu_check_par(par);
@@ -401,18 +437,34 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     }
     int n_teams, team_ctas;
     ygpu_choose_teams(c->max_ctas, n, max_nu, &n_teams, &team_ctas);
-    if (c->ctl_cap < n_teams) {
-        cudaFree(c->d_ctl);
-        c->d_ctl = nullptr;
-        CK(cudaMalloc((void**)&c->d_ctl, sizeof(TeamCtl) * (size_t)n_teams));
-        c->ctl_cap = n_teams;
-    }
     // queue order: largest instance first (longest-processing-time first)
     std::vector<int> order(n);
     for (int k = 0; k < n; k++) order[k] = k;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         return (size_t)inst[a].nx * inst[a].ny * inst[a].nz > (size_t)inst[b].nx * inst[b].ny * inst[b].nz;
     });
+    // uneven batches that fit the GPU at once: one team per instance, CTAs in
+    // proportion to its unknowns
+    std::vector<size_t> nus(n);
+    for (int q = 0; q < n; q++) nus[q] = (size_t)2 * inst[order[q]].nx * inst[order[q]].ny;
+    std::vector<int> map;
+    int map_grid = 0;
+    const bool mapped = n > 1 && ygpu_plan_teams(c->max_ctas, n, nus.data(), map, &map_grid);
+    const int n_ctl = mapped ? n : n_teams;
+    if (c->ctl_cap < n_ctl) {
+        cudaFree(c->d_ctl);
+        c->d_ctl = nullptr;
+        CK(cudaMalloc((void**)&c->d_ctl, sizeof(TeamCtl) * (size_t)n_ctl));
+        c->ctl_cap = n_ctl;
+    }
+    if (mapped && c->map_cap < (int)map.size()) {
+        cudaFree(c->d_map);
+        c->d_map = nullptr;
+        CK(cudaMalloc((void**)&c->d_map, sizeof(int) * map.size()));
+        c->map_cap = (int)map.size();
+    }
+    if (mapped)
+        CK(cudaMemcpyAsync(c->d_map, map.data(), sizeof(int) * map.size(), cudaMemcpyHostToDevice, c->stream));
     c->h_insts.resize(n);
     for (int q = 0; q < n; q++) {
         const int k = order[q];
@@ -424,8 +476,8 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     CK(cudaMemcpyAsync(c->d_insts, c->h_insts.data(), sizeof(Inst) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->d_out, 0, sizeof(InstOut) * (size_t)n, c->stream));
     CK(cudaEventRecord(c->e0, c->stream));
-    st = ygpu_launch_solver(c->device, c->stream, c->d_insts, n, *par, c->d_ctl, n_teams, team_ctas, c->d_misc,
-                            c->d_misc + 1);
+    st = ygpu_launch_solver(c->device, c->stream, c->d_insts, n, *par, c->d_ctl, n_ctl, team_ctas, c->d_misc,
+                            c->d_misc + 1, mapped ? c->d_map : nullptr, map_grid);
     if (st) return st;
     CK(cudaEventRecord(c->e1, c->stream));
     c->h_out.resize(n);

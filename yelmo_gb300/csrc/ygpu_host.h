@@ -1,5 +1,6 @@
 // ygpu_host.h -- host-side declarations shared by the library's translation units.
 #pragma once
+#include <vector>
 
 #include <cuda_runtime.h>
 
@@ -17,7 +18,8 @@ void ygpu_set_error(const char* fmt, ...);
 
 // ygpu_solver.cu
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
-                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort);
+                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort,
+                       const int* d_map = nullptr, int map_grid = 0);
 int ygpu_solver_max_ctas(int device);
 
 // Step kernels of the Picard loop (one cooperative launch each)
@@ -25,9 +27,17 @@ enum { YG_STEP_SETUP = 0, YG_STEP_PRE = 1, YG_STEP_KRYLOV = 2, YG_STEP_POST = 3,
 struct StepShape {
     int grid, team_ctas;           // heavy steps: CTAs, CTAs per team
     int kgrid, ktc;                // Krylov step: CTAs, CTAs per team
+    const int* map = nullptr;      // device team map of the heavy steps (NULL: uniform teams)
+    const int* kmap = nullptr;     // device team map of the Krylov step
 };
 int ygpu_init_constants(int device);
 int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh);
+// one team per instance, CTA counts from a plan (ygpu_plan_teams) already on the device
+int ygpu_step_shape_mapped(int device, int grid, const int* d_map, StepShape* sh);
+// CTAs per instance in proportion to its unknowns (at least one, at most its
+// single-solve team); false when the instances outnumber max_ctas. map gets
+// the layout run_step reads: [grid] CTA -> instance, then (first, count) pairs.
+bool ygpu_plan_teams(int max_ctas, int n_inst, const size_t* nu, std::vector<int>& map, int* grid);
 int ygpu_launch_step(int step, cudaStream_t s, const StepShape& sh, const Inst* d_insts, int n_inst,
                      const ygpu_dyn_par& P, TeamCtl* ctls, int* d_done, int* d_abort);
 int ygpu_sm_count(int device);

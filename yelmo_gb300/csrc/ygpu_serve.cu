@@ -115,12 +115,18 @@ struct ygpu_server {
     std::vector<Slot> slots;
     std::vector<int> active;       // slots on the GPU, largest instance first
     bool active_dirty = false;
+    bool plan_dirty = true;
+    StepShape tick_shape;
     // device arrays
     Inst* d_insts = nullptr;       // active list
     Inst* d_new = nullptr;         // instances being admitted
     InstOut* d_out = nullptr;      // one per slot
     TeamCtl* d_ctl = nullptr;
     int* d_misc = nullptr;         // [0] finished count, [1] abort flag
+    int* d_map = nullptr;          // team plan of the active list (3 * max_ctas ints)
+    int* d_map_new = nullptr;      // team plan of the admitted list
+    int* h_map = nullptr;
+    int* h_map_new = nullptr;
     // pinned host mirrors
     Inst* h_insts = nullptr;
     Inst* h_new = nullptr;
@@ -231,6 +237,26 @@ static std::vector<Admit> admit_locked(ygpu_server* S) {
     return got;
 }
 
+// Launch shape of n instances (nu[q] unknowns each): one team per instance with
+// CTAs in proportion to its size when they fit the GPU at once, else uniform
+// teams. The plan goes through the pinned h_map into d_map on the stream.
+static int plan_shape(ygpu_server* S, int n, const std::vector<size_t>& nu, int* h_map, int* d_map,
+                      StepShape* sh) {
+    std::vector<int> map;
+    int grid = 0;
+    if (n > 1 && ygpu_plan_teams(S->max_ctas, n, nu.data(), map, &grid)) {
+        memcpy(h_map, map.data(), sizeof(int) * map.size());
+        if (cudaMemcpyAsync(d_map, h_map, sizeof(int) * map.size(), cudaMemcpyHostToDevice, S->stream) != cudaSuccess)
+            return YGPU_ERR_CUDA;
+        if (ygpu_step_shape_mapped(S->cfg.device, grid, d_map, sh) == YGPU_OK) return YGPU_OK;
+    }
+    size_t max_nu = 0;
+    for (size_t v : nu) max_nu = std::max(max_nu, v);
+    int n_teams, team_ctas;
+    ygpu_choose_teams(S->max_ctas, n, max_nu, &n_teams, &team_ctas);
+    return ygpu_step_shape(S->cfg.device, n_teams, team_ctas, sh);
+}
+
 static int prepare_admitted(ygpu_server* S, const std::vector<Admit>& got) {
     const ygpu_server_cfg& C = S->cfg;
     const ygpu_dyn_par& P = C.par;
@@ -253,12 +279,10 @@ static int prepare_admitted(ygpu_server* S, const std::vector<Admit>& got) {
     }
     const int n = (int)got.size();
     SCK(cudaMemcpyAsync(S->d_new, S->h_new, sizeof(Inst) * (size_t)n, cudaMemcpyHostToDevice, S->stream), "upload");
-    int n_teams, team_ctas;
-    size_t max_nu = 0;
-    for (const Admit& a : got) max_nu = std::max(max_nu, (size_t)2 * S->slots[a.slot].inst.n2);
-    ygpu_choose_teams(S->max_ctas, n, max_nu, &n_teams, &team_ctas);
+    std::vector<size_t> nu;
+    for (const Admit& a : got) nu.push_back((size_t)2 * S->slots[a.slot].inst.n2);
     StepShape sh;
-    int st = ygpu_step_shape(C.device, n_teams, team_ctas, &sh);
+    int st = plan_shape(S, n, nu, S->h_map_new, S->d_map_new, &sh);
     if (!st) st = ygpu_launch_step(YG_STEP_SETUP, S->stream, sh, S->d_new, n, P, S->d_ctl, S->d_misc, S->d_misc + 1);
     if (!st && P.ssa_iter_max == 0)
         st = ygpu_launch_step(YG_STEP_FINAL, S->stream, sh, S->d_new, n, P, S->d_ctl, S->d_misc, S->d_misc + 1);
@@ -278,13 +302,17 @@ static int run_tick(ygpu_server* S) {
         SCK(cudaMemcpyAsync(S->d_insts, S->h_insts, sizeof(Inst) * (size_t)n, cudaMemcpyHostToDevice, S->stream),
             "active upload");
         S->active_dirty = false;
+        S->plan_dirty = true;
     }
-    size_t max_nu = 0;
-    for (int s : S->active) max_nu = std::max(max_nu, (size_t)2 * S->slots[s].inst.n2);
-    int n_teams, team_ctas;
-    ygpu_choose_teams(S->max_ctas, n, max_nu, &n_teams, &team_ctas);
-    StepShape sh;
-    int st = ygpu_step_shape(S->cfg.device, n_teams, team_ctas, &sh);
+    // the plan changes with the active list only
+    int st = YGPU_OK;
+    if (S->plan_dirty) {
+        std::vector<size_t> nu;
+        for (int s : S->active) nu.push_back((size_t)2 * S->slots[s].inst.n2);
+        st = plan_shape(S, n, nu, S->h_map, S->d_map, &S->tick_shape);
+        S->plan_dirty = false;
+    }
+    const StepShape sh = S->tick_shape;
     for (int step : {YG_STEP_PRE, YG_STEP_KRYLOV, YG_STEP_POST}) {
         if (st) break;
         st = ygpu_launch_step(step, S->stream, sh, S->d_insts, n, P, S->d_ctl, S->d_misc, S->d_misc + 1);
@@ -377,6 +405,10 @@ extern "C" ygpu_server* ygpu_server_create(const ygpu_server_cfg* cfg) {
     if (cfg->kind != YGPU_KIND_SSA && cfg->kind != YGPU_KIND_DIVA) { ygpu_set_error("bad solver kind %d", cfg->kind); return nullptr; }
     if (cfg->dH_sigma < 0.0) { ygpu_set_error("dH_sigma must be >= 0"); return nullptr; }
     if (cudaSetDevice(cfg->device) != cudaSuccess) { ygpu_set_error("cannot use device %d", cfg->device); return nullptr; }
+    // the step kernels' non-inlined phases need more than the default 1 KB of stack per thread
+    size_t stack = 0;
+    cudaDeviceGetLimit(&stack, cudaLimitStackSize);
+    if (stack < 4096) cudaDeviceSetLimit(cudaLimitStackSize, 4096);
     ygpu_server* S = new ygpu_server();
     S->cfg = *cfg;
     S->mixed = (cfg->par.precision == YGPU_PREC_MIXED);
@@ -395,6 +427,10 @@ extern "C" ygpu_server* ygpu_server_create(const ygpu_server_cfg* cfg) {
     ok = ok && cudaMalloc((void**)&S->d_out, sizeof(InstOut) * ms) == cudaSuccess;
     ok = ok && cudaMalloc((void**)&S->d_ctl, sizeof(TeamCtl) * (size_t)S->max_ctas) == cudaSuccess;
     ok = ok && cudaMalloc((void**)&S->d_misc, 64) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&S->d_map, sizeof(int) * 3 * (size_t)S->max_ctas) == cudaSuccess;
+    ok = ok && cudaMalloc((void**)&S->d_map_new, sizeof(int) * 3 * (size_t)S->max_ctas) == cudaSuccess;
+    ok = ok && cudaMallocHost((void**)&S->h_map, sizeof(int) * 3 * (size_t)S->max_ctas) == cudaSuccess;
+    ok = ok && cudaMallocHost((void**)&S->h_map_new, sizeof(int) * 3 * (size_t)S->max_ctas) == cudaSuccess;
     ok = ok && cudaMallocHost((void**)&S->h_insts, sizeof(Inst) * ms) == cudaSuccess;
     ok = ok && cudaMallocHost((void**)&S->h_new, sizeof(Inst) * ms) == cudaSuccess;
     ok = ok && cudaMallocHost((void**)&S->h_out, sizeof(InstOut) * ms) == cudaSuccess;
@@ -407,7 +443,8 @@ extern "C" ygpu_server* ygpu_server_create(const ygpu_server_cfg* cfg) {
         ygpu_server_destroy(S);
         return nullptr;
     }
-    S->held = sizeof(Inst) * 2 * ms + sizeof(InstOut) * ms + sizeof(TeamCtl) * (size_t)S->max_ctas + 64;
+    S->held = sizeof(Inst) * 2 * ms + sizeof(InstOut) * ms + sizeof(TeamCtl) * (size_t)S->max_ctas + 64 +
+              2 * sizeof(int) * 3 * (size_t)S->max_ctas;
     if (S->held > cfg->hbm_budget) {
         ygpu_set_error("hbm_budget %llu is below the server's fixed %zu bytes", cfg->hbm_budget, S->held);
         ygpu_server_destroy(S);
@@ -444,6 +481,10 @@ extern "C" void ygpu_server_destroy(ygpu_server* S) {
     cudaFree(S->d_out);
     cudaFree(S->d_ctl);
     cudaFree(S->d_misc);
+    cudaFree(S->d_map);
+    cudaFree(S->d_map_new);
+    cudaFreeHost(S->h_map);
+    cudaFreeHost(S->h_map_new);
     cudaFreeHost(S->h_insts);
     cudaFreeHost(S->h_new);
     cudaFreeHost(S->h_out);

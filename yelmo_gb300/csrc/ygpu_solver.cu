@@ -2095,17 +2095,32 @@ __device__ __noinline__ void step_post(const Inst& I, const ygpu_dyn_par& P, Tea
 // Step kernels: teams of CTAs, instances assigned round-robin in queue order
 // ---------------------------------------------------------------------------
 
+// Team layout of a launch: uniform teams of team_ctas CTAs taking instances
+// round-robin, or (map != NULL) one team per instance with its own CTA count:
+// map[cta] = instance of the CTA (-1: idle), map[grid + 2q] / [grid + 2q + 1] =
+// first CTA and CTA count of instance q's team.
 template <int STEP>
 YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamCtl* ctls, int team_ctas,
-                     int* abort_all, int* done_count) {
+                     int* abort_all, int* done_count, const int* map) {
     __shared__ Inst sI;
     __shared__ int s_skip;
     Team T;
-    T.ncta = team_ctas;
-    T.cta = blockIdx.x % team_ctas;
+    int team, n_teams;
+    if (map) {
+        team = map[blockIdx.x];
+        if (team < 0) return;
+        const int* tm = map + gridDim.x + 2 * team;
+        T.ncta = tm[1];
+        T.cta = blockIdx.x - tm[0];
+        n_teams = n_inst;          // the loop below visits instance `team` only
+    } else {
+        T.ncta = team_ctas;
+        T.cta = blockIdx.x % team_ctas;
+        team = blockIdx.x / team_ctas;
+        n_teams = gridDim.x / team_ctas;
+    }
     T.tid = T.cta * blockDim.x + threadIdx.x;
-    T.nthr = team_ctas * blockDim.x;
-    const int team = blockIdx.x / team_ctas, n_teams = gridDim.x / team_ctas;
+    T.nthr = T.ncta * blockDim.x;
     T.ctl = ctls + team;
     T.parity = 0;
     T.abort_all = abort_all;
@@ -2133,24 +2148,24 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
 #define YG_KBLOCK 512
 
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_setup(const Inst* insts, int n_inst, ygpu_dyn_par P,
-                                                            TeamCtl* ctls, int tc, int* ab, int* dc) {
-    run_step<YG_STEP_SETUP>(insts, n_inst, P, ctls, tc, ab, dc);
+                                                            TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
+    run_step<YG_STEP_SETUP>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_pre(const Inst* insts, int n_inst, ygpu_dyn_par P,
-                                                          TeamCtl* ctls, int tc, int* ab, int* dc) {
-    run_step<YG_STEP_PRE>(insts, n_inst, P, ctls, tc, ab, dc);
+                                                          TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
+    run_step<YG_STEP_PRE>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
 __global__ void __launch_bounds__(YG_KBLOCK, 1) ygpu_k_krylov(const Inst* insts, int n_inst, ygpu_dyn_par P,
-                                                              TeamCtl* ctls, int tc, int* ab, int* dc) {
-    run_step<YG_STEP_KRYLOV>(insts, n_inst, P, ctls, tc, ab, dc);
+                                                              TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
+    run_step<YG_STEP_KRYLOV>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_post(const Inst* insts, int n_inst, ygpu_dyn_par P,
-                                                           TeamCtl* ctls, int tc, int* ab, int* dc) {
-    run_step<YG_STEP_POST>(insts, n_inst, P, ctls, tc, ab, dc);
+                                                           TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
+    run_step<YG_STEP_POST>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_final(const Inst* insts, int n_inst, ygpu_dyn_par P,
-                                                            TeamCtl* ctls, int tc, int* ab, int* dc) {
-    run_step<YG_STEP_FINAL>(insts, n_inst, P, ctls, tc, ab, dc);
+                                                            TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
+    run_step<YG_STEP_FINAL>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
 
 // ---------------------------------------------------------------------------
@@ -2264,8 +2279,9 @@ static int max_ctas_of(const void* kern, int block) {
 }
 
 static int coop(const void* kern, int grid, int block, cudaStream_t s, const Inst* insts, int n_inst,
-                const ygpu_dyn_par& P, TeamCtl* ctls, int tc, int* ab, int* dc) {
-    void* args[] = {(void*)&insts, (void*)&n_inst, (void*)&P, (void*)&ctls, (void*)&tc, (void*)&ab, (void*)&dc};
+                const ygpu_dyn_par& P, TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
+    void* args[] = {(void*)&insts, (void*)&n_inst, (void*)&P, (void*)&ctls, (void*)&tc, (void*)&ab, (void*)&dc,
+                    (void*)&map};
     cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), args, 0, s);
     if (e != cudaSuccess) {
         ygpu_set_error("cooperative launch of a solver step failed: %s", cudaGetErrorString(e));
@@ -2296,7 +2312,26 @@ int ygpu_init_constants(int device) {
     return YGPU_OK;
 }
 
+int ygpu_step_shape_mapped(int device, int grid, const int* d_map, StepShape* sh) {
+    // one team per instance with its own CTA count; the Krylov kernel uses the
+    // same map when it has as many resident CTAs, else (kgrid = 0) the caller
+    // must use a uniform shape
+    static int kmax_dev[64];
+    const int dslot = (device >= 0 && device < 64) ? device : 0;
+    if (kmax_dev[dslot] == 0) kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK);
+    if (kmax_dev[dslot] < grid) return YGPU_ERR_BAD_ARG;
+    sh->grid = grid;
+    sh->team_ctas = 1;
+    sh->kgrid = grid;
+    sh->ktc = 1;
+    sh->map = d_map;
+    sh->kmap = d_map;
+    return YGPU_OK;
+}
+
 int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh) {
+    sh->map = nullptr;
+    sh->kmap = nullptr;
     // Krylov launch shape: the lean kernel; teams of as many CTAs as the heavy
     // teams (each CTA twice the threads), fewer teams if fewer CTAs are resident
     static int kmax_dev[64];
@@ -2327,15 +2362,15 @@ int ygpu_launch_step(int step, cudaStream_t s, const StepShape& sh, const Inst* 
                      const ygpu_dyn_par& P, TeamCtl* ctls, int* d_done, int* d_abort) {
     switch (step) {
         case YG_STEP_SETUP:
-            return coop((const void*)ygpu_k_setup, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done);
+            return coop((const void*)ygpu_k_setup, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
         case YG_STEP_PRE:
-            return coop((const void*)ygpu_k_pre, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done);
+            return coop((const void*)ygpu_k_pre, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
         case YG_STEP_KRYLOV:
-            return coop((const void*)ygpu_k_krylov, sh.kgrid, YG_KBLOCK, s, d_insts, n_inst, P, ctls, sh.ktc, d_abort, d_done);
+            return coop((const void*)ygpu_k_krylov, sh.kgrid, YG_KBLOCK, s, d_insts, n_inst, P, ctls, sh.ktc, d_abort, d_done, sh.kmap);
         case YG_STEP_POST:
-            return coop((const void*)ygpu_k_post, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done);
+            return coop((const void*)ygpu_k_post, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
         case YG_STEP_FINAL:
-            return coop((const void*)ygpu_k_final, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done);
+            return coop((const void*)ygpu_k_final, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
         default:
             ygpu_set_error("bad solver step %d", step);
             return YGPU_ERR_BAD_ARG;
@@ -2343,15 +2378,20 @@ int ygpu_launch_step(int step, cudaStream_t s, const StepShape& sh, const Inst* 
 }
 
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
-                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort) {
-    // d_done: count of finished instances; d_abort: launch-wide abort flag
+                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort, const int* d_map,
+                       int map_grid) {
+    // d_done: count of finished instances; d_abort: launch-wide abort flag.
+    // With a team map (one team per instance) n_teams is the number of control
+    // blocks to clear (n_inst) and map_grid the CTAs of the plan.
     int st;
     if ((st = ygpu_init_constants(device))) return st;
     if (cudaMemsetAsync(d_done, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
     if (cudaMemsetAsync(d_abort, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
     if (cudaMemsetAsync(d_ctls, 0, sizeof(TeamCtl) * (size_t)n_teams, stream) != cudaSuccess) return YGPU_ERR_CUDA;
     StepShape sh;
-    if ((st = ygpu_step_shape(device, n_teams, team_ctas, &sh))) return st;
+    if (d_map) st = ygpu_step_shape_mapped(device, map_grid, d_map, &sh);
+    else st = ygpu_step_shape(device, n_teams, team_ctas, &sh);
+    if (st) return st;
     if ((st = ygpu_launch_step(YG_STEP_SETUP, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort))) return st;
     // Picard iterations: one pre / Krylov / post launch each; the host reads the
     // count of finished instances every few iterations
