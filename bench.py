@@ -347,20 +347,29 @@ def main():
                 lat.append(st1["device_ms"])
         u_single = None if ensemble else devs[0]["ux_bar" if kind == abi.KIND_DIVA else "ux_b"].cpu().numpy().reshape(
             (insts[0].nx, insts[0].ny), order="F")
-        # batched throughput
+        # batched throughput; the mixed arm also times every step kernel launch
+        # with CUDA events on the solver stream and counts the launches
         barrier()
         clk = ClockSampler(local)
-        if prec == "mixed":
-            clk.start()
-        step_ms, sts = [], None
+        step_ms, sts, all_sts = [], None, []
+        launches = 0
         for s in range(args.warmup + args.steps):
             reset(range(batch))
+            if s == args.warmup and prec == "mixed":
+                clk.start()
+                gpu.step_timing(True)
+                launches = gpu.kernel_launches()
             sts = solver.solve_batch(kind, par, fields)
             if s >= args.warmup:
                 step_ms.append(sts[0]["device_ms"])
+                all_sts.append(sts)
         barrier()
+        steps_timing = None
         if prec == "mixed":
             clocks = clk.stop()
+            launches = gpu.kernel_launches() - launches
+            steps_timing = gpu.step_timing_get()
+            gpu.step_timing(False)
         vel = "ux_bar" if kind == abi.KIND_DIVA else "ux_b"
         u_batch = [d[vel].cpu().numpy().reshape((i.nx, i.ny), order="F") for d, i in zip(devs, insts)]
         tot_ms = sum(step_ms)
@@ -369,7 +378,8 @@ def main():
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             tot_ms = float(t.item())
         res[prec] = {"lat": lat, "st1": st1, "step_ms": step_ms, "tot_ms": tot_ms, "sts": sts,
-                     "u_single": u_single, "u_batch": u_batch}
+                     "u_single": u_single, "u_batch": u_batch, "all_sts": all_sts, "launches": launches,
+                     "steps_timing": steps_timing}
 
     # e2e: the C-ABI drop-in on host buffers (host-device copies inside the timed region)
     e2e_times = []
@@ -399,11 +409,21 @@ def main():
     if tight is not None:
         vel = "ux_bar" if kind == abi.KIND_DIVA else "ux_b"
         err_vs_oracle = {"mixed": rel_l2(mixed["u_single"], tight[vel]), "fp64": rel_l2(fp64["u_single"], tight[vel])}
-    # roofline of the solver kernel over the batched step
-    alg = sum(gpu.algorithmic_bytes(st, kind, i.nx, i.ny, i.nz, mixed=True)
-              for st, i in zip(mixed["sts"], insts))
+    # roofline of the dominant kernel (the Krylov step) over the timed batched
+    # steps: algorithmic bytes of its launches / their CUDA-event time
+    cg = insts[0].par.lis_opt.split("-i ")[1].split()[0] in ("cg", "minres")
+    alg_steps = {"pre": 0.0, "krylov": 0.0, "post": 0.0}
+    for sts_k in mixed["all_sts"]:
+        for st, i in zip(sts_k, insts):
+            for k, v in gpu.algorithmic_bytes(st, kind, i.nx, i.ny, i.nz, mixed=True, cg=cg, by_step=True).items():
+                alg_steps[k] += v
+    tm = mixed["steps_timing"]
+    kr_ms, kr_n = tm["krylov"]
+    achieved = alg_steps["krylov"] / (kr_ms / 1e3) / 1e9 if kr_ms > 0 else None
+    per_step = {k: {"launches": tm[k][1], "ms": tm[k][0],
+                    "achieved_gbs": (alg_steps[k] / (tm[k][0] / 1e3) / 1e9) if k in alg_steps and tm[k][0] > 0
+                    else None} for k in tm}
     avg_ms = statistics.mean(mixed["step_ms"])
-    achieved = alg / (avg_ms / 1e3) / 1e9
     try:
         peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
         peak_src = "measured"
@@ -426,13 +446,18 @@ def main():
         "rel_err_vs_oracle": err_vs_oracle,
         "rel_err_mixed_vs_fp64_max": err_mixed_vs_fp64,
         "picard_iters": [s["ssa_iter_now"] for s in mixed["sts"][:4]],
-        "gpu_launches": K,
+        "gpu_launches": mixed["launches"],
         "e2e": ({"value": 1.0 / statistics.mean(e2e_times), "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                 "d2h_bytes_per_step": d2h, "path": "ygpu_calc_velocity_diva on host buffers, one solve per step"}
+                 "d2h_bytes_per_step": d2h,
+                 "path": ("ygpu_calc_velocity_diva" if kind == abi.KIND_DIVA else "ygpu_calc_velocity_ssa")
+                 + " on host buffers, one solve per step"}
                 if e2e_times else None),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "ygpu_solve_kernel (batched step, one launch)",
-                     "peak_source": peak_src},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "kernel": "ygpu_k_krylov", "launches": kr_n,
+                     "alg_bytes_per_launch": alg_steps["krylov"] / max(kr_n, 1),
+                     "avg_launch_ms": kr_ms / max(kr_n, 1), "peak_source": peak_src},
+        "step_kernels": per_step,
         "phase_ms_single": mixed["st1"]["phase_ms"] if mixed["st1"] else None,
         "clocks": clocks,
         "cpu_baseline": cpu_base,

@@ -385,6 +385,17 @@ int ygpu_server_wait(ygpu_server* srv, int request_id, double timeout_s, ygpu_st
 int ygpu_server_fetch(ygpu_server* srv, int member, int field, double* host);
 int ygpu_server_get_info(ygpu_server* srv, ygpu_server_info* info);
 
+/* ======================================================================== */
+/* Launch accounting (no counterpart in the reference; for benchmarks).      */
+/* ======================================================================== */
+/* Kernels this library has launched in the process so far. */
+unsigned long long ygpu_kernel_launches(void);
+/* on != 0: time every solver step launch with CUDA events on its stream (and
+   clear the totals); 0: stop. Steps: 0 setup, 1 pre, 2 Krylov, 3 post, 4 final. */
+void ygpu_step_timing(int on);
+/* Device milliseconds and launch counts per step since ygpu_step_timing(1). */
+void ygpu_step_timing_get(double ms[5], long long count[5]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -485,6 +485,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     int abort_flag = 0;
     CK(cudaMemcpyAsync(&abort_flag, c->d_misc + 1, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    ygpu_step_timing_flush();
     float ms = 0.f;
     cudaEventElapsedTime(&ms, c->e0, c->e1);
     int worst = YGPU_OK;

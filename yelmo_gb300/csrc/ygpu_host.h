@@ -31,6 +31,8 @@ struct StepShape {
     const int* kmap = nullptr;     // device team map of the Krylov step
 };
 int ygpu_init_constants(int device);
+void ygpu_count_launches(unsigned long long n);
+void ygpu_step_timing_flush();
 int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh);
 // one team per instance, CTA counts from a plan (ygpu_plan_teams) already on the device
 int ygpu_step_shape_mapped(int device, int grid, const int* d_map, StepShape* sh);

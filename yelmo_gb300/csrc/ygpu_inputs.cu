@@ -223,6 +223,7 @@ int ygpu_dyn_inputs_device(cudaStream_t s, const double* H, const double* zb, co
         ygpu_set_error("input kernels: %s", cudaGetErrorString(e));
         return YGPU_ERR_CUDA;
     }
+    ygpu_count_launches(4);
     return YGPU_OK;
 }
 
@@ -234,5 +235,6 @@ int ygpu_ssa_masks_device(cudaStream_t s, int* mx, int* my, const int* mf, const
         ygpu_set_error("mask kernel: %s", cudaGetErrorString(e));
         return YGPU_ERR_CUDA;
     }
+    ygpu_count_launches(1);
     return YGPU_OK;
 }

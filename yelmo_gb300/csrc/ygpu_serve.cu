@@ -264,8 +264,10 @@ static int prepare_admitted(ygpu_server* S, const std::vector<Admit>& got) {
         const Slot& sl = S->slots[got[q].slot];
         const Member& M = *got[q].member;
         const int n2 = M.nx * M.ny;
-        if (C.dH_sigma > 0.0)
+        if (C.dH_sigma > 0.0) {
             k_step_thickness<<<(n2 + 255) / 256, 256, 0, S->stream>>>(M.H, n2, got[q].key, C.dH_sigma);
+            ygpu_count_launches(1);
+        }
         int st = ygpu_dyn_inputs_device(S->stream, M.H, M.f.z_bed, M.f.z_sl, M.f_ice, M.H_grnd, M.z_srf, M.f_grnd,
                                         M.fgx, M.fgy, M.mask_frnt, M.dzsdx, M.dzsdy, M.taud_x, M.taud_y, M.taul_x,
                                         M.taul_y, M.f.dx, C.grad_lim, C.taud_lim, P.rho_ice, P.rho_sw, P.g,
@@ -322,6 +324,7 @@ static int run_tick(ygpu_server* S) {
         "output read");
     SCK(cudaMemcpyAsync(S->h_abort, S->d_misc + 1, sizeof(int), cudaMemcpyDeviceToHost, S->stream), "abort read");
     SCK(cudaStreamSynchronize(S->stream), "tick");
+    ygpu_step_timing_flush();
     S->ticks++;
     return YGPU_OK;
 }

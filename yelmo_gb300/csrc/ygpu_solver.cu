@@ -21,6 +21,9 @@
 //               error matrix, basal stress and basal velocity
 #include <cuda_runtime.h>
 #include <stdlib.h>
+#include <vector>
+#include <mutex>
+#include <atomic>
 
 #include <math.h>
 #include <stdio.h>
@@ -2255,6 +2258,7 @@ int ygpu_launch_csr(cudaStream_t stream, int n, const int* ptr, const int* idx, 
         ygpu_set_error("cooperative launch of the CSR solve failed: %s", cudaGetErrorString(e));
         return YGPU_ERR_CUDA;
     }
+    ygpu_count_launches(1);
     return YGPU_OK;
 }
 
@@ -2358,8 +2362,104 @@ int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh) {
     return YGPU_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Launch accounting: a count of every kernel this library launches, and (when
+// switched on) CUDA-event timing of each step launch on its own stream.
+// ---------------------------------------------------------------------------
+namespace {
+std::atomic<unsigned long long> g_launches{0};
+struct StepTimer {
+    std::mutex mu;
+    bool on = false;
+    struct Rec { cudaEvent_t a, b; int kind; };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> spare;
+    double ms[5] = {0, 0, 0, 0, 0};
+    long long n[5] = {0, 0, 0, 0, 0};
+    cudaEvent_t get() {
+        if (!spare.empty()) {
+            cudaEvent_t e = spare.back();
+            spare.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+} g_timer;
+}  // namespace
+
+void ygpu_count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+extern "C" unsigned long long ygpu_kernel_launches(void) { return g_launches.load(); }
+
+extern "C" void ygpu_step_timing(int on) {
+    std::lock_guard<std::mutex> lk(g_timer.mu);
+    g_timer.on = (on != 0);
+    if (on) {
+        for (int k = 0; k < 5; k++) { g_timer.ms[k] = 0.0; g_timer.n[k] = 0; }
+    }
+}
+
+// Folds the timed launches whose streams have finished into the totals.
+void ygpu_step_timing_flush() {
+    std::lock_guard<std::mutex> lk(g_timer.mu);
+    std::vector<StepTimer::Rec> keep;
+    for (auto& r : g_timer.pending) {
+        if (cudaEventQuery(r.b) != cudaSuccess) {
+            cudaGetLastError();
+            keep.push_back(r);
+            continue;
+        }
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            g_timer.ms[r.kind] += ms;
+            g_timer.n[r.kind] += 1;
+        }
+        cudaGetLastError();
+        g_timer.spare.push_back(r.a);
+        g_timer.spare.push_back(r.b);
+    }
+    g_timer.pending.swap(keep);
+}
+
+extern "C" void ygpu_step_timing_get(double ms[5], long long count[5]) {
+    ygpu_step_timing_flush();
+    std::lock_guard<std::mutex> lk(g_timer.mu);
+    for (int k = 0; k < 5; k++) {
+        if (ms) ms[k] = g_timer.ms[k];
+        if (count) count[k] = g_timer.n[k];
+    }
+}
+
+static int launch_step_raw(int step, cudaStream_t s, const StepShape& sh, const Inst* d_insts, int n_inst,
+                           const ygpu_dyn_par& P, TeamCtl* ctls, int* d_done, int* d_abort);
+
 int ygpu_launch_step(int step, cudaStream_t s, const StepShape& sh, const Inst* d_insts, int n_inst,
                      const ygpu_dyn_par& P, TeamCtl* ctls, int* d_done, int* d_abort) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    bool timed = false;
+    if (step >= 0 && step < 5) {
+        std::lock_guard<std::mutex> lk(g_timer.mu);
+        if (g_timer.on) {
+            a = g_timer.get();
+            b = g_timer.get();
+            timed = (a && b);
+        }
+    }
+    if (timed) cudaEventRecord(a, s);
+    const int st = launch_step_raw(step, s, sh, d_insts, n_inst, P, ctls, d_done, d_abort);
+    if (st == YGPU_OK) ygpu_count_launches(1);
+    if (timed) {
+        cudaEventRecord(b, s);
+        std::lock_guard<std::mutex> lk(g_timer.mu);
+        g_timer.pending.push_back({a, b, step});
+    }
+    return st;
+}
+
+static int launch_step_raw(int step, cudaStream_t s, const StepShape& sh, const Inst* d_insts, int n_inst,
+                           const ygpu_dyn_par& P, TeamCtl* ctls, int* d_done, int* d_abort) {
     switch (step) {
         case YG_STEP_SETUP:
             return coop((const void*)ygpu_k_setup, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);

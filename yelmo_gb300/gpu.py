@@ -35,6 +35,7 @@ EXPORTS = [
     "ygpu_solve_device", "ygpu_solve_batch_device", "ygpu_solve_device_noalloc",
     "ygpu_server_create", "ygpu_server_destroy", "ygpu_server_add_member", "ygpu_server_submit",
     "ygpu_server_poll", "ygpu_server_wait", "ygpu_server_fetch", "ygpu_server_get_info",
+    "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get",
 ]
 
 
@@ -86,6 +87,9 @@ def lib(build_if_missing: bool = True):
     L.ygpu_server_wait.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(abi.Stats), dp]
     L.ygpu_server_fetch.argtypes = [C.c_void_p, C.c_int, C.c_int, dp]
     L.ygpu_server_get_info.argtypes = [C.c_void_p, C.POINTER(abi.ServerInfo)]
+    L.ygpu_kernel_launches.restype = C.c_ulonglong
+    L.ygpu_step_timing.argtypes = [C.c_int]
+    L.ygpu_step_timing_get.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -236,6 +240,27 @@ class DeviceSolver:
         return [s.as_dict() for s in sts]
 
 
+STEP_NAMES = ("setup", "pre", "krylov", "post", "final")
+
+
+def kernel_launches() -> int:
+    """Kernels the library has launched in this process."""
+    return int(lib().ygpu_kernel_launches())
+
+
+def step_timing(on: bool):
+    """Switch CUDA-event timing of every solver step launch on (clearing the totals) or off."""
+    lib().ygpu_step_timing(1 if on else 0)
+
+
+def step_timing_get() -> dict:
+    """{step: (device ms, launches)} since step_timing(True)."""
+    ms = (C.c_double * 5)()
+    n = (C.c_longlong * 5)()
+    lib().ygpu_step_timing_get(ms, n)
+    return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(STEP_NAMES)}
+
+
 def host_io_bytes(kind: int, nx: int, ny: int, nz: int):
     """Bytes the host-pointer drop-in copies in and out (ygpu_calc_velocity_* staging)."""
     b2, b3, i2, bz = 8 * nx * ny, 8 * nx * ny * nz, 4 * nx * ny, 8 * nz
@@ -250,31 +275,34 @@ def host_io_bytes(kind: int, nx: int, ny: int, nz: int):
 
 
 def algorithmic_bytes(stats: dict, kind: int, nx: int, ny: int, nz: int, mixed: bool, energy: bool = True,
-                      cg: bool = True) -> float:
-    """Algorithmic HBM bytes of one solve: each distinct array read once and
-    written once per phase, with the per-cell counts of the hot-path scope
-    (column pass (3nz+14)w DIVA / (3nz+10)w SSA, matrix-free operator 8w+2,
-    Krylov vector passes) times the phase counts the solve reports."""
+                      cg: bool = True, by_step: bool = False):
+    """Algorithmic HBM bytes of one solve: every distinct array read once and
+    written once per kernel pass, per cell (w = 8 B FP64, 4 B FP32):
+
+    - pre step, per Picard iteration: strain rates 7w, column pass (3nz+14)w
+      DIVA / (3nz+10)w SSA (read u, taub, H, f_ice, c_bed, f_slide, f_grnd,
+      visc_prev, ATT; write visc, N, F2, beta), faces 20w+8, system 16w+8;
+    - Krylov step: pipelined CG iteration 42w+8 (read the operator input,
+      N, N_ab, two drag arrays, the row flags, the preconditioner and eight
+      recurrence vectors; write the eight vectors and the next operator
+      input), BiCGSTAB iteration 62w+16 (two operator applies of 8w+8 and
+      46w of vector passes); mixed mode: each FP64 defect-correction step
+      186 B (FP64 operator 66, residual 48, conversions 32, update 40) and the
+      FP32 coefficient copies 72 B per Picard iteration;
+    - post step, per Picard iteration: epilogue 16w+8.
+
+    Returns the total, or {step: bytes} with by_step."""
     n2 = nx * ny
     w = 8
     picard = stats["ssa_iter_now"]
     lin = stats["ssa_lin_iter"]
     col = (3 * nz + (14 if kind == abi.KIND_DIVA else 10)) * w
-    strain = 7 * w
-    faces = 20 * w + 8
-    system = 16 * w + 8
-    epilogue = 16 * w + 8
-    per_picard = strain + col + faces + system + epilogue
-    if not mixed:
-        op = 8 * w + 2
-        vec = (28 if cg else 44) * w               # CG: 14 distinct 2-component array passes; BiCGSTAB: 22
-        krylov = lin * ((1 if cg else 2) * op + vec)
-    else:
-        wf = 4
-        op = 8 * wf + 2
-        vec = (28 if cg else 44) * wf
-        krylov = lin * ((1 if cg else 2) * op + vec)
-        outer = stats.get("outer_iter", 0)
-        krylov += outer * ((8 * w + 2) + 6 * w + 8 * wf)   # FP64 residual + conversions
-        krylov += picard * (4 * wf + 2 * 2 * wf + 2 * 2 * w)  # FP32 coefficient copies
-    return float(n2) * (picard * per_picard + krylov)
+    pre = 7 * w + col + (20 * w + 8) + (16 * w + 8)
+    post = 16 * w + 8
+    wk = 4 if mixed else 8
+    it_bytes = (42 * wk + 8) if cg else (62 * wk + 16)
+    krylov = lin * it_bytes
+    if mixed:
+        krylov += stats.get("outer_iter", 0) * 186 + picard * 72
+    steps = {"pre": float(n2) * picard * pre, "krylov": float(n2) * krylov, "post": float(n2) * picard * post}
+    return steps if by_step else sum(steps.values())
