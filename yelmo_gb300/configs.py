@@ -250,7 +250,10 @@ def served_member(i: int, seed: int = 99, nz: int = 10, lo: int = 64, hi: int = 
 
 
 def continent_diva(n: int = 801, seed: int = 4242, nz: int = 20) -> Instance:
-    """Large DIVA solve: spectral bed (~30 % floating), random domes, power-law friction."""
+    """Large DIVA solve: spectral bed (k^-2, rms 600 m, mean -200 m), twelve
+    seeded domes (3000 m, radii 5-11 % of the domain) over a 300 m ice sheet
+    inside 45 % of the domain radius, capped at 4000 m. About 30 % of the ice
+    floats (28.5 % at 801 x 801). Power-law friction, q = 1/3."""
     dx = 4e3 * 800.0 / (n - 1)
     bed = spectral_field(n, n, dx, 600.0, -200.0, seed)
     x = (np.arange(n) - (n - 1) / 2.0) * dx
@@ -259,9 +262,11 @@ def continent_diva(n: int = 801, seed: int = 4242, nz: int = 20) -> Instance:
     rad = uniform01(seed + 2, 12)
     L = (n - 1) * dx
     for (cx, cy), rr in zip(cen, rad):
-        x0, y0, R = (cx - 0.5) * 0.6 * L, (cy - 0.5) * 0.6 * L, (0.15 + 0.2 * rr) * L
+        x0, y0, R = (cx - 0.5) * 0.6 * L, (cy - 0.5) * 0.6 * L, (0.05 + 0.06 * rr) * L
         d = np.sqrt((x[:, None] - x0) ** 2 + (x[None, :] - y0) ** 2)
         H = H + 3000.0 * np.sqrt(np.maximum(0.0, 1.0 - (d / R) ** 2))
+    r = np.sqrt(x[:, None] ** 2 + x[None, :] ** 2)
+    H = np.where(r < 0.45 * L, np.maximum(H, 300.0), H)
     H = np.minimum(H, 4000.0)
     zeta = calc_zeta(nz)
     ATT = _temperature_att(H, zeta, Ts=-25.0, Tb=-1.0)

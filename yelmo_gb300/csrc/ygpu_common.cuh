@@ -230,7 +230,8 @@ YG_DEV bool team_barrier(Team& T) {
     return s_ok != 0;
 }
 
-YG_DEV double warp_sum(double v) {
+template <typename V>
+YG_DEV V warp_sum(V v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -238,27 +239,23 @@ YG_DEV double warp_sum(double v) {
 
 // All-reduce (sum) of nv <= YG_RED_MAX values over the team, deterministic
 // for a fixed launch shape. Every thread passes its partials; every thread
-// gets the totals. Also acts as a team barrier.
-YG_DEV bool team_allreduce_impl(Team& T, double* vals, int nv);
-YG_DEV bool team_allreduce(Team& T, double* vals, int nv) {
-    unsigned long long t0 = global_ns();
-    bool ok = team_allreduce_impl(T, vals, nv);
-    T.sync_ns += (double)(global_ns() - t0);
-    return ok;
-}
-YG_DEV bool team_allreduce_impl(Team& T, double* vals, int nv) {
+// gets the totals. Also acts as a team barrier. The warp-level sums run in the
+// partials' type V (FP32 partials of the mixed inner solve stay off the FP64
+// pipe); the CTA and team levels sum in FP64.
+template <typename V>
+YG_DEV bool team_allreduce_impl(Team& T, const V* in, double* out, int nv) {
     __shared__ double s_red[32][YG_RED_MAX];
     __shared__ double s_tot[YG_RED_MAX];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int k = 0; k < nv; k++) {
-        double w = warp_sum(vals[k]);
-        if (lane == 0) s_red[wid][k] = w;
+        V w = warp_sum<V>(in[k]);
+        if (lane == 0) s_red[wid][k] = (double)w;
     }
     __syncthreads();
     if (wid == 0) {
         for (int k = 0; k < nv; k++) {
             double w = (lane < nw) ? s_red[lane][k] : 0.0;
-            w = warp_sum(w);
+            w = warp_sum<double>(w);
             if (lane == 0) {
                 if (T.ncta > 1) T.ctl->slots[T.parity][T.cta][k] = w;
                 else s_tot[k] = w;
@@ -271,17 +268,25 @@ YG_DEV bool team_allreduce_impl(Team& T, double* vals, int nv) {
             for (int k = 0; k < nv; k++) {
                 double w = 0.0;
                 for (int c = lane; c < T.ncta; c += 32) w += __ldcg(&T.ctl->slots[T.parity][c][k]);
-                w = warp_sum(w);
+                w = warp_sum<double>(w);
                 if (lane == 0) s_tot[k] = w;
             }
         }
         T.parity ^= 1;
     }
     __syncthreads();
-    for (int k = 0; k < nv; k++) vals[k] = s_tot[k];
+    for (int k = 0; k < nv; k++) out[k] = s_tot[k];
     __syncthreads();
     return true;
 }
+template <typename V>
+YG_DEV bool team_allreduce_w(Team& T, const V* in, double* out, int nv) {
+    unsigned long long t0 = global_ns();
+    bool ok = team_allreduce_impl<V>(T, in, out, nv);
+    T.sync_ns += (double)(global_ns() - t0);
+    return ok;
+}
+YG_DEV bool team_allreduce(Team& T, double* vals, int nv) { return team_allreduce_w<double>(T, vals, vals, nv); }
 
 // Integer all-reduce helpers via the double path (exact for |v| < 2^53).
 YG_DEV bool team_allreduce_or_max(Team& T, double* vals, int nv) { return team_allreduce(T, vals, nv); }

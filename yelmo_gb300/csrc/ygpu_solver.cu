@@ -59,6 +59,26 @@ YG_DEV Geo make_geo(const Inst& I, const ygpu_dyn_par& P) {
     return G;
 }
 
+// Grid constants of the operators in the arithmetic T, converted once per
+// solve instead of once per row (a double -> float conversion runs on the FP64
+// pipe).
+template <typename T>
+struct OpK {
+    T dyodx, dxody, inv_dx, inv_dy, inv_dxdx, inv_dydy, inv_dxdy;
+};
+template <typename T>
+YG_DEV OpK<T> make_opk(const Geo& G) {
+    OpK<T> K;
+    K.dyodx = (T)G.dyodx;
+    K.dxody = (T)G.dxody;
+    K.inv_dx = T(1.0 / G.dx);
+    K.inv_dy = T(1.0 / G.dy);
+    K.inv_dxdx = T(1.0 / (G.dx * G.dx));
+    K.inv_dydy = T(1.0 / (G.dy * G.dy));
+    K.inv_dxdy = T(1.0 / (G.dx * G.dy));
+    return K;
+}
+
 // ---------------------------------------------------------------------------
 // Quadrature helpers (restated gq2D_to_nodes_*, see the oracle for the rule)
 // ---------------------------------------------------------------------------
@@ -403,8 +423,8 @@ YG_DEV float* shear_f32(const Inst& I, int axis) {
 
 // R = float (mixed mode): FP32 arithmetic, the FP64 output plus an FP32 copy
 // that the column pass reads
-template <typename R>
-__device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, const double* vcur) {
+template <typename R, typename VS>
+__device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, const VS* vcur) {
     const int nz = G.nz, n2 = G.n2;
     const double* f = I.f_ice;
     float* sx32 = shear_f32(I, 0);
@@ -436,9 +456,12 @@ __device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, c
 // Phase: column pass -- viscosity, relaxation, depth integrals, beta (aa)
 // R is the arithmetic of the viscosity (double: FP64 solve; float: mixed)
 // ---------------------------------------------------------------------------
-template <typename R>
+// VD is the storage of the new viscosity (double, or float for the FP32
+// working copy of the mixed mode); log(visc) is kept in R. vcur (the caller's
+// FP64 viscosity) is read only when no log is carried yet (first iteration).
+template <typename R, typename VD>
 __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T,
-                                          const double* vcur, double* vnew, const double* sdudx,
+                                          const double* vcur, VD* vnew, const double* sdudx,
                                           const double* sdudy, const double* sdvdx, const double* sdvdy, bool relax,
                                           bool diva, bool first_copy, bool have_log, bool visc_only = false) {
     const int nz = G.nz, n2 = G.n2;
@@ -449,8 +472,9 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
     const double* zeta = I.zeta;
     const double* f = I.f_ice;
     const int vm = P.visc_method;
-    // A^(-1/n) at the nodes: FP32 storage in the mixed mode
+    // A^(-1/n) at the nodes and log(visc): FP32 storage in the mixed mode
     const R* attp_r = (const R*)I.attp;
+    R* lv = (R*)I.lvis;
     for (int c = T.tid; c < n2; c += T.nthr) {
         Nb n = make_nb(G, c);
         if (first_copy) {
@@ -543,21 +567,20 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                 R ep = glen3 ? rcbrt(e) : pow(e, p1);
                 v = R(0.5) * ep * attp_r[ck];
             }
-            double vd;
+            R vr;
             if (relax) {
                 // picard_relax_visc in log space; log of the current viscosity carried between iterations
-                const R lc = have_log ? (R)I.lvis[ck] : log((R)vcur[ck]);
+                const R lc = have_log ? lv[ck] : log((R)vcur[ck]);
                 const R L = (R(1) - rel) * lc + rel * log(v);
-                vd = (double)exp(L);
-                I.lvis[ck] = (double)L;
+                vr = exp(L);
+                lv[ck] = L;
             } else {
-                vd = (double)v;
-                if (!visc_only) I.lvis[ck] = log(vd);
+                vr = v;
+                if (!visc_only) lv[ck] = log(vr);
             }
-            vnew[ck] = vd;
+            vnew[ck] = (VD)vr;
             // trapezoid integrals (integrate_trapezoid1D_pt, yelmo_tools.f90:1092-1122),
             // in the viscosity arithmetic R
-            const R vr = (R)vd;
             const R omz = (R)(1.0 - zeta[k]);
             const R g = (Hr / vr) * (omz * omz);
             if (k > 0) {
@@ -799,11 +822,11 @@ YG_DEV int dof_u(const Geo& G, int ii, int jj, int plane) {
 // around it: sum over the slots holding mm of H(l,:) . val(dofs). val(d) must
 // return 0 for d < 0.
 template <typename T, typename CT, typename V>
-YG_DEV T member_elems(const Geo& G, const CT* N, const CT* Nab, int mm, V val) {
+YG_DEV T member_elems(const Geo& G, const OpK<T>& K, const CT* N, const CT* Nab, int mm, V val) {
     const int pl = (mm >= G.n2) ? 1 : 0;
     const int c = mm - pl * G.n2;
     const int i = c % G.nx, j = c / G.nx;
-    const T dyodx = (T)G.dyodx, dxody = (T)G.dxody;
+    const T dyodx = K.dyodx, dxody = K.dxody;
     T acc = T(0);
     // cells: ux -> (i,j),(i+1,j); uy -> (i,j),(i,j+1)
 #pragma unroll
@@ -845,14 +868,15 @@ YG_DEV T member_elems(const Geo& G, const CT* N, const CT* Nab, int mm, V val) {
 // unknowns (no Dirichlet, tied or ghost columns) is the 9-point stencil
 // K = -A_residual * dx*dy (the identity the reference's test_ssa_energy pins).
 template <typename T, typename CT>
-YG_DEV T energy_row_fast(const Geo& G, const CT* N, const CT* Nab, const CT* dgx, const CT* dgy, const T* v, int u) {
+YG_DEV T energy_row_fast(const Geo& G, const OpK<T>& K, const CT* N, const CT* Nab, const CT* dgx, const CT* dgy,
+                         const T* v, int u) {
     const int nx = G.nx, ny = G.ny, n2 = G.n2;
     const int pl = (u >= n2) ? 1 : 0;
     const int c = u - pl * n2;
     const int i = c % nx, j = c / nx;
     const int im1 = (i == 0) ? nx - 1 : i - 1, ip1 = (i == nx - 1) ? 0 : i + 1;
     const int jm1 = (j == 0) ? ny - 1 : j - 1, jp1 = (j == ny - 1) ? 0 : j + 1;
-    const T dyodx = (T)G.dyodx, dxody = (T)G.dxody;
+    const T dyodx = K.dyodx, dxody = K.dxody;
     const T* U = v;
     const T* V = v + n2;
     if (pl == 0) {
@@ -884,14 +908,73 @@ YG_DEV T energy_row_fast(const Geo& G, const CT* N, const CT* Nab, const CT* dgx
     }
 }
 
+// Both rows of cell c = (i, j) on the interior stencil (the two rows of
+// energy_row_fast with the same arithmetic, sharing the index math and the
+// loads of N, N_ab and the velocities both rows read).
+template <typename T, typename CT>
+YG_DEV void energy_cell_fast(const Geo& G, const OpK<T>& K, const CT* N, const CT* Nab, const CT* dgx, const CT* dgy,
+                             const T* v, int c, int i, int j, T& yx, T& yy) {
+    const int nx = G.nx, ny = G.ny, n2 = G.n2;
+    const int im1 = (i == 0) ? nx - 1 : i - 1, ip1 = (i == nx - 1) ? 0 : i + 1;
+    const int jm1 = (j == 0) ? ny - 1 : j - 1, jp1 = (j == ny - 1) ? 0 : j + 1;
+    const T dyodx = K.dyodx, dxody = K.dxody;
+    const T* U = v;
+    const T* V = v + n2;
+    const int c_ip1 = ip1 + nx * j, c_im1 = im1 + nx * j, c_jp1 = i + nx * jp1, c_jm1 = i + nx * jm1;
+    const T Ni = (T)N[c], Npx = (T)N[c_ip1], Npy = (T)N[c_jp1];
+    const T Bc = (T)Nab[c], Bmx = (T)Nab[c_jm1], Bmy = (T)Nab[c_im1];
+    const T Uc = U[c], Vc = V[c];
+    const T U_ip1 = U[c_ip1], U_im1 = U[c_im1], U_jp1 = U[c_jp1], U_jm1 = U[c_jm1], U_im1jp1 = U[im1 + nx * jp1];
+    const T V_ip1 = V[c_ip1], V_im1 = V[c_im1], V_jp1 = V[c_jp1], V_jm1 = V[c_jm1], V_ip1jm1 = V[ip1 + nx * jm1];
+    {
+        const T Np = Npx, Bm = Bmx;
+        T y = (T(4) * dyodx * (Np + Ni) + dxody * (Bc + Bm) + (T)dgx[c]) * Uc;
+        y -= T(4) * dyodx * Np * U_ip1;
+        y -= T(4) * dyodx * Ni * U_im1;
+        y -= dxody * Bc * U_jp1;
+        y -= dxody * Bm * U_jm1;
+        y += (T(2) * Ni + Bc) * Vc;
+        y -= (T(2) * Np + Bc) * V_ip1;
+        y += (T(2) * Np + Bm) * V_ip1jm1;
+        y -= (T(2) * Ni + Bm) * V_jm1;
+        yx = y;
+    }
+    {
+        const T Np = Npy, Bm = Bmy;
+        T y = (T(4) * dxody * (Np + Ni) + dyodx * (Bc + Bm) + (T)dgy[c]) * Vc;
+        y -= T(4) * dxody * Np * V_jp1;
+        y -= T(4) * dxody * Ni * V_jm1;
+        y -= dyodx * Bc * V_ip1;
+        y -= dyodx * Bm * V_im1;
+        y += (T(2) * Ni + Bc) * Uc;
+        y -= (T(2) * Np + Bc) * U_jp1;
+        y += (T(2) * Np + Bm) * U_im1jp1;
+        y -= (T(2) * Ni + Bm) * U_im1;
+        yy = y;
+    }
+}
+
+template <typename T, typename CT>
+__device__ __noinline__ T energy_row_general(const Inst& I, const Geo& G, const OpK<T>& K, const CT* N,
+                                             const CT* Nab, const CT* dgx, const CT* dgy, const T* v, int u);
+
 // Row u of K v (identity on Dirichlet and tied rows)
 template <typename T, typename CT>
-YG_DEV T energy_row(const Inst& I, const Geo& G, const CT* N, const CT* Nab, const CT* dgx, const CT* dgy,
-                    const T* v, int u) {
+YG_DEV T energy_row(const Inst& I, const Geo& G, const OpK<T>& K, const CT* N, const CT* Nab, const CT* dgx,
+                    const CT* dgy, const T* v, int u) {
     // the interior stencil is evaluated for every row (its neighbour indices are
     // always in range), so its loads do not wait on the row-kind load
-    const T yf = energy_row_fast<T, CT>(G, N, Nab, dgx, dgy, v, u);
+    const T yf = energy_row_fast<T, CT>(G, K, N, Nab, dgx, dgy, v, u);
     if (I.rpart[u] == 1) return yf;
+    return energy_row_general<T, CT>(I, G, K, N, Nab, dgx, dgy, v, u);
+}
+
+// Row u of K v outside the interior stencil: Dirichlet and tied rows are the
+// identity; free rows sum the element derivatives of the unknown and of the
+// unknowns tied to it
+template <typename T, typename CT>
+__device__ __noinline__ T energy_row_general(const Inst& I, const Geo& G, const OpK<T>& K, const CT* N,
+                                             const CT* Nab, const CT* dgx, const CT* dgy, const T* v, int u) {
     if (I.ukind[u] != DOF_FREE) return v[u];
     const int* emap = I.emap;
     auto val = [&](int d) -> T {
@@ -901,13 +984,13 @@ YG_DEV T energy_row(const Inst& I, const Geo& G, const CT* N, const CT* Nab, con
     };
     const T vr = v[u];
     T acc = ((u < G.n2) ? (T)dgx[u] : (T)dgy[u - G.n2]) * vr;
-    acc += member_elems<T>(G, N, Nab, u, val);
+    acc += member_elems<T>(G, K, N, Nab, u, val);
     const int* mem = I.mem + 3 * u;
     for (int m = 0; m < 3; m++) {
         int mm = mem[m];
         if (mm < 0) break;
         acc += ((mm < G.n2) ? (T)dgx[mm] : (T)dgy[mm - G.n2]) * vr;
-        acc += member_elems<T>(G, N, Nab, mm, val);
+        acc += member_elems<T>(G, K, N, Nab, mm, val);
     }
     return acc;
 }
@@ -916,8 +999,8 @@ YG_DEV T energy_row(const Inst& I, const Geo& G, const CT* N, const CT* Nab, con
 // Residual operator (solver_ssa_ac.f90:73-848, matrix-free)
 // ---------------------------------------------------------------------------
 template <typename T, typename CT>
-YG_DEV T residual_row(const Inst& I, const Geo& G, const CT* N, const CT* Nab, const CT* dgx, const CT* dgy,
-                      const T* v, int u, T* diag_out) {
+YG_DEV T residual_row(const Inst& I, const Geo& G, const OpK<T>& K, const CT* N, const CT* Nab, const CT* dgx,
+                      const CT* dgy, const T* v, int u, T* diag_out) {
     const int rk = I.ukind[u];
     if (rk == RROW_ID) {
         if (diag_out) *diag_out = T(1);
@@ -933,8 +1016,8 @@ YG_DEV T residual_row(const Inst& I, const Geo& G, const CT* N, const CT* Nab, c
     const int i = c % nx, j = c / nx;
     const int im1 = (i == 0) ? nx - 1 : i - 1, ip1 = (i == nx - 1) ? 0 : i + 1;
     const int jm1 = (j == 0) ? ny - 1 : j - 1, jp1 = (j == ny - 1) ? 0 : j + 1;
-    const T inv_dx = T(1.0 / G.dx), inv_dy = T(1.0 / G.dy);
-    const T inv_dxdx = T(1.0 / (G.dx * G.dx)), inv_dydy = T(1.0 / (G.dy * G.dy)), inv_dxdy = T(1.0 / (G.dx * G.dy));
+    const T inv_dx = K.inv_dx, inv_dy = K.inv_dy;
+    const T inv_dxdx = K.inv_dxdx, inv_dydy = K.inv_dydy, inv_dxdy = K.inv_dxdy;
 #define VX(a, b) v[(a) + nx * (b)]
 #define VY(a, b) v[n2 + (a) + nx * (b)]
 #define NN(a, b) ((T)N[(a) + nx * (b)])
@@ -999,11 +1082,28 @@ YG_DEV T residual_row(const Inst& I, const Geo& G, const CT* N, const CT* Nab, c
 }
 
 template <typename T, typename CT>
-YG_DEV T operator_row(const Inst& I, const Geo& G, bool energy, const CT* N, const CT* Nab, const CT* dgx,
-                      const CT* dgy, const T* v, int u) {
-    if (energy) return energy_row<T, CT>(I, G, N, Nab, dgx, dgy, v, u);
-    return residual_row<T, CT>(I, G, N, Nab, dgx, dgy, v, u, nullptr);
+YG_DEV T operator_row(const Inst& I, const Geo& G, const OpK<T>& K, bool energy, const CT* N, const CT* Nab,
+                      const CT* dgx, const CT* dgy, const T* v, int u) {
+    if (energy) return energy_row<T, CT>(I, G, K, N, Nab, dgx, dgy, v, u);
+    return residual_row<T, CT>(I, G, K, N, Nab, dgx, dgy, v, u, nullptr);
 }
+
+// Cells c = first, first + stride, ... of an nx-wide grid with (i, j) kept
+// incrementally (no division per cell)
+struct CellWalk {
+    int c, i, j, di, dj, nx;
+    YG_DEV CellWalk(int first, int stride, int nx_) : c(first), i(first % nx_), j(first / nx_), di(stride % nx_),
+                                                      dj(stride / nx_), nx(nx_) {}
+    YG_DEV void next() {
+        c += di + dj * nx;
+        i += di;
+        j += dj;
+        if (i >= nx) {
+            i -= nx;
+            j++;
+        }
+    }
+};
 
 // Operator functors for the Krylov solvers: row(u, v) = (A v)_u
 template <typename T, typename CT>
@@ -1012,8 +1112,25 @@ struct StencilOp {
     const Geo* G;
     bool energy;
     const CT *N, *Nab, *dgx, *dgy;
-    YG_DEV T row(int u, const T* v) const { return operator_row<T, CT>(*I, *G, energy, N, Nab, dgx, dgy, v, u); }
-    // FP32: two rows per thread and trip, both rows' loads issued before either store
+    OpK<T> K;
+    YG_DEV T row(int u, const T* v) const { return operator_row<T, CT>(*I, *G, K, energy, N, Nab, dgx, dgy, v, u); }
+    YG_DEV int nx() const { return G->nx; }
+    YG_DEV int n2() const { return G->n2; }
+    // both rows of cell c = (i, j): ux row c and uy row n2 + c
+    YG_DEV void cell(int c, int i, int j, const T* v, T& y0, T& y1) const {
+        const int n2 = G->n2;
+        if (energy) {
+            energy_cell_fast<T, CT>(*G, K, N, Nab, dgx, dgy, v, c, i, j, y0, y1);
+            if (I->rpart[c] != 1) y0 = energy_row_general<T, CT>(*I, *G, K, N, Nab, dgx, dgy, v, c);
+            if (I->rpart[n2 + c] != 1) y1 = energy_row_general<T, CT>(*I, *G, K, N, Nab, dgx, dgy, v, n2 + c);
+        } else {
+            y0 = residual_row<T, CT>(*I, *G, K, N, Nab, dgx, dgy, v, c, nullptr);
+            y1 = residual_row<T, CT>(*I, *G, K, N, Nab, dgx, dgy, v, n2 + c, nullptr);
+        }
+    }
+    // y = A v. Row k belongs to thread k mod nthr, as in the callers' vector
+    // loops that read y right after without a barrier. FP32: two rows per
+    // thread and trip, both rows' loads issued before either store.
     YG_DEV void operator()(Team& Tm, const T* v, T* y) const {
         const int nu = G->nu;
         if (sizeof(T) != sizeof(float)) {
@@ -1223,6 +1340,7 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
     const bool drag = (P.ssa_vel_lim_method == YGPU_VEL_LIM_DRAG);
     const int n2 = G.n2, nx = G.nx, ny = G.ny;
     const double* N = I.visc_int;
+    const OpK<double> K64 = make_opk<double>(G);
     double bn2 = 0.0;
     for (int u = T.tid; u < G.nu; u += T.nthr) {
         const int pl = (u >= n2) ? 1 : 0, c = u - pl * n2;
@@ -1257,12 +1375,12 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
                         if (dd < 0) return 0.0;
                         return (I.ukind[dd] == DOF_DIR) ? I.dval[dd] : 0.0;
                     };
-                    b = b - member_elems<double>(G, N, I.Nab, mm, lift);
+                    b = b - member_elems<double>(G, K64, N, I.Nab, mm, lift);
                     auto unit = [&](int dd) -> double {
                         if (dd < 0) return 0.0;
                         return (I.emap[dd] == u) ? 1.0 : 0.0;
                     };
-                    d = d + (mpl ? I.drag_y[mc] : I.drag_x[mc]) + member_elems<double>(G, N, I.Nab, mm, unit);
+                    d = d + (mpl ? I.drag_y[mc] : I.drag_x[mc]) + member_elems<double>(G, K64, N, I.Nab, mm, unit);
                 }
                 x0 = uval;
             }
@@ -1278,13 +1396,13 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
             } else if (rk == RROW_FRONT) {
                 b = pl ? I.taul_y[c] : I.taul_x[c];
                 x0 = uval;
-                residual_row<double, double>(I, G, N, I.Nab, I.drag_x, I.drag_y, I.x, u, &d);
+                residual_row<double, double>(I, G, K64, N, I.Nab, I.drag_x, I.drag_y, I.x, u, &d);
             } else {
                 const double w = (mask == 4) ? 0.5 : 1.0;
                 double lr = drag ? w * (pl ? I.lr_y[c] : I.lr_x[c]) : 0.0;
                 b = (pl ? I.taud_y[c] : I.taud_x[c]) - lr;
                 x0 = uval;
-                residual_row<double, double>(I, G, N, I.Nab, I.drag_x, I.drag_y, I.x, u, &d);
+                residual_row<double, double>(I, G, K64, N, I.Nab, I.drag_x, I.drag_y, I.x, u, &d);
             }
         }
         if (P.lin_initx_zeros) x0 = 0.0;
@@ -1398,8 +1516,11 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             a1 += wk * uk;
             a2 += rk * rk;
         }
-        double red[3] = {(double)a0, (double)a1, (double)a2};
-        if (!(ok = team_allreduce(Tm, red, 3))) return YGPU_ERR_TIMEOUT;
+        double red[3];
+        {
+            const T part[3] = {a0, a1, a2};
+            if (!(ok = team_allreduce_w<T>(Tm, part, red, 3))) return YGPU_ERR_TIMEOUT;
+        }
         // lead thread: gam_old / alpha_old of the recurrence
         double gam_old = 1.0, alpha_old = 1.0;
         if (lead) {
@@ -1431,9 +1552,9 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             a0 = a1 = a2 = T(0);
             // one row's loads (operator row, nine vectors, preconditioner)
             struct RowIn { T n, m, z, q, s, p, x, r, u, w, mi; };
-            auto load = [&](int k) {
+            auto load = [&](int k, T nk) {
                 RowIn R;
-                R.n = A.row(k, mc);
+                R.n = nk;
                 R.m = mc[k]; R.z = z[k]; R.q = q[k]; R.s = s[k]; R.p = p[k];
                 R.x = x[k]; R.r = r[k]; R.u = u[k]; R.w = w[k]; R.mi = Mi(k);
                 return R;
@@ -1454,23 +1575,30 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
                 a1 += wk * uk;
                 a2 += rk * rk;
             };
+            // one cell per thread and trip: both of its rows' loads (the shared
+            // stencil loads included) precede either row's stores. Rows c and
+            // n2 + c belong to the thread of cell c here; every use of these
+            // vectors with the row-k-per-thread-k mapping (restart, true
+            // residual, the caller) follows a team all-reduce.
             if (sizeof(T) == sizeof(float)) {
-                // FP32: two rows per thread and trip, both rows' loads before
-                // either row's stores (FP64 keeps one row: register budget)
-                for (int k0 = Tm.tid; k0 < nu; k0 += 2 * Tm.nthr) {
-                    const int k1 = k0 + Tm.nthr;
-                    const bool h1 = k1 < nu;
-                    const RowIn R0 = load(k0);
-                    const RowIn R1 = load(h1 ? k1 : k0);
-                    update(k0, R0);
-                    if (h1) update(k1, R1);
+                const int n2 = A.n2();
+                for (CellWalk cw(Tm.tid, Tm.nthr, A.nx()); cw.c < n2; cw.next()) {
+                    T y0, y1;
+                    A.cell(cw.c, cw.i, cw.j, mc, y0, y1);
+                    const RowIn R0 = load(cw.c, y0);
+                    const RowIn R1 = load(n2 + cw.c, y1);
+                    update(cw.c, R0);
+                    update(n2 + cw.c, R1);
                 }
             } else {
-                for (int k = Tm.tid; k < nu; k += Tm.nthr) update(k, load(k));
+                // FP64: one row per trip (the two-row body exceeds the register budget)
+                for (int k = Tm.tid; k < nu; k += Tm.nthr) update(k, load(k, A.row(k, mc)));
             }
             it++;
-            red[0] = (double)a0; red[1] = (double)a1; red[2] = (double)a2;
-            if (!(ok = team_allreduce(Tm, red, 3))) return YGPU_ERR_TIMEOUT;
+            {
+                const T part[3] = {a0, a1, a2};
+                if (!(ok = team_allreduce_w<T>(Tm, part, red, 3))) return YGPU_ERR_TIMEOUT;
+            }
             { T* t = mc; mc = mn; mn = t; }
             if (lead) {
                 const double rel = sqrt(red[2]) / bnrm;
@@ -1543,8 +1671,8 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
         p[u] = T(0);
         a0 += ru * ru;
     }
-    double red[2] = {(double)a0, 0.0};
-    if (!(ok = team_allreduce(Tm, red, 1))) return YGPU_ERR_TIMEOUT;
+    double red[2] = {0.0, 0.0};
+    if (!(ok = team_allreduce_w<T>(Tm, &a0, red, 1))) return YGPU_ERR_TIMEOUT;
     // lead-thread state of the recurrence
     double rho = red[0], rho_old = 1.0, alpha = 1.0, omega = 1.0;     // (rt, r) with rt = r
     if (lead) {
@@ -1576,8 +1704,8 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
         A(Tm, ph, v);
         T tvp = T(0);
         for (int u = Tm.tid; u < nu; u += Tm.nthr) tvp += rt[u] * v[u];
-        double tv = (double)tvp;
-        if (!(ok = team_allreduce(Tm, &tv, 1))) return YGPU_ERR_TIMEOUT;
+        double tv = 0.0;
+        if (!(ok = team_allreduce_w<T>(Tm, &tvp, &tv, 1))) return YGPU_ERR_TIMEOUT;
         if (lead) {
             if (tv == 0.0 || !isfinite(tv)) s_flag = 2;
             else {
@@ -1596,8 +1724,8 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
             sh[u] = precond ? (T)dinv[u] * su : su;
             ssp += su * su;
         }
-        double ss = (double)ssp;
-        if (!(ok = team_allreduce(Tm, &ss, 1))) return YGPU_ERR_TIMEOUT;
+        double ss = 0.0;
+        if (!(ok = team_allreduce_w<T>(Tm, &ssp, &ss, 1))) return YGPU_ERR_TIMEOUT;
         if (lead) {
             s_sc[3] = sqrt(ss) / bnrm;
             s_flag = (s_sc[3] <= tol) ? 1 : 0;
@@ -1616,8 +1744,11 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
             ts0 += tu * s[u];
             ts1 += tu * tu;
         }
-        double ts[2] = {(double)ts0, (double)ts1};
-        if (!(ok = team_allreduce(Tm, ts, 2))) return YGPU_ERR_TIMEOUT;
+        double ts[2];
+        {
+            const T part[2] = {ts0, ts1};
+            if (!(ok = team_allreduce_w<T>(Tm, part, ts, 2))) return YGPU_ERR_TIMEOUT;
+        }
         if (lead) {
             if (ts[1] == 0.0 || !isfinite(ts[1])) s_flag = 2;
             else {
@@ -1637,8 +1768,11 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
             rr0 += ru * ru;
             rr1 += rt[u] * ru;
         }
-        double rr[2] = {(double)rr0, (double)rr1};
-        if (!(ok = team_allreduce(Tm, rr, 2))) return YGPU_ERR_TIMEOUT;
+        double rr[2];
+        {
+            const T part[2] = {rr0, rr1};
+            if (!(ok = team_allreduce_w<T>(Tm, part, rr, 2))) return YGPU_ERR_TIMEOUT;
+        }
         if (lead) {
             s_sc[3] = sqrt(rr[0]) / bnrm;
             s_flag = (s_sc[3] <= tol) ? 1 : ((omega == 0.0) ? 2 : 0);
@@ -1663,7 +1797,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
     // MINRES requests run CG on the symmetric energy system, BiCGSTAB on the residual one
     const bool use_cg = energy ? (P.lin_solver != YGPU_LIN_BICGSTAB) : false;
     outer = 0;
-    const StencilOp<double, double> A64{&I, &G, energy, I.visc_int, I.Nab, I.drag_x, I.drag_y};
+    const StencilOp<double, double> A64{&I, &G, energy, I.visc_int, I.Nab, I.drag_x, I.drag_y, make_opk<double>(G)};
     if (P.precision != YGPU_PREC_MIXED) {
         if (use_cg)
             return krylov_pcg_pipe<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.rt, I.v, I.ph, I.m2, I.z, I.q, I.s,
@@ -1671,7 +1805,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         return krylov_bicgstab<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.rt, I.p, I.v, I.s, I.t, I.ph, I.sh,
                                        P.lin_maxiter, P.lin_tol, bnrm, pre, iters, relres, ok);
     }
-    const StencilOp<float, float> A32{&I, &G, energy, I.fN, I.fNab, I.fdrag_x, I.fdrag_y};
+    const StencilOp<float, float> A32{&I, &G, energy, I.fN, I.fNab, I.fdrag_x, I.fdrag_y, make_opk<float>(G)};
     // ---- mixed: FP32 coefficients, FP32 inner Krylov, FP64 outer residual ----
     for (int c = T.tid; c < G.n2; c += T.nthr) {
         I.fN[c] = (float)I.visc_int[c];
@@ -1928,6 +2062,14 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
     const int in_alt = out->in_alt;
     double* vcur = in_alt ? I.visc_alt : I.visc;
     double* vnew = in_alt ? I.visc : I.visc_alt;
+    // mixed mode: FP32 working copies of the viscosity in the visc_alt storage
+    // (current one: vf[in_alt] from the second iteration on; the first reads
+    // the caller's FP64 viscosity)
+    const bool mixed = (P.precision == YGPU_PREC_MIXED);
+    float* vf0 = (float*)I.visc_alt;
+    float* vf1 = vf0 + (size_t)G.n2 * G.nz;
+    const float* vcur_f = in_alt ? vf1 : vf0;
+    float* vnew_f = in_alt ? vf0 : vf1;
     const bool relax = diva ? true : (P.visc_method != 0);
     PhaseClock clk;
     clk.start();
@@ -1937,16 +2079,17 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
     if (P.visc_method == 1 || diva) {
         if (P.visc_method == 1) phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
         if (diva) {
-            if (P.precision == YGPU_PREC_MIXED) phase_shear<float>(I, G, T, vcur);
-            else phase_shear<double>(I, G, T, vcur);
+            if (!mixed) phase_shear<double, double>(I, G, T, vcur);
+            else if (iter == 1) phase_shear<float, double>(I, G, T, I.visc);
+            else phase_shear<float, float>(I, G, T, vcur_f);
         }
         if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
     }
     t1 = clk.lap();
-    if (P.precision == YGPU_PREC_MIXED)
-        phase_column<float>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
+    if (mixed)
+        phase_column<float, float>(I, P, G, T, I.visc, vnew_f, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
     else
-        phase_column<double>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
+        phase_column<double, double>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
     if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
     t2 = clk.lap();
     phase_faces(I, P, G, T, diva);
@@ -2009,6 +2152,18 @@ __device__ __noinline__ void step_krylov(const Inst& I, const ygpu_dyn_par& P, T
 // passes after the Picard loop (also for ssa_iter_max = 0)
 __device__ __noinline__ bool final_passes(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, bool diva,
                                           int in_alt, bool looped) {
+    if (P.precision == YGPU_PREC_MIXED) {
+        // the final FP32 viscosity goes to the caller's FP64 array first; the
+        // passes below then read it there
+        if (looped) {
+            const size_t n3 = (size_t)G.n2 * G.nz;
+            const float* vf = (const float*)I.visc_alt + (in_alt ? n3 : 0);
+            for (size_t k = T.tid; k < n3; k += T.nthr) I.visc[k] = (double)vf[k];
+            if (!team_barrier(T)) return false;
+        }
+        in_alt = 0;
+        looped = false;
+    }
     double* vcur = in_alt ? I.visc_alt : I.visc;
     // viscosity of the last linear system (before the last update)
     const double* vlast = looped ? (in_alt ? I.visc : I.visc_alt) : vcur;
@@ -2037,7 +2192,7 @@ __device__ __noinline__ bool final_passes(const Inst& I, const ygpu_dyn_par& P, 
         P1.precision = YGPU_PREC_FP64;     // the diagnostic pass reads FP64 powers
         phase_att_powers(I, P1, G, T);
         if (!team_barrier(T)) return false;
-        phase_column<double>(I, P1, G, T, vcur, vcur, sdudx, sdudy, sdvdx, sdvdy, false, false, false, false, true);
+        phase_column<double, double>(I, P1, G, T, vcur, vcur, sdudx, sdudy, sdvdx, sdvdy, false, false, false, false, true);
         if (!team_barrier(T)) return false;
     }
     // the caller's visc_eff must hold the final viscosity
