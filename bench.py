@@ -318,7 +318,8 @@ def main():
     devs = [gpu.to_device(f, f"cuda:{local}") for f in hosts]
     pristine = [{k: d[k].clone() for k in gpu.STATE_NAMES} for d in devs]
     fields = [gpu.make_fields(d, i.nx, i.ny, i.nz, i.dx, i.dx, i.n_glen) for d, i in zip(devs, insts)]
-    solver = gpu.DeviceSolver(local)
+    solver = gpu.DeviceSolver(local)          # batched steps
+    solver1 = gpu.DeviceSolver(local)         # single-solve latency
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     def reset(idx):
@@ -335,14 +336,20 @@ def main():
 
     res = {}
     clocks = None
+    tuned = {}
+    from yelmo_gb300.autotune import autotune
     for prec in ("fp64", "mixed"):
         par = insts[0].par.with_(precision=prec)
+        # launch tuning by measurement (untimed): the batch, and the single solve
+        tb = autotune(solver, kind, par, fields, lambda: reset(range(batch)))
+        t1 = None if ensemble else autotune(solver1, kind, par, fields[:1], lambda: reset([0]))
+        tuned[prec] = {"batch": tb["tuning"], "single": t1["tuning"] if t1 else None}
         # single-solve latency (instance 0)
         lat, st1 = [], None
         n_single = 0 if ensemble else args.warmup + args.steps
         for s in range(n_single):
             reset([0])
-            st1 = solver.solve(kind, par, fields[0])
+            st1 = solver1.solve(kind, par, fields[0])
             if s >= args.warmup:
                 lat.append(st1["device_ms"])
         u_single = None if ensemble else devs[0]["ux_bar" if kind == abi.KIND_DIVA else "ux_b"].cpu().numpy().reshape(
@@ -458,12 +465,14 @@ def main():
                      "alg_bytes_per_launch": alg_steps["krylov"] / max(kr_n, 1),
                      "avg_launch_ms": kr_ms / max(kr_n, 1), "peak_source": peak_src},
         "step_kernels": per_step,
+        "tuning": tuned,
         "phase_ms_single": mixed["st1"]["phase_ms"] if mixed["st1"] else None,
         "clocks": clocks,
         "cpu_baseline": cpu_base,
     }
     print(json.dumps(line))
     solver.close()
+    solver1.close()
     if dist is not None:
         dist.destroy_process_group()
 

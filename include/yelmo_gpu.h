@@ -274,6 +274,22 @@ void*     ygpu_ctx_stream(ygpu_ctx* ctx);
 #define YGPU_KIND_SSA   0
 #define YGPU_KIND_DIVA  1
 
+/*
+ * Launch tuning of a context (no counterpart in the reference): how often the
+ * host checks for finished solves, whether each chunk of Picard iterations
+ * between checks runs as one CUDA graph (captured once per launch shape and
+ * parameters, then replayed), and the team size (unknowns per CTA of a solve;
+ * smaller teams synchronise faster, larger ones have more threads per row).
+ * yelmo_gb300/autotune.py picks these by measurement for a workload.
+ */
+typedef struct ygpu_tuning {
+    int check_every;            /* Picard iterations between host checks (1..64), default 4 */
+    int use_graphs;             /* 1: chunk graphs (default), 0: one launch per step        */
+    int unknowns_per_cta;       /* team sizing, default 512                                 */
+} ygpu_tuning;
+void ygpu_tuning_defaults(ygpu_tuning* t);
+int  ygpu_ctx_set_tuning(ygpu_ctx* ctx, const ygpu_tuning* t);
+
 /* One solve on device-resident fields; enqueued on the context stream and
    synchronised before return (stats filled). */
 int ygpu_solve_device(ygpu_ctx* ctx, int kind, const ygpu_dyn_par* par,

@@ -49,3 +49,40 @@ def test_batch_equals_single(precision):
                 assert e <= 1e-6, (k, name, e)
     finally:
         solver.close()
+
+
+def test_graph_chunks_equal_step_launches():
+    """Chunks of Picard iterations replayed as CUDA graphs give the same bits as
+    one launch per step, with the same number of kernel launches counted."""
+    torch = pytest.importorskip("torch")
+    insts = _instances(5)
+    par = insts[0].par.with_(precision="mixed")
+    out = {}
+    for graphs in (False, True):
+        solver = gpu.DeviceSolver(0)
+        try:
+            solver.set_tuning(check_every=4, use_graphs=graphs, unknowns_per_cta=512)
+            devs, fields = zip(*[_device(inst) for inst in insts])
+            torch.cuda.synchronize()
+            n0 = gpu.kernel_launches()
+            sts = solver.solve_batch(abi.KIND_SSA, par, list(fields))
+            n1 = gpu.kernel_launches()
+            assert all(st["status"] == 0 for st in sts)
+            out[graphs] = ([d["ux_b"].cpu().numpy() for d in devs], [st["ssa_iter_now"] for st in sts], n1 - n0)
+        finally:
+            solver.close()
+    for a, b in zip(out[False][0], out[True][0]):
+        np.testing.assert_array_equal(a, b)
+    assert out[False][1] == out[True][1]
+    assert out[False][2] == out[True][2] > 0
+
+
+def test_tuning_rejects_out_of_range():
+    solver = gpu.DeviceSolver(0)
+    try:
+        with pytest.raises(gpu.YgpuError):
+            solver.set_tuning(check_every=0)
+        with pytest.raises(gpu.YgpuError):
+            solver.set_tuning(unknowns_per_cta=1)
+    finally:
+        solver.close()

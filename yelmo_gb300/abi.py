@@ -89,6 +89,11 @@ class Fields(C.Structure):
         "ATT", "zeta_aa", "z_sl", "z_bed", "z_srf")]
 
 
+class Tuning(C.Structure):
+    """ygpu_tuning."""
+    _fields_ = [("check_every", C.c_int), ("use_graphs", C.c_int), ("unknowns_per_cta", C.c_int)]
+
+
 class ServerCfg(C.Structure):
     """ygpu_server_cfg."""
     _fields_ = [

@@ -1,0 +1,61 @@
+"""Launch autotuner: picks a context's tuning (team size, host-check interval,
+chunk graphs) for a workload by timing a fixed number of Picard iterations of
+its batched solve under each candidate.
+
+    best = autotune(solver, kind, par, fields, reset)
+
+``fields`` are the device fields of the batch (gpu.make_fields), ``reset()``
+restores their state between trials (the solves update it in place). Every
+trial runs exactly ``iters`` Picard iterations (no convergence exit), so the
+trials do equal work. The chosen tuning is left set on the solver.
+"""
+from __future__ import annotations
+
+import itertools
+import time
+
+DEFAULT_GRID = {
+    "unknowns_per_cta": (256, 512, 1024, 2048),
+    "check_every": (4, 8),
+    "use_graphs": (True,),
+}
+
+
+def autotune(solver, kind: int, par, fields: list, reset, iters: int = 8, grid: dict | None = None,
+             reps: int = 1) -> dict:
+    import torch
+    grid = grid or DEFAULT_GRID
+    trial_par = par.with_(ssa_iter_max=iters, ssa_iter_conv=0.0)
+    results = []
+    keys = list(grid)
+    for values in itertools.product(*(grid[k] for k in keys)):
+        cand = dict(zip(keys, values))
+        solver.set_tuning(**cand)
+        best = float("inf")
+        for _ in range(reps + 1):          # the first run captures the chunk graph
+            reset()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            solver.solve_batch(kind, trial_par, fields)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        results.append((best, cand))
+    results.sort(key=lambda r: r[0])
+    best_t, best = results[0]
+    # graphs on/off at the chosen shape
+    for g in (False,):
+        cand = dict(best, use_graphs=g)
+        solver.set_tuning(**cand)
+        t = float("inf")
+        for _ in range(reps + 1):
+            reset()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            solver.solve_batch(kind, trial_par, fields)
+            torch.cuda.synchronize()
+            t = min(t, time.perf_counter() - t0)
+        if t < best_t:
+            best_t, best = t, cand
+    solver.set_tuning(**best)
+    return {"tuning": best, "trial_ms": best_t * 1e3, "iters": iters,
+            "candidates": [{"ms": r[0] * 1e3, **r[1]} for r in results]}

@@ -166,6 +166,11 @@ struct ygpu_ctx {
     int ctl_cap = 0;
     int* d_map = nullptr;           // team plan of a batch (ygpu_plan_teams)
     int map_cap = 0;
+    GraphCache graph;               // chunk graph of the last launch shape
+    bool use_graphs = true;
+    int check_every = 4;            // Picard iterations between host checks
+    int unknowns_per_cta = 0;       // team size: unknowns per CTA (0: 2 x block)
+    int* h_flags = nullptr;         // pinned: finished count, abort flag
     int* d_misc = nullptr;          // [0] queue, [1] abort, [2..3] csr out
     double* d_miscd = nullptr;
     int max_ctas = 0;
@@ -189,12 +194,34 @@ static int grow(char** p, size_t* cap, size_t need) {
     return YGPU_OK;
 }
 
+extern "C" void ygpu_tuning_defaults(ygpu_tuning* t) {
+    if (!t) return;
+    t->check_every = 4;
+    t->use_graphs = 1;
+    t->unknowns_per_cta = 2 * YG_BLOCK;
+}
+
+extern "C" int ygpu_ctx_set_tuning(ygpu_ctx* c, const ygpu_tuning* t) {
+    if (!c || !t) { ygpu_set_error("NULL argument"); return YGPU_ERR_BAD_ARG; }
+    if (t->check_every < 1 || t->check_every > 64 || t->unknowns_per_cta < 32 || t->unknowns_per_cta > (1 << 20)) {
+        ygpu_set_error("tuning out of range: check_every %d (1..64), unknowns_per_cta %d (32..2^20)", t->check_every,
+                       t->unknowns_per_cta);
+        return YGPU_ERR_BAD_ARG;
+    }
+    c->check_every = t->check_every;
+    c->use_graphs = (t->use_graphs != 0);
+    c->unknowns_per_cta = t->unknowns_per_cta;
+    ygpu_graph_cache_clear(&c->graph);
+    return YGPU_OK;
+}
+
 extern "C" ygpu_ctx* ygpu_ctx_create(int device) {
     ygpu_ctx* c = new ygpu_ctx();
     c->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreate(&c->e0) != cudaSuccess || cudaEventCreate(&c->e1) != cudaSuccess ||
-        cudaMalloc((void**)&c->d_misc, 64) != cudaSuccess || cudaMalloc((void**)&c->d_miscd, 64) != cudaSuccess) {
+        cudaMalloc((void**)&c->d_misc, 64) != cudaSuccess || cudaMalloc((void**)&c->d_miscd, 64) != cudaSuccess ||
+        cudaMallocHost((void**)&c->h_flags, 2 * sizeof(int)) != cudaSuccess) {
         ygpu_set_error("context creation on device %d failed: %s", device, cudaGetErrorString(cudaGetLastError()));
         delete c;
         return nullptr;
@@ -219,6 +246,8 @@ extern "C" void ygpu_ctx_destroy(ygpu_ctx* c) {
     cudaFree(c->d_out);
     cudaFree(c->d_ctl);
     cudaFree(c->d_map);
+    ygpu_graph_cache_clear(&c->graph);
+    if (c->h_flags) cudaFreeHost(c->h_flags);
     cudaFree(c->d_misc);
     cudaFree(c->d_miscd);
     if (c->e0) cudaEventDestroy(c->e0);
@@ -335,8 +364,9 @@ void ygpu_fill_inst(Inst& I, int kind, const ygpu_fields* f) {
     I.z_sl = f->z_sl; I.z_bed = f->z_bed;
 }
 
-int ygpu_single_team_ctas(int max_ctas, size_t nu) {
-    int want = (int)((nu + 2 * YG_BLOCK - 1) / (2 * YG_BLOCK));
+int ygpu_single_team_ctas(int max_ctas, size_t nu, int unknowns_per_cta) {
+    const int upc = unknowns_per_cta > 0 ? unknowns_per_cta : 2 * YG_BLOCK;
+    int want = (int)((nu + upc - 1) / upc);
     const char* v = getenv("YGPU_TEAM_CTAS");
     int tc = (v && *v) ? atoi(v) : want;
     if (tc < 1) tc = 1;
@@ -351,11 +381,11 @@ static int env_int(const char* name, int dflt) {
 }
 
 // Launch shape of a batch: (n_teams, team_ctas).
-void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, int* team_ctas) {
+void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, int* team_ctas, int upc) {
     int maxc = max_ctas > 0 ? max_ctas : 1;
     if (n_inst == 1) {
         // one team over the GPU, sized to the instance
-        *team_ctas = ygpu_single_team_ctas(maxc, max_nu);
+        *team_ctas = ygpu_single_team_ctas(maxc, max_nu, upc);
         *n_teams = 1;
         return;
     }
@@ -376,12 +406,12 @@ void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, in
     *n_teams = nt;
 }
 
-bool ygpu_plan_teams(int max_ctas, int n, const size_t* nu, std::vector<int>& map, int* grid) {
+bool ygpu_plan_teams(int max_ctas, int n, const size_t* nu, std::vector<int>& map, int* grid, int upc) {
     if (n < 1 || n > max_ctas) return false;
     if (const char* v = getenv("YGPU_UNIFORM_TEAMS"))
         if (*v && atoi(v) != 0) return false;
     std::vector<int> cnt(n, 1), cap(n);
-    for (int q = 0; q < n; q++) cap[q] = ygpu_single_team_ctas(max_ctas, nu[q]);
+    for (int q = 0; q < n; q++) cap[q] = ygpu_single_team_ctas(max_ctas, nu[q], upc);
     // greedy: the next CTA goes to the instance with the most unknowns per CTA
     std::priority_queue<std::pair<double, int>> pq;
     for (int q = 0; q < n; q++)
@@ -436,7 +466,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
         c->insts_cap = n;
     }
     int n_teams, team_ctas;
-    ygpu_choose_teams(c->max_ctas, n, max_nu, &n_teams, &team_ctas);
+    ygpu_choose_teams(c->max_ctas, n, max_nu, &n_teams, &team_ctas, c->unknowns_per_cta);
     // queue order: largest instance first (longest-processing-time first)
     std::vector<int> order(n);
     for (int k = 0; k < n; k++) order[k] = k;
@@ -449,7 +479,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     for (int q = 0; q < n; q++) nus[q] = (size_t)2 * inst[order[q]].nx * inst[order[q]].ny;
     std::vector<int> map;
     int map_grid = 0;
-    const bool mapped = n > 1 && ygpu_plan_teams(c->max_ctas, n, nus.data(), map, &map_grid);
+    const bool mapped = n > 1 && ygpu_plan_teams(c->max_ctas, n, nus.data(), map, &map_grid, c->unknowns_per_cta);
     const int n_ctl = mapped ? n : n_teams;
     if (c->ctl_cap < n_ctl) {
         cudaFree(c->d_ctl);
@@ -477,7 +507,8 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     CK(cudaMemsetAsync(c->d_out, 0, sizeof(InstOut) * (size_t)n, c->stream));
     CK(cudaEventRecord(c->e0, c->stream));
     st = ygpu_launch_solver(c->device, c->stream, c->d_insts, n, *par, c->d_ctl, n_ctl, team_ctas, c->d_misc,
-                            c->d_misc + 1, mapped ? c->d_map : nullptr, map_grid);
+                            c->d_misc + 1, mapped ? c->d_map : nullptr, map_grid, c->use_graphs ? &c->graph : nullptr,
+                            c->h_flags, c->check_every);
     if (st) return st;
     CK(cudaEventRecord(c->e1, c->stream));
     c->h_out.resize(n);

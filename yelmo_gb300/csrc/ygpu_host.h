@@ -17,9 +17,7 @@ struct TeamCtl;
 void ygpu_set_error(const char* fmt, ...);
 
 // ygpu_solver.cu
-int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
-                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort,
-                       const int* d_map = nullptr, int map_grid = 0);
+
 int ygpu_solver_max_ctas(int device);
 
 // Step kernels of the Picard loop (one cooperative launch each)
@@ -39,9 +37,43 @@ int ygpu_step_shape_mapped(int device, int grid, const int* d_map, StepShape* sh
 // CTAs per instance in proportion to its unknowns (at least one, at most its
 // single-solve team); false when the instances outnumber max_ctas. map gets
 // the layout run_step reads: [grid] CTA -> instance, then (first, count) pairs.
-bool ygpu_plan_teams(int max_ctas, int n_inst, const size_t* nu, std::vector<int>& map, int* grid);
+bool ygpu_plan_teams(int max_ctas, int n_inst, const size_t* nu, std::vector<int>& map, int* grid,
+                     int unknowns_per_cta = 0);
 int ygpu_launch_step(int step, cudaStream_t s, const StepShape& sh, const Inst* d_insts, int n_inst,
                      const ygpu_dyn_par& P, TeamCtl* ctls, int* d_done, int* d_abort);
+
+// A CUDA graph of one chunk of Picard iterations, reused while the key matches.
+struct GraphKey {
+    const Inst* insts;
+    int n_inst;
+    StepShape sh;
+    ygpu_dyn_par P;
+    TeamCtl* ctls;
+    int *done, *abort_;
+    int check;
+    int* h_flags;
+    bool timed;                    // step timing events inside the graph
+};
+struct GraphEvents {
+    cudaEvent_t a, b;
+    int kind;
+};
+struct GraphCache {
+    bool valid = false;
+    GraphKey key;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<GraphEvents> ev;   // event pairs of the timed launches
+};
+void ygpu_step_timing_add(int kind, double ms);
+void ygpu_graph_cache_clear(GraphCache* gc);
+bool ygpu_step_timing_on();
+
+// The whole solve of n_inst instances on `stream`: setup, the Picard loop as
+// step launches (or chunk graphs with gc and pinned h_flags[2]), final passes.
+int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
+                       TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort,
+                       const int* d_map = nullptr, int map_grid = 0, GraphCache* gc = nullptr,
+                       int* h_flags = nullptr, int check_every = 4);
 int ygpu_sm_count(int device);
 size_t ygpu_teamctl_bytes();
 size_t ygpu_inst_bytes();
@@ -65,5 +97,5 @@ void ygpu_fill_inst(Inst& I, int kind, const ygpu_fields* f);
 size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed);
 void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed);
 size_t ygpu_align256(size_t b);
-int ygpu_single_team_ctas(int max_ctas, size_t nu);
-void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, int* team_ctas);
+int ygpu_single_team_ctas(int max_ctas, size_t nu, int unknowns_per_cta = 0);
+void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, int* team_ctas, int upc = 0);

@@ -21,6 +21,7 @@
 //               error matrix, basal stress and basal velocity
 #include <cuda_runtime.h>
 #include <stdlib.h>
+#include <string.h>
 #include <vector>
 #include <mutex>
 #include <atomic>
@@ -2578,6 +2579,13 @@ void ygpu_step_timing_flush() {
     g_timer.pending.swap(keep);
 }
 
+void ygpu_step_timing_add(int kind, double ms) {
+    std::lock_guard<std::mutex> lk(g_timer.mu);
+    if (!g_timer.on || kind < 0 || kind >= 5) return;
+    g_timer.ms[kind] += ms;
+    g_timer.n[kind] += 1;
+}
+
 extern "C" void ygpu_step_timing_get(double ms[5], long long count[5]) {
     ygpu_step_timing_flush();
     std::lock_guard<std::mutex> lk(g_timer.mu);
@@ -2632,9 +2640,71 @@ static int launch_step_raw(int step, cudaStream_t s, const StepShape& sh, const 
     }
 }
 
+bool ygpu_step_timing_on() {
+    std::lock_guard<std::mutex> lk(g_timer.mu);
+    return g_timer.on;
+}
+
+void ygpu_graph_cache_clear(GraphCache* gc) {
+    if (!gc) return;
+    if (gc->exec) cudaGraphExecDestroy(gc->exec);
+    for (auto& e : gc->ev) {
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    gc->ev.clear();
+    gc->exec = nullptr;
+    gc->valid = false;
+}
+
+// Captures `iters` Picard iterations (pre / Krylov / post launches) and the
+// read-back of the finished count and abort flag into pinned host memory as
+// one CUDA graph. Returns false (nothing captured, stream usable) on failure.
+// With step timing on, every launch is bracketed by event-record nodes whose
+// times are read after each replay.
+static bool capture_chunk(cudaStream_t stream, const StepShape& sh, const Inst* d_insts, int n_inst,
+                          const ygpu_dyn_par& P, TeamCtl* d_ctls, int* d_done, int* d_abort, int iters,
+                          int* h_flags, GraphCache* gc, bool timed) {
+    if (timed) {
+        for (int k = 0; k < 3 * iters; k++) {
+            GraphEvents e{nullptr, nullptr, YG_STEP_PRE + k % 3};
+            if (cudaEventCreate(&e.a) != cudaSuccess || cudaEventCreate(&e.b) != cudaSuccess) {
+                cudaGetLastError();
+                if (e.a) cudaEventDestroy(e.a);
+                if (e.b) cudaEventDestroy(e.b);
+                return false;
+            }
+            gc->ev.push_back(e);
+        }
+    }
+    cudaGraphExec_t* exec = &gc->exec;
+    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    bool ok = true;
+    int k = 0;
+    for (int it = 0; it < iters && ok; it++)
+        for (int step : {YG_STEP_PRE, YG_STEP_KRYLOV, YG_STEP_POST}) {
+            if (ok && timed) ok = cudaEventRecord(gc->ev[k].a, stream) == cudaSuccess;
+            if (ok) ok = (launch_step_raw(step, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort) == YGPU_OK);
+            if (ok && timed) ok = cudaEventRecord(gc->ev[k].b, stream) == cudaSuccess;
+            k++;
+        }
+    if (ok) ok = cudaMemcpyAsync(h_flags, d_done, sizeof(int), cudaMemcpyDeviceToHost, stream) == cudaSuccess;
+    if (ok) ok = cudaMemcpyAsync(h_flags + 1, d_abort, sizeof(int), cudaMemcpyDeviceToHost, stream) == cudaSuccess;
+    cudaGraph_t g = nullptr;
+    const bool ended = cudaStreamEndCapture(stream, &g) == cudaSuccess;
+    ok = ok && ended && g;
+    if (ok) ok = cudaGraphInstantiate(exec, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return ok;
+}
+
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
                        TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort, const int* d_map,
-                       int map_grid) {
+                       int map_grid, GraphCache* gc, int* h_flags, int check_every) {
     // d_done: count of finished instances; d_abort: launch-wide abort flag.
     // With a team map (one team per instance) n_teams is the number of control
     // blocks to clear (n_inst) and map_grid the CTAs of the plan.
@@ -2649,9 +2719,52 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
     if (st) return st;
     if ((st = ygpu_launch_step(YG_STEP_SETUP, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort))) return st;
     // Picard iterations: one pre / Krylov / post launch each; the host reads the
-    // count of finished instances every few iterations
-    const int check = 4;
-    for (int it = 0; it < P.ssa_iter_max; it++) {
+    // count of finished instances every `check` iterations. With a graph cache
+    // and pinned flags, each chunk of `check` iterations is one CUDA graph
+    // (captured once per launch shape and parameters, then replayed).
+    const int check = check_every > 0 ? check_every : 4;
+    const bool use_graph = gc && h_flags && P.ssa_iter_max >= check;
+    const bool timed = ygpu_step_timing_on();
+    if (use_graph) {
+        GraphKey key;
+        memset(&key, 0, sizeof(key));
+        key.insts = d_insts; key.n_inst = n_inst; key.sh = sh; key.ctls = d_ctls;
+        memcpy(&key.P, &P, sizeof(P));   // bytes, padding included, for the memcmp below
+        key.done = d_done; key.abort_ = d_abort; key.check = check; key.h_flags = h_flags;
+        key.timed = timed;
+        if (!gc->valid || memcmp(&gc->key, &key, sizeof(key)) != 0) {
+            ygpu_graph_cache_clear(gc);
+            if (capture_chunk(stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort, check, h_flags, gc, timed)) {
+                memcpy(&gc->key, &key, sizeof(key));
+                gc->valid = true;
+            } else {
+                ygpu_graph_cache_clear(gc);
+            }
+        }
+    }
+    int it = 0;
+    if (use_graph && gc->valid) {
+        // whole chunks as graph replays
+        while (it + check <= P.ssa_iter_max) {
+            if (cudaGraphLaunch(gc->exec, stream) != cudaSuccess || cudaStreamSynchronize(stream) != cudaSuccess) {
+                ygpu_set_error("solver graph failed: %s", cudaGetErrorString(cudaGetLastError()));
+                return YGPU_ERR_CUDA;
+            }
+            ygpu_count_launches(3ull * check);
+            if (timed)
+                for (const GraphEvents& e : gc->ev) {
+                    float ms = 0.f;
+                    if (cudaEventElapsedTime(&ms, e.a, e.b) == cudaSuccess) ygpu_step_timing_add(e.kind, ms);
+                    cudaGetLastError();
+                }
+            it += check;
+            if (h_flags[0] >= n_inst || h_flags[1]) {
+                it = P.ssa_iter_max;
+                break;
+            }
+        }
+    }
+    for (; it < P.ssa_iter_max; it++) {
         for (int step : {YG_STEP_PRE, YG_STEP_KRYLOV, YG_STEP_POST})
             if ((st = ygpu_launch_step(step, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort))) return st;
         if ((it + 1) % check == 0 || it + 1 == P.ssa_iter_max) {

@@ -35,7 +35,8 @@ EXPORTS = [
     "ygpu_solve_device", "ygpu_solve_batch_device", "ygpu_solve_device_noalloc",
     "ygpu_server_create", "ygpu_server_destroy", "ygpu_server_add_member", "ygpu_server_submit",
     "ygpu_server_poll", "ygpu_server_wait", "ygpu_server_fetch", "ygpu_server_get_info",
-    "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get",
+    "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get", "ygpu_tuning_defaults",
+    "ygpu_ctx_set_tuning",
 ]
 
 
@@ -88,6 +89,8 @@ def lib(build_if_missing: bool = True):
     L.ygpu_server_fetch.argtypes = [C.c_void_p, C.c_int, C.c_int, dp]
     L.ygpu_server_get_info.argtypes = [C.c_void_p, C.POINTER(abi.ServerInfo)]
     L.ygpu_kernel_launches.restype = C.c_ulonglong
+    L.ygpu_tuning_defaults.argtypes = [C.POINTER(abi.Tuning)]
+    L.ygpu_ctx_set_tuning.argtypes = [C.c_void_p, C.POINTER(abi.Tuning)]
     L.ygpu_step_timing.argtypes = [C.c_int]
     L.ygpu_step_timing_get.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     _lib = L
@@ -229,6 +232,13 @@ class DeviceSolver:
         out = st.as_dict()
         out["return"] = r
         return out
+
+    def set_tuning(self, check_every: int = 4, use_graphs: bool = True, unknowns_per_cta: int = 512):
+        """ygpu_ctx_set_tuning: host-check interval, chunk graphs, team size."""
+        t = abi.Tuning(check_every, 1 if use_graphs else 0, unknowns_per_cta)
+        _check(self.L.ygpu_ctx_set_tuning(self.ctx, C.byref(t)))
+        self.tuning = {"check_every": check_every, "use_graphs": bool(use_graphs),
+                       "unknowns_per_cta": unknowns_per_cta}
 
     def solve_batch(self, kind: int, par: YdynParams, fields: list) -> list:
         n = len(fields)
