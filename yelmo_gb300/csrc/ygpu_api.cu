@@ -277,7 +277,9 @@ static ygpu_ctx* default_ctx() {
 size_t ygpu_align256(size_t b) { return (b + 255) & ~(size_t)255; }
 static size_t al(size_t b) { return ygpu_align256(b); }
 
-size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed) {
+static size_t tile_blocks(int nx, int ny) { return (size_t)((nx + 3) / 4) * ((ny + 3) / 4); }
+
+size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block) {
     size_t n2 = (size_t)nx * ny, nu = 2 * n2, n3 = n2 * nz;
     size_t b = al(n3 * 8);               // visc_alt
     b += al(4 * n3 * 8) + al(n3 * 8);    // attp, lvis
@@ -285,10 +287,11 @@ size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed) {
     b += 15 * al(nu * 8);                // linear system
     b += 6 * al(nu * 4);                 // ukind, emap, mem(3), rpart
     if (mixed) b += 4 * al(n2 * 4) + 13 * al(nu * 4);
+    if (mixed && block) b += al(tile_blocks(nx, ny) * 1024 * 4);
     return b;
 }
 
-void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed) {
+void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed, bool block) {
     size_t n2 = (size_t)nx * ny, nu = 2 * n2, n3 = n2 * nz;
     char* p = base;
     auto D = [&](size_t n) { double* r = (double*)p; p += al(n * 8); return r; };
@@ -310,7 +313,9 @@ void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool m
         I.fdinv = Fv(nu); I.fx = Fv(nu); I.fr = Fv(nu); I.fp = Fv(nu); I.fq = Fv(nu); I.fz = Fv(nu);
         I.frt = Fv(nu); I.fv = Fv(nu); I.fs = Fv(nu); I.ft = Fv(nu); I.fph = Fv(nu); I.fsh = Fv(nu);
         I.fm2 = Fv(nu);
+        I.fminv = block ? Fv(tile_blocks(nx, ny) * 1024) : nullptr;
     } else {
+        I.fminv = nullptr;
         I.fN = I.fNab = I.fdrag_x = I.fdrag_y = I.fdinv = nullptr;
         I.fx = I.fr = I.fp = I.fq = I.fz = I.frt = I.fv = I.fs = I.ft = I.fph = I.fsh = I.fm2 = nullptr;
     }
@@ -452,7 +457,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     size_t total = 0, max_nu = 0;
     for (int k = 0; k < n; k++) {
         off[k] = total;
-        total += al(ygpu_inst_scratch_bytes(inst[k].nx, inst[k].ny, inst[k].nz, mixed));
+        total += al(ygpu_inst_scratch_bytes(inst[k].nx, inst[k].ny, inst[k].nz, mixed, ygpu_wants_block(*par)));
         max_nu = std::max(max_nu, (size_t)2 * inst[k].nx * inst[k].ny);
     }
     if ((st = grow(&c->arena, &c->arena_cap, total))) return st;
@@ -500,7 +505,8 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
         const int k = order[q];
         Inst& I = c->h_insts[q];
         ygpu_fill_inst(I, kind, &inst[k]);
-        ygpu_inst_scratch_carve(I, c->arena + off[k], inst[k].nx, inst[k].ny, inst[k].nz, mixed);
+        ygpu_inst_scratch_carve(I, c->arena + off[k], inst[k].nx, inst[k].ny, inst[k].nz, mixed,
+                                ygpu_wants_block(*par));
         I.out = c->d_out + k;      // outputs stay in caller order
     }
     CK(cudaMemcpyAsync(c->d_insts, c->h_insts.data(), sizeof(Inst) * (size_t)n, cudaMemcpyHostToDevice, c->stream));

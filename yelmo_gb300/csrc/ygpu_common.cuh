@@ -141,6 +141,7 @@ struct Inst {
     int *ukind, *emap, *mem, *rpart;
     // mixed precision scratch (nu entries; coefficient copies n2)
     float *fN, *fNab, *fdrag_x, *fdrag_y, *fdinv;
+    float* fminv;                  // mixed, block preconditioner: inverse of each 4x4-cell tile block (32x32)
     float *fx, *fr, *fp, *fq, *fz, *frt, *fv, *fs, *ft, *fph, *fsh, *fm2;
     InstOut* out;
     int visc_final_in_alt;         // set by the kernel: final visc is in visc_alt

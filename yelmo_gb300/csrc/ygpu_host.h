@@ -94,8 +94,12 @@ struct ygpu_fields;
 int ygpu_check_par(const ygpu_dyn_par* p);
 int ygpu_fields_check(int kind, const ygpu_fields* f);
 void ygpu_fill_inst(Inst& I, int kind, const ygpu_fields* f);
-size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed);
-void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed);
+// block: scratch for the tile-block preconditioner (mixed mode, -p ilu)
+size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block = false);
+void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed, bool block = false);
+inline bool ygpu_wants_block(const ygpu_dyn_par& p) {
+    return p.precision == YGPU_PREC_MIXED && p.lin_precond == YGPU_PRE_ILU0 && p.ssa_solver == YGPU_SSA_ENERGY;
+}
 size_t ygpu_align256(size_t b);
 int ygpu_single_team_ctas(int max_ctas, size_t nu, int unknowns_per_cta = 0);
 void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, int* team_ctas, int upc = 0);

@@ -95,7 +95,7 @@ extern "C" int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, cons
     const size_t off_ctl = ygpu_align256(off_out + sizeof(InstOut));
     const size_t off_misc = ygpu_align256(off_ctl + ygpu_teamctl_bytes());
     const size_t off_arena = ygpu_align256(off_misc + 2 * sizeof(int));
-    const size_t need = off_arena + ygpu_inst_scratch_bytes(f->nx, f->ny, f->nz, mixed);
+    const size_t need = off_arena + ygpu_inst_scratch_bytes(f->nx, f->ny, f->nz, mixed, ygpu_wants_block(*par));
     if (need > (size_t)YGPU_NOALLOC_SCRATCH_BYTES) {
         ygpu_set_error("instance %dx%dx%d needs %zu bytes of scratch, more than the %zu of the "
                        "allocation-free entry point (use ygpu_solve_device)",
@@ -105,7 +105,7 @@ extern "C" int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, cons
     char* base = S->base;
     Inst h;
     ygpu_fill_inst(h, kind, f);
-    ygpu_inst_scratch_carve(h, base + off_arena, f->nx, f->ny, f->nz, mixed);
+    ygpu_inst_scratch_carve(h, base + off_arena, f->nx, f->ny, f->nz, mixed, ygpu_wants_block(*par));
     InstOut* d_out = (InstOut*)(base + off_out);
     h.out = d_out;
     Inst* d_inst = (Inst*)(base + off_inst);

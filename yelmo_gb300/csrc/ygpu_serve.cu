@@ -108,6 +108,7 @@ struct ygpu_server {
     int max_ctas = 1;
     int max_slots = 1;
     bool mixed = false;
+    bool block = false;            // tile-block preconditioner scratch
     size_t held = 0;               // device bytes held
     std::deque<Member> members;
     std::deque<Request> requests;  // index = request id; references stay valid on growth
@@ -185,14 +186,14 @@ static std::vector<Admit> admit_locked(ygpu_server* S) {
     std::vector<Admit> got;
     const size_t need_max = [&] {
         size_t m = 0;
-        for (const Member& M : S->members) m = std::max(m, ygpu_inst_scratch_bytes(M.nx, M.ny, M.nz, S->mixed));
+        for (const Member& M : S->members) m = std::max(m, ygpu_inst_scratch_bytes(M.nx, M.ny, M.nz, S->mixed, S->block));
         return m;
     }();
     for (auto it = S->waiting.begin(); it != S->waiting.end();) {
         Request& R = S->requests[*it];
         Member& M = S->members[R.member];
         if (M.busy) { ++it; continue; }
-        const size_t need = ygpu_inst_scratch_bytes(M.nx, M.ny, M.nz, S->mixed);
+        const size_t need = ygpu_inst_scratch_bytes(M.nx, M.ny, M.nz, S->mixed, S->block);
         int s = -1;
         for (int k = 0; k < (int)S->slots.size(); k++)
             if (S->slots[k].req < 0 && S->slots[k].bytes >= need) { s = k; break; }
@@ -226,7 +227,7 @@ static std::vector<Admit> admit_locked(ygpu_server* S) {
         R.t_admit = now_s();
         R.step = M.steps++;
         ygpu_fill_inst(sl.inst, S->cfg.kind, &M.f);
-        ygpu_inst_scratch_carve(sl.inst, sl.scratch, M.nx, M.ny, M.nz, S->mixed);
+        ygpu_inst_scratch_carve(sl.inst, sl.scratch, M.nx, M.ny, M.nz, S->mixed, S->block);
         sl.inst.out = S->d_out + s;
         const unsigned long long key = smix_host(R.seed) ^
                                        smix_host(0x5851F42D4C957F2Dull * ((unsigned long long)R.member + 1)) ^
@@ -415,6 +416,7 @@ extern "C" ygpu_server* ygpu_server_create(const ygpu_server_cfg* cfg) {
     ygpu_server* S = new ygpu_server();
     S->cfg = *cfg;
     S->mixed = (cfg->par.precision == YGPU_PREC_MIXED);
+    S->block = ygpu_wants_block(cfg->par);
     S->max_ctas = ygpu_solver_max_ctas(cfg->device);
     if (S->max_ctas < 1 || ygpu_init_constants(cfg->device)) {
         ygpu_set_error("solver kernels cannot be resident on device %d", cfg->device);
@@ -508,7 +510,7 @@ extern "C" int ygpu_server_add_member(ygpu_server* S, const ygpu_fields* h, int*
         if (!q) { ygpu_set_error("a member input (H_ice, z_bed, z_sl, c_bed, f_slide, ATT, zeta_aa) is NULL"); return YGPU_ERR_BAD_ARG; }
     const int kind = S->cfg.kind;
     const size_t bytes = member_bytes(kind, h->nx, h->ny, h->nz);
-    const size_t scratch = ygpu_inst_scratch_bytes(h->nx, h->ny, h->nz, S->mixed);
+    const size_t scratch = ygpu_inst_scratch_bytes(h->nx, h->ny, h->nz, S->mixed, S->block);
     std::lock_guard<std::mutex> lk(S->mu);
     if (!S->fatal.empty()) { ygpu_set_error("server stopped: %s", S->fatal.c_str()); return YGPU_ERR_CUDA; }
     // the member and, if no slot exists yet, one slot for it must fit the budget

@@ -1789,6 +1789,333 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
 }
 
 // ---------------------------------------------------------------------------
+// Block preconditioner on C-grid tiles (the GPU form of LIS's -p ilu: block
+// Jacobi, each block the exact inverse of a 4 x 4-cell tile of the operator)
+//
+// A tile holds the 32 unknowns of 16 cells; lane l of a warp owns unknown
+// (cell l/2 of the tile, component l%2): cell (4 tx + (l/2)%4, 4 ty + l/8),
+// ux for even l, uy for odd l. The tile block keeps the couplings of free rows
+// to free columns inside the tile (Dirichlet, tied and out-of-grid rows are
+// identity rows), so it is symmetric for the energy operator; Gauss-Jordan in
+// registers (lane j holds column j) inverts it, and the inverse is stored
+// column-major: minv[t*1024 + k*32 + l] = (block^-1)[l][k]. Applying it is a
+// 32 x 32 matrix-vector product per warp through shuffles.
+// ---------------------------------------------------------------------------
+#define YG_TILE 4
+
+YG_DEV int tile_count(const Geo& G) { return ((G.nx + YG_TILE - 1) / YG_TILE) * ((G.ny + YG_TILE - 1) / YG_TILE); }
+
+// unknown of lane l in tile t, or -1 outside the grid
+YG_DEV int tile_unknown(const Geo& G, int t, int l) {
+    const int ntx = (G.nx + YG_TILE - 1) / YG_TILE;
+    const int tx = t % ntx, ty = t / ntx;
+    const int cl = l >> 1;
+    const int i = tx * YG_TILE + (cl & 3), j = ty * YG_TILE + (cl >> 2);
+    if (i >= G.nx || j >= G.ny) return -1;
+    return ((l & 1) ? G.n2 : 0) + i + G.nx * j;
+}
+
+// lane of unknown u inside tile t, or -1 when u is in another tile
+YG_DEV int tile_lane(const Geo& G, int t, int u) {
+    const int pl = (u >= G.n2) ? 1 : 0;
+    const int c = u - pl * G.n2;
+    const int i = c % G.nx, j = c / G.nx;
+    const int ntx = (G.nx + YG_TILE - 1) / YG_TILE;
+    if ((i / YG_TILE) + ntx * (j / YG_TILE) != t) return -1;
+    return 2 * ((i % YG_TILE) + YG_TILE * (j % YG_TILE)) + pl;
+}
+
+// coefficient of free column col in free row u outside the interior stencil
+// (energy_row_general applied to the unit vector of col)
+template <typename T, typename CT>
+__device__ __noinline__ T energy_coef_general(const Inst& I, const Geo& G, const OpK<T>& K, const CT* N,
+                                              const CT* Nab, const CT* dgx, const CT* dgy, int u, int col) {
+    const int* emap = I.emap;
+    auto unit = [&](int d) -> T { return (d >= 0 && emap[d] == col) ? T(1) : T(0); };
+    const T vr = (u == col) ? T(1) : T(0);
+    T acc = ((u < G.n2) ? (T)dgx[u] : (T)dgy[u - G.n2]) * vr;
+    acc += member_elems<T>(G, K, N, Nab, u, unit);
+    const int* mem = I.mem + 3 * u;
+    for (int m = 0; m < 3; m++) {
+        int mm = mem[m];
+        if (mm < 0) break;
+        acc += ((mm < G.n2) ? (T)dgx[mm] : (T)dgy[mm - G.n2]) * vr;
+        acc += member_elems<T>(G, K, N, Nab, mm, unit);
+    }
+    return acc;
+}
+
+// Builds and inverts every tile block of the energy operator A (team-wide, one
+// warp per tile). The row of each lane goes through the tile's inverse storage
+// (row-major) to reach the lanes that hold the columns.
+template <typename T, typename CT>
+__device__ __noinline__ void block_setup(const Inst& I, const Geo& G, Team& Tm, const StencilOp<T, CT>& A, T* minv) {
+    const int lane = threadIdx.x & 31;
+    const int gw = Tm.tid >> 5, nw = Tm.nthr >> 5;
+    const int nt = tile_count(G);
+    const int nx = G.nx, ny = G.ny, n2 = G.n2;
+    for (int t = gw; t < nt; t += nw) {
+        T* M = minv + (size_t)t * 1024;
+        const int u = tile_unknown(G, t, lane);
+        // row of this lane: zero, then its in-tile couplings
+        for (int k = 0; k < 32; k++) M[lane * 32 + k] = T(0);
+        if (u < 0 || I.ukind[u] != DOF_FREE) {
+            M[lane * 32 + lane] = T(1);
+        } else {
+            const int pl = (u >= n2) ? 1 : 0;
+            const int c = u - pl * n2;
+            const int i = c % nx, j = c / nx;
+            const int im1 = (i == 0) ? nx - 1 : i - 1, ip1 = (i == nx - 1) ? 0 : i + 1;
+            const int jm1 = (j == 0) ? ny - 1 : j - 1, jp1 = (j == ny - 1) ? 0 : j + 1;
+            // the nine columns of the row's stencil and, on the interior stencil, their coefficients
+            int col[9];
+            T cf[9];
+            const bool fast = (I.rpart[u] == 1);
+            const T dyodx = A.K.dyodx, dxody = A.K.dxody;
+            if (pl == 0) {
+                col[0] = c; col[1] = ip1 + nx * j; col[2] = im1 + nx * j; col[3] = i + nx * jp1; col[4] = i + nx * jm1;
+                col[5] = n2 + c; col[6] = n2 + ip1 + nx * j; col[7] = n2 + ip1 + nx * jm1; col[8] = n2 + i + nx * jm1;
+                if (fast) {
+                    const T Ni = (T)A.N[c], Np = (T)A.N[ip1 + nx * j], Bc = (T)A.Nab[c], Bm = (T)A.Nab[i + nx * jm1];
+                    cf[0] = T(4) * dyodx * (Np + Ni) + dxody * (Bc + Bm) + (T)A.dgx[c];
+                    cf[1] = -T(4) * dyodx * Np; cf[2] = -T(4) * dyodx * Ni;
+                    cf[3] = -dxody * Bc; cf[4] = -dxody * Bm;
+                    cf[5] = T(2) * Ni + Bc; cf[6] = -(T(2) * Np + Bc); cf[7] = T(2) * Np + Bm; cf[8] = -(T(2) * Ni + Bm);
+                }
+            } else {
+                col[0] = u; col[1] = n2 + i + nx * jp1; col[2] = n2 + i + nx * jm1; col[3] = n2 + ip1 + nx * j;
+                col[4] = n2 + im1 + nx * j;
+                col[5] = c; col[6] = i + nx * jp1; col[7] = im1 + nx * jp1; col[8] = im1 + nx * j;
+                if (fast) {
+                    const T Ni = (T)A.N[c], Np = (T)A.N[i + nx * jp1], Bc = (T)A.Nab[c], Bm = (T)A.Nab[im1 + nx * j];
+                    cf[0] = T(4) * dxody * (Np + Ni) + dyodx * (Bc + Bm) + (T)A.dgy[c];
+                    cf[1] = -T(4) * dxody * Np; cf[2] = -T(4) * dxody * Ni;
+                    cf[3] = -dyodx * Bc; cf[4] = -dyodx * Bm;
+                    cf[5] = T(2) * Ni + Bc; cf[6] = -(T(2) * Np + Bc); cf[7] = T(2) * Np + Bm; cf[8] = -(T(2) * Ni + Bm);
+                }
+            }
+#pragma unroll 1
+            for (int q = 0; q < 9; q++) {
+                const int cu = col[q];
+                const int cl = tile_lane(G, t, cu);
+                if (cl < 0 || I.ukind[cu] != DOF_FREE) continue;
+                const T v = fast ? cf[q] : energy_coef_general<T, CT>(I, G, A.K, A.N, A.Nab, A.dgx, A.dgy, u, cu);
+                M[lane * 32 + cl] += v;
+            }
+        }
+        __syncwarp();
+        // symmetric diagonal scaling S B S (S = |diag|^-1/2) before the FP32
+        // inversion: the viscosity contrast of the ice makes the raw blocks far
+        // worse conditioned than the scaled ones
+        const T dl = M[lane * 32 + lane];
+        const T sl = (dl > T(0) && isfinite(dl)) ? T(1) / sqrt(dl) : T(1);
+        // lane j takes column j of the scaled block, and column j of the identity
+        T a[32], x[32];
+#pragma unroll
+        for (int r = 0; r < 32; r++) {
+            const T sr = __shfl_sync(0xffffffffu, sl, r);
+            a[r] = sr * M[r * 32 + lane] * sl;
+            x[r] = (r == lane) ? T(1) : T(0);
+        }
+        __syncwarp();
+        // Gauss-Jordan without pivoting (symmetric positive definite blocks). A
+        // pivot below 1e-5 of its original diagonal (a tile block that is
+        // singular on its own, e.g. a floating tile without basal drag, whose
+        // rigid translations have no energy inside the tile) or a non-finite one
+        // turns the whole tile into Jacobi.
+        const T d0 = a[lane];
+        bool bad = false;
+#pragma unroll
+        for (int k = 0; k < 32; k++) {
+            const T p = __shfl_sync(0xffffffffu, a[k], k);
+            const T dk = __shfl_sync(0xffffffffu, d0, k);
+            if (!(p > T(1e-5) * fabs(dk)) || !isfinite(p)) bad = true;
+            const T ip = bad ? T(0) : T(1) / p;
+            a[k] *= ip;
+            x[k] *= ip;
+#pragma unroll
+            for (int r = 0; r < 32; r++) {
+                if (r == k) continue;
+                const T f = __shfl_sync(0xffffffffu, a[r], k);     // A[r][k]
+                a[r] -= f * a[k];
+                x[r] -= f * x[k];
+            }
+        }
+        bad = __any_sync(0xffffffffu, bad);
+        if (bad) {
+#pragma unroll
+            for (int r = 0; r < 32; r++) x[r] = T(0);
+            x[lane] = T(1);       // unscaled below: 1/d, or 1 where the diagonal is not positive
+        }
+        // column `lane` of the inverse S (SBS)^-1 S, column-major: element
+        // (r, lane) at lane * 32 + r
+#pragma unroll
+        for (int r = 0; r < 32; r++) {
+            const T sr = __shfl_sync(0xffffffffu, sl, r);
+            M[lane * 32 + r] = sr * x[r] * sl;
+        }
+        __syncwarp();
+    }
+}
+
+// out = M^-1 in for the whole team (tile mapping; the caller separates it from
+// row-mapped loops by team barriers)
+template <typename T>
+YG_DEV T block_apply_lane(const T* M, T w, int lane) {
+    T acc = T(0);
+#pragma unroll
+    for (int k = 0; k < 32; k++) acc += M[k * 32 + lane] * __shfl_sync(0xffffffffu, w, k);
+    return acc;
+}
+
+// Pipelined CG (as krylov_pcg_pipe) with the tile-block preconditioner: every
+// loop runs over tiles, one warp per tile and one unknown per lane, so the
+// preconditioner is applied to a tile's freshly computed vector through warp
+// shuffles in the same pass.
+template <typename T, typename Op>
+__device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op& A, const T* __restrict__ minv,
+                                                T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
+                                                T* __restrict__ u, T* __restrict__ w, T* m0, T* m1, T* __restrict__ z,
+                                                T* __restrict__ q, T* __restrict__ s, T* __restrict__ p, int maxiter,
+                                                double tol, double bnrm, int& iters, double& relres, bool& ok) {
+    __shared__ double s_ab[3];
+    __shared__ int s_flag;
+    const bool lead = (threadIdx.x == 0);
+    const int lane = threadIdx.x & 31, gw = Tm.tid >> 5, nw = Tm.nthr >> 5, nt = tile_count(G);
+    ok = true;
+    iters = 0;
+    int it = 0;
+    for (int restart = 0; restart < 8; restart++) {
+        // r = b - A x, u = M r
+        for (int t = gw; t < nt; t += nw) {
+            const int k = tile_unknown(G, t, lane);
+            const T rk = (k >= 0) ? b[k] - A.row(k, x) : T(0);
+            const T uk = block_apply_lane(minv + (size_t)t * 1024, rk, lane);
+            if (k >= 0) { r[k] = rk; u[k] = uk; }
+        }
+        if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
+        // w = A u, m = M w, partial dots
+        T a0 = T(0), a1 = T(0), a2 = T(0);
+        for (int t = gw; t < nt; t += nw) {
+            const int k = tile_unknown(G, t, lane);
+            const T wk = (k >= 0) ? A.row(k, u) : T(0);
+            const T mk = block_apply_lane(minv + (size_t)t * 1024, wk, lane);
+            if (k >= 0) {
+                w[k] = wk;
+                m0[k] = mk;
+                z[k] = T(0); q[k] = T(0); s[k] = T(0); p[k] = T(0);
+                const T rk = r[k], uk = u[k];
+                a0 += rk * uk;
+                a1 += wk * uk;
+                a2 += rk * rk;
+            }
+        }
+        double red[3];
+        {
+            const T part[3] = {a0, a1, a2};
+            if (!(ok = team_allreduce_w<T>(Tm, part, red, 3))) return YGPU_ERR_TIMEOUT;
+        }
+        double gam_old = 1.0, alpha_old = 1.0;
+        if (lead) {
+            const double rel = sqrt(red[2]) / bnrm;
+            s_ab[2] = rel;
+            if (rel <= tol) s_flag = 1;
+            else {
+                const double gam = red[0], del = red[1];
+                const double alpha = gam / del;
+                if (!isfinite(alpha) || del == 0.0) s_flag = 2;
+                else {
+                    s_flag = 0;
+                    s_ab[0] = alpha;
+                    s_ab[1] = 0.0;
+                    gam_old = gam;
+                    alpha_old = alpha;
+                }
+            }
+        }
+        __syncthreads();
+        relres = s_ab[2];
+        if (s_flag == 1) { iters = it; return YGPU_OK; }
+        if (s_flag == 2) { iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
+        T* mc = m0;
+        T* mn = m1;
+        bool recheck = false;
+        while (it < maxiter) {
+            const T a = (T)s_ab[0], bt = (T)s_ab[1];
+            a0 = a1 = a2 = T(0);
+            for (int t = gw; t < nt; t += nw) {
+                const int k = tile_unknown(G, t, lane);
+                T wk = T(0);
+                if (k >= 0) {
+                    const T nk = A.row(k, mc);
+                    const T zk = nk + bt * z[k];
+                    const T qk = mc[k] + bt * q[k];
+                    const T sk = w[k] + bt * s[k];
+                    const T pk = u[k] + bt * p[k];
+                    z[k] = zk; q[k] = qk; s[k] = sk; p[k] = pk;
+                    x[k] = x[k] + a * pk;
+                    const T rk = r[k] - a * sk;
+                    const T uk = u[k] - a * qk;
+                    wk = w[k] - a * zk;
+                    r[k] = rk; u[k] = uk; w[k] = wk;
+                    a0 += rk * uk;
+                    a1 += wk * uk;
+                    a2 += rk * rk;
+                }
+                const T mk = block_apply_lane(minv + (size_t)t * 1024, wk, lane);
+                if (k >= 0) mn[k] = mk;
+            }
+            it++;
+            {
+                const T part[3] = {a0, a1, a2};
+                if (!(ok = team_allreduce_w<T>(Tm, part, red, 3))) return YGPU_ERR_TIMEOUT;
+            }
+            { T* tt = mc; mc = mn; mn = tt; }
+            if (lead) {
+                const double rel = sqrt(red[2]) / bnrm;
+                s_ab[2] = rel;
+                if (!isfinite(rel)) s_flag = 2;
+                else if (rel <= tol) s_flag = 1;
+                else {
+                    const double gam = red[0], del = red[1];
+                    const double beta = gam / gam_old;
+                    const double alpha = gam / (del - beta * gam / alpha_old);
+                    if (!isfinite(alpha) || !isfinite(beta) || del == 0.0) s_flag = 3;
+                    else {
+                        s_flag = 0;
+                        s_ab[0] = alpha;
+                        s_ab[1] = beta;
+                        gam_old = gam;
+                        alpha_old = alpha;
+                    }
+                }
+            }
+            __syncthreads();
+            const int flag = s_flag;
+            relres = s_ab[2];
+            if (flag == 2) { iters = it; return YGPU_BREAKDOWN; }
+            if (flag == 1) { recheck = true; break; }
+            if (flag == 3) {
+                if (it < maxiter) { iters = it; return YGPU_BREAKDOWN; }
+                break;
+            }
+        }
+        iters = it;
+        if (!recheck) return YGPU_MAXITER;
+        double tr = 0.0;
+        for (int k = Tm.tid; k < G.nu; k += Tm.nthr) {
+            const double rk = (double)b[k] - (double)A.row(k, x);
+            tr += rk * rk;
+        }
+        if (!(ok = team_allreduce(Tm, &tr, 1))) return YGPU_ERR_TIMEOUT;
+        relres = sqrt(tr) / bnrm;
+        if (relres <= tol) return YGPU_OK;
+        if (it >= maxiter) return YGPU_MAXITER;
+    }
+    return YGPU_MAXITER;
+}
+
+// ---------------------------------------------------------------------------
 // Linear solve of one Picard iteration: FP64, or FP32 inside FP64 defect correction
 // ---------------------------------------------------------------------------
 __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, double bnrm, int& iters,
@@ -1807,20 +2134,17 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
                                        P.lin_maxiter, P.lin_tol, bnrm, pre, iters, relres, ok);
     }
     const StencilOp<float, float> A32{&I, &G, energy, I.fN, I.fNab, I.fdrag_x, I.fdrag_y, make_opk<float>(G)};
-    // ---- mixed: FP32 coefficients, FP32 inner Krylov, FP64 outer residual ----
-    for (int c = T.tid; c < G.n2; c += T.nthr) {
-        I.fN[c] = (float)I.visc_int[c];
-        I.fNab[c] = (float)I.Nab[c];
-        I.fdrag_x[c] = (float)I.drag_x[c];
-        I.fdrag_y[c] = (float)I.drag_y[c];
-    }
-    for (int u = T.tid; u < G.nu; u += T.nthr) I.fdinv[u] = (float)I.dinv[u];
-    if (!(ok = team_barrier(T))) return YGPU_ERR_TIMEOUT;
+    // ---- mixed: FP32 coefficients (copied by the pre step, with the tile-block
+    // inverses of -p ilu), FP32 inner Krylov, FP64 outer residual ----
+    const bool block = use_cg && energy && P.lin_precond == YGPU_PRE_ILU0 && I.fminv;
     const double inner_tol = (P.inner_tol > 0.0) ? P.inner_tol : 1e-3;
-    const int inner_max = (P.inner_maxiter > 0) ? P.inner_maxiter : P.lin_maxiter;
+    // inner solves are capped: one that cannot reach inner_tol in FP32 (an
+    // operator too ill-conditioned for single precision) still hands its
+    // progress to the FP64 defect correction instead of running to lin_maxiter
+    const int inner_max = (P.inner_maxiter > 0) ? P.inner_maxiter : (P.lin_maxiter < 400 ? P.lin_maxiter : 400);
     int total = 0;
     int status = YGPU_MAXITER;
-    const int max_outer = 60;
+    const int max_outer = 200;           // total inner iterations stay below lin_maxiter
     for (int o = 0; o < max_outer; o++) {
         // r64 = b - A64 x (FP64 residual of the outer iterate)
         A64(T, I.x, I.q);
@@ -1844,7 +2168,10 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         int it = 0;
         double rel_in = 0.0;
         int st;
-        if (use_cg)
+        if (use_cg && block)
+            st = krylov_pcg_pipe_blk<float>(T, G, A32, I.fminv, I.fx, I.fr, I.frt, I.fv, I.ft, I.fph, I.fm2, I.fz,
+                                            I.fq, I.fs, I.fp, inner_max, inner_tol, 1.0, it, rel_in, ok);
+        else if (use_cg)
             st = krylov_pcg_pipe<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.frt, I.fv, I.ft, I.fph, I.fm2, I.fz,
                                         I.fq, I.fs, I.fp, inner_max, inner_tol, 1.0, pre, it, rel_in, ok);
         else
@@ -2098,6 +2425,23 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
     t3 = clk.lap();
     phase_system(I, P, G, T, bn2);
     if (!team_allreduce(T, &bn2, 1)) { status = YGPU_ERR_TIMEOUT; goto out_; }
+    if (mixed) {
+        // FP32 copies of the operator coefficients and the Jacobi diagonal for
+        // the inner solves, and the tile-block inverses of -p ilu
+        for (int c = T.tid; c < G.n2; c += T.nthr) {
+            I.fN[c] = (float)I.visc_int[c];
+            I.fNab[c] = (float)I.Nab[c];
+            I.fdrag_x[c] = (float)I.drag_x[c];
+            I.fdrag_y[c] = (float)I.drag_y[c];
+        }
+        for (int u = T.tid; u < G.nu; u += T.nthr) I.fdinv[u] = (float)I.dinv[u];
+        if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
+        if (I.fminv && P.ssa_solver == YGPU_SSA_ENERGY && P.lin_precond == YGPU_PRE_ILU0) {
+            const StencilOp<float, float> A32{&I, &G, true, I.fN, I.fNab, I.fdrag_x, I.fdrag_y, make_opk<float>(G)};
+            block_setup<float, float>(I, G, T, A32, I.fminv);
+            if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
+        }
+    }
     t4 = clk.lap();
 out_:
     if (lead) {
@@ -2686,9 +3030,11 @@ static bool capture_chunk(cudaStream_t stream, const StepShape& sh, const Inst* 
     int k = 0;
     for (int it = 0; it < iters && ok; it++)
         for (int step : {YG_STEP_PRE, YG_STEP_KRYLOV, YG_STEP_POST}) {
-            if (ok && timed) ok = cudaEventRecord(gc->ev[k].a, stream) == cudaSuccess;
+            // external records: real event-record nodes of the graph (a plain record
+            // inside a capture only orders the capture)
+            if (ok && timed) ok = cudaEventRecordWithFlags(gc->ev[k].a, stream, cudaEventRecordExternal) == cudaSuccess;
             if (ok) ok = (launch_step_raw(step, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort) == YGPU_OK);
-            if (ok && timed) ok = cudaEventRecord(gc->ev[k].b, stream) == cudaSuccess;
+            if (ok && timed) ok = cudaEventRecordWithFlags(gc->ev[k].b, stream, cudaEventRecordExternal) == cudaSuccess;
             k++;
         }
     if (ok) ok = cudaMemcpyAsync(h_flags, d_done, sizeof(int), cudaMemcpyDeviceToHost, stream) == cudaSuccess;
