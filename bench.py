@@ -61,7 +61,39 @@ def make_instances(workload: str, batch: int):
         raise SystemExit(f"unknown workload {workload}")
     for inst in insts:
         inst.par = inst.par.with_(**BENCH_TOL)
+        if workload == "continent_diva":
+            # power-law friction with q = 1/3 settles into a Picard 2-cycle at the
+            # beta_min floor, so this workload runs the namelist's own Picard
+            # settings (ssa_iter_max 20, ssa_iter_conv 1e-2): every solve is 20
+            # Picard iterations, each with a linear solve to 1e-9
+            inst.par = inst.par.with_(ssa_iter_max=20, ssa_iter_conv=1e-2)
     return insts
+
+
+LARGE_CELLS = 200_000     # above this, CPU samples are a few Picard iterations of one solve
+
+
+def _cpu_sample(inst, oracle, n_max=5, budget_s=20.0):
+    """Seconds per full solve of the oracle: whole solves, or for large grids two
+    Picard iterations scaled to ssa_iter_max (the iterations those solves take)."""
+    f0 = oracle.prepare(inst)
+    if inst.nx * inst.ny > LARGE_CELLS:
+        k = 2
+        f = _copy(f0)
+        t = time.perf_counter()
+        oracle.calc_velocity(f, inst, inst.par.with_(ssa_iter_max=k))
+        per_solve = (time.perf_counter() - t) * inst.par.ssa_iter_max / k
+        return [per_solve], f"{k} Picard iterations of one solve, scaled to {inst.par.ssa_iter_max}", f0
+    times = []
+    t_all = time.perf_counter()
+    while True:
+        f = _copy(f0)
+        t = time.perf_counter()
+        oracle.calc_velocity(f, inst)
+        times.append(time.perf_counter() - t)
+        if time.perf_counter() - t_all > budget_s or len(times) >= n_max:
+            break
+    return times, f"{len(times)} full solves of the same workload", f0
 
 
 def describe(inst, batch):
@@ -138,14 +170,23 @@ def run_reference(args, insts, rank, world):
     inst = insts[0]
     f0 = oracle.prepare(inst)
     times, out = [], None
+    large = inst.nx * inst.ny > LARGE_CELLS
+    k = 2
     for s in range(args.warmup + args.steps):
         f = _copy(f0)
         t = time.perf_counter()
-        out = oracle.calc_velocity(f, inst)
-        dt = time.perf_counter() - t
+        if large:
+            # bounded sample: two Picard iterations, scaled to the solve's ssa_iter_max
+            out = oracle.calc_velocity(f, inst, inst.par.with_(ssa_iter_max=k))
+            dt = (time.perf_counter() - t) * inst.par.ssa_iter_max / k
+        else:
+            out = oracle.calc_velocity(f, inst)
+            dt = time.perf_counter() - t
         if s >= args.warmup:
             times.append(dt)
     value = len(times) / sum(times)
+    sample = (f"{k} Picard iterations per step scaled to {inst.par.ssa_iter_max}" if large
+              else f"{len(times)} full solves")
     return {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
@@ -154,7 +195,7 @@ def run_reference(args, insts, rank, world):
         "config": {"workload": describe(inst, 1), "picard_tol": inst.par.ssa_iter_conv, "lin": inst.par.lis_opt},
         "latency_ms": {"p50": 1e3 * float(np.percentile(times, 50)), "p99": 1e3 * float(np.percentile(times, 99))},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": f"{len(times)} full solves (oracle: C FP64 restatement, OpenMP, {cores} threads)"},
+                         "sample": f"{sample} (oracle: C FP64 restatement, OpenMP, {cores} threads)"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "picard_iters": out["ssa_iter_now"], "lin_iters": out["ssa_lin_iter"],
     }
@@ -166,24 +207,16 @@ def cpu_baseline_leg(inst, budget_s=20.0):
     import oracle
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
-    f0 = oracle.prepare(inst)
-    times = []
-    t_all = time.perf_counter()
-    while True:
-        f = _copy(f0)
-        t = time.perf_counter()
-        oracle.calc_velocity(f, inst)
-        times.append(time.perf_counter() - t)
-        if time.perf_counter() - t_all > budget_s or len(times) >= 5:
-            break
+    times, sample, f0 = _cpu_sample(inst, oracle, budget_s=budget_s)
+    base = {"value": len(times) / sum(times), "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": f"{sample} (oracle: C FP64 restatement, OpenMP, {cores} threads)"}
+    if inst.nx * inst.ny > LARGE_CELLS:
+        return base, None
     tight = _copy(f0)
     par_t = inst.par.with_(ssa_iter_max=800, ssa_iter_conv=1e-10,
                            ssa_lis_opt_energy="-i cg -p jacobi -maxiter 20000 -tol 1.0e-12",
                            ssa_lis_opt_residual="-i bicgstab -p jacobi -maxiter 20000 -tol 1.0e-12")
     oracle.calc_velocity(tight, inst, par_t)
-    base = {"value": len(times) / sum(times), "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": f"{len(times)} full solves of the same workload (oracle: C FP64 restatement, "
-                      f"OpenMP, {cores} threads)"}
     return base, tight
 
 
@@ -286,7 +319,7 @@ def main():
             run_served(args)
         return
     args.warmup = max(args.warmup, 3)
-    batch = args.batch or (256 if args.workload == "ensemble" else 16)
+    batch = args.batch or {"ensemble": 256, "continent_diva": 1}.get(args.workload, 16)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
