@@ -103,6 +103,21 @@ def describe(inst, batch):
     return f"{inst.name} {inst.nx}x{inst.ny}x{inst.nz} dx={inst.dx/1e3:g}km cold {kind} solve"
 
 
+def max_over_ranks(ms: float, dist=None, device: str = "cpu") -> float:
+    """The timed span of a replica run: the maximum over ranks (every rank gets it)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, batch: int, steps: int, max_ms: float) -> float:
+    """Whole-job solves/s: every rank solves `batch` instances per step."""
+    return world * batch * steps / (max_ms / 1e3)
+
+
 def rel_l2(a, b):
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
 
@@ -412,11 +427,7 @@ def main():
             gpu.step_timing(False)
         vel = "ux_bar" if kind == abi.KIND_DIVA else "ux_b"
         u_batch = [d[vel].cpu().numpy().reshape((i.nx, i.ny), order="F") for d, i in zip(devs, insts)]
-        tot_ms = sum(step_ms)
-        if dist is not None:
-            t = torch.tensor([tot_ms], device=f"cuda:{local}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tot_ms = float(t.item())
+        tot_ms = max_over_ranks(sum(step_ms), dist, f"cuda:{local}")
         res[prec] = {"lat": lat, "st1": st1, "step_ms": step_ms, "tot_ms": tot_ms, "sts": sts,
                      "u_single": u_single, "u_batch": u_batch, "all_sts": all_sts, "launches": launches,
                      "steps_timing": steps_timing}
@@ -441,8 +452,8 @@ def main():
         return
     mixed, fp64 = res["mixed"], res["fp64"]
     K = len(mixed["step_ms"])
-    value = world * batch * K / (mixed["tot_ms"] / 1e3)
-    value64 = world * batch * K / (fp64["tot_ms"] / 1e3)
+    value = replica_throughput(world, batch, K, mixed["tot_ms"])
+    value64 = replica_throughput(world, batch, K, fp64["tot_ms"])
     # error of the mixed batch against the FP64 batch, per instance
     err_mixed_vs_fp64 = max(rel_l2(a, b) for a, b in zip(mixed["u_batch"], fp64["u_batch"]))
     err_vs_oracle = None
