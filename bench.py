@@ -118,6 +118,24 @@ def replica_throughput(world: int, batch: int, steps: int, max_ms: float) -> flo
     return world * batch * steps / (max_ms / 1e3)
 
 
+# ncu captures behind roofline.traffic: DRAM bytes over algorithmic bytes of one
+# Krylov launch of the same workload (profiles/<kernel>_<workload>.md)
+TRAFFIC_PROFILES = {"marine_diva": "ygpu_k_krylov_marine_diva_b16.md"}
+
+
+def dram_over_algorithmic(workload: str):
+    name = TRAFFIC_PROFILES.get(workload)
+    if not name:
+        return None
+    try:
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if line.startswith("dram_over_algorithmic:"):
+                return float(line.split(":")[1])
+    except OSError:
+        return None
+    return None
+
+
 def rel_l2(a, b):
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
 
@@ -475,6 +493,7 @@ def main():
                     "achieved_gbs": (alg_steps[k] / (tm[k][0] / 1e3) / 1e9) if k in alg_steps and tm[k][0] > 0
                     else None} for k in tm}
     avg_ms = statistics.mean(mixed["step_ms"])
+    ratio = dram_over_algorithmic(args.workload)
     try:
         peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
         peak_src = "measured"
@@ -504,7 +523,11 @@ def main():
                  + " on host buffers, one solve per step"}
                 if e2e_times else None),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
+                     "frac": (achieved / peak) if achieved else None,
+                     "traffic": (ratio * alg_steps["krylov"] / max(kr_n, 1)) if ratio else None,
+                     "traffic_note": ("bytes per launch: DRAM/algorithmic ratio of the ncu capture in profiles/"
+                                      + TRAFFIC_PROFILES.get(args.workload, "") + " times this run's average "
+                                      "algorithmic bytes per launch") if ratio else None,
                      "kernel": "ygpu_k_krylov", "launches": kr_n,
                      "alg_bytes_per_launch": alg_steps["krylov"] / max(kr_n, 1),
                      "avg_launch_ms": kr_ms / max(kr_n, 1), "peak_source": peak_src},
