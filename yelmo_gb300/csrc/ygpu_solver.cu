@@ -1356,6 +1356,22 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
                 b = 0.0;
                 d = 0.0;
                 const int* mem = I.mem + 3 * u;
+                // interior rows (no members, only free or zero-Dirichlet columns):
+                // nothing to lift, and the diagonal of the 9-point stencil in closed form
+                const bool fast = (I.rpart[u] == 1);
+                if (fast) {
+                    const int i = c % nx, j = c / nx;
+                    const int im1 = (i == 0) ? nx - 1 : i - 1, ip1 = (i == nx - 1) ? 0 : i + 1;
+                    const int jm1 = (j == 0) ? ny - 1 : j - 1, jp1 = (j == ny - 1) ? 0 : j + 1;
+                    const double Ni = N[c], Bc = I.Nab[c];
+                    if (pl == 0) {
+                        const double Np = N[ip1 + nx * j], Bm = I.Nab[i + nx * jm1];
+                        d = 4.0 * K64.dyodx * (Np + Ni) + K64.dxody * (Bc + Bm) + I.drag_x[c];
+                    } else {
+                        const double Np = N[i + nx * jp1], Bm = I.Nab[im1 + nx * j];
+                        d = 4.0 * K64.dxody * (Np + Ni) + K64.dyodx * (Bc + Bm) + I.drag_y[c];
+                    }
+                }
                 for (int m = -1; m < 3; m++) {
                     int mm = (m < 0) ? u : mem[m];
                     if (mm < 0) break;
@@ -1372,6 +1388,7 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
                     } else {
                         b = b - (mpl ? I.taud_y[mc] : I.taud_x[mc]) * G.dxdy;
                     }
+                    if (fast) break;         // forcing done; diagonal above
                     auto lift = [&](int dd) -> double {
                         if (dd < 0) return 0.0;
                         return (I.ukind[dd] == DOF_DIR) ? I.dval[dd] : 0.0;
@@ -2649,12 +2666,20 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
 }
 
 #define YG_KBLOCK 512
+// the pre step (viscosity column pass, faces, system) runs 512-thread CTAs at
+// 128 registers: twice the warps per SM of 256 threads at 255 registers
+#define YG_PBLOCK 384
 
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_setup(const Inst* insts, int n_inst, ygpu_dyn_par P,
                                                             TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
     run_step<YG_STEP_SETUP>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
-__global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_pre(const Inst* insts, int n_inst, ygpu_dyn_par P,
+__global__ void __launch_bounds__(YG_PBLOCK, 1) ygpu_k_pre(const Inst* insts, int n_inst, ygpu_dyn_par P,
+                                                          TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
+    run_step<YG_STEP_PRE>(insts, n_inst, P, ctls, tc, ab, dc, map);
+}
+// FP64 solves: the FP64 column pass needs the full register file (256 threads)
+__global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_pre64(const Inst* insts, int n_inst, ygpu_dyn_par P,
                                                           TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
     run_step<YG_STEP_PRE>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
@@ -2971,7 +2996,11 @@ static int launch_step_raw(int step, cudaStream_t s, const StepShape& sh, const 
         case YG_STEP_SETUP:
             return coop((const void*)ygpu_k_setup, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
         case YG_STEP_PRE:
-            return coop((const void*)ygpu_k_pre, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
+            if (P.precision == YGPU_PREC_MIXED)
+                return coop((const void*)ygpu_k_pre, sh.grid, YG_PBLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas,
+                            d_abort, d_done, sh.map);
+            return coop((const void*)ygpu_k_pre64, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas,
+                        d_abort, d_done, sh.map);
         case YG_STEP_KRYLOV:
             return coop((const void*)ygpu_k_krylov, sh.kgrid, YG_KBLOCK, s, d_insts, n_inst, P, ctls, sh.ktc, d_abort, d_done, sh.kmap);
         case YG_STEP_POST:
@@ -3131,7 +3160,10 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
 int ygpu_solver_max_ctas(int device) {
     int nsm = 0, bps = 0, b2 = 0, b3 = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ygpu_k_pre, YG_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ygpu_k_pre, YG_PBLOCK, 0);
+    int b4 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b4, ygpu_k_pre64, YG_BLOCK, 0);
+    if (b4 < bps) bps = b4;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, ygpu_k_post, YG_BLOCK, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, ygpu_k_setup, YG_BLOCK, 0);
     if (b2 < bps) bps = b2;
