@@ -363,7 +363,7 @@ typedef struct ygpu_server_cfg {
     int    lateral_bc;          /* YGPU_LATBC_*                                  */
     double dH_sigma;            /* standard deviation of the per-step dH (m)     */
     unsigned long long hbm_budget; /* device bytes the server may hold         */
-    int    max_slots;           /* solves on the GPU at once (0: one per SM)     */
+    int    max_slots;           /* solves on the GPU at once (0: 16)             */
 } ygpu_server_cfg;
 
 typedef struct ygpu_server_info {

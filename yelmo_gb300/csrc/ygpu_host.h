@@ -19,6 +19,7 @@ void ygpu_set_error(const char* fmt, ...);
 // ygpu_solver.cu
 
 int ygpu_solver_max_ctas(int device);
+size_t ygpu_solver_stack_bytes();
 
 // Step kernels of the Picard loop (one cooperative launch each)
 enum { YG_STEP_SETUP = 0, YG_STEP_PRE = 1, YG_STEP_KRYLOV = 2, YG_STEP_POST = 3, YG_STEP_FINAL = 4 };

@@ -59,6 +59,17 @@ static int noalloc_setup(int dev, DeviceSetup** out) {
         }
         S.base = (char*)p;
         S.max_ctas = ygpu_solver_max_ctas(dev);
+        // the step kernels' stack must fit the context's stack limit: raising it
+        // would reserve device memory, which this entry point does not do
+        size_t limit = 0;
+        cudaDeviceGetLimit(&limit, cudaLimitStackSize);
+        const size_t need = ygpu_solver_stack_bytes();
+        if (need > limit) {
+            ygpu_set_error("the solver kernels need %zu bytes of stack per thread, the context allows %zu: create "
+                           "a context (ygpu_ctx_create) once, or raise cudaLimitStackSize, before this call",
+                           need, limit);
+            return YGPU_ERR_CUDA;
+        }
         if (S.max_ctas < 1) {
             ygpu_set_error("solver kernel cannot be resident on device %d", dev);
             return YGPU_ERR_CUDA;

@@ -2666,9 +2666,9 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
 }
 
 #define YG_KBLOCK 512
-// the pre step (viscosity column pass, faces, system) runs 512-thread CTAs at
-// 128 registers: twice the warps per SM of 256 threads at 255 registers
-#define YG_PBLOCK 384
+// the mixed-precision pre step (FP32 column pass, faces, system) runs 512-thread
+// CTAs at 128 registers: twice the warps per SM of 256 threads at 255 registers
+#define YG_PBLOCK 512
 
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_setup(const Inst* insts, int n_inst, ygpu_dyn_par P,
                                                             TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
@@ -3155,6 +3155,19 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
     }
     // instances not finished by the loop (ssa_iter_max = 0) get their final passes
     return ygpu_launch_step(YG_STEP_FINAL, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort);
+}
+
+// Largest per-thread local memory (stack) of the step kernels, in bytes.
+size_t ygpu_solver_stack_bytes() {
+    const void* k[] = {(const void*)ygpu_k_setup, (const void*)ygpu_k_pre, (const void*)ygpu_k_pre64,
+                       (const void*)ygpu_k_krylov, (const void*)ygpu_k_post, (const void*)ygpu_k_final};
+    size_t m = 0;
+    for (const void* f : k) {
+        cudaFuncAttributes a;
+        if (cudaFuncGetAttributes(&a, f) == cudaSuccess && a.localSizeBytes > m) m = a.localSizeBytes;
+    }
+    cudaGetLastError();
+    return m;
 }
 
 int ygpu_solver_max_ctas(int device) {
