@@ -288,6 +288,9 @@ typedef struct ygpu_tuning {
     int check_every;            /* Picard iterations between host checks (1..64), default 4 */
     int use_graphs;             /* 1: chunk graphs (default), 0: one launch per step        */
     int unknowns_per_cta;       /* team sizing, default 512                                 */
+    unsigned long long max_active_unknowns; /* batches with more unknowns run as a queue:
+                                   continuous batching with at most this many unknowns on the
+                                   GPU at once (default 1.5 M; 0: always one lockstep batch)  */
 } ygpu_tuning;
 void ygpu_tuning_defaults(ygpu_tuning* t);
 int  ygpu_ctx_set_tuning(ygpu_ctx* ctx, const ygpu_tuning* t);
@@ -298,10 +301,12 @@ int ygpu_solve_device(ygpu_ctx* ctx, int kind, const ygpu_dyn_par* par,
                       const ygpu_fields* f, ygpu_stats* stats);
 
 /*
- * Batched solve: n_inst independent instances of uneven size in one persistent
- * launch. Each instance is solved by a team of CTAs that takes instances from
- * a device work queue until the queue is empty. stats may be NULL or an array
- * of n_inst entries.
+ * Batched solve: n_inst independent instances of uneven size. A batch within
+ * the context's max_active_unknowns runs in lockstep (every instance on the GPU,
+ * one team of CTAs each); a larger one runs as a queue: instances are admitted
+ * largest first as others finish, each tick advancing the active ones by one
+ * Picard iteration (continuous batching). stats may be NULL or an array of
+ * n_inst entries.
  */
 int ygpu_solve_batch_device(ygpu_ctx* ctx, int kind, const ygpu_dyn_par* par,
                             int n_inst, const ygpu_fields* inst, ygpu_stats* stats);

@@ -25,12 +25,17 @@ def _device(inst):
     return dev, gpu.make_fields(dev, inst.nx, inst.ny, inst.nz, inst.dx, inst.dx, inst.n_glen)
 
 
+@pytest.mark.parametrize("queue", [False, True])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_batch_equals_single(precision):
+def test_batch_equals_single(precision, queue):
+    """Lockstep batch, and the queue (continuous batching: at most ~2 instances'
+    unknowns on the GPU at once, the rest admitted as others finish)."""
     torch = pytest.importorskip("torch")
     insts = _instances()
     par = insts[0].par.with_(precision=precision)
     solver = gpu.DeviceSolver(0)
+    if queue:
+        solver.set_tuning(max_active_unknowns=2 * 2 * 41 * 41)
     try:
         single = []
         for inst in insts:

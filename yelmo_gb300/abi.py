@@ -91,7 +91,8 @@ class Fields(C.Structure):
 
 class Tuning(C.Structure):
     """ygpu_tuning."""
-    _fields_ = [("check_every", C.c_int), ("use_graphs", C.c_int), ("unknowns_per_cta", C.c_int)]
+    _fields_ = [("check_every", C.c_int), ("use_graphs", C.c_int), ("unknowns_per_cta", C.c_int),
+                ("max_active_unknowns", C.c_ulonglong)]
 
 
 class ServerCfg(C.Structure):

@@ -1,6 +1,7 @@
 """Launch autotuner: picks a context's tuning (team size, host-check interval,
-chunk graphs) for a workload by timing a fixed number of Picard iterations of
-its batched solve under each candidate.
+chunk graphs, lockstep batch or queue) for a workload by timing a fixed number
+of Picard iterations of its batched solve under each candidate (and, for the
+batch-or-queue choice, full solves).
 
     best = autotune(solver, kind, par, fields, reset)
 
@@ -56,6 +57,23 @@ def autotune(solver, kind: int, par, fields: list, reset, iters: int = 8, grid: 
             t = min(t, time.perf_counter() - t0)
         if t < best_t:
             best_t, best = t, cand
+    # lockstep batch or queue (continuous batching): full solves with the real
+    # convergence test, since the queue's gain comes from instances that finish
+    # at different iterations
+    total_nu = sum(2 * f.nx * f.ny for f in fields)
+    if len(fields) > 1 and total_nu > 1_500_000:
+        full = []
+        for U in (1_500_000, 4_000_000, 0):
+            cand = dict(best, max_active_unknowns=U)
+            solver.set_tuning(**cand)
+            reset()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            solver.solve_batch(kind, par, fields)
+            torch.cuda.synchronize()
+            full.append((time.perf_counter() - t0, cand))
+        full.sort(key=lambda r: r[0])
+        best = full[0][1]
     solver.set_tuning(**best)
     return {"tuning": best, "trial_ms": best_t * 1e3, "iters": iters,
             "candidates": [{"ms": r[0] * 1e3, **r[1]} for r in results]}

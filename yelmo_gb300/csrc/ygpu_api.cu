@@ -170,6 +170,7 @@ struct ygpu_ctx {
     bool use_graphs = true;
     int check_every = 4;            // Picard iterations between host checks
     int unknowns_per_cta = 0;       // team size: unknowns per CTA (0: 2 x block)
+    size_t max_active_unknowns = 1500000;   // batches beyond this run as a queue (continuous batching)
     int* h_flags = nullptr;         // pinned: finished count, abort flag
     int* d_misc = nullptr;          // [0] queue, [1] abort, [2..3] csr out
     double* d_miscd = nullptr;
@@ -199,6 +200,7 @@ extern "C" void ygpu_tuning_defaults(ygpu_tuning* t) {
     t->check_every = 4;
     t->use_graphs = 1;
     t->unknowns_per_cta = 2 * YG_BLOCK;
+    t->max_active_unknowns = 1500000;
 }
 
 extern "C" int ygpu_ctx_set_tuning(ygpu_ctx* c, const ygpu_tuning* t) {
@@ -211,6 +213,7 @@ extern "C" int ygpu_ctx_set_tuning(ygpu_ctx* c, const ygpu_tuning* t) {
     c->check_every = t->check_every;
     c->use_graphs = (t->use_graphs != 0);
     c->unknowns_per_cta = t->unknowns_per_cta;
+    c->max_active_unknowns = t->max_active_unknowns;
     ygpu_graph_cache_clear(&c->graph);
     return YGPU_OK;
 }
@@ -555,9 +558,221 @@ extern "C" int ygpu_solve_device(ygpu_ctx* c, int kind, const ygpu_dyn_par* par,
     return solve_batch(c, kind, par, 1, f, stats);
 }
 
+// Batches larger than one wave: continuous batching over a work queue. At most
+// `max_active_unknowns` unknowns are on the GPU at once; each tick runs one
+// Picard iteration (pre / Krylov / post) of the active instances, retires the
+// finished ones and admits the next instances of the queue (largest first) into
+// their scratch slots, so no instance waits for the slowest of the whole batch.
+static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, const ygpu_fields* inst,
+                       ygpu_stats* stats) {
+    const bool mixed = (par->precision == YGPU_PREC_MIXED);
+    const bool block = ygpu_wants_block(*par);
+    const size_t U = c->max_active_unknowns;
+    std::vector<int> order(n);
+    for (int k = 0; k < n; k++) order[k] = k;
+    auto nu_of = [&](int k) { return (size_t)2 * inst[k].nx * inst[k].ny; };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (size_t)inst[a].nx * inst[a].ny * inst[a].nz > (size_t)inst[b].nx * inst[b].ny * inst[b].nz;
+    });
+    // slots: enough for the smallest instances to fill U, each sized for the largest
+    size_t nu_min = nu_of(order[n - 1]), slot_bytes = 0;
+    for (int k = 0; k < n; k++)
+        slot_bytes = std::max(slot_bytes, al(ygpu_inst_scratch_bytes(inst[k].nx, inst[k].ny, inst[k].nz, mixed, block)));
+    int n_slots = (int)std::min<size_t>((size_t)n, std::max<size_t>(1, U / std::max<size_t>(nu_min, 1) + 1));
+    n_slots = std::min(n_slots, c->max_ctas > 0 ? c->max_ctas : 1);
+    int st;
+    if ((st = grow(&c->arena, &c->arena_cap, slot_bytes * (size_t)n_slots))) return st;
+    const int cap = std::max(n, 2 * n_slots);
+    if (c->insts_cap < cap) {
+        cudaFree(c->d_insts);
+        cudaFree(c->d_out);
+        c->d_insts = nullptr;
+        c->d_out = nullptr;
+        CK(cudaMalloc((void**)&c->d_insts, sizeof(Inst) * (size_t)cap));
+        CK(cudaMalloc((void**)&c->d_out, sizeof(InstOut) * (size_t)cap));
+        c->insts_cap = cap;
+    }
+    const int n_ctl = c->max_ctas > 0 ? c->max_ctas : 1;
+    if (c->ctl_cap < n_ctl) {
+        cudaFree(c->d_ctl);
+        c->d_ctl = nullptr;
+        CK(cudaMalloc((void**)&c->d_ctl, sizeof(TeamCtl) * (size_t)n_ctl));
+        c->ctl_cap = n_ctl;
+    }
+    const int map_need = 3 * n_ctl;
+    if (c->map_cap < map_need) {
+        cudaFree(c->d_map);
+        c->d_map = nullptr;
+        CK(cudaMalloc((void**)&c->d_map, sizeof(int) * (size_t)map_need));
+        c->map_cap = map_need;
+    }
+    if ((st = ygpu_init_constants(c->device))) return st;
+    // device layout: outputs per instance (caller order); active list, then admitted list
+    InstOut* d_out = c->d_out;
+    Inst* d_active = c->d_insts;
+    Inst* d_new = c->d_insts + n_slots;
+    int* d_done = c->d_misc;
+    int* d_abort = c->d_misc + 1;
+    CK(cudaMemsetAsync(d_out, 0, sizeof(InstOut) * (size_t)n, c->stream));
+    CK(cudaMemsetAsync(c->d_misc, 0, 2 * sizeof(int), c->stream));
+    CK(cudaMemsetAsync(c->d_ctl, 0, sizeof(TeamCtl) * (size_t)n_ctl, c->stream));
+    CK(cudaEventRecord(c->e0, c->stream));
+    std::vector<int> slot_of(n, -1), free_slots;
+    for (int k = n_slots - 1; k >= 0; k--) free_slots.push_back(k);
+    std::vector<int> active;             // instance indices, largest first
+    std::vector<Inst> h_active, h_new;
+    c->h_out.resize(n);
+    size_t active_nu = 0;
+    int next = 0, abort_flag = 0;
+    auto shape_of = [&](const std::vector<int>& ids, StepShape* sh) -> int {
+        std::vector<size_t> nus;
+        for (int k : ids) nus.push_back(nu_of(k));
+        std::vector<int> map;
+        int grid = 0;
+        if (ids.size() > 1 && ygpu_plan_teams(c->max_ctas, (int)ids.size(), nus.data(), map, &grid, c->unknowns_per_cta)) {
+            if (cudaMemcpyAsync(c->d_map, map.data(), sizeof(int) * map.size(), cudaMemcpyHostToDevice, c->stream) !=
+                cudaSuccess)
+                return YGPU_ERR_CUDA;
+            // the host vector must outlive the copy
+            if (cudaStreamSynchronize(c->stream) != cudaSuccess) return YGPU_ERR_CUDA;
+            if (ygpu_step_shape_mapped(c->device, grid, c->d_map, sh) == YGPU_OK) return YGPU_OK;
+        }
+        size_t mx = 0;
+        for (size_t v : nus) mx = std::max(mx, v);
+        int nt, tc;
+        ygpu_choose_teams(c->max_ctas, (int)ids.size(), mx, &nt, &tc, c->unknowns_per_cta);
+        return ygpu_step_shape(c->device, nt, tc, sh);
+    };
+    while (next < n || !active.empty()) {
+        // admit
+        std::vector<int> adm;
+        while (next < n && !free_slots.empty() &&
+               ((active.empty() && adm.empty()) || active_nu + nu_of(order[next]) <= U)) {
+            const int k = order[next++];
+            const int s = free_slots.back();
+            free_slots.pop_back();
+            slot_of[k] = s;
+            Inst I;
+            ygpu_fill_inst(I, kind, &inst[k]);
+            ygpu_inst_scratch_carve(I, c->arena + slot_bytes * (size_t)s, inst[k].nx, inst[k].ny, inst[k].nz, mixed,
+                                    block);
+            I.out = d_out + k;
+            h_new.push_back(I);
+            adm.push_back(k);
+            active_nu += nu_of(k);
+        }
+        if (!adm.empty()) {
+            CK(cudaMemcpyAsync(d_new, h_new.data(), sizeof(Inst) * h_new.size(), cudaMemcpyHostToDevice, c->stream));
+            StepShape sh;
+            if ((st = shape_of(adm, &sh))) return st;
+            if ((st = ygpu_launch_step(YG_STEP_SETUP, c->stream, sh, d_new, (int)adm.size(), *par, c->d_ctl, d_done,
+                                       d_abort)))
+                return st;
+            if (par->ssa_iter_max == 0 &&
+                (st = ygpu_launch_step(YG_STEP_FINAL, c->stream, sh, d_new, (int)adm.size(), *par, c->d_ctl, d_done,
+                                       d_abort)))
+                return st;
+            CK(cudaStreamSynchronize(c->stream));
+            h_new.clear();
+            for (int k : adm) active.push_back(k);
+            std::stable_sort(active.begin(), active.end(), [&](int a, int b) { return nu_of(a) > nu_of(b); });
+            h_active.clear();
+            for (int k : active) {
+                Inst I;
+                ygpu_fill_inst(I, kind, &inst[k]);
+                ygpu_inst_scratch_carve(I, c->arena + slot_bytes * (size_t)slot_of[k], inst[k].nx, inst[k].ny,
+                                        inst[k].nz, mixed, block);
+                I.out = d_out + k;
+                h_active.push_back(I);
+            }
+            CK(cudaMemcpyAsync(d_active, h_active.data(), sizeof(Inst) * h_active.size(), cudaMemcpyHostToDevice,
+                               c->stream));
+        }
+        if (active.empty()) continue;
+        // one Picard iteration of every active instance
+        StepShape sh;
+        if ((st = shape_of(active, &sh))) return st;
+        for (int step : {YG_STEP_PRE, YG_STEP_KRYLOV, YG_STEP_POST})
+            if ((st = ygpu_launch_step(step, c->stream, sh, d_active, (int)active.size(), *par, c->d_ctl, d_done,
+                                       d_abort)))
+                return st;
+        CK(cudaMemcpyAsync(c->h_out.data(), d_out, sizeof(InstOut) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(c->h_flags + 1, d_abort, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        ygpu_step_timing_flush();
+        abort_flag = c->h_flags[1];
+        if (abort_flag) break;
+        // retire
+        std::vector<int> keep;
+        for (int k : active) {
+            if (c->h_out[k].done) {
+                free_slots.push_back(slot_of[k]);
+                active_nu -= nu_of(k);
+            } else {
+                keep.push_back(k);
+            }
+        }
+        if (keep.size() != active.size()) {
+            active.swap(keep);
+            h_active.clear();
+            for (int k : active) {
+                Inst I;
+                ygpu_fill_inst(I, kind, &inst[k]);
+                ygpu_inst_scratch_carve(I, c->arena + slot_bytes * (size_t)slot_of[k], inst[k].nx, inst[k].ny,
+                                        inst[k].nz, mixed, block);
+                I.out = d_out + k;
+                h_active.push_back(I);
+            }
+            if (!active.empty())
+                CK(cudaMemcpyAsync(d_active, h_active.data(), sizeof(Inst) * h_active.size(), cudaMemcpyHostToDevice,
+                                   c->stream));
+        }
+    }
+    CK(cudaEventRecord(c->e1, c->stream));
+    CK(cudaMemcpyAsync(c->h_out.data(), d_out, sizeof(InstOut) * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->e0, c->e1);
+    int worst = YGPU_OK;
+    for (int k = 0; k < n; k++) {
+        const InstOut& o = c->h_out[k];
+        int s_k = abort_flag ? YGPU_ERR_TIMEOUT : o.status;
+        if (stats) {
+            ygpu_stats& S = stats[k];
+            S.ssa_iter_now = o.iter_now;
+            S.ssa_lin_iter = o.lin_iter;
+            S.ssa_lin_fail = o.lin_fail;
+            S.ssa_lim_n = o.lim_n;
+            S.ssa_resid = o.resid;
+            S.lin_resid = o.lin_resid;
+            S.outer_iter = o.outer_iter;
+            S.status = s_k;
+            S.device_ms = ms;
+            for (int q = 0; q < 10; q++) S.phase_ms[q] = o.phase_ns[q] * 1e-6;
+        }
+        if (s_k < 0 && (worst >= 0 || s_k < worst)) worst = s_k;
+        else if (worst >= 0 && s_k > worst) worst = s_k;
+    }
+    if (abort_flag) ygpu_set_error("a device-side wait hit its iteration limit (team barrier timeout)");
+    return worst;
+}
+
 extern "C" int ygpu_solve_batch_device(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n_inst,
                                        const ygpu_fields* inst, ygpu_stats* stats) {
     if (!c) { ygpu_set_error("context is NULL"); return YGPU_ERR_BAD_ARG; }
+    if (n_inst > 1 && c->max_active_unknowns > 0) {
+        size_t total = 0;
+        for (int k = 0; k < n_inst; k++) total += (size_t)2 * inst[k].nx * inst[k].ny;
+        if (total > c->max_active_unknowns) {
+            int st = ygpu_check_par(par);
+            if (st) return st;
+            if (kind != YGPU_KIND_SSA && kind != YGPU_KIND_DIVA) { ygpu_set_error("bad solver kind %d", kind); return YGPU_ERR_BAD_ARG; }
+            for (int k = 0; k < n_inst; k++)
+                if ((st = ygpu_fields_check(kind, &inst[k]))) return st;
+            CK(cudaSetDevice(c->device));
+            return solve_queue(c, kind, par, n_inst, inst, stats);
+        }
+    }
     return solve_batch(c, kind, par, n_inst, inst, stats);
 }
 

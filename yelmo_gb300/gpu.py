@@ -233,12 +233,13 @@ class DeviceSolver:
         out["return"] = r
         return out
 
-    def set_tuning(self, check_every: int = 4, use_graphs: bool = True, unknowns_per_cta: int = 512):
-        """ygpu_ctx_set_tuning: host-check interval, chunk graphs, team size."""
-        t = abi.Tuning(check_every, 1 if use_graphs else 0, unknowns_per_cta)
+    def set_tuning(self, check_every: int = 4, use_graphs: bool = True, unknowns_per_cta: int = 512,
+                   max_active_unknowns: int = 1_500_000):
+        """ygpu_ctx_set_tuning: host-check interval, chunk graphs, team size, queue threshold."""
+        t = abi.Tuning(check_every, 1 if use_graphs else 0, unknowns_per_cta, max_active_unknowns)
         _check(self.L.ygpu_ctx_set_tuning(self.ctx, C.byref(t)))
         self.tuning = {"check_every": check_every, "use_graphs": bool(use_graphs),
-                       "unknowns_per_cta": unknowns_per_cta}
+                       "unknowns_per_cta": unknowns_per_cta, "max_active_unknowns": max_active_unknowns}
 
     def solve_batch(self, kind: int, par: YdynParams, fields: list) -> list:
         n = len(fields)
