@@ -324,7 +324,7 @@ def run_served(args):
         "config": {"workload": f"served ensemble stream: {n_mem} SSA members, sides 64-321 "
                                f"({cells} cells resident), warm starts, continuous batching",
                    "rates_req_s": rates, "picard_tol": insts[0].par.ssa_iter_conv, "lin": insts[0].par.lis_opt,
-                   "hbm_budget_gb": 150, "max_slots": args.max_slots or 16, "parallelism": "replicas x1"},
+                   "hbm_budget_gb": 150, "max_slots": args.max_slots or "one per SM", "max_active_unknowns": 1500000, "parallelism": "replicas x1"},
         "latency_ms": {"p50": top_m["p50_ms"], "p99": top_m["p99_ms"]},
         "served_mixed": out["mixed"], "served_fp64": out["fp64"],
         "mixed_over_fp64": top_m["throughput"] / top_d["throughput"],
@@ -346,7 +346,7 @@ def main():
     ap.add_argument("--rates", default="10,100,500,2000", help="served workload: offered req/s")
     ap.add_argument("--seconds", type=float, default=5.0, help="served workload: arrival span per rate")
     ap.add_argument("--max-requests", type=int, default=1500, help="served workload: requests per rate")
-    ap.add_argument("--max-slots", type=int, default=0, help="served workload: solves on the GPU at once (0: the library default, 16)")
+    ap.add_argument("--max-slots", type=int, default=0, help="served workload: solves on the GPU at once (0: one per SM, load-limited by unknowns)")
     args = ap.parse_args()
     if args.workload == "served" and args.impl == "ours":
         if int(os.environ.get("RANK", "0")) == 0:

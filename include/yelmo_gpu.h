@@ -353,7 +353,8 @@ int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, const ygpu_fiel
  * run in submission order, one at a time.
  *
  * Admission by device memory: the server never holds more than hbm_budget
- * bytes. A member that does not fit is refused (YGPU_ERR_ADMISSION); a request
+ * bytes. Admission by load: at most max_slots solves and max_active_unknowns
+ * unknowns are on the GPU at once. A member that does not fit is refused (YGPU_ERR_ADMISSION); a request
  * waits until a slot (the scratch of one solve, sized for the largest member)
  * is free or can be allocated within the budget.
  */
@@ -368,7 +369,9 @@ typedef struct ygpu_server_cfg {
     int    lateral_bc;          /* YGPU_LATBC_*                                  */
     double dH_sigma;            /* standard deviation of the per-step dH (m)     */
     unsigned long long hbm_budget; /* device bytes the server may hold         */
-    int    max_slots;           /* solves on the GPU at once (0: 16)             */
+    int    max_slots;           /* solves on the GPU at once (0: one per SM)     */
+    unsigned long long max_active_unknowns; /* admission also stops at this many unknowns
+                                   on the GPU (0: 1.5 M)                           */
 } ygpu_server_cfg;
 
 typedef struct ygpu_server_info {

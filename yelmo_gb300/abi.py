@@ -101,6 +101,7 @@ class ServerCfg(C.Structure):
         ("device", C.c_int), ("kind", C.c_int), ("par", DynPar),
         ("grad_lim", C.c_double), ("taud_lim", C.c_double), ("lateral_bc", C.c_int),
         ("dH_sigma", C.c_double), ("hbm_budget", C.c_ulonglong), ("max_slots", C.c_int),
+        ("max_active_unknowns", C.c_ulonglong),
     ]
 
 

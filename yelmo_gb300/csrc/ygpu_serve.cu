@@ -109,6 +109,8 @@ struct ygpu_server {
     int max_slots = 1;
     bool mixed = false;
     bool block = false;            // tile-block preconditioner scratch
+    size_t max_active_nu = 0;      // admission: unknowns of the active solves
+    size_t active_nu = 0;
     size_t held = 0;               // device bytes held
     std::deque<Member> members;
     std::deque<Request> requests;  // index = request id; references stay valid on growth
@@ -193,6 +195,9 @@ static std::vector<Admit> admit_locked(ygpu_server* S) {
         Request& R = S->requests[*it];
         Member& M = S->members[R.member];
         if (M.busy) { ++it; continue; }
+        const size_t nu = (size_t)2 * M.nx * M.ny;
+        const bool idle = S->active.empty() && got.empty();
+        if (!idle && S->active_nu + nu > S->max_active_nu) break;     // FIFO: wait for retirements
         const size_t need = ygpu_inst_scratch_bytes(M.nx, M.ny, M.nz, S->mixed, S->block);
         int s = -1;
         for (int k = 0; k < (int)S->slots.size(); k++)
@@ -223,6 +228,7 @@ static std::vector<Admit> admit_locked(ygpu_server* S) {
         sl.member = R.member;
         sl.work = (size_t)M.nx * M.ny * M.nz;
         M.busy = true;
+        S->active_nu += nu;
         R.state = 1;
         R.t_admit = now_s();
         R.step = M.steps++;
@@ -359,6 +365,7 @@ static void retire_locked(ygpu_server* S) {
         St.device_ms = (R.t_done - R.t_admit) * 1e3;
         for (int q = 0; q < 10; q++) St.phase_ms[q] = o.phase_ns[q] * 1e-6;
         S->members[R.member].busy = false;
+        S->active_nu -= (size_t)2 * S->members[R.member].nx * S->members[R.member].ny;
         sl.req = -1;
         sl.member = -1;
         S->completed++;
@@ -423,11 +430,13 @@ extern "C" ygpu_server* ygpu_server_create(const ygpu_server_cfg* cfg) {
         delete S;
         return nullptr;
     }
-    // default concurrency: 16 solves. Every tick advances all active solves by
-    // one Picard iteration and waits for the slowest linear solve among them;
-    // fewer, larger teams waste less of the tick (256 uneven members: 116
-    // solves/s at 16, 96 at 64, 62 at 152 concurrent solves)
-    S->max_slots = cfg->max_slots > 0 ? cfg->max_slots : std::min(16, ygpu_sm_count(cfg->device));
+    // Concurrency: every tick advances all active solves by one Picard iteration
+    // and waits for the slowest linear solve among them, so fewer, larger teams
+    // waste less of the tick. By default at most 1.5 M unknowns are active (256
+    // uneven members of 64-321 cells a side: 116 solves/s with 16 active, 96
+    // with 64, 62 with 152), and never more solves than SMs.
+    S->max_slots = cfg->max_slots > 0 ? cfg->max_slots : ygpu_sm_count(cfg->device);
+    S->max_active_nu = cfg->max_active_unknowns > 0 ? (size_t)cfg->max_active_unknowns : (size_t)1500000;
     if (S->max_slots > 4096) S->max_slots = 4096;
     const int ms = S->max_slots;
     bool ok = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) == cudaSuccess;

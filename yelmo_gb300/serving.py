@@ -22,7 +22,7 @@ class Server:
     """One serving loop on one GPU."""
 
     def __init__(self, par: YdynParams, device: int = 0, dH_sigma: float = 5.0,
-                 hbm_budget: float = 150e9, max_slots: int = 0):
+                 hbm_budget: float = 150e9, max_slots: int = 0, max_active_unknowns: int = 0):
         self.L = lib()
         cfg = abi.ServerCfg()
         cfg.device = device
@@ -34,6 +34,7 @@ class Server:
         cfg.dH_sigma = dH_sigma
         cfg.hbm_budget = int(hbm_budget)
         cfg.max_slots = max_slots
+        cfg.max_active_unknowns = max_active_unknowns
         self.par = par
         self.srv = self.L.ygpu_server_create(C.byref(cfg))
         if not self.srv:
