@@ -374,19 +374,13 @@ void ygpu_fill_inst(Inst& I, int kind, const ygpu_fields* f) {
 
 int ygpu_single_team_ctas(int max_ctas, size_t nu, int unknowns_per_cta) {
     const int upc = unknowns_per_cta > 0 ? unknowns_per_cta : 2 * YG_BLOCK;
-    int want = (int)((nu + upc - 1) / upc);
-    const char* v = getenv("YGPU_TEAM_CTAS");
-    int tc = (v && *v) ? atoi(v) : want;
+    int tc = (int)((nu + upc - 1) / upc);
     if (tc < 1) tc = 1;
     if (tc > max_ctas) tc = max_ctas;
     if (tc > YG_MAX_TEAM_CTAS) tc = YG_MAX_TEAM_CTAS;
     return tc;
 }
 
-static int env_int(const char* name, int dflt) {
-    const char* v = getenv(name);
-    return (v && *v) ? atoi(v) : dflt;
-}
 
 // Launch shape of a batch: (n_teams, team_ctas).
 void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, int* team_ctas, int upc) {
@@ -403,8 +397,7 @@ void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, in
     int by_size = (int)(max_nu / 4096);
     if (auto_tc > by_size) auto_tc = by_size;
     if (auto_tc < 1) auto_tc = 1;
-    int tc = env_int("YGPU_BATCH_TEAM_CTAS", auto_tc);
-    if (tc < 1) tc = 1;
+    int tc = auto_tc;
     if (tc > maxc) tc = maxc;
     if (tc > YG_MAX_TEAM_CTAS) tc = YG_MAX_TEAM_CTAS;
     int nt = maxc / tc;
@@ -416,8 +409,6 @@ void ygpu_choose_teams(int max_ctas, int n_inst, size_t max_nu, int* n_teams, in
 
 bool ygpu_plan_teams(int max_ctas, int n, const size_t* nu, std::vector<int>& map, int* grid, int upc) {
     if (n < 1 || n > max_ctas) return false;
-    if (const char* v = getenv("YGPU_UNIFORM_TEAMS"))
-        if (*v && atoi(v) != 0) return false;
     std::vector<int> cnt(n, 1), cap(n);
     for (int q = 0; q < n; q++) cap[q] = ygpu_single_team_ctas(max_ctas, nu[q], upc);
     // greedy: the next CTA goes to the instance with the most unknowns per CTA

@@ -2872,10 +2872,6 @@ int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh) {
         return YGPU_ERR_CUDA;
     }
     int ktc = team_ctas;
-    if (const char* e = getenv("YGPU_KRYLOV_CTAS")) {
-        const int v = atoi(e);
-        if (v > 0) ktc = v;
-    }
     if (ktc < 1) ktc = 1;
     if (ktc > kmax) ktc = kmax;
     int knt = kmax / ktc;
