@@ -242,6 +242,21 @@ int ygpu_linear_solver_matrix_solve(int nmax, const int* a_ptr, const int* a_ind
                                     double* x_value, const char* lis_opt,
                                     int* lin_iter, int* status, double* L2_rel_norm);
 
+/*
+ * neff_hook of calc_velocity_diva (velocity_diva.f90:390-400; the hook of
+ * calc_ydyn, src/yelmo_dynamics.f90:357-411): after every Picard iteration the
+ * hook recomputes c_bed (in place) from the iteration's basal velocity ux_b,
+ * uy_b (host arrays, nx*ny, Fortran order), as a steady hydrology does for the
+ * effective pressure; the solve has converged only when c_bed also changed by
+ * less than ssa_iter_conv (relative L1). ygpu_set_neff_hook sets the hook of
+ * the calling thread (NULL clears it); it applies to the DIVA solves of
+ * ygpu_calc_velocity_diva (c_bed is then in/out: the hook receives the caller's
+ * array) and of ygpu_solve_device (the hook receives a library buffer and the
+ * device c_bed is updated).
+ */
+typedef void (*ygpu_neff_hook)(void* user, double* c_bed, const double* ux_b, const double* uy_b, int nx, int ny);
+void ygpu_set_neff_hook(ygpu_neff_hook hook, void* user);
+
 /* ======================================================================== */
 /* Device-resident API: the solve on fields already in GPU memory.           */
 /* ======================================================================== */

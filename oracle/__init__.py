@@ -34,6 +34,8 @@ def lib():
         L = C.CDLL(LIB_PATH)
         abi.declare_velocity(L.orc_calc_velocity_ssa, abi.SSA_ARGS)
         abi.declare_velocity(L.orc_calc_velocity_diva, abi.DIVA_ARGS)
+        abi.declare_velocity(L.orc_calc_velocity_diva_hook, abi.DIVA_ARGS)
+        L.orc_calc_velocity_diva_hook.argtypes = L.orc_calc_velocity_diva_hook.argtypes + [abi.NEFF_HOOK, C.c_void_p]
         abi.declare_inputs(L.orc_calc_dyn_inputs)
         abi.declare_masks(L.orc_set_ssa_masks)
         dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
@@ -81,13 +83,18 @@ def prepare(inst) -> dict:
     return f
 
 
-def calc_velocity(fields: dict, inst, par=None) -> dict:
-    """Run orc_calc_velocity_ssa / _diva on ``fields`` (updated in place)."""
+def calc_velocity(fields: dict, inst, par=None, neff_hook=None) -> dict:
+    """Run orc_calc_velocity_ssa / _diva on ``fields`` (updated in place);
+    neff_hook(c_bed, ux_b, uy_b) as in yelmo_gb300.gpu.calc_velocity (DIVA)."""
     par = par or inst.par
     cpar = par.to_c()
     if par.solver == "ssa":
         return abi.call_velocity(lib().orc_calc_velocity_ssa, abi.SSA_ARGS, fields, inst.dx, inst.dx,
                                  inst.n_glen, cpar)
+    if neff_hook:
+        cb = abi.neff_hook(neff_hook)
+        return abi.call_velocity(lib().orc_calc_velocity_diva_hook, abi.DIVA_ARGS, fields, inst.dx, inst.dx,
+                                 inst.n_glen, cpar, extra=(cb, None))
     return abi.call_velocity(lib().orc_calc_velocity_diva, abi.DIVA_ARGS, fields, inst.dx, inst.dx,
                              inst.n_glen, cpar)
 

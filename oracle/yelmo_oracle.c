@@ -2131,6 +2131,43 @@ int orc_calc_velocity_ssa(double* ux_b, double* uy_b, double* taub_acx, double* 
     return status;
 }
 
+/* calc_velocity_diva with the optional neff_hook (velocity_diva.f90:390-400):
+   after every Picard iteration the hook recomputes c_bed from the basal velocity,
+   and the iteration has converged only if c_bed also changed by less than
+   ssa_iter_conv in relative L1 */
+static int diva_solve(double* ux, double* uy, double* ux_bar, double* uy_bar, double* ux_b, double* uy_b,
+                      double* ux_i, double* uy_i, double* taub_acx, double* taub_acy, double* beta,
+                      double* beta_acx, double* beta_acy, double* beta_eff, double* visc_eff, double* visc_eff_int,
+                      double* duxdz, double* duydz, int* mx, int* my, double* ssa_err_acx, double* ssa_err_acy,
+                      int* ssa_iter_now, int* ssa_lin_iter, int* ssa_lin_fail, int* ssa_lim_n, double* c_bed,
+                      const double* f_slide, const double* taud_acx, const double* taud_acy,
+                      const double* taul_int_acx, const double* taul_int_acy, const double* H_ice,
+                      const double* f_ice, const double* H_grnd, const double* f_grnd, const double* f_grnd_acx,
+                      const double* f_grnd_acy, const double* ATT, const double* zeta_aa, const double* z_sl,
+                      const double* z_bed, double dx, double dy, double n_glen, int nx, int ny, int nz,
+                      const ygpu_dyn_par* p, orc_neff_hook hook, void* user);
+
+int orc_calc_velocity_diva_hook(double* ux, double* uy, double* ux_bar, double* uy_bar, double* ux_b, double* uy_b,
+                                double* ux_i, double* uy_i, double* taub_acx, double* taub_acy, double* beta,
+                                double* beta_acx, double* beta_acy, double* beta_eff, double* visc_eff,
+                                double* visc_eff_int, double* duxdz, double* duydz, int* mx, int* my,
+                                double* ssa_err_acx, double* ssa_err_acy, int* ssa_iter_now, int* ssa_lin_iter,
+                                int* ssa_lin_fail, int* ssa_lim_n, double* c_bed, const double* f_slide,
+                                const double* taud_acx, const double* taud_acy, const double* taul_int_acx,
+                                const double* taul_int_acy, const double* H_ice, const double* f_ice,
+                                const double* H_grnd, const double* f_grnd, const double* f_grnd_acx,
+                                const double* f_grnd_acy, const double* ATT, const double* zeta_aa,
+                                const double* z_sl, const double* z_bed, const double* z_srf, double dx, double dy,
+                                double n_glen, int nx, int ny, int nz, const ygpu_dyn_par* p, orc_neff_hook hook,
+                                void* user) {
+    (void)z_srf;
+    return diva_solve(ux, uy, ux_bar, uy_bar, ux_b, uy_b, ux_i, uy_i, taub_acx, taub_acy, beta, beta_acx, beta_acy,
+                      beta_eff, visc_eff, visc_eff_int, duxdz, duydz, mx, my, ssa_err_acx, ssa_err_acy, ssa_iter_now,
+                      ssa_lin_iter, ssa_lin_fail, ssa_lim_n, c_bed, f_slide, taud_acx, taud_acy, taul_int_acx,
+                      taul_int_acy, H_ice, f_ice, H_grnd, f_grnd, f_grnd_acx, f_grnd_acy, ATT, zeta_aa, z_sl, z_bed,
+                      dx, dy, n_glen, nx, ny, nz, p, hook, user);
+}
+
 int orc_calc_velocity_diva(double* ux, double* uy, double* ux_bar, double* uy_bar, double* ux_b, double* uy_b,
                            double* ux_i, double* uy_i, double* taub_acx, double* taub_acy, double* beta,
                            double* beta_acx, double* beta_acy, double* beta_eff, double* visc_eff,
@@ -2144,10 +2181,30 @@ int orc_calc_velocity_diva(double* ux, double* uy, double* ux_bar, double* uy_ba
                            const double* z_bed, const double* z_srf, double dx, double dy, double n_glen, int nx,
                            int ny, int nz, const ygpu_dyn_par* p) {
     (void)z_srf;
+    /* without a hook c_bed is only read */
+    return diva_solve(ux, uy, ux_bar, uy_bar, ux_b, uy_b, ux_i, uy_i, taub_acx, taub_acy, beta, beta_acx, beta_acy,
+                      beta_eff, visc_eff, visc_eff_int, duxdz, duydz, mx, my, ssa_err_acx, ssa_err_acy, ssa_iter_now,
+                      ssa_lin_iter, ssa_lin_fail, ssa_lim_n, (double*)c_bed, f_slide, taud_acx, taud_acy,
+                      taul_int_acx, taul_int_acy, H_ice, f_ice, H_grnd, f_grnd, f_grnd_acx, f_grnd_acy, ATT, zeta_aa,
+                      z_sl, z_bed, dx, dy, n_glen, nx, ny, nz, p, NULL, NULL);
+}
+
+static int diva_solve(double* ux, double* uy, double* ux_bar, double* uy_bar, double* ux_b, double* uy_b,
+                      double* ux_i, double* uy_i, double* taub_acx, double* taub_acy, double* beta,
+                      double* beta_acx, double* beta_acy, double* beta_eff, double* visc_eff, double* visc_eff_int,
+                      double* duxdz, double* duydz, int* mx, int* my, double* ssa_err_acx, double* ssa_err_acy,
+                      int* ssa_iter_now, int* ssa_lin_iter, int* ssa_lin_fail, int* ssa_lim_n, double* c_bed,
+                      const double* f_slide, const double* taud_acx, const double* taud_acy,
+                      const double* taul_int_acx, const double* taul_int_acy, const double* H_ice,
+                      const double* f_ice, const double* H_grnd, const double* f_grnd, const double* f_grnd_acx,
+                      const double* f_grnd_acy, const double* ATT, const double* zeta_aa, const double* z_sl,
+                      const double* z_bed, double dx, double dy, double n_glen, int nx, int ny, int nz,
+                      const ygpu_dyn_par* p, orc_neff_hook hook, void* user) {
     if (nx < 3 || ny < 3 || nz < 2) return YGPU_ERR_BAD_ARG;
     size_t n2 = (size_t)nx * ny, n3 = n2 * nz;
     int bc = p->boundaries;
     double* visc_nm1 = malloc(n3 * sizeof(double));
+    double* cb_nm1 = hook ? malloc(n2 * sizeof(double)) : NULL;
     double* uxp = malloc(n2 * sizeof(double));
     double* uyp = malloc(n2 * sizeof(double));
     double* bex = malloc(n2 * sizeof(double));
@@ -2222,8 +2279,22 @@ int orc_calc_velocity_diva(double* ux, double* uy, double* ux_bar, double* uy_ba
             }
         }
         if (conv < 0) { status = YGPU_ERR_NONFINITE; break; }
+        if (hook) {
+            /* neff_hook: c_bed from this iteration's basal velocity; converged only
+               if c_bed changed by less than ssa_iter_conv (relative L1) */
+            memcpy(cb_nm1, c_bed, n2 * sizeof(double));
+            hook(user, c_bed, ux_b, uy_b, nx, ny);
+            double dsum = 0.0, csum = 0.0;
+            for (size_t c = 0; c < n2; c++) {
+                dsum += fabs(c_bed[c] - cb_nm1[c]);
+                csum += fabs(c_bed[c]);
+            }
+            if (dsum > p->ssa_iter_conv * (csum > TOL_UNDERFLOW ? csum : TOL_UNDERFLOW) && iter < p->ssa_iter_max)
+                conv = 0;
+        }
         if (conv) break;
     }
+    free(cb_nm1);
     if (status >= 0) {
         *ssa_lim_n = count_lim_faces(ux_bar, uy_bar, mx, my, p->ssa_vel_max, drag, bc, nx, ny);
         vel_horizontal_3D(ux, uy, ux_b, uy_b, taub_acx, taub_acy, visc_eff, H_ice, f_ice, zeta_aa, bc, nx, ny, nz);

@@ -106,6 +106,27 @@ int orc_calc_velocity_diva(
     double dx, double dy, double n_glen,
     int nx, int ny, int nz, const ygpu_dyn_par* par);
 
+/* neff_hook of calc_velocity_diva: c_bed (in/out) from the basal velocity */
+typedef void (*orc_neff_hook)(void* user, double* c_bed, const double* ux_b, const double* uy_b, int nx, int ny);
+int orc_calc_velocity_diva_hook(
+    double* ux, double* uy, double* ux_bar, double* uy_bar,
+    double* ux_b, double* uy_b, double* ux_i, double* uy_i,
+    double* taub_acx, double* taub_acy,
+    double* beta, double* beta_acx, double* beta_acy, double* beta_eff,
+    double* visc_eff, double* visc_eff_int, double* duxdz, double* duydz,
+    int* ssa_mask_acx, int* ssa_mask_acy, double* ssa_err_acx, double* ssa_err_acy,
+    int* ssa_iter_now, int* ssa_lin_iter, int* ssa_lin_fail, int* ssa_lim_n,
+    double* c_bed, const double* f_slide,
+    const double* taud_acx, const double* taud_acy,
+    const double* taul_int_acx, const double* taul_int_acy,
+    const double* H_ice, const double* f_ice, const double* H_grnd, const double* f_grnd,
+    const double* f_grnd_acx, const double* f_grnd_acy,
+    const double* ATT, const double* zeta_aa,
+    const double* z_sl, const double* z_bed, const double* z_srf,
+    double dx, double dy, double n_glen,
+    int nx, int ny, int nz, const ygpu_dyn_par* par, orc_neff_hook hook, void* user);
+
+
 int orc_set_ssa_masks(int* mask_acx, int* mask_acy, const int* mask_frnt,
                       const double* f_ice, const double* f_grnd, int lateral_bc, int bc,
                       int nx, int ny);

@@ -181,10 +181,25 @@ def ptr(a: np.ndarray, kind: str):
     return a.ctypes.data_as(_dp if kind == "d" else _ip)
 
 
-def call_velocity(fn, args, fields: dict, dx, dy, n_glen, par: DynPar):
+# neff_hook of calc_velocity_diva: (user, c_bed in/out, ux_b, uy_b, nx, ny)
+NEFF_HOOK = C.CFUNCTYPE(None, C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_int)
+
+
+def neff_hook(fn):
+    """Wrap fn(c_bed, ux_b, uy_b) -- (nx, ny) Fortran-ordered views, c_bed
+    updated in place -- as a C callback (keep the result alive during the call)."""
+    def _cb(user, cb, ub, vb, nx, ny):
+        n = nx * ny
+        view = lambda p: np.ctypeslib.as_array(p, shape=(n,)).reshape((nx, ny), order="F")
+        fn(view(cb), view(ub), view(vb))
+    return NEFF_HOOK(_cb)
+
+
+def call_velocity(fn, args, fields: dict, dx, dy, n_glen, par: DynPar, extra=()):
     """Call a calc_velocity_* style entry with a dict of named numpy arrays.
 
     Scalars ssa_iter_now etc. are returned in a dict; arrays are updated in place.
+    `extra` arguments are appended after the parameters.
     """
     nx, ny = fields["H_ice"].shape
     nz = fields["zeta_aa"].shape[0]
@@ -196,7 +211,7 @@ def call_velocity(fn, args, fields: dict, dx, dy, n_glen, par: DynPar):
         else:
             cargs.append(ptr(fields[n], t))
     st = fn(*cargs, C.c_double(dx), C.c_double(dy), C.c_double(n_glen),
-            C.c_int(nx), C.c_int(ny), C.c_int(nz), C.byref(par))
+            C.c_int(nx), C.c_int(ny), C.c_int(nz), C.byref(par), *extra)
     out = {n: v.value for n, v in scal.items()}
     out["status"] = int(st)
     return out

@@ -169,6 +169,7 @@ struct ygpu_ctx {
     GraphCache graph;               // chunk graph of the last launch shape
     bool use_graphs = true;
     int check_every = 4;            // Picard iterations between host checks
+    std::vector<double> hook_buf;   // host buffers of the neff hook
     int unknowns_per_cta = 0;       // team size: unknowns per CTA (0: 2 x block)
     size_t max_active_unknowns = 1500000;   // batches beyond this run as a queue (continuous batching)
     int* h_flags = nullptr;         // pinned: finished count, abort flag
@@ -260,6 +261,14 @@ extern "C" void ygpu_ctx_destroy(ygpu_ctx* c) {
 }
 
 extern "C" void* ygpu_ctx_stream(ygpu_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+// neff hook of the calling thread (DIVA single solves)
+static thread_local ygpu_neff_hook t_hook = nullptr;
+static thread_local void* t_hook_user = nullptr;
+extern "C" void ygpu_set_neff_hook(ygpu_neff_hook hook, void* user) {
+    t_hook = hook;
+    t_hook_user = hook ? user : nullptr;
+}
 
 // default context of the calling thread (host-pointer entry points)
 static thread_local ygpu_ctx* t_ctx = nullptr;
@@ -438,7 +447,7 @@ bool ygpu_plan_teams(int max_ctas, int n, const size_t* nu, std::vector<int>& ma
 }
 
 static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, const ygpu_fields* inst,
-                       ygpu_stats* stats) {
+                       ygpu_stats* stats, double* host_cbed = nullptr) {
     int st = ygpu_check_par(par);
     if (st) return st;
     if (kind != YGPU_KIND_SSA && kind != YGPU_KIND_DIVA) { ygpu_set_error("bad solver kind %d", kind); return YGPU_ERR_BAD_ARG; }
@@ -505,10 +514,31 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     }
     CK(cudaMemcpyAsync(c->d_insts, c->h_insts.data(), sizeof(Inst) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->d_out, 0, sizeof(InstOut) * (size_t)n, c->stream));
+    // neff hook of the calling thread: single DIVA solves, one iteration at a time
+    NeffRun hr;
+    const bool hooked = (t_hook && kind == YGPU_KIND_DIVA && n == 1);
+    if (hooked) {
+        const size_t n2 = (size_t)inst[0].nx * inst[0].ny;
+        c->hook_buf.resize(4 * n2);
+        hr.fn = t_hook;
+        hr.user = t_hook_user;
+        hr.nx = inst[0].nx;
+        hr.ny = inst[0].ny;
+        hr.d_out = c->d_out;
+        hr.d_cbed = (double*)inst[0].c_bed;
+        hr.d_uxb = inst[0].ux_b;
+        hr.d_uyb = inst[0].uy_b;
+        hr.h_cbed = host_cbed ? host_cbed : c->hook_buf.data();
+        hr.h_uxb = c->hook_buf.data() + n2;
+        hr.h_uyb = c->hook_buf.data() + 2 * n2;
+        hr.h_prev = c->hook_buf.data() + 3 * n2;
+        const int one = 1;
+        CK(cudaMemcpyAsync(&c->d_out[0].defer, &one, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    }
     CK(cudaEventRecord(c->e0, c->stream));
     st = ygpu_launch_solver(c->device, c->stream, c->d_insts, n, *par, c->d_ctl, n_ctl, team_ctas, c->d_misc,
                             c->d_misc + 1, mapped ? c->d_map : nullptr, map_grid, c->use_graphs ? &c->graph : nullptr,
-                            c->h_flags, c->check_every);
+                            c->h_flags, c->check_every, hooked ? &hr : nullptr);
     if (st) return st;
     CK(cudaEventRecord(c->e1, c->stream));
     c->h_out.resize(n);
@@ -942,7 +972,9 @@ extern "C" int ygpu_calc_velocity_diva(double* ux, double* uy, double* ux_bar, d
     f.ATT = d(a_att); f.zeta_aa = d(a_z); f.z_sl = d(a_zsl); f.z_bed = d(a_zb); f.z_srf = d(a_zs);
     ygpu_stats sts;
     memset(&sts, 0, sizeof(sts));
-    st = solve_batch(c, YGPU_KIND_DIVA, par, 1, &f, &sts);
+    // with a neff hook the hook updates the caller's c_bed in place (as the
+    // reference's c_bed argument of the hook), and the device copy follows it
+    st = solve_batch(c, YGPU_KIND_DIVA, par, 1, &f, &sts, t_hook ? (double*)c_bed : nullptr);
     if (st == YGPU_ERR_CUDA || st == YGPU_ERR_NOMEM || st == YGPU_ERR_BAD_ARG) return st;
     int st2 = S.download(c);
     if (st2) return st2;

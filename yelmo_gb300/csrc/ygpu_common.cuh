@@ -104,6 +104,8 @@ struct InstOut {
     int lin_st;
     int lin_outer;
     double lin_rr;
+    int defer;         // set by the host: a finished solve waits for the host (neff hook)
+    int want_finish;   // the post step found the solve finished (deferred)
     double phase_ns[10];   // device time per phase: setup, strain, column, faces, system, krylov, epilogue,
                            // final, and the all-reduce share of the solve and of the Krylov phase
 };

@@ -11,6 +11,7 @@
 #endif
 
 struct Inst;
+struct InstOut;
 struct TeamCtl;
 
 // error message of the calling thread (ygpu_last_error)
@@ -69,12 +70,23 @@ void ygpu_step_timing_add(int kind, double ms);
 void ygpu_graph_cache_clear(GraphCache* gc);
 bool ygpu_step_timing_on();
 
+// A host hook between Picard iterations (neff_hook) of a single-instance solve
+struct NeffRun {
+    ygpu_neff_hook fn;
+    void* user;
+    int nx, ny;
+    InstOut* d_out;                // the instance's outputs (defer is set)
+    double *d_cbed, *d_uxb, *d_uyb;
+    double *h_cbed, *h_uxb, *h_uyb, *h_prev;   // host buffers of nx*ny
+};
+
 // The whole solve of n_inst instances on `stream`: setup, the Picard loop as
-// step launches (or chunk graphs with gc and pinned h_flags[2]), final passes.
+// step launches (or chunk graphs with gc and pinned h_flags[2]; or one
+// iteration at a time around a host hook), final passes.
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
                        TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort,
                        const int* d_map = nullptr, int map_grid = 0, GraphCache* gc = nullptr,
-                       int* h_flags = nullptr, int check_every = 4);
+                       int* h_flags = nullptr, int check_every = 4, const NeffRun* hook = nullptr);
 int ygpu_sm_count(int device);
 size_t ygpu_teamctl_bytes();
 size_t ygpu_inst_bytes();

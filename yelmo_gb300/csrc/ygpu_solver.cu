@@ -2585,6 +2585,12 @@ __device__ __noinline__ void step_post(const Inst& I, const ygpu_dyn_par& P, Tea
                    out->lin_it, out->lin_st);
         if (status == YGPU_OK && (red[3] > 0.0 || !isfinite(resid))) status = YGPU_ERR_NONFINITE;
         finish = (status != YGPU_OK) || resid < P.ssa_iter_conv || out->iter_now >= P.ssa_iter_max;
+        // with a host hook between iterations the host decides (it may find the
+        // hook's fields still changing); errors finish at once
+        if (finish && status == YGPU_OK && out->defer) {
+            if (lead) out->want_finish = 1;
+            finish = false;
+        }
     }
     const double t6 = clk.lap();
     if (finish && status == YGPU_OK) {
@@ -3075,7 +3081,7 @@ static bool capture_chunk(cudaStream_t stream, const StepShape& sh, const Inst* 
 
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
                        TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort, const int* d_map,
-                       int map_grid, GraphCache* gc, int* h_flags, int check_every) {
+                       int map_grid, GraphCache* gc, int* h_flags, int check_every, const NeffRun* hook) {
     // d_done: count of finished instances; d_abort: launch-wide abort flag.
     // With a team map (one team per instance) n_teams is the number of control
     // blocks to clear (n_inst) and map_grid the CTAs of the plan.
@@ -3094,7 +3100,7 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
     // and pinned flags, each chunk of `check` iterations is one CUDA graph
     // (captured once per launch shape and parameters, then replayed).
     const int check = check_every > 0 ? check_every : 4;
-    const bool use_graph = gc && h_flags && P.ssa_iter_max >= check;
+    const bool use_graph = gc && h_flags && P.ssa_iter_max >= check && !hook;
     const bool timed = ygpu_step_timing_on();
     if (use_graph) {
         GraphKey key;
@@ -3114,6 +3120,50 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
         }
     }
     int it = 0;
+    if (hook) {
+        // one iteration at a time, the host hook between iterations
+        const size_t n2 = (size_t)hook->nx * hook->ny;
+        for (; it < P.ssa_iter_max; it++) {
+            for (int step : {YG_STEP_PRE, YG_STEP_KRYLOV, YG_STEP_POST})
+                if ((st = ygpu_launch_step(step, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort))) return st;
+            InstOut o;
+            int ab = 0;
+            if (cudaMemcpyAsync(&o, hook->d_out, sizeof(InstOut), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+                cudaMemcpyAsync(&ab, d_abort, sizeof(int), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+                cudaMemcpyAsync(hook->h_uxb, hook->d_uxb, n2 * 8, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+                cudaMemcpyAsync(hook->h_uyb, hook->d_uyb, n2 * 8, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+                cudaMemcpyAsync(hook->h_cbed, hook->d_cbed, n2 * 8, cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+                cudaStreamSynchronize(stream) != cudaSuccess) {
+                ygpu_set_error("solver step failed: %s", cudaGetErrorString(cudaGetLastError()));
+                return YGPU_ERR_CUDA;
+            }
+            if (ab || o.done) break;
+            // the hook, and the relative L1 change of c_bed (velocity_diva.f90:396-399)
+            memcpy(hook->h_prev, hook->h_cbed, n2 * 8);
+            hook->fn(hook->user, hook->h_cbed, hook->h_uxb, hook->h_uyb, hook->nx, hook->ny);
+            double dsum = 0.0, csum = 0.0;
+            for (size_t c = 0; c < n2; c++) {
+                dsum += fabs(hook->h_cbed[c] - hook->h_prev[c]);
+                csum += fabs(hook->h_cbed[c]);
+            }
+            const bool cb_converged = !(dsum > P.ssa_iter_conv * (csum > 1e-15 ? csum : 1e-15));
+            if (cudaMemcpyAsync(hook->d_cbed, hook->h_cbed, n2 * 8, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
+                ygpu_set_error("c_bed upload failed: %s", cudaGetErrorString(cudaGetLastError()));
+                return YGPU_ERR_CUDA;
+            }
+            if (o.want_finish && (cb_converged || o.iter_now >= P.ssa_iter_max)) break;   // final passes below
+            if (o.want_finish) {
+                const int zero = 0;
+                if (cudaMemcpyAsync(&hook->d_out->want_finish, &zero, sizeof(int), cudaMemcpyHostToDevice, stream) !=
+                        cudaSuccess ||
+                    cudaStreamSynchronize(stream) != cudaSuccess) {
+                    ygpu_set_error("solver state update failed: %s", cudaGetErrorString(cudaGetLastError()));
+                    return YGPU_ERR_CUDA;
+                }
+            }
+        }
+        return ygpu_launch_step(YG_STEP_FINAL, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort);
+    }
     if (use_graph && gc->valid) {
         // whole chunks as graph replays
         while (it + check <= P.ssa_iter_max) {

@@ -36,7 +36,7 @@ EXPORTS = [
     "ygpu_server_create", "ygpu_server_destroy", "ygpu_server_add_member", "ygpu_server_submit",
     "ygpu_server_poll", "ygpu_server_wait", "ygpu_server_fetch", "ygpu_server_get_info",
     "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get", "ygpu_tuning_defaults",
-    "ygpu_ctx_set_tuning",
+    "ygpu_ctx_set_tuning", "ygpu_set_neff_hook",
 ]
 
 
@@ -90,6 +90,8 @@ def lib(build_if_missing: bool = True):
     L.ygpu_server_get_info.argtypes = [C.c_void_p, C.POINTER(abi.ServerInfo)]
     L.ygpu_kernel_launches.restype = C.c_ulonglong
     L.ygpu_tuning_defaults.argtypes = [C.POINTER(abi.Tuning)]
+    L.ygpu_set_neff_hook.argtypes = [abi.NEFF_HOOK, C.c_void_p]
+    L.ygpu_set_neff_hook.restype = None
     L.ygpu_ctx_set_tuning.argtypes = [C.c_void_p, C.POINTER(abi.Tuning)]
     L.ygpu_step_timing.argtypes = [C.c_int]
     L.ygpu_step_timing_get.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
@@ -107,15 +109,26 @@ def _check(st, allow_linear=True):
     return st
 
 
-def calc_velocity(fields: dict, dx: float, n_glen: float, par: YdynParams, dy: float | None = None) -> dict:
-    """calc_velocity_ssa / calc_velocity_diva on the GPU (host arrays, updated in place)."""
+def calc_velocity(fields: dict, dx: float, n_glen: float, par: YdynParams, dy: float | None = None,
+                  neff_hook=None) -> dict:
+    """calc_velocity_ssa / calc_velocity_diva on the GPU (host arrays, updated in place).
+
+    neff_hook(c_bed, ux_b, uy_b): DIVA only, called after every Picard iteration to
+    update c_bed in place (fields["c_bed"] is then in/out)."""
     L = lib()
     cpar = par.to_c()
     dy = dx if dy is None else dy
     if par.solver == "ssa":
         out = abi.call_velocity(L.ygpu_calc_velocity_ssa, abi.SSA_ARGS, fields, dx, dy, n_glen, cpar)
     else:
-        out = abi.call_velocity(L.ygpu_calc_velocity_diva, abi.DIVA_ARGS, fields, dx, dy, n_glen, cpar)
+        cb = abi.neff_hook(neff_hook) if neff_hook else None
+        if cb:
+            L.ygpu_set_neff_hook(cb, None)
+        try:
+            out = abi.call_velocity(L.ygpu_calc_velocity_diva, abi.DIVA_ARGS, fields, dx, dy, n_glen, cpar)
+        finally:
+            if cb:
+                L.ygpu_set_neff_hook(abi.NEFF_HOOK(), None)
     _check(out["status"])
     return out
 
