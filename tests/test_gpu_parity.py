@@ -3,7 +3,7 @@
 Bit-exact: the calc_ydyn prologue (flotation H_grnd, grounded fractions, ice
 front mask, driving and lateral stress) and the SSA masks. Converged solve:
 velocities, viscosity and friction within 1e-6 relative L2 of the oracle when
-both are converged tightly (spec parity bar), FP64 and mixed precision.
+both are converged tightly (the parity bar), FP64 and mixed precision.
 """
 import numpy as np
 import pytest

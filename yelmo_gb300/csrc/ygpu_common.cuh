@@ -117,7 +117,7 @@ YG_DEV unsigned long long global_ns() {
 }
 
 // Descriptor of one instance (device memory). Field pointers follow
-// ygpu_fields; the rest is scratch owned by the host driver.
+// ygpu_fields; the rest is scratch that the host code carves for the solve.
 struct Inst {
     int nx, ny, nz, n2, nu;
     int kind;                      // YGPU_KIND_*
