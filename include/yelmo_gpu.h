@@ -67,9 +67,9 @@ extern "C" {
 #define YGPU_LIN_MINRES       2
 #define YGPU_PRE_NONE         0
 #define YGPU_PRE_JACOBI       1
-#define YGPU_PRE_ILU0         2   /* GPU, mixed precision, energy form: block Jacobi with the exact
-                                     inverse of each 4x4-cell tile block (32 unknowns); Jacobi
-                                     elsewhere (FP64 solves, residual form)                    */
+#define YGPU_PRE_ILU0         2   /* GPU, energy form with CG: block Jacobi with the exact inverse
+                                     of each 4x4-cell tile block (32 unknowns, inverted in FP32);
+                                     Jacobi for the residual form and BiCGSTAB                  */
 
 /* ---- arithmetic of the GPU solve ---- */
 #define YGPU_PREC_FP64        0   /* plain FP64 solve: the drop-in                         */

@@ -1,6 +1,6 @@
-"""Tile-block preconditioner (-p ilu on the energy form, mixed precision).
+"""Tile-block preconditioner (-p ilu on the energy form, FP64 and mixed precision).
 
-The inner FP32 CG is preconditioned by the exact inverses of the 4 x 4-cell
+The CG (the inner FP32 one in mixed precision) is preconditioned by the exact inverses of the 4 x 4-cell
 tile blocks of the operator (block Jacobi). The converged solution must not
 depend on the preconditioner: it matches the oracle's FP64 solve within the
 parity bar, on grids whose sides are and are not multiples of the tile, and
@@ -18,17 +18,18 @@ pytestmark = pytest.mark.gpu
 ILU = "-i cg -p ilu -maxiter 20000 -tol 1.0e-11"
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", ["dome_ssa_energy", "marine_diva", "continent_diva"])
-def test_block_preconditioned_mixed_matches_oracle(name):
+def test_block_preconditioned_matches_oracle(name, precision):
     inst = case(name)
     f0 = _prepare_shared(inst)
     fo, fg, fj = _copy(f0), _copy(f0), _copy(f0)
     outo = oracle.calc_velocity(fo, inst)
-    par_b = inst.par.with_(precision="mixed", ssa_lis_opt_energy=ILU)
+    par_b = inst.par.with_(precision=precision, ssa_lis_opt_energy=ILU)
     outg = gpu.calc_velocity(fg, inst.dx, inst.n_glen, par_b)
     _compare(inst, fo, fg, outo, outg, TOL)
     # the same solve with Jacobi takes more linear iterations
-    outj = gpu.calc_velocity(fj, inst.dx, inst.n_glen, inst.par.with_(precision="mixed"))
+    outj = gpu.calc_velocity(fj, inst.dx, inst.n_glen, inst.par.with_(precision=precision))
     assert outg["ssa_lin_iter"] < outj["ssa_lin_iter"], (outg["ssa_lin_iter"], outj["ssa_lin_iter"])
 
 

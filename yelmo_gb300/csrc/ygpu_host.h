@@ -111,7 +111,7 @@ void ygpu_fill_inst(Inst& I, int kind, const ygpu_fields* f);
 size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block = false);
 void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed, bool block = false);
 inline bool ygpu_wants_block(const ygpu_dyn_par& p) {
-    return p.precision == YGPU_PREC_MIXED && p.lin_precond == YGPU_PRE_ILU0 && p.ssa_solver == YGPU_SSA_ENERGY;
+    return p.lin_precond == YGPU_PRE_ILU0 && p.ssa_solver == YGPU_SSA_ENERGY && p.lin_solver != YGPU_LIN_BICGSTAB;
 }
 size_t ygpu_align256(size_t b);
 int ygpu_single_team_ctas(int max_ctas, size_t nu, int unknowns_per_cta = 0);

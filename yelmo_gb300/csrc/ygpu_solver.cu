@@ -1977,11 +1977,11 @@ __device__ __noinline__ void block_setup(const Inst& I, const Geo& G, Team& Tm, 
 
 // out = M^-1 in for the whole team (tile mapping; the caller separates it from
 // row-mapped loops by team barriers)
-template <typename T>
-YG_DEV T block_apply_lane(const T* M, T w, int lane) {
+template <typename T, typename MT>
+YG_DEV T block_apply_lane(const MT* M, T w, int lane) {
     T acc = T(0);
 #pragma unroll
-    for (int k = 0; k < 32; k++) acc += M[k * 32 + lane] * __shfl_sync(0xffffffffu, w, k);
+    for (int k = 0; k < 32; k++) acc += (T)M[k * 32 + lane] * __shfl_sync(0xffffffffu, w, k);
     return acc;
 }
 
@@ -1990,7 +1990,7 @@ YG_DEV T block_apply_lane(const T* M, T w, int lane) {
 // preconditioner is applied to a tile's freshly computed vector through warp
 // shuffles in the same pass.
 template <typename T, typename Op>
-__device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op& A, const T* __restrict__ minv,
+__device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op& A, const float* __restrict__ minv,
                                                 T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
                                                 T* __restrict__ u, T* __restrict__ w, T* m0, T* m1, T* __restrict__ z,
                                                 T* __restrict__ q, T* __restrict__ s, T* __restrict__ p, int maxiter,
@@ -2144,6 +2144,11 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
     outer = 0;
     const StencilOp<double, double> A64{&I, &G, energy, I.visc_int, I.Nab, I.drag_x, I.drag_y, make_opk<double>(G)};
     if (P.precision != YGPU_PREC_MIXED) {
+        // -p ilu on the energy form: the FP32 tile inverses (built by the pre step)
+        // precondition the FP64 CG
+        if (use_cg && energy && P.lin_precond == YGPU_PRE_ILU0 && I.fminv)
+            return krylov_pcg_pipe_blk<double>(T, G, A64, I.fminv, I.x, I.b, I.r, I.rt, I.v, I.ph, I.m2, I.z, I.q,
+                                               I.s, I.p, P.lin_maxiter, P.lin_tol, bnrm, iters, relres, ok);
         if (use_cg)
             return krylov_pcg_pipe<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.rt, I.v, I.ph, I.m2, I.z, I.q, I.s,
                                            I.p, P.lin_maxiter, P.lin_tol, bnrm, pre, iters, relres, ok);
@@ -2442,6 +2447,12 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
     t3 = clk.lap();
     phase_system(I, P, G, T, bn2);
     if (!team_allreduce(T, &bn2, 1)) { status = YGPU_ERR_TIMEOUT; goto out_; }
+    if (!mixed && I.fminv && P.ssa_solver == YGPU_SSA_ENERGY && P.lin_precond == YGPU_PRE_ILU0) {
+        // FP64 solve with -p ilu: FP32 tile inverses from the FP64 coefficients
+        const StencilOp<float, double> Ab{&I, &G, true, I.visc_int, I.Nab, I.drag_x, I.drag_y, make_opk<float>(G)};
+        block_setup<float, double>(I, G, T, Ab, I.fminv);
+        if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
+    }
     if (mixed) {
         // FP32 copies of the operator coefficients and the Jacobi diagonal for
         // the inner solves, and the tile-block inverses of -p ilu
