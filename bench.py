@@ -15,8 +15,9 @@ Modes:
   correction.
 - The plain FP64 throughput, and single-solve latency p50/p99 for both precisions, are
   reported beside it.
-- ``e2e`` times the C-ABI drop-in ``ygpu_calc_velocity_diva`` on host buffers, with the
-  host-device copies inside the timed region.
+- ``e2e`` times the batched C-ABI entry ``ygpu_solve_batch_host`` on host buffers (the
+  same B solves per step, the host-device copies inside the timed region);
+  ``e2e_single`` the drop-in ``ygpu_calc_velocity_diva``, one solve per step.
 
 ``--workload ensemble`` runs the batched uneven ensemble instead: 256 SSA instances with
 sides in {41, 81, 121, 161}.
@@ -451,19 +452,32 @@ def main():
                      "u_single": u_single, "u_batch": u_batch, "all_sts": all_sts, "launches": launches,
                      "steps_timing": steps_timing}
 
-    # e2e: the C-ABI drop-in on host buffers (host-device copies inside the timed region)
-    e2e_times = []
+    # e2e: the batched C-ABI entry on host buffers (the whole batch per step, the
+    # host-device copies inside the timed region), and the single-solve drop-in
+    par_m = insts[0].par.with_(precision="mixed")
+    n_e2e = args.warmup + max(3, args.steps // 2)
+    e2e_times, e2e1_times = [], []
+    barrier()
+    for s in range(n_e2e):
+        fs = [_copy(h) for h in hosts]
+        t = time.perf_counter()
+        sts_h = gpu.calc_velocity_batch(fs, [i.dx for i in insts], insts[0].n_glen, par_m)
+        dt = time.perf_counter() - t
+        assert all(st["status"] == 0 for st in sts_h), sts_h
+        if s >= args.warmup:
+            e2e_times.append(dt)
+    e2e_ms = max_over_ranks(1e3 * sum(e2e_times), dist, f"cuda:{local}")
     if not ensemble:
-        par_m = insts[0].par.with_(precision="mixed")
-        for s in range(args.warmup + max(3, args.steps // 2)):
+        for s in range(n_e2e):
             f = _copy(hosts[0])
             t = time.perf_counter()
             gpu.calc_velocity(f, insts[0].dx, insts[0].n_glen, par_m)
             dt = time.perf_counter() - t
             if s >= args.warmup:
-                e2e_times.append(dt)
+                e2e1_times.append(dt)
     i0 = insts[0]
-    h2d, d2h = gpu.host_io_bytes(kind, i0.nx, i0.ny, i0.nz)
+    io = [gpu.host_io_bytes(kind, i.nx, i.ny, i.nz) for i in insts]
+    h2d, d2h = sum(a for a, _ in io), sum(b for _, b in io)
 
     if rank != 0:
         if dist is not None:
@@ -518,11 +532,13 @@ def main():
         "rel_err_mixed_vs_fp64_max": err_mixed_vs_fp64,
         "picard_iters": [s["ssa_iter_now"] for s in mixed["sts"][:4]],
         "gpu_launches": mixed["launches"],
-        "e2e": ({"value": 1.0 / statistics.mean(e2e_times), "unit": "solves/s", "h2d_bytes_per_step": h2d,
-                 "d2h_bytes_per_step": d2h,
-                 "path": ("ygpu_calc_velocity_diva" if kind == abi.KIND_DIVA else "ygpu_calc_velocity_ssa")
-                 + " on host buffers, one solve per step"}
-                if e2e_times else None),
+        "e2e": {"value": replica_throughput(world, batch, len(e2e_times), e2e_ms), "unit": "solves/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "path": f"ygpu_solve_batch_host on host buffers, {batch} solves per step"},
+        "e2e_single": ({"value": 1.0 / statistics.mean(e2e1_times), "unit": "solves/s",
+                        "h2d_bytes_per_step": io[0][0], "d2h_bytes_per_step": io[0][1],
+                        "path": ("ygpu_calc_velocity_diva" if kind == abi.KIND_DIVA else "ygpu_calc_velocity_ssa")
+                        + " on host buffers, one solve per step"} if e2e1_times else None),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "traffic": (ratio * alg_steps["krylov"] / max(kr_n, 1)) if ratio else None,

@@ -327,6 +327,16 @@ int ygpu_solve_batch_device(ygpu_ctx* ctx, int kind, const ygpu_dyn_par* par,
                             int n_inst, const ygpu_fields* inst, ygpu_stats* stats);
 
 /*
+ * Batched solve on HOST arrays (no counterpart in the reference): `host` holds
+ * n ygpu_fields of host pointers with the layouts and directions of
+ * ygpu_calc_velocity_ssa / _diva; the library copies them to the device, solves
+ * the batch as ygpu_solve_batch_device on the calling thread's default context
+ * and copies the in/out fields back.
+ */
+int ygpu_solve_batch_host(int kind, const ygpu_dyn_par* par, int n_inst, const ygpu_fields* host,
+                          ygpu_stats* stats);
+
+/*
  * ygpu_solve_device_noalloc -- no counterpart in the reference.
  * One solve on device-resident fields, like ygpu_solve_device, for callers that
  * cannot allocate device memory: a host capturing its work into a CUDA graph,

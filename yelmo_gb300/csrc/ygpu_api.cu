@@ -6,6 +6,7 @@
 
 #include <math.h>
 #include <stdarg.h>
+#include <stddef.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -982,6 +983,76 @@ extern "C" int ygpu_calc_velocity_diva(double* ux, double* uy, double* ux_bar, d
     *ssa_lin_fail = sts.ssa_lin_fail;
     *ssa_lim_n = sts.ssa_lim_n;
     return st;
+}
+
+// Batched solve on HOST arrays: every instance's fields (ygpu_fields of host
+// pointers) go to the device, the batch runs as ygpu_solve_batch_device, and the
+// in/out fields come back -- the arrays and directions of the single drop-ins.
+extern "C" int ygpu_solve_batch_host(int kind, const ygpu_dyn_par* par, int n, const ygpu_fields* host,
+                                     ygpu_stats* stats) {
+    int st = ygpu_check_par(par);
+    if (st) return st;
+    if (kind != YGPU_KIND_SSA && kind != YGPU_KIND_DIVA) { ygpu_set_error("bad solver kind %d", kind); return YGPU_ERR_BAD_ARG; }
+    if (n < 1 || !host) { ygpu_set_error("no instances"); return YGPU_ERR_BAD_ARG; }
+    for (int k = 0; k < n; k++)
+        if ((st = ygpu_fields_check(kind, &host[k]))) return st;
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const bool diva = (kind == YGPU_KIND_DIVA);
+    Staging S;
+    std::vector<std::vector<size_t>> ids(n);
+    // (field offset in ygpu_fields, 3D?, in, out) in the order of the single drop-ins
+    struct FD { size_t off; int dims; bool in, out, diva_only; };
+#define FO(name) offsetof(ygpu_fields, name)
+    static const FD tab[] = {
+        {FO(ux), 3, false, true, true}, {FO(uy), 3, false, true, true},
+        {FO(ux_bar), 2, true, true, true}, {FO(uy_bar), 2, true, true, true},
+        {FO(ux_b), 2, true, true, false}, {FO(uy_b), 2, true, true, false},
+        {FO(ux_i), 3, false, true, true}, {FO(uy_i), 3, false, true, true},
+        {FO(taub_acx), 2, true, true, false}, {FO(taub_acy), 2, true, true, false},
+        {FO(beta), 2, true, true, false}, {FO(beta_acx), 2, true, true, false}, {FO(beta_acy), 2, true, true, false},
+        {FO(beta_eff), 2, false, true, true},
+        {FO(visc_eff), 3, true, true, false}, {FO(visc_eff_int), 2, false, true, false},
+        {FO(duxdz), 3, false, true, true}, {FO(duydz), 3, false, true, true},
+        {FO(ssa_err_acx), 2, false, true, false}, {FO(ssa_err_acy), 2, false, true, false},
+        {FO(ssa_mask_acx), -2, true, false, false}, {FO(ssa_mask_acy), -2, true, false, false},
+        {FO(c_bed), 2, true, false, false}, {FO(f_slide), 2, true, false, false},
+        {FO(taud_acx), 2, true, false, false}, {FO(taud_acy), 2, true, false, false},
+        {FO(taul_int_acx), 2, true, false, false}, {FO(taul_int_acy), 2, true, false, false},
+        {FO(H_ice), 2, true, false, false}, {FO(f_ice), 2, true, false, false},
+        {FO(H_grnd), 2, true, false, false}, {FO(f_grnd), 2, true, false, false},
+        {FO(f_grnd_acx), 2, true, false, false}, {FO(f_grnd_acy), 2, true, false, false},
+        {FO(ATT), 3, true, false, false}, {FO(zeta_aa), 1, true, false, false},
+        {FO(z_sl), 2, true, false, false}, {FO(z_bed), 2, true, false, false}, {FO(z_srf), 2, true, false, false},
+    };
+#undef FO
+    const int nt = (int)(sizeof(tab) / sizeof(tab[0]));
+    for (int k = 0; k < n; k++) {
+        const ygpu_fields& h = host[k];
+        const size_t b2 = (size_t)h.nx * h.ny * 8, b3 = b2 * h.nz, i2 = (size_t)h.nx * h.ny * 4;
+        for (int q = 0; q < nt; q++) {
+            void* ptr = *(void* const*)((const char*)&h + tab[q].off);
+            if (!ptr || (tab[q].diva_only && !diva)) {
+                ids[k].push_back((size_t)-1);
+                continue;
+            }
+            const size_t bytes = tab[q].dims == 3 ? b3 : tab[q].dims == 2 ? b2 : tab[q].dims == -2 ? i2 : (size_t)h.nz * 8;
+            ids[k].push_back(S.add(ptr, bytes, tab[q].in, tab[q].out));
+        }
+    }
+    if ((st = S.upload(c))) return st;
+    std::vector<ygpu_fields> dev(n);
+    for (int k = 0; k < n; k++) {
+        dev[k] = host[k];
+        for (int q = 0; q < nt; q++) {
+            void** slot = (void**)((char*)&dev[k] + tab[q].off);
+            *slot = (ids[k][q] == (size_t)-1) ? nullptr : S.args[ids[k][q]].dev;
+        }
+    }
+    st = ygpu_solve_batch_device(c, kind, par, n, dev.data(), stats);
+    if (st == YGPU_ERR_CUDA || st == YGPU_ERR_NOMEM || st == YGPU_ERR_BAD_ARG) return st;
+    int st2 = S.download(c);
+    return st2 ? st2 : st;
 }
 
 extern "C" int ygpu_set_ssa_masks(int* mx, int* my, const int* mf, const double* f_ice, const double* f_grnd,

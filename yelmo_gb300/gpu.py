@@ -9,6 +9,8 @@ Mirrors the reference's solver interface for Python hosts:
 * ``calc_dyn_inputs(inst)`` / ``set_ssa_masks(...)`` / ``prepare(inst)`` -- the
   fields calc_ydyn derives before the solve and set_ssa_masks, on the GPU.
 * ``linear_solver_matrix_solve(...)`` -- the CSR seam of solver_linear.F90:151.
+* ``calc_velocity_batch(fields_list, dx, n_glen, par)`` -- many host states
+  in one call (one batched solve on the device).
 * ``DeviceSolver`` -- solves on device-resident fields (no host copies).
 
 There is no CPU fallback: if the library cannot be loaded, or no CUDA device is
@@ -36,7 +38,7 @@ EXPORTS = [
     "ygpu_server_create", "ygpu_server_destroy", "ygpu_server_add_member", "ygpu_server_submit",
     "ygpu_server_poll", "ygpu_server_wait", "ygpu_server_fetch", "ygpu_server_get_info",
     "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get", "ygpu_tuning_defaults",
-    "ygpu_ctx_set_tuning", "ygpu_set_neff_hook",
+    "ygpu_ctx_set_tuning", "ygpu_set_neff_hook", "ygpu_solve_batch_host",
 ]
 
 
@@ -75,6 +77,8 @@ def lib(build_if_missing: bool = True):
                                     C.POINTER(abi.Stats)]
     L.ygpu_solve_batch_device.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.DynPar), C.c_int,
                                           C.POINTER(abi.Fields), C.POINTER(abi.Stats)]
+    L.ygpu_solve_batch_host.argtypes = [C.c_int, C.POINTER(abi.DynPar), C.c_int, C.POINTER(abi.Fields),
+                                        C.POINTER(abi.Stats)]
     L.ygpu_solve_device_noalloc.argtypes = [C.c_int, C.POINTER(abi.DynPar), C.POINTER(abi.Fields),
                                             C.POINTER(abi.Stats), C.c_void_p]
     ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
@@ -131,6 +135,41 @@ def calc_velocity(fields: dict, dx: float, n_glen: float, par: YdynParams, dy: f
                 L.ygpu_set_neff_hook(abi.NEFF_HOOK(), None)
     _check(out["status"])
     return out
+
+
+_FIELDS_3D = {"ux", "uy", "ux_i", "uy_i", "visc_eff", "duxdz", "duydz", "ATT"}
+
+
+def calc_velocity_batch(fields: list, dx, n_glen: float, par: YdynParams) -> list:
+    """calc_velocity on a batch of host states in one call (ygpu_solve_batch_host).
+
+    fields: dicts as for calc_velocity, updated in place; dx: one grid spacing or
+    one per instance (dy = dx). Returns the per-instance stats dicts."""
+    n = len(fields)
+    if n == 0:
+        return []
+    dxs = list(dx) if isinstance(dx, (list, tuple)) else [dx] * n
+    kind = abi.KIND_SSA if par.solver == "ssa" else abi.KIND_DIVA
+    names = {a for a, t in (abi.SSA_ARGS if kind == abi.KIND_SSA else abi.DIVA_ARGS) if t != "s"}
+    arr = (abi.Fields * n)()
+    for k, f in enumerate(fields):
+        nx, ny = f["H_ice"].shape
+        nz = f["zeta_aa"].shape[0]
+        F = arr[k]
+        F.nx, F.ny, F.nz, F.dx, F.dy, F.n_glen = nx, ny, nz, dxs[k], dxs[k], n_glen
+        for name, _ in abi.Fields._fields_[6:]:
+            if name not in names:
+                continue
+            a = f[name]
+            want = (nz,) if name == "zeta_aa" else (nx, ny, nz) if name in _FIELDS_3D else (nx, ny)
+            if a.shape != want:
+                raise ValueError(f"instance {k}, {name}: shape {a.shape}, expected {want}")
+            abi.ptr(a, "i" if name.startswith("ssa_mask") else "d")
+            setattr(F, name, a.ctypes.data)
+    sts = (abi.Stats * n)()
+    cpar = par.to_c()
+    _check(lib().ygpu_solve_batch_host(kind, C.byref(cpar), n, arr, sts))
+    return [s.as_dict() for s in sts]
 
 
 def calc_dyn_inputs(inst) -> dict:
