@@ -12,9 +12,11 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <queue>
+#include <thread>
 #include <vector>
 
 #include "ygpu_common.cuh"
@@ -159,6 +161,8 @@ struct ygpu_ctx {
     size_t arena_cap = 0;
     char* fbuf = nullptr;           // fields of host-pointer calls
     size_t fbuf_cap = 0;
+    char* hbuf = nullptr;           // pinned host mirror of fbuf
+    size_t hbuf_cap = 0;
     Inst* d_insts = nullptr;
     int insts_cap = 0;
     InstOut* d_out = nullptr;
@@ -247,6 +251,7 @@ extern "C" void ygpu_ctx_destroy(ygpu_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->arena);
     cudaFree(c->fbuf);
+    if (c->hbuf) cudaFreeHost(c->hbuf);
     cudaFree(c->d_insts);
     cudaFree(c->d_out);
     cudaFree(c->d_ctl);
@@ -806,31 +811,95 @@ struct HostArg {
     size_t bytes;
     bool in, out;
     void* dev;
+    size_t off;          // offset in the staging buffers
 };
 
+// Copies of many host segments, on several host threads when they are large
+// (pieces of at most 4 MiB taken from a shared counter).
+struct Seg {
+    void* dst;
+    const void* src;
+    size_t n;
+};
+
+static void copy_segments(const std::vector<Seg>& segs) {
+    size_t total = 0;
+    for (const Seg& g : segs) total += g.n;
+    unsigned hw = std::thread::hardware_concurrency();
+    unsigned T = total >= ((size_t)32 << 20) ? std::min(16u, std::max(1u, hw)) : 1u;
+    if (T <= 1) {
+        for (const Seg& g : segs) memcpy(g.dst, g.src, g.n);
+        return;
+    }
+    const size_t piece = (size_t)4 << 20;
+    std::vector<Seg> pieces;
+    for (const Seg& g : segs)
+        for (size_t o = 0; o < g.n; o += piece)
+            pieces.push_back({(char*)g.dst + o, (const char*)g.src + o, std::min(piece, g.n - o)});
+    std::atomic<size_t> next(0);
+    auto work = [&]() {
+        for (size_t i; (i = next.fetch_add(1)) < pieces.size();)
+            memcpy(pieces[i].dst, pieces[i].src, pieces[i].n);
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < T; t++) th.emplace_back(work);
+    work();
+    for (auto& t : th) t.join();
+}
+
+// Host staging of the host-pointer entries. The arrays are packed into one
+// pinned host buffer, in the order in-only, in/out, out-only, mirrored by the
+// device buffer: the inputs go up in one copy and the results come back in one.
 struct Staging {
     std::vector<HostArg> args;
+    size_t up = 0, down = 0, tot = 0;   // [0, up) goes up, [down, tot) comes back
     size_t add(void* h, size_t bytes, bool in, bool out) {
-        args.push_back({h, bytes, in, out, nullptr});
+        args.push_back({h, bytes, in, out, nullptr, 0});
         return args.size() - 1;
     }
     int upload(ygpu_ctx* c) {
-        size_t tot = 0;
-        for (auto& a : args) tot += al(a.bytes);
+        size_t off = 0;
+        for (int cls = 0; cls < 3; cls++) {
+            if (cls == 1) down = off;
+            if (cls == 2) up = off;
+            for (auto& a : args) {
+                const int ac = (a.in && !a.out) ? 0 : (a.in && a.out) ? 1 : 2;
+                if (ac != cls) continue;
+                a.off = off;
+                off += al(a.bytes);
+            }
+        }
+        tot = off;
         int st = grow(&c->fbuf, &c->fbuf_cap, tot);
         if (st) return st;
-        char* p = c->fbuf;
-        for (auto& a : args) {
-            a.dev = p;
-            p += al(a.bytes);
-            if (a.in) CK(cudaMemcpyAsync(a.dev, a.host, a.bytes, cudaMemcpyHostToDevice, c->stream));
+        if (c->hbuf_cap < tot) {
+            if (c->hbuf) cudaFreeHost(c->hbuf);
+            c->hbuf = nullptr;
+            c->hbuf_cap = 0;
+            if (cudaHostAlloc((void**)&c->hbuf, tot, cudaHostAllocDefault) != cudaSuccess) {
+                cudaGetLastError();
+                c->hbuf = nullptr;
+                ygpu_set_error("pinned host allocation of %zu bytes failed", tot);
+                return YGPU_ERR_NOMEM;
+            }
+            c->hbuf_cap = tot;
         }
+        std::vector<Seg> segs;
+        for (auto& a : args) {
+            a.dev = c->fbuf + a.off;
+            if (a.in) segs.push_back({c->hbuf + a.off, a.host, a.bytes});
+        }
+        copy_segments(segs);
+        if (up) CK(cudaMemcpyAsync(c->fbuf, c->hbuf, up, cudaMemcpyHostToDevice, c->stream));
         return YGPU_OK;
     }
     int download(ygpu_ctx* c) {
-        for (auto& a : args)
-            if (a.out) CK(cudaMemcpyAsync(a.host, a.dev, a.bytes, cudaMemcpyDeviceToHost, c->stream));
+        if (tot > down) CK(cudaMemcpyAsync(c->hbuf + down, c->fbuf + down, tot - down, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
+        std::vector<Seg> segs;
+        for (auto& a : args)
+            if (a.out) segs.push_back({a.host, c->hbuf + a.off, a.bytes});
+        copy_segments(segs);
         return YGPU_OK;
     }
 };
