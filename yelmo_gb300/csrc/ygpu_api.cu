@@ -304,6 +304,7 @@ size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block) {
     b += 16 * al(n2 * 8);                // 2D scratch
     b += 15 * al(nu * 8);                // linear system
     b += 6 * al(nu * 4);                 // ukind, emap, mem(3), rpart
+    b += al((n2 + 1) * 4);               // active cell list
     if (mixed) b += 4 * al(n2 * 4) + 13 * al(nu * 4);
     if (block) b += al(tile_blocks(nx, ny) * 1024 * 4);
     return b;
@@ -326,6 +327,7 @@ void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool m
     I.rt = D(nu); I.v = D(nu); I.s = D(nu); I.t = D(nu); I.ph = D(nu); I.sh = D(nu); I.dval = D(nu);
     I.m2 = D(nu);
     I.ukind = Iv(nu); I.emap = Iv(nu); I.mem = Iv(3 * nu); I.rpart = Iv(nu);
+    I.acell = Iv(n2 + 1);
     if (mixed) {
         I.fN = Fv(n2); I.fNab = Fv(n2); I.fdrag_x = Fv(n2); I.fdrag_y = Fv(n2);
         I.fdinv = Fv(nu); I.fx = Fv(nu); I.fr = Fv(nu); I.fp = Fv(nu); I.fq = Fv(nu); I.fz = Fv(nu);

@@ -141,6 +141,8 @@ struct Inst {
     // linear system (nu entries each)
     double *x, *b, *r, *p, *q, *z, *dinv, *rt, *v, *s, *t, *ph, *sh, *dval, *m2;
     int *ukind, *emap, *mem, *rpart;
+    // cells with a non-identity row, in cell order (n2 + 1 ints; [n2] = count)
+    int* acell;
     // mixed precision scratch (nu entries; coefficient copies n2)
     float *fN, *fNab, *fdrag_x, *fdrag_y, *fdinv;
     float* fminv;                  // mixed, block preconditioner: inverse of each 4x4-cell tile block (32x32)
@@ -290,6 +292,40 @@ YG_DEV bool team_allreduce_w(Team& T, const V* in, double* out, int nv) {
     return ok;
 }
 YG_DEV bool team_allreduce(Team& T, double* vals, int nv) { return team_allreduce_w<double>(T, vals, vals, nv); }
+
+// Exclusive prefix sums over the team's CTAs, in CTA rank order, of nv <=
+// YG_RED_MAX per-CTA values held by thread 0 (exact for integers below 2^53),
+// and their totals; every thread gets both. Also acts as a team barrier.
+YG_DEV bool team_scan_cta(Team& T, const double* mine, double* before, double* total, int nv) {
+    __shared__ double s_b[YG_RED_MAX], s_t[YG_RED_MAX];
+    if (T.ncta == 1) {
+        if (threadIdx.x == 0)
+            for (int k = 0; k < nv; k++) { s_b[k] = 0.0; s_t[k] = mine[k]; }
+    } else {
+        if (threadIdx.x == 0)
+            for (int k = 0; k < nv; k++) T.ctl->slots[T.parity][T.cta][k] = mine[k];
+        if (!team_barrier(T)) return false;
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            for (int k = 0; k < nv; k++) {
+                double wb = 0.0, wt = 0.0;
+                for (int c = lane; c < T.ncta; c += 32) {
+                    const double v = __ldcg(&T.ctl->slots[T.parity][c][k]);
+                    wt += v;
+                    if (c < T.cta) wb += v;
+                }
+                wb = warp_sum<double>(wb);
+                wt = warp_sum<double>(wt);
+                if (lane == 0) { s_b[k] = wb; s_t[k] = wt; }
+            }
+        }
+        T.parity ^= 1;
+    }
+    __syncthreads();
+    for (int k = 0; k < nv; k++) { before[k] = s_b[k]; total[k] = s_t[k]; }
+    __syncthreads();
+    return true;
+}
 
 // Integer all-reduce helpers via the double path (exact for |v| < 2^53).
 YG_DEV bool team_allreduce_or_max(Team& T, double* vals, int nv) { return team_allreduce(T, vals, nv); }

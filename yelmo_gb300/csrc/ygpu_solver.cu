@@ -1089,23 +1089,6 @@ YG_DEV T operator_row(const Inst& I, const Geo& G, const OpK<T>& K, bool energy,
     return residual_row<T, CT>(I, G, K, N, Nab, dgx, dgy, v, u, nullptr);
 }
 
-// Cells c = first, first + stride, ... of an nx-wide grid with (i, j) kept
-// incrementally (no division per cell)
-struct CellWalk {
-    int c, i, j, di, dj, nx;
-    YG_DEV CellWalk(int first, int stride, int nx_) : c(first), i(first % nx_), j(first / nx_), di(stride % nx_),
-                                                      dj(stride / nx_), nx(nx_) {}
-    YG_DEV void next() {
-        c += di + dj * nx;
-        i += di;
-        j += dj;
-        if (i >= nx) {
-            i -= nx;
-            j++;
-        }
-    }
-};
-
 // Operator functors for the Krylov solvers: row(u, v) = (A v)_u
 template <typename T, typename CT>
 struct StencilOp {
@@ -1114,6 +1097,7 @@ struct StencilOp {
     bool energy;
     const CT *N, *Nab, *dgx, *dgy;
     OpK<T> K;
+    const int* acell = nullptr;    // active-cell list of the Krylov loops (nullptr: every cell)
     YG_DEV T row(int u, const T* v) const { return operator_row<T, CT>(*I, *G, K, energy, N, Nab, dgx, dgy, v, u); }
     YG_DEV int nx() const { return G->nx; }
     YG_DEV int n2() const { return G->n2; }
@@ -1168,6 +1152,54 @@ struct CsrOp {
 // ---------------------------------------------------------------------------
 // Solve setup: unknown classification (energy) or row kinds (residual)
 // ---------------------------------------------------------------------------
+// Active-cell list of the Krylov loops (I.acell): the cells with at least one
+// non-identity row, in cell order (so the margin cells, whose rows take the
+// general operator path, stay spread over the warps). Each CTA compacts a
+// contiguous range of cells at the offset the CTAs before it leave, so the
+// list does not depend on timing. Identity rows (Dirichlet and tied unknowns
+// of the energy form, identity rows of the residual form) enter the solve with
+// x = b, so their residual and Krylov vectors stay zero and the iterations
+// skip the cells whose two rows are identity.
+__device__ __noinline__ bool build_active_cells(const Inst& I, const Geo& G, Team& T, bool energy) {
+    const int n2 = G.n2;
+    auto ident = [&](int u) { return energy ? (I.ukind[u] != DOF_FREE) : (I.ukind[u] == RROW_ID); };
+    auto active = [&](int c) { return !(ident(c) && ident(n2 + c)); };
+    const int per = (n2 + T.ncta - 1) / T.ncta;
+    const int lo = min(n2, T.cta * per), hi = min(n2, lo + per);
+    __shared__ int s_cnt;
+    __shared__ int s_w[32];
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    int my = 0;
+    for (int c = lo + (int)threadIdx.x; c < hi; c += blockDim.x) my += active(c) ? 1 : 0;
+    my = warp_sum<int>(my);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&s_cnt, my);
+    __syncthreads();
+    const double mine = (double)s_cnt;
+    double before, total;
+    if (!team_scan_cta(T, &mine, &before, &total, 1)) return false;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int off = (int)before;
+    for (int base = lo; base < hi; base += blockDim.x) {
+        const int c = base + (int)threadIdx.x;
+        const bool f = (c < hi) && active(c);
+        const unsigned m = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) s_w[wid] = __popc(m);
+        __syncthreads();
+        int wbase = 0, tot = 0;
+        for (int w = 0; w < nw; w++) {
+            const int n = s_w[w];
+            wbase += (w < wid) ? n : 0;
+            tot += n;
+        }
+        if (f) I.acell[off + wbase + __popc(m & ((1u << lane) - 1u))] = c;
+        off += tot;
+        __syncthreads();
+    }
+    if (T.cta == 0 && threadIdx.x == 0) I.acell[n2] = (int)total;
+    return team_barrier(T);
+}
+
 __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T) {
     const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
     const int nx = G.nx, ny = G.ny, n2 = G.n2;
@@ -1236,7 +1268,7 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
             I.emap[u] = u;
         }
     }
-    if (!energy) return team_barrier(T);
+    if (!energy) return team_barrier(T) && build_active_cells(I, G, T, false);
     if (!team_barrier(T)) return false;
     // pass 2: resolve tied chains to their free root (depth <= 8)
     double bad = 0.0;
@@ -1330,7 +1362,7 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
         }
         I.rpart[u] = fast;
     }
-    return team_barrier(T);
+    return team_barrier(T) && build_active_cells(I, G, T, true);
 }
 
 // ---------------------------------------------------------------------------
@@ -1423,7 +1455,11 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
                 residual_row<double, double>(I, G, K64, N, I.Nab, I.drag_x, I.drag_y, I.x, u, &d);
             }
         }
-        if (P.lin_initx_zeros) x0 = 0.0;
+        // identity rows start at their solution (x = b) also with -initx_zeros:
+        // the Krylov loops skip cells whose two rows are identity
+        const bool ident = energy ? (I.ukind[u] != DOF_FREE) : (I.ukind[u] == RROW_ID);
+        if (P.lin_initx_zeros && !ident) x0 = 0.0;
+        if (ident) x0 = b;
         I.b[u] = b;
         I.x[u] = x0;
         I.dinv[u] = (d != 0.0) ? 1.0 / d : 1.0;
@@ -1494,6 +1530,8 @@ __device__ __noinline__ int krylov_cg(Team& Tm, int nu, const Op& A, const CT* d
 // The recursively updated residual is checked against b - A x when it reaches
 // the tolerance; if the true residual is above it, the recursion restarts from
 // the true residual.
+#define YG_ITEM_CACHE 8
+#define YG_ITEM_BLOCK 512
 template <typename T, typename Op, typename CT>
 __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const CT* __restrict__ dinv,
                                             T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
@@ -1510,6 +1548,25 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
     ok = true;
     iters = 0;
     auto Mi = [&](int k) -> T { return precond ? (T)dinv[k] : T(1); };
+    // Work items of the iteration loop: cells (FP32, both rows of a cell per
+    // item) or rows (FP64), over the active cells when the operator has a list.
+    // The first YG_ITEM_CACHE items of each thread are looked up once per
+    // call and kept in shared memory (thread-private slots).
+    const bool by_cell = (sizeof(T) == sizeof(float));
+    const int n2 = A.n2();
+    const int nact = A.acell ? A.acell[n2] : n2;
+    const int nitem = by_cell ? nact : 2 * nact;
+    auto item = [&](int t) -> int {
+        if (!A.acell) return t;
+        if (by_cell || t < nact) return A.acell[t];
+        return n2 + A.acell[t - nact];
+    };
+    __shared__ int s_item[YG_ITEM_CACHE * YG_ITEM_BLOCK];
+    const int cache = (blockDim.x <= YG_ITEM_BLOCK) ? YG_ITEM_CACHE : 0;
+    {
+        int q = 0;
+        for (int t = Tm.tid; t < nitem && q < cache; t += Tm.nthr, q++) s_item[q * blockDim.x + threadIdx.x] = item(t);
+    }
     int it = 0;
     for (int restart = 0; restart < 8; restart++) {
         // r = b - A x, u = M r
@@ -1528,6 +1585,7 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             w[k] = wk;
             const T mk = Mi(k) * wk;
             m0[k] = mk;
+            m1[k] = T(0);
             z[k] = T(0); q[k] = T(0); s[k] = T(0); p[k] = T(0);
             const T rk = r[k], uk = u[k];
             a0 += rk * uk;
@@ -1598,19 +1656,23 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             // n2 + c belong to the thread of cell c here; every use of these
             // vectors with the row-k-per-thread-k mapping (restart, true
             // residual, the caller) follows a team all-reduce.
-            if (sizeof(T) == sizeof(float)) {
-                const int n2 = A.n2();
-                for (CellWalk cw(Tm.tid, Tm.nthr, A.nx()); cw.c < n2; cw.next()) {
+            // With an active-cell list the cells whose two rows are identity are
+            // skipped: all their vectors are zero (m1 included) and x = b there.
+            int q = 0;
+            for (int t = Tm.tid; t < nitem; t += Tm.nthr, q++) {
+                const int k = (q < cache) ? s_item[q * blockDim.x + threadIdx.x] : item(t);
+                if (by_cell) {
+                    const int j = k / A.nx(), i = k - j * A.nx();
                     T y0, y1;
-                    A.cell(cw.c, cw.i, cw.j, mc, y0, y1);
-                    const RowIn R0 = load(cw.c, y0);
-                    const RowIn R1 = load(n2 + cw.c, y1);
-                    update(cw.c, R0);
-                    update(n2 + cw.c, R1);
+                    A.cell(k, i, j, mc, y0, y1);
+                    const RowIn R0 = load(k, y0);
+                    const RowIn R1 = load(n2 + k, y1);
+                    update(k, R0);
+                    update(n2 + k, R1);
+                } else {
+                    // FP64: one row per item (the two-row body exceeds the register budget)
+                    update(k, load(k, A.row(k, mc)));
                 }
-            } else {
-                // FP64: one row per trip (the two-row body exceeds the register budget)
-                for (int k = Tm.tid; k < nu; k += Tm.nthr) update(k, load(k, A.row(k, mc)));
             }
             it++;
             {
@@ -2142,7 +2204,8 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
     // MINRES requests run CG on the symmetric energy system, BiCGSTAB on the residual one
     const bool use_cg = energy ? (P.lin_solver != YGPU_LIN_BICGSTAB) : false;
     outer = 0;
-    const StencilOp<double, double> A64{&I, &G, energy, I.visc_int, I.Nab, I.drag_x, I.drag_y, make_opk<double>(G)};
+    const StencilOp<double, double> A64{&I, &G, energy, I.visc_int, I.Nab, I.drag_x, I.drag_y, make_opk<double>(G),
+                                        I.acell};
     if (P.precision != YGPU_PREC_MIXED) {
         // -p ilu on the energy form: the FP32 tile inverses (built by the pre step)
         // precondition the FP64 CG
@@ -2155,7 +2218,8 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         return krylov_bicgstab<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.rt, I.p, I.v, I.s, I.t, I.ph, I.sh,
                                        P.lin_maxiter, P.lin_tol, bnrm, pre, iters, relres, ok);
     }
-    const StencilOp<float, float> A32{&I, &G, energy, I.fN, I.fNab, I.fdrag_x, I.fdrag_y, make_opk<float>(G)};
+    const StencilOp<float, float> A32{&I, &G, energy, I.fN, I.fNab, I.fdrag_x, I.fdrag_y, make_opk<float>(G),
+                                      I.acell};
     // ---- mixed: FP32 coefficients (copied by the pre step, with the tile-block
     // inverses of -p ilu), FP32 inner Krylov, FP64 outer residual ----
     const bool block = use_cg && energy && P.lin_precond == YGPU_PRE_ILU0 && I.fminv;
