@@ -1180,6 +1180,7 @@ __device__ __noinline__ bool build_active_cells(const Inst& I, const Geo& G, Tea
     if (!team_scan_cta(T, &mine, &before, &total, 1)) return false;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     int off = (int)before;
+    int bad = 0;
     for (int base = lo; base < hi; base += blockDim.x) {
         const int c = base + (int)threadIdx.x;
         const bool f = (c < hi) && active(c);
@@ -1192,12 +1193,18 @@ __device__ __noinline__ bool build_active_cells(const Inst& I, const Geo& G, Tea
             wbase += (w < wid) ? n : 0;
             tot += n;
         }
-        if (f) I.acell[off + wbase + __popc(m & ((1u << lane) - 1u))] = c;
+        const int pos = off + wbase + __popc(m & ((1u << lane) - 1u));
+        if (f) {
+            if (pos >= 0 && pos < n2) I.acell[pos] = c;
+            else bad = 1;
+        }
         off += tot;
         __syncthreads();
     }
-    if (T.cta == 0 && threadIdx.x == 0) I.acell[n2] = (int)total;
-    return team_barrier(T);
+    if (!(total >= 0.0 && total <= (double)n2)) bad = 1;
+    if (bad) atomicExch(T.abort_all, 1);      // an inconsistent team count: fail the launch
+    if (T.cta == 0 && threadIdx.x == 0) I.acell[n2] = bad ? 0 : (int)total;
+    return team_barrier(T) && !bad;
 }
 
 __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T) {
@@ -1554,7 +1561,7 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
     // call and kept in shared memory (thread-private slots).
     const bool by_cell = (sizeof(T) == sizeof(float));
     const int n2 = A.n2();
-    const int nact = A.acell ? A.acell[n2] : n2;
+    const int nact = A.acell ? min(max(A.acell[n2], 0), n2) : n2;
     const int nitem = by_cell ? nact : 2 * nact;
     auto item = [&](int t) -> int {
         if (!A.acell) return t;
