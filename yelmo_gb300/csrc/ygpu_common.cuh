@@ -157,9 +157,14 @@ struct Inst {
 #define YG_MAX_TEAM_CTAS 1024
 #define YG_RED_MAX 4
 
+// Team barrier: every CTA adds 1 to `count` with a release reduction and
+// waits (one thread, acquire loads) until count reaches its target, which
+// grows by the team's CTA count at each barrier. `base` holds count at the
+// start of a launch (CTA 0 stores it at the end of the previous launch, after
+// its last arrival; every CTA reads it before its first).
 struct TeamCtl {
     unsigned int count;
-    unsigned int gen;
+    unsigned int base;
     int abort;
     int inst;                      // instance the team works on (work queue)
     double slots[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
@@ -172,7 +177,7 @@ struct Team {
     TeamCtl* ctl;
     int* abort_all;                // whole-launch abort flag (timeout anywhere)
     double sync_ns;                // time CTA 0 / thread 0 spent in team all-reduces
-    unsigned gen;                  // thread 0: generation of the team barrier (mirrors ctl->gen)
+    unsigned gen;                  // thread 0: count target of the last team barrier
 };
 
 YG_DEV unsigned ld_acquire_u32(const unsigned int* p) {
@@ -191,44 +196,35 @@ YG_DEV int ld_acquire_s32(const int* p) {
 // launch returns at once, and the kernel reports YGPU_ERR_TIMEOUT.
 #define YG_SPIN_LIMIT (1u << 22)
 
-YG_DEV unsigned atom_add_acqrel_u32(unsigned int* p, unsigned v) {
-    unsigned old;
-    asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-    return old;
+YG_DEV void red_release_add_u32(unsigned int* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Returns false if the launch is aborting. Arrival: fence + acq_rel atomic on
-// the team counter; the last CTA resets it and bumps the generation; the
-// others poll the generation with acquire loads (no sleep: one thread per CTA).
+// Returns false if the launch is aborting. The release reduction by thread 0
+// follows a __syncthreads, so the CTA's earlier writes are ordered before its
+// arrival; the closing __syncthreads orders the CTA's later reads after thread
+// 0's acquire. Counts wrap: the comparison is on the signed difference.
 YG_DEV bool team_barrier(Team& T) {
     __syncthreads();
     __shared__ int s_ok;
     if (threadIdx.x == 0) {
         int ok = 1;
         if (T.ncta > 1) {
-            const unsigned gen = T.gen;
-            __threadfence();
-            unsigned arrived = atom_add_acqrel_u32(&T.ctl->count, 1u);
-            if (arrived == (unsigned)T.ncta - 1u) {
-                T.ctl->count = 0u;
-                atom_add_acqrel_u32(&T.ctl->gen, 1u);
-            } else {
-                unsigned n = 0;
-                while (ld_acquire_u32(&T.ctl->gen) == gen) {
-                    if ((++n & 1023u) == 0u) {
-                        if (ld_acquire_s32(T.abort_all)) { ok = 0; break; }
-                        if (n > YG_SPIN_LIMIT) {
-                            atomicExch(T.abort_all, 1);
-                            atomicExch(&T.ctl->abort, 1);
-                            ok = 0;
-                            break;
-                        }
+            T.gen += (unsigned)T.ncta;
+            red_release_add_u32(&T.ctl->count, 1u);
+            unsigned n = 0;
+            while ((int)(ld_acquire_u32(&T.ctl->count) - T.gen) < 0) {
+                if ((++n & 1023u) == 0u) {
+                    if (ld_acquire_s32(T.abort_all)) { ok = 0; break; }
+                    if (n > YG_SPIN_LIMIT) {
+                        atomicExch(T.abort_all, 1);
+                        atomicExch(&T.ctl->abort, 1);
+                        ok = 0;
+                        break;
                     }
                 }
             }
-            T.gen = gen + 1u;
         }
-        if (ok && ld_acquire_s32(T.abort_all)) ok = 0;
         s_ok = ok;
     }
     __syncthreads();

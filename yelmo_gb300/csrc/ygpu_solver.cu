@@ -2733,7 +2733,7 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
     T.parity = 0;
     T.abort_all = abort_all;
     T.sync_ns = 0.0;
-    T.gen = (threadIdx.x == 0) ? ld_acquire_u32(&T.ctl->gen) : 0u;
+    T.gen = (threadIdx.x == 0) ? ld_acquire_u32(&T.ctl->base) : 0u;
     for (int q = team; q < n_inst; q += n_teams) {
         if (threadIdx.x == 0) {
             sI = insts[q];
@@ -2751,6 +2751,7 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
         }
         __syncthreads();
     }
+    if (T.cta == 0 && threadIdx.x == 0) T.ctl->base = T.gen;
 }
 
 #define YG_KBLOCK 512
