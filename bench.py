@@ -455,7 +455,7 @@ def main():
     # e2e: the batched C-ABI entry on host buffers (the whole batch per step, the
     # host-device copies inside the timed region), and the single-solve drop-in
     par_m = insts[0].par.with_(precision="mixed")
-    n_e2e = args.warmup + max(3, args.steps // 2)
+    n_e2e = args.warmup + max(3, args.steps)
     e2e_times, e2e1_times = [], []
     barrier()
     for s in range(n_e2e):

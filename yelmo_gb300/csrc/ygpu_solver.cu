@@ -1552,6 +1552,7 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
     __shared__ double s_ab[3];     // alpha, beta, relres
     __shared__ int s_flag;         // 0 continue, 1 converged, 2 breakdown
     const bool lead = (threadIdx.x == 0);
+    using W = T;                   // precision of the scalar recurrences
     ok = true;
     iters = 0;
     auto Mi = [&](int k) -> T { return precond ? (T)dinv[k] : T(1); };
@@ -1688,15 +1689,17 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             }
             { T* t = mc; mc = mn; mn = t; }
             if (lead) {
-                const double rel = sqrt(red[2]) / bnrm;
+                // FP32 inner solves: the recurrence scalars in FP32 (its division
+                // and square root are far faster than FP64's on this part)
+                const W rel = sqrt((W)red[2]) / (W)bnrm;
                 s_ab[2] = rel;
                 if (!isfinite(rel)) s_flag = 2;
-                else if (rel <= tol) s_flag = 1;
+                else if (rel <= (W)tol) s_flag = 1;
                 else {
-                    const double gam = red[0], del = red[1];
-                    const double beta = gam / gam_old;
-                    const double alpha = gam / (del - beta * gam / alpha_old);
-                    if (!isfinite(alpha) || !isfinite(beta) || del == 0.0) s_flag = 3;
+                    const W gam = (W)red[0], del = (W)red[1];
+                    const W beta = gam / (W)gam_old;
+                    const W alpha = gam / (del - beta * gam / (W)alpha_old);
+                    if (!isfinite(alpha) || !isfinite(beta) || del == W(0)) s_flag = 3;
                     else {
                         s_flag = 0;
                         s_ab[0] = alpha;
@@ -1747,6 +1750,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
     __shared__ double s_sc[4];     // alpha, omega, beta, relres
     __shared__ int s_flag;         // 0 continue, 1 converged, 2 breakdown
     const bool lead = (threadIdx.x == 0);
+    using W = T;                   // precision of the scalar recurrences (FP32 in the inner solves)
     ok = true;
     iters = 0;
     A(Tm, x, v);
@@ -1774,7 +1778,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
         __syncthreads();           // every thread has read the previous s_flag / s_sc[3]
         if (lead) {
             s_flag = (rho == 0.0 || !isfinite(rho)) ? 2 : 0;
-            s_sc[2] = (it == 1) ? 0.0 : (rho / rho_old) * (alpha / omega);
+            s_sc[2] = (it == 1) ? 0.0 : (double)(((W)rho / (W)rho_old) * ((W)alpha / (W)omega));
             s_sc[1] = omega;
         }
         __syncthreads();
@@ -1796,7 +1800,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
         if (lead) {
             if (tv == 0.0 || !isfinite(tv)) s_flag = 2;
             else {
-                alpha = rho / tv;
+                alpha = (double)((W)rho / (W)tv);
                 s_sc[0] = alpha;
                 s_flag = 0;
             }
@@ -1811,11 +1815,31 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
             sh[u] = precond ? (T)dinv[u] * su : su;
             ssp += su * su;
         }
-        double ss = 0.0;
-        if (!(ok = team_allreduce_w<T>(Tm, &ssp, &ss, 1))) return YGPU_ERR_TIMEOUT;
+        // ||s|| rides on the next all-reduce: t = A sh is computed before the
+        // early-convergence test on s, which saves an all-reduce per iteration
+        // (the last iteration's t is then unused)
+        if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
+        A(Tm, sh, t);
+        T ts0 = T(0), ts1 = T(0);
+        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+            const T tu = t[u];
+            ts0 += tu * s[u];
+            ts1 += tu * tu;
+        }
+        double ts[3];
+        {
+            const T part[3] = {ts0, ts1, ssp};
+            if (!(ok = team_allreduce_w<T>(Tm, part, ts, 3))) return YGPU_ERR_TIMEOUT;
+        }
         if (lead) {
-            s_sc[3] = sqrt(ss) / bnrm;
-            s_flag = (s_sc[3] <= tol) ? 1 : 0;
+            s_sc[3] = (double)(sqrt((W)ts[2]) / (W)bnrm);
+            if (s_sc[3] <= tol) s_flag = 1;
+            else if (ts[1] == 0.0 || !isfinite(ts[1])) s_flag = 2;
+            else {
+                omega = (double)((W)ts[0] / (W)ts[1]);
+                s_sc[1] = omega;
+                s_flag = 0;
+            }
         }
         __syncthreads();
         if (s_flag == 1) {
@@ -1824,27 +1848,6 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
             if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
             return YGPU_OK;
         }
-        A(Tm, sh, t);
-        T ts0 = T(0), ts1 = T(0);
-        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
-            const T tu = t[u];
-            ts0 += tu * s[u];
-            ts1 += tu * tu;
-        }
-        double ts[2];
-        {
-            const T part[2] = {ts0, ts1};
-            if (!(ok = team_allreduce_w<T>(Tm, part, ts, 2))) return YGPU_ERR_TIMEOUT;
-        }
-        if (lead) {
-            if (ts[1] == 0.0 || !isfinite(ts[1])) s_flag = 2;
-            else {
-                omega = ts[0] / ts[1];
-                s_sc[1] = omega;
-                s_flag = 0;
-            }
-        }
-        __syncthreads();
         if (s_flag == 2) return YGPU_BREAKDOWN;
         const T om = (T)s_sc[1];
         T rr0 = T(0), rr1 = T(0);
@@ -1861,7 +1864,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
             if (!(ok = team_allreduce_w<T>(Tm, part, rr, 2))) return YGPU_ERR_TIMEOUT;
         }
         if (lead) {
-            s_sc[3] = sqrt(rr[0]) / bnrm;
+            s_sc[3] = (double)(sqrt((W)rr[0]) / (W)bnrm);
             s_flag = (s_sc[3] <= tol) ? 1 : ((omega == 0.0) ? 2 : 0);
             rho_old = rho;
             rho = rr[1];
@@ -2067,6 +2070,7 @@ __device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op
     __shared__ double s_ab[3];
     __shared__ int s_flag;
     const bool lead = (threadIdx.x == 0);
+    using W = T;                   // precision of the scalar recurrences
     const int lane = threadIdx.x & 31, gw = Tm.tid >> 5, nw = Tm.nthr >> 5, nt = tile_count(G);
     ok = true;
     iters = 0;
@@ -2158,15 +2162,17 @@ __device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op
             }
             { T* tt = mc; mc = mn; mn = tt; }
             if (lead) {
-                const double rel = sqrt(red[2]) / bnrm;
+                // FP32 inner solves: the recurrence scalars in FP32 (its division
+                // and square root are far faster than FP64's on this part)
+                const W rel = sqrt((W)red[2]) / (W)bnrm;
                 s_ab[2] = rel;
                 if (!isfinite(rel)) s_flag = 2;
-                else if (rel <= tol) s_flag = 1;
+                else if (rel <= (W)tol) s_flag = 1;
                 else {
-                    const double gam = red[0], del = red[1];
-                    const double beta = gam / gam_old;
-                    const double alpha = gam / (del - beta * gam / alpha_old);
-                    if (!isfinite(alpha) || !isfinite(beta) || del == 0.0) s_flag = 3;
+                    const W gam = (W)red[0], del = (W)red[1];
+                    const W beta = gam / (W)gam_old;
+                    const W alpha = gam / (del - beta * gam / (W)alpha_old);
+                    if (!isfinite(alpha) || !isfinite(beta) || del == W(0)) s_flag = 3;
                     else {
                         s_flag = 0;
                         s_ab[0] = alpha;
