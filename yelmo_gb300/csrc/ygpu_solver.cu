@@ -1089,6 +1089,42 @@ YG_DEV T operator_row(const Inst& I, const Geo& G, const OpK<T>& K, bool energy,
     return residual_row<T, CT>(I, G, K, N, Nab, dgx, dgy, v, u, nullptr);
 }
 
+#define YG_ITEM_CACHE 8
+#define YG_ITEM_BLOCK 512
+// Per-thread work items of the Krylov loops cached in shared memory
+// (thread-private slots: slot q of a thread at q * blockDim.x + threadIdx.x),
+// one buffer for all the solvers of a kernel.
+__shared__ int g_item_cache[YG_ITEM_CACHE * YG_ITEM_BLOCK];
+
+// Rows a thread owns in the BiCGSTAB loops: items t = tid, tid + nthr, ... of
+// the team, row t without an active-cell list, else the listed cells' ux rows
+// then their uy rows.
+struct RowItems {
+    const int* ac;
+    int n2, nact, nitem, cache;
+    YG_DEV int lookup(int t) const {
+        if (!ac) return t;
+        return (t < nact) ? ac[t] : n2 + ac[t - nact];
+    }
+    YG_DEV int row(int t, int q) const {
+        return (q < cache) ? g_item_cache[q * blockDim.x + threadIdx.x] : lookup(t);
+    }
+};
+YG_DEV RowItems make_row_items(const Team& Tm, const int* ac, int n2, int nu) {
+    RowItems R;
+    R.ac = ac;
+    R.n2 = n2;
+    R.nact = ac ? min(max(ac[n2], 0), n2) : n2;
+    R.nitem = ac ? 2 * R.nact : nu;
+    R.cache = (blockDim.x <= YG_ITEM_BLOCK) ? YG_ITEM_CACHE : 0;
+    int q = 0;
+    for (int t = Tm.tid; t < R.nitem && q < R.cache; t += Tm.nthr, q++)
+        g_item_cache[q * blockDim.x + threadIdx.x] = R.lookup(t);
+    return R;
+}
+template <typename Op>
+YG_DEV const int* op_acell(const Op& A) { return A.acell; }
+
 // Operator functors for the Krylov solvers: row(u, v) = (A v)_u
 template <typename T, typename CT>
 struct StencilOp {
@@ -1111,6 +1147,30 @@ struct StencilOp {
         } else {
             y0 = residual_row<T, CT>(*I, *G, K, N, Nab, dgx, dgy, v, c, nullptr);
             y1 = residual_row<T, CT>(*I, *G, K, N, Nab, dgx, dgy, v, n2 + c, nullptr);
+        }
+    }
+    // y = A v on the rows of R (the rows of the thread's items, as in the
+    // callers' vector loops that read y right after without a barrier). FP32:
+    // two rows per thread and trip, both rows' loads issued before either store.
+    YG_DEV void apply(Team& Tm, const T* v, T* y, const RowItems& R) const {
+        if (sizeof(T) != sizeof(float)) {
+            int q = 0;
+            for (int t = Tm.tid; t < R.nitem; t += Tm.nthr, q++) {
+                const int k = R.row(t, q);
+                y[k] = row(k, v);
+            }
+            return;
+        }
+        int q0 = 0;
+        for (int t0 = Tm.tid; t0 < R.nitem; t0 += 2 * Tm.nthr, q0 += 2) {
+            const int t1 = t0 + Tm.nthr;
+            const bool h1 = t1 < R.nitem;
+            const int k0 = R.row(t0, q0);
+            const int k1 = h1 ? R.row(t1, q0 + 1) : k0;
+            const T y0 = row(k0, v);
+            const T y1 = row(k1, v);
+            y[k0] = y0;
+            if (h1) y[k1] = y1;
         }
     }
     // y = A v. Row k belongs to thread k mod nthr, as in the callers' vector
@@ -1139,6 +1199,15 @@ struct CsrOp {
     const int* ptr;
     const int* idx;
     const double* val;
+    const int* acell = nullptr;     // no active-cell list: every row
+    YG_DEV int n2() const { return n; }
+    YG_DEV void apply(Team& Tm, const double* v, double* y, const RowItems& R) const {
+        int q = 0;
+        for (int t = Tm.tid; t < R.nitem; t += Tm.nthr, q++) {
+            const int k = R.row(t, q);
+            y[k] = row(k, v);
+        }
+    }
     YG_DEV double row(int r, const double* v) const {
         double s = 0.0;
         for (int k = ptr[r]; k < ptr[r + 1]; k++) s += val[k] * v[idx[k]];
@@ -1537,8 +1606,7 @@ __device__ __noinline__ int krylov_cg(Team& Tm, int nu, const Op& A, const CT* d
 // The recursively updated residual is checked against b - A x when it reaches
 // the tolerance; if the true residual is above it, the recursion restarts from
 // the true residual.
-#define YG_ITEM_CACHE 8
-#define YG_ITEM_BLOCK 512
+
 template <typename T, typename Op, typename CT>
 __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const CT* __restrict__ dinv,
                                             T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
@@ -1569,7 +1637,7 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
         if (by_cell || t < nact) return A.acell[t];
         return n2 + A.acell[t - nact];
     };
-    __shared__ int s_item[YG_ITEM_CACHE * YG_ITEM_BLOCK];
+    int* s_item = g_item_cache;
     const int cache = (blockDim.x <= YG_ITEM_BLOCK) ? YG_ITEM_CACHE : 0;
     {
         int q = 0;
@@ -1740,7 +1808,10 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
 
 // BiCGSTAB with Jacobi (van der Vorst 1992, as in the oracle). The scalar
 // recurrences run on one thread per CTA and are broadcast through shared
-// memory (see krylov_pcg_pipe).
+// memory (see krylov_pcg_pipe). With an active-cell list the iterations visit
+// the rows of the listed cells only: identity rows enter with x = b, so r, rt
+// and p are zero there, and p_hat and s_hat (the operator inputs, read at
+// neighbouring columns) are cleared on every row at the start.
 template <typename T, typename Op, typename CT>
 __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const CT* __restrict__ dinv,
                                             T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
@@ -1760,10 +1831,14 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
         r[u] = ru;
         rt[u] = ru;
         p[u] = T(0);
+        ph[u] = T(0);
+        sh[u] = T(0);
         a0 += ru * ru;
     }
     double red[2] = {0.0, 0.0};
     if (!(ok = team_allreduce_w<T>(Tm, &a0, red, 1))) return YGPU_ERR_TIMEOUT;
+    // rows of this thread in the iterations (its own cache slots)
+    const RowItems R = make_row_items(Tm, op_acell(A), A.n2(), nu);
     // lead-thread state of the recurrence
     double rho = red[0], rho_old = 1.0, alpha = 1.0, omega = 1.0;     // (rt, r) with rt = r
     if (lead) {
@@ -1785,16 +1860,24 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
         if (s_flag == 2) return YGPU_BREAKDOWN;
         {
             const T beta = (T)s_sc[2], om = (T)s_sc[1];
-            for (int u = Tm.tid; u < nu; u += Tm.nthr) {
+            int q = 0;
+            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+                const int u = R.row(e, q);
                 T pu = (it == 1) ? r[u] : r[u] + beta * (p[u] - om * v[u]);
                 p[u] = pu;
                 ph[u] = precond ? (T)dinv[u] * pu : pu;
             }
         }
         if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
-        A(Tm, ph, v);
+        A.apply(Tm, ph, v, R);
         T tvp = T(0);
-        for (int u = Tm.tid; u < nu; u += Tm.nthr) tvp += rt[u] * v[u];
+        {
+            int q = 0;
+            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+                const int u = R.row(e, q);
+                tvp += rt[u] * v[u];
+            }
+        }
         double tv = 0.0;
         if (!(ok = team_allreduce_w<T>(Tm, &tvp, &tv, 1))) return YGPU_ERR_TIMEOUT;
         if (lead) {
@@ -1809,22 +1892,30 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
         if (s_flag == 2) return YGPU_BREAKDOWN;
         const T al = (T)s_sc[0];
         T ssp = T(0);
-        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
-            T su = r[u] - al * v[u];
-            s[u] = su;
-            sh[u] = precond ? (T)dinv[u] * su : su;
-            ssp += su * su;
+        {
+            int q = 0;
+            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+                const int u = R.row(e, q);
+                T su = r[u] - al * v[u];
+                s[u] = su;
+                sh[u] = precond ? (T)dinv[u] * su : su;
+                ssp += su * su;
+            }
         }
         // ||s|| rides on the next all-reduce: t = A sh is computed before the
         // early-convergence test on s, which saves an all-reduce per iteration
         // (the last iteration's t is then unused)
         if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
-        A(Tm, sh, t);
+        A.apply(Tm, sh, t, R);
         T ts0 = T(0), ts1 = T(0);
-        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
-            const T tu = t[u];
-            ts0 += tu * s[u];
-            ts1 += tu * tu;
+        {
+            int q = 0;
+            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+                const int u = R.row(e, q);
+                const T tu = t[u];
+                ts0 += tu * s[u];
+                ts1 += tu * tu;
+            }
         }
         double ts[3];
         {
@@ -1844,19 +1935,27 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
         __syncthreads();
         if (s_flag == 1) {
             relres = s_sc[3];
-            for (int u = Tm.tid; u < nu; u += Tm.nthr) x[u] = x[u] + al * ph[u];
+            int q = 0;
+            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+                const int u = R.row(e, q);
+                x[u] = x[u] + al * ph[u];
+            }
             if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
             return YGPU_OK;
         }
         if (s_flag == 2) return YGPU_BREAKDOWN;
         const T om = (T)s_sc[1];
         T rr0 = T(0), rr1 = T(0);
-        for (int u = Tm.tid; u < nu; u += Tm.nthr) {
-            x[u] = x[u] + al * ph[u] + om * sh[u];
-            T ru = s[u] - om * t[u];
-            r[u] = ru;
-            rr0 += ru * ru;
-            rr1 += rt[u] * ru;
+        {
+            int q = 0;
+            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+                const int u = R.row(e, q);
+                x[u] = x[u] + al * ph[u] + om * sh[u];
+                T ru = s[u] - om * t[u];
+                r[u] = ru;
+                rr0 += ru * ru;
+                rr1 += rt[u] * ru;
+            }
         }
         double rr[2];
         {
