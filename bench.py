@@ -546,6 +546,7 @@ def main():
                                       + TRAFFIC_PROFILES.get(args.workload, "") + " times this run's average "
                                       "algorithmic bytes per launch") if ratio else None,
                      "kernel": "ygpu_k_krylov", "launches": kr_n,
+                     "active_cells": mixed["sts"][0].get("active_cells"), "cells": i0.nx * i0.ny,
                      "alg_bytes_per_launch": alg_steps["krylov"] / max(kr_n, 1),
                      "avg_launch_ms": kr_ms / max(kr_n, 1), "peak_source": peak_src},
         "step_kernels": per_step,

@@ -135,6 +135,7 @@ typedef struct ygpu_stats {
                                    column (viscosity, integrals, beta), faces, linear system,
                                    Krylov, epilogue, final passes; then the time spent in
                                    team all-reduces over the solve and within the Krylov phase */
+    int    active_cells;        /* cells with a non-identity row: the cells the Krylov iterations visit */
 } ygpu_stats;
 
 /* ---- parameter helpers -------------------------------------------------- */

@@ -58,7 +58,7 @@ class Stats(C.Structure):
         ("ssa_iter_now", C.c_int), ("ssa_lin_iter", C.c_int), ("ssa_lin_fail", C.c_int),
         ("ssa_lim_n", C.c_int), ("ssa_resid", C.c_double), ("lin_resid", C.c_double),
         ("outer_iter", C.c_int), ("status", C.c_int), ("device_ms", C.c_double),
-        ("phase_ms", C.c_double * 10),
+        ("phase_ms", C.c_double * 10), ("active_cells", C.c_int),
     ]
 
     PHASES = ("setup", "strain", "column", "faces", "system", "krylov", "epilogue", "final", "sync_all",

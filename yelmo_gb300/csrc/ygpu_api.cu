@@ -568,7 +568,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
             S.ssa_lim_n = o.lim_n;
             S.ssa_resid = o.resid;
             S.lin_resid = o.lin_resid;
-            S.outer_iter = o.outer_iter;
+            S.outer_iter = o.outer_iter; S.active_cells = o.n_active;
             S.status = s_k;
             S.device_ms = ms;
             for (int q = 0; q < 10; q++) S.phase_ms[q] = o.phase_ns[q] * 1e-6;
@@ -773,7 +773,7 @@ static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
             S.ssa_lim_n = o.lim_n;
             S.ssa_resid = o.resid;
             S.lin_resid = o.lin_resid;
-            S.outer_iter = o.outer_iter;
+            S.outer_iter = o.outer_iter; S.active_cells = o.n_active;
             S.status = s_k;
             S.device_ms = ms;
             for (int q = 0; q < 10; q++) S.phase_ms[q] = o.phase_ns[q] * 1e-6;

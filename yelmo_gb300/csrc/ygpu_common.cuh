@@ -96,6 +96,7 @@ struct InstOut {
     int lin_status;    // status of the last linear solve
     int outer_iter;    // mixed: defect-correction steps
     int converged;
+    int n_active;      // cells with a non-identity row (the Krylov iterations visit these)
     // state carried between the step kernels of the Picard loop
     int done;          // solve finished (converged, iteration limit or error)
     int in_alt;        // the current viscosity lives in visc_alt

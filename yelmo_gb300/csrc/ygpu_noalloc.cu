@@ -149,7 +149,7 @@ extern "C" int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, cons
         stats->ssa_lim_n = o.lim_n;
         stats->ssa_resid = o.resid;
         stats->lin_resid = o.lin_resid;
-        stats->outer_iter = o.outer_iter;
+        stats->outer_iter = o.outer_iter; stats->active_cells = o.n_active;
         stats->status = status;
         for (int q = 0; q < 10; q++) stats->phase_ms[q] = o.phase_ns[q] * 1e-6;
     }

@@ -360,7 +360,7 @@ static void retire_locked(ygpu_server* S) {
         St.ssa_lim_n = o.lim_n;
         St.ssa_resid = o.resid;
         St.lin_resid = o.lin_resid;
-        St.outer_iter = o.outer_iter;
+        St.outer_iter = o.outer_iter; St.active_cells = o.n_active;
         St.status = R.status;
         St.device_ms = (R.t_done - R.t_admit) * 1e3;
         for (int q = 0; q < 10; q++) St.phase_ms[q] = o.phase_ns[q] * 1e-6;

@@ -1272,7 +1272,10 @@ __device__ __noinline__ bool build_active_cells(const Inst& I, const Geo& G, Tea
     }
     if (!(total >= 0.0 && total <= (double)n2)) bad = 1;
     if (bad) atomicExch(T.abort_all, 1);      // an inconsistent team count: fail the launch
-    if (T.cta == 0 && threadIdx.x == 0) I.acell[n2] = bad ? 0 : (int)total;
+    if (T.cta == 0 && threadIdx.x == 0) {
+        I.acell[n2] = bad ? 0 : (int)total;
+        I.out->n_active = I.acell[n2];
+    }
     return team_barrier(T) && !bad;
 }
 

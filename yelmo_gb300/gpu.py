@@ -345,13 +345,15 @@ def algorithmic_bytes(stats: dict, kind: int, nx: int, ny: int, nz: int, mixed: 
     - pre step, per Picard iteration: strain rates 7w, column pass (3nz+14)w
       DIVA / (3nz+10)w SSA (read u, taub, H, f_ice, c_bed, f_slide, f_grnd,
       visc_prev, ATT; write visc, N, F2, beta), faces 20w+8, system 16w+8;
-    - Krylov step: pipelined CG iteration 42w+8 (read the operator input,
+    - Krylov step, per active cell (a cell with a non-identity row; the
+      iterations skip the others): pipelined CG iteration 42w+8 (read the operator input,
       N, N_ab, two drag arrays, the row flags, the preconditioner and eight
       recurrence vectors; write the eight vectors and the next operator
       input), BiCGSTAB iteration 62w+16 (two operator applies of 8w+8 and
-      46w of vector passes); mixed mode: each FP64 defect-correction step
-      186 B (FP64 operator 66, residual 48, conversions 32, update 40) and the
-      FP32 coefficient copies 72 B per Picard iteration;
+      46w of vector passes); mixed mode, per cell: each FP64 defect-correction
+      step 186 B (FP64 operator 66, residual 48, conversions 32, update 40);
+    - mixed mode, pre step: the FP32 coefficient copies, 72 B per cell and
+      Picard iteration;
     - post step, per Picard iteration: epilogue 16w+8.
 
     Returns the total, or {step: bytes} with by_step."""
@@ -364,8 +366,10 @@ def algorithmic_bytes(stats: dict, kind: int, nx: int, ny: int, nz: int, mixed: 
     post = 16 * w + 8
     wk = 4 if mixed else 8
     it_bytes = (42 * wk + 8) if cg else (62 * wk + 16)
-    krylov = lin * it_bytes
+    n_act = stats.get("active_cells") or n2
+    krylov = float(n_act) * lin * it_bytes
     if mixed:
-        krylov += stats.get("outer_iter", 0) * 186 + picard * 72
-    steps = {"pre": float(n2) * picard * pre, "krylov": float(n2) * krylov, "post": float(n2) * picard * post}
+        krylov += float(n2) * stats.get("outer_iter", 0) * 186
+        pre += 72
+    steps = {"pre": float(n2) * picard * pre, "krylov": krylov, "post": float(n2) * picard * post}
     return steps if by_step else sum(steps.values())
