@@ -305,6 +305,7 @@ size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block) {
     b += 15 * al(nu * 8);                // linear system
     b += 6 * al(nu * 4);                 // ukind, emap, mem(3), rpart
     b += al((n2 + 1) * 4);               // active cell list
+    b += al(n2);                         // cell flags
     if (mixed) b += 4 * al(n2 * 4) + 13 * al(nu * 4);
     if (block) b += al(tile_blocks(nx, ny) * 1024 * 4);
     return b;
@@ -328,6 +329,8 @@ void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool m
     I.m2 = D(nu);
     I.ukind = Iv(nu); I.emap = Iv(nu); I.mem = Iv(3 * nu); I.rpart = Iv(nu);
     I.acell = Iv(n2 + 1);
+    I.cflag = (unsigned char*)p;
+    p += al(n2);
     if (mixed) {
         I.fN = Fv(n2); I.fNab = Fv(n2); I.fdrag_x = Fv(n2); I.fdrag_y = Fv(n2);
         I.fdinv = Fv(nu); I.fx = Fv(nu); I.fr = Fv(nu); I.fp = Fv(nu); I.fq = Fv(nu); I.fz = Fv(nu);

@@ -144,6 +144,8 @@ struct Inst {
     int *ukind, *emap, *mem, *rpart;
     // cells with a non-identity row, in cell order (n2 + 1 ints; [n2] = count)
     int* acell;
+    // per-cell flags of the solve's fixed inputs, set by the setup step (CF_*)
+    unsigned char* cflag;
     // mixed precision scratch (nu entries; coefficient copies n2)
     float *fN, *fNab, *fdrag_x, *fdrag_y, *fdinv;
     float* fminv;                  // mixed, block preconditioner: inverse of each 4x4-cell tile block (32x32)

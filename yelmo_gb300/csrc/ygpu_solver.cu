@@ -137,16 +137,24 @@ YG_DEV Nb make_nb(const Geo& G, int c) {
 #define CI(ii, jj) ((ii) + G.nx * (jj))
 
 // active faces (calc_active_faces, deformation.f90:1316-1344)
-YG_DEV bool act_x(const Geo& G, const double* f_ice, int i, int j) {
-    int im1, ip1, jm1, jp1;
-    nbr_bc(i, j, G.nx, G.ny, G.bc, im1, ip1, jm1, jp1);
-    return f_ice[CI(i, j)] == 1.0 || f_ice[CI(ip1, j)] == 1.0;
+// Per-cell flags of a solve's fixed inputs (Inst::cflag, set once by the setup
+// step): the phases test these bits instead of comparing FP64 fields, whose
+// compares run on the slow FP64 pipe of this part.
+#define CF_ICE 1u      // f_ice == 1
+#define CF_ACTX 2u     // x face active: f_ice == 1 on either side (acx ice mask)
+#define CF_ACTY 4u     // y face active
+#define CF_OCN 8u      // ice-free and z_bed < z_sl
+YG_DEV unsigned char cell_flags(const Geo& G, const Inst& I, int c) {
+    const Nb n = make_nb(G, c);
+    const bool ice = (I.f_ice[c] == 1.0);
+    unsigned fl = ice ? CF_ICE : 0u;
+    if (ice || I.f_ice[CI(n.ip1, n.j)] == 1.0) fl |= CF_ACTX;
+    if (ice || I.f_ice[CI(n.i, n.jp1)] == 1.0) fl |= CF_ACTY;
+    if (!ice && I.z_bed[c] < I.z_sl[c]) fl |= CF_OCN;
+    return (unsigned char)fl;
 }
-YG_DEV bool act_y(const Geo& G, const double* f_ice, int i, int j) {
-    int im1, ip1, jm1, jp1;
-    nbr_bc(i, j, G.nx, G.ny, G.bc, im1, ip1, jm1, jp1);
-    return f_ice[CI(i, j)] == 1.0 || f_ice[CI(i, jp1)] == 1.0;
-}
+YG_DEV bool act_x(const Geo& G, const unsigned char* fl, int i, int j) { return (fl[CI(i, j)] & CF_ACTX) != 0; }
+YG_DEV bool act_y(const Geo& G, const unsigned char* fl, int i, int j) { return (fl[CI(i, j)] & CF_ACTY) != 0; }
 
 // acx-field to quadrature nodes of cell nb (corner = mean of the acx faces above/below)
 template <typename F, typename V>
@@ -222,52 +230,53 @@ YG_DEV double deriv_active(double vm, double v0, double vp, bool am, bool ap, do
     return 0.0;
 }
 
-__device__ __noinline__ void phase_strain(const Inst& I, const Geo& G, Team& T, const double* ux, const double* uy, double* sdudx,
-                         double* sdudy, double* sdvdx, double* sdvdy) {
-    const double* f = I.f_ice;
+template <typename SD>
+__device__ __noinline__ void phase_strain(const Inst& I, const Geo& G, Team& T, const double* ux, const double* uy, SD* sdudx,
+                                          SD* sdudy, SD* sdvdx, SD* sdvdy) {
+    const unsigned char* fl = I.cflag;
     const double dx = G.dx, dy = G.dy;
     for (int c = T.tid; c < G.n2; c += T.nthr) {
         Nb n = make_nb(G, c);
         const int i = n.i, j = n.j;
         double dudx = (ux[CI(n.ip1, j)] - ux[CI(n.im1, j)]) / (2.0 * dx);
-        double dudy = deriv_active(ux[CI(i, n.jm1)], ux[c], ux[CI(i, n.jp1)], act_x(G, f, i, n.jm1), act_x(G, f, i, n.jp1), dy);
-        double dvdx = deriv_active(uy[CI(n.im1, j)], uy[c], uy[CI(n.ip1, j)], act_y(G, f, n.im1, j), act_y(G, f, n.ip1, j), dx);
+        double dudy = deriv_active(ux[CI(i, n.jm1)], ux[c], ux[CI(i, n.jp1)], act_x(G, fl, i, n.jm1), act_x(G, fl, i, n.jp1), dy);
+        double dvdx = deriv_active(uy[CI(n.im1, j)], uy[c], uy[CI(n.ip1, j)], act_y(G, fl, n.im1, j), act_y(G, fl, n.ip1, j), dx);
         double dvdy = (uy[CI(i, n.jp1)] - uy[CI(i, n.jm1)]) / (2.0 * dy);
         int d1, d2, d3;
-        if (f[c] == 1.0 && f[CI(n.ip1, j)] < 1.0) {
+        if ((fl[c] & CF_ICE) && !(fl[CI(n.ip1, j)] & CF_ICE)) {
             int im2;
             nbr_bc(n.im1, j, G.nx, G.ny, G.bc, im2, d1, d2, d3);
-            if (f[CI(n.im1, j)] == 1.0 && im2 != n.im1)
+            if ((fl[CI(n.im1, j)] & CF_ICE) && im2 != n.im1)
                 dudx = (1.0 * ux[CI(im2, j)] - 4.0 * ux[CI(n.im1, j)] + 3.0 * ux[c]) / (2.0 * dx);
             else
                 dudx = (ux[c] - ux[CI(n.im1, j)]) / dx;
-        } else if (f[c] < 1.0 && f[CI(n.ip1, j)] == 1.0) {
+        } else if (!(fl[c] & CF_ICE) && (fl[CI(n.ip1, j)] & CF_ICE)) {
             int ip2;
             nbr_bc(n.ip1, j, G.nx, G.ny, G.bc, d1, ip2, d2, d3);
-            if (ip2 != n.ip1 && f[CI(ip2, j)] == 1.0)
+            if (ip2 != n.ip1 && (fl[CI(ip2, j)] & CF_ICE))
                 dudx = -(1.0 * ux[CI(ip2, j)] - 4.0 * ux[CI(n.ip1, j)] + 3.0 * ux[c]) / (2.0 * dx);
             else
                 dudx = (ux[CI(n.ip1, j)] - ux[c]) / dx;
         }
-        if (f[c] == 1.0 && f[CI(i, n.jp1)] < 1.0) {
+        if ((fl[c] & CF_ICE) && !(fl[CI(i, n.jp1)] & CF_ICE)) {
             int jm2;
             nbr_bc(i, n.jm1, G.nx, G.ny, G.bc, d1, d2, jm2, d3);
-            if (f[CI(i, n.jm1)] == 1.0 && jm2 != n.jm1)
+            if ((fl[CI(i, n.jm1)] & CF_ICE) && jm2 != n.jm1)
                 dvdy = (1.0 * uy[CI(i, jm2)] - 4.0 * uy[CI(i, n.jm1)] + 3.0 * uy[c]) / (2.0 * dy);
             else
                 dvdy = (uy[c] - uy[CI(i, n.jm1)]) / dy;
-        } else if (f[c] < 1.0 && f[CI(i, n.jp1)] == 1.0) {
+        } else if (!(fl[c] & CF_ICE) && (fl[CI(i, n.jp1)] & CF_ICE)) {
             int jp2;
             nbr_bc(i, n.jp1, G.nx, G.ny, G.bc, d1, d2, d3, jp2);
-            if (jp2 != n.jp1 && f[CI(i, jp2)] == 1.0)
+            if (jp2 != n.jp1 && (fl[CI(i, jp2)] & CF_ICE))
                 dvdy = -(1.0 * uy[CI(i, jp2)] - 4.0 * uy[CI(i, n.jp1)] + 3.0 * uy[c]) / (2.0 * dy);
             else
                 dvdy = (uy[CI(i, n.jp1)] - uy[c]) / dy;
         }
-        sdudx[c] = dudx;
-        sdudy[c] = dudy;
-        sdvdx[c] = dvdx;
-        sdvdy[c] = dvdy;
+        sdudx[c] = (SD)dudx;
+        sdudy[c] = (SD)dudy;
+        sdvdx[c] = (SD)dvdx;
+        sdvdy[c] = (SD)dvdy;
     }
 }
 
@@ -299,10 +308,10 @@ YG_DEV double beta_raw(const Inst& I, const ygpu_dyn_par& P, const Geo& G, int i
                 auto cb = [&](int a, int b) { return I.c_bed[CI(a, b)]; };
                 auto aa = [&](int a, int b) { return I.f_ice[CI(a, b)] == 1.0 && I.f_grnd[CI(a, b)] > 0.0; };
                 nodes_aa(G, n, cb, aa, true, cbn);
-                bool ax[6] = {act_x(G, I.f_ice, n.im1, n.jm1), act_x(G, I.f_ice, n.im1, n.j), act_x(G, I.f_ice, n.im1, n.jp1),
-                              act_x(G, I.f_ice, n.i, n.jm1), act_x(G, I.f_ice, n.i, n.j), act_x(G, I.f_ice, n.i, n.jp1)};
-                bool ay[6] = {act_y(G, I.f_ice, n.im1, n.jm1), act_y(G, I.f_ice, n.i, n.jm1), act_y(G, I.f_ice, n.ip1, n.jm1),
-                              act_y(G, I.f_ice, n.im1, n.j), act_y(G, I.f_ice, n.i, n.j), act_y(G, I.f_ice, n.ip1, n.j)};
+                bool ax[6] = {act_x(G, I.cflag, n.im1, n.jm1), act_x(G, I.cflag, n.im1, n.j), act_x(G, I.cflag, n.im1, n.jp1),
+                              act_x(G, I.cflag, n.i, n.jm1), act_x(G, I.cflag, n.i, n.j), act_x(G, I.cflag, n.i, n.jp1)};
+                bool ay[6] = {act_y(G, I.cflag, n.im1, n.jm1), act_y(G, I.cflag, n.i, n.jm1), act_y(G, I.cflag, n.ip1, n.jm1),
+                              act_y(G, I.cflag, n.im1, n.j), act_y(G, I.cflag, n.i, n.j), act_y(G, I.cflag, n.ip1, n.j)};
                 auto vx = [&](int a, int b) { return ux_b[CI(a, b)]; };
                 auto vy = [&](int a, int b) { return uy_b[CI(a, b)]; };
                 nodes_acx(G, n, vx, ax, uxn);
@@ -460,10 +469,10 @@ __device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, c
 // VD is the storage of the new viscosity (double, or float for the FP32
 // working copy of the mixed mode); log(visc) is kept in R. vcur (the caller's
 // FP64 viscosity) is read only when no log is carried yet (first iteration).
-template <typename R, typename VD>
+template <typename R, typename VD, typename SR = double>
 __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T,
-                                          const double* vcur, VD* vnew, const double* sdudx,
-                                          const double* sdudy, const double* sdvdx, const double* sdvdy, bool relax,
+                                          const double* vcur, VD* vnew, const SR* sdudx,
+                                          const SR* sdudy, const SR* sdvdx, const SR* sdvdy, bool relax,
                                           bool diva, bool first_copy, bool have_log, bool visc_only = false) {
     const int nz = G.nz, n2 = G.n2;
     const R p1 = (R)((1.0 - I.n_glen) / (2.0 * I.n_glen));
@@ -486,17 +495,18 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                 I.tbp_y[c] = I.taub_y[c];
             }
         }
-        const bool ice = (f[c] == 1.0);
+        const bool ice = (I.cflag[c] & CF_ICE) != 0;
         const double Hc = I.H[c];
         // quadrature-node horizontal strain rates (independent of k)
         R dudxn[4], dudyn[4], dvdxn[4], dvdyn[4];
         bool ax[6], ay[6];
         R e_aa = R(0);
         if (ice && vm == 1) {
-            ax[0] = act_x(G, f, n.im1, n.jm1); ax[1] = act_x(G, f, n.im1, n.j); ax[2] = act_x(G, f, n.im1, n.jp1);
-            ax[3] = act_x(G, f, n.i, n.jm1); ax[4] = act_x(G, f, n.i, n.j); ax[5] = act_x(G, f, n.i, n.jp1);
-            ay[0] = act_y(G, f, n.im1, n.jm1); ay[1] = act_y(G, f, n.i, n.jm1); ay[2] = act_y(G, f, n.ip1, n.jm1);
-            ay[3] = act_y(G, f, n.im1, n.j); ay[4] = act_y(G, f, n.i, n.j); ay[5] = act_y(G, f, n.ip1, n.j);
+            const unsigned char* fl = I.cflag;
+            ax[0] = act_x(G, fl, n.im1, n.jm1); ax[1] = act_x(G, fl, n.im1, n.j); ax[2] = act_x(G, fl, n.im1, n.jp1);
+            ax[3] = act_x(G, fl, n.i, n.jm1); ax[4] = act_x(G, fl, n.i, n.j); ax[5] = act_x(G, fl, n.i, n.jp1);
+            ay[0] = act_y(G, fl, n.im1, n.jm1); ay[1] = act_y(G, fl, n.i, n.jm1); ay[2] = act_y(G, fl, n.ip1, n.jm1);
+            ay[3] = act_y(G, fl, n.im1, n.j); ay[4] = act_y(G, fl, n.i, n.j); ay[5] = act_y(G, fl, n.ip1, n.j);
             nodes_acx(G, n, [&](int a, int b) { return sdudx[CI(a, b)]; }, ax, dudxn);
             nodes_acx(G, n, [&](int a, int b) { return sdudy[CI(a, b)]; }, ax, dudyn);
             nodes_acy(G, n, [&](int a, int b) { return sdvdx[CI(a, b)]; }, ay, dvdxn);
@@ -779,8 +789,9 @@ __device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, c
             double v[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                bool ice = (I.f_ice[cc[q]] == 1.0);
-                bool ocn = (!ice) && (I.z_bed[cc[q]] < I.z_sl[cc[q]]);
+                const unsigned fq = I.cflag[cc[q]];
+                bool ice = (fq & CF_ICE) != 0;
+                bool ocn = (fq & CF_OCN) != 0;
                 nice += ice;
                 anyocn = anyocn || ocn;
                 v[q] = ice ? I.visc_int[cc[q]] : 0.0;
@@ -2553,6 +2564,7 @@ __device__ __noinline__ void step_setup(const Inst& I, const ygpu_dyn_par& P, Te
     for (int c = T.tid; c < G.n2; c += T.nthr) {
         I.err_x[c] = 1.0;
         I.err_y[c] = 1.0;
+        I.cflag[c] = cell_flags(G, I, c);
         if (!diva) {
             // set_inactive_margins (velocity_general.f90:1687-1750), SSA only
             Nb n = make_nb(G, c);
@@ -2605,8 +2617,17 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
     double t1 = 0, t2 = 0, t3 = 0, t4 = 0;
     int status = YGPU_OK;
     double bn2 = 0.0;
+    // mixed mode: the strain rates in FP32 (the column pass computes in FP32),
+    // stored in the first half of the same scratch arrays
+    float* fsdudx = (float*)sdudx;
+    float* fsdudy = (float*)sdudy;
+    float* fsdvdx = (float*)sdvdx;
+    float* fsdvdy = (float*)sdvdy;
     if (P.visc_method == 1 || diva) {
-        if (P.visc_method == 1) phase_strain(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
+        if (P.visc_method == 1) {
+            if (mixed) phase_strain<float>(I, G, T, I.u_x, I.u_y, fsdudx, fsdudy, fsdvdx, fsdvdy);
+            else phase_strain<double>(I, G, T, I.u_x, I.u_y, sdudx, sdudy, sdvdx, sdvdy);
+        }
         if (diva) {
             if (!mixed) phase_shear<double, double>(I, G, T, vcur);
             else if (iter == 1) phase_shear<float, double>(I, G, T, I.visc);
@@ -2616,7 +2637,8 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
     }
     t1 = clk.lap();
     if (mixed)
-        phase_column<float, float>(I, P, G, T, I.visc, vnew_f, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
+        phase_column<float, float, float>(I, P, G, T, I.visc, vnew_f, fsdudx, fsdudy, fsdvdx, fsdvdy, relax, diva, true,
+                                          iter > 1);
     else
         phase_column<double, double>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
     if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
