@@ -232,6 +232,42 @@ int ygpu_calc_dyn_inputs(const double* H_ice, const double* z_bed, const double*
                          int boundaries, int nx, int ny);
 
 /*
+ * Post-solve diagnostics of calc_ydyn (src/yelmo_dynamics.f90:304-336 and the
+ * DIVA depth averages of :642-644), on the GPU. All arrays are (nx,ny) or
+ * (nx,ny,nz) column-major like the solver fields; f_ice is f_ice_dyn.
+ *   ux_i_bar, uy_i_bar    calc_vertical_integrated_2D(ux_i / uy_i, zeta_aa), yelmo_tools.f90:1064
+ *   qq_acx, qq_acy        calc_ice_flux (upwind thickness), velocity_general.f90:1752
+ *   qq_gl_acx, qq_gl_acy  calc_grounding_line_flux, velocity_general.f90:1825
+ *   qq, taub, taud, uxy_b, uxy_i_bar, uxy_bar, uxy(:,:,k)
+ *                         calc_magnitude_from_staggered, yelmo_tools.f90:287
+ *   ux_s, uy_s, uxy_s     the top layer of ux, uy, uxy (yelmo_dynamics.f90:330-333)
+ *   f_vbvs                calc_vel_ratio(uxy_b, uxy_s), velocity_general.f90:1888
+ * Optional groups: ux_i/uy_i/zeta_aa NULL skips the depth averages (ux_i_bar
+ * and uy_i_bar are then inputs, or NULL to skip uxy_i_bar); ux/uy NULL skips
+ * uxy, the surface fields and f_vbvs. Computed in FP64 without contraction:
+ * bit-exact with a CPU evaluation of the same expressions.
+ */
+typedef struct ygpu_dyn_diag {
+    int nx, ny, nz;
+    double dx, dy;
+    /* inputs */
+    const double *ux_bar, *uy_bar, *ux_b, *uy_b, *taub_acx, *taub_acy, *taud_acx, *taud_acy;
+    const double *H_ice, *f_ice, *f_grnd;
+    const double *ux_i, *uy_i, *zeta_aa;   /* 3D shear velocity (DIVA) and the layers */
+    const double *ux, *uy;                 /* 3D velocity */
+    /* outputs (ux_i_bar / uy_i_bar: outputs with ux_i, else inputs) */
+    double *ux_i_bar, *uy_i_bar;
+    double *qq_acx, *qq_acy, *qq, *qq_gl_acx, *qq_gl_acy;
+    double *taub, *taud, *uxy_b, *uxy_i_bar, *uxy_bar, *uxy;
+    double *ux_s, *uy_s, *uxy_s, *f_vbvs;
+} ygpu_dyn_diag;
+
+/* host arrays (staged through the calling thread's default context) */
+int ygpu_calc_dyn_diagnostics(const ygpu_dyn_diag* fields, int boundaries);
+/* device arrays, on `stream` (a cudaStream_t; NULL: the default stream); asynchronous */
+int ygpu_calc_dyn_diagnostics_device(void* stream, const ygpu_dyn_diag* fields, int boundaries);
+
+/*
  * ygpu_linear_solver_matrix_solve -- GPU Krylov solve of a CSR system, the
  * drop-in for linear_solver_matrix_solve (solver_linear.F90:151-190) with the
  * linear_solver_class arrays (1-based a_ptr/a_index as Fortran holds them).

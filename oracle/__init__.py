@@ -46,6 +46,8 @@ def lib():
                                        C.c_double, C.c_int, ip, dp]
         L.orc_linear_solve.restype = C.c_int
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_calc_dyn_diagnostics.argtypes = [C.POINTER(abi.DynDiag), C.c_int]
+        L.orc_calc_dyn_diagnostics.restype = C.c_int
         _lib = L
     return _lib
 
@@ -125,6 +127,17 @@ def assemble_csr(energy: bool, f: dict, dx: float, dy: float, boundaries: str, N
     if nnz < 0:
         raise RuntimeError(f"orc_assemble_csr failed ({nnz})")
     return ptr_, idx[:nnz].copy(), val[:nnz].copy(), b, x, cf
+
+
+def calc_dyn_diagnostics(arrays: dict, dx: float, dy: float, boundaries: str) -> dict:
+    """orc_calc_dyn_diagnostics on the arrays of yelmo_gb300.gpu.diagnostics_arrays (filled in place)."""
+    nx, ny = arrays["H_ice"].shape
+    nz = arrays["zeta_aa"].shape[0] if "zeta_aa" in arrays else (arrays["ux"].shape[2] if "ux" in arrays else 1)
+    D = abi.dyn_diag(arrays, nx, ny, nz, dx, dy)
+    st = lib().orc_calc_dyn_diagnostics(C.byref(D), abi.BOUNDARY_CODES[boundaries])
+    if st != 0:
+        raise RuntimeError(f"orc_calc_dyn_diagnostics failed ({st})")
+    return arrays
 
 
 def linear_solve(ptr_, idx, val, b, x, method, precond, maxiter, tol, initx_zeros=False):

@@ -2309,3 +2309,104 @@ static int diva_solve(double* ux, double* uy, double* ux_bar, double* uy_bar, do
     free(F2); free(F2x); free(F2y);
     return status;
 }
+
+
+/* ======================================================================== */
+/* Post-solve diagnostics (yelmo_dynamics.f90:304-336, :642-644)            */
+/* ======================================================================== */
+
+#define ORC_TOL_UNDERFLOW 1e-15
+
+/* integrate_trapezoid1D_pt, yelmo_tools.f90:1092-1122 */
+static double diag_trapz(const double* v, const double* zeta, size_t c, size_t n2, int nz) {
+    double s = 0.0;
+    for (int k = 1; k < nz; k++) {
+        double mid = 0.5 * (v[(size_t)k * n2 + c] + v[(size_t)(k - 1) * n2 + c]);
+        s = s + mid * (zeta[k] - zeta[k - 1]);
+    }
+    return s;
+}
+
+/* calc_magnitude_from_staggered, yelmo_tools.f90:287-339 */
+static double diag_mag(const double* u, const double* v, const double* f_ice, size_t c, size_t cxm, size_t cym) {
+    double unow = 0.0, vnow = 0.0;
+    if (f_ice[c] == 1.0) {
+        unow = 0.5 * (u[cxm] + u[c]);
+        vnow = 0.5 * (v[cym] + v[c]);
+        if (fabs(unow) < ORC_TOL_UNDERFLOW) unow = 0.0;
+        if (fabs(vnow) < ORC_TOL_UNDERFLOW) vnow = 0.0;
+    }
+    double m = sqrt(unow * unow + vnow * vnow);
+    if (fabs(m) < ORC_TOL_UNDERFLOW) m = 0.0;
+    return m;
+}
+
+/* is_gl_face, velocity_general.f90:1873-1882 */
+static int diag_gl_face(double fg0, double fg1, double fi0, double fi1) {
+    return (fg0 > 0.0 && fg1 == 0.0 && fi1 > 0.0) || (fg1 > 0.0 && fg0 == 0.0 && fi0 > 0.0);
+}
+
+int orc_calc_dyn_diagnostics(const ygpu_dyn_diag* D, int bc) {
+    if (!D || D->nx < 2 || D->ny < 2) return YGPU_ERR_BAD_ARG;
+    const int nx = D->nx, ny = D->ny, nz = D->nz;
+    const size_t n2 = (size_t)nx * ny;
+    int px, py;
+    periodic_dirs(bc, &px, &py);
+    /* depth averages of the shear velocity (calc_ydyn_diva, yelmo_dynamics.f90:642-644) */
+    if (D->ux_i)
+        for (size_t c = 0; c < n2; c++) {
+            D->ux_i_bar[c] = diag_trapz(D->ux_i, D->zeta_aa, c, n2, nz);
+            D->uy_i_bar[c] = diag_trapz(D->uy_i, D->zeta_aa, c, n2, nz);
+        }
+    /* calc_ice_flux, velocity_general.f90:1752-1823 (upwind thickness; the last
+       face of a non-periodic direction stays 0) */
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            int im1, ip1, jm1, jp1;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            const size_t c = (size_t)i + (size_t)nx * j;
+            double qx = 0.0, qy = 0.0;
+            if (i < nx - 1 || px) {
+                double area = (D->ux_bar[c] >= 0.0) ? D->H_ice[c] * D->dy : D->H_ice[ip1 + (size_t)nx * j] * D->dy;
+                qx = area * D->ux_bar[c];
+            }
+            if (j < ny - 1 || py) {
+                double area = (D->uy_bar[c] >= 0.0) ? D->H_ice[c] * D->dx : D->H_ice[i + (size_t)nx * jp1] * D->dx;
+                qy = area * D->uy_bar[c];
+            }
+            D->qq_acx[c] = qx;
+            D->qq_acy[c] = qy;
+        }
+    /* calc_grounding_line_flux, velocity_general.f90:1825-1886; magnitudes */
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            int im1, ip1, jm1, jp1;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            const size_t c = (size_t)i + (size_t)nx * j, cx = ip1 + (size_t)nx * j, cy = i + (size_t)nx * jp1;
+            const size_t cxm = im1 + (size_t)nx * j, cym = i + (size_t)nx * jm1;
+            D->qq_gl_acx[c] = diag_gl_face(D->f_grnd[c], D->f_grnd[cx], D->f_ice[c], D->f_ice[cx]) ? D->qq_acx[c] : 0.0;
+            D->qq_gl_acy[c] = diag_gl_face(D->f_grnd[c], D->f_grnd[cy], D->f_ice[c], D->f_ice[cy]) ? D->qq_acy[c] : 0.0;
+            D->qq[c] = diag_mag(D->qq_acx, D->qq_acy, D->f_ice, c, cxm, cym);
+            D->taub[c] = diag_mag(D->taub_acx, D->taub_acy, D->f_ice, c, cxm, cym);
+            D->taud[c] = diag_mag(D->taud_acx, D->taud_acy, D->f_ice, c, cxm, cym);
+            const double ub = diag_mag(D->ux_b, D->uy_b, D->f_ice, c, cxm, cym);
+            D->uxy_b[c] = ub;
+            if (D->uxy_i_bar && D->ux_i_bar) D->uxy_i_bar[c] = diag_mag(D->ux_i_bar, D->uy_i_bar, D->f_ice, c, cxm, cym);
+            D->uxy_bar[c] = diag_mag(D->ux_bar, D->uy_bar, D->f_ice, c, cxm, cym);
+            if (D->ux) {
+                double us = 0.0;
+                for (int k = 0; k < nz; k++) {
+                    const size_t o = (size_t)k * n2;
+                    us = diag_mag(D->ux + o, D->uy + o, D->f_ice, c, cxm, cym);
+                    D->uxy[o + c] = us;
+                }
+                const size_t top = (size_t)(nz - 1) * n2;
+                D->ux_s[c] = D->ux[top + c];
+                D->uy_s[c] = D->uy[top + c];
+                D->uxy_s[c] = us;
+                /* calc_vel_ratio, velocity_general.f90:1888-1905 */
+                D->f_vbvs[c] = (us > 0.0) ? fmin(1.0, ub / us) : 1.0;
+            }
+        }
+    return YGPU_OK;
+}

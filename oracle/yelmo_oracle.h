@@ -151,6 +151,11 @@ void orc_dyn_par_defaults(ygpu_dyn_par* par);
 int  orc_parse_lis_opt(const char* opts, ygpu_dyn_par* par);
 void orc_set_threads(int n);
 
+/* Post-solve diagnostics of calc_ydyn (yelmo_dynamics.f90:304-336, :642-644):
+   depth averages, ice and grounding-line fluxes, magnitudes, surface fields,
+   f_vbvs; the same groups and NULL conventions as ygpu_calc_dyn_diagnostics. */
+int orc_calc_dyn_diagnostics(const ygpu_dyn_diag* D, int boundaries);
+
 #ifdef __cplusplus
 }
 #endif

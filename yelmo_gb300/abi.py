@@ -73,6 +73,33 @@ class Stats(C.Structure):
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
+DIAG_INPUTS = ("ux_bar", "uy_bar", "ux_b", "uy_b", "taub_acx", "taub_acy", "taud_acx", "taud_acy",
+               "H_ice", "f_ice", "f_grnd", "ux_i", "uy_i", "zeta_aa", "ux", "uy")
+DIAG_OUTPUTS = ("ux_i_bar", "uy_i_bar", "qq_acx", "qq_acy", "qq", "qq_gl_acx", "qq_gl_acy", "taub", "taud",
+                "uxy_b", "uxy_i_bar", "uxy_bar", "uxy", "ux_s", "uy_s", "uxy_s", "f_vbvs")
+
+
+class DynDiag(C.Structure):
+    """ygpu_dyn_diag: arrays of the post-solve diagnostics."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("dx", C.c_double), ("dy", C.c_double)] + \
+        [(n, C.c_void_p) for n in DIAG_INPUTS + DIAG_OUTPUTS]
+
+
+def dyn_diag(arrays: dict, nx: int, ny: int, nz: int, dx: float, dy: float) -> DynDiag:
+    """A DynDiag over the numpy arrays of `arrays` (absent names stay NULL)."""
+    D = DynDiag()
+    D.nx, D.ny, D.nz, D.dx, D.dy = nx, ny, nz, dx, dy
+    for n in DIAG_INPUTS + DIAG_OUTPUTS:
+        a = arrays.get(n)
+        if a is None:
+            continue
+        want = (nz,) if n == "zeta_aa" else (nx, ny, nz) if n in ("ux_i", "uy_i", "ux", "uy", "uxy") else (nx, ny)
+        if a.shape != want:
+            raise ValueError(f"{n}: shape {a.shape}, expected {want}")
+        ptr(a, "d")
+        setattr(D, n, a.ctypes.data)
+    return D
+
 
 class Fields(C.Structure):
     """ygpu_fields: device pointers of one instance."""

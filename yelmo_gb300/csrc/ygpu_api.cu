@@ -17,6 +17,7 @@
 #include <string>
 #include <queue>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "ygpu_common.cuh"
@@ -1177,6 +1178,74 @@ extern "C" int ygpu_calc_dyn_inputs(const double* H_ice, const double* z_bed, co
                                 d(a_fy), (int*)S.args[a_mf].dev, d(a_dx), d(a_dy), d(a_tx), d(a_ty), d(a_lx), d(a_ly),
                                 dx, grad_lim, taud_lim, rho_ice, rho_sw, g, boundaries, nx, ny);
     if (st) return st;
+    return S.download(c);
+}
+
+static int dyn_diag_check(const ygpu_dyn_diag* D, int bc) {
+    if (!D || D->nx < 2 || D->ny < 2 || !(D->dx > 0.0) || !(D->dy > 0.0) || bc < 0 || bc > 6) {
+        ygpu_set_error("bad arguments");
+        return YGPU_ERR_BAD_ARG;
+    }
+    if (any_null({D->ux_bar, D->uy_bar, D->ux_b, D->uy_b, D->taub_acx, D->taub_acy, D->taud_acx, D->taud_acy, D->H_ice,
+                  D->f_ice, D->f_grnd, D->qq_acx, D->qq_acy, D->qq, D->qq_gl_acx, D->qq_gl_acy, D->taub, D->taud,
+                  D->uxy_b, D->uxy_bar})) {
+        ygpu_set_error("a required diagnostics array is NULL");
+        return YGPU_ERR_BAD_ARG;
+    }
+    if (D->ux_i && (any_null({D->uy_i, D->zeta_aa, D->ux_i_bar, D->uy_i_bar}) || D->nz < 2)) {
+        ygpu_set_error("ux_i needs uy_i, zeta_aa, ux_i_bar, uy_i_bar and nz >= 2");
+        return YGPU_ERR_BAD_ARG;
+    }
+    if (D->uxy_i_bar && (!D->ux_i_bar || !D->uy_i_bar)) {
+        ygpu_set_error("uxy_i_bar needs ux_i_bar and uy_i_bar");
+        return YGPU_ERR_BAD_ARG;
+    }
+    if (D->ux && (any_null({D->uy, D->uxy, D->ux_s, D->uy_s, D->uxy_s, D->f_vbvs}) || D->nz < 1)) {
+        ygpu_set_error("ux needs uy, uxy, ux_s, uy_s, uxy_s, f_vbvs and nz >= 1");
+        return YGPU_ERR_BAD_ARG;
+    }
+    return YGPU_OK;
+}
+
+extern "C" int ygpu_calc_dyn_diagnostics_device(void* stream, const ygpu_dyn_diag* D, int boundaries) {
+    int st = dyn_diag_check(D, boundaries);
+    if (st) return st;
+    return ygpu_dyn_diagnostics_device((cudaStream_t)stream, *D, boundaries);
+}
+
+// host arrays: in-only inputs, the depth averages in or out, every other output out
+extern "C" int ygpu_calc_dyn_diagnostics(const ygpu_dyn_diag* H, int boundaries) {
+    int st = dyn_diag_check(H, boundaries);
+    if (st) return st;
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const size_t b2 = (size_t)H->nx * H->ny * 8, b3 = b2 * (size_t)(H->nz > 0 ? H->nz : 0);
+    Staging S;
+    ygpu_dyn_diag D = *H;
+    std::vector<std::pair<size_t, const void**>> map;
+    auto in = [&](const double* const* src, const double** dst, size_t bytes) {
+        if (*src) map.push_back({S.add((void*)*src, bytes, 1, 0), (const void**)dst});
+    };
+    auto out = [&](double* const* src, double** dst, size_t bytes, bool also_in) {
+        if (*src) map.push_back({S.add((void*)*src, bytes, also_in, 1), (const void**)dst});
+    };
+    in(&H->ux_bar, &D.ux_bar, b2); in(&H->uy_bar, &D.uy_bar, b2); in(&H->ux_b, &D.ux_b, b2); in(&H->uy_b, &D.uy_b, b2);
+    in(&H->taub_acx, &D.taub_acx, b2); in(&H->taub_acy, &D.taub_acy, b2);
+    in(&H->taud_acx, &D.taud_acx, b2); in(&H->taud_acy, &D.taud_acy, b2);
+    in(&H->H_ice, &D.H_ice, b2); in(&H->f_ice, &D.f_ice, b2); in(&H->f_grnd, &D.f_grnd, b2);
+    in(&H->ux_i, &D.ux_i, b3); in(&H->uy_i, &D.uy_i, b3); in(&H->zeta_aa, &D.zeta_aa, (size_t)H->nz * 8);
+    in(&H->ux, &D.ux, b3); in(&H->uy, &D.uy, b3);
+    const bool avg_out = (H->ux_i != nullptr);
+    out(&H->ux_i_bar, &D.ux_i_bar, b2, !avg_out); out(&H->uy_i_bar, &D.uy_i_bar, b2, !avg_out);
+    out(&H->qq_acx, &D.qq_acx, b2, false); out(&H->qq_acy, &D.qq_acy, b2, false); out(&H->qq, &D.qq, b2, false);
+    out(&H->qq_gl_acx, &D.qq_gl_acx, b2, false); out(&H->qq_gl_acy, &D.qq_gl_acy, b2, false);
+    out(&H->taub, &D.taub, b2, false); out(&H->taud, &D.taud, b2, false); out(&H->uxy_b, &D.uxy_b, b2, false);
+    out(&H->uxy_i_bar, &D.uxy_i_bar, b2, false); out(&H->uxy_bar, &D.uxy_bar, b2, false);
+    out(&H->uxy, &D.uxy, b3, false); out(&H->ux_s, &D.ux_s, b2, false); out(&H->uy_s, &D.uy_s, b2, false);
+    out(&H->uxy_s, &D.uxy_s, b2, false); out(&H->f_vbvs, &D.f_vbvs, b2, false);
+    if ((st = S.upload(c))) return st;
+    for (auto& m : map) *m.second = S.args[m.first].dev;
+    if ((st = ygpu_dyn_diagnostics_device(c->stream, D, boundaries))) return st;
     return S.download(c);
 }
 

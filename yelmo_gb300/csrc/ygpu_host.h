@@ -99,6 +99,7 @@ int ygpu_dyn_inputs_device(cudaStream_t s, const double* H, const double* zb, co
                            double* dzsdx, double* dzsdy, double* tdx, double* tdy, double* tlx, double* tly,
                            double dx, double grad_lim, double taud_lim, double rho_ice, double rho_sw, double g,
                            int bc, int nx, int ny);
+int ygpu_dyn_diagnostics_device(cudaStream_t s, const ygpu_dyn_diag& D, int bc);
 int ygpu_ssa_masks_device(cudaStream_t s, int* mx, int* my, const int* mf, const double* f_ice, const double* f_grnd,
                           int lat, int bc, int nx, int ny);
 

@@ -238,3 +238,112 @@ int ygpu_ssa_masks_device(cudaStream_t s, int* mx, int* my, const int* mf, const
     ygpu_count_launches(1);
     return YGPU_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Post-solve diagnostics of calc_ydyn (yelmo_dynamics.f90:304-336, :642-644)
+// ---------------------------------------------------------------------------
+#define YG_TOL_UNDERFLOW 1e-15
+
+// integrate_trapezoid1D_pt (yelmo_tools.f90:1092-1122) of the column of cell c
+__device__ double trapz_column(const double* v, const double* zeta, int c, int n2, int nz) {
+    double s = 0.0;
+    for (int k = 1; k < nz; k++) {
+        const double mid = 0.5 * (v[(size_t)k * n2 + c] + v[(size_t)(k - 1) * n2 + c]);
+        s = s + mid * (zeta[k] - zeta[k - 1]);
+    }
+    return s;
+}
+
+// is_gl_face of calc_grounding_line_flux (velocity_general.f90:1873-1882)
+__device__ bool gl_face(double fg0, double fg1, double fi0, double fi1) {
+    return (fg0 > 0.0 && fg1 == 0.0 && fi1 > 0.0) || (fg1 > 0.0 && fg0 == 0.0 && fi0 > 0.0);
+}
+
+// depth averages of the shear velocity, ice flux (calc_ice_flux,
+// velocity_general.f90:1752-1823) and grounding-line flux (:1825-1886)
+__global__ void k_diag_faces(ygpu_dyn_diag D, int bc) {
+    const int nx = D.nx, ny = D.ny, n2 = nx * ny;
+    bool px, py;
+    periodic_dirs(bc, px, py);
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n2; c += gridDim.x * blockDim.x) {
+        const int i = c % nx, j = c / nx;
+        int im1, ip1, jm1, jp1;
+        nbr_bc(i, j, nx, ny, bc, im1, ip1, jm1, jp1);
+        if (D.ux_i) {
+            D.ux_i_bar[c] = trapz_column(D.ux_i, D.zeta_aa, c, n2, D.nz);
+            D.uy_i_bar[c] = trapz_column(D.uy_i, D.zeta_aa, c, n2, D.nz);
+        }
+        const int cx = ip1 + nx * j, cy = i + nx * jp1;
+        double qx = 0.0, qy = 0.0;
+        if (i < nx - 1 || px) {
+            const double area = (D.ux_bar[c] >= 0.0) ? D.H_ice[c] * D.dy : D.H_ice[cx] * D.dy;
+            qx = area * D.ux_bar[c];
+        }
+        if (j < ny - 1 || py) {
+            const double area = (D.uy_bar[c] >= 0.0) ? D.H_ice[c] * D.dx : D.H_ice[cy] * D.dx;
+            qy = area * D.uy_bar[c];
+        }
+        D.qq_acx[c] = qx;
+        D.qq_acy[c] = qy;
+        D.qq_gl_acx[c] = gl_face(D.f_grnd[c], D.f_grnd[cx], D.f_ice[c], D.f_ice[cx]) ? qx : 0.0;
+        D.qq_gl_acy[c] = gl_face(D.f_grnd[c], D.f_grnd[cy], D.f_ice[c], D.f_ice[cy]) ? qy : 0.0;
+    }
+}
+
+// calc_magnitude_from_staggered (yelmo_tools.f90:287-339) at cell (i, j)
+__device__ double mag_staggered(const double* u, const double* v, const double* f_ice, int c, int cxm, int cym) {
+    double unow = 0.0, vnow = 0.0;
+    if (f_ice[c] == 1.0) {
+        unow = 0.5 * (u[cxm] + u[c]);
+        vnow = 0.5 * (v[cym] + v[c]);
+        if (fabs(unow) < YG_TOL_UNDERFLOW) unow = 0.0;
+        if (fabs(vnow) < YG_TOL_UNDERFLOW) vnow = 0.0;
+    }
+    double m = sqrt(unow * unow + vnow * vnow);
+    if (fabs(m) < YG_TOL_UNDERFLOW) m = 0.0;
+    return m;
+}
+
+// magnitudes, surface fields and f_vbvs (calc_vel_ratio, velocity_general.f90:1888-1905)
+__global__ void k_diag_cells(ygpu_dyn_diag D, int bc) {
+    const int nx = D.nx, ny = D.ny, n2 = nx * ny, nz = D.nz;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n2; c += gridDim.x * blockDim.x) {
+        const int i = c % nx, j = c / nx;
+        int im1, ip1, jm1, jp1;
+        nbr_bc(i, j, nx, ny, bc, im1, ip1, jm1, jp1);
+        const int cxm = im1 + nx * j, cym = i + nx * jm1;
+        D.qq[c] = mag_staggered(D.qq_acx, D.qq_acy, D.f_ice, c, cxm, cym);
+        D.taub[c] = mag_staggered(D.taub_acx, D.taub_acy, D.f_ice, c, cxm, cym);
+        D.taud[c] = mag_staggered(D.taud_acx, D.taud_acy, D.f_ice, c, cxm, cym);
+        const double ub = mag_staggered(D.ux_b, D.uy_b, D.f_ice, c, cxm, cym);
+        D.uxy_b[c] = ub;
+        if (D.uxy_i_bar && D.ux_i_bar) D.uxy_i_bar[c] = mag_staggered(D.ux_i_bar, D.uy_i_bar, D.f_ice, c, cxm, cym);
+        D.uxy_bar[c] = mag_staggered(D.ux_bar, D.uy_bar, D.f_ice, c, cxm, cym);
+        if (D.ux) {
+            double us = 0.0;
+            for (int k = 0; k < nz; k++) {
+                const size_t o = (size_t)k * n2;
+                us = mag_staggered(D.ux + o, D.uy + o, D.f_ice, c, cxm, cym);
+                D.uxy[o + c] = us;
+            }
+            const size_t top = (size_t)(nz - 1) * n2;
+            D.ux_s[c] = D.ux[top + c];
+            D.uy_s[c] = D.uy[top + c];
+            D.uxy_s[c] = us;
+            D.f_vbvs[c] = (us > 0.0) ? fmin(1.0, ub / us) : 1.0;
+        }
+    }
+}
+
+int ygpu_dyn_diagnostics_device(cudaStream_t s, const ygpu_dyn_diag& D, int bc) {
+    const int gb = grid_for(D.nx * D.ny);
+    k_diag_faces<<<gb, 256, 0, s>>>(D, bc);
+    k_diag_cells<<<gb, 256, 0, s>>>(D, bc);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        ygpu_set_error("diagnostic kernels: %s", cudaGetErrorString(e));
+        return YGPU_ERR_CUDA;
+    }
+    ygpu_count_launches(2);
+    return YGPU_OK;
+}

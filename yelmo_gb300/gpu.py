@@ -38,7 +38,8 @@ EXPORTS = [
     "ygpu_server_create", "ygpu_server_destroy", "ygpu_server_add_member", "ygpu_server_submit",
     "ygpu_server_poll", "ygpu_server_wait", "ygpu_server_fetch", "ygpu_server_get_info",
     "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get", "ygpu_tuning_defaults",
-    "ygpu_ctx_set_tuning", "ygpu_set_neff_hook", "ygpu_solve_batch_host",
+    "ygpu_ctx_set_tuning", "ygpu_set_neff_hook", "ygpu_solve_batch_host", "ygpu_calc_dyn_diagnostics",
+    "ygpu_calc_dyn_diagnostics_device",
 ]
 
 
@@ -77,6 +78,8 @@ def lib(build_if_missing: bool = True):
                                     C.POINTER(abi.Stats)]
     L.ygpu_solve_batch_device.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.DynPar), C.c_int,
                                           C.POINTER(abi.Fields), C.POINTER(abi.Stats)]
+    L.ygpu_calc_dyn_diagnostics.argtypes = [C.POINTER(abi.DynDiag), C.c_int]
+    L.ygpu_calc_dyn_diagnostics_device.argtypes = [C.c_void_p, C.POINTER(abi.DynDiag), C.c_int]
     L.ygpu_solve_batch_host.argtypes = [C.c_int, C.POINTER(abi.DynPar), C.c_int, C.POINTER(abi.Fields),
                                         C.POINTER(abi.Stats)]
     L.ygpu_solve_device_noalloc.argtypes = [C.c_int, C.POINTER(abi.DynPar), C.POINTER(abi.Fields),
@@ -170,6 +173,38 @@ def calc_velocity_batch(fields: list, dx, n_glen: float, par: YdynParams) -> lis
     cpar = par.to_c()
     _check(lib().ygpu_solve_batch_host(kind, C.byref(cpar), n, arr, sts))
     return [s.as_dict() for s in sts]
+
+
+def diagnostics_arrays(fields: dict, nz: int, want_3d: bool = True, want_avg: bool = True) -> dict:
+    """Inputs of the post-solve diagnostics taken from a solve's field dict, with
+    zeroed output arrays (the groups: depth averages from ux_i, 3D magnitudes from ux)."""
+    nx, ny = fields["H_ice"].shape
+    out = {k: fields[k] for k in abi.DIAG_INPUTS[:11]}
+    if want_avg and "ux_i" in fields:
+        out.update(ux_i=fields["ux_i"], uy_i=fields["uy_i"], zeta_aa=fields["zeta_aa"])
+    if want_3d and "ux" in fields:
+        out.update(ux=fields["ux"], uy=fields["uy"])
+    for k in abi.DIAG_OUTPUTS:
+        if k == "uxy":
+            if "ux" in out:
+                out[k] = np.zeros((nx, ny, nz), order="F")
+        elif k in ("ux_s", "uy_s", "uxy_s", "f_vbvs") and "ux" not in out:
+            continue
+        elif k in ("ux_i_bar", "uy_i_bar", "uxy_i_bar") and "ux_i" not in out:
+            continue
+        else:
+            out[k] = np.zeros((nx, ny), order="F")
+    return out
+
+
+def calc_dyn_diagnostics(arrays: dict, dx: float, dy: float, boundaries: str) -> dict:
+    """Post-solve diagnostics on the GPU (ygpu_calc_dyn_diagnostics); the output
+    arrays of `arrays` (see diagnostics_arrays) are filled in place."""
+    nx, ny = arrays["H_ice"].shape
+    nz = arrays["zeta_aa"].shape[0] if "zeta_aa" in arrays else (arrays["ux"].shape[2] if "ux" in arrays else 1)
+    D = abi.dyn_diag(arrays, nx, ny, nz, dx, dy)
+    _check(lib().ygpu_calc_dyn_diagnostics(C.byref(D), abi.BOUNDARY_CODES[boundaries]))
+    return arrays
 
 
 def calc_dyn_inputs(inst) -> dict:
