@@ -194,6 +194,64 @@ def _copy(f):
     return {k: (v.copy(order="F") if isinstance(v, np.ndarray) else v) for k, v in f.items()}
 
 
+def diagnostics_leg(device: str, steps: int, warmup: int) -> dict:
+    """Time the post-solve diagnostics kernels (ygpu_calc_dyn_diagnostics_device)
+    on one 801 x 801 x 20 field set resident in HBM (seeded values; every group
+    on), CUDA events on the launching stream. Algorithmic bytes per cell: 31
+    2D arrays (11 inputs, 16 outputs, and 4 re-read by the second kernel) and
+    5 3D arrays (ux_i, uy_i, ux, uy in, uxy out) of 8 B."""
+    import ctypes as C
+    import torch
+    from yelmo_gb300 import abi, gpu
+    nx = ny = 801
+    nz = 20
+    gen = torch.Generator(device=device).manual_seed(7)
+    arrays, keep = {}, []
+
+    def field(n, *shape, scale=100.0):
+        t = torch.rand(*shape, dtype=torch.float64, device=device, generator=gen) * scale
+        keep.append(t)
+        arrays[n] = t
+    for n in abi.DIAG_INPUTS:
+        if n == "zeta_aa":
+            t = torch.linspace(0.0, 1.0, nz, dtype=torch.float64, device=device) ** 2
+            keep.append(t)
+            arrays[n] = t
+        elif n in ("ux_i", "uy_i", "ux", "uy"):
+            field(n, nz * nx * ny)
+        else:
+            field(n, nx * ny)
+    arrays["f_ice"].copy_((arrays["f_ice"] > 30.0).double())
+    arrays["f_grnd"].copy_((arrays["f_grnd"] > 50.0).double())
+    for n in abi.DIAG_OUTPUTS:
+        t = torch.zeros(nz * nx * ny if n == "uxy" else nx * ny, dtype=torch.float64, device=device)
+        keep.append(t)
+        arrays[n] = t
+    D = abi.DynDiag()
+    D.nx, D.ny, D.nz, D.dx, D.dy = nx, ny, nz, 4e3, 4e3
+    for n, t in arrays.items():
+        setattr(D, n, t.data_ptr())
+    L = gpu.lib()
+    stream = torch.cuda.current_stream(device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    times = []
+    for s in range(warmup + steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = L.ygpu_calc_dyn_diagnostics_device(C.c_void_p(stream.cuda_stream), C.byref(D), 0)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        if st != 0:
+            raise RuntimeError(f"diagnostics failed ({st}): {gpu.last_error()}")
+        if s >= warmup:
+            times.append(e0.elapsed_time(e1))
+    ms = statistics.mean(times)
+    alg = float(nx * ny) * (31 * 8 + 5 * nz * 8)
+    return {"workload": "801x801x20 synthetic fields, every group", "ms_per_call": ms,
+            "alg_bytes_per_call": alg, "achieved_gbs": alg / (ms / 1e3) / 1e9, "kernels": 2}
+
+
 def run_reference(args, insts, rank, world):
     """CPU reference arm: the oracle (FP64 restatement of the reference path) on all host cores."""
     if rank != 0:
@@ -475,6 +533,7 @@ def main():
             dt = time.perf_counter() - t
             if s >= args.warmup:
                 e2e1_times.append(dt)
+    diag = diagnostics_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
     i0 = insts[0]
     io = [gpu.host_io_bytes(kind, i.nx, i.ny, i.nz) for i in insts]
     h2d, d2h = sum(a for a, _ in io), sum(b for _, b in io)
@@ -553,6 +612,7 @@ def main():
         "tuning": tuned,
         "phase_ms_single": mixed["st1"]["phase_ms"] if mixed["st1"] else None,
         "clocks": clocks,
+        "diagnostics": (dict(diag, frac=diag["achieved_gbs"] / peak) if diag else None),
         "cpu_baseline": cpu_base,
     }
     print(json.dumps(line))
