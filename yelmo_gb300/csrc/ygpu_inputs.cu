@@ -293,7 +293,8 @@ __global__ void k_diag_faces(ygpu_dyn_diag D, int bc) {
 // calc_magnitude_from_staggered (yelmo_tools.f90:287-339) at cell (i, j)
 __device__ double mag_staggered(const double* u, const double* v, const double* f_ice, int c, int cxm, int cym) {
     double unow = 0.0, vnow = 0.0;
-    if (f_ice[c] == 1.0) {
+    if (f_ice[c] != 1.0) return 0.0;      // sqrt(0): the ice-free value, without the FP64 square root
+    {
         unow = 0.5 * (u[cxm] + u[c]);
         vnow = 0.5 * (v[cym] + v[c]);
         if (fabs(unow) < YG_TOL_UNDERFLOW) unow = 0.0;

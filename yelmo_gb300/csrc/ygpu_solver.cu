@@ -1121,13 +1121,15 @@ struct RowItems {
         return (q < cache) ? g_item_cache[q * blockDim.x + threadIdx.x] : lookup(t);
     }
 };
-YG_DEV RowItems make_row_items(const Team& Tm, const int* ac, int n2, int nu) {
+// use_cache = false: the rows are looked up every time (for a caller whose
+// items must survive calls of the solvers, which refill the cache)
+YG_DEV RowItems make_row_items(const Team& Tm, const int* ac, int n2, int nu, bool use_cache = true) {
     RowItems R;
     R.ac = ac;
     R.n2 = n2;
     R.nact = ac ? min(max(ac[n2], 0), n2) : n2;
     R.nitem = ac ? 2 * R.nact : nu;
-    R.cache = (blockDim.x <= YG_ITEM_BLOCK) ? YG_ITEM_CACHE : 0;
+    R.cache = (use_cache && blockDim.x <= YG_ITEM_BLOCK) ? YG_ITEM_CACHE : 0;
     int q = 0;
     for (int t = Tm.tid; t < R.nitem && q < R.cache; t += Tm.nthr, q++)
         g_item_cache[q * blockDim.x + threadIdx.x] = R.lookup(t);
@@ -2357,11 +2359,19 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
     int total = 0;
     int status = YGPU_MAXITER;
     const int max_outer = 200;           // total inner iterations stay below lin_maxiter
+    // The outer passes visit the rows of the active cells only (identity rows
+    // hold x = b, a zero residual and a zero correction, cleared here once).
+    const RowItems R = make_row_items(T, I.acell, G.n2, G.nu, false);
+    for (int u = T.tid; u < G.nu; u += T.nthr) {
+        I.fr[u] = 0.0f;
+        I.fx[u] = 0.0f;
+    }
     for (int o = 0; o < max_outer; o++) {
         // r64 = b - A64 x (FP64 residual of the outer iterate)
-        A64(T, I.x, I.q);
+        A64.apply(T, I.x, I.q, R);
         double rr = 0.0;
-        for (int u = T.tid; u < G.nu; u += T.nthr) {
+        for (int e = T.tid; e < R.nitem; e += T.nthr) {
+            const int u = R.lookup(e);
             double ru = I.b[u] - I.q[u];
             I.r[u] = ru;
             rr += ru * ru;
@@ -2372,7 +2382,8 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         if (total >= P.lin_maxiter) { status = YGPU_MAXITER; break; }
         // inner FP32 solve of A d = r, d0 = 0, scaled by ||r||
         const double nr = sqrt(rr), sc = 1.0 / nr;
-        for (int u = T.tid; u < G.nu; u += T.nthr) {
+        for (int e = T.tid; e < R.nitem; e += T.nthr) {
+            const int u = R.lookup(e);
             I.fr[u] = (float)(I.r[u] * sc);
             I.fx[u] = 0.0f;
         }
@@ -2393,7 +2404,10 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         total += it;
         outer++;
         // x += d (FP64 accumulation)
-        for (int u = T.tid; u < G.nu; u += T.nthr) I.x[u] = I.x[u] + (double)I.fx[u] * nr;
+        for (int e = T.tid; e < R.nitem; e += T.nthr) {
+            const int u = R.lookup(e);
+            I.x[u] = I.x[u] + (double)I.fx[u] * nr;
+        }
         if (!(ok = team_barrier(T))) return YGPU_ERR_TIMEOUT;
         if (st == YGPU_BREAKDOWN && it <= 1) { status = YGPU_BREAKDOWN; break; }
     }
