@@ -607,6 +607,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
         double vi = ice ? (double)vint * Hc : VISC_MIN;
         if (vi < VISC_MIN) vi = VISC_MIN;
         I.visc_int[c] = vi;
+        if (I.fN) I.fN[c] = (float)vi;     // mixed mode: the FP32 copy of the inner solves
         // calc_F_integral (n = 2), velocity_diva.f90:824-869
         if (diva) I.F2[c] = ice ? (double)f2 : 0.0;
         // calc_beta: SSA uses the iterate, DIVA the basal velocity
@@ -781,6 +782,10 @@ __device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, c
             I.drag_x[c] = wx * mx_b + wx * kx;
             I.drag_y[c] = wy * my_b + wy * ky;
         }
+        if (I.fdrag_x) {               // mixed mode: FP32 copies of the inner solves
+            I.fdrag_x[c] = (float)I.drag_x[c];
+            I.fdrag_y[c] = (float)I.drag_y[c];
+        }
         // stagger_visc_aa_ab, solver_ssa_ac.f90:1000-1067
         {
             const int cc[4] = {c, CI(n.ip1, j), CI(i, n.jp1), CI(n.ip1, n.jp1)};
@@ -797,6 +802,7 @@ __device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, c
                 v[q] = ice ? I.visc_int[cc[q]] : 0.0;
             }
             I.Nab[c] = (anyocn || nice == 0) ? 0.0 : ((v[0] + v[1]) + (v[2] + v[3])) / (double)nice;
+            if (I.fNab) I.fNab[c] = (float)I.Nab[c];
         }
     }
 }
@@ -1555,6 +1561,7 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
         I.b[u] = b;
         I.x[u] = x0;
         I.dinv[u] = (d != 0.0) ? 1.0 / d : 1.0;
+        if (I.fdinv) I.fdinv[u] = (float)I.dinv[u];
         bn2 += b * b;
     }
     bnorm2 = bn2;
@@ -2669,16 +2676,9 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
         if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
     }
     if (mixed) {
-        // FP32 copies of the operator coefficients and the Jacobi diagonal for
-        // the inner solves, and the tile-block inverses of -p ilu
-        for (int c = T.tid; c < G.n2; c += T.nthr) {
-            I.fN[c] = (float)I.visc_int[c];
-            I.fNab[c] = (float)I.Nab[c];
-            I.fdrag_x[c] = (float)I.drag_x[c];
-            I.fdrag_y[c] = (float)I.drag_y[c];
-        }
-        for (int u = T.tid; u < G.nu; u += T.nthr) I.fdinv[u] = (float)I.dinv[u];
-        if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
+        // the FP32 copies of the operator coefficients and the Jacobi diagonal
+        // were written by the phases that produce them; the tile-block
+        // inverses of -p ilu are built from them here
         if (I.fminv && P.ssa_solver == YGPU_SSA_ENERGY && P.lin_precond == YGPU_PRE_ILU0) {
             const StencilOp<float, float> A32{&I, &G, true, I.fN, I.fNab, I.fdrag_x, I.fdrag_y, make_opk<float>(G)};
             block_setup<float, float>(I, G, T, A32, I.fminv);
