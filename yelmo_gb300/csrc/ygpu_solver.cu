@@ -2920,7 +2920,10 @@ __global__ void __launch_bounds__(YG_KBLOCK, 1) ygpu_k_krylov(const Inst* insts,
                                                               TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
     run_step<YG_STEP_KRYLOV>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
-__global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_post(const Inst* insts, int n_inst, ygpu_dyn_par P,
+// the post step (epilogue of a Picard iteration) runs 512-thread CTAs: twice the warps
+// per SM of 256 threads, for a pass bound by load latency
+#define YG_POBLOCK 512
+__global__ void __launch_bounds__(YG_POBLOCK, 1) ygpu_k_post(const Inst* insts, int n_inst, ygpu_dyn_par P,
                                                            TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
     run_step<YG_STEP_POST>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
@@ -3233,7 +3236,7 @@ static int launch_step_raw(int step, cudaStream_t s, const StepShape& sh, const 
         case YG_STEP_KRYLOV:
             return coop((const void*)ygpu_k_krylov, sh.kgrid, YG_KBLOCK, s, d_insts, n_inst, P, ctls, sh.ktc, d_abort, d_done, sh.kmap);
         case YG_STEP_POST:
-            return coop((const void*)ygpu_k_post, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
+            return coop((const void*)ygpu_k_post, sh.grid, YG_POBLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
         case YG_STEP_FINAL:
             return coop((const void*)ygpu_k_final, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
         default:
@@ -3450,7 +3453,7 @@ int ygpu_solver_max_ctas(int device) {
     int b4 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b4, ygpu_k_pre64, YG_BLOCK, 0);
     if (b4 < bps) bps = b4;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, ygpu_k_post, YG_BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, ygpu_k_post, YG_POBLOCK, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b3, ygpu_k_setup, YG_BLOCK, 0);
     if (b2 < bps) bps = b2;
     if (b3 < bps) bps = b3;
