@@ -46,6 +46,7 @@ extern "C" {
 #define YGPU_BND_PERIODIC     4
 #define YGPU_BND_PERIODIC_X   5
 #define YGPU_BND_PERIODIC_Y   6
+#define YGPU_BND_MASK         7   /* "mask": INFINITE for the velocity solve; own border rows in advection */
 
 /* ---- ydyn.ssa_solver ("residual" | "energy"), velocity_ssa.f90:25 ---- */
 #define YGPU_SSA_RESIDUAL     0
@@ -266,6 +267,22 @@ typedef struct ygpu_dyn_diag {
 int ygpu_calc_dyn_diagnostics(const ygpu_dyn_diag* fields, int boundaries);
 /* device arrays, on `stream` (a cudaStream_t; NULL: the default stream); asynchronous */
 int ygpu_calc_dyn_diagnostics_device(void* stream, const ygpu_dyn_diag* fields, int boundaries);
+
+/*
+ * ygpu_calc_advec2D_impl_lis -- calc_advec2D with solver = "impl-lis"
+ * (src/physics/solver_advection.f90:20-145) on the GPU: the implicit upwind
+ * system of linear_solver_matrix_advection_csr_2D (:171-487), assembled on the
+ * device, solved with BiCGSTAB and Jacobi to a relative residual of 1e-12
+ * (:119), the transport of the MASK_ICE_FIXED cells (calc_fixed_cell_transport,
+ * :489-546) and dvdt = (var_new - var)/dt. mask_ice holds MASK_ICE_* (0 none,
+ * 1 fixed, 2 dynamic). boundaries is YGPU_BND_* or YGPU_BND_MASK ("mask",
+ * whose advection borders are Neumann rows). lin_iter / lin_status: the
+ * Krylov iterations and the LIS-style status (0, 2, 4; negative on error).
+ */
+int ygpu_calc_advec2D_impl_lis(double* dvdt, const double* var, const double* ux, const double* uy,
+                               const double* var_dot, const int* mask_ice, const double* var_ref,
+                               double dx, double dy, double dt, int boundaries, int nx, int ny,
+                               int* lin_iter, int* lin_status);
 
 /*
  * ygpu_linear_solver_matrix_solve -- GPU Krylov solve of a CSR system, the

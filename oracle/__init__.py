@@ -48,6 +48,9 @@ def lib():
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_calc_dyn_diagnostics.argtypes = [C.POINTER(abi.DynDiag), C.c_int]
         L.orc_calc_dyn_diagnostics.restype = C.c_int
+        L.orc_calc_advec2D_impl_lis.argtypes = [dp] * 5 + [ip, dp, C.c_double, C.c_double, C.c_double,
+                                                           C.c_int, C.c_int, C.c_int, ip, ip]
+        L.orc_calc_advec2D_impl_lis.restype = C.c_int
         _lib = L
     return _lib
 
@@ -138,6 +141,21 @@ def calc_dyn_diagnostics(arrays: dict, dx: float, dy: float, boundaries: str) ->
     if st != 0:
         raise RuntimeError(f"orc_calc_dyn_diagnostics failed ({st})")
     return arrays
+
+
+def calc_advec2D_impl_lis(var, ux, uy, var_dot, mask_ice, var_ref, dx, dy, dt, boundaries: str):
+    """orc_calc_advec2D_impl_lis: (dvdt, lin_iter, lin_status); boundaries as for
+    yelmo_gb300.gpu.calc_advec2D_impl_lis (\"mask\" has its own advection borders)."""
+    nx, ny = var.shape
+    dvdt = np.zeros((nx, ny), order="F")
+    it, st = C.c_int(0), C.c_int(0)
+    code = abi.ADV_BOUNDARY_CODES[boundaries]
+    r = lib().orc_calc_advec2D_impl_lis(abi.ptr(dvdt, "d"), abi.ptr(var, "d"), abi.ptr(ux, "d"), abi.ptr(uy, "d"),
+                                        abi.ptr(var_dot, "d"), abi.ptr(mask_ice, "i"), abi.ptr(var_ref, "d"),
+                                        dx, dy, dt, code, nx, ny, C.byref(it), C.byref(st))
+    if r < 0:
+        raise RuntimeError(f"orc_calc_advec2D_impl_lis failed ({r})")
+    return dvdt, it.value, st.value
 
 
 def linear_solve(ptr_, idx, val, b, x, method, precond, maxiter, tol, initx_zeros=False):

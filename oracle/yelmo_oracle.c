@@ -2410,3 +2410,163 @@ int orc_calc_dyn_diagnostics(const ygpu_dyn_diag* D, int bc) {
         }
     return YGPU_OK;
 }
+
+
+/* ======================================================================== */
+/* Implicit upwind advection, calc_advec2D(solver = "impl-lis")             */
+/* ======================================================================== */
+
+enum { ADV_PERIODIC = 0, ADV_ZERO = 1, ADV_INFINITE = 2, ADV_OUTFLOW = 3 };
+
+/* define_advection_bcs, solver_advection.f90:548-622 (right, upper, left, lower) */
+static void adv_kinds(int code, int k[4]) {
+    switch (code) {
+        case YGPU_BND_MISMIP3D:
+        case YGPU_BND_TROUGH: k[0] = ADV_ZERO; k[1] = ADV_PERIODIC; k[2] = ADV_INFINITE; k[3] = ADV_PERIODIC; break;
+        case YGPU_BND_INFINITE: k[0] = k[1] = k[2] = k[3] = ADV_OUTFLOW; break;
+        case YGPU_BND_MASK: k[0] = k[1] = k[2] = k[3] = ADV_INFINITE; break;
+        case YGPU_BND_PERIODIC: k[0] = k[1] = k[2] = k[3] = ADV_PERIODIC; break;
+        case YGPU_BND_PERIODIC_X: k[0] = ADV_PERIODIC; k[1] = ADV_OUTFLOW; k[2] = ADV_PERIODIC; k[3] = ADV_OUTFLOW; break;
+        case YGPU_BND_PERIODIC_Y: k[0] = ADV_OUTFLOW; k[1] = ADV_PERIODIC; k[2] = ADV_OUTFLOW; k[3] = ADV_PERIODIC; break;
+        default: k[0] = k[1] = k[2] = k[3] = ADV_ZERO; break;
+    }
+}
+
+/* calc_upwind_faces (:670-755) of all cells, after limit_border_inflow (:646-668)
+   on copies of ux, uy */
+static void adv_upwind_faces(int nx, int ny, int code, const int* k, const double* ux, const double* uy,
+                             const double* H, double* u1, double* u2, double* v1, double* v2, double* Hx1,
+                             double* Hx2, double* Hy1, double* Hy2) {
+    const size_t n = (size_t)nx * ny;
+    double* uxl = malloc(n * sizeof(double));
+    double* uyl = malloc(n * sizeof(double));
+    memcpy(uxl, ux, n * sizeof(double));
+    memcpy(uyl, uy, n * sizeof(double));
+    for (int j = 0; j < ny; j++) {
+        if (k[2] == ADV_OUTFLOW && uxl[0 + (size_t)nx * j] > 0.0) uxl[0 + (size_t)nx * j] = 0.0;
+        if (k[0] == ADV_OUTFLOW && uxl[(nx - 2) + (size_t)nx * j] < 0.0) uxl[(nx - 2) + (size_t)nx * j] = 0.0;
+    }
+    for (int i = 0; i < nx; i++) {
+        if (k[3] == ADV_OUTFLOW && uyl[i] > 0.0) uyl[i] = 0.0;
+        if (k[1] == ADV_OUTFLOW && uyl[i + (size_t)nx * (ny - 2)] < 0.0) uyl[i + (size_t)nx * (ny - 2)] = 0.0;
+    }
+    const int bc = (code == YGPU_BND_MASK) ? YGPU_BND_INFINITE : code;
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            int im1, ip1, jm1, jp1;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            const size_t c = (size_t)i + (size_t)nx * j;
+            u1[c] = uxl[im1 + (size_t)nx * j];
+            u2[c] = uxl[c];
+            v1[c] = uyl[i + (size_t)nx * jm1];
+            v2[c] = uyl[c];
+            if (i == 0 && k[2] != ADV_PERIODIC) u1[c] = 0.0;
+            if (i == nx - 1 && k[0] != ADV_PERIODIC) u2[c] = 0.0;
+            if (j == 0 && k[3] != ADV_PERIODIC) v1[c] = 0.0;
+            if (j == ny - 1 && k[1] != ADV_PERIODIC) v2[c] = 0.0;
+            Hx1[c] = (u1[c] >= 0.0) ? H[im1 + (size_t)nx * j] : H[c];
+            Hx2[c] = (u2[c] >= 0.0) ? H[c] : H[ip1 + (size_t)nx * j];
+            Hy1[c] = (v1[c] >= 0.0) ? H[i + (size_t)nx * jm1] : H[c];
+            Hy2[c] = (v2[c] >= 0.0) ? H[c] : H[i + (size_t)nx * jp1];
+        }
+    free(uxl);
+    free(uyl);
+}
+
+int orc_calc_advec2D_impl_lis(double* dvdt, const double* var, const double* ux, const double* uy,
+                              const double* F, const int* mask, const double* Href, double dx, double dy, double dt,
+                              int code, int nx, int ny, int* lin_iter, int* lin_status) {
+    if (nx < 3 || ny < 3 || !(dt > 0.0)) return YGPU_ERR_BAD_ARG;
+    const size_t n = (size_t)nx * ny;
+    int k[4];
+    adv_kinds(code, k);
+    int row_bc[4];
+    for (int q = 0; q < 4; q++) row_bc[q] = (k[q] == ADV_ZERO || k[q] == ADV_INFINITE);
+    const double dt_darea = dt / (dx * dy), WOVI = 1.0;
+    double* buf = calloc(8 * n, sizeof(double));
+    double *u1 = buf, *u2 = buf + n, *v1 = buf + 2 * n, *v2 = buf + 3 * n;
+    double *Hx1 = buf + 4 * n, *Hx2 = buf + 5 * n, *Hy1 = buf + 6 * n, *Hy2 = buf + 7 * n;
+    adv_upwind_faces(nx, ny, code, k, ux, uy, var, u1, u2, v1, v2, Hx1, Hx2, Hy1, Hy2);
+    int* ptr = malloc((n + 1) * sizeof(int));
+    int* idx = malloc(5 * n * sizeof(int));
+    double* val = calloc(5 * n, sizeof(double));
+    double* b = malloc(n * sizeof(double));
+    double* x = malloc(n * sizeof(double));
+    int kk = 0;
+    ptr[0] = 0;
+    /* rows of linear_solver_matrix_advection_csr_2D (:258-481), row r = i + nx j */
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const size_t r = (size_t)i + (size_t)nx * j;
+            const int im1 = (i == 0) ? nx - 1 : i - 1, ip1 = (i == nx - 1) ? 0 : i + 1;
+            const int jm1 = (j == 0) ? ny - 1 : j - 1, jp1 = (j == ny - 1) ? 0 : j + 1;
+            const int use_border_bc = (mask[r] != 0);
+            const double H = var[r];
+            if (mask[r] == 1) {
+                idx[kk] = (int)r; val[kk++] = 1.0;
+                b[r] = Href[r]; x[r] = Href[r];
+            } else if (use_border_bc && row_bc[0] && i == nx - 1) {
+                if (k[0] == ADV_INFINITE) {
+                    idx[kk] = (int)r; val[kk++] = 1.0;
+                    idx[kk] = im1 + nx * j; val[kk++] = -1.0;
+                    b[r] = 0.0; x[r] = H;
+                } else { idx[kk] = (int)r; val[kk++] = 1.0; b[r] = 0.0; x[r] = 0.0; }
+            } else if (use_border_bc && row_bc[1] && j == ny - 1) {
+                if (k[1] == ADV_INFINITE) {
+                    idx[kk] = (int)r; val[kk++] = 1.0;
+                    idx[kk] = i + nx * jm1; val[kk++] = -1.0;
+                    b[r] = 0.0; x[r] = H;
+                } else { idx[kk] = (int)r; val[kk++] = 1.0; b[r] = 0.0; x[r] = 0.0; }
+            } else if (use_border_bc && row_bc[2] && i == 0) {
+                if (k[2] == ADV_INFINITE) {
+                    idx[kk] = (int)r; val[kk++] = 1.0;
+                    idx[kk] = ip1 + nx * j; val[kk++] = -1.0;
+                    b[r] = 0.0; x[r] = H;
+                } else { idx[kk] = (int)r; val[kk++] = 1.0; b[r] = 0.0; x[r] = 0.0; }
+            } else if (use_border_bc && row_bc[3] && j == 0) {
+                if (k[3] == ADV_INFINITE) {
+                    idx[kk] = (int)r; val[kk++] = 1.0;
+                    idx[kk] = i + nx * jp1; val[kk++] = -1.0;
+                    b[r] = 0.0; x[r] = H;
+                } else { idx[kk] = (int)r; val[kk++] = 1.0; b[r] = 0.0; x[r] = 0.0; }
+            } else {
+                double aS = 0.0, aW = 0.0, aC = 1.0, aE = 0.0, aN = 0.0;
+                if (v1[r] > 0.0) aS = -(dt_darea * v1[r] * dx * WOVI);
+                if (u1[r] > 0.0) aW = -(dt_darea * u1[r] * dy * WOVI);
+                if (v1[r] < 0.0) aC = aC - dt_darea * v1[r] * dx * WOVI;
+                if (u1[r] < 0.0) aC = aC - dt_darea * u1[r] * dy * WOVI;
+                if (u2[r] > 0.0) aC = aC + dt_darea * u2[r] * dy * WOVI;
+                if (v2[r] > 0.0) aC = aC + dt_darea * v2[r] * dx * WOVI;
+                if (u2[r] < 0.0) aE = dt_darea * u2[r] * dy * WOVI;
+                if (v2[r] < 0.0) aN = dt_darea * v2[r] * dx * WOVI;
+                idx[kk] = i + nx * jm1; val[kk++] = aS;
+                idx[kk] = im1 + nx * j; val[kk++] = aW;
+                idx[kk] = (int)r; val[kk++] = aC;
+                idx[kk] = ip1 + nx * j; val[kk++] = aE;
+                idx[kk] = i + nx * jp1; val[kk++] = aN;
+                const double fx = u2[r] * Hx2[r] * dy - u1[r] * Hx1[r] * dy;
+                const double fy = v2[r] * Hy2[r] * dx - v1[r] * Hy1[r] * dx;
+                b[r] = H + dt * F[r] - (1.0 - WOVI) * dt_darea * (fx + fy);
+                x[r] = H;
+            }
+            ptr[r + 1] = kk;
+        }
+    int it = 0;
+    double rr = 0.0;
+    int st = orc_linear_solve((int)n, ptr, idx, val, b, x, YGPU_LIN_BICGSTAB, YGPU_PRE_JACOBI, 1000, 1e-12, 0, &it,
+                              &rr);
+    *lin_iter = it;
+    *lin_status = st;
+    /* calc_fixed_cell_transport on the solution, then dvdt */
+    int any_fixed = 0;
+    for (size_t c = 0; c < n; c++) any_fixed |= (mask[c] == 1);
+    if (any_fixed) adv_upwind_faces(nx, ny, code, k, ux, uy, x, u1, u2, v1, v2, Hx1, Hx2, Hy1, Hy2);
+    for (size_t c = 0; c < n; c++) {
+        double vn = x[c];
+        if (mask[c] == 1)
+            vn = var[c] + dt * F[c] - dt_darea * ((u2[c] * Hx2[c] - u1[c] * Hx1[c]) * dy + (v2[c] * Hy2[c] - v1[c] * Hy1[c]) * dx);
+        dvdt[c] = (vn - var[c]) / dt;
+    }
+    free(buf); free(ptr); free(idx); free(val); free(b); free(x);
+    return st < 0 ? st : YGPU_OK;
+}

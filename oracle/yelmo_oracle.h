@@ -156,6 +156,15 @@ void orc_set_threads(int n);
    f_vbvs; the same groups and NULL conventions as ygpu_calc_dyn_diagnostics. */
 int orc_calc_dyn_diagnostics(const ygpu_dyn_diag* D, int boundaries);
 
+/* calc_advec2D(solver = "impl-lis"), solver_advection.f90:20-145: the CSR system of
+   linear_solver_matrix_advection_csr_2D (:171-487) solved with this oracle's BiCGSTAB
+   and Jacobi to 1e-12, calc_fixed_cell_transport (:489-546), dvdt. Same arguments as
+   ygpu_calc_advec2D_impl_lis. */
+int orc_calc_advec2D_impl_lis(double* dvdt, const double* var, const double* ux, const double* uy,
+                              const double* var_dot, const int* mask_ice, const double* var_ref,
+                              double dx, double dy, double dt, int boundaries, int nx, int ny,
+                              int* lin_iter, int* lin_status);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,6 +21,9 @@ STATUS_NAMES = {
 }
 
 # boundary codes, yelmo_tools.f90:14-20 and boundary_code() :248-271
+# boundary strings of the advection entry: "mask" has its own code there
+ADV_BOUNDARY_CODES = {"zeros": 0, "infinite": 1, "MISMIP3D": 2, "TROUGH": 3, "periodic": 4,
+                      "periodic-x": 5, "periodic-y": 6, "mask": 7}
 BOUNDARY_CODES = {
     "zeros": 0, "infinite": 1, "mask": 1, "MISMIP3D": 2, "TROUGH": 3,
     "periodic": 4, "periodic-x": 5, "periodic-y": 6,

@@ -183,6 +183,7 @@ struct ygpu_ctx {
     double* d_miscd = nullptr;
     int max_ctas = 0;
     int csr_max_ctas = 0;
+    int adv_max_ctas = 0;
     int sms = 0;
     std::vector<Inst> h_insts;
     std::vector<InstOut> h_out;
@@ -242,6 +243,7 @@ extern "C" ygpu_ctx* ygpu_ctx_create(int device) {
     if (stack < 4096) cudaDeviceSetLimit(cudaLimitStackSize, 4096);
     c->max_ctas = ygpu_solver_max_ctas(device);
     c->csr_max_ctas = ygpu_csr_max_ctas(device);
+    c->adv_max_ctas = ygpu_adv_max_ctas(device);
     c->sms = ygpu_sm_count(device);
     return c;
 }
@@ -854,22 +856,24 @@ static void copy_segments(const std::vector<Seg>& segs) {
 }
 
 // Host staging of the host-pointer entries. The arrays are packed into one
-// pinned host buffer, in the order in-only, in/out, out-only, mirrored by the
-// device buffer: the inputs go up in one copy and the results come back in one.
+// pinned host buffer, in the order in-only, in/out, out-only, then device-only
+// scratch, mirrored by the device buffer: the inputs go up in one copy and the
+// results come back in one.
 struct Staging {
     std::vector<HostArg> args;
-    size_t up = 0, down = 0, tot = 0;   // [0, up) goes up, [down, tot) comes back
+    size_t up = 0, down = 0, dend = 0, tot = 0;   // [0, up) goes up, [down, dend) comes back; scratch after
     size_t add(void* h, size_t bytes, bool in, bool out) {
         args.push_back({h, bytes, in, out, nullptr, 0});
         return args.size() - 1;
     }
     int upload(ygpu_ctx* c) {
         size_t off = 0;
-        for (int cls = 0; cls < 3; cls++) {
+        for (int cls = 0; cls < 4; cls++) {
             if (cls == 1) down = off;
             if (cls == 2) up = off;
+            if (cls == 3) dend = off;
             for (auto& a : args) {
-                const int ac = (a.in && !a.out) ? 0 : (a.in && a.out) ? 1 : 2;
+                const int ac = (a.in && !a.out) ? 0 : (a.in && a.out) ? 1 : a.out ? 2 : 3;
                 if (ac != cls) continue;
                 a.off = off;
                 off += al(a.bytes);
@@ -878,17 +882,17 @@ struct Staging {
         tot = off;
         int st = grow(&c->fbuf, &c->fbuf_cap, tot);
         if (st) return st;
-        if (c->hbuf_cap < tot) {
+        if (c->hbuf_cap < dend) {          // the pinned mirror leaves the scratch out
             if (c->hbuf) cudaFreeHost(c->hbuf);
             c->hbuf = nullptr;
             c->hbuf_cap = 0;
-            if (cudaHostAlloc((void**)&c->hbuf, tot, cudaHostAllocDefault) != cudaSuccess) {
+            if (cudaHostAlloc((void**)&c->hbuf, dend, cudaHostAllocDefault) != cudaSuccess) {
                 cudaGetLastError();
                 c->hbuf = nullptr;
-                ygpu_set_error("pinned host allocation of %zu bytes failed", tot);
+                ygpu_set_error("pinned host allocation of %zu bytes failed", dend);
                 return YGPU_ERR_NOMEM;
             }
-            c->hbuf_cap = tot;
+            c->hbuf_cap = dend;
         }
         std::vector<Seg> segs;
         for (auto& a : args) {
@@ -900,7 +904,7 @@ struct Staging {
         return YGPU_OK;
     }
     int download(ygpu_ctx* c) {
-        if (tot > down) CK(cudaMemcpyAsync(c->hbuf + down, c->fbuf + down, tot - down, cudaMemcpyDeviceToHost, c->stream));
+        if (dend > down) CK(cudaMemcpyAsync(c->hbuf + down, c->fbuf + down, dend - down, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         std::vector<Seg> segs;
         for (auto& a : args)
@@ -1247,6 +1251,48 @@ extern "C" int ygpu_calc_dyn_diagnostics(const ygpu_dyn_diag* H, int boundaries)
     for (auto& m : map) *m.second = S.args[m.first].dev;
     if ((st = ygpu_dyn_diagnostics_device(c->stream, D, boundaries))) return st;
     return S.download(c);
+}
+
+extern "C" int ygpu_calc_advec2D_impl_lis(double* dvdt, const double* var, const double* ux, const double* uy,
+                                          const double* var_dot, const int* mask_ice, const double* var_ref,
+                                          double dx, double dy, double dt, int boundaries, int nx, int ny,
+                                          int* lin_iter, int* lin_status) {
+    if (nx < 3 || ny < 3 || !(dx > 0.0) || !(dy > 0.0) || !(dt > 0.0) || boundaries < 0 || boundaries > 7 ||
+        (size_t)nx * ny > (size_t)(1 << 28) ||
+        any_null({dvdt, var, ux, uy, var_dot, mask_ice, var_ref, lin_iter, lin_status})) {
+        ygpu_set_error("bad arguments");
+        return YGPU_ERR_BAD_ARG;
+    }
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const size_t n = (size_t)nx * ny, b2 = n * 8;
+    Staging S;
+    size_t a_v = S.add((void*)var, b2, 1, 0), a_ux = S.add((void*)ux, b2, 1, 0), a_uy = S.add((void*)uy, b2, 1, 0);
+    size_t a_f = S.add((void*)var_dot, b2, 1, 0), a_m = S.add((void*)mask_ice, n * 4, 1, 0);
+    size_t a_r = S.add((void*)var_ref, b2, 1, 0), a_d = S.add(dvdt, b2, 0, 1);
+    size_t a_w = S.add(nullptr, b2 * 16, 0, 0);
+    if (c->ctl_cap < 1) {
+        CK(cudaMalloc((void**)&c->d_ctl, sizeof(TeamCtl)));
+        c->ctl_cap = 1;
+    }
+    int st = S.upload(c);
+    if (st) return st;
+    int nct = (int)((n + 2 * YG_BLOCK - 1) / (2 * YG_BLOCK));
+    if (nct > c->adv_max_ctas) nct = c->adv_max_ctas;
+    if (nct > YG_MAX_TEAM_CTAS) nct = YG_MAX_TEAM_CTAS;
+    if (nct < 1) nct = 1;
+    auto d = [&](size_t k) { return (double*)S.args[k].dev; };
+    st = ygpu_launch_advect(c->stream, nx, ny, boundaries, dx, dy, dt, d(a_v), d(a_ux), d(a_uy), d(a_f), d(a_r),
+                            (const int*)S.args[a_m].dev, d(a_d), d(a_w), c->d_misc + 2, c->d_miscd, c->d_ctl,
+                            c->d_misc + 1, nct);
+    if (st) return st;
+    int outi[2];
+    CK(cudaMemcpyAsync(outi, c->d_misc + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    st = S.download(c);
+    if (st) return st;
+    *lin_iter = outi[0];
+    *lin_status = outi[1];
+    return outi[1] < 0 ? outi[1] : YGPU_OK;
 }
 
 extern "C" int ygpu_linear_solver_matrix_solve(int nmax, const int* a_ptr, const int* a_index, const double* a_value,

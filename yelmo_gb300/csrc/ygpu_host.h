@@ -94,6 +94,11 @@ int ygpu_launch_csr(cudaStream_t stream, int n, const int* ptr, const int* idx, 
                     double* x, double* work, int method, int precond, int maxiter, double tol, int initx_zeros,
                     int* d_out_i, double* d_out_d, TeamCtl* d_ctl, int* d_abort, int n_ctas);
 int ygpu_csr_max_ctas(int device);
+int ygpu_adv_max_ctas(int device);
+int ygpu_launch_advect(cudaStream_t stream, int nx, int ny, int code, double dx, double dy, double dt,
+                       const double* var, const double* ux, const double* uy, const double* F, const double* Href,
+                       const int* mask, double* dvdt, double* work, int* d_out_i, double* d_out_d, TeamCtl* d_ctl,
+                       int* d_abort, int n_ctas);
 int ygpu_dyn_inputs_device(cudaStream_t s, const double* H, const double* zb, const double* zsl, double* f_ice,
                            double* H_grnd, double* z_srf, double* f_grnd, double* fgx, double* fgy, int* mf,
                            double* dzsdx, double* dzsdy, double* tdx, double* tdy, double* tlx, double* tly,

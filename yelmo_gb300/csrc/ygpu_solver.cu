@@ -3023,6 +3023,255 @@ int ygpu_launch_csr(cudaStream_t stream, int n, const int* ptr, const int* idx, 
     return YGPU_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Implicit upwind advection: calc_advec2D(solver = "impl-lis")
+// (solver_advection.f90:20-145): the system of
+// linear_solver_matrix_advection_csr_2D (:171-487), solved with BiCGSTAB and
+// Jacobi to 1e-12 (the option string of :119), then the transport of the
+// prescribed cells (calc_fixed_cell_transport, :489-546) and dvdt.
+// ---------------------------------------------------------------------------
+enum { ADV_PERIODIC = 0, ADV_ZERO = 1, ADV_INFINITE = 2, ADV_OUTFLOW = 3 };
+#define YG_MASK_ICE_NONE 0
+#define YG_MASK_ICE_FIXED 1
+
+// define_advection_bcs (:548-622): kinds of the right, upper, left, lower borders
+YG_DEV void adv_border_kinds(int code, int k[4]) {
+    switch (code) {
+        case YGPU_BND_MISMIP3D:
+        case YGPU_BND_TROUGH: k[0] = ADV_ZERO; k[1] = ADV_PERIODIC; k[2] = ADV_INFINITE; k[3] = ADV_PERIODIC; break;
+        case YGPU_BND_INFINITE: k[0] = k[1] = k[2] = k[3] = ADV_OUTFLOW; break;
+        case YGPU_BND_MASK: k[0] = k[1] = k[2] = k[3] = ADV_INFINITE; break;
+        case YGPU_BND_PERIODIC: k[0] = k[1] = k[2] = k[3] = ADV_PERIODIC; break;
+        case YGPU_BND_PERIODIC_X: k[0] = ADV_PERIODIC; k[1] = ADV_OUTFLOW; k[2] = ADV_PERIODIC; k[3] = ADV_OUTFLOW; break;
+        case YGPU_BND_PERIODIC_Y: k[0] = ADV_OUTFLOW; k[1] = ADV_PERIODIC; k[2] = ADV_OUTFLOW; k[3] = ADV_PERIODIC; break;
+        default: k[0] = k[1] = k[2] = k[3] = ADV_ZERO; break;
+    }
+}
+
+struct AdvJob {
+    int nx, ny, code;                  // YGPU_BND_* or YGPU_BND_MASK
+    double dx, dy, dt;
+    const double *var, *ux, *uy, *F, *Href;
+    const int* mask;
+    double* dvdt;
+    double *c, *x, *b, *dinv, *r, *rt, *p, *v, *s, *t, *ph, *sh;   // c: 5 per row
+    int* out_iters;
+    int* out_status;
+    double* out_relres;
+};
+
+// Face velocities of cell (i, j) after limit_border_inflow (:646-668): no flow
+// from an "outflow" border cell into its inner neighbour
+struct AdvFaces {
+    double ux1, ux2, uy1, uy2;
+};
+YG_DEV double adv_ux(const AdvJob& J, const int* k, int i, int j) {
+    double u = J.ux[i + J.nx * j];
+    if (k[2] == ADV_OUTFLOW && i == 0 && u > 0.0) u = 0.0;
+    if (k[0] == ADV_OUTFLOW && i == J.nx - 2 && u < 0.0) u = 0.0;
+    return u;
+}
+YG_DEV double adv_uy(const AdvJob& J, const int* k, int i, int j) {
+    double u = J.uy[i + J.nx * j];
+    if (k[3] == ADV_OUTFLOW && j == 0 && u > 0.0) u = 0.0;
+    if (k[1] == ADV_OUTFLOW && j == J.ny - 2 && u < 0.0) u = 0.0;
+    return u;
+}
+// calc_upwind_faces (:670-755) for cell (i, j): the velocities of its four
+// faces (1: left/bottom, 2: right/top) and the upstream values of H there
+YG_DEV AdvFaces adv_faces(const AdvJob& J, const int* k, int i, int j, const double* H, double Hf[4]) {
+    const int nx = J.nx, ny = J.ny;
+    const int bc = (J.code == YGPU_BND_MASK) ? YGPU_BND_INFINITE : J.code;
+    int im1, ip1, jm1, jp1;
+    nbr_bc(i, j, nx, ny, bc, im1, ip1, jm1, jp1);
+    AdvFaces f;
+    f.ux1 = adv_ux(J, k, im1, j);
+    f.ux2 = adv_ux(J, k, i, j);
+    f.uy1 = adv_uy(J, k, i, jm1);
+    f.uy2 = adv_uy(J, k, i, j);
+    if (i == 0 && k[2] != ADV_PERIODIC) f.ux1 = 0.0;
+    if (i == nx - 1 && k[0] != ADV_PERIODIC) f.ux2 = 0.0;
+    if (j == 0 && k[3] != ADV_PERIODIC) f.uy1 = 0.0;
+    if (j == ny - 1 && k[1] != ADV_PERIODIC) f.uy2 = 0.0;
+    const int c = i + nx * j;
+    Hf[0] = (f.ux1 >= 0.0) ? H[im1 + nx * j] : H[c];
+    Hf[1] = (f.ux2 >= 0.0) ? H[c] : H[ip1 + nx * j];
+    Hf[2] = (f.uy1 >= 0.0) ? H[i + nx * jm1] : H[c];
+    Hf[3] = (f.uy2 >= 0.0) ? H[c] : H[i + nx * jp1];
+    return f;
+}
+
+// The advection matrix: five coefficients per row in the slot order of the
+// assembly, S (i,j-1), W (i-1,j), C, E (i+1,j), N (i,j+1), with columns wrapped
+// periodically as there (border rows only use in-range columns)
+struct Adv5Op {
+    int nx, ny, n;
+    const double* c;
+    const int* acell = nullptr;        // every row
+    YG_DEV int n2() const { return n; }
+    YG_DEV double row(int r, const double* v) const {
+        const int i = r % nx, j = r / nx;
+        const int im1 = (i == 0) ? nx - 1 : i - 1, ip1 = (i == nx - 1) ? 0 : i + 1;
+        const int jm1 = (j == 0) ? ny - 1 : j - 1, jp1 = (j == ny - 1) ? 0 : j + 1;
+        const double* a = c + 5 * (size_t)r;
+        double y = a[0] * v[i + nx * jm1];
+        y = y + a[1] * v[im1 + nx * j];
+        y = y + a[2] * v[r];
+        y = y + a[3] * v[ip1 + nx * j];
+        y = y + a[4] * v[i + nx * jp1];
+        return y;
+    }
+    YG_DEV void operator()(Team& Tm, const double* v, double* y) const {
+        for (int r = Tm.tid; r < n; r += Tm.nthr) y[r] = row(r, v);
+    }
+    YG_DEV void apply(Team& Tm, const double* v, double* y, const RowItems& R) const {
+        int q = 0;
+        for (int t = Tm.tid; t < R.nitem; t += Tm.nthr, q++) {
+            const int k = R.row(t, q);
+            y[k] = row(k, v);
+        }
+    }
+};
+
+__global__ void __launch_bounds__(YG_BLOCK) ygpu_adv_kernel(AdvJob J, TeamCtl* ctl, int* abort_all) {
+    Team T;
+    T.ncta = gridDim.x;
+    T.cta = blockIdx.x;
+    T.tid = blockIdx.x * blockDim.x + threadIdx.x;
+    T.nthr = gridDim.x * blockDim.x;
+    T.ctl = ctl;
+    T.parity = 0;
+    T.abort_all = abort_all;
+    T.sync_ns = 0.0;
+    T.gen = 0u;
+    const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+    const int nx = J.nx, ny = J.ny, n = nx * ny;
+    int k[4];
+    adv_border_kinds(J.code, k);
+    const bool row_bc[4] = {k[0] == ADV_ZERO || k[0] == ADV_INFINITE, k[1] == ADV_ZERO || k[1] == ADV_INFINITE,
+                            k[2] == ADV_ZERO || k[2] == ADV_INFINITE, k[3] == ADV_ZERO || k[3] == ADV_INFINITE};
+    const double dt_darea = J.dt / (J.dx * J.dy);
+    const double WOVI = 1.0;
+    // rows of linear_solver_matrix_advection_csr_2D (:258-481)
+    double bn = 0.0;
+    for (int r = T.tid; r < n; r += T.nthr) {
+        const int i = r % nx, j = r / nx;
+        double a[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        double b, x0;
+        const int m = J.mask[r];
+        const bool use_border_bc = (m != YG_MASK_ICE_NONE);
+        const double H = J.var[r];
+        if (m == YG_MASK_ICE_FIXED) {
+            a[2] = 1.0;
+            b = J.Href[r];
+            x0 = J.Href[r];
+        } else if (use_border_bc && row_bc[0] && i == nx - 1) {          // right
+            a[2] = 1.0;
+            if (k[0] == ADV_INFINITE) { a[1] = -1.0; b = 0.0; x0 = H; } else { b = 0.0; x0 = 0.0; }
+        } else if (use_border_bc && row_bc[1] && j == ny - 1) {          // top
+            a[2] = 1.0;
+            if (k[1] == ADV_INFINITE) { a[0] = -1.0; b = 0.0; x0 = H; } else { b = 0.0; x0 = 0.0; }
+        } else if (use_border_bc && row_bc[2] && i == 0) {               // left
+            a[2] = 1.0;
+            if (k[2] == ADV_INFINITE) { a[3] = -1.0; b = 0.0; x0 = H; } else { b = 0.0; x0 = 0.0; }
+        } else if (use_border_bc && row_bc[3] && j == 0) {               // bottom
+            a[2] = 1.0;
+            if (k[3] == ADV_INFINITE) { a[4] = -1.0; b = 0.0; x0 = H; } else { b = 0.0; x0 = 0.0; }
+        } else {                                                          // inner point
+            double Hf[4];
+            const AdvFaces f = adv_faces(J, k, i, j, J.var, Hf);
+            if (f.uy1 > 0.0) a[0] = -(dt_darea * f.uy1 * J.dx * WOVI);
+            if (f.ux1 > 0.0) a[1] = -(dt_darea * f.ux1 * J.dy * WOVI);
+            a[2] = 1.0;
+            if (f.uy1 < 0.0) a[2] = a[2] - dt_darea * f.uy1 * J.dx * WOVI;
+            if (f.ux1 < 0.0) a[2] = a[2] - dt_darea * f.ux1 * J.dy * WOVI;
+            if (f.ux2 > 0.0) a[2] = a[2] + dt_darea * f.ux2 * J.dy * WOVI;
+            if (f.uy2 > 0.0) a[2] = a[2] + dt_darea * f.uy2 * J.dx * WOVI;
+            if (f.ux2 < 0.0) a[3] = dt_darea * f.ux2 * J.dy * WOVI;
+            if (f.uy2 < 0.0) a[4] = dt_darea * f.uy2 * J.dx * WOVI;
+            const double fx = f.ux2 * Hf[1] * J.dy - f.ux1 * Hf[0] * J.dy;
+            const double fy = f.uy2 * Hf[3] * J.dx - f.uy1 * Hf[2] * J.dx;
+            b = H + J.dt * J.F[r] - (1.0 - WOVI) * dt_darea * (fx + fy);
+            x0 = H;
+        }
+        for (int q = 0; q < 5; q++) J.c[5 * (size_t)r + q] = a[q];
+        J.b[r] = b;
+        J.x[r] = x0;
+        J.dinv[r] = (a[2] != 0.0) ? 1.0 / a[2] : 1.0;
+        bn += b * b;
+    }
+    if (!team_allreduce(T, &bn, 1)) {
+        if (lead) { *J.out_status = YGPU_ERR_TIMEOUT; *J.out_iters = 0; *J.out_relres = 0.0; }
+        return;
+    }
+    int iters = 0, status = YGPU_OK;
+    double relres = 0.0;
+    bool ok = true;
+    if (bn == 0.0) {
+        // homogeneous system: x = 0 (solver_linear.F90:162-174)
+        for (int r = T.tid; r < n; r += T.nthr) J.x[r] = 0.0;
+    } else {
+        const Adv5Op A{nx, ny, n, J.c};
+        status = krylov_bicgstab<double>(T, n, A, J.dinv, J.x, J.b, J.r, J.rt, J.p, J.v, J.s, J.t, J.ph, J.sh, 1000,
+                                         1e-12, sqrt(bn), true, iters, relres, ok);
+        if (!ok) status = YGPU_ERR_TIMEOUT;
+    }
+    if (!team_barrier(T)) status = YGPU_ERR_TIMEOUT;
+    // linear_solver_save_advection, calc_fixed_cell_transport on the solution, dvdt
+    for (int r = T.tid; r < n; r += T.nthr) {
+        double vn = J.x[r];
+        if (J.mask[r] == YG_MASK_ICE_FIXED) {
+            const int i = r % nx, j = r / nx;
+            double Hf[4];
+            const AdvFaces f = adv_faces(J, k, i, j, J.x, Hf);
+            vn = J.var[r] + J.dt * J.F[r] -
+                 dt_darea * ((f.ux2 * Hf[1] - f.ux1 * Hf[0]) * J.dy + (f.uy2 * Hf[3] - f.uy1 * Hf[2]) * J.dx);
+        }
+        J.dvdt[r] = (vn - J.var[r]) / J.dt;
+    }
+    if (lead) {
+        *J.out_iters = iters;
+        *J.out_status = status;
+        *J.out_relres = relres;
+    }
+}
+
+int ygpu_adv_max_ctas(int device) {
+    int nsm = 0, bps = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ygpu_adv_kernel, YG_BLOCK, 0);
+    return nsm * bps;
+}
+
+// work: 16 n doubles of device scratch
+int ygpu_launch_advect(cudaStream_t stream, int nx, int ny, int code, double dx, double dy, double dt,
+                       const double* var, const double* ux, const double* uy, const double* F, const double* Href,
+                       const int* mask, double* dvdt, double* work, int* d_out_i, double* d_out_d, TeamCtl* d_ctl,
+                       int* d_abort, int n_ctas) {
+    AdvJob J;
+    J.nx = nx; J.ny = ny; J.code = code; J.dx = dx; J.dy = dy; J.dt = dt;
+    J.var = var; J.ux = ux; J.uy = uy; J.F = F; J.Href = Href; J.mask = mask; J.dvdt = dvdt;
+    const size_t n = (size_t)nx * ny;
+    J.c = work;
+    double* w = work + 5 * n;
+    double** slots[11] = {&J.x, &J.b, &J.dinv, &J.r, &J.rt, &J.p, &J.v, &J.s, &J.t, &J.ph, &J.sh};
+    for (int q = 0; q < 11; q++) *slots[q] = w + (size_t)q * n;
+    J.out_iters = d_out_i;
+    J.out_status = d_out_i + 1;
+    J.out_relres = d_out_d;
+    if (cudaMemsetAsync(d_abort, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    if (cudaMemsetAsync(d_ctl, 0, sizeof(TeamCtl), stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    void* args[] = {(void*)&J, (void*)&d_ctl, (void*)&d_abort};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)ygpu_adv_kernel, dim3(n_ctas), dim3(YG_BLOCK), args, 0,
+                                                stream);
+    if (e != cudaSuccess) {
+        ygpu_set_error("cooperative launch of the advection solve failed: %s", cudaGetErrorString(e));
+        return YGPU_ERR_CUDA;
+    }
+    ygpu_count_launches(1);
+    return YGPU_OK;
+}
+
 int ygpu_csr_max_ctas(int device) {
     int nsm = 0, bps = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);

@@ -39,7 +39,7 @@ EXPORTS = [
     "ygpu_server_poll", "ygpu_server_wait", "ygpu_server_fetch", "ygpu_server_get_info",
     "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get", "ygpu_tuning_defaults",
     "ygpu_ctx_set_tuning", "ygpu_set_neff_hook", "ygpu_solve_batch_host", "ygpu_calc_dyn_diagnostics",
-    "ygpu_calc_dyn_diagnostics_device",
+    "ygpu_calc_dyn_diagnostics_device", "ygpu_calc_advec2D_impl_lis",
 ]
 
 
@@ -85,6 +85,8 @@ def lib(build_if_missing: bool = True):
     L.ygpu_solve_device_noalloc.argtypes = [C.c_int, C.POINTER(abi.DynPar), C.POINTER(abi.Fields),
                                             C.POINTER(abi.Stats), C.c_void_p]
     ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
+    L.ygpu_calc_advec2D_impl_lis.argtypes = [dp] * 5 + [ip, dp, C.c_double, C.c_double, C.c_double,
+                                                        C.c_int, C.c_int, C.c_int, ip, ip]
     L.ygpu_linear_solver_matrix_solve.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_char_p, ip, ip, dp]
     L.ygpu_server_create.restype = C.c_void_p
     L.ygpu_server_create.argtypes = [C.POINTER(abi.ServerCfg)]
@@ -205,6 +207,22 @@ def calc_dyn_diagnostics(arrays: dict, dx: float, dy: float, boundaries: str) ->
     D = abi.dyn_diag(arrays, nx, ny, nz, dx, dy)
     _check(lib().ygpu_calc_dyn_diagnostics(C.byref(D), abi.BOUNDARY_CODES[boundaries]))
     return arrays
+
+
+def calc_advec2D_impl_lis(var, ux, uy, var_dot, mask_ice, var_ref, dx: float, dy: float, dt: float,
+                          boundaries: str):
+    """calc_advec2D(solver = "impl-lis") on the GPU (ygpu_calc_advec2D_impl_lis):
+    returns (dvdt, lin_iter, lin_status). mask_ice: int32 MASK_ICE_* (0 none,
+    1 fixed, 2 dynamic)."""
+    nx, ny = var.shape
+    dvdt = np.zeros((nx, ny), order="F")
+    it, st = C.c_int(0), C.c_int(0)
+    r = lib().ygpu_calc_advec2D_impl_lis(abi.ptr(dvdt, "d"), abi.ptr(var, "d"), abi.ptr(ux, "d"), abi.ptr(uy, "d"),
+                                         abi.ptr(var_dot, "d"), abi.ptr(mask_ice, "i"), abi.ptr(var_ref, "d"),
+                                         dx, dy, dt, abi.ADV_BOUNDARY_CODES[boundaries], nx, ny,
+                                         C.byref(it), C.byref(st))
+    _check(r)
+    return dvdt, it.value, st.value
 
 
 def calc_dyn_inputs(inst) -> dict:
