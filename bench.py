@@ -252,6 +252,54 @@ def diagnostics_leg(device: str, steps: int, warmup: int) -> dict:
             "alg_bytes_per_call": alg, "achieved_gbs": alg / (ms / 1e3) / 1e9, "kernels": 2}
 
 
+def advection_leg(device: str, steps: int, warmup: int) -> dict:
+    """Time calc_advec2D(impl-lis) on the device (ygpu_advec2D_impl_lis_device)
+    on a 801 x 801 grid resident in HBM: seeded thickness, velocities and source,
+    every cell dynamic, dt = 1 a. Algorithmic bytes per cell: assembly 108 B
+    (6 inputs, 5 coefficients, b, x, the Jacobi diagonal), per BiCGSTAB
+    iteration 224 B (two 5-point applies of 56 B and 14 vector streams of 8 B),
+    and 36 B for the update and dvdt."""
+    import ctypes as C
+    import torch
+    from yelmo_gb300 import gpu
+    nx = ny = 801
+    gen = torch.Generator(device=device).manual_seed(11)
+    n = nx * ny
+    r = lambda s: torch.randn(n, dtype=torch.float64, device=device, generator=gen) * s
+    H = r(300.0).abs()
+    ux, uy, F = r(150.0), r(150.0), r(0.5)
+    mask = torch.full((n,), 2, dtype=torch.int32, device=device)
+    dvdt = torch.zeros(n, dtype=torch.float64, device=device)
+    solver = gpu.DeviceSolver(int(device.split(":")[1]))
+    L = gpu.lib()
+    it, st = C.c_int(0), C.c_int(0)
+    times, iters = [], []
+    try:
+        # CUDA events on the context's stream, around the solve's launches
+        ts = torch.cuda.ExternalStream(L.ygpu_ctx_stream(solver.ctx), device=device)
+        for s in range(warmup + steps):
+            torch.cuda.synchronize(device)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ts)
+            rc = L.ygpu_advec2D_impl_lis_device(solver.ctx, dvdt.data_ptr(), H.data_ptr(), ux.data_ptr(), uy.data_ptr(),
+                                                F.data_ptr(), mask.data_ptr(), H.data_ptr(), 4e3, 4e3, 1.0, 0, nx, ny,
+                                                C.byref(it), C.byref(st))
+            e1.record(ts)
+            torch.cuda.synchronize(device)
+            if rc != 0:
+                raise RuntimeError(f"advection failed ({rc}): {gpu.last_error()}")
+            if s >= warmup:
+                times.append(e0.elapsed_time(e1))
+                iters.append(it.value)
+    finally:
+        solver.close()
+    ms = statistics.mean(times)
+    alg = float(n) * (108 + statistics.mean(iters) * 224 + 36)
+    return {"workload": "801x801 implicit upwind step, BiCGSTAB + Jacobi to 1e-12", "ms_per_call": ms,
+            "bicgstab_iters": statistics.mean(iters), "alg_bytes_per_call": alg,
+            "achieved_gbs": alg / (ms / 1e3) / 1e9, "status": st.value}
+
+
 def run_reference(args, insts, rank, world):
     """CPU reference arm: the oracle (FP64 restatement of the reference path) on all host cores."""
     if rank != 0:
@@ -534,6 +582,7 @@ def main():
             if s >= args.warmup:
                 e2e1_times.append(dt)
     diag = diagnostics_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
+    adv = advection_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
     i0 = insts[0]
     io = [gpu.host_io_bytes(kind, i.nx, i.ny, i.nz) for i in insts]
     h2d, d2h = sum(a for a, _ in io), sum(b for _, b in io)
@@ -613,6 +662,7 @@ def main():
         "phase_ms_single": mixed["st1"]["phase_ms"] if mixed["st1"] else None,
         "clocks": clocks,
         "diagnostics": (dict(diag, frac=diag["achieved_gbs"] / peak) if diag else None),
+        "advection": (dict(adv, frac=adv["achieved_gbs"] / peak) if adv else None),
         "cpu_baseline": cpu_base,
     }
     print(json.dumps(line))

@@ -283,6 +283,12 @@ int ygpu_calc_advec2D_impl_lis(double* dvdt, const double* var, const double* ux
                                const double* var_dot, const int* mask_ice, const double* var_ref,
                                double dx, double dy, double dt, int boundaries, int nx, int ny,
                                int* lin_iter, int* lin_status);
+struct ygpu_ctx;
+/* the same on device arrays, on ctx's stream (scratch from its arena); synchronises */
+int ygpu_advec2D_impl_lis_device(struct ygpu_ctx* ctx, double* dvdt, const double* var, const double* ux,
+                                 const double* uy, const double* var_dot, const int* mask_ice,
+                                 const double* var_ref, double dx, double dy, double dt, int boundaries,
+                                 int nx, int ny, int* lin_iter, int* lin_status);
 
 /*
  * ygpu_linear_solver_matrix_solve -- GPU Krylov solve of a CSR system, the

@@ -172,3 +172,25 @@ def test_gpu_matches_oracle(bc):
     err = np.linalg.norm(d_g - d_o) / np.linalg.norm(d_o)
     assert err <= 1e-9, err
     assert abs(it_g - it_o) <= max(2, it_o // 5), (it_g, it_o)
+
+
+@pytest.mark.gpu
+def test_gpu_device_entry_equals_host_entry():
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    H, ux, uy, F, mask, Href = _fields(nx=40, ny=33, seed=9)
+    d_h, it_h, st_h = gpu.calc_advec2D_impl_lis(H, ux, uy, F, mask, Href, 8e3, 8e3, 3.0, "periodic-x")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a.ravel(order="F"))).cuda()
+    dH, dux, duy, dF, dm, dR = t(H), t(ux), t(uy), t(F), t(mask), t(Href)
+    out = torch.zeros_like(dH)
+    solver = gpu.DeviceSolver(0)
+    it, st = C.c_int(0), C.c_int(0)
+    try:
+        torch.cuda.synchronize()
+        rc = gpu.lib().ygpu_advec2D_impl_lis_device(solver.ctx, out.data_ptr(), dH.data_ptr(), dux.data_ptr(),
+                                                    duy.data_ptr(), dF.data_ptr(), dm.data_ptr(), dR.data_ptr(),
+                                                    8e3, 8e3, 3.0, 5, 40, 33, C.byref(it), C.byref(st))
+    finally:
+        solver.close()
+    assert rc == 0 and st.value == st_h == 0 and it.value == it_h
+    np.testing.assert_array_equal(out.cpu().numpy().reshape((40, 33), order="F"), d_h)

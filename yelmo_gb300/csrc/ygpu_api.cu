@@ -1295,6 +1295,41 @@ extern "C" int ygpu_calc_advec2D_impl_lis(double* dvdt, const double* var, const
     return outi[1] < 0 ? outi[1] : YGPU_OK;
 }
 
+// device arrays on a context's stream; scratch from the context's arena;
+// synchronises to return the iteration count and status
+extern "C" int ygpu_advec2D_impl_lis_device(ygpu_ctx* c, double* dvdt, const double* var, const double* ux,
+                                            const double* uy, const double* var_dot, const int* mask_ice,
+                                            const double* var_ref, double dx, double dy, double dt, int boundaries,
+                                            int nx, int ny, int* lin_iter, int* lin_status) {
+    if (!c || nx < 3 || ny < 3 || !(dx > 0.0) || !(dy > 0.0) || !(dt > 0.0) || boundaries < 0 || boundaries > 7 ||
+        (size_t)nx * ny > (size_t)(1 << 28) ||
+        any_null({dvdt, var, ux, uy, var_dot, mask_ice, var_ref, lin_iter, lin_status})) {
+        ygpu_set_error("bad arguments");
+        return YGPU_ERR_BAD_ARG;
+    }
+    CK(cudaSetDevice(c->device));
+    const size_t n = (size_t)nx * ny;
+    int st = grow(&c->arena, &c->arena_cap, n * 8 * 16);
+    if (st) return st;
+    if (c->ctl_cap < 1) {
+        CK(cudaMalloc((void**)&c->d_ctl, sizeof(TeamCtl)));
+        c->ctl_cap = 1;
+    }
+    int nct = (int)((n + 2 * YG_BLOCK - 1) / (2 * YG_BLOCK));
+    if (nct > c->adv_max_ctas) nct = c->adv_max_ctas;
+    if (nct > YG_MAX_TEAM_CTAS) nct = YG_MAX_TEAM_CTAS;
+    if (nct < 1) nct = 1;
+    st = ygpu_launch_advect(c->stream, nx, ny, boundaries, dx, dy, dt, var, ux, uy, var_dot, var_ref, mask_ice, dvdt,
+                            (double*)c->arena, c->d_misc + 2, c->d_miscd, c->d_ctl, c->d_misc + 1, nct);
+    if (st) return st;
+    int outi[2];
+    CK(cudaMemcpyAsync(outi, c->d_misc + 2, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *lin_iter = outi[0];
+    *lin_status = outi[1];
+    return outi[1] < 0 ? outi[1] : YGPU_OK;
+}
+
 extern "C" int ygpu_linear_solver_matrix_solve(int nmax, const int* a_ptr, const int* a_index, const double* a_value,
                                                const double* b_value, double* x_value, const char* lis_opt,
                                                int* lin_iter, int* status, double* L2_rel_norm) {

@@ -39,7 +39,7 @@ EXPORTS = [
     "ygpu_server_poll", "ygpu_server_wait", "ygpu_server_fetch", "ygpu_server_get_info",
     "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get", "ygpu_tuning_defaults",
     "ygpu_ctx_set_tuning", "ygpu_set_neff_hook", "ygpu_solve_batch_host", "ygpu_calc_dyn_diagnostics",
-    "ygpu_calc_dyn_diagnostics_device", "ygpu_calc_advec2D_impl_lis",
+    "ygpu_calc_dyn_diagnostics_device", "ygpu_calc_advec2D_impl_lis", "ygpu_advec2D_impl_lis_device",
 ]
 
 
@@ -87,6 +87,8 @@ def lib(build_if_missing: bool = True):
     ip, dp = C.POINTER(C.c_int), C.POINTER(C.c_double)
     L.ygpu_calc_advec2D_impl_lis.argtypes = [dp] * 5 + [ip, dp, C.c_double, C.c_double, C.c_double,
                                                         C.c_int, C.c_int, C.c_int, ip, ip]
+    L.ygpu_advec2D_impl_lis_device.argtypes = [C.c_void_p] + [C.c_void_p] * 7 + [C.c_double, C.c_double, C.c_double,
+                                                                              C.c_int, C.c_int, C.c_int, ip, ip]
     L.ygpu_linear_solver_matrix_solve.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_char_p, ip, ip, dp]
     L.ygpu_server_create.restype = C.c_void_p
     L.ygpu_server_create.argtypes = [C.POINTER(abi.ServerCfg)]
