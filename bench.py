@@ -350,6 +350,11 @@ def cpu_baseline_leg(inst, budget_s=20.0):
     times, sample, f0 = _cpu_sample(inst, oracle, budget_s=budget_s)
     base = {"value": len(times) / sum(times), "unit": "solves/s", "cores": cores, "kind": "port",
             "sample": f"{sample} (oracle: C FP64 restatement, OpenMP, {cores} threads)"}
+    # the same on one thread (one solve, or the two-iteration sample of large grids)
+    oracle.set_threads(1)
+    t1, sample1, _ = _cpu_sample(inst, oracle, n_max=1, budget_s=0.0)
+    oracle.set_threads(cores)
+    base["one_thread"] = {"value": len(t1) / sum(t1), "unit": "solves/s", "sample": sample1}
     if inst.nx * inst.ny > LARGE_CELLS:
         return base, None
     tight = _copy(f0)
