@@ -405,8 +405,9 @@ def algorithmic_bytes(stats: dict, kind: int, nx: int, ny: int, nz: int, mixed: 
       N, N_ab, two drag arrays, the row flags, the preconditioner and eight
       recurrence vectors; write the eight vectors and the next operator
       input), BiCGSTAB iteration 62w+16 (two operator applies of 8w+8 and
-      46w of vector passes); mixed mode, per cell: each FP64 defect-correction
-      step 186 B (FP64 operator 66, residual 48, conversions 32, update 40);
+      46w of vector passes); mixed mode, per active cell: each FP64
+      defect-correction step 186 B (FP64 operator 66, residual 48,
+      conversions 32, update 40);
     - mixed mode, pre step: the FP32 coefficient copies, 72 B per cell and
       Picard iteration;
     - post step, per Picard iteration: epilogue 16w+8.
@@ -424,7 +425,7 @@ def algorithmic_bytes(stats: dict, kind: int, nx: int, ny: int, nz: int, mixed: 
     n_act = stats.get("active_cells") or n2
     krylov = float(n_act) * lin * it_bytes
     if mixed:
-        krylov += float(n2) * stats.get("outer_iter", 0) * 186
+        krylov += float(n_act) * stats.get("outer_iter", 0) * 186
         pre += 72
     steps = {"pre": float(n2) * picard * pre, "krylov": krylov, "post": float(n2) * picard * post}
     return steps if by_step else sum(steps.values())
