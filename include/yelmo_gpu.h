@@ -391,7 +391,9 @@ int ygpu_solve_batch_device(ygpu_ctx* ctx, int kind, const ygpu_dyn_par* par,
  * n ygpu_fields of host pointers with the layouts and directions of
  * ygpu_calc_velocity_ssa / _diva; the library copies them to the device, solves
  * the batch as ygpu_solve_batch_device on the calling thread's default context
- * and copies the in/out fields back.
+ * and copies the in/out fields back. A single DIVA instance (n_inst = 1) with a
+ * neff hook set runs the hook as ygpu_calc_velocity_diva does, and c_bed comes
+ * back with the hook's last update.
  */
 int ygpu_solve_batch_host(int kind, const ygpu_dyn_par* par, int n_inst, const ygpu_fields* host,
                           ygpu_stats* stats);

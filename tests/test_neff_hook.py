@@ -82,3 +82,21 @@ def test_gpu_noop_hook_equals_plain_solve():
     assert outa["ssa_iter_now"] == outb["ssa_iter_now"] == len(calls)
     for k in ("ux_bar", "uy_bar", "visc_eff"):
         assert rel_l2(fb[k], fa[k]) <= 1e-12, k
+
+
+@pytest.mark.gpu
+def test_gpu_hook_through_batch_host_entry():
+    """ygpu_solve_batch_host with one DIVA state and a hook: the same solve as the
+    drop-in with the hook, and c_bed comes back with the hook's last update."""
+    from yelmo_gb300 import gpu
+    inst = _case()
+    f0 = _prepare_shared(inst)
+    fa, fb = _copy(f0), _copy(f0)
+    calls_a, calls_b = [], []
+    outa = gpu.calc_velocity(fa, inst.dx, inst.n_glen, inst.par, neff_hook=_speed_hook(f0["c_bed"].copy(), calls_a))
+    stb = gpu.calc_velocity_batch([fb], [inst.dx], inst.n_glen, inst.par,
+                                  neff_hook=_speed_hook(f0["c_bed"].copy(), calls_b))[0]
+    assert stb["status"] == 0 and stb["ssa_iter_now"] == outa["ssa_iter_now"] == len(calls_b)
+    assert not np.array_equal(fb["c_bed"], f0["c_bed"])
+    for k in ("ux_bar", "uy_bar", "visc_eff", "c_bed"):
+        assert rel_l2(fb[k], fa[k]) <= 1e-12, k

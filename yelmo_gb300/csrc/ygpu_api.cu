@@ -1106,6 +1106,7 @@ extern "C" int ygpu_solve_batch_host(int kind, const ygpu_dyn_par* par, int n, c
     };
 #undef FO
     const int nt = (int)(sizeof(tab) / sizeof(tab[0]));
+    const bool hooked_cbed = (t_hook != nullptr && diva && n == 1);
     for (int k = 0; k < n; k++) {
         const ygpu_fields& h = host[k];
         const size_t b2 = (size_t)h.nx * h.ny * 8, b3 = b2 * h.nz, i2 = (size_t)h.nx * h.ny * 4;
@@ -1116,7 +1117,9 @@ extern "C" int ygpu_solve_batch_host(int kind, const ygpu_dyn_par* par, int n, c
                 continue;
             }
             const size_t bytes = tab[q].dims == 3 ? b3 : tab[q].dims == 2 ? b2 : tab[q].dims == -2 ? i2 : (size_t)h.nz * 8;
-            ids[k].push_back(S.add(ptr, bytes, tab[q].in, tab[q].out));
+            // a single DIVA solve with a neff hook updates c_bed (as the drop-in does)
+            const bool cbed_out = hooked_cbed && tab[q].off == offsetof(ygpu_fields, c_bed);
+            ids[k].push_back(S.add(ptr, bytes, tab[q].in, tab[q].out || cbed_out));
         }
     }
     if ((st = S.upload(c))) return st;

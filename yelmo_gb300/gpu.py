@@ -147,11 +147,12 @@ def calc_velocity(fields: dict, dx: float, n_glen: float, par: YdynParams, dy: f
 _FIELDS_3D = {"ux", "uy", "ux_i", "uy_i", "visc_eff", "duxdz", "duydz", "ATT"}
 
 
-def calc_velocity_batch(fields: list, dx, n_glen: float, par: YdynParams) -> list:
+def calc_velocity_batch(fields: list, dx, n_glen: float, par: YdynParams, neff_hook=None) -> list:
     """calc_velocity on a batch of host states in one call (ygpu_solve_batch_host).
 
     fields: dicts as for calc_velocity, updated in place; dx: one grid spacing or
-    one per instance (dy = dx). Returns the per-instance stats dicts."""
+    one per instance (dy = dx). neff_hook: as for calc_velocity, for a single
+    DIVA state. Returns the per-instance stats dicts."""
     n = len(fields)
     if n == 0:
         return []
@@ -175,7 +176,15 @@ def calc_velocity_batch(fields: list, dx, n_glen: float, par: YdynParams) -> lis
             setattr(F, name, a.ctypes.data)
     sts = (abi.Stats * n)()
     cpar = par.to_c()
-    _check(lib().ygpu_solve_batch_host(kind, C.byref(cpar), n, arr, sts))
+    L = lib()
+    cb = abi.neff_hook(neff_hook) if neff_hook else None
+    if cb:
+        L.ygpu_set_neff_hook(cb, None)
+    try:
+        _check(L.ygpu_solve_batch_host(kind, C.byref(cpar), n, arr, sts))
+    finally:
+        if cb:
+            L.ygpu_set_neff_hook(abi.NEFF_HOOK(), None)
     return [s.as_dict() for s in sts]
 
 
