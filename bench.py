@@ -252,6 +252,54 @@ def diagnostics_leg(device: str, steps: int, warmup: int) -> dict:
             "alg_bytes_per_call": alg, "achieved_gbs": alg / (ms / 1e3) / 1e9, "kernels": 2}
 
 
+def jacobian_leg(device: str, steps: int, warmup: int) -> dict:
+    """Time the velocity Jacobian (ygpu_calc_jacobian_vel_3D_device, both term
+    sets) on one 801 x 801 field set resident in HBM: 20 layers (nz_aa) and 21
+    layer interfaces (nz_ac), seeded velocities, ice on ~80 % of the cells with
+    margins, CUDA events on the launching stream. Algorithmic bytes per cell:
+    ux, uy, the six ux/uy components (8 nz_aa words), uz and dzx, dzy, dzz
+    (4 nz_ac words), and six 2D inputs, of 8 B."""
+    import ctypes as C
+    import torch
+    from yelmo_gb300 import abi, gpu
+    nx = ny = 801
+    nza, nzc = 20, 21
+    n2 = nx * ny
+    gen = torch.Generator(device=device).manual_seed(13)
+    r = lambda *s: torch.randn(*s, dtype=torch.float64, device=device, generator=gen)
+    f_ice = (torch.rand(n2, dtype=torch.float64, device=device, generator=gen) < 0.8).double()
+    a = {"ux": r(nza * n2) * 100.0, "uy": r(nza * n2) * 100.0, "uz": r(nzc * n2),
+         "H_ice": (r(n2).abs() * 1000.0 + 200.0) * f_ice, "f_ice": f_ice,
+         "dzsdx": r(n2) * 1e-3, "dzsdy": r(n2) * 1e-3, "dzbdx": r(n2) * 1e-2, "dzbdy": r(n2) * 1e-2,
+         "zeta_aa": torch.linspace(0.0, 1.0, nza, dtype=torch.float64, device=device) ** 2,
+         "zeta_ac": torch.linspace(0.0, 1.0, nzc, dtype=torch.float64, device=device) ** 2}
+    for n in abi.JAC_OUTPUTS:
+        a[n] = torch.zeros((nza if n in abi.JAC_OUTPUTS[:6] else nzc) * n2, dtype=torch.float64, device=device)
+    J = abi.JVel()
+    J.nx, J.ny, J.nz_aa, J.nz_ac, J.dx, J.dy = nx, ny, nza, nzc, 4e3, 4e3
+    for n, t in a.items():
+        setattr(J, n, t.data_ptr())
+    L = gpu.lib()
+    stream = torch.cuda.current_stream(device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    times = []
+    for s in range(warmup + steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = L.ygpu_calc_jacobian_vel_3D_device(C.c_void_p(stream.cuda_stream), C.byref(J), 0,
+                                                abi.JAC_UXY | abi.JAC_UZ)
+        e1.record(stream)
+        torch.cuda.synchronize(device)
+        if st != 0:
+            raise RuntimeError(f"Jacobian failed ({st}): {gpu.last_error()}")
+        if s >= warmup:
+            times.append(e0.elapsed_time(e1))
+    ms = statistics.mean(times)
+    alg = float(n2) * 8.0 * (8 * nza + 4 * nzc + 6)
+    return {"workload": "801x801, nz_aa 20, nz_ac 21, synthetic fields, ice on ~80 % of cells",
+            "ms_per_call": ms, "alg_bytes_per_call": alg, "achieved_gbs": alg / (ms / 1e3) / 1e9, "kernels": 1}
+
 def advection_leg(device: str, steps: int, warmup: int) -> dict:
     """Time calc_advec2D(impl-lis) on the device (ygpu_advec2D_impl_lis_device)
     on a 801 x 801 grid resident in HBM: seeded thickness, velocities and source,
@@ -588,6 +636,7 @@ def main():
                 e2e1_times.append(dt)
     diag = diagnostics_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
     adv = advection_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
+    jac = jacobian_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
     i0 = insts[0]
     io = [gpu.host_io_bytes(kind, i.nx, i.ny, i.nz) for i in insts]
     h2d, d2h = sum(a for a, _ in io), sum(b for _, b in io)
@@ -668,6 +717,7 @@ def main():
         "clocks": clocks,
         "diagnostics": (dict(diag, frac=diag["achieved_gbs"] / peak) if diag else None),
         "advection": (dict(adv, frac=adv["achieved_gbs"] / peak) if adv else None),
+        "jacobian": (dict(jac, frac=jac["achieved_gbs"] / peak) if jac else None),
         "cpu_baseline": cpu_base,
     }
     print(json.dumps(line))

@@ -269,6 +269,56 @@ int ygpu_calc_dyn_diagnostics(const ygpu_dyn_diag* fields, int boundaries);
 int ygpu_calc_dyn_diagnostics_device(void* stream, const ygpu_dyn_diag* fields, int boundaries);
 
 /*
+ * ygpu_calc_gradient_column_ac -- calc_gradient_column_ac
+ * (src/yelmo_tools.f90:479-571): the surface or base gradient on the faces for
+ * the sigma-coordinate transform, with the cliff at faces to ice-free ocean
+ * replaced by the ice-side neighbour face. mask_ocn is nonzero where the bed
+ * lies below sea level (calc_ydyn passes z_bed < z_sl,
+ * src/yelmo_dynamics.f90:243-246). Host arrays; the _device form takes device
+ * arrays and runs on `stream` asynchronously.
+ */
+int ygpu_calc_gradient_column_ac(double* dvdx_c, double* dvdy_c, const double* dvdx, const double* dvdy,
+                                 const double* f_ice, const int* mask_ocn, int boundaries, int nx, int ny);
+int ygpu_calc_gradient_column_ac_device(void* stream, double* dvdx_c, double* dvdy_c, const double* dvdx,
+                                        const double* dvdy, const double* f_ice, const int* mask_ocn,
+                                        int boundaries, int nx, int ny);
+
+/*
+ * Velocity Jacobian of calc_ydyn (src/yelmo_dynamics.f90:248-296):
+ *   YGPU_JAC_UXY  calc_jacobian_vel_3D_uxyterms (src/physics/deformation.f90:397-716):
+ *                 dxz, dyz (three-point unequal-spacing derivatives in z on the faces,
+ *                 where the face thickness is positive), dxx, dxy, dyx, dyy (centred,
+ *                 one-sided at the ice margin, cross derivatives over faces with a
+ *                 velocity solution) with the sigma-transform corrections; dzx, dzy,
+ *                 dzz are zeroed (if given), as that routine does.
+ *   YGPU_JAC_UZ   calc_jacobian_vel_3D_uzterms (:718-961): dzz, dzx, dzy of uz on
+ *                 the fully ice-covered cells, zero elsewhere.
+ * Both flags: the two routines in that order, as calc_ydyn runs them for a given uz.
+ * ux, uy and the six ux/uy components are (nx,ny,nz_aa); uz and dzx, dzy, dzz are
+ * (nx,ny,nz_ac). dzsdx ... dzbdy are the column gradients
+ * (ygpu_calc_gradient_column_ac). f_grnd, an argument of both reference routines,
+ * is read by neither and is not taken. nz_aa >= 3 and nz_ac >= 3. FP64 without
+ * contraction: bit-exact with a CPU evaluation of the same expressions.
+ */
+#define YGPU_JAC_UXY 1
+#define YGPU_JAC_UZ  2
+typedef struct ygpu_jvel {
+    int nx, ny, nz_aa, nz_ac;
+    double dx, dy;
+    /* inputs */
+    const double *ux, *uy, *uz, *H_ice, *f_ice;
+    const double *dzsdx, *dzsdy, *dzbdx, *dzbdy;
+    const double *zeta_aa, *zeta_ac;
+    /* outputs */
+    double *dxx, *dxy, *dxz, *dyx, *dyy, *dyz, *dzx, *dzy, *dzz;
+} ygpu_jvel;
+
+/* host arrays (staged through the calling thread's default context) */
+int ygpu_calc_jacobian_vel_3D(const ygpu_jvel* jvel, int boundaries, int terms);
+/* device arrays, on `stream` (a cudaStream_t; NULL: the default stream); asynchronous */
+int ygpu_calc_jacobian_vel_3D_device(void* stream, const ygpu_jvel* jvel, int boundaries, int terms);
+
+/*
  * ygpu_calc_advec2D_impl_lis -- calc_advec2D with solver = "impl-lis"
  * (src/physics/solver_advection.f90:20-145) on the GPU: the implicit upwind
  * system of linear_solver_matrix_advection_csr_2D (:171-487), assembled on the

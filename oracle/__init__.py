@@ -51,6 +51,8 @@ def lib():
         L.orc_calc_advec2D_impl_lis.argtypes = [dp] * 5 + [ip, dp, C.c_double, C.c_double, C.c_double,
                                                            C.c_int, C.c_int, C.c_int, ip, ip]
         L.orc_calc_advec2D_impl_lis.restype = C.c_int
+        L.orc_calc_gradient_column_ac.argtypes = [dp] * 5 + [ip, C.c_int, C.c_int, C.c_int]
+        L.orc_calc_jacobian_vel_3D.argtypes = [C.POINTER(abi.JVel), C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -157,6 +159,28 @@ def calc_advec2D_impl_lis(var, ux, uy, var_dot, mask_ice, var_ref, dx, dy, dt, b
         raise RuntimeError(f"orc_calc_advec2D_impl_lis failed ({r})")
     return dvdt, it.value, st.value
 
+
+def calc_gradient_column_ac(dvdx, dvdy, f_ice, mask_ocn, boundaries: str):
+    """orc_calc_gradient_column_ac: (dvdx_c, dvdy_c)."""
+    nx, ny = f_ice.shape
+    gx = np.zeros((nx, ny), order="F")
+    gy = np.zeros((nx, ny), order="F")
+    ocn = np.asfortranarray(mask_ocn, dtype=np.int32)
+    st = lib().orc_calc_gradient_column_ac(abi.ptr(gx, "d"), abi.ptr(gy, "d"), abi.ptr(dvdx, "d"),
+                                           abi.ptr(dvdy, "d"), abi.ptr(f_ice, "d"), abi.ptr(ocn, "i"),
+                                           abi.BOUNDARY_CODES[boundaries], nx, ny)
+    if st != 0:
+        raise RuntimeError(f"orc_calc_gradient_column_ac failed ({st})")
+    return gx, gy
+
+
+def calc_jacobian_vel_3D(arrays: dict, dx: float, dy: float, boundaries: str, terms: int = 3) -> dict:
+    """orc_calc_jacobian_vel_3D on the arrays of yelmo_gb300.gpu.jacobian_arrays (filled in place)."""
+    J = abi.jvel(arrays, dx, dy)
+    st = lib().orc_calc_jacobian_vel_3D(C.byref(J), abi.BOUNDARY_CODES[boundaries], int(terms))
+    if st != 0:
+        raise RuntimeError(f"orc_calc_jacobian_vel_3D failed ({st})")
+    return arrays
 
 def linear_solve(ptr_, idx, val, b, x, method, precond, maxiter, tol, initx_zeros=False):
     it = C.c_int(0)

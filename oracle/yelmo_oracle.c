@@ -2413,6 +2413,256 @@ int orc_calc_dyn_diagnostics(const ygpu_dyn_diag* D, int bc) {
 
 
 /* ======================================================================== */
+/* Column gradients and the velocity Jacobian (calc_ydyn,                   */
+/* yelmo_dynamics.f90:243-296)                                              */
+/* ======================================================================== */
+
+/* calc_gradient_column_ac, yelmo_tools.f90:479-571 */
+int orc_calc_gradient_column_ac(double* dvdx_c, double* dvdy_c, const double* dvdx, const double* dvdy,
+                                const double* f_ice, const int* mask_ocn, int bc, int nx, int ny) {
+    if (nx < 2 || ny < 2) return YGPU_ERR_BAD_ARG;
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            int im1, ip1, jm1, jp1, im2, ip2, jm2, jp2;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            const size_t c = ID2(i, j);
+            int ice_0 = f_ice[c] == 1.0, ice_1 = f_ice[ID2(ip1, j)] == 1.0;
+            dvdx_c[c] = 0.0;
+            if (ice_0 && ice_1) {
+                dvdx_c[c] = dvdx[c];
+            } else if ((ice_0 && !mask_ocn[ID2(ip1, j)]) || (ice_1 && !mask_ocn[c])) {
+                dvdx_c[c] = dvdx[c];
+            } else if (ice_0) {
+                if (im1 != i && f_ice[ID2(im1, j)] == 1.0) dvdx_c[c] = dvdx[ID2(im1, j)];
+            } else if (ice_1) {
+                nbr(ip1, j, nx, ny, bc, &im2, &ip2, &jm2, &jp2);
+                if (ip2 != ip1 && f_ice[ID2(ip2, j)] == 1.0) dvdx_c[c] = dvdx[ID2(ip1, j)];
+            }
+            ice_1 = f_ice[ID2(i, jp1)] == 1.0;
+            dvdy_c[c] = 0.0;
+            if (ice_0 && ice_1) {
+                dvdy_c[c] = dvdy[c];
+            } else if ((ice_0 && !mask_ocn[ID2(i, jp1)]) || (ice_1 && !mask_ocn[c])) {
+                dvdy_c[c] = dvdy[c];
+            } else if (ice_0) {
+                if (jm1 != j && f_ice[ID2(i, jm1)] == 1.0) dvdy_c[c] = dvdy[ID2(i, jm1)];
+            } else if (ice_1) {
+                nbr(i, jp1, nx, ny, bc, &im2, &ip2, &jm2, &jp2);
+                if (jp2 != jp1 && f_ice[ID2(i, jp2)] == 1.0) dvdy_c[c] = dvdy[ID2(i, jp1)];
+            }
+        }
+    return YGPU_OK;
+}
+
+/* The unequal-spacing first derivatives of the Jacobian routines (Singh and
+   Bhadauria): 3-point forward at the base, centred inside, 3-point backward at
+   the top (or, for uz, first order). u is one column, stride n2. */
+static double jac_vderiv(const double* u, size_t c, size_t n2, const double* z, int k, int nz, double Hn,
+                         int top3) {
+#define U_(kk) u[(size_t)(kk) * n2 + c]
+    double h1, h2;
+    if (k == 0) {
+        h1 = Hn * (z[1] - z[0]);
+        h2 = Hn * (z[2] - z[1]);
+        return -(2.0 * h1 + h2) / (h1 * (h1 + h2)) * U_(0) + (h1 + h2) / (h1 * h2) * U_(1) -
+               h1 / (h2 * (h1 + h2)) * U_(2);
+    }
+    if (k < nz - 1) {
+        h1 = Hn * (z[k] - z[k - 1]);
+        h2 = Hn * (z[k + 1] - z[k]);
+        return -h2 / (h1 * (h1 + h2)) * U_(k - 1) - (h1 - h2) / (h1 * h2) * U_(k) + h1 / (h2 * (h1 + h2)) * U_(k + 1);
+    }
+    if (!top3) return (U_(k) - U_(k - 1)) / (Hn * (z[k] - z[k - 1]));
+    h1 = Hn * (z[k - 1] - z[k - 2]);
+    h2 = Hn * (z[k] - z[k - 1]);
+    return h2 / (h1 * (h1 + h2)) * U_(k - 2) - (h1 + h2) / (h1 * h2) * U_(k - 1) +
+           (h1 + 2.0 * h2) / (h2 * (h1 + h2)) * U_(k);
+#undef U_
+}
+
+/* calc_jacobian_vel_3D_uxyterms, deformation.f90:397-716 */
+static void jac_uxyterms(const ygpu_jvel* J, int bc) {
+    const int nx = J->nx, ny = J->ny, nz = J->nz_aa;
+    const size_t n2 = (size_t)nx * ny;
+    const double *f = J->f_ice, *H = J->H_ice, *ux = J->ux, *uy = J->uy, *za = J->zeta_aa;
+    const double dx = J->dx, dy = J->dy;
+    memset(J->dxx, 0, n2 * nz * sizeof(double));
+    memset(J->dxy, 0, n2 * nz * sizeof(double));
+    memset(J->dxz, 0, n2 * nz * sizeof(double));
+    memset(J->dyx, 0, n2 * nz * sizeof(double));
+    memset(J->dyy, 0, n2 * nz * sizeof(double));
+    memset(J->dyz, 0, n2 * nz * sizeof(double));
+    if (J->dzx) {
+        memset(J->dzx, 0, n2 * J->nz_ac * sizeof(double));
+        memset(J->dzy, 0, n2 * J->nz_ac * sizeof(double));
+        memset(J->dzz, 0, n2 * J->nz_ac * sizeof(double));
+    }
+    /* step 1: dxz, dyz on the faces where the staggered thickness is positive (:464-561) */
+#pragma omp parallel for collapse(2)
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            int im1, ip1, jm1, jp1;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            const size_t c = ID2(i, j);
+            double Hx, Hy;
+            if (f[c] == 1.0 && f[ID2(ip1, j)] < 1.0) Hx = H[c];
+            else if (f[c] < 1.0 && f[ID2(ip1, j)] == 1.0) Hx = H[ID2(ip1, j)];
+            else Hx = 0.5 * (H[c] + H[ID2(ip1, j)]);
+            if (f[c] == 1.0 && f[ID2(i, jp1)] < 1.0) Hy = H[c];
+            else if (f[c] < 1.0 && f[ID2(i, jp1)] == 1.0) Hy = H[ID2(i, jp1)];
+            else Hy = 0.5 * (H[c] + H[ID2(i, jp1)]);
+            for (int k = 0; k < nz; k++) {
+                if (Hx > 0.0) J->dxz[k * n2 + c] = jac_vderiv(ux, c, n2, za, k, nz, Hx, 1);
+                if (Hy > 0.0) J->dyz[k * n2 + c] = jac_vderiv(uy, c, n2, za, k, nz, Hy, 1);
+            }
+        }
+    /* step 2: horizontal derivatives and the sigma-transform corrections (:565-710) */
+    unsigned char* ax = malloc(n2);
+    unsigned char* ay = malloc(n2);
+    active_faces(ax, ay, f, bc, nx, ny);
+#pragma omp parallel for collapse(2)
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            int im1, ip1, jm1, jp1;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            const size_t c = ID2(i, j);
+            for (int k = 0; k < nz; k++) {
+                const size_t o = k * n2;
+                const double* uxk = ux + o;
+                const double* uyk = uy + o;
+                double dxx = (uxk[ID2(ip1, j)] - uxk[ID2(im1, j)]) / (2.0 * dx);
+                double dxy = deriv_active(uxk[ID2(i, jm1)], uxk[c], uxk[ID2(i, jp1)], ax[ID2(i, jm1)],
+                                          ax[ID2(i, jp1)], dy);
+                double dyx = deriv_active(uyk[ID2(im1, j)], uyk[c], uyk[ID2(ip1, j)], ay[ID2(im1, j)],
+                                          ay[ID2(ip1, j)], dx);
+                double dyy = (uyk[ID2(i, jp1)] - uyk[ID2(i, jm1)]) / (2.0 * dy);
+                /* one-sided at the ice margin */
+                if (f[c] == 1.0 && f[ID2(ip1, j)] < 1.0) {
+                    if (im1 > 0 && f[ID2(im1, j)] == 1.0)
+                        dxx = (1.0 * uxk[ID2(im1 - 1, j)] - 4.0 * uxk[ID2(im1, j)] + 3.0 * uxk[c]) / (2.0 * dx);
+                    else
+                        dxx = (uxk[c] - uxk[ID2(im1, j)]) / dx;
+                } else if (f[c] < 1.0 && f[ID2(ip1, j)] == 1.0) {
+                    if (ip1 < nx - 1 && f[ID2(ip1 + 1, j)] == 1.0)
+                        dxx = -(1.0 * uxk[ID2(ip1 + 1, j)] - 4.0 * uxk[ID2(ip1, j)] + 3.0 * uxk[c]) / (2.0 * dx);
+                    else
+                        dxx = (uxk[ID2(ip1, j)] - uxk[c]) / dx;
+                }
+                if (f[c] == 1.0 && f[ID2(i, jp1)] < 1.0) {
+                    if (jm1 > 0 && f[ID2(i, jm1)] == 1.0)
+                        dyy = (1.0 * uyk[ID2(i, jm1 - 1)] - 4.0 * uyk[ID2(i, jm1)] + 3.0 * uyk[c]) / (2.0 * dy);
+                    else
+                        dyy = (uyk[c] - uyk[ID2(i, jm1)]) / dy;
+                } else if (f[c] < 1.0 && f[ID2(i, jp1)] == 1.0) {
+                    if (jp1 < ny - 1 && f[ID2(i, jp1 + 1)] == 1.0)
+                        dyy = -(1.0 * uyk[ID2(i, jp1 + 1)] - 4.0 * uyk[ID2(i, jp1)] + 3.0 * uyk[c]) / (2.0 * dy);
+                    else
+                        dyy = (uyk[ID2(i, jp1)] - uyk[c]) / dy;
+                }
+                const double zk = za[k];
+                const double c_x = -((1.0 - zk) * J->dzbdx[c] + zk * J->dzsdx[c]);
+                const double c_y = -((1.0 - zk) * J->dzbdy[c] + zk * J->dzsdy[c]);
+                const double dzbdx_acy = mean4_act(J->dzbdx[c], J->dzbdx[ID2(i, jp1)], J->dzbdx[ID2(im1, j)],
+                                                   J->dzbdx[ID2(im1, jp1)], ax[c], ax[ID2(i, jp1)], ax[ID2(im1, j)],
+                                                   ax[ID2(im1, jp1)]);
+                const double dzsdx_acy = mean4_act(J->dzsdx[c], J->dzsdx[ID2(i, jp1)], J->dzsdx[ID2(im1, j)],
+                                                   J->dzsdx[ID2(im1, jp1)], ax[c], ax[ID2(i, jp1)], ax[ID2(im1, j)],
+                                                   ax[ID2(im1, jp1)]);
+                const double c_x_acy = -((1.0 - zk) * dzbdx_acy + zk * dzsdx_acy);
+                const double dzbdy_acx = mean4_act(J->dzbdy[c], J->dzbdy[ID2(ip1, j)], J->dzbdy[ID2(i, jm1)],
+                                                   J->dzbdy[ID2(ip1, jm1)], ay[c], ay[ID2(ip1, j)], ay[ID2(i, jm1)],
+                                                   ay[ID2(ip1, jm1)]);
+                const double dzsdy_acx = mean4_act(J->dzsdy[c], J->dzsdy[ID2(ip1, j)], J->dzsdy[ID2(i, jm1)],
+                                                   J->dzsdy[ID2(ip1, jm1)], ay[c], ay[ID2(ip1, j)], ay[ID2(i, jm1)],
+                                                   ay[ID2(ip1, jm1)]);
+                const double c_y_acx = -((1.0 - zk) * dzbdy_acx + zk * dzsdy_acx);
+                J->dxx[o + c] = dxx + c_x * J->dxz[o + c];
+                J->dxy[o + c] = dxy + c_y_acx * J->dxz[o + c];
+                J->dyx[o + c] = dyx + c_x_acy * J->dyz[o + c];
+                J->dyy[o + c] = dyy + c_y * J->dyz[o + c];
+            }
+        }
+    free(ax);
+    free(ay);
+}
+
+/* calc_jacobian_vel_3D_uzterms, deformation.f90:718-961 */
+static void jac_uzterms(const ygpu_jvel* J, int bc) {
+    const int nx = J->nx, ny = J->ny, nz = J->nz_ac;
+    const size_t n2 = (size_t)nx * ny;
+    const double *f = J->f_ice, *uz = J->uz, *zc = J->zeta_ac;
+    memset(J->dzx, 0, n2 * nz * sizeof(double));
+    memset(J->dzy, 0, n2 * nz * sizeof(double));
+    memset(J->dzz, 0, n2 * nz * sizeof(double));
+    /* step 1: dzz on the ice-covered cells (:782-842) */
+#pragma omp parallel for collapse(2)
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const size_t c = ID2(i, j);
+            if (f[c] != 1.0) continue;
+            for (int k = 0; k < nz; k++) J->dzz[k * n2 + c] = jac_vderiv(uz, c, n2, zc, k, nz, J->H_ice[c], 0);
+        }
+    /* step 2: dzx, dzy with the corrections (:846-955) */
+#pragma omp parallel for collapse(2)
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            int im1, ip1, jm1, jp1;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            const size_t c = ID2(i, j);
+            if (f[c] != 1.0) continue;
+            for (int k = 0; k < nz; k++) {
+                const size_t o = k * n2;
+                const double* u = uz + o;
+                double dzx = (u[ID2(ip1, j)] - u[ID2(im1, j)]) / (2.0 * J->dx);
+                double dzy = (u[ID2(i, jp1)] - u[ID2(i, jm1)]) / (2.0 * J->dy);
+                if (f[ID2(ip1, j)] < 1.0 && f[ID2(im1, j)] < 1.0) {
+                    dzx = 0.0;
+                } else if (f[ID2(ip1, j)] < 1.0 && f[ID2(im1, j)] == 1.0) {
+                    if (im1 > 0 && f[ID2(im1 - 1, j)] == 1.0)
+                        dzx = (1.0 * u[ID2(im1 - 1, j)] - 4.0 * u[ID2(im1, j)] + 3.0 * u[c]) / (2.0 * J->dx);
+                    else
+                        dzx = (u[c] - u[ID2(im1, j)]) / J->dx;
+                } else if (f[ID2(ip1, j)] == 1.0 && f[ID2(im1, j)] < 1.0) {
+                    if (ip1 < nx - 1 && f[ID2(ip1 + 1, j)] == 1.0)
+                        dzx = -(1.0 * u[ID2(ip1 + 1, j)] - 4.0 * u[ID2(ip1, j)] + 3.0 * u[c]) / (2.0 * J->dx);
+                    else
+                        dzx = (u[ID2(ip1, j)] - u[c]) / J->dx;
+                }
+                if (f[ID2(i, jp1)] < 1.0 && f[ID2(i, jm1)] < 1.0) {
+                    dzy = 0.0;
+                } else if (f[ID2(i, jp1)] < 1.0 && f[ID2(i, jm1)] == 1.0) {
+                    if (jm1 > 0 && f[ID2(i, jm1 - 1)] == 1.0)
+                        dzy = (1.0 * u[ID2(i, jm1 - 1)] - 4.0 * u[ID2(i, jm1)] + 3.0 * u[c]) / (2.0 * J->dy);
+                    else
+                        dzy = (u[c] - u[ID2(i, jm1)]) / J->dy;
+                } else if (f[ID2(i, jp1)] == 1.0 && f[ID2(i, jm1)] < 1.0) {
+                    if (jp1 < ny - 1 && f[ID2(i, jp1 + 1)] == 1.0)
+                        dzy = -(1.0 * u[ID2(i, jp1 + 1)] - 4.0 * u[ID2(i, jp1)] + 3.0 * u[c]) / (2.0 * J->dy);
+                    else
+                        dzy = (u[ID2(i, jp1)] - u[c]) / J->dy;
+                }
+                const double dzbdx_aa = 0.5 * (J->dzbdx[c] + J->dzbdx[ID2(im1, j)]);
+                const double dzbdy_aa = 0.5 * (J->dzbdy[c] + J->dzbdy[ID2(i, jm1)]);
+                const double dzsdx_aa = 0.5 * (J->dzsdx[c] + J->dzsdx[ID2(im1, j)]);
+                const double dzsdy_aa = 0.5 * (J->dzsdy[c] + J->dzsdy[ID2(i, jm1)]);
+                const double c_x = -((1.0 - zc[k]) * dzbdx_aa + zc[k] * dzsdx_aa);
+                const double c_y = -((1.0 - zc[k]) * dzbdy_aa + zc[k] * dzsdy_aa);
+                J->dzx[o + c] = dzx + c_x * J->dzz[o + c];
+                J->dzy[o + c] = dzy + c_y * J->dzz[o + c];
+            }
+        }
+}
+
+int orc_calc_jacobian_vel_3D(const ygpu_jvel* J, int bc, int terms) {
+    if (!J || J->nx < 2 || J->ny < 2 || terms < 1 || terms > 3) return YGPU_ERR_BAD_ARG;
+    if ((terms & YGPU_JAC_UXY) && J->nz_aa < 3) return YGPU_ERR_BAD_ARG;
+    if ((terms & YGPU_JAC_UZ) && J->nz_ac < 3) return YGPU_ERR_BAD_ARG;
+    if (terms & YGPU_JAC_UXY) jac_uxyterms(J, bc);
+    if (terms & YGPU_JAC_UZ) jac_uzterms(J, bc);
+    return YGPU_OK;
+}
+
+/* ======================================================================== */
 /* Implicit upwind advection, calc_advec2D(solver = "impl-lis")             */
 /* ======================================================================== */
 

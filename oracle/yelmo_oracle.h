@@ -156,6 +156,13 @@ void orc_set_threads(int n);
    f_vbvs; the same groups and NULL conventions as ygpu_calc_dyn_diagnostics. */
 int orc_calc_dyn_diagnostics(const ygpu_dyn_diag* D, int boundaries);
 
+/* calc_gradient_column_ac (yelmo_tools.f90:479-571) and the velocity Jacobian
+   (calc_jacobian_vel_3D_uxyterms / _uzterms, deformation.f90:397-961), in the
+   reference's two passes per routine; the same arguments as the ygpu_ entries. */
+int orc_calc_gradient_column_ac(double* dvdx_c, double* dvdy_c, const double* dvdx, const double* dvdy,
+                                const double* f_ice, const int* mask_ocn, int boundaries, int nx, int ny);
+int orc_calc_jacobian_vel_3D(const ygpu_jvel* J, int boundaries, int terms);
+
 /* calc_advec2D(solver = "impl-lis"), solver_advection.f90:20-145: the CSR system of
    linear_solver_matrix_advection_csr_2D (:171-487) solved with this oracle's BiCGSTAB
    and Jacobi to 1e-12, calc_fixed_cell_transport (:489-546), dvdt. Same arguments as

@@ -104,6 +104,45 @@ def dyn_diag(arrays: dict, nx: int, ny: int, nz: int, dx: float, dy: float) -> D
     return D
 
 
+JAC_INPUTS = ("ux", "uy", "uz", "H_ice", "f_ice", "dzsdx", "dzsdy", "dzbdx", "dzbdy", "zeta_aa", "zeta_ac")
+JAC_OUTPUTS = ("dxx", "dxy", "dxz", "dyx", "dyy", "dyz", "dzx", "dzy", "dzz")
+JAC_UXY, JAC_UZ = 1, 2
+
+
+class JVel(C.Structure):
+    """ygpu_jvel: arrays of the velocity Jacobian."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz_aa", C.c_int), ("nz_ac", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double)] + [(n, C.c_void_p) for n in JAC_INPUTS + JAC_OUTPUTS]
+
+
+def jvel(arrays: dict, dx: float, dy: float) -> JVel:
+    """A JVel over the numpy arrays of `arrays` (absent names stay NULL); the
+    layer counts come from zeta_aa / zeta_ac."""
+    nx, ny = arrays["H_ice"].shape
+    nza = arrays["zeta_aa"].shape[0] if "zeta_aa" in arrays else 0
+    nzc = arrays["zeta_ac"].shape[0] if "zeta_ac" in arrays else (arrays["dzz"].shape[2] if "dzz" in arrays else 0)
+    J = JVel()
+    J.nx, J.ny, J.nz_aa, J.nz_ac, J.dx, J.dy = nx, ny, nza, nzc, dx, dy
+    for n in JAC_INPUTS + JAC_OUTPUTS:
+        a = arrays.get(n)
+        if a is None:
+            continue
+        if n == "zeta_aa":
+            want = (nza,)
+        elif n == "zeta_ac":
+            want = (nzc,)
+        elif n in ("ux", "uy", "dxx", "dxy", "dxz", "dyx", "dyy", "dyz"):
+            want = (nx, ny, nza)
+        elif n in ("uz", "dzx", "dzy", "dzz"):
+            want = (nx, ny, nzc)
+        else:
+            want = (nx, ny)
+        if a.shape != want:
+            raise ValueError(f"{n}: shape {a.shape}, expected {want}")
+        ptr(a, "d")
+        setattr(J, n, a.ctypes.data)
+    return J
+
 class Fields(C.Structure):
     """ygpu_fields: device pointers of one instance."""
     _fields_ = [

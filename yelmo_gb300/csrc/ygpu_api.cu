@@ -1256,6 +1256,111 @@ extern "C" int ygpu_calc_dyn_diagnostics(const ygpu_dyn_diag* H, int boundaries)
     return S.download(c);
 }
 
+static int gradient_column_check(double* gx_c, double* gy_c, const double* gx, const double* gy, const double* f_ice,
+                                 const int* ocn, int bc, int nx, int ny) {
+    if (nx < 2 || ny < 2 || bc < 0 || bc > 6 || (size_t)nx * ny > (size_t)(1 << 28) ||
+        any_null({gx_c, gy_c, gx, gy, f_ice, ocn})) {
+        ygpu_set_error("bad arguments");
+        return YGPU_ERR_BAD_ARG;
+    }
+    return YGPU_OK;
+}
+
+extern "C" int ygpu_calc_gradient_column_ac_device(void* stream, double* dvdx_c, double* dvdy_c, const double* dvdx,
+                                                   const double* dvdy, const double* f_ice, const int* mask_ocn,
+                                                   int boundaries, int nx, int ny) {
+    int st = gradient_column_check(dvdx_c, dvdy_c, dvdx, dvdy, f_ice, mask_ocn, boundaries, nx, ny);
+    if (st) return st;
+    return ygpu_gradient_column_device((cudaStream_t)stream, dvdx_c, dvdy_c, dvdx, dvdy, f_ice, mask_ocn, boundaries,
+                                       nx, ny);
+}
+
+extern "C" int ygpu_calc_gradient_column_ac(double* dvdx_c, double* dvdy_c, const double* dvdx, const double* dvdy,
+                                            const double* f_ice, const int* mask_ocn, int boundaries, int nx,
+                                            int ny) {
+    int st = gradient_column_check(dvdx_c, dvdy_c, dvdx, dvdy, f_ice, mask_ocn, boundaries, nx, ny);
+    if (st) return st;
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const size_t n = (size_t)nx * ny, b2 = n * 8;
+    Staging S;
+    size_t a_gx = S.add((void*)dvdx, b2, 1, 0), a_gy = S.add((void*)dvdy, b2, 1, 0);
+    size_t a_f = S.add((void*)f_ice, b2, 1, 0), a_o = S.add((void*)mask_ocn, n * 4, 1, 0);
+    size_t a_cx = S.add(dvdx_c, b2, 0, 1), a_cy = S.add(dvdy_c, b2, 0, 1);
+    if ((st = S.upload(c))) return st;
+    auto d = [&](size_t a) { return (double*)S.args[a].dev; };
+    if ((st = ygpu_gradient_column_device(c->stream, d(a_cx), d(a_cy), d(a_gx), d(a_gy), d(a_f),
+                                          (const int*)S.args[a_o].dev, boundaries, nx, ny)))
+        return st;
+    return S.download(c);
+}
+
+static int jacobian_check(const ygpu_jvel* J, int bc, int terms) {
+    if (!J || J->nx < 2 || J->ny < 2 || !(J->dx > 0.0) || !(J->dy > 0.0) || bc < 0 || bc > 6 || terms < 1 ||
+        terms > 3 || (size_t)J->nx * J->ny > (size_t)(1 << 28)) {
+        ygpu_set_error("bad arguments");
+        return YGPU_ERR_BAD_ARG;
+    }
+    if (any_null({J->H_ice, J->f_ice, J->dzsdx, J->dzsdy, J->dzbdx, J->dzbdy})) {
+        ygpu_set_error("H_ice, f_ice and the four column gradients are required");
+        return YGPU_ERR_BAD_ARG;
+    }
+    if ((terms & YGPU_JAC_UXY) &&
+        (J->nz_aa < 3 || any_null({J->ux, J->uy, J->zeta_aa, J->dxx, J->dxy, J->dxz, J->dyx, J->dyy, J->dyz}))) {
+        ygpu_set_error("the ux/uy terms need ux, uy, zeta_aa, dxx ... dyz and nz_aa >= 3");
+        return YGPU_ERR_BAD_ARG;
+    }
+    const bool dz_out = (terms & YGPU_JAC_UZ) || J->dzx || J->dzy || J->dzz;
+    if (dz_out && (J->nz_ac < 1 || any_null({J->dzx, J->dzy, J->dzz}))) {
+        ygpu_set_error("dzx, dzy, dzz go together and need nz_ac >= 1");
+        return YGPU_ERR_BAD_ARG;
+    }
+    if ((terms & YGPU_JAC_UZ) && (J->nz_ac < 3 || any_null({J->uz, J->zeta_ac}))) {
+        ygpu_set_error("the uz terms need uz, zeta_ac and nz_ac >= 3");
+        return YGPU_ERR_BAD_ARG;
+    }
+    return YGPU_OK;
+}
+
+extern "C" int ygpu_calc_jacobian_vel_3D_device(void* stream, const ygpu_jvel* J, int boundaries, int terms) {
+    int st = jacobian_check(J, boundaries, terms);
+    if (st) return st;
+    return ygpu_jacobian_device((cudaStream_t)stream, *J, boundaries, terms);
+}
+
+// host arrays: the inputs of the requested terms in, their components out
+extern "C" int ygpu_calc_jacobian_vel_3D(const ygpu_jvel* H, int boundaries, int terms) {
+    int st = jacobian_check(H, boundaries, terms);
+    if (st) return st;
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const size_t b2 = (size_t)H->nx * H->ny * 8;
+    const bool uxy = terms & YGPU_JAC_UXY, uzt = terms & YGPU_JAC_UZ;
+    const size_t ba = uxy ? b2 * (size_t)H->nz_aa : 0, bc3 = b2 * (size_t)(H->nz_ac > 0 ? H->nz_ac : 0);
+    Staging S;
+    ygpu_jvel D = *H;
+    std::vector<std::pair<size_t, const void**>> map;
+    auto in = [&](const double* src, const double** dst, size_t bytes) {
+        map.push_back({S.add((void*)src, bytes, 1, 0), (const void**)dst});
+    };
+    auto out = [&](double* src, double** dst, size_t bytes) {
+        map.push_back({S.add((void*)src, bytes, 0, 1), (const void**)dst});
+    };
+    in(H->H_ice, &D.H_ice, b2); in(H->f_ice, &D.f_ice, b2);
+    in(H->dzsdx, &D.dzsdx, b2); in(H->dzsdy, &D.dzsdy, b2); in(H->dzbdx, &D.dzbdx, b2); in(H->dzbdy, &D.dzbdy, b2);
+    if (uxy) {
+        in(H->ux, &D.ux, ba); in(H->uy, &D.uy, ba); in(H->zeta_aa, &D.zeta_aa, (size_t)H->nz_aa * 8);
+        out(H->dxx, &D.dxx, ba); out(H->dxy, &D.dxy, ba); out(H->dxz, &D.dxz, ba);
+        out(H->dyx, &D.dyx, ba); out(H->dyy, &D.dyy, ba); out(H->dyz, &D.dyz, ba);
+    }
+    if (uzt) { in(H->uz, &D.uz, bc3); in(H->zeta_ac, &D.zeta_ac, (size_t)H->nz_ac * 8); }
+    if (H->dzx) { out(H->dzx, &D.dzx, bc3); out(H->dzy, &D.dzy, bc3); out(H->dzz, &D.dzz, bc3); }
+    if ((st = S.upload(c))) return st;
+    for (auto& m : map) *m.second = S.args[m.first].dev;
+    if ((st = ygpu_jacobian_device(c->stream, D, boundaries, terms))) return st;
+    return S.download(c);
+}
+
 extern "C" int ygpu_calc_advec2D_impl_lis(double* dvdt, const double* var, const double* ux, const double* uy,
                                           const double* var_dot, const int* mask_ice, const double* var_ref,
                                           double dx, double dy, double dt, int boundaries, int nx, int ny,

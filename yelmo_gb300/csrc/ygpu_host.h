@@ -105,6 +105,9 @@ int ygpu_dyn_inputs_device(cudaStream_t s, const double* H, const double* zb, co
                            double dx, double grad_lim, double taud_lim, double rho_ice, double rho_sw, double g,
                            int bc, int nx, int ny);
 int ygpu_dyn_diagnostics_device(cudaStream_t s, const ygpu_dyn_diag& D, int bc);
+int ygpu_gradient_column_device(cudaStream_t s, double* gx_c, double* gy_c, const double* gx, const double* gy,
+                                const double* f_ice, const int* mask_ocn, int bc, int nx, int ny);
+int ygpu_jacobian_device(cudaStream_t s, const ygpu_jvel& J, int bc, int terms);
 int ygpu_ssa_masks_device(cudaStream_t s, int* mx, int* my, const int* mf, const double* f_ice, const double* f_grnd,
                           int lat, int bc, int nx, int ny);
 

@@ -348,3 +348,295 @@ int ygpu_dyn_diagnostics_device(cudaStream_t s, const ygpu_dyn_diag& D, int bc) 
     ygpu_count_launches(2);
     return YGPU_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Column gradients and the velocity Jacobian of calc_ydyn
+// (src/yelmo_dynamics.f90:243-296)
+// ---------------------------------------------------------------------------
+
+// calc_gradient_column_ac (yelmo_tools.f90:479-571): the face keeps its
+// gradient between two ice-covered cells and at a margin to ice-free land; at a
+// face to ice-free ocean it takes the ice-side neighbour face if that face lies
+// between two ice-covered cells; otherwise zero.
+__global__ void k_gradient_column(int nx, int ny, int bc, const double* __restrict__ gx,
+                                  const double* __restrict__ gy, const double* __restrict__ f_ice,
+                                  const int* __restrict__ ocn, double* __restrict__ gx_c, double* __restrict__ gy_c) {
+    const int n2 = nx * ny;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n2; c += gridDim.x * blockDim.x) {
+        const int i = c % nx, j = c / nx;
+        int im1, ip1, jm1, jp1;
+        nbr_bc(i, j, nx, ny, bc, im1, ip1, jm1, jp1);
+        {
+            const int c1 = ip1 + nx * j;
+            const bool ice0 = f_ice[c] == 1.0, ice1 = f_ice[c1] == 1.0;
+            double v = 0.0;
+            if (ice0 && ice1) {
+                v = gx[c];
+            } else if ((ice0 && !ocn[c1]) || (ice1 && !ocn[c])) {
+                v = gx[c];
+            } else if (ice0) {
+                if (im1 != i && f_ice[im1 + nx * j] == 1.0) v = gx[im1 + nx * j];
+            } else if (ice1) {
+                int am1, ap1, bm1, bp1;
+                nbr_bc(ip1, j, nx, ny, bc, am1, ap1, bm1, bp1);
+                if (ap1 != ip1 && f_ice[ap1 + nx * j] == 1.0) v = gx[c1];
+            }
+            gx_c[c] = v;
+        }
+        {
+            const int c1 = i + nx * jp1;
+            const bool ice0 = f_ice[c] == 1.0, ice1 = f_ice[c1] == 1.0;
+            double v = 0.0;
+            if (ice0 && ice1) {
+                v = gy[c];
+            } else if ((ice0 && !ocn[c1]) || (ice1 && !ocn[c])) {
+                v = gy[c];
+            } else if (ice0) {
+                if (jm1 != j && f_ice[i + nx * jm1] == 1.0) v = gy[i + nx * jm1];
+            } else if (ice1) {
+                int am1, ap1, bm1, bp1;
+                nbr_bc(i, jp1, nx, ny, bc, am1, ap1, bm1, bp1);
+                if (bp1 != jp1 && f_ice[i + nx * bp1] == 1.0) v = gy[c1];
+            }
+            gy_c[c] = v;
+        }
+    }
+}
+
+// calc_active_faces (deformation.f90:1316-1344) of the x face right of (a, b)
+// and of the y face above it
+YG_DEV bool jac_act_x(const double* f, int a, int b, int nx, int ny, int bc) {
+    int am1, ap1, bm1, bp1;
+    nbr_bc(a, b, nx, ny, bc, am1, ap1, bm1, bp1);
+    return f[a + nx * b] == 1.0 || f[ap1 + nx * b] == 1.0;
+}
+YG_DEV bool jac_act_y(const double* f, int a, int b, int nx, int ny, int bc) {
+    int am1, ap1, bm1, bp1;
+    nbr_bc(a, b, nx, ny, bc, am1, ap1, bm1, bp1);
+    return f[a + nx * b] == 1.0 || f[a + nx * bp1] == 1.0;
+}
+
+// deriv_active (deformation.f90:1346-1368)
+YG_DEV double jac_deriv_active(double vm, double v0, double vp, bool am, bool ap, double h) {
+    if (am && ap) return (vp - vm) / (2.0 * h);
+    if (ap) return (vp - v0) / h;
+    if (am) return (v0 - vm) / h;
+    return 0.0;
+}
+
+// mean4_active (deformation.f90:1370-1391)
+YG_DEV double jac_mean4(double v1, double v2, double v3, double v4, bool a1, bool a2, bool a3, bool a4) {
+    const int n = (int)a1 + (int)a2 + (int)a3 + (int)a4;
+    if (n == 0) return 0.0;
+    double s = (a1 ? v1 : 0.0) + (a2 ? v2 : 0.0);
+    s = s + (a3 ? v3 : 0.0);
+    s = s + (a4 ? v4 : 0.0);
+    return s / (double)n;
+}
+
+// First derivative in z at layer k of a column with heights z (scaled by the
+// thickness Hn): three-point unequal-spacing formulas (Singh and Bhadauria),
+// one-sided at the base and, with top3, at the top; else first order there.
+YG_DEV double jac_dz(const double* __restrict__ u, const double* __restrict__ z, size_t c, size_t n2, int k, int nz,
+                     double Hn, bool top3) {
+    auto U = [&](int kk) { return __ldg(u + (size_t)kk * n2 + c); };
+    if (k == 0) {
+        const double h1 = Hn * (z[1] - z[0]), h2 = Hn * (z[2] - z[1]);
+        return -(2.0 * h1 + h2) / (h1 * (h1 + h2)) * U(0) + (h1 + h2) / (h1 * h2) * U(1) -
+               h1 / (h2 * (h1 + h2)) * U(2);
+    }
+    if (k < nz - 1) {
+        const double h1 = Hn * (z[k] - z[k - 1]), h2 = Hn * (z[k + 1] - z[k]);
+        return -h2 / (h1 * (h1 + h2)) * U(k - 1) - (h1 - h2) / (h1 * h2) * U(k) + h1 / (h2 * (h1 + h2)) * U(k + 1);
+    }
+    if (!top3) return (U(k) - U(k - 1)) / (Hn * (z[k] - z[k - 1]));
+    const double h1 = Hn * (z[k - 1] - z[k - 2]), h2 = Hn * (z[k] - z[k - 1]);
+    return h2 / (h1 * (h1 + h2)) * U(k - 2) - (h1 + h2) / (h1 * h2) * U(k - 1) +
+           (h1 + 2.0 * h2) / (h2 * (h1 + h2)) * U(k);
+}
+
+// Margin stencil of a derivative along one direction at cell c: 0 centred,
+// 1 three-point backward, 2 two-point backward, 3 three-point forward,
+// 4 two-point forward, 5 zero.
+YG_DEV double jac_dh(int mode, double um2, double um1, double u0, double up1, double up2, double h) {
+    switch (mode) {
+        case 1: return (1.0 * um2 - 4.0 * um1 + 3.0 * u0) / (2.0 * h);
+        case 2: return (u0 - um1) / h;
+        case 3: return -(1.0 * up2 - 4.0 * up1 + 3.0 * u0) / (2.0 * h);
+        case 4: return (up1 - u0) / h;
+        case 5: return 0.0;
+        default: return (up1 - um1) / (2.0 * h);
+    }
+}
+
+// calc_jacobian_vel_3D_uxyterms (deformation.f90:397-716) for the column at (i, j)
+YG_DEV void jac_uxy_column(const ygpu_jvel& J, int bc, int i, int j, int im1, int ip1, int jm1, int jp1) {
+    const int nx = J.nx, ny = J.ny, nz = J.nz_aa;
+    const size_t n2 = (size_t)nx * ny, c = (size_t)i + (size_t)nx * j;
+    const double* __restrict__ f = J.f_ice;
+    const double* __restrict__ H = J.H_ice;
+    const size_t cxp = ip1 + (size_t)nx * j, cxm = im1 + (size_t)nx * j;
+    const size_t cyp = i + (size_t)nx * jp1, cym = i + (size_t)nx * jm1;
+    const bool ice = f[c] == 1.0;
+    // face thicknesses (:473-487)
+    double Hx, Hy;
+    if (ice && f[cxp] < 1.0) Hx = H[c];
+    else if (f[c] < 1.0 && f[cxp] == 1.0) Hx = H[cxp];
+    else Hx = 0.5 * (H[c] + H[cxp]);
+    if (ice && f[cyp] < 1.0) Hy = H[c];
+    else if (f[c] < 1.0 && f[cyp] == 1.0) Hy = H[cyp];
+    else Hy = 0.5 * (H[c] + H[cyp]);
+    // margin stencils of dxx and dyy (:590-637)
+    int mx = 0, my = 0;
+    if (ice && f[cxp] < 1.0) mx = (im1 > 0 && f[cxm] == 1.0) ? 1 : 2;
+    else if (f[c] < 1.0 && f[cxp] == 1.0) mx = (ip1 < nx - 1 && f[cxp + 1] == 1.0) ? 3 : 4;
+    if (ice && f[cyp] < 1.0) my = (jm1 > 0 && f[cym] == 1.0) ? 1 : 2;
+    else if (f[c] < 1.0 && f[cyp] == 1.0) my = (jp1 < ny - 1 && f[cyp + nx] == 1.0) ? 3 : 4;
+    // faces with a velocity solution and the cross gradients over them (:654-666)
+    const bool ax_jm1 = jac_act_x(f, i, jm1, nx, ny, bc), ax_jp1 = jac_act_x(f, i, jp1, nx, ny, bc);
+    const bool ax_0 = jac_act_x(f, i, j, nx, ny, bc), ax_im1 = jac_act_x(f, im1, j, nx, ny, bc);
+    const bool ax_im1_jp1 = jac_act_x(f, im1, jp1, nx, ny, bc);
+    const bool ay_im1 = jac_act_y(f, im1, j, nx, ny, bc), ay_ip1 = jac_act_y(f, ip1, j, nx, ny, bc);
+    const bool ay_0 = jac_act_y(f, i, j, nx, ny, bc), ay_jm1 = jac_act_y(f, i, jm1, nx, ny, bc);
+    const bool ay_ip1_jm1 = jac_act_y(f, ip1, jm1, nx, ny, bc);
+    const double* bx = J.dzbdx;
+    const double* by = J.dzbdy;
+    const double* sx = J.dzsdx;
+    const double* sy = J.dzsdy;
+    const size_t cxm_yp = im1 + (size_t)nx * jp1, cxp_ym = ip1 + (size_t)nx * jm1;
+    const double dzbdx_acy = jac_mean4(bx[c], bx[cyp], bx[cxm], bx[cxm_yp], ax_0, ax_jp1, ax_im1, ax_im1_jp1);
+    const double dzsdx_acy = jac_mean4(sx[c], sx[cyp], sx[cxm], sx[cxm_yp], ax_0, ax_jp1, ax_im1, ax_im1_jp1);
+    const double dzbdy_acx = jac_mean4(by[c], by[cxp], by[cym], by[cxp_ym], ay_0, ay_ip1, ay_jm1, ay_ip1_jm1);
+    const double dzsdy_acx = jac_mean4(sy[c], sy[cxp], sy[cym], sy[cxp_ym], ay_0, ay_ip1, ay_jm1, ay_ip1_jm1);
+    const double bxc = bx[c], byc = by[c], sxc = sx[c], syc = sy[c];
+    const double* __restrict__ ux = J.ux;
+    const double* __restrict__ uy = J.uy;
+    for (int k = 0; k < nz; k++) {
+        const size_t o = (size_t)k * n2;
+        const double dxz = (Hx > 0.0) ? jac_dz(ux, J.zeta_aa, c, n2, k, nz, Hx, true) : 0.0;
+        const double dyz = (Hy > 0.0) ? jac_dz(uy, J.zeta_aa, c, n2, k, nz, Hy, true) : 0.0;
+        const double* uxk = ux + o;
+        const double* uyk = uy + o;
+        const double x0 = __ldg(uxk + c), y0 = __ldg(uyk + c);
+        const double xm1 = __ldg(uxk + cxm), xp1 = __ldg(uxk + cxp);
+        const double ym1 = __ldg(uyk + cym), yp1 = __ldg(uyk + cyp);
+        const double xm2 = (mx == 1) ? __ldg(uxk + cxm - 1) : 0.0, xp2 = (mx == 3) ? __ldg(uxk + cxp + 1) : 0.0;
+        const double ym2 = (my == 1) ? __ldg(uyk + cym - nx) : 0.0, yp2 = (my == 3) ? __ldg(uyk + cyp + nx) : 0.0;
+        double dxx = jac_dh(mx, xm2, xm1, x0, xp1, xp2, J.dx);
+        double dyy = jac_dh(my, ym2, ym1, y0, yp1, yp2, J.dy);
+        double dxy = jac_deriv_active(__ldg(uxk + cym), x0, __ldg(uxk + cyp), ax_jm1, ax_jp1, J.dy);
+        double dyx = jac_deriv_active(__ldg(uyk + cxm), y0, __ldg(uyk + cxp), ay_im1, ay_ip1, J.dx);
+        // sigma-transform corrections (:639-675)
+        const double zk = J.zeta_aa[k];
+        const double c_x = -((1.0 - zk) * bxc + zk * sxc);
+        const double c_y = -((1.0 - zk) * byc + zk * syc);
+        const double c_x_acy = -((1.0 - zk) * dzbdx_acy + zk * dzsdx_acy);
+        const double c_y_acx = -((1.0 - zk) * dzbdy_acx + zk * dzsdy_acx);
+        dxx = dxx + c_x * dxz;
+        dxy = dxy + c_y_acx * dxz;
+        dyx = dyx + c_x_acy * dyz;
+        dyy = dyy + c_y * dyz;
+        J.dxx[o + c] = dxx;
+        J.dxy[o + c] = dxy;
+        J.dxz[o + c] = dxz;
+        J.dyx[o + c] = dyx;
+        J.dyy[o + c] = dyy;
+        J.dyz[o + c] = dyz;
+    }
+}
+
+// calc_jacobian_vel_3D_uzterms (deformation.f90:718-961) for the column at (i, j)
+YG_DEV void jac_uz_column(const ygpu_jvel& J, int i, int j, int im1, int ip1, int jm1, int jp1) {
+    const int nx = J.nx, ny = J.ny, nz = J.nz_ac;
+    const size_t n2 = (size_t)nx * ny, c = (size_t)i + (size_t)nx * j;
+    const double* __restrict__ f = J.f_ice;
+    if (f[c] != 1.0) {
+        for (int k = 0; k < nz; k++) {
+            const size_t o = (size_t)k * n2 + c;
+            J.dzx[o] = 0.0;
+            J.dzy[o] = 0.0;
+            J.dzz[o] = 0.0;
+        }
+        return;
+    }
+    const size_t cxp = ip1 + (size_t)nx * j, cxm = im1 + (size_t)nx * j;
+    const size_t cyp = i + (size_t)nx * jp1, cym = i + (size_t)nx * jm1;
+    int mx = 0, my = 0;
+    if (f[cxp] < 1.0 && f[cxm] < 1.0) mx = 5;
+    else if (f[cxp] < 1.0 && f[cxm] == 1.0) mx = (im1 > 0 && f[cxm - 1] == 1.0) ? 1 : 2;
+    else if (f[cxp] == 1.0 && f[cxm] < 1.0) mx = (ip1 < nx - 1 && f[cxp + 1] == 1.0) ? 3 : 4;
+    if (f[cyp] < 1.0 && f[cym] < 1.0) my = 5;
+    else if (f[cyp] < 1.0 && f[cym] == 1.0) my = (jm1 > 0 && f[cym - nx] == 1.0) ? 1 : 2;
+    else if (f[cyp] == 1.0 && f[cym] < 1.0) my = (jp1 < ny - 1 && f[cyp + nx] == 1.0) ? 3 : 4;
+    const double Hn = J.H_ice[c];
+    const double dzbdx_aa = 0.5 * (J.dzbdx[c] + J.dzbdx[cxm]);
+    const double dzbdy_aa = 0.5 * (J.dzbdy[c] + J.dzbdy[cym]);
+    const double dzsdx_aa = 0.5 * (J.dzsdx[c] + J.dzsdx[cxm]);
+    const double dzsdy_aa = 0.5 * (J.dzsdy[c] + J.dzsdy[cym]);
+    const double* __restrict__ uz = J.uz;
+    for (int k = 0; k < nz; k++) {
+        const size_t o = (size_t)k * n2;
+        const double* uzk = uz + o;
+        const double dzz = jac_dz(uz, J.zeta_ac, c, n2, k, nz, Hn, false);
+        const double z0 = __ldg(uzk + c);
+        double dzx = (mx == 5) ? 0.0
+                               : jac_dh(mx, (mx == 1) ? __ldg(uzk + cxm - 1) : 0.0, __ldg(uzk + cxm), z0,
+                                        __ldg(uzk + cxp), (mx == 3) ? __ldg(uzk + cxp + 1) : 0.0, J.dx);
+        double dzy = (my == 5) ? 0.0
+                               : jac_dh(my, (my == 1) ? __ldg(uzk + cym - nx) : 0.0, __ldg(uzk + cym), z0,
+                                        __ldg(uzk + cyp), (my == 3) ? __ldg(uzk + cyp + nx) : 0.0, J.dy);
+        const double zk = J.zeta_ac[k];
+        const double c_x = -((1.0 - zk) * dzbdx_aa + zk * dzsdx_aa);
+        const double c_y = -((1.0 - zk) * dzbdy_aa + zk * dzsdy_aa);
+        dzx = dzx + c_x * dzz;
+        dzy = dzy + c_y * dzz;
+        J.dzx[o + c] = dzx;
+        J.dzy[o + c] = dzy;
+        J.dzz[o + c] = dzz;
+    }
+}
+
+// One thread per column: the ux/uy terms, then the uz terms (or the zeroing of
+// dzx, dzy, dzz that the ux/uy routine starts with).
+__global__ void __launch_bounds__(256) k_jacobian(ygpu_jvel J, int bc, int terms) {
+    const int nx = J.nx, ny = J.ny, n2 = nx * ny;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n2; c += gridDim.x * blockDim.x) {
+        const int i = c % nx, j = c / nx;
+        int im1, ip1, jm1, jp1;
+        nbr_bc(i, j, nx, ny, bc, im1, ip1, jm1, jp1);
+        if (terms & YGPU_JAC_UXY) jac_uxy_column(J, bc, i, j, im1, ip1, jm1, jp1);
+        if (terms & YGPU_JAC_UZ) {
+            jac_uz_column(J, i, j, im1, ip1, jm1, jp1);
+        } else if (J.dzx) {
+            for (int k = 0; k < J.nz_ac; k++) {
+                const size_t o = (size_t)k * n2 + c;
+                J.dzx[o] = 0.0;
+                J.dzy[o] = 0.0;
+                J.dzz[o] = 0.0;
+            }
+        }
+    }
+}
+
+int ygpu_gradient_column_device(cudaStream_t s, double* gx_c, double* gy_c, const double* gx, const double* gy,
+                                const double* f_ice, const int* mask_ocn, int bc, int nx, int ny) {
+    k_gradient_column<<<grid_for(nx * ny), 256, 0, s>>>(nx, ny, bc, gx, gy, f_ice, mask_ocn, gx_c, gy_c);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        ygpu_set_error("column gradient kernel: %s", cudaGetErrorString(e));
+        return YGPU_ERR_CUDA;
+    }
+    ygpu_count_launches(1);
+    return YGPU_OK;
+}
+
+int ygpu_jacobian_device(cudaStream_t s, const ygpu_jvel& J, int bc, int terms) {
+    k_jacobian<<<grid_for(J.nx * J.ny), 256, 0, s>>>(J, bc, terms);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        ygpu_set_error("Jacobian kernel: %s", cudaGetErrorString(e));
+        return YGPU_ERR_CUDA;
+    }
+    ygpu_count_launches(1);
+    return YGPU_OK;
+}

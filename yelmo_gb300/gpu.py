@@ -40,6 +40,8 @@ EXPORTS = [
     "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get", "ygpu_tuning_defaults",
     "ygpu_ctx_set_tuning", "ygpu_set_neff_hook", "ygpu_solve_batch_host", "ygpu_calc_dyn_diagnostics",
     "ygpu_calc_dyn_diagnostics_device", "ygpu_calc_advec2D_impl_lis", "ygpu_advec2D_impl_lis_device",
+    "ygpu_calc_gradient_column_ac", "ygpu_calc_gradient_column_ac_device", "ygpu_calc_jacobian_vel_3D",
+    "ygpu_calc_jacobian_vel_3D_device",
 ]
 
 
@@ -90,6 +92,10 @@ def lib(build_if_missing: bool = True):
     L.ygpu_advec2D_impl_lis_device.argtypes = [C.c_void_p] + [C.c_void_p] * 7 + [C.c_double, C.c_double, C.c_double,
                                                                               C.c_int, C.c_int, C.c_int, ip, ip]
     L.ygpu_linear_solver_matrix_solve.argtypes = [C.c_int, ip, ip, dp, dp, dp, C.c_char_p, ip, ip, dp]
+    L.ygpu_calc_gradient_column_ac.argtypes = [dp] * 5 + [ip, C.c_int, C.c_int, C.c_int]
+    L.ygpu_calc_gradient_column_ac_device.argtypes = [C.c_void_p] * 7 + [C.c_int, C.c_int, C.c_int]
+    L.ygpu_calc_jacobian_vel_3D.argtypes = [C.POINTER(abi.JVel), C.c_int, C.c_int]
+    L.ygpu_calc_jacobian_vel_3D_device.argtypes = [C.c_void_p, C.POINTER(abi.JVel), C.c_int, C.c_int]
     L.ygpu_server_create.restype = C.c_void_p
     L.ygpu_server_create.argtypes = [C.POINTER(abi.ServerCfg)]
     L.ygpu_server_destroy.argtypes = [C.c_void_p]
@@ -235,6 +241,42 @@ def calc_advec2D_impl_lis(var, ux, uy, var_dot, mask_ice, var_ref, dx: float, dy
     _check(r)
     return dvdt, it.value, st.value
 
+
+def calc_gradient_column_ac(dvdx, dvdy, f_ice, mask_ocn, boundaries: str):
+    """calc_gradient_column_ac on the GPU: (dvdx_c, dvdy_c). mask_ocn: nonzero
+    where the bed lies below sea level."""
+    nx, ny = f_ice.shape
+    gx = np.zeros((nx, ny), order="F")
+    gy = np.zeros((nx, ny), order="F")
+    ocn = np.asfortranarray(mask_ocn, dtype=np.int32)
+    _check(lib().ygpu_calc_gradient_column_ac(abi.ptr(gx, "d"), abi.ptr(gy, "d"), abi.ptr(dvdx, "d"),
+                                              abi.ptr(dvdy, "d"), abi.ptr(f_ice, "d"), abi.ptr(ocn, "i"),
+                                              abi.BOUNDARY_CODES[boundaries], nx, ny))
+    return gx, gy
+
+
+def jacobian_arrays(inputs: dict, terms: int = abi.JAC_UXY | abi.JAC_UZ) -> dict:
+    """`inputs` (JAC_INPUTS names) with zeroed output arrays for `terms`."""
+    nx, ny = inputs["H_ice"].shape
+    out = dict(inputs)
+    nza = inputs["zeta_aa"].shape[0] if "zeta_aa" in inputs else 0
+    nzc = inputs["zeta_ac"].shape[0] if "zeta_ac" in inputs else 0
+    if terms & abi.JAC_UXY:
+        for n in abi.JAC_OUTPUTS[:6]:
+            out[n] = np.zeros((nx, ny, nza), order="F")
+    if nzc:
+        for n in abi.JAC_OUTPUTS[6:]:
+            out[n] = np.zeros((nx, ny, nzc), order="F")
+    return out
+
+
+def calc_jacobian_vel_3D(arrays: dict, dx: float, dy: float, boundaries: str,
+                         terms: int = abi.JAC_UXY | abi.JAC_UZ) -> dict:
+    """Velocity Jacobian on the GPU (ygpu_calc_jacobian_vel_3D); the output arrays
+    of `arrays` (see jacobian_arrays) are filled in place."""
+    J = abi.jvel(arrays, dx, dy)
+    _check(lib().ygpu_calc_jacobian_vel_3D(C.byref(J), abi.BOUNDARY_CODES[boundaries], int(terms)))
+    return arrays
 
 def calc_dyn_inputs(inst) -> dict:
     d = inst.input_buffers()
