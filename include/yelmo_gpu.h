@@ -297,8 +297,10 @@ int ygpu_calc_gradient_column_ac_device(void* stream, double* dvdx_c, double* dv
  * ux, uy and the six ux/uy components are (nx,ny,nz_aa); uz and dzx, dzy, dzz are
  * (nx,ny,nz_ac). dzsdx ... dzbdy are the column gradients
  * (ygpu_calc_gradient_column_ac). f_grnd, an argument of both reference routines,
- * is read by neither and is not taken. nz_aa >= 3 and nz_ac >= 3. FP64 without
- * contraction: bit-exact with a CPU evaluation of the same expressions.
+ * is read by neither and is not taken. 3 <= nz_aa, nz_ac <= 1000. FP64; the
+ * layer loops carry no division (the vertical derivative in difference form with
+ * per-layer weights, reciprocals of dx, dy and H), so results agree with the
+ * reference expressions to rounding, not bit for bit.
  */
 #define YGPU_JAC_UXY 1
 #define YGPU_JAC_UZ  2

@@ -1297,7 +1297,7 @@ extern "C" int ygpu_calc_gradient_column_ac(double* dvdx_c, double* dvdy_c, cons
 
 static int jacobian_check(const ygpu_jvel* J, int bc, int terms) {
     if (!J || J->nx < 2 || J->ny < 2 || !(J->dx > 0.0) || !(J->dy > 0.0) || bc < 0 || bc > 6 || terms < 1 ||
-        terms > 3 || (size_t)J->nx * J->ny > (size_t)(1 << 28)) {
+        terms > 3 || (size_t)J->nx * J->ny > (size_t)(1 << 28) || J->nz_aa > 1000 || J->nz_ac > 1000) {
         ygpu_set_error("bad arguments");
         return YGPU_ERR_BAD_ARG;
     }

@@ -416,82 +416,122 @@ YG_DEV bool jac_act_y(const double* f, int a, int b, int nx, int ny, int bc) {
     return f[a + nx * b] == 1.0 || f[a + nx * bp1] == 1.0;
 }
 
-// deriv_active (deformation.f90:1346-1368)
-YG_DEV double jac_deriv_active(double vm, double v0, double vp, bool am, bool ap, double h) {
-    if (am && ap) return (vp - vm) / (2.0 * h);
-    if (ap) return (vp - v0) / h;
-    if (am) return (v0 - vm) / h;
-    return 0.0;
-}
-
-// mean4_active (deformation.f90:1370-1391)
+// mean4_active (deformation.f90:1370-1391); the count's reciprocal from a table
 YG_DEV double jac_mean4(double v1, double v2, double v3, double v4, bool a1, bool a2, bool a3, bool a4) {
     const int n = (int)a1 + (int)a2 + (int)a3 + (int)a4;
-    if (n == 0) return 0.0;
     double s = (a1 ? v1 : 0.0) + (a2 ? v2 : 0.0);
     s = s + (a3 ? v3 : 0.0);
     s = s + (a4 ? v4 : 0.0);
-    return s / (double)n;
+    const double r = n == 4 ? 0.25 : n == 2 ? 0.5 : n == 1 ? 1.0 : n == 3 ? (1.0 / 3.0) : 0.0;
+    return s * r;
 }
 
-// First derivative in z at layer k of a column with heights z (scaled by the
-// thickness Hn): three-point unequal-spacing formulas (Singh and Bhadauria),
-// one-sided at the base and, with top3, at the top; else first order there.
-YG_DEV double jac_dz(const double* __restrict__ u, const double* __restrict__ z, size_t c, size_t n2, int k, int nz,
-                     double Hn, bool top3) {
-    auto U = [&](int kk) { return __ldg(u + (size_t)kk * n2 + c); };
+// FP64 on this GPU issues at 2 FMA per clock per SM, so the Jacobian keeps every
+// division out of its layer loops. The three-point unequal-spacing derivative of
+// the reference (Singh and Bhadauria; deformation.f90:508-540, :805-836) is
+// rewritten in difference form,
+//     du/dz (k) = (a_k (u[p] - u[p-1]) + b_k (u[p+1] - u[p])) / H,  p = clamp(k, 1, nz-2),
+// with the layer weights a_k, b_k of the zeta spacing (the same polynomial, the
+// thickness factored out). The top layer of uz takes the first-order difference
+// (a = 0). The weights are computed once per block into shared memory.
+YG_DEV void jac_layer_weights(const double* z, int nz, int k, bool top3, double& a, double& b) {
     if (k == 0) {
-        const double h1 = Hn * (z[1] - z[0]), h2 = Hn * (z[2] - z[1]);
-        return -(2.0 * h1 + h2) / (h1 * (h1 + h2)) * U(0) + (h1 + h2) / (h1 * h2) * U(1) -
-               h1 / (h2 * (h1 + h2)) * U(2);
+        const double d1 = z[1] - z[0], d2 = z[2] - z[1];
+        a = (2.0 * d1 + d2) / (d1 * (d1 + d2));
+        b = -d1 / (d2 * (d1 + d2));
+    } else if (k < nz - 1) {
+        const double d1 = z[k] - z[k - 1], d2 = z[k + 1] - z[k];
+        a = d2 / (d1 * (d1 + d2));
+        b = d1 / (d2 * (d1 + d2));
+    } else if (top3) {
+        const double d1 = z[k - 1] - z[k - 2], d2 = z[k] - z[k - 1];
+        a = -d2 / (d1 * (d1 + d2));
+        b = (d1 + 2.0 * d2) / (d2 * (d1 + d2));
+    } else {
+        a = 0.0;
+        b = 1.0 / (z[k] - z[k - 1]);
     }
-    if (k < nz - 1) {
-        const double h1 = Hn * (z[k] - z[k - 1]), h2 = Hn * (z[k + 1] - z[k]);
-        return -h2 / (h1 * (h1 + h2)) * U(k - 1) - (h1 - h2) / (h1 * h2) * U(k) + h1 / (h2 * (h1 + h2)) * U(k + 1);
-    }
-    if (!top3) return (U(k) - U(k - 1)) / (Hn * (z[k] - z[k - 1]));
-    const double h1 = Hn * (z[k - 1] - z[k - 2]), h2 = Hn * (z[k] - z[k - 1]);
-    return h2 / (h1 * (h1 + h2)) * U(k - 2) - (h1 + h2) / (h1 * h2) * U(k - 1) +
-           (h1 + 2.0 * h2) / (h2 * (h1 + h2)) * U(k);
 }
 
-// Margin stencil of a derivative along one direction at cell c: 0 centred,
-// 1 three-point backward, 2 two-point backward, 3 three-point forward,
-// 4 two-point forward, 5 zero.
-YG_DEV double jac_dh(int mode, double um2, double um1, double u0, double up1, double up2, double h) {
+// Running pair of layer differences (u[p] - u[p-1], u[p+1] - u[p]) of one column
+struct JacWindow {
+    const double* u;
+    size_t c, n2;
+    int p, nz;
+    double up, dA, dB;
+    YG_DEV void init(const double* u_, size_t c_, size_t n2_, int nz_) {
+        u = u_; c = c_; n2 = n2_; nz = nz_; p = 1;
+        const double u0 = __ldg(u + c), u1 = __ldg(u + n2 + c);
+        up = __ldg(u + 2 * n2 + c);
+        dA = u1 - u0;
+        dB = up - u1;
+    }
+    // the derivative at layer k (k ascending), times rH = 1/H
+    YG_DEV double at(int k, double a, double b, double rH) {
+        if (k > p && k < nz - 1) {
+            p = k;
+            const double un = __ldg(u + (size_t)(k + 1) * n2 + c);
+            dA = dB;
+            dB = un - up;
+            up = un;
+        }
+        return fma(b, dB, a * dA) * rH;
+    }
+};
+
+// Margin stencil of a derivative along one direction: 0 centred, 1 three-point
+// backward, 2 two-point backward, 3 three-point forward, 4 two-point forward,
+// 5 zero (deformation.f90:590-637, :866-929). r1 = 1/h, r2 = 1/(2h).
+YG_DEV double jac_dh(int mode, double um2, double um1, double u0, double up1, double up2, double r1, double r2) {
     switch (mode) {
-        case 1: return (1.0 * um2 - 4.0 * um1 + 3.0 * u0) / (2.0 * h);
-        case 2: return (u0 - um1) / h;
-        case 3: return -(1.0 * up2 - 4.0 * up1 + 3.0 * u0) / (2.0 * h);
-        case 4: return (up1 - u0) / h;
+        case 1: return fma(3.0, u0, fma(-4.0, um1, um2)) * r2;
+        case 2: return (u0 - um1) * r1;
+        case 3: return -(fma(3.0, u0, fma(-4.0, up1, up2)) * r2);
+        case 4: return (up1 - u0) * r1;
         case 5: return 0.0;
-        default: return (up1 - um1) / (2.0 * h);
+        default: return (up1 - um1) * r2;
     }
 }
+
+// deriv_active (deformation.f90:1346-1368) with the reciprocals of h and 2h
+YG_DEV double jac_deriv_active(double vm, double v0, double vp, bool am, bool ap, double r1, double r2) {
+    if (am && ap) return (vp - vm) * r2;
+    if (ap) return (vp - v0) * r1;
+    if (am) return (v0 - vm) * r1;
+    return 0.0;
+}
+
+struct JacConst {
+    double rdx, r2dx, rdy, r2dy;
+    const double *wa_aa, *wb_aa, *z_aa, *wa_ac, *wb_ac, *z_ac;   // shared memory
+};
 
 // calc_jacobian_vel_3D_uxyterms (deformation.f90:397-716) for the column at (i, j)
-YG_DEV void jac_uxy_column(const ygpu_jvel& J, int bc, int i, int j, int im1, int ip1, int jm1, int jp1) {
+YG_DEV void jac_uxy_column(const ygpu_jvel& J, const JacConst& K, int bc, int i, int j, int im1, int ip1, int jm1,
+                           int jp1) {
     const int nx = J.nx, ny = J.ny, nz = J.nz_aa;
     const size_t n2 = (size_t)nx * ny, c = (size_t)i + (size_t)nx * j;
     const double* __restrict__ f = J.f_ice;
     const double* __restrict__ H = J.H_ice;
     const size_t cxp = ip1 + (size_t)nx * j, cxm = im1 + (size_t)nx * j;
     const size_t cyp = i + (size_t)nx * jp1, cym = i + (size_t)nx * jm1;
-    const bool ice = f[c] == 1.0;
+    const bool ice = f[c] == 1.0, ice_xp = f[cxp] == 1.0, ice_yp = f[cyp] == 1.0;
+    const bool less = f[c] < 1.0, less_xp = f[cxp] < 1.0, less_yp = f[cyp] < 1.0;
     // face thicknesses (:473-487)
     double Hx, Hy;
-    if (ice && f[cxp] < 1.0) Hx = H[c];
-    else if (f[c] < 1.0 && f[cxp] == 1.0) Hx = H[cxp];
+    if (ice && less_xp) Hx = H[c];
+    else if (less && ice_xp) Hx = H[cxp];
     else Hx = 0.5 * (H[c] + H[cxp]);
-    if (ice && f[cyp] < 1.0) Hy = H[c];
-    else if (f[c] < 1.0 && f[cyp] == 1.0) Hy = H[cyp];
+    if (ice && less_yp) Hy = H[c];
+    else if (less && ice_yp) Hy = H[cyp];
     else Hy = 0.5 * (H[c] + H[cyp]);
+    const double rHx = Hx > 0.0 ? 1.0 / Hx : 0.0, rHy = Hy > 0.0 ? 1.0 / Hy : 0.0;
     // margin stencils of dxx and dyy (:590-637)
     int mx = 0, my = 0;
-    if (ice && f[cxp] < 1.0) mx = (im1 > 0 && f[cxm] == 1.0) ? 1 : 2;
-    else if (f[c] < 1.0 && f[cxp] == 1.0) mx = (ip1 < nx - 1 && f[cxp + 1] == 1.0) ? 3 : 4;
-    if (ice && f[cyp] < 1.0) my = (jm1 > 0 && f[cym] == 1.0) ? 1 : 2;
-    else if (f[c] < 1.0 && f[cyp] == 1.0) my = (jp1 < ny - 1 && f[cyp + nx] == 1.0) ? 3 : 4;
+    if (ice && less_xp) mx = (im1 > 0 && f[cxm] == 1.0) ? 1 : 2;
+    else if (less && ice_xp) mx = (ip1 < nx - 1 && f[cxp + 1] == 1.0) ? 3 : 4;
+    if (ice && less_yp) my = (jm1 > 0 && f[cym] == 1.0) ? 1 : 2;
+    else if (less && ice_yp) my = (jp1 < ny - 1 && f[cyp + nx] == 1.0) ? 3 : 4;
     // faces with a velocity solution and the cross gradients over them (:654-666)
     const bool ax_jm1 = jac_act_x(f, i, jm1, nx, ny, bc), ax_jp1 = jac_act_x(f, i, jp1, nx, ny, bc);
     const bool ax_0 = jac_act_x(f, i, j, nx, ny, bc), ax_im1 = jac_act_x(f, im1, j, nx, ny, bc);
@@ -504,38 +544,36 @@ YG_DEV void jac_uxy_column(const ygpu_jvel& J, int bc, int i, int j, int im1, in
     const double* sx = J.dzsdx;
     const double* sy = J.dzsdy;
     const size_t cxm_yp = im1 + (size_t)nx * jp1, cxp_ym = ip1 + (size_t)nx * jm1;
-    const double dzbdx_acy = jac_mean4(bx[c], bx[cyp], bx[cxm], bx[cxm_yp], ax_0, ax_jp1, ax_im1, ax_im1_jp1);
-    const double dzsdx_acy = jac_mean4(sx[c], sx[cyp], sx[cxm], sx[cxm_yp], ax_0, ax_jp1, ax_im1, ax_im1_jp1);
-    const double dzbdy_acx = jac_mean4(by[c], by[cxp], by[cym], by[cxp_ym], ay_0, ay_ip1, ay_jm1, ay_ip1_jm1);
-    const double dzsdy_acx = jac_mean4(sy[c], sy[cxp], sy[cym], sy[cxp_ym], ay_0, ay_ip1, ay_jm1, ay_ip1_jm1);
-    const double bxc = bx[c], byc = by[c], sxc = sx[c], syc = sy[c];
+    const double bx_acy = jac_mean4(bx[c], bx[cyp], bx[cxm], bx[cxm_yp], ax_0, ax_jp1, ax_im1, ax_im1_jp1);
+    const double sx_acy = jac_mean4(sx[c], sx[cyp], sx[cxm], sx[cxm_yp], ax_0, ax_jp1, ax_im1, ax_im1_jp1);
+    const double by_acx = jac_mean4(by[c], by[cxp], by[cym], by[cxp_ym], ay_0, ay_ip1, ay_jm1, ay_ip1_jm1);
+    const double sy_acx = jac_mean4(sy[c], sy[cxp], sy[cym], sy[cxp_ym], ay_0, ay_ip1, ay_jm1, ay_ip1_jm1);
+    // sigma-transform factors (:639-675): c(zeta) = -((1-zeta) b + zeta s) = -(b + zeta (s - b))
+    const double bxc = bx[c], byc = by[c];
+    const double gxc = sx[c] - bxc, gyc = sy[c] - byc, gx_acy = sx_acy - bx_acy, gy_acx = sy_acx - by_acx;
     const double* __restrict__ ux = J.ux;
     const double* __restrict__ uy = J.uy;
+    JacWindow wx, wy;
+    wx.init(ux, c, n2, nz);
+    wy.init(uy, c, n2, nz);
     for (int k = 0; k < nz; k++) {
         const size_t o = (size_t)k * n2;
-        const double dxz = (Hx > 0.0) ? jac_dz(ux, J.zeta_aa, c, n2, k, nz, Hx, true) : 0.0;
-        const double dyz = (Hy > 0.0) ? jac_dz(uy, J.zeta_aa, c, n2, k, nz, Hy, true) : 0.0;
+        const double wa = K.wa_aa[k], wb = K.wb_aa[k], zk = K.z_aa[k];
+        const double dxz = (Hx > 0.0) ? wx.at(k, wa, wb, rHx) : 0.0;
+        const double dyz = (Hy > 0.0) ? wy.at(k, wa, wb, rHy) : 0.0;
         const double* uxk = ux + o;
         const double* uyk = uy + o;
         const double x0 = __ldg(uxk + c), y0 = __ldg(uyk + c);
-        const double xm1 = __ldg(uxk + cxm), xp1 = __ldg(uxk + cxp);
-        const double ym1 = __ldg(uyk + cym), yp1 = __ldg(uyk + cyp);
         const double xm2 = (mx == 1) ? __ldg(uxk + cxm - 1) : 0.0, xp2 = (mx == 3) ? __ldg(uxk + cxp + 1) : 0.0;
         const double ym2 = (my == 1) ? __ldg(uyk + cym - nx) : 0.0, yp2 = (my == 3) ? __ldg(uyk + cyp + nx) : 0.0;
-        double dxx = jac_dh(mx, xm2, xm1, x0, xp1, xp2, J.dx);
-        double dyy = jac_dh(my, ym2, ym1, y0, yp1, yp2, J.dy);
-        double dxy = jac_deriv_active(__ldg(uxk + cym), x0, __ldg(uxk + cyp), ax_jm1, ax_jp1, J.dy);
-        double dyx = jac_deriv_active(__ldg(uyk + cxm), y0, __ldg(uyk + cxp), ay_im1, ay_ip1, J.dx);
-        // sigma-transform corrections (:639-675)
-        const double zk = J.zeta_aa[k];
-        const double c_x = -((1.0 - zk) * bxc + zk * sxc);
-        const double c_y = -((1.0 - zk) * byc + zk * syc);
-        const double c_x_acy = -((1.0 - zk) * dzbdx_acy + zk * dzsdx_acy);
-        const double c_y_acx = -((1.0 - zk) * dzbdy_acx + zk * dzsdy_acx);
-        dxx = dxx + c_x * dxz;
-        dxy = dxy + c_y_acx * dxz;
-        dyx = dyx + c_x_acy * dyz;
-        dyy = dyy + c_y * dyz;
+        double dxx = jac_dh(mx, xm2, __ldg(uxk + cxm), x0, __ldg(uxk + cxp), xp2, K.rdx, K.r2dx);
+        double dyy = jac_dh(my, ym2, __ldg(uyk + cym), y0, __ldg(uyk + cyp), yp2, K.rdy, K.r2dy);
+        double dxy = jac_deriv_active(__ldg(uxk + cym), x0, __ldg(uxk + cyp), ax_jm1, ax_jp1, K.rdy, K.r2dy);
+        double dyx = jac_deriv_active(__ldg(uyk + cxm), y0, __ldg(uyk + cxp), ay_im1, ay_ip1, K.rdx, K.r2dx);
+        dxx = fma(-fma(zk, gxc, bxc), dxz, dxx);
+        dxy = fma(-fma(zk, gy_acx, by_acx), dxz, dxy);
+        dyx = fma(-fma(zk, gx_acy, bx_acy), dyz, dyx);
+        dyy = fma(-fma(zk, gyc, byc), dyz, dyy);
         J.dxx[o + c] = dxx;
         J.dxy[o + c] = dxy;
         J.dxz[o + c] = dxz;
@@ -546,11 +584,11 @@ YG_DEV void jac_uxy_column(const ygpu_jvel& J, int bc, int i, int j, int im1, in
 }
 
 // calc_jacobian_vel_3D_uzterms (deformation.f90:718-961) for the column at (i, j)
-YG_DEV void jac_uz_column(const ygpu_jvel& J, int i, int j, int im1, int ip1, int jm1, int jp1) {
+YG_DEV void jac_uz_column(const ygpu_jvel& J, const JacConst& K, int i, int j, int im1, int ip1, int jm1, int jp1) {
     const int nx = J.nx, ny = J.ny, nz = J.nz_ac;
     const size_t n2 = (size_t)nx * ny, c = (size_t)i + (size_t)nx * j;
     const double* __restrict__ f = J.f_ice;
-    if (f[c] != 1.0) {
+    if (!(f[c] == 1.0)) {
         for (int k = 0; k < nz; k++) {
             const size_t o = (size_t)k * n2 + c;
             J.dzx[o] = 0.0;
@@ -561,35 +599,37 @@ YG_DEV void jac_uz_column(const ygpu_jvel& J, int i, int j, int im1, int ip1, in
     }
     const size_t cxp = ip1 + (size_t)nx * j, cxm = im1 + (size_t)nx * j;
     const size_t cyp = i + (size_t)nx * jp1, cym = i + (size_t)nx * jm1;
+    const bool ixp = f[cxp] == 1.0, ixm = f[cxm] == 1.0, iyp = f[cyp] == 1.0, iym = f[cym] == 1.0;
+    const bool lxp = f[cxp] < 1.0, lxm = f[cxm] < 1.0, lyp = f[cyp] < 1.0, lym = f[cym] < 1.0;
     int mx = 0, my = 0;
-    if (f[cxp] < 1.0 && f[cxm] < 1.0) mx = 5;
-    else if (f[cxp] < 1.0 && f[cxm] == 1.0) mx = (im1 > 0 && f[cxm - 1] == 1.0) ? 1 : 2;
-    else if (f[cxp] == 1.0 && f[cxm] < 1.0) mx = (ip1 < nx - 1 && f[cxp + 1] == 1.0) ? 3 : 4;
-    if (f[cyp] < 1.0 && f[cym] < 1.0) my = 5;
-    else if (f[cyp] < 1.0 && f[cym] == 1.0) my = (jm1 > 0 && f[cym - nx] == 1.0) ? 1 : 2;
-    else if (f[cyp] == 1.0 && f[cym] < 1.0) my = (jp1 < ny - 1 && f[cyp + nx] == 1.0) ? 3 : 4;
-    const double Hn = J.H_ice[c];
-    const double dzbdx_aa = 0.5 * (J.dzbdx[c] + J.dzbdx[cxm]);
-    const double dzbdy_aa = 0.5 * (J.dzbdy[c] + J.dzbdy[cym]);
-    const double dzsdx_aa = 0.5 * (J.dzsdx[c] + J.dzsdx[cxm]);
-    const double dzsdy_aa = 0.5 * (J.dzsdy[c] + J.dzsdy[cym]);
+    if (lxp && lxm) mx = 5;
+    else if (lxp && ixm) mx = (im1 > 0 && f[cxm - 1] == 1.0) ? 1 : 2;
+    else if (ixp && lxm) mx = (ip1 < nx - 1 && f[cxp + 1] == 1.0) ? 3 : 4;
+    if (lyp && lym) my = 5;
+    else if (lyp && iym) my = (jm1 > 0 && f[cym - nx] == 1.0) ? 1 : 2;
+    else if (iyp && lym) my = (jp1 < ny - 1 && f[cyp + nx] == 1.0) ? 3 : 4;
+    const double rH = 1.0 / J.H_ice[c];
+    // correction factors on the cell (:935-944)
+    const double bxa = 0.5 * (J.dzbdx[c] + J.dzbdx[cxm]), bya = 0.5 * (J.dzbdy[c] + J.dzbdy[cym]);
+    const double gxa = 0.5 * (J.dzsdx[c] + J.dzsdx[cxm]) - bxa, gya = 0.5 * (J.dzsdy[c] + J.dzsdy[cym]) - bya;
     const double* __restrict__ uz = J.uz;
+    JacWindow wz;
+    wz.init(uz, c, n2, nz);
     for (int k = 0; k < nz; k++) {
         const size_t o = (size_t)k * n2;
         const double* uzk = uz + o;
-        const double dzz = jac_dz(uz, J.zeta_ac, c, n2, k, nz, Hn, false);
+        const double dzz = wz.at(k, K.wa_ac[k], K.wb_ac[k], rH);
         const double z0 = __ldg(uzk + c);
-        double dzx = (mx == 5) ? 0.0
-                               : jac_dh(mx, (mx == 1) ? __ldg(uzk + cxm - 1) : 0.0, __ldg(uzk + cxm), z0,
-                                        __ldg(uzk + cxp), (mx == 3) ? __ldg(uzk + cxp + 1) : 0.0, J.dx);
-        double dzy = (my == 5) ? 0.0
-                               : jac_dh(my, (my == 1) ? __ldg(uzk + cym - nx) : 0.0, __ldg(uzk + cym), z0,
-                                        __ldg(uzk + cyp), (my == 3) ? __ldg(uzk + cyp + nx) : 0.0, J.dy);
-        const double zk = J.zeta_ac[k];
-        const double c_x = -((1.0 - zk) * dzbdx_aa + zk * dzsdx_aa);
-        const double c_y = -((1.0 - zk) * dzbdy_aa + zk * dzsdy_aa);
-        dzx = dzx + c_x * dzz;
-        dzy = dzy + c_y * dzz;
+        double dzx = 0.0, dzy = 0.0;
+        if (mx != 5)
+            dzx = jac_dh(mx, (mx == 1) ? __ldg(uzk + cxm - 1) : 0.0, __ldg(uzk + cxm), z0, __ldg(uzk + cxp),
+                         (mx == 3) ? __ldg(uzk + cxp + 1) : 0.0, K.rdx, K.r2dx);
+        if (my != 5)
+            dzy = jac_dh(my, (my == 1) ? __ldg(uzk + cym - nx) : 0.0, __ldg(uzk + cym), z0, __ldg(uzk + cyp),
+                         (my == 3) ? __ldg(uzk + cyp + nx) : 0.0, K.rdy, K.r2dy);
+        const double zk = K.z_ac[k];
+        dzx = fma(-fma(zk, gxa, bxa), dzz, dzx);
+        dzy = fma(-fma(zk, gya, bya), dzz, dzy);
         J.dzx[o + c] = dzx;
         J.dzy[o + c] = dzy;
         J.dzz[o + c] = dzz;
@@ -597,16 +637,39 @@ YG_DEV void jac_uz_column(const ygpu_jvel& J, int i, int j, int im1, int ip1, in
 }
 
 // One thread per column: the ux/uy terms, then the uz terms (or the zeroing of
-// dzx, dzy, dzz that the ux/uy routine starts with).
+// dzx, dzy, dzz that the ux/uy routine starts with). Dynamic shared memory:
+// the layer weights and levels, 3 (nz_aa + nz_ac) doubles.
 __global__ void __launch_bounds__(256) k_jacobian(ygpu_jvel J, int bc, int terms) {
+    extern __shared__ double jac_sh[];
+    const int nza = (terms & YGPU_JAC_UXY) ? J.nz_aa : 0, nzc = (terms & YGPU_JAC_UZ) ? J.nz_ac : 0;
+    JacConst K;
+    double* wa_aa = jac_sh;
+    double* wb_aa = wa_aa + nza;
+    double* z_aa = wb_aa + nza;
+    double* wa_ac = z_aa + nza;
+    double* wb_ac = wa_ac + nzc;
+    double* z_ac = wb_ac + nzc;
+    for (int k = threadIdx.x; k < nza; k += blockDim.x) {
+        jac_layer_weights(J.zeta_aa, nza, k, true, wa_aa[k], wb_aa[k]);
+        z_aa[k] = J.zeta_aa[k];
+    }
+    for (int k = threadIdx.x; k < nzc; k += blockDim.x) {
+        jac_layer_weights(J.zeta_ac, nzc, k, false, wa_ac[k], wb_ac[k]);
+        z_ac[k] = J.zeta_ac[k];
+    }
+    __syncthreads();
+    K.wa_aa = wa_aa; K.wb_aa = wb_aa; K.z_aa = z_aa;
+    K.wa_ac = wa_ac; K.wb_ac = wb_ac; K.z_ac = z_ac;
+    K.rdx = 1.0 / J.dx; K.r2dx = 1.0 / (2.0 * J.dx);
+    K.rdy = 1.0 / J.dy; K.r2dy = 1.0 / (2.0 * J.dy);
     const int nx = J.nx, ny = J.ny, n2 = nx * ny;
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n2; c += gridDim.x * blockDim.x) {
         const int i = c % nx, j = c / nx;
         int im1, ip1, jm1, jp1;
         nbr_bc(i, j, nx, ny, bc, im1, ip1, jm1, jp1);
-        if (terms & YGPU_JAC_UXY) jac_uxy_column(J, bc, i, j, im1, ip1, jm1, jp1);
+        if (terms & YGPU_JAC_UXY) jac_uxy_column(J, K, bc, i, j, im1, ip1, jm1, jp1);
         if (terms & YGPU_JAC_UZ) {
-            jac_uz_column(J, i, j, im1, ip1, jm1, jp1);
+            jac_uz_column(J, K, i, j, im1, ip1, jm1, jp1);
         } else if (J.dzx) {
             for (int k = 0; k < J.nz_ac; k++) {
                 const size_t o = (size_t)k * n2 + c;
@@ -631,7 +694,9 @@ int ygpu_gradient_column_device(cudaStream_t s, double* gx_c, double* gy_c, cons
 }
 
 int ygpu_jacobian_device(cudaStream_t s, const ygpu_jvel& J, int bc, int terms) {
-    k_jacobian<<<grid_for(J.nx * J.ny), 256, 0, s>>>(J, bc, terms);
+    const int nza = (terms & YGPU_JAC_UXY) ? J.nz_aa : 0, nzc = (terms & YGPU_JAC_UZ) ? J.nz_ac : 0;
+    const size_t smem = 3 * sizeof(double) * (size_t)(nza + nzc);
+    k_jacobian<<<grid_for(J.nx * J.ny), 256, smem, s>>>(J, bc, terms);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         ygpu_set_error("Jacobian kernel: %s", cudaGetErrorString(e));
