@@ -479,26 +479,42 @@ struct JacWindow {
     }
 };
 
-// Margin stencil of a derivative along one direction: 0 centred, 1 three-point
-// backward, 2 two-point backward, 3 three-point forward, 4 two-point forward,
-// 5 zero (deformation.f90:590-637, :866-929). r1 = 1/h, r2 = 1/(2h).
-YG_DEV double jac_dh(int mode, double um2, double um1, double u0, double up1, double up2, double r1, double r2) {
+// A horizontal derivative as s1 (u[a] - u[b]) + s2 (u[cc] - u[d]) over the
+// offsets of one layer, chosen once per column so that the layer loop carries
+// no branch. Margin stencils (deformation.f90:590-637, :866-929): mode 0
+// centred, 1 three-point backward, 2 two-point backward, 3 three-point forward,
+// 4 two-point forward, 5 zero; r1 = 1/h, r2 = 1/(2h). The three-point forms
+// are the reference's (u[-2] - 4 u[-1] + 3 u[0]) / 2h regrouped as
+// 3/2h (u[0] - u[-1]) - 1/2h (u[-1] - u[-2]) (and mirrored).
+struct JacTap {
+    int a, b, cc, d;
+    double s1, s2;
+};
+
+YG_DEV JacTap jac_tap_margin(int mode, int m2, int m1, int c0, int p1, int p2, double r1, double r2) {
     switch (mode) {
-        case 1: return fma(3.0, u0, fma(-4.0, um1, um2)) * r2;
-        case 2: return (u0 - um1) * r1;
-        case 3: return -(fma(3.0, u0, fma(-4.0, up1, up2)) * r2);
-        case 4: return (up1 - u0) * r1;
-        case 5: return 0.0;
-        default: return (up1 - um1) * r2;
+        case 1: return {c0, m1, m1, m2, 3.0 * r2, -r2};
+        case 2: return {c0, m1, c0, c0, r1, 0.0};
+        case 3: return {p1, c0, p2, p1, 3.0 * r2, -r2};
+        case 4: return {p1, c0, c0, c0, r1, 0.0};
+        case 5: return {c0, c0, c0, c0, 0.0, 0.0};
+        default: return {p1, m1, c0, c0, r2, 0.0};
     }
 }
 
-// deriv_active (deformation.f90:1346-1368) with the reciprocals of h and 2h
-YG_DEV double jac_deriv_active(double vm, double v0, double vp, bool am, bool ap, double r1, double r2) {
-    if (am && ap) return (vp - vm) * r2;
-    if (ap) return (vp - v0) * r1;
-    if (am) return (v0 - vm) * r1;
-    return 0.0;
+// deriv_active (deformation.f90:1346-1368) as a one-difference tap
+YG_DEV JacTap jac_tap_active(int m, int c0, int p, bool am, bool ap, double r1, double r2) {
+    if (am && ap) return {p, m, c0, c0, r2, 0.0};
+    if (ap) return {p, c0, c0, c0, r1, 0.0};
+    if (am) return {c0, m, c0, c0, r1, 0.0};
+    return {c0, c0, c0, c0, 0.0, 0.0};
+}
+
+YG_DEV double jac_tap2(const JacTap& t, const double* __restrict__ u) {
+    return fma(t.s2, __ldg(u + t.cc) - __ldg(u + t.d), t.s1 * (__ldg(u + t.a) - __ldg(u + t.b)));
+}
+YG_DEV double jac_tap1(const JacTap& t, const double* __restrict__ u) {
+    return t.s1 * (__ldg(u + t.a) - __ldg(u + t.b));
 }
 
 struct JacConst {
@@ -553,6 +569,12 @@ YG_DEV void jac_uxy_column(const ygpu_jvel& J, const JacConst& K, int bc, int i,
     const double gxc = sx[c] - bxc, gyc = sy[c] - byc, gx_acy = sx_acy - bx_acy, gy_acx = sy_acx - by_acx;
     const double* __restrict__ ux = J.ux;
     const double* __restrict__ uy = J.uy;
+    // horizontal stencils of this column (offsets within a layer)
+    const int ic = (int)c, ixm = (int)cxm, ixp = (int)cxp, iym = (int)cym, iyp = (int)cyp;
+    const JacTap txx = jac_tap_margin(mx, mx == 1 ? ixm - 1 : ic, ixm, ic, ixp, mx == 3 ? ixp + 1 : ic, K.rdx, K.r2dx);
+    const JacTap tyy = jac_tap_margin(my, my == 1 ? iym - nx : ic, iym, ic, iyp, my == 3 ? iyp + nx : ic, K.rdy, K.r2dy);
+    const JacTap txy = jac_tap_active(iym, ic, iyp, ax_jm1, ax_jp1, K.rdy, K.r2dy);
+    const JacTap tyx = jac_tap_active(ixm, ic, ixp, ay_im1, ay_ip1, K.rdx, K.r2dx);
     JacWindow wx, wy;
     wx.init(ux, c, n2, nz);
     wy.init(uy, c, n2, nz);
@@ -563,13 +585,10 @@ YG_DEV void jac_uxy_column(const ygpu_jvel& J, const JacConst& K, int bc, int i,
         const double dyz = (Hy > 0.0) ? wy.at(k, wa, wb, rHy) : 0.0;
         const double* uxk = ux + o;
         const double* uyk = uy + o;
-        const double x0 = __ldg(uxk + c), y0 = __ldg(uyk + c);
-        const double xm2 = (mx == 1) ? __ldg(uxk + cxm - 1) : 0.0, xp2 = (mx == 3) ? __ldg(uxk + cxp + 1) : 0.0;
-        const double ym2 = (my == 1) ? __ldg(uyk + cym - nx) : 0.0, yp2 = (my == 3) ? __ldg(uyk + cyp + nx) : 0.0;
-        double dxx = jac_dh(mx, xm2, __ldg(uxk + cxm), x0, __ldg(uxk + cxp), xp2, K.rdx, K.r2dx);
-        double dyy = jac_dh(my, ym2, __ldg(uyk + cym), y0, __ldg(uyk + cyp), yp2, K.rdy, K.r2dy);
-        double dxy = jac_deriv_active(__ldg(uxk + cym), x0, __ldg(uxk + cyp), ax_jm1, ax_jp1, K.rdy, K.r2dy);
-        double dyx = jac_deriv_active(__ldg(uyk + cxm), y0, __ldg(uyk + cxp), ay_im1, ay_ip1, K.rdx, K.r2dx);
+        double dxx = jac_tap2(txx, uxk);
+        double dyy = jac_tap2(tyy, uyk);
+        double dxy = jac_tap1(txy, uxk);
+        double dyx = jac_tap1(tyx, uyk);
         dxx = fma(-fma(zk, gxc, bxc), dxz, dxx);
         dxy = fma(-fma(zk, gy_acx, by_acx), dxz, dxy);
         dyx = fma(-fma(zk, gx_acy, bx_acy), dyz, dyx);
@@ -599,19 +618,22 @@ YG_DEV void jac_uz_column(const ygpu_jvel& J, const JacConst& K, int i, int j, i
     }
     const size_t cxp = ip1 + (size_t)nx * j, cxm = im1 + (size_t)nx * j;
     const size_t cyp = i + (size_t)nx * jp1, cym = i + (size_t)nx * jm1;
-    const bool ixp = f[cxp] == 1.0, ixm = f[cxm] == 1.0, iyp = f[cyp] == 1.0, iym = f[cym] == 1.0;
+    const bool exp_ = f[cxp] == 1.0, exm = f[cxm] == 1.0, eyp = f[cyp] == 1.0, eym = f[cym] == 1.0;
     const bool lxp = f[cxp] < 1.0, lxm = f[cxm] < 1.0, lyp = f[cyp] < 1.0, lym = f[cym] < 1.0;
     int mx = 0, my = 0;
     if (lxp && lxm) mx = 5;
-    else if (lxp && ixm) mx = (im1 > 0 && f[cxm - 1] == 1.0) ? 1 : 2;
-    else if (ixp && lxm) mx = (ip1 < nx - 1 && f[cxp + 1] == 1.0) ? 3 : 4;
+    else if (lxp && exm) mx = (im1 > 0 && f[cxm - 1] == 1.0) ? 1 : 2;
+    else if (exp_ && lxm) mx = (ip1 < nx - 1 && f[cxp + 1] == 1.0) ? 3 : 4;
     if (lyp && lym) my = 5;
-    else if (lyp && iym) my = (jm1 > 0 && f[cym - nx] == 1.0) ? 1 : 2;
-    else if (iyp && lym) my = (jp1 < ny - 1 && f[cyp + nx] == 1.0) ? 3 : 4;
+    else if (lyp && eym) my = (jm1 > 0 && f[cym - nx] == 1.0) ? 1 : 2;
+    else if (eyp && lym) my = (jp1 < ny - 1 && f[cyp + nx] == 1.0) ? 3 : 4;
     const double rH = 1.0 / J.H_ice[c];
     // correction factors on the cell (:935-944)
     const double bxa = 0.5 * (J.dzbdx[c] + J.dzbdx[cxm]), bya = 0.5 * (J.dzbdy[c] + J.dzbdy[cym]);
     const double gxa = 0.5 * (J.dzsdx[c] + J.dzsdx[cxm]) - bxa, gya = 0.5 * (J.dzsdy[c] + J.dzsdy[cym]) - bya;
+    const int ic = (int)c, ixm = (int)cxm, ixp = (int)cxp, iym = (int)cym, iyp = (int)cyp;
+    const JacTap tzx = jac_tap_margin(mx, mx == 1 ? ixm - 1 : ic, ixm, ic, ixp, mx == 3 ? ixp + 1 : ic, K.rdx, K.r2dx);
+    const JacTap tzy = jac_tap_margin(my, my == 1 ? iym - nx : ic, iym, ic, iyp, my == 3 ? iyp + nx : ic, K.rdy, K.r2dy);
     const double* __restrict__ uz = J.uz;
     JacWindow wz;
     wz.init(uz, c, n2, nz);
@@ -619,17 +641,9 @@ YG_DEV void jac_uz_column(const ygpu_jvel& J, const JacConst& K, int i, int j, i
         const size_t o = (size_t)k * n2;
         const double* uzk = uz + o;
         const double dzz = wz.at(k, K.wa_ac[k], K.wb_ac[k], rH);
-        const double z0 = __ldg(uzk + c);
-        double dzx = 0.0, dzy = 0.0;
-        if (mx != 5)
-            dzx = jac_dh(mx, (mx == 1) ? __ldg(uzk + cxm - 1) : 0.0, __ldg(uzk + cxm), z0, __ldg(uzk + cxp),
-                         (mx == 3) ? __ldg(uzk + cxp + 1) : 0.0, K.rdx, K.r2dx);
-        if (my != 5)
-            dzy = jac_dh(my, (my == 1) ? __ldg(uzk + cym - nx) : 0.0, __ldg(uzk + cym), z0, __ldg(uzk + cyp),
-                         (my == 3) ? __ldg(uzk + cyp + nx) : 0.0, K.rdy, K.r2dy);
         const double zk = K.z_ac[k];
-        dzx = fma(-fma(zk, gxa, bxa), dzz, dzx);
-        dzy = fma(-fma(zk, gya, bya), dzz, dzy);
+        const double dzx = fma(-fma(zk, gxa, bxa), dzz, jac_tap2(tzx, uzk));
+        const double dzy = fma(-fma(zk, gya, bya), dzz, jac_tap2(tzy, uzk));
         J.dzx[o + c] = dzx;
         J.dzy[o + c] = dzy;
         J.dzz[o + c] = dzz;
