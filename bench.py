@@ -300,6 +300,61 @@ def jacobian_leg(device: str, steps: int, warmup: int) -> dict:
     return {"workload": "801x801, nz_aa 20, nz_ac 21, synthetic fields, ice on ~80 % of cells",
             "ms_per_call": ms, "alg_bytes_per_call": alg, "achieved_gbs": alg / (ms / 1e3) / 1e9, "kernels": 1}
 
+def vertical_velocity_leg(device: str, steps: int, warmup: int) -> dict:
+    """Time the vertical velocity (ygpu_calc_uz_3D_device, uz_method 1 and 4) on
+    one 801 x 801 field set resident in HBM: 20 layers, 21 interfaces, seeded
+    velocities and rates, ice on ~80 % of the cells, half of them with the column
+    rate of the thickness step, CUDA events on the launching stream. Algorithmic
+    bytes per cell: ux, uy (2 nz_aa words), uz, uz_star (2 nz_ac words), ten 2D
+    inputs and uz_srf_err, of 8 B; uz_flux adds ux_bar, uy_bar, dHidt_dyn and the
+    4-byte mask_kin."""
+    import ctypes as C
+    import torch
+    from yelmo_gb300 import abi, gpu
+    nx = ny = 801
+    nza, nzc = 20, 21
+    n2 = nx * ny
+    gen = torch.Generator(device=device).manual_seed(17)
+    r = lambda *s: torch.randn(*s, dtype=torch.float64, device=device, generator=gen)
+    f_ice = (torch.rand(n2, dtype=torch.float64, device=device, generator=gen) < 0.8).double()
+    za = torch.linspace(0.0, 1.0, nza, dtype=torch.float64, device=device) ** 2
+    zc = torch.cat([za[:1], 0.5 * (za[1:] + za[:-1]), za[-1:]])
+    a = {"ux": r(nza * n2) * 100.0, "uy": r(nza * n2) * 100.0, "H_ice": (r(n2).abs() * 1000.0 + 200.0) * f_ice,
+         "f_ice": f_ice, "smb": r(n2) * 0.3, "bmb": r(n2) * 0.1, "dzbdt": r(n2) * 0.01, "dzsdt": r(n2) * 0.1,
+         "dzsdx": r(n2) * 1e-3, "dzsdy": r(n2) * 1e-3, "dzbdx": r(n2) * 1e-2, "dzbdy": r(n2) * 1e-2,
+         "zeta_aa": za, "zeta_ac": zc, "ux_bar": r(n2) * 50.0, "uy_bar": r(n2) * 50.0, "dHidt_dyn": r(n2) * 0.1,
+         "mask_kin": (torch.rand(n2, device=device, generator=gen) < 0.5).int(),
+         "uz": torch.zeros(nzc * n2, dtype=torch.float64, device=device),
+         "uz_star": torch.zeros(nzc * n2, dtype=torch.float64, device=device),
+         "uz_srf_err": torch.zeros(n2, dtype=torch.float64, device=device)}
+    U = abi.Uz3D()
+    U.nx, U.ny, U.nz_aa, U.nz_ac, U.dx, U.dy, U.use_bmb = nx, ny, nza, nzc, 4e3, 4e3, 1
+    for n, t in a.items():
+        setattr(U, n, t.data_ptr())
+    L = gpu.lib()
+    stream = torch.cuda.current_stream(device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    out = {}
+    for name, method in (("uz_aa", abi.UZ_AA), ("uz_flux", abi.UZ_FLUX)):
+        times = []
+        for s in range(warmup + steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st = L.ygpu_calc_uz_3D_device(C.c_void_p(stream.cuda_stream), C.byref(U), 0, method)
+            e1.record(stream)
+            torch.cuda.synchronize(device)
+            if st != 0:
+                raise RuntimeError(f"vertical velocity failed ({st}): {gpu.last_error()}")
+            if s >= warmup:
+                times.append(e0.elapsed_time(e1))
+        ms = statistics.mean(times)
+        alg = float(n2) * (8.0 * (2 * nza + 2 * nzc + 11) + (28.0 if method == abi.UZ_FLUX else 0.0))
+        out[name] = {"ms_per_call": ms, "alg_bytes_per_call": alg, "achieved_gbs": alg / (ms / 1e3) / 1e9}
+    out["workload"] = "801x801, nz_aa 20, nz_ac 21, synthetic fields, ice on ~80 % of cells"
+    out["kernels"] = 1
+    return out
+
 def advection_leg(device: str, steps: int, warmup: int) -> dict:
     """Time calc_advec2D(impl-lis) on the device (ygpu_advec2D_impl_lis_device)
     on a 801 x 801 grid resident in HBM: seeded thickness, velocities and source,
@@ -637,6 +692,7 @@ def main():
     diag = diagnostics_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
     adv = advection_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
     jac = jacobian_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
+    uzl = vertical_velocity_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
     i0 = insts[0]
     io = [gpu.host_io_bytes(kind, i.nx, i.ny, i.nz) for i in insts]
     h2d, d2h = sum(a for a, _ in io), sum(b for _, b in io)
@@ -718,6 +774,8 @@ def main():
         "diagnostics": (dict(diag, frac=diag["achieved_gbs"] / peak) if diag else None),
         "advection": (dict(adv, frac=adv["achieved_gbs"] / peak) if adv else None),
         "jacobian": (dict(jac, frac=jac["achieved_gbs"] / peak) if jac else None),
+        "vertical_velocity": ({k: (dict(v, frac=v["achieved_gbs"] / peak) if isinstance(v, dict) else v)
+                               for k, v in uzl.items()} if uzl else None),
         "cpu_baseline": cpu_base,
     }
     print(json.dumps(line))

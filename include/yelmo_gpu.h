@@ -315,6 +315,41 @@ typedef struct ygpu_jvel {
     double *dxx, *dxy, *dxz, *dyx, *dyy, *dyz, *dzx, *dzy, *dzz;
 } ygpu_jvel;
 
+/*
+ * Vertical velocity of calc_ydyn (src/yelmo_dynamics.f90:259-290), by uz_method:
+ *   YGPU_UZ_AA   (1) calc_uz_3D_aa (src/physics/velocity_general.f90:683-945): uz
+ *                    integrated upward from the kinematic base value with the
+ *                    sigma-corrected horizontal divergence, and the advective
+ *                    uz_star = uz + coordinate terms;
+ *   YGPU_UZ_FLUX (4) calc_uz_3D_flux (:947-1116): uz_star from the layer mass budgets
+ *                    with upwind face thicknesses, corrected to the applied transport
+ *                    -dHidt_dyn where mask_kin == 1, and uz = uz_star - coordinate terms.
+ * uz_method 2 and 3 (calc_uz_3D, calc_uz_3D_jac) map fields to quadrature nodes with
+ * fesm-utils' gq2D/gq3D and are not built (YGPU_ERR_BAD_ARG). Ice-free cells take
+ * dzbdt - max(smb, 0). nz_ac = nz_aa + 1, 2 <= nz_aa <= 1000. ux_bar, uy_bar, dHidt_dyn
+ * and mask_kin are read by YGPU_UZ_FLUX only. uz_srf_err (optional, NULL to skip) is
+ * uz_star(:,:,nz_ac) + smb on the fully ice-covered cells and 0 elsewhere
+ * (yelmo_dynamics.f90:283-290). FP64, agreeing with the reference expressions to
+ * rounding.
+ */
+#define YGPU_UZ_AA   1
+#define YGPU_UZ_FLUX 4
+typedef struct ygpu_uz3d {
+    int nx, ny, nz_aa, nz_ac;
+    double dx, dy;
+    int use_bmb;
+    /* inputs */
+    const double *ux, *uy, *H_ice, *f_ice, *smb, *bmb, *dzbdt, *dzsdt;
+    const double *dzsdx, *dzsdy, *dzbdx, *dzbdy, *zeta_aa, *zeta_ac;
+    const double *ux_bar, *uy_bar, *dHidt_dyn;
+    const int* mask_kin;
+    /* outputs */
+    double *uz, *uz_star, *uz_srf_err;
+} ygpu_uz3d;
+
+int ygpu_calc_uz_3D(const ygpu_uz3d* f, int boundaries, int method);
+int ygpu_calc_uz_3D_device(void* stream, const ygpu_uz3d* f, int boundaries, int method);
+
 /* host arrays (staged through the calling thread's default context) */
 int ygpu_calc_jacobian_vel_3D(const ygpu_jvel* jvel, int boundaries, int terms);
 /* device arrays, on `stream` (a cudaStream_t; NULL: the default stream); asynchronous */

@@ -53,6 +53,7 @@ def lib():
         L.orc_calc_advec2D_impl_lis.restype = C.c_int
         L.orc_calc_gradient_column_ac.argtypes = [dp] * 5 + [ip, C.c_int, C.c_int, C.c_int]
         L.orc_calc_jacobian_vel_3D.argtypes = [C.POINTER(abi.JVel), C.c_int, C.c_int]
+        L.orc_calc_uz_3D.argtypes = [C.POINTER(abi.Uz3D), C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -180,6 +181,14 @@ def calc_jacobian_vel_3D(arrays: dict, dx: float, dy: float, boundaries: str, te
     st = lib().orc_calc_jacobian_vel_3D(C.byref(J), abi.BOUNDARY_CODES[boundaries], int(terms))
     if st != 0:
         raise RuntimeError(f"orc_calc_jacobian_vel_3D failed ({st})")
+    return arrays
+
+def calc_uz_3D(arrays: dict, dx: float, dy: float, boundaries: str, method: int = 1, use_bmb: bool = True) -> dict:
+    """orc_calc_uz_3D on the arrays of yelmo_gb300.gpu.uz_arrays (filled in place)."""
+    U = abi.uz3d(arrays, dx, dy, use_bmb)
+    st = lib().orc_calc_uz_3D(C.byref(U), abi.BOUNDARY_CODES[boundaries], int(method))
+    if st != 0:
+        raise RuntimeError(f"orc_calc_uz_3D failed ({st})")
     return arrays
 
 def linear_solve(ptr_, idx, val, b, x, method, precond, maxiter, tol, initx_zeros=False):

@@ -2663,6 +2663,171 @@ int orc_calc_jacobian_vel_3D(const ygpu_jvel* J, int bc, int terms) {
 }
 
 /* ======================================================================== */
+/* Vertical velocity (calc_ydyn, yelmo_dynamics.f90:259-290)                */
+/* ======================================================================== */
+
+static inline double flush_tiny(double v) { return fabs(v) < TOL_UNDERFLOW ? 0.0 : v; }
+
+/* calc_uz_3D_aa, velocity_general.f90:683-945 (0-based: ac level kc, aa layer ka) */
+static void uz_aa(const ygpu_uz3d* U, int bc) {
+    const int nx = U->nx, ny = U->ny, nza = U->nz_aa, nzc = U->nz_ac;
+    const size_t n2 = (size_t)nx * ny;
+    const double *za = U->zeta_aa, *zc = U->zeta_ac, *ux = U->ux, *uy = U->uy;
+    const double f_bmb = U->use_bmb ? 1.0 : 0.0;
+#pragma omp parallel for collapse(2)
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            int im1, ip1, jm1, jp1;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            const size_t c = ID2(i, j), cxm = ID2(im1, j), cym = ID2(i, jm1);
+            const double dzsdt_now = U->dzsdt[c], dzbdt_now = U->dzbdt[c];
+#define UX(ii, k) ux[(size_t)(k) * n2 + (ii)]
+#define UY(ii, k) uy[(size_t)(k) * n2 + (ii)]
+            if (U->f_ice[c] == 1.0) {
+                const double H_now = U->H_ice[c], H_inv = 1.0 / H_now;
+                const double dzbdx_aa = 0.5 * (U->dzbdx[c] + U->dzbdx[cxm]);
+                const double dzbdy_aa = 0.5 * (U->dzbdy[c] + U->dzbdy[cym]);
+                const double dzsdx_aa = 0.5 * (U->dzsdx[c] + U->dzsdx[cxm]);
+                const double dzsdy_aa = 0.5 * (U->dzsdy[c] + U->dzsdy[cym]);
+                double ux_aa = 0.5 * (UX(cxm, 0) + UX(c, 0));
+                double uy_aa = 0.5 * (UY(cym, 0) + UY(c, 0));
+                const double uz_grid = 0.0;
+                /* basal value, Greve and Blatter (2009) Eq. 5.31 */
+                double u0 = dzbdt_now + uz_grid + f_bmb * U->bmb[c] + ux_aa * dzbdx_aa + uy_aa * dzbdy_aa;
+                U->uz[c] = flush_tiny(u0);
+                for (int kc = 1; kc < nzc; kc++) {
+                    const int ka = kc - 1;
+                    const double duxdx_aa = (UX(c, ka) - UX(cxm, ka)) / U->dx;
+                    const double duydy_aa = (UY(c, ka) - UY(cym, ka)) / U->dy;
+                    double duxdz_aa, duydz_aa;
+                    int hi, lo;
+                    if (kc == 1) { hi = 1; lo = 0; }
+                    else if (kc == nzc - 1) { hi = nza - 1; lo = nza - 2; }
+                    else { hi = kc; lo = kc - 2; }
+                    duxdz_aa = (0.5 * (UX(c, hi) + UX(cxm, hi)) - 0.5 * (UX(c, lo) + UX(cxm, lo))) / (za[hi] - za[lo]);
+                    duydz_aa = (0.5 * (UY(c, hi) + UY(cym, hi)) - 0.5 * (UY(c, lo) + UY(cym, lo))) / (za[hi] - za[lo]);
+                    const double c_x = -H_inv * ((1.0 - zc[kc]) * dzbdx_aa + zc[kc] * dzsdx_aa);
+                    const double c_y = -H_inv * ((1.0 - zc[kc]) * dzbdy_aa + zc[kc] * dzsdy_aa);
+                    const double duxdx_now = duxdx_aa + c_x * duxdz_aa;
+                    const double duydy_now = duydy_aa + c_y * duydz_aa;
+                    const double u = U->uz[(size_t)(kc - 1) * n2 + c] - H_now * (zc[kc] - zc[kc - 1]) * (duxdx_now + duydy_now);
+                    U->uz[(size_t)kc * n2 + c] = flush_tiny(u);
+                }
+                /* uz_star, Greve and Blatter (2009) Eq. 5.148 (no 1/H) */
+                for (int kc = 0; kc < nzc; kc++) {
+                    if (kc == 0) {
+                        ux_aa = 0.5 * (UX(cxm, 0) + UX(c, 0));
+                        uy_aa = 0.5 * (UY(cym, 0) + UY(c, 0));
+                    } else if (kc == nzc - 1) {
+                        ux_aa = 0.5 * (UX(cxm, kc - 1) + UX(c, kc - 1));
+                        uy_aa = 0.5 * (UY(cym, kc - 1) + UY(c, kc - 1));
+                    } else {
+                        ux_aa = 0.25 * (UX(cxm, kc) + UX(c, kc) + UX(cxm, kc - 1) + UX(c, kc - 1));
+                        uy_aa = 0.25 * (UY(cym, kc) + UY(c, kc) + UY(cym, kc - 1) + UY(c, kc - 1));
+                    }
+                    const double z = zc[kc];
+                    const double c_x = -ux_aa * ((1.0 - z) * dzbdx_aa + z * dzsdx_aa);
+                    const double c_y = -uy_aa * ((1.0 - z) * dzbdy_aa + z * dzsdy_aa);
+                    const double c_t = -((1.0 - z) * dzbdt_now + z * dzsdt_now);
+                    U->uz_star[(size_t)kc * n2 + c] = flush_tiny(U->uz[(size_t)kc * n2 + c] + c_x + c_y + c_t);
+                }
+            } else {
+                for (int kc = 0; kc < nzc; kc++) {
+                    const double u = flush_tiny(dzbdt_now - fmax(U->smb[c], 0.0));
+                    U->uz[(size_t)kc * n2 + c] = u;
+                    U->uz_star[(size_t)kc * n2 + c] = u;
+                }
+            }
+        }
+}
+
+/* calc_uz_3D_flux, velocity_general.f90:947-1116 */
+static void uz_flux(const ygpu_uz3d* U, int bc) {
+    const int nx = U->nx, ny = U->ny, nza = U->nz_aa, nzc = U->nz_ac;
+    const size_t n2 = (size_t)nx * ny;
+    const double *zc = U->zeta_ac, *ux = U->ux, *uy = U->uy, *H = U->H_ice;
+    const double f_bmb = U->use_bmb ? 1.0 : 0.0;
+    double* dzeta = malloc((size_t)nza * sizeof(double));
+    for (int k = 0; k < nza; k++) dzeta[k] = zc[k + 1] - zc[k];
+#pragma omp parallel for collapse(2)
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            int im1, ip1, jm1, jp1;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            const size_t c = ID2(i, j), cxm = ID2(im1, j), cym = ID2(i, jm1);
+            const size_t cxp = ID2(ip1, j), cyp = ID2(i, jp1);
+            if (U->f_ice[c] == 1.0) {
+                const double Hx_w = (U->ux_bar[cxm] >= 0.0) ? H[cxm] : H[c];
+                const double Hx_e = (U->ux_bar[c] >= 0.0) ? H[c] : H[cxp];
+                const double Hy_s = (U->uy_bar[cym] >= 0.0) ? H[cym] : H[c];
+                const double Hy_n = (U->uy_bar[c] >= 0.0) ? H[c] : H[cyp];
+                double D[1001];
+                for (int k = 0; k < nza; k++)
+                    D[k] = dzeta[k] * ((Hx_e * UX(c, k) - Hx_w * UX(cxm, k)) / U->dx +
+                                       (Hy_n * UY(c, k) - Hy_s * UY(cym, k)) / U->dy);
+                if (U->mask_kin[c] == 1) {
+                    double tot = 0.0;
+                    for (int k = 0; k < nza; k++) tot += D[k];
+                    const double corr = -U->dHidt_dyn[c] - tot;
+                    for (int k = 0; k < nza; k++) D[k] = D[k] + dzeta[k] * corr;
+                }
+                const double dHdt = U->dzsdt[c] - U->dzbdt[c];
+                double* us = U->uz_star;
+                us[c] = f_bmb * U->bmb[c];
+                for (int k = 0; k < nza; k++)
+                    us[(size_t)(k + 1) * n2 + c] = us[(size_t)k * n2 + c] - dzeta[k] * dHdt - D[k];
+                const double dzbdx_aa = 0.5 * (U->dzbdx[c] + U->dzbdx[cxm]);
+                const double dzbdy_aa = 0.5 * (U->dzbdy[c] + U->dzbdy[cym]);
+                const double dzsdx_aa = 0.5 * (U->dzsdx[c] + U->dzsdx[cxm]);
+                const double dzsdy_aa = 0.5 * (U->dzsdy[c] + U->dzsdy[cym]);
+                for (int kc = 0; kc < nzc; kc++) {
+                    double ux_aa, uy_aa;
+                    if (kc == 0) {
+                        ux_aa = 0.5 * (UX(cxm, 0) + UX(c, 0));
+                        uy_aa = 0.5 * (UY(cym, 0) + UY(c, 0));
+                    } else if (kc == nzc - 1) {
+                        ux_aa = 0.5 * (UX(cxm, kc - 1) + UX(c, kc - 1));
+                        uy_aa = 0.5 * (UY(cym, kc - 1) + UY(c, kc - 1));
+                    } else {
+                        ux_aa = 0.25 * (UX(cxm, kc) + UX(c, kc) + UX(cxm, kc - 1) + UX(c, kc - 1));
+                        uy_aa = 0.25 * (UY(cym, kc) + UY(c, kc) + UY(cym, kc - 1) + UY(c, kc - 1));
+                    }
+                    const double z = zc[kc];
+                    const double c_x = -ux_aa * ((1.0 - z) * dzbdx_aa + z * dzsdx_aa);
+                    const double c_y = -uy_aa * ((1.0 - z) * dzbdy_aa + z * dzsdy_aa);
+                    const double c_t = -((1.0 - z) * U->dzbdt[c] + z * U->dzsdt[c]);
+                    const size_t o = (size_t)kc * n2 + c;
+                    U->uz[o] = flush_tiny(us[o] - (c_x + c_y + c_t));
+                    us[o] = flush_tiny(us[o]);
+                }
+            } else {
+                for (int kc = 0; kc < nzc; kc++) {
+                    const double u = flush_tiny(U->dzbdt[c] - fmax(U->smb[c], 0.0));
+                    U->uz[(size_t)kc * n2 + c] = u;
+                    U->uz_star[(size_t)kc * n2 + c] = u;
+                }
+            }
+#undef UX
+#undef UY
+        }
+    free(dzeta);
+}
+
+int orc_calc_uz_3D(const ygpu_uz3d* U, int bc, int method) {
+    if (!U || U->nx < 2 || U->ny < 2 || U->nz_aa < 2 || U->nz_aa > 1000 || U->nz_ac != U->nz_aa + 1)
+        return YGPU_ERR_BAD_ARG;
+    if (method == YGPU_UZ_AA) uz_aa(U, bc);
+    else if (method == YGPU_UZ_FLUX) uz_flux(U, bc);
+    else return YGPU_ERR_BAD_ARG;
+    if (U->uz_srf_err) {
+        const size_t n2 = (size_t)U->nx * U->ny, top = (size_t)(U->nz_ac - 1) * n2;
+        for (size_t c = 0; c < n2; c++)
+            U->uz_srf_err[c] = (U->f_ice[c] == 1.0) ? U->uz_star[top + c] + U->smb[c] : 0.0;
+    }
+    return YGPU_OK;
+}
+
+/* ======================================================================== */
 /* Implicit upwind advection, calc_advec2D(solver = "impl-lis")             */
 /* ======================================================================== */
 

@@ -163,6 +163,10 @@ int orc_calc_gradient_column_ac(double* dvdx_c, double* dvdy_c, const double* dv
                                 const double* f_ice, const int* mask_ocn, int boundaries, int nx, int ny);
 int orc_calc_jacobian_vel_3D(const ygpu_jvel* J, int boundaries, int terms);
 
+/* Vertical velocity by uz_method (calc_uz_3D_aa, calc_uz_3D_flux,
+   velocity_general.f90:683-1116) and uz_srf_err; the arguments of ygpu_calc_uz_3D. */
+int orc_calc_uz_3D(const ygpu_uz3d* U, int boundaries, int method);
+
 /* calc_advec2D(solver = "impl-lis"), solver_advection.f90:20-145: the CSR system of
    linear_solver_matrix_advection_csr_2D (:171-487) solved with this oracle's BiCGSTAB
    and Jacobi to 1e-12, calc_fixed_cell_transport (:489-546), dvdt. Same arguments as

@@ -143,6 +143,37 @@ def jvel(arrays: dict, dx: float, dy: float) -> JVel:
         setattr(J, n, a.ctypes.data)
     return J
 
+UZ_INPUTS = ("ux", "uy", "H_ice", "f_ice", "smb", "bmb", "dzbdt", "dzsdt", "dzsdx", "dzsdy", "dzbdx", "dzbdy",
+             "zeta_aa", "zeta_ac", "ux_bar", "uy_bar", "dHidt_dyn", "mask_kin")
+UZ_OUTPUTS = ("uz", "uz_star", "uz_srf_err")
+UZ_AA, UZ_FLUX = 1, 4
+
+
+class Uz3D(C.Structure):
+    """ygpu_uz3d: arrays of the vertical velocity."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz_aa", C.c_int), ("nz_ac", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("use_bmb", C.c_int)] + \
+        [(n, C.c_void_p) for n in UZ_INPUTS + UZ_OUTPUTS]
+
+
+def uz3d(arrays: dict, dx: float, dy: float, use_bmb: bool = True) -> Uz3D:
+    """A Uz3D over the numpy arrays of `arrays` (absent names stay NULL)."""
+    nx, ny = arrays["H_ice"].shape
+    nza, nzc = arrays["zeta_aa"].shape[0], arrays["zeta_ac"].shape[0]
+    U = Uz3D()
+    U.nx, U.ny, U.nz_aa, U.nz_ac, U.dx, U.dy, U.use_bmb = nx, ny, nza, nzc, dx, dy, int(bool(use_bmb))
+    for n in UZ_INPUTS + UZ_OUTPUTS:
+        a = arrays.get(n)
+        if a is None:
+            continue
+        want = {"zeta_aa": (nza,), "zeta_ac": (nzc,), "ux": (nx, ny, nza), "uy": (nx, ny, nza),
+                "uz": (nx, ny, nzc), "uz_star": (nx, ny, nzc)}.get(n, (nx, ny))
+        if a.shape != want:
+            raise ValueError(f"{n}: shape {a.shape}, expected {want}")
+        ptr(a, "i" if n == "mask_kin" else "d")
+        setattr(U, n, a.ctypes.data)
+    return U
+
 class Fields(C.Structure):
     """ygpu_fields: device pointers of one instance."""
     _fields_ = [

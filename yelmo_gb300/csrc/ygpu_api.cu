@@ -1361,6 +1361,69 @@ extern "C" int ygpu_calc_jacobian_vel_3D(const ygpu_jvel* H, int boundaries, int
     return S.download(c);
 }
 
+static int uz3d_check(const ygpu_uz3d* U, int bc, int method) {
+    if (!U || U->nx < 2 || U->ny < 2 || !(U->dx > 0.0) || !(U->dy > 0.0) || bc < 0 || bc > 6 ||
+        U->nz_aa < 2 || U->nz_aa > 1000 || U->nz_ac != U->nz_aa + 1 || (size_t)U->nx * U->ny > (size_t)(1 << 28)) {
+        ygpu_set_error("bad arguments (nz_ac = nz_aa + 1, 2 <= nz_aa <= 1000)");
+        return YGPU_ERR_BAD_ARG;
+    }
+    if (method != YGPU_UZ_AA && method != YGPU_UZ_FLUX) {
+        ygpu_set_error("uz_method %d: only 1 (uz_aa) and 4 (uz_flux) are built; 2 and 3 need gq2D/gq3D", method);
+        return YGPU_ERR_BAD_ARG;
+    }
+    if (any_null({U->ux, U->uy, U->H_ice, U->f_ice, U->smb, U->bmb, U->dzbdt, U->dzsdt, U->dzsdx, U->dzsdy,
+                  U->dzbdx, U->dzbdy, U->zeta_aa, U->zeta_ac, U->uz, U->uz_star})) {
+        ygpu_set_error("a required vertical-velocity array is NULL");
+        return YGPU_ERR_BAD_ARG;
+    }
+    if (method == YGPU_UZ_FLUX && any_null({U->ux_bar, U->uy_bar, U->dHidt_dyn, U->mask_kin})) {
+        ygpu_set_error("uz_flux needs ux_bar, uy_bar, dHidt_dyn and mask_kin");
+        return YGPU_ERR_BAD_ARG;
+    }
+    return YGPU_OK;
+}
+
+extern "C" int ygpu_calc_uz_3D_device(void* stream, const ygpu_uz3d* U, int boundaries, int method) {
+    int st = uz3d_check(U, boundaries, method);
+    if (st) return st;
+    return ygpu_uz3d_device((cudaStream_t)stream, *U, boundaries, method);
+}
+
+extern "C" int ygpu_calc_uz_3D(const ygpu_uz3d* H, int boundaries, int method) {
+    int st = uz3d_check(H, boundaries, method);
+    if (st) return st;
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const size_t n = (size_t)H->nx * H->ny, b2 = n * 8, ba = b2 * (size_t)H->nz_aa, bc3 = b2 * (size_t)H->nz_ac;
+    Staging S;
+    ygpu_uz3d D = *H;
+    std::vector<std::pair<size_t, const void**>> map;
+    auto in = [&](const void* src, const void** dst, size_t bytes) {
+        map.push_back({S.add((void*)src, bytes, 1, 0), dst});
+    };
+    auto out = [&](double* src, double** dst, size_t bytes) {
+        map.push_back({S.add((void*)src, bytes, 0, 1), (const void**)dst});
+    };
+    in(H->ux, (const void**)&D.ux, ba); in(H->uy, (const void**)&D.uy, ba);
+    const double* const* f2[] = {&H->H_ice, &H->f_ice, &H->smb, &H->bmb, &H->dzbdt, &H->dzsdt,
+                                 &H->dzsdx, &H->dzsdy, &H->dzbdx, &H->dzbdy};
+    const double** d2[] = {&D.H_ice, &D.f_ice, &D.smb, &D.bmb, &D.dzbdt, &D.dzsdt,
+                           &D.dzsdx, &D.dzsdy, &D.dzbdx, &D.dzbdy};
+    for (int q = 0; q < 10; q++) in(*f2[q], (const void**)d2[q], b2);
+    in(H->zeta_aa, (const void**)&D.zeta_aa, (size_t)H->nz_aa * 8);
+    in(H->zeta_ac, (const void**)&D.zeta_ac, (size_t)H->nz_ac * 8);
+    if (method == YGPU_UZ_FLUX) {
+        in(H->ux_bar, (const void**)&D.ux_bar, b2); in(H->uy_bar, (const void**)&D.uy_bar, b2);
+        in(H->dHidt_dyn, (const void**)&D.dHidt_dyn, b2); in(H->mask_kin, (const void**)&D.mask_kin, n * 4);
+    }
+    out(H->uz, &D.uz, bc3); out(H->uz_star, &D.uz_star, bc3);
+    if (H->uz_srf_err) out(H->uz_srf_err, &D.uz_srf_err, b2);
+    if ((st = S.upload(c))) return st;
+    for (auto& m : map) *m.second = S.args[m.first].dev;
+    if ((st = ygpu_uz3d_device(c->stream, D, boundaries, method))) return st;
+    return S.download(c);
+}
+
 extern "C" int ygpu_calc_advec2D_impl_lis(double* dvdt, const double* var, const double* ux, const double* uy,
                                           const double* var_dot, const int* mask_ice, const double* var_ref,
                                           double dx, double dy, double dt, int boundaries, int nx, int ny,

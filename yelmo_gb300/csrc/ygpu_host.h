@@ -108,6 +108,7 @@ int ygpu_dyn_diagnostics_device(cudaStream_t s, const ygpu_dyn_diag& D, int bc);
 int ygpu_gradient_column_device(cudaStream_t s, double* gx_c, double* gy_c, const double* gx, const double* gy,
                                 const double* f_ice, const int* mask_ocn, int bc, int nx, int ny);
 int ygpu_jacobian_device(cudaStream_t s, const ygpu_jvel& J, int bc, int terms);
+int ygpu_uz3d_device(cudaStream_t s, const ygpu_uz3d& U, int bc, int method);
 int ygpu_ssa_masks_device(cudaStream_t s, int* mx, int* my, const int* mf, const double* f_ice, const double* f_grnd,
                           int lat, int bc, int nx, int ny);
 

@@ -695,6 +695,153 @@ __global__ void __launch_bounds__(256) k_jacobian(ygpu_jvel J, int bc, int terms
     }
 }
 
+// ---------------------------------------------------------------------------
+// Vertical velocity (calc_uz_3D_aa / calc_uz_3D_flux, velocity_general.f90:683-1116)
+// ---------------------------------------------------------------------------
+
+YG_DEV double flush_tiny(double v) { return fabs(v) < YG_TOL_UNDERFLOW ? 0.0 : v; }
+
+// Horizontal velocity at level kc of the interfaces from the face means of the
+// layers, ua(k) = (u[im1] + u[i]) / 2: the base and top layers at the ends, the
+// mean of the two adjacent layers between (velocity_general.f90:850-866).
+YG_DEV double uz_level_mean(int kc, int nzc, double ua_k, double ua_km1) {
+    if (kc == 0) return ua_k;
+    if (kc == nzc - 1) return ua_km1;
+    return 0.5 * (ua_k + ua_km1);
+}
+
+// One thread per column. Shared memory: zeta_ac, its spacing dzc[kc] =
+// zeta_ac[kc] - zeta_ac[kc-1] and, for YGPU_UZ_AA, the reciprocal spacing of the
+// zeta_aa pair of the vertical derivative at each level (3 nz_ac doubles).
+__global__ void __launch_bounds__(256) k_uz3d(ygpu_uz3d U, int bc, int method) {
+    extern __shared__ double uz_sh[];
+    const int nza = U.nz_aa, nzc = U.nz_ac;
+    double* zc = uz_sh;
+    double* dzc = zc + nzc;
+    double* rdz = dzc + nzc;
+    for (int k = threadIdx.x; k < nzc; k += blockDim.x) {
+        zc[k] = U.zeta_ac[k];
+        dzc[k] = k > 0 ? U.zeta_ac[k] - U.zeta_ac[k - 1] : 0.0;
+        int hi = k, lo = k - 2;                        // centred on layer k-1
+        if (k <= 1) { hi = 1; lo = 0; }
+        else if (k == nzc - 1) { hi = nza - 1; lo = nza - 2; }
+        rdz[k] = 1.0 / (U.zeta_aa[hi] - U.zeta_aa[lo]);
+    }
+    __syncthreads();
+    const double rdx = 1.0 / U.dx, rdy = 1.0 / U.dy, f_bmb = U.use_bmb ? 1.0 : 0.0;
+    const int nx = U.nx, ny = U.ny;
+    const size_t n2 = (size_t)nx * ny;
+    const double* __restrict__ ux = U.ux;
+    const double* __restrict__ uy = U.uy;
+    for (int cc = blockIdx.x * blockDim.x + threadIdx.x; cc < nx * ny; cc += gridDim.x * blockDim.x) {
+        const int i = cc % nx, j = cc / nx;
+        int im1, ip1, jm1, jp1;
+        nbr_bc(i, j, nx, ny, bc, im1, ip1, jm1, jp1);
+        const size_t c = cc, cxm = im1 + (size_t)nx * j, cym = i + (size_t)nx * jm1;
+        const double dzbdt = U.dzbdt[c], dzsdt = U.dzsdt[c];
+        double top_star = 0.0;
+        if (!(U.f_ice[c] == 1.0)) {
+            const double u = flush_tiny(dzbdt - fmax(U.smb[c], 0.0));
+            for (int kc = 0; kc < nzc; kc++) {
+                U.uz[(size_t)kc * n2 + c] = u;
+                U.uz_star[(size_t)kc * n2 + c] = u;
+            }
+            if (U.uz_srf_err) U.uz_srf_err[c] = 0.0;
+            continue;
+        }
+        const double H = U.H_ice[c];
+        const double bxa = 0.5 * (U.dzbdx[c] + U.dzbdx[cxm]), bya = 0.5 * (U.dzbdy[c] + U.dzbdy[cym]);
+        const double gxa = 0.5 * (U.dzsdx[c] + U.dzsdx[cxm]) - bxa, gya = 0.5 * (U.dzsdy[c] + U.dzsdy[cym]) - bya;
+        const double gt = dzsdt - dzbdt;
+        auto UA = [&](int k) { return 0.5 * (__ldg(ux + (size_t)k * n2 + c) + __ldg(ux + (size_t)k * n2 + cxm)); };
+        auto VA = [&](int k) { return 0.5 * (__ldg(uy + (size_t)k * n2 + c) + __ldg(uy + (size_t)k * n2 + cym)); };
+        if (method == YGPU_UZ_AA) {
+            const double rH = 1.0 / H;
+            double ua_m2 = 0.0, va_m2 = 0.0, ua_m1 = 0.0, va_m1 = 0.0;
+            double ua_0 = UA(0), va_0 = VA(0);
+            // basal value (:776-778)
+            double uz = flush_tiny(dzbdt + f_bmb * U.bmb[c] + ua_0 * bxa + va_0 * bya);
+            for (int kc = 0; kc < nzc; kc++) {
+                if (kc > 0) {
+                    // window: ua_0 = layer kc (if any), ua_m1 = kc-1, ua_m2 = kc-2
+                    ua_m2 = ua_m1; va_m2 = va_m1;
+                    ua_m1 = ua_0; va_m1 = va_0;
+                    if (kc < nza) { ua_0 = UA(kc); va_0 = VA(kc); }
+                    const int ka = kc - 1;
+                    const double duxdx = (__ldg(ux + (size_t)ka * n2 + c) - __ldg(ux + (size_t)ka * n2 + cxm)) * rdx;
+                    const double duydy = (__ldg(uy + (size_t)ka * n2 + c) - __ldg(uy + (size_t)ka * n2 + cym)) * rdy;
+                    double dux, duy;                           // ua(hi) - ua(lo)
+                    if (kc == 1) { dux = ua_0 - ua_m1; duy = va_0 - va_m1; }
+                    else if (kc == nzc - 1) { dux = ua_m1 - ua_m2; duy = va_m1 - va_m2; }
+                    else { dux = ua_0 - ua_m2; duy = va_0 - va_m2; }
+                    const double cx = -rH * fma(zc[kc], gxa, bxa), cy = -rH * fma(zc[kc], gya, bya);
+                    const double div = fma(cx, dux * rdz[kc], duxdx) + fma(cy, duy * rdz[kc], duydy);
+                    uz = flush_tiny(fma(-(H * dzc[kc]), div, uz));
+                }
+                // uz_star (:845-880)
+                const double xa = uz_level_mean(kc, nzc, kc < nza ? ua_0 : 0.0, ua_m1);
+                const double ya = uz_level_mean(kc, nzc, kc < nza ? va_0 : 0.0, va_m1);
+                const double z = zc[kc];
+                const double us = ((uz - xa * fma(z, gxa, bxa)) - ya * fma(z, gya, bya)) - fma(z, gt, dzbdt);
+                const size_t o = (size_t)kc * n2 + c;
+                U.uz[o] = uz;
+                U.uz_star[o] = flush_tiny(us);
+                top_star = flush_tiny(us);
+            }
+        } else {
+            // calc_uz_3D_flux: layer divergences with upwind face thickness (:1043-1056)
+            const double* Hi = U.H_ice;
+            const size_t cxp = ip1 + (size_t)nx * j, cyp = i + (size_t)nx * jp1;
+            const double Hx_w = (U.ux_bar[cxm] >= 0.0) ? Hi[cxm] : Hi[c];
+            const double Hx_e = (U.ux_bar[c] >= 0.0) ? Hi[c] : Hi[cxp];
+            const double Hy_s = (U.uy_bar[cym] >= 0.0) ? Hi[cym] : Hi[c];
+            const double Hy_n = (U.uy_bar[c] >= 0.0) ? Hi[c] : Hi[cyp];
+            auto Dk = [&](int k) {
+                const size_t o = (size_t)k * n2;
+                const double fx = fma(Hx_e, __ldg(ux + o + c), -(Hx_w * __ldg(ux + o + cxm)));
+                const double fy = fma(Hy_n, __ldg(uy + o + c), -(Hy_s * __ldg(uy + o + cym)));
+                return dzc[k + 1] * fma(fx, rdx, fy * rdy);
+            };
+            double q = gt;                                 // dzeta-weighted rate per layer
+            if (U.mask_kin[c] == 1) {
+                double tot = 0.0;
+                for (int k = 0; k < nza; k++) tot += Dk(k);
+                q = gt + (-U.dHidt_dyn[c] - tot);          // dHdt + D_corr
+            }
+            double us = f_bmb * U.bmb[c];
+            double ua_m1 = 0.0, va_m1 = 0.0, ua_0 = UA(0), va_0 = VA(0);
+            for (int kc = 0; kc < nzc; kc++) {
+                if (kc > 0) {
+                    us = fma(-dzc[kc], q, us) - Dk(kc - 1);
+                    ua_m1 = ua_0; va_m1 = va_0;
+                    if (kc < nza) { ua_0 = UA(kc); va_0 = VA(kc); }
+                }
+                const double xa = uz_level_mean(kc, nzc, kc < nza ? ua_0 : 0.0, ua_m1);
+                const double ya = uz_level_mean(kc, nzc, kc < nza ? va_0 : 0.0, va_m1);
+                const double z = zc[kc];
+                const double corr = (-(xa * fma(z, gxa, bxa)) - ya * fma(z, gya, bya)) - fma(z, gt, dzbdt);
+                const size_t o = (size_t)kc * n2 + c;
+                U.uz[o] = flush_tiny(us - corr);
+                U.uz_star[o] = flush_tiny(us);
+                top_star = flush_tiny(us);
+            }
+        }
+        if (U.uz_srf_err) U.uz_srf_err[c] = top_star + U.smb[c];
+    }
+}
+
+int ygpu_uz3d_device(cudaStream_t s, const ygpu_uz3d& U, int bc, int method) {
+    const size_t smem = 3 * sizeof(double) * (size_t)U.nz_ac;
+    k_uz3d<<<grid_for(U.nx * U.ny), 256, smem, s>>>(U, bc, method);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        ygpu_set_error("vertical velocity kernel: %s", cudaGetErrorString(e));
+        return YGPU_ERR_CUDA;
+    }
+    ygpu_count_launches(1);
+    return YGPU_OK;
+}
+
 int ygpu_gradient_column_device(cudaStream_t s, double* gx_c, double* gy_c, const double* gx, const double* gy,
                                 const double* f_ice, const int* mask_ocn, int bc, int nx, int ny) {
     k_gradient_column<<<grid_for(nx * ny), 256, 0, s>>>(nx, ny, bc, gx, gy, f_ice, mask_ocn, gx_c, gy_c);

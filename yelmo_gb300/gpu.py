@@ -41,7 +41,7 @@ EXPORTS = [
     "ygpu_ctx_set_tuning", "ygpu_set_neff_hook", "ygpu_solve_batch_host", "ygpu_calc_dyn_diagnostics",
     "ygpu_calc_dyn_diagnostics_device", "ygpu_calc_advec2D_impl_lis", "ygpu_advec2D_impl_lis_device",
     "ygpu_calc_gradient_column_ac", "ygpu_calc_gradient_column_ac_device", "ygpu_calc_jacobian_vel_3D",
-    "ygpu_calc_jacobian_vel_3D_device",
+    "ygpu_calc_jacobian_vel_3D_device", "ygpu_calc_uz_3D", "ygpu_calc_uz_3D_device",
 ]
 
 
@@ -96,6 +96,8 @@ def lib(build_if_missing: bool = True):
     L.ygpu_calc_gradient_column_ac_device.argtypes = [C.c_void_p] * 7 + [C.c_int, C.c_int, C.c_int]
     L.ygpu_calc_jacobian_vel_3D.argtypes = [C.POINTER(abi.JVel), C.c_int, C.c_int]
     L.ygpu_calc_jacobian_vel_3D_device.argtypes = [C.c_void_p, C.POINTER(abi.JVel), C.c_int, C.c_int]
+    L.ygpu_calc_uz_3D.argtypes = [C.POINTER(abi.Uz3D), C.c_int, C.c_int]
+    L.ygpu_calc_uz_3D_device.argtypes = [C.c_void_p, C.POINTER(abi.Uz3D), C.c_int, C.c_int]
     L.ygpu_server_create.restype = C.c_void_p
     L.ygpu_server_create.argtypes = [C.POINTER(abi.ServerCfg)]
     L.ygpu_server_destroy.argtypes = [C.c_void_p]
@@ -276,6 +278,26 @@ def calc_jacobian_vel_3D(arrays: dict, dx: float, dy: float, boundaries: str,
     of `arrays` (see jacobian_arrays) are filled in place."""
     J = abi.jvel(arrays, dx, dy)
     _check(lib().ygpu_calc_jacobian_vel_3D(C.byref(J), abi.BOUNDARY_CODES[boundaries], int(terms)))
+    return arrays
+
+def uz_arrays(inputs: dict, srf_err: bool = True) -> dict:
+    """`inputs` (UZ_INPUTS names) with zeroed uz, uz_star (and uz_srf_err)."""
+    nx, ny = inputs["H_ice"].shape
+    nzc = inputs["zeta_ac"].shape[0]
+    out = dict(inputs)
+    out["uz"] = np.zeros((nx, ny, nzc), order="F")
+    out["uz_star"] = np.zeros((nx, ny, nzc), order="F")
+    if srf_err:
+        out["uz_srf_err"] = np.zeros((nx, ny), order="F")
+    return out
+
+
+def calc_uz_3D(arrays: dict, dx: float, dy: float, boundaries: str, method: int = abi.UZ_AA,
+               use_bmb: bool = True) -> dict:
+    """Vertical velocity on the GPU (ygpu_calc_uz_3D, uz_method 1 or 4); the
+    output arrays of `arrays` (see uz_arrays) are filled in place."""
+    U = abi.uz3d(arrays, dx, dy, use_bmb)
+    _check(lib().ygpu_calc_uz_3D(C.byref(U), abi.BOUNDARY_CODES[boundaries], int(method)))
     return arrays
 
 def calc_dyn_inputs(inst) -> dict:
