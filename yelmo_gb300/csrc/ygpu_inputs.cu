@@ -699,7 +699,13 @@ __global__ void __launch_bounds__(256) k_jacobian(ygpu_jvel J, int bc, int terms
 // Vertical velocity (calc_uz_3D_aa / calc_uz_3D_flux, velocity_general.f90:683-1116)
 // ---------------------------------------------------------------------------
 
-YG_DEV double flush_tiny(double v) { return fabs(v) < YG_TOL_UNDERFLOW ? 0.0 : v; }
+// |v| < 1e-15 -> 0, evaluated on the integer pipe: the magnitude bits of a
+// double order like its absolute value (NaN and inf compare above any finite
+// bound), so the test is the same as fabs(v) < 1e-15 without an FP64 compare.
+YG_DEV double flush_tiny(double v) {
+    const unsigned long long mag = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+    return mag < (unsigned long long)__double_as_longlong(YG_TOL_UNDERFLOW) ? 0.0 : v;
+}
 
 // Horizontal velocity at level kc of the interfaces from the face means of the
 // layers, ua(k) = (u[im1] + u[i]) / 2: the base and top layers at the ends, the
