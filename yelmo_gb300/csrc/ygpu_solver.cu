@@ -431,8 +431,9 @@ YG_DEV float* shear_f32(const Inst& I, int axis) {
     return (float*)I.attp + (4 + axis) * n3;
 }
 
-// R = float (mixed mode): FP32 arithmetic, the FP64 output plus an FP32 copy
-// that the column pass reads
+// R = float (mixed mode): FP32 arithmetic into the FP32 copies that the column
+// pass reads; the caller's FP64 duxdz / duydz are those floats widened, written
+// once by the final passes rather than every iteration
 template <typename R, typename VS>
 __device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, const VS* vcur) {
     const int nz = G.nz, n2 = G.n2;
@@ -452,11 +453,12 @@ __device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, c
             const R gx = (va != R(0)) ? (tx / va) * omz : R(0);
             va = stag_margin<R>(vc, (R)vcur[o + cy], fc, fy);
             const R gy = (va != R(0)) ? (ty / va) * omz : R(0);
-            I.duxdz[o + c] = (double)gx;
-            I.duydz[o + c] = (double)gy;
             if (sizeof(R) == sizeof(float)) {
                 sx32[o + c] = (float)gx;
                 sy32[o + c] = (float)gy;
+            } else {
+                I.duxdz[o + c] = (double)gx;
+                I.duydz[o + c] = (double)gy;
             }
         }
     }
@@ -567,10 +569,15 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
             } else {
                 R e = e_aa;
                 if (diva) {
-                    const double* dz = I.duxdz + (size_t)k * n2;
-                    const double* dzy = I.duydz + (size_t)k * n2;
-                    R dzx = (R)(0.5 * (dz[c] + dz[CI(n.im1, n.j)]));
-                    R dzyv = (R)(0.5 * (dzy[c] + dzy[CI(n.i, n.jm1)]));
+                    // the FP64 shear, or (mixed) its FP32 copy widened: the same values
+                    const size_t o = (size_t)k * n2;
+                    const bool f32 = (sizeof(R) == sizeof(float));
+                    const float* fx = f32 ? shear_f32(I, 0) + o : nullptr;
+                    const float* fy = f32 ? shear_f32(I, 1) + o : nullptr;
+                    auto shx = [&](int q) { return f32 ? (double)fx[q] : I.duxdz[o + q]; };
+                    auto shy = [&](int q) { return f32 ? (double)fy[q] : I.duydz[o + q]; };
+                    R dzx = (R)(0.5 * (shx(c) + shx(CI(n.im1, n.j))));
+                    R dzyv = (R)(0.5 * (shy(c) + shy(CI(n.i, n.jm1))));
                     e = e + R(0.25) * (dzx * dzx);
                     e = e + R(0.25) * (dzyv * dzyv);
                 }
@@ -2747,6 +2754,15 @@ __device__ __noinline__ bool final_passes(const Inst& I, const ygpu_dyn_par& P, 
             const size_t n3 = (size_t)G.n2 * G.nz;
             const float* vf = (const float*)I.visc_alt + (in_alt ? n3 : 0);
             for (size_t k = T.tid; k < n3; k += T.nthr) I.visc[k] = (double)vf[k];
+            if (diva) {
+                // the shear of the last iteration, kept in FP32 by the loop
+                const float* sx = shear_f32(I, 0);
+                const float* sy = shear_f32(I, 1);
+                for (size_t k = T.tid; k < n3; k += T.nthr) {
+                    I.duxdz[k] = (double)sx[k];
+                    I.duydz[k] = (double)sy[k];
+                }
+            }
             if (!team_barrier(T)) return false;
         }
         in_alt = 0;
