@@ -350,7 +350,7 @@ JAC_TOL = 1e-12
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("bc", ["zeros", "periodic", "MISMIP3D", "infinite"])
+@pytest.mark.parametrize("bc", BCS)
 def test_gpu_jacobian_matches_oracle(bc):
     inst, a, (sx, sy, bx, by, ocn) = _solved_state(bc)
     for g, h in (((sx, sy), ("dzsdx", "dzsdy")), ((bx, by), ("dzbdx", "dzbdy"))):

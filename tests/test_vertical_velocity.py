@@ -223,7 +223,7 @@ UZ_TOL = 1e-12
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("bc", ["zeros", "periodic", "MISMIP3D", "infinite"])
+@pytest.mark.parametrize("bc", BCS)
 def test_gpu_uz_matches_oracle(bc):
     inst, a = _solved_inputs(bc)
     for method in (abi.UZ_AA, abi.UZ_FLUX):

@@ -707,31 +707,35 @@ YG_DEV double flush_tiny(double v) {
     return mag < (unsigned long long)__double_as_longlong(YG_TOL_UNDERFLOW) ? 0.0 : v;
 }
 
-// Horizontal velocity at level kc of the interfaces from the face means of the
-// layers, ua(k) = (u[im1] + u[i]) / 2: the base and top layers at the ends, the
-// mean of the two adjacent layers between (velocity_general.f90:850-866).
-YG_DEV double uz_level_mean(int kc, int nzc, double ua_k, double ua_km1) {
-    if (kc == 0) return ua_k;
-    if (kc == nzc - 1) return ua_km1;
-    return 0.5 * (ua_k + ua_km1);
+// Horizontal velocity at level kc of the interfaces, times 4, from the face sums
+// of the layers sa(k) = u[im1] + u[i]: the base and top layers at the ends, the
+// two adjacent layers between (velocity_general.f90:850-866, where the level
+// value is their mean).
+YG_DEV double uz_level_sum4(int kc, int nzc, double sa_k, double sa_km1) {
+    if (kc == 0) return sa_k + sa_k;
+    if (kc == nzc - 1) return sa_km1 + sa_km1;
+    return sa_k + sa_km1;
 }
 
 // One thread per column. Shared memory: zeta_ac, its spacing dzc[kc] =
-// zeta_ac[kc] - zeta_ac[kc-1] and, for YGPU_UZ_AA, the reciprocal spacing of the
-// zeta_aa pair of the vertical derivative at each level (3 nz_ac doubles).
+// zeta_ac[kc] - zeta_ac[kc-1] and, for YGPU_UZ_AA, half the reciprocal spacing
+// of the zeta_aa pair of the vertical derivative at each level (3 nz_ac doubles).
+// FP64 issues at 2 FMA per clock per SM on this GPU: the level loops carry face
+// sums instead of means, the 1/2 and 1/4 of the means sit in per-column
+// constants (exact power-of-two scalings), and the coordinate terms are FMAs.
 __global__ void __launch_bounds__(256) k_uz3d(ygpu_uz3d U, int bc, int method) {
     extern __shared__ double uz_sh[];
     const int nza = U.nz_aa, nzc = U.nz_ac;
     double* zc = uz_sh;
     double* dzc = zc + nzc;
-    double* rdz = dzc + nzc;
+    double* hrdz = dzc + nzc;
     for (int k = threadIdx.x; k < nzc; k += blockDim.x) {
         zc[k] = U.zeta_ac[k];
         dzc[k] = k > 0 ? U.zeta_ac[k] - U.zeta_ac[k - 1] : 0.0;
         int hi = k, lo = k - 2;                        // centred on layer k-1
         if (k <= 1) { hi = 1; lo = 0; }
         else if (k == nzc - 1) { hi = nza - 1; lo = nza - 2; }
-        rdz[k] = 1.0 / (U.zeta_aa[hi] - U.zeta_aa[lo]);
+        hrdz[k] = 0.5 / (U.zeta_aa[hi] - U.zeta_aa[lo]);
     }
     __syncthreads();
     const double rdx = 1.0 / U.dx, rdy = 1.0 / U.dy, f_bmb = U.use_bmb ? 1.0 : 0.0;
@@ -758,41 +762,59 @@ __global__ void __launch_bounds__(256) k_uz3d(ygpu_uz3d U, int bc, int method) {
         const double H = U.H_ice[c];
         const double bxa = 0.5 * (U.dzbdx[c] + U.dzbdx[cxm]), bya = 0.5 * (U.dzbdy[c] + U.dzbdy[cym]);
         const double gxa = 0.5 * (U.dzsdx[c] + U.dzsdx[cxm]) - bxa, gya = 0.5 * (U.dzsdy[c] + U.dzsdy[cym]) - bya;
+        // slopes of the coordinate terms at level z: fma(z, g4, b4) = ((1-z) dzb + z dzs) / 4
+        const double bx4 = 0.25 * bxa, gx4 = 0.25 * gxa, by4 = 0.25 * bya, gy4 = 0.25 * gya;
         const double gt = dzsdt - dzbdt;
-        auto UA = [&](int k) { return 0.5 * (__ldg(ux + (size_t)k * n2 + c) + __ldg(ux + (size_t)k * n2 + cxm)); };
-        auto VA = [&](int k) { return 0.5 * (__ldg(uy + (size_t)k * n2 + c) + __ldg(uy + (size_t)k * n2 + cym)); };
+        auto SA = [&](int k) { return __ldg(ux + (size_t)k * n2 + c) + __ldg(ux + (size_t)k * n2 + cxm); };
+        auto SV = [&](int k) { return __ldg(uy + (size_t)k * n2 + c) + __ldg(uy + (size_t)k * n2 + cym); };
+        // the coordinate terms at level kc (:867-876): c_x = -(tx/4) ((1-z) dzbdx + z dzsdx)
+        // = -tx fma(z, gx4, bx4), c_y likewise, c_t = -fma(z, gt, dzbdt);
+        // plus_c(v) = v + c_x + c_y + c_t, minus_c(v) = v - (c_x + c_y + c_t)
+        auto plus_c = [&](double v, int kc, double tx, double ty) {
+            const double z = zc[kc];
+            v = v - fma(z, gt, dzbdt);
+            v = fma(-tx, fma(z, gx4, bx4), v);
+            return fma(-ty, fma(z, gy4, by4), v);
+        };
+        auto minus_c = [&](double v, int kc, double tx, double ty) {
+            const double z = zc[kc];
+            v = v + fma(z, gt, dzbdt);
+            v = fma(tx, fma(z, gx4, bx4), v);
+            return fma(ty, fma(z, gy4, by4), v);
+        };
         if (method == YGPU_UZ_AA) {
-            const double rH = 1.0 / H;
-            double ua_m2 = 0.0, va_m2 = 0.0, ua_m1 = 0.0, va_m1 = 0.0;
-            double ua_0 = UA(0), va_0 = VA(0);
-            // basal value (:776-778)
-            double uz = flush_tiny(dzbdt + f_bmb * U.bmb[c] + ua_0 * bxa + va_0 * bya);
+            const double r4H = 4.0 / H;
+            double sa_m2 = 0.0, sv_m2 = 0.0, sa_m1 = 0.0, sv_m1 = 0.0;
+            double sa_0 = SA(0), sv_0 = SV(0);
+            // basal value (:776-778), ux_aa = sa/2
+            double uz = flush_tiny(dzbdt + f_bmb * U.bmb[c] + (0.5 * sa_0) * bxa + (0.5 * sv_0) * bya);
             for (int kc = 0; kc < nzc; kc++) {
                 if (kc > 0) {
-                    // window: ua_0 = layer kc (if any), ua_m1 = kc-1, ua_m2 = kc-2
-                    ua_m2 = ua_m1; va_m2 = va_m1;
-                    ua_m1 = ua_0; va_m1 = va_0;
-                    if (kc < nza) { ua_0 = UA(kc); va_0 = VA(kc); }
+                    // window: sa_0 = layer kc (if any), sa_m1 = kc-1, sa_m2 = kc-2
+                    sa_m2 = sa_m1; sv_m2 = sv_m1;
+                    sa_m1 = sa_0; sv_m1 = sv_0;
+                    if (kc < nza) { sa_0 = SA(kc); sv_0 = SV(kc); }
                     const int ka = kc - 1;
                     const double duxdx = (__ldg(ux + (size_t)ka * n2 + c) - __ldg(ux + (size_t)ka * n2 + cxm)) * rdx;
                     const double duydy = (__ldg(uy + (size_t)ka * n2 + c) - __ldg(uy + (size_t)ka * n2 + cym)) * rdy;
-                    double dux, duy;                           // ua(hi) - ua(lo)
-                    if (kc == 1) { dux = ua_0 - ua_m1; duy = va_0 - va_m1; }
-                    else if (kc == nzc - 1) { dux = ua_m1 - ua_m2; duy = va_m1 - va_m2; }
-                    else { dux = ua_0 - ua_m2; duy = va_0 - va_m2; }
-                    const double cx = -rH * fma(zc[kc], gxa, bxa), cy = -rH * fma(zc[kc], gya, bya);
-                    const double div = fma(cx, dux * rdz[kc], duxdx) + fma(cy, duy * rdz[kc], duydy);
+                    double dsx, dsy;                           // sa(hi) - sa(lo)
+                    if (kc == 1) { dsx = sa_0 - sa_m1; dsy = sv_0 - sv_m1; }
+                    else if (kc == nzc - 1) { dsx = sa_m1 - sa_m2; dsy = sv_m1 - sv_m2; }
+                    else { dsx = sa_0 - sa_m2; dsy = sv_0 - sv_m2; }
+                    // c_x duxdz = -(1/H) ((1-z) dzb + z dzs) (sa(hi) - sa(lo)) / (2 dzeta)
+                    const double z = zc[kc];
+                    const double cx = -r4H * hrdz[kc] * fma(z, gx4, bx4), cy = -r4H * hrdz[kc] * fma(z, gy4, by4);
+                    const double div = fma(cx, dsx, duxdx) + fma(cy, dsy, duydy);
                     uz = flush_tiny(fma(-(H * dzc[kc]), div, uz));
                 }
                 // uz_star (:845-880)
-                const double xa = uz_level_mean(kc, nzc, kc < nza ? ua_0 : 0.0, ua_m1);
-                const double ya = uz_level_mean(kc, nzc, kc < nza ? va_0 : 0.0, va_m1);
-                const double z = zc[kc];
-                const double us = ((uz - xa * fma(z, gxa, bxa)) - ya * fma(z, gya, bya)) - fma(z, gt, dzbdt);
+                const double tx = uz_level_sum4(kc, nzc, kc < nza ? sa_0 : 0.0, sa_m1);
+                const double ty = uz_level_sum4(kc, nzc, kc < nza ? sv_0 : 0.0, sv_m1);
+                const double us = flush_tiny(plus_c(uz, kc, tx, ty));
                 const size_t o = (size_t)kc * n2 + c;
                 U.uz[o] = uz;
-                U.uz_star[o] = flush_tiny(us);
-                top_star = flush_tiny(us);
+                U.uz_star[o] = us;
+                top_star = us;
             }
         } else {
             // calc_uz_3D_flux: layer divergences with upwind face thickness (:1043-1056)
@@ -802,11 +824,12 @@ __global__ void __launch_bounds__(256) k_uz3d(ygpu_uz3d U, int bc, int method) {
             const double Hx_e = (U.ux_bar[c] >= 0.0) ? Hi[c] : Hi[cxp];
             const double Hy_s = (U.uy_bar[cym] >= 0.0) ? Hi[cym] : Hi[c];
             const double Hy_n = (U.uy_bar[c] >= 0.0) ? Hi[c] : Hi[cyp];
+            const double ex = Hx_e * rdx, wx = Hx_w * rdx, ny_ = Hy_n * rdy, sy = Hy_s * rdy;
             auto Dk = [&](int k) {
                 const size_t o = (size_t)k * n2;
-                const double fx = fma(Hx_e, __ldg(ux + o + c), -(Hx_w * __ldg(ux + o + cxm)));
-                const double fy = fma(Hy_n, __ldg(uy + o + c), -(Hy_s * __ldg(uy + o + cym)));
-                return dzc[k + 1] * fma(fx, rdx, fy * rdy);
+                const double fx = fma(ex, __ldg(ux + o + c), -(wx * __ldg(ux + o + cxm)));
+                const double fl = fma(ny_, __ldg(uy + o + c), fma(-sy, __ldg(uy + o + cym), fx));
+                return dzc[k + 1] * fl;
             };
             double q = gt;                                 // dzeta-weighted rate per layer
             if (U.mask_kin[c] == 1) {
@@ -815,19 +838,17 @@ __global__ void __launch_bounds__(256) k_uz3d(ygpu_uz3d U, int bc, int method) {
                 q = gt + (-U.dHidt_dyn[c] - tot);          // dHdt + D_corr
             }
             double us = f_bmb * U.bmb[c];
-            double ua_m1 = 0.0, va_m1 = 0.0, ua_0 = UA(0), va_0 = VA(0);
+            double sa_m1 = 0.0, sv_m1 = 0.0, sa_0 = SA(0), sv_0 = SV(0);
             for (int kc = 0; kc < nzc; kc++) {
                 if (kc > 0) {
                     us = fma(-dzc[kc], q, us) - Dk(kc - 1);
-                    ua_m1 = ua_0; va_m1 = va_0;
-                    if (kc < nza) { ua_0 = UA(kc); va_0 = VA(kc); }
+                    sa_m1 = sa_0; sv_m1 = sv_0;
+                    if (kc < nza) { sa_0 = SA(kc); sv_0 = SV(kc); }
                 }
-                const double xa = uz_level_mean(kc, nzc, kc < nza ? ua_0 : 0.0, ua_m1);
-                const double ya = uz_level_mean(kc, nzc, kc < nza ? va_0 : 0.0, va_m1);
-                const double z = zc[kc];
-                const double corr = (-(xa * fma(z, gxa, bxa)) - ya * fma(z, gya, bya)) - fma(z, gt, dzbdt);
+                const double tx = uz_level_sum4(kc, nzc, kc < nza ? sa_0 : 0.0, sa_m1);
+                const double ty = uz_level_sum4(kc, nzc, kc < nza ? sv_0 : 0.0, sv_m1);
                 const size_t o = (size_t)kc * n2 + c;
-                U.uz[o] = flush_tiny(us - corr);
+                U.uz[o] = flush_tiny(minus_c(us, kc, tx, ty));
                 U.uz_star[o] = flush_tiny(us);
                 top_star = flush_tiny(us);
             }
