@@ -19,7 +19,11 @@
  * (tests/test_ssa_energy*.f90), the converged solve by the reference's
  * analytic benchmarks (A2 radial shelf, tests/bench/src/shelf.jl). The
  * quadrature rule and LIS iterates are restated and unpinned; only converged
- * solutions are compared.
+ * solutions are compared. The routines around the solve (post-solve diagnostics,
+ * column gradients, velocity Jacobian, vertical velocity, implicit advection)
+ * have no known-answer test in the reference; they are pinned by independent
+ * restatements in the tests and by analytic cases (exactness of the difference
+ * formulas on polynomials, incompressible flow, column mass balance).
  */
 #ifndef YELMO_ORACLE_H
 #define YELMO_ORACLE_H
