@@ -307,6 +307,61 @@ def radial_shelf(dx_km: float = 10.0, H: float = 400.0, R_s: float = 300e3, L: f
     return inst
 
 
+def schoof_slab_u(y, alpha: float, H0: float, A: float, W: float, m: float, rho_ice: float, g: float):
+    """Schoof (2006) ice stream on a plastic bed, n = 3 (tests/yelmo_trough.f90:1349-1400):
+    till yield stress tau_c = f |y/L|^m, f = rho g H alpha, L = W / (1+m)^(1/m), and the
+    along-stream velocity u(y), zero for |y| > W. Returns (u, tau_c)."""
+    y = np.asarray(y, dtype=np.float64)
+    f = rho_ice * g * H0 * alpha
+    B = A ** (-1.0 / 3.0)
+    L = W / (1.0 + m) ** (1.0 / m)
+    s = np.abs(y / L)
+    m1 = m + 1.0
+    bracket = ((y / L) ** 4 - m1 ** (4.0 / m)) / 4.0 \
+        - 3.0 * (s ** (m + 4.0) - m1 ** (1.0 + 4.0 / m)) / (m1 * (m + 4.0)) \
+        + 3.0 * (s ** (2.0 * m + 4.0) - m1 ** (2.0 + 4.0 / m)) / (m1 ** 2 * (2.0 * m + 4.0)) \
+        - (s ** (3.0 * m + 4.0) - m1 ** (3.0 + 4.0 / m)) / (m1 ** 3 * (3.0 * m + 4.0))
+    u = -2.0 * f ** 3 * L ** 4 / (B ** 3 * H0 ** 3) * bracket
+    u = np.where(np.abs(y) > W, 0.0, u)
+    return u, f * s ** m
+
+
+def schoof_slab(dx_km: float = 2.0, lx: float = 100e3, ly: float = 80e3, alpha: float = 1e-3,
+                H0: float = 1000.0, W: float = 25e3, m: float = 1.55, A: float = 1e-16,
+                nz: int = 5) -> Instance:
+    """Schoof (2006) slab (the reference's SLAB-S06 domain, tests/yelmo_trough.f90:174-182,
+    259-307, par/yelmo_SLAB-S06.nml): periodic in x and y, uniform thickness H0 on a bed
+    sloping down in x by alpha, SSA (energy form, visc_method 2) on a plastic bed
+    (beta_method 4, q = 0, u0 = 1 m/a) whose c_bed is the analytic till yield stress.
+    The slope enters only the driving stress, as the reference's uniform background
+    slope: slab_state sets taud_acx = -rho g H0 alpha (grounded, flowing towards +x)."""
+    dx = dx_km * 1e3
+    nx, ny = int(round(lx / dx)), int(round(ly / dx))
+    y = -(ny // 2) * dx + dx * np.arange(ny)
+    par = YdynParams(solver="ssa", ssa_solver="energy", visc_method=2, beta_method=4, beta_q=0.0,
+                     beta_u0=1.0, beta_gl_scale=0, beta_gl_stag=0, beta_gl_f=1.0, beta_min=0.0,
+                     eps_0=1e-6, boundaries="periodic", ssa_lat_bc="marine", ssa_vel_max=10000.0)
+    u, tauc = schoof_slab_u(y, alpha, H0, A, W, m, par.rho_ice, par.g)
+    c_bed = np.broadcast_to(tauc[None, :], (nx, ny))
+    inst = Instance("schoof_slab", par, dx, _F(np.full((nx, ny), H0)), _F(np.full((nx, ny), 10000.0)),
+                    _F(np.zeros((nx, ny))), _F(np.full((nx, ny, nz), A)), calc_zeta(nz),
+                    _F(np.zeros((nx, ny))), _F(c_bed), _F(np.ones((nx, ny))))
+    inst.extra = {"y": y, "u": u, "taud": par.rho_ice * par.g * H0 * alpha, "W": W}
+    return inst
+
+
+def slab_state(inst: Instance, inputs: dict) -> dict:
+    """State of the Schoof slab: the driving stress of the background slope, and the
+    analytic velocity as the start (as the reference initialises ux_b, ux_bar)."""
+    f = inst.state(inputs)
+    f["taud_acx"][:] = -inst.extra["taud"]
+    f["taud_acy"][:] = 0.0
+    u = np.broadcast_to(inst.extra["u"][None, :], (inst.nx, inst.ny))
+    for k in ("ux_b", "ux_bar"):
+        f[k][:] = u
+    return f
+
+
 def shelf_state(inst: Instance, inputs: dict) -> dict:
     """Cold state of the A2 shelf with the imposed staggered friction (beta_gl_stag = -1)."""
     f = inst.state(inputs)
