@@ -1,5 +1,6 @@
 """Golden fixtures (tests/golden/*.npz, written by tests/golden/make_golden.py):
-small seeded solves of the oracle converged tightly.
+small seeded solves of the oracle converged tightly, and the oracle's post-solve
+diagnostics, velocity Jacobian and vertical velocity on seeded fields.
 
 CPU: the oracle built here reproduces them (the masks bit for bit, the fields
 to 1e-10), which pins it across compilers and machines. GPU: the GPU solver,
@@ -11,7 +12,7 @@ import numpy as np
 import pytest
 
 from tests.cases import rel_l2
-from tests.golden.make_golden import OUT_KEYS, golden_cases
+from tests.golden.make_golden import OUT_KEYS, POST_BCS, golden_cases, post_solve_outputs
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 NAMES = sorted(golden_cases())
@@ -56,3 +57,39 @@ def test_gpu_matches_golden(name, precision):
     vel = ("ux_b", "uy_b") if inst.par.solver == "ssa" else ("ux_bar", "uy_bar", "ux_b", "uy_b")
     for k in vel + ("visc_eff", "visc_eff_int", "taub_acx", "taub_acy"):
         assert rel_l2(f[k], outputs[k]) <= 1e-6, (k, rel_l2(f[k], outputs[k]))
+
+
+def _load_post(bc):
+    d = np.load(os.path.join(HERE, f"post_solve_{bc}.npz"))
+    inputs = {k[3:]: np.asfortranarray(d[k]) for k in d.files if k.startswith("in_")}
+    outputs = {k[4:]: d[k] for k in d.files if k.startswith("out_")}
+    return inputs, outputs
+
+
+def _check_post(got, want, tol):
+    assert set(got) == set(want)
+    for k, v in want.items():
+        scale = float(np.max(np.abs(v))) if v.size else 0.0
+        np.testing.assert_allclose(got[k], v, rtol=0, atol=tol * scale + 1e-300, err_msg=k)
+
+
+@pytest.mark.parametrize("bc", POST_BCS)
+def test_oracle_reproduces_post_solve_golden(bc):
+    import oracle
+    inputs, outputs = _load_post(bc)
+    _check_post(post_solve_outputs(oracle, inputs, bc), outputs, 1e-14)
+
+
+# The diagnostics evaluate the reference expressions as written (bit-exact with
+# the oracle on one machine); the Jacobian and vertical-velocity kernels keep
+# divisions out of their layer loops and agree to rounding.
+@pytest.mark.gpu
+@pytest.mark.parametrize("bc", POST_BCS)
+def test_gpu_matches_post_solve_golden(bc):
+    from yelmo_gb300 import gpu
+    inputs, outputs = _load_post(bc)
+    got = post_solve_outputs(gpu, inputs, bc)
+    _check_post({k: v for k, v in got.items() if k.startswith("diag_")},
+                {k: v for k, v in outputs.items() if k.startswith("diag_")}, 1e-14)
+    _check_post({k: v for k, v in got.items() if not k.startswith("diag_")},
+                {k: v for k, v in outputs.items() if not k.startswith("diag_")}, 1e-12)
