@@ -68,3 +68,22 @@ def test_defaults_match_namelist():
         if k in ("no_slip",):
             continue
         assert getattr(p, k) == getattr(q, k), k
+
+
+def test_struct_builders_reject_misshaped_arrays():
+    """abi.jvel / abi.uz3d / abi.dyn_diag check every array's shape against the
+    grid before any pointer reaches the library."""
+    import numpy as np
+    nx, ny, nz = 6, 5, 4
+    z = np.linspace(0.0, 1.0, nz)
+    base = {"H_ice": np.zeros((nx, ny), order="F"), "f_ice": np.ones((nx, ny), order="F"),
+            "zeta_aa": z, "zeta_ac": np.linspace(0.0, 1.0, nz + 1)}
+    good = dict(base, ux=np.zeros((nx, ny, nz), order="F"))
+    abi.jvel(good, 1e3, 1e3)
+    abi.uz3d(good, 1e3, 1e3)
+    with pytest.raises(ValueError):
+        abi.jvel(dict(base, ux=np.zeros((nx, ny, nz + 1), order="F")), 1e3, 1e3)
+    with pytest.raises(ValueError):
+        abi.uz3d(dict(base, uz=np.zeros((nx, ny, nz), order="F")), 1e3, 1e3)
+    with pytest.raises(ValueError):
+        abi.dyn_diag({"ux_bar": np.zeros((nx, ny + 1), order="F")}, nx, ny, nz, 1e3, 1e3)
