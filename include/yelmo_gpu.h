@@ -68,9 +68,11 @@ extern "C" {
 #define YGPU_LIN_MINRES       2
 #define YGPU_PRE_NONE         0
 #define YGPU_PRE_JACOBI       1
-#define YGPU_PRE_ILU0         2   /* GPU, energy form with CG: block Jacobi with the exact inverse
-                                     of each 4x4-cell tile block (32 unknowns, inverted in FP32);
-                                     Jacobi for the residual form and BiCGSTAB                  */
+#define YGPU_PRE_ILU0         2   /* requested "-p ilu"; what runs for it on the GPU is reported
+                                     in ygpu_stats.lin_precond_run                            */
+#define YGPU_PRE_TILE_BLOCK   3   /* run only (never parsed): block Jacobi with the exact inverse
+                                     of each 4x4-cell tile block (32 unknowns, inverted in FP32),
+                                     what "-p ilu" runs for CG on the energy form             */
 
 /* ---- arithmetic of the GPU solve ---- */
 #define YGPU_PREC_FP64        0   /* plain FP64 solve: the drop-in                         */
@@ -137,7 +139,14 @@ typedef struct ygpu_stats {
                                    Krylov, epilogue, final passes; then the time spent in
                                    team all-reduces over the solve and within the Krylov phase */
     int    active_cells;        /* cells with a non-identity row: the cells the Krylov iterations visit */
+    int    lin_solver_run;      /* YGPU_LIN_* the GPU ran for the requested method: MINRES
+                                   requests run CG (energy form) or BiCGSTAB (residual form) */
+    int    lin_precond_run;     /* YGPU_PRE_* the GPU ran for the requested preconditioner   */
 } ygpu_stats;
+
+/* The Krylov method and preconditioner the GPU runs for a parameter set (the
+   values ygpu_stats.lin_solver_run / lin_precond_run report). */
+void ygpu_lin_method_run(const ygpu_dyn_par* par, int* lin_solver_run, int* lin_precond_run);
 
 /* ---- parameter helpers -------------------------------------------------- */
 /* Defaults of input/yelmo_defaults.nml &ydyn (:140-172) and &Earth constants. */
@@ -453,6 +462,9 @@ typedef struct ygpu_tuning {
     unsigned long long max_active_unknowns; /* batches with more unknowns run as a queue:
                                    continuous batching with at most this many unknowns on the
                                    GPU at once (default 1.5 M; 0: always one lockstep batch)  */
+    int spin_log2;              /* for tests of the timeout path: a wait of a team of CTAs
+                                   gives up after 2^spin_log2 polls (1..22) instead of 2^22
+                                   (0, the default), and the solve returns YGPU_ERR_TIMEOUT */
 } ygpu_tuning;
 void ygpu_tuning_defaults(ygpu_tuning* t);
 int  ygpu_ctx_set_tuning(ygpu_ctx* ctx, const ygpu_tuning* t);
@@ -488,18 +500,21 @@ int ygpu_solve_batch_host(int kind, const ygpu_dyn_par* par, int n_inst, const y
 /*
  * ygpu_solve_device_noalloc -- no counterpart in the reference.
  * One solve on device-resident fields, like ygpu_solve_device, for callers that
- * cannot allocate device memory: a host capturing its work into a CUDA graph,
- * a host whose device memory belongs to another runtime or pool, a server that
- * must not grow after start-up. The call allocates nothing: its scratch is a
- * fixed array of YGPU_NOALLOC_SCRATCH_BYTES inside the library, held by every
+ * cannot allocate device memory: a host whose device memory belongs to another
+ * runtime or to a pool allocator that must account for every byte, or a server
+ * that must not grow after start-up. The call allocates nothing: its scratch is
+ * a fixed array of YGPU_NOALLOC_SCRATCH_BYTES inside the library, held by every
  * GPU that loads the library until the process exits. Instances whose scratch
  * does not fit are rejected with YGPU_ERR_BAD_ARG (a 161x161x10 FP64 solve needs
- * about 24 MB). The first call on a device looks up the array's device address;
- * make that first call before any stream capture. All calls share the array and
- * it keeps the last call's contents: calls that overlap on the GPU race, so
- * serialise them. stream is a cudaStream_t (NULL: the legacy default stream);
- * the call returns after that stream has finished the solve. stats->device_ms
- * is 0 (no events are created).
+ * about 24 MB). The first call on a device looks up the array's device address
+ * and checks that the kernels' stack (about 1 KB per thread) fits the context's
+ * stack limit, which it does not raise; make that first call before any stream
+ * capture. All calls share the array and it keeps the last call's contents:
+ * calls that overlap on the GPU race, so serialise them. A neff hook is not run
+ * here: with one set on the calling thread a DIVA solve returns YGPU_ERR_BAD_ARG.
+ * stream is a cudaStream_t (NULL: the legacy default stream); the call returns
+ * after that stream has finished the solve. stats->device_ms is 0 (no events
+ * are created).
  */
 #define YGPU_NOALLOC_SCRATCH_BYTES (64u << 20)
 int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, const ygpu_fields* f,

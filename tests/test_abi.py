@@ -87,3 +87,21 @@ def test_struct_builders_reject_misshaped_arrays():
         abi.uz3d(dict(base, uz=np.zeros((nx, ny, nz), order="F")), 1e3, 1e3)
     with pytest.raises(ValueError):
         abi.dyn_diag({"ux_bar": np.zeros((nx, ny + 1), order="F")}, nx, ny, nz, 1e3, 1e3)
+
+
+@pytest.mark.parametrize("solver,opt,want", [
+    ("energy", "-i cg -p jacobi", (abi.LIN_CG, abi.PRE_JACOBI)),
+    ("energy", "-i cg -p ilu", (abi.LIN_CG, abi.PRE_TILE_BLOCK)),
+    ("energy", "-i minres -p jacobi", (abi.LIN_CG, abi.PRE_JACOBI)),
+    ("energy", "-i bicgstab -p ilu", (abi.LIN_BICGSTAB, abi.PRE_JACOBI)),
+    ("residual", "-i minres -p jacobi", (abi.LIN_BICGSTAB, abi.PRE_JACOBI)),
+    ("residual", "-i cg -p none", (abi.LIN_BICGSTAB, abi.PRE_NONE)),
+])
+def test_method_run_is_reported(solver, opt, want):
+    """ygpu_lin_method_run names the Krylov method and preconditioner the GPU runs
+    for a request (the values the solve's stats carry), so a substitution is visible."""
+    L = gpu.lib()
+    p = YdynParams(ssa_solver=solver, ssa_lis_opt_energy=opt, ssa_lis_opt_residual=opt).to_c()
+    s, pc = C.c_int(-1), C.c_int(-1)
+    L.ygpu_lin_method_run(C.byref(p), C.byref(s), C.byref(pc))
+    assert (s.value, pc.value) == want

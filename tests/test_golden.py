@@ -93,3 +93,18 @@ def test_gpu_matches_post_solve_golden(bc):
                 {k: v for k, v in outputs.items() if k.startswith("diag_")}, 1e-14)
     _check_post({k: v for k, v in got.items() if not k.startswith("diag_")},
                 {k: v for k, v in outputs.items() if not k.startswith("diag_")}, 1e-12)
+
+
+def test_continent_fixture_matches_its_builder():
+    """The full-size continent fixture (make_continent_golden.py) was solved on the
+    inputs the seeded builder makes: the oracle's prologue here gives its masks bit
+    for bit, and it stopped at the Picard limit."""
+    import oracle
+    from tests.golden.make_continent_golden import NAME, PICARD_ITERS, VEL_KEYS, continent_case
+    d = np.load(os.path.join(HERE, NAME + ".npz"))
+    f0 = oracle.prepare(continent_case())
+    for k in ("ssa_mask_acx", "ssa_mask_acy"):
+        np.testing.assert_array_equal(f0[k], d[k].astype(np.int32), err_msg=k)
+    assert int(d["ssa_iter_now"]) == PICARD_ITERS
+    for k in VEL_KEYS:
+        assert d[k].shape == f0["H_ice"].shape and np.all(np.isfinite(d[k])), k

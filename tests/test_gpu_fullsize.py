@@ -1,0 +1,115 @@
+"""The GPU solve against the oracle at the full sizes of the benchmark workloads.
+
+- Dome SSA, 81 x 81, dx 16 km, residual form with BiCGSTAB: the oracle's ILU(0)
+  request converged to a Picard change < 1e-10 and a linear residual < 1e-12.
+- Marine DIVA, 161 x 161 x 10, dx 8 km, energy form with CG: the same.
+- Continent DIVA, 801 x 801 x 20, dx 4 km, power-law friction q = 1/3: its Picard
+  iteration settles into a cycle near a 2e-3 change and never converges tightly, so
+  both solvers stop after the namelist's 20 Picard iterations with every linear solve
+  converged to 1e-12 (a Picard-limit comparison), against the oracle's answer in
+  tests/golden/continent_diva_801_picard20.npz (make_continent_golden.py).
+
+The SSA masks and the prologue are bit-exact; velocities (2D and 3D), viscosity,
+basal stress and the effective friction are held to 1e-6 relative L2 (the parity
+bar). FP64 runs at the oracle's tolerances; mixed precision runs its inner FP32
+solves inside the FP64 defect correction, with the Picard change to 1e-9 (its FP32
+viscosity sets the fixed point to about 1e-7).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tests.cases import rel_l2
+from yelmo_gb300 import configs, gpu
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+FP64_SET = dict(ssa_iter_max=400, ssa_iter_conv=1e-10,
+                ssa_lis_opt_energy="-i cg -p jacobi -maxiter 50000 -tol 1.0e-12",
+                ssa_lis_opt_residual="-i bicgstab -p ilu -maxiter 50000 -tol 1.0e-12")
+MIXED_SET = dict(ssa_iter_max=400, ssa_iter_conv=1e-9,
+                 ssa_lis_opt_energy="-i cg -p jacobi -maxiter 50000 -tol 1.0e-11",
+                 ssa_lis_opt_residual="-i bicgstab -p ilu -maxiter 50000 -tol 1.0e-11")
+
+
+def _copy(f):
+    return {k: (v.copy(order="F") if isinstance(v, np.ndarray) else v) for k, v in f.items()}
+
+
+def _workload(name):
+    return {"dome_ssa_81": configs.dome_ssa, "marine_diva_161": configs.marine_diva}[name]()
+
+
+_ORACLE = {}
+
+
+def _oracle_answer(name):
+    """The oracle's tightly converged answer and the shared input state (cached per
+    workload: the oracle takes a few seconds at 161 x 161)."""
+    if name not in _ORACLE:
+        inst = _workload(name)
+        inst.par = inst.par.with_(**FP64_SET)
+        f0 = oracle.prepare(inst)
+        fo = _copy(f0)
+        out = oracle.calc_velocity(fo, inst)
+        assert out["status"] == 0 and out["ssa_iter_now"] < FP64_SET["ssa_iter_max"], out
+        _ORACLE[name] = (inst, f0, fo, out)
+    return _ORACLE[name]
+
+
+@pytest.mark.parametrize("name", ["dome_ssa_81", "marine_diva_161"])
+def test_fullsize_prologue_and_masks_bit_exact(name):
+    inst, f0, _, _ = _oracle_answer(name)
+    g = gpu.prepare(inst)
+    for k in ("ssa_mask_acx", "ssa_mask_acy", "mask_frnt", "f_ice", "f_grnd", "f_grnd_acx", "f_grnd_acy",
+              "H_grnd", "taud_acx", "taud_acy", "taul_int_acx", "taul_int_acy"):
+        assert np.array_equal(g[k], f0[k]), k
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("name", ["dome_ssa_81", "marine_diva_161"])
+def test_fullsize_solve_matches_oracle(name, precision):
+    inst, f0, fo, outo = _oracle_answer(name)
+    par = inst.par.with_(**(FP64_SET if precision == "fp64" else MIXED_SET)).with_(precision=precision)
+    fg = _copy(f0)
+    outg = gpu.calc_velocity(fg, inst.dx, inst.n_glen, par)
+    assert outg["status"] == 0, outg
+    keys = ["ux_b", "uy_b", "visc_eff", "visc_eff_int", "taub_acx", "taub_acy", "beta_acx", "beta_acy"]
+    if inst.par.solver != "ssa":
+        keys += ["ux_bar", "uy_bar", "ux", "uy", "duxdz", "duydz", "beta_eff"]
+    errs = {k: rel_l2(fg[k], fo[k]) for k in keys}
+    print(name, precision, outg, {k: f"{e:.2e}" for k, e in errs.items()})
+    for k, e in errs.items():
+        assert e <= TOL, (k, e, errs)
+    assert np.array_equal(fg["ssa_mask_acx"], fo["ssa_mask_acx"])
+    assert np.array_equal(fg["ssa_mask_acy"], fo["ssa_mask_acy"])
+    assert abs(outg["ssa_lim_n"] - outo["ssa_lim_n"]) <= 2
+
+
+def _continent():
+    from tests.golden.make_continent_golden import NAME, continent_case
+    inst = continent_case()
+    d = np.load(os.path.join(HERE, "golden", NAME + ".npz"))
+    return inst, d
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_continent_picard_limit_matches_oracle_fixture(precision):
+    """801 x 801 x 20: both solvers stop at the 20th Picard iteration, every linear
+    solve converged to 1e-12 (mixed: FP32 inner solves, FP64 defect correction)."""
+    inst, d = _continent()
+    f = gpu.prepare(inst)
+    # the rebuilt inputs have the discrete structure the oracle solved
+    assert np.array_equal(f["ssa_mask_acx"], d["ssa_mask_acx"].astype(np.int32))
+    assert np.array_equal(f["ssa_mask_acy"], d["ssa_mask_acy"].astype(np.int32))
+    out = gpu.calc_velocity(f, inst.dx, inst.n_glen, inst.par.with_(precision=precision))
+    assert out["status"] == 0 and out["ssa_iter_now"] == int(d["ssa_iter_now"]), out
+    errs = {k: rel_l2(f[k], d[k].astype(np.float64)) for k in ("ux_bar", "uy_bar", "ux_b", "uy_b")}
+    print("continent", precision, out, {k: f"{e:.2e}" for k, e in errs.items()})
+    for k, e in errs.items():
+        assert e <= TOL, (k, e, errs)

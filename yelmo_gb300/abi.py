@@ -32,7 +32,7 @@ LATBC_CODES = {"none": 0, "floating": 1, "float": 1, "marine": 2, "all": 3}
 SSA_SOLVER_CODES = {"residual": 0, "energy": 1}
 VEL_LIM_CODES = {"clip": 0, "drag": 1}
 LIN_CG, LIN_BICGSTAB, LIN_MINRES = 0, 1, 2
-PRE_NONE, PRE_JACOBI, PRE_ILU0 = 0, 1, 2
+PRE_NONE, PRE_JACOBI, PRE_ILU0, PRE_TILE_BLOCK = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 KIND_SSA, KIND_DIVA = 0, 1
 
@@ -62,6 +62,7 @@ class Stats(C.Structure):
         ("ssa_lim_n", C.c_int), ("ssa_resid", C.c_double), ("lin_resid", C.c_double),
         ("outer_iter", C.c_int), ("status", C.c_int), ("device_ms", C.c_double),
         ("phase_ms", C.c_double * 10), ("active_cells", C.c_int),
+        ("lin_solver_run", C.c_int), ("lin_precond_run", C.c_int),
     ]
 
     PHASES = ("setup", "strain", "column", "faces", "system", "krylov", "epilogue", "final", "sync_all",
@@ -192,7 +193,7 @@ class Fields(C.Structure):
 class Tuning(C.Structure):
     """ygpu_tuning."""
     _fields_ = [("check_every", C.c_int), ("use_graphs", C.c_int), ("unknowns_per_cta", C.c_int),
-                ("max_active_unknowns", C.c_ulonglong)]
+                ("max_active_unknowns", C.c_ulonglong), ("spin_log2", C.c_int)]
 
 
 class ServerCfg(C.Structure):

@@ -178,6 +178,7 @@ struct ygpu_ctx {
     std::vector<double> hook_buf;   // host buffers of the neff hook
     int unknowns_per_cta = 0;       // team size: unknowns per CTA (0: 2 x block)
     size_t max_active_unknowns = 1500000;   // batches beyond this run as a queue (continuous batching)
+    int spin_log2 = 0;              // team waits give up after 2^spin_log2 polls (0: the default 2^22)
     int* h_flags = nullptr;         // pinned: finished count, abort flag
     int* d_misc = nullptr;          // [0] queue, [1] abort, [2..3] csr out
     double* d_miscd = nullptr;
@@ -209,19 +210,22 @@ extern "C" void ygpu_tuning_defaults(ygpu_tuning* t) {
     t->use_graphs = 1;
     t->unknowns_per_cta = 2 * YG_BLOCK;
     t->max_active_unknowns = 1500000;
+    t->spin_log2 = 0;
 }
 
 extern "C" int ygpu_ctx_set_tuning(ygpu_ctx* c, const ygpu_tuning* t) {
     if (!c || !t) { ygpu_set_error("NULL argument"); return YGPU_ERR_BAD_ARG; }
-    if (t->check_every < 1 || t->check_every > 64 || t->unknowns_per_cta < 32 || t->unknowns_per_cta > (1 << 20)) {
-        ygpu_set_error("tuning out of range: check_every %d (1..64), unknowns_per_cta %d (32..2^20)", t->check_every,
-                       t->unknowns_per_cta);
+    if (t->check_every < 1 || t->check_every > 64 || t->unknowns_per_cta < 32 || t->unknowns_per_cta > (1 << 20) ||
+        t->spin_log2 < 0 || t->spin_log2 > 22) {
+        ygpu_set_error("tuning out of range: check_every %d (1..64), unknowns_per_cta %d (32..2^20), spin_log2 %d "
+                       "(0..22)", t->check_every, t->unknowns_per_cta, t->spin_log2);
         return YGPU_ERR_BAD_ARG;
     }
     c->check_every = t->check_every;
     c->use_graphs = (t->use_graphs != 0);
     c->unknowns_per_cta = t->unknowns_per_cta;
     c->max_active_unknowns = t->max_active_unknowns;
+    c->spin_log2 = t->spin_log2;
     ygpu_graph_cache_clear(&c->graph);
     return YGPU_OK;
 }
@@ -237,7 +241,8 @@ extern "C" ygpu_ctx* ygpu_ctx_create(int device) {
         delete c;
         return nullptr;
     }
-    // the solver kernel's non-inlined phases need more than the default 1 KB of stack per thread
+    // the step kernels' non-inlined phases take up to about 1 KB of stack per thread
+    // (ptxas' cumulative stack size), at the default limit: give them 4 KB
     size_t stack = 0;
     cudaDeviceGetLimit(&stack, cudaLimitStackSize);
     if (stack < 4096) cudaDeviceSetLimit(cudaLimitStackSize, 4096);
@@ -277,6 +282,21 @@ static thread_local void* t_hook_user = nullptr;
 extern "C" void ygpu_set_neff_hook(ygpu_neff_hook hook, void* user) {
     t_hook = hook;
     t_hook_user = hook ? user : nullptr;
+}
+bool ygpu_neff_hook_is_set() { return t_hook != nullptr; }
+
+// The method and preconditioner linear_solve (ygpu_solver.cu) runs for a
+// parameter set: CG on the energy form unless BiCGSTAB is asked for, BiCGSTAB
+// on the residual form; "-p ilu" is the tile block preconditioner with CG on
+// the energy form and Jacobi otherwise.
+extern "C" void ygpu_lin_method_run(const ygpu_dyn_par* p, int* solver, int* precond) {
+    if (!p) return;
+    const bool energy = (p->ssa_solver == YGPU_SSA_ENERGY);
+    const bool cg = energy && p->lin_solver != YGPU_LIN_BICGSTAB;
+    int pc = p->lin_precond;
+    if (pc == YGPU_PRE_ILU0) pc = cg ? YGPU_PRE_TILE_BLOCK : YGPU_PRE_JACOBI;
+    if (solver) *solver = cg ? YGPU_LIN_CG : YGPU_LIN_BICGSTAB;
+    if (precond) *precond = pc;
 }
 
 // default context of the calling thread (host-pointer entry points)
@@ -551,7 +571,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     CK(cudaEventRecord(c->e0, c->stream));
     st = ygpu_launch_solver(c->device, c->stream, c->d_insts, n, *par, c->d_ctl, n_ctl, team_ctas, c->d_misc,
                             c->d_misc + 1, mapped ? c->d_map : nullptr, map_grid, c->use_graphs ? &c->graph : nullptr,
-                            c->h_flags, c->check_every, hooked ? &hr : nullptr);
+                            c->h_flags, c->check_every, hooked ? &hr : nullptr, c->spin_log2);
     if (st) return st;
     CK(cudaEventRecord(c->e1, c->stream));
     c->h_out.resize(n);
@@ -575,6 +595,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
             S.ssa_resid = o.resid;
             S.lin_resid = o.lin_resid;
             S.outer_iter = o.outer_iter; S.active_cells = o.n_active;
+            ygpu_lin_method_run(par, &S.lin_solver_run, &S.lin_precond_run);
             S.status = s_k;
             S.device_ms = ms;
             for (int q = 0; q < 10; q++) S.phase_ms[q] = o.phase_ns[q] * 1e-6;
@@ -650,6 +671,8 @@ static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     CK(cudaMemsetAsync(d_out, 0, sizeof(InstOut) * (size_t)n, c->stream));
     CK(cudaMemsetAsync(c->d_misc, 0, 2 * sizeof(int), c->stream));
     CK(cudaMemsetAsync(c->d_ctl, 0, sizeof(TeamCtl) * (size_t)n_ctl, c->stream));
+    if (c->spin_log2 > 0)
+        CK(cudaMemset2DAsync(&c->d_ctl[0].spin_log2, sizeof(TeamCtl), c->spin_log2, 1, (size_t)n_ctl, c->stream));
     CK(cudaEventRecord(c->e0, c->stream));
     std::vector<int> slot_of(n, -1), free_slots;
     for (int k = n_slots - 1; k >= 0; k--) free_slots.push_back(k);
@@ -780,6 +803,7 @@ static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
             S.ssa_resid = o.resid;
             S.lin_resid = o.lin_resid;
             S.outer_iter = o.outer_iter; S.active_cells = o.n_active;
+            ygpu_lin_method_run(par, &S.lin_solver_run, &S.lin_precond_run);
             S.status = s_k;
             S.device_ms = ms;
             for (int q = 0; q < 10; q++) S.phase_ms[q] = o.phase_ns[q] * 1e-6;

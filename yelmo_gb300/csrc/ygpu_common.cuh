@@ -170,6 +170,7 @@ struct TeamCtl {
     unsigned int base;
     int abort;
     int inst;                      // instance the team works on (work queue)
+    unsigned char spin_log2;       // 0: waits give up after YG_SPIN_LIMIT polls; k: after 2^k
     double slots[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
 };
 
@@ -181,6 +182,7 @@ struct Team {
     int* abort_all;                // whole-launch abort flag (timeout anywhere)
     double sync_ns;                // time CTA 0 / thread 0 spent in team all-reduces
     unsigned gen;                  // thread 0: count target of the last team barrier
+    unsigned spin_lim;             // thread 0: polls after which a wait gives up
 };
 
 YG_DEV unsigned ld_acquire_u32(const unsigned int* p) {
@@ -196,8 +198,14 @@ YG_DEV int ld_acquire_s32(const int* p) {
 
 // Spin budget of one barrier wait: 2^22 acquire polls of the L2 (about a
 // second or more). A wait that runs out sets the abort flags; every later wait of the
-// launch returns at once, and the kernel reports YGPU_ERR_TIMEOUT.
+// launch returns at once, and the kernel reports YGPU_ERR_TIMEOUT. The control
+// block can lower the budget to 2^spin_log2 polls (ygpu_tuning.spin_log2, for tests
+// of the timeout path).
 #define YG_SPIN_LIMIT (1u << 22)
+YG_DEV unsigned team_spin_limit(const TeamCtl* c) {
+    const unsigned k = *(const volatile unsigned char*)&c->spin_log2;
+    return (k == 0u || k > 22u) ? YG_SPIN_LIMIT : (1u << k);
+}
 
 YG_DEV void red_release_add_u32(unsigned int* p, unsigned v) {
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
@@ -217,9 +225,10 @@ YG_DEV bool team_barrier(Team& T) {
             red_release_add_u32(&T.ctl->count, 1u);
             unsigned n = 0;
             while ((int)(ld_acquire_u32(&T.ctl->count) - T.gen) < 0) {
-                if ((++n & 1023u) == 0u) {
+                ++n;
+                if ((n & 1023u) == 0u || n >= T.spin_lim) {
                     if (ld_acquire_s32(T.abort_all)) { ok = 0; break; }
-                    if (n > YG_SPIN_LIMIT) {
+                    if (n >= T.spin_lim) {
                         atomicExch(T.abort_all, 1);
                         atomicExch(&T.ctl->abort, 1);
                         ok = 0;

@@ -86,7 +86,8 @@ struct NeffRun {
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
                        TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort,
                        const int* d_map = nullptr, int map_grid = 0, GraphCache* gc = nullptr,
-                       int* h_flags = nullptr, int check_every = 4, const NeffRun* hook = nullptr);
+                       int* h_flags = nullptr, int check_every = 4, const NeffRun* hook = nullptr,
+                       int spin_log2 = 0);
 int ygpu_sm_count(int device);
 size_t ygpu_teamctl_bytes();
 size_t ygpu_inst_bytes();
@@ -115,6 +116,8 @@ int ygpu_ssa_masks_device(cudaStream_t s, int* mx, int* my, const int* mf, const
 // ygpu_api.cu internals shared with the other translation units
 struct ygpu_fields;
 int ygpu_check_par(const ygpu_dyn_par* p);
+// a neff hook is set on the calling thread (ygpu_set_neff_hook)
+bool ygpu_neff_hook_is_set();
 int ygpu_fields_check(int kind, const ygpu_fields* f);
 void ygpu_fill_inst(Inst& I, int kind, const ygpu_fields* f);
 // block: scratch for the tile-block preconditioner (mixed mode, -p ilu)

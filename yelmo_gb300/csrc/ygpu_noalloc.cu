@@ -1,13 +1,19 @@
 // ygpu_noalloc.cu -- a solve entry point that allocates no device memory.
 //
-// Some callers cannot call cudaMalloc: a host that captures its work into a
-// CUDA graph (allocation is not allowed during stream capture), a Fortran or
-// C host whose device memory is owned by another runtime or pool allocator,
-// or a long-running server that must not grow its footprint after start-up.
-// ygpu_solve_device_noalloc solves one instance on device-resident fields the
-// caller passes, exactly like ygpu_solve_device, but keeps all of its scratch
-// (instance descriptor, team control block, Krylov vectors, viscosity
-// buffers) in the file-scope array below instead of a context arena.
+// Some callers cannot call cudaMalloc: a Fortran or C host whose device memory
+// is owned by another runtime or by a pool allocator that must see every
+// allocation, or a long-running server that must not grow its footprint after
+// start-up. ygpu_solve_device_noalloc solves one instance on device-resident
+// fields the caller passes, with the same kernels and the same answer as
+// ygpu_solve_device, but keeps all of its scratch (instance descriptor, team
+// control block, Krylov vectors, viscosity buffers) in the file-scope array
+// below instead of a context arena. It has no neff hook: with a hook set on the
+// calling thread, a DIVA solve is refused (the hook's per-iteration round trip
+// belongs to the context entry points).
+//
+// The first call on a device also checks that the step kernels' stack (ptxas'
+// cumulative stack size, about 1 KB per thread) fits the context's stack
+// limit; it does not raise the limit, since that reserves device memory.
 //
 // The array has a fixed size, YGPU_NOALLOC_SCRATCH_BYTES (64 MiB), and every
 // GPU that loads this library holds it until the process exits. Its device
@@ -89,6 +95,11 @@ extern "C" int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, cons
         return YGPU_ERR_BAD_ARG;
     }
     if ((st = ygpu_fields_check(kind, f))) return st;
+    if (kind == YGPU_KIND_DIVA && ygpu_neff_hook_is_set()) {
+        ygpu_set_error("a neff hook is set on this thread: the allocation-free entry point does not run it "
+                       "(use ygpu_solve_device or ygpu_calc_velocity_diva, or clear the hook)");
+        return YGPU_ERR_BAD_ARG;
+    }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) {
@@ -150,6 +161,7 @@ extern "C" int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, cons
         stats->ssa_resid = o.resid;
         stats->lin_resid = o.lin_resid;
         stats->outer_iter = o.outer_iter; stats->active_cells = o.n_active;
+        ygpu_lin_method_run(par, &stats->lin_solver_run, &stats->lin_precond_run);
         stats->status = status;
         for (int q = 0; q < 10; q++) stats->phase_ms[q] = o.phase_ns[q] * 1e-6;
     }

@@ -361,6 +361,7 @@ static void retire_locked(ygpu_server* S) {
         St.ssa_resid = o.resid;
         St.lin_resid = o.lin_resid;
         St.outer_iter = o.outer_iter; St.active_cells = o.n_active;
+        ygpu_lin_method_run(&S->cfg.par, &St.lin_solver_run, &St.lin_precond_run);
         St.status = R.status;
         St.device_ms = (R.t_done - R.t_admit) * 1e3;
         for (int q = 0; q < 10; q++) St.phase_ms[q] = o.phase_ns[q] * 1e-6;
@@ -416,7 +417,8 @@ extern "C" ygpu_server* ygpu_server_create(const ygpu_server_cfg* cfg) {
     if (cfg->kind != YGPU_KIND_SSA && cfg->kind != YGPU_KIND_DIVA) { ygpu_set_error("bad solver kind %d", cfg->kind); return nullptr; }
     if (cfg->dH_sigma < 0.0) { ygpu_set_error("dH_sigma must be >= 0"); return nullptr; }
     if (cudaSetDevice(cfg->device) != cudaSuccess) { ygpu_set_error("cannot use device %d", cfg->device); return nullptr; }
-    // the step kernels' non-inlined phases need more than the default 1 KB of stack per thread
+    // the step kernels' non-inlined phases take up to about 1 KB of stack per thread
+    // (ptxas' cumulative stack size), at the default limit: give them 4 KB
     size_t stack = 0;
     cudaDeviceGetLimit(&stack, cudaLimitStackSize);
     if (stack < 4096) cudaDeviceSetLimit(cudaLimitStackSize, 4096);

@@ -2894,6 +2894,7 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
     T.abort_all = abort_all;
     T.sync_ns = 0.0;
     T.gen = (threadIdx.x == 0) ? ld_acquire_u32(&T.ctl->base) : 0u;
+    T.spin_lim = (threadIdx.x == 0) ? team_spin_limit(T.ctl) : 0u;
     for (int q = team; q < n_inst; q += n_teams) {
         if (threadIdx.x == 0) {
             sI = insts[q];
@@ -2973,6 +2974,7 @@ __global__ void __launch_bounds__(YG_BLOCK) ygpu_csr_kernel(CsrJob J, TeamCtl* c
     T.abort_all = abort_all;
     T.sync_ns = 0.0;
     T.gen = 0u;
+    T.spin_lim = YG_SPIN_LIMIT;
     const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
     // Jacobi diagonal and ||b||
     double bn = 0.0;
@@ -3160,6 +3162,7 @@ __global__ void __launch_bounds__(YG_BLOCK) ygpu_adv_kernel(AdvJob J, TeamCtl* c
     T.abort_all = abort_all;
     T.sync_ns = 0.0;
     T.gen = 0u;
+    T.spin_lim = YG_SPIN_LIMIT;
     const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
     const int nx = J.nx, ny = J.ny, n = nx * ny;
     int k[4];
@@ -3576,7 +3579,8 @@ static bool capture_chunk(cudaStream_t stream, const StepShape& sh, const Inst* 
 
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
                        TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort, const int* d_map,
-                       int map_grid, GraphCache* gc, int* h_flags, int check_every, const NeffRun* hook) {
+                       int map_grid, GraphCache* gc, int* h_flags, int check_every, const NeffRun* hook,
+                       int spin_log2) {
     // d_done: count of finished instances; d_abort: launch-wide abort flag.
     // With a team map (one team per instance) n_teams is the number of control
     // blocks to clear (n_inst) and map_grid the CTAs of the plan.
@@ -3585,6 +3589,10 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
     if (cudaMemsetAsync(d_done, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
     if (cudaMemsetAsync(d_abort, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
     if (cudaMemsetAsync(d_ctls, 0, sizeof(TeamCtl) * (size_t)n_teams, stream) != cudaSuccess) return YGPU_ERR_CUDA;
+    // a lower spin budget for the team waits (tests of the timeout path)
+    if (spin_log2 > 0 && cudaMemset2DAsync(&d_ctls[0].spin_log2, sizeof(TeamCtl), spin_log2, 1, (size_t)n_teams,
+                                           stream) != cudaSuccess)
+        return YGPU_ERR_CUDA;
     StepShape sh;
     if (d_map) st = ygpu_step_shape_mapped(device, map_grid, d_map, &sh);
     else st = ygpu_step_shape(device, n_teams, team_ctas, &sh);

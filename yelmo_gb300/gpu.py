@@ -41,7 +41,7 @@ EXPORTS = [
     "ygpu_ctx_set_tuning", "ygpu_set_neff_hook", "ygpu_solve_batch_host", "ygpu_calc_dyn_diagnostics",
     "ygpu_calc_dyn_diagnostics_device", "ygpu_calc_advec2D_impl_lis", "ygpu_advec2D_impl_lis_device",
     "ygpu_calc_gradient_column_ac", "ygpu_calc_gradient_column_ac_device", "ygpu_calc_jacobian_vel_3D",
-    "ygpu_calc_jacobian_vel_3D_device", "ygpu_calc_uz_3D", "ygpu_calc_uz_3D_device",
+    "ygpu_calc_jacobian_vel_3D_device", "ygpu_calc_uz_3D", "ygpu_calc_uz_3D_device", "ygpu_lin_method_run",
 ]
 
 
@@ -114,6 +114,8 @@ def lib(build_if_missing: bool = True):
     L.ygpu_ctx_set_tuning.argtypes = [C.c_void_p, C.POINTER(abi.Tuning)]
     L.ygpu_step_timing.argtypes = [C.c_int]
     L.ygpu_step_timing_get.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
+    L.ygpu_lin_method_run.argtypes = [C.POINTER(abi.DynPar), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.ygpu_lin_method_run.restype = None
     _lib = L
     return L
 
@@ -414,9 +416,10 @@ class DeviceSolver:
         return out
 
     def set_tuning(self, check_every: int = 4, use_graphs: bool = True, unknowns_per_cta: int = 512,
-                   max_active_unknowns: int = 1_500_000):
-        """ygpu_ctx_set_tuning: host-check interval, chunk graphs, team size, queue threshold."""
-        t = abi.Tuning(check_every, 1 if use_graphs else 0, unknowns_per_cta, max_active_unknowns)
+                   max_active_unknowns: int = 1_500_000, spin_log2: int = 0):
+        """ygpu_ctx_set_tuning: host-check interval, chunk graphs, team size, queue threshold;
+        spin_log2 > 0 lowers the team waits' spin budget to 2^spin_log2 polls (tests)."""
+        t = abi.Tuning(check_every, 1 if use_graphs else 0, unknowns_per_cta, max_active_unknowns, spin_log2)
         _check(self.L.ygpu_ctx_set_tuning(self.ctx, C.byref(t)))
         self.tuning = {"check_every": check_every, "use_graphs": bool(use_graphs),
                        "unknowns_per_cta": unknowns_per_cta, "max_active_unknowns": max_active_unknowns}
