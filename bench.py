@@ -409,24 +409,26 @@ def run_reference(args, insts, rank, world):
         return None
     import oracle
     cores = os.cpu_count() or 1
-    oracle.set_threads(cores)
     inst = insts[0]
     f0 = oracle.prepare(inst)
     times, out = [], None
     large = inst.nx * inst.ny > LARGE_CELLS
     k = 2
-    for s in range(args.warmup + args.steps):
-        f = _copy(f0)
-        t = time.perf_counter()
-        if large:
-            # bounded sample: two Picard iterations, scaled to the solve's ssa_iter_max
-            out = oracle.calc_velocity(f, inst, inst.par.with_(ssa_iter_max=k))
-            dt = (time.perf_counter() - t) * inst.par.ssa_iter_max / k
-        else:
-            out = oracle.calc_velocity(f, inst)
-            dt = time.perf_counter() - t
-        if s >= args.warmup:
-            times.append(dt)
+    with oracle.timing_build():
+        oracle.set_threads(cores)
+        for s in range(args.warmup + args.steps):
+            f = _copy(f0)
+            t = time.perf_counter()
+            if large:
+                # bounded sample: two Picard iterations, scaled to the solve's ssa_iter_max
+                out = oracle.calc_velocity(f, inst, inst.par.with_(ssa_iter_max=k))
+                dt = (time.perf_counter() - t) * inst.par.ssa_iter_max / k
+            else:
+                out = oracle.calc_velocity(f, inst)
+                dt = time.perf_counter() - t
+            if s >= args.warmup:
+                times.append(dt)
+    flags = oracle.timing_flags()
     value = len(times) / sum(times)
     sample = (f"{k} Picard iterations per step scaled to {inst.par.ssa_iter_max}" if large
               else f"{len(times)} full solves")
@@ -438,7 +440,8 @@ def run_reference(args, insts, rank, world):
         "config": {"workload": describe(inst, 1), "picard_tol": inst.par.ssa_iter_conv, "lin": inst.par.lis_opt},
         "latency_ms": {"p50": 1e3 * float(np.percentile(times, 50)), "p99": 1e3 * float(np.percentile(times, 99))},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": f"{sample} (oracle: C FP64 restatement, OpenMP, {cores} threads)"},
+                         "sample": f"{sample} (oracle: C FP64 restatement, OpenMP, {cores} threads, "
+                                   f"gcc {flags})"},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "picard_iters": out["ssa_iter_now"], "lin_iters": out["ssa_lin_iter"],
     }
@@ -449,15 +452,18 @@ def cpu_baseline_leg(inst, budget_s=20.0):
     solution, the checker of the GPU results."""
     import oracle
     cores = os.cpu_count() or 1
-    oracle.set_threads(cores)
-    times, sample, f0 = _cpu_sample(inst, oracle, budget_s=budget_s)
-    base = {"value": len(times) / sum(times), "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": f"{sample} (oracle: C FP64 restatement, OpenMP, {cores} threads)"}
-    # the same on one thread (one solve, or the two-iteration sample of large grids)
-    oracle.set_threads(1)
-    t1, sample1, _ = _cpu_sample(inst, oracle, n_max=1, budget_s=0.0)
-    oracle.set_threads(cores)
+    flags = oracle.timing_flags()
+    with oracle.timing_build():
+        oracle.set_threads(cores)
+        times, sample, f0 = _cpu_sample(inst, oracle, budget_s=budget_s)
+        base = {"value": len(times) / sum(times), "unit": "solves/s", "cores": cores, "kind": "port",
+                "sample": f"{sample} (oracle: C FP64 restatement, OpenMP, {cores} threads, gcc {flags})"}
+        # the same on one thread (one solve, or the two-iteration sample of large grids)
+        oracle.set_threads(1)
+        t1, sample1, _ = _cpu_sample(inst, oracle, n_max=1, budget_s=0.0)
+        oracle.set_threads(cores)
     base["one_thread"] = {"value": len(t1) / sum(t1), "unit": "solves/s", "sample": sample1}
+    oracle.set_threads(cores)
     if inst.nx * inst.ny > LARGE_CELLS:
         return base, None
     tight = _copy(f0)

@@ -333,16 +333,29 @@ typedef struct ygpu_jvel {
  *   YGPU_UZ_FLUX (4) calc_uz_3D_flux (:947-1116): uz_star from the layer mass budgets
  *                    with upwind face thicknesses, corrected to the applied transport
  *                    -dHidt_dyn where mask_kin == 1, and uz = uz_star - coordinate terms.
- * uz_method 2 and 3 (calc_uz_3D, calc_uz_3D_jac) map fields to quadrature nodes with
- * fesm-utils' gq2D/gq3D and are not built (YGPU_ERR_BAD_ARG). Ice-free cells take
- * dzbdt - max(smb, 0). nz_ac = nz_aa + 1, 2 <= nz_aa <= 1000. ux_bar, uy_bar, dHidt_dyn
- * and mask_kin are read by YGPU_UZ_FLUX only. uz_srf_err (optional, NULL to skip) is
- * uz_star(:,:,nz_ac) + smb on the fully ice-covered cells and 0 elsewhere
- * (yelmo_dynamics.f90:283-290). FP64, agreeing with the reference expressions to
- * rounding.
+ *   YGPU_UZ_NODES (2) calc_uz_3D (:346-681): the same integration with the base and
+ *                    surface gradients, the velocities and the per-layer horizontal
+ *                    strain rates (calc_strain_rate_horizontal_2D, deformation.f90:
+ *                    1393-1507) taken to the cell centre by the 2D Gauss quadrature;
+ *   YGPU_UZ_JAC  (3) calc_uz_3D_jac (:41-344), the namelist default: the divergence
+ *                    from the velocity Jacobian's dxx and dyy (jac_dxx, jac_dyy, the
+ *                    ux/uy terms of ygpu_calc_jacobian_vel_3D) by the 3D quadrature.
+ * The quadratures restate fesm-utils' gq2D/gq3D, which the reference does not vendor:
+ * corner values are means of the active faces (acx/acy fields) or of the four cells
+ * (aa fields) around each cell corner, and at vertical corners also of the two layers
+ * (or ac levels) that meet there; the 2 (2D) or 8 (3D) Gauss-Legendre nodes at
+ * +-1/sqrt(3) of the half cell interpolate them bilinearly (trilinearly) and the
+ * equal-weight node mean is the cell value. Ice-free cells take dzbdt - max(smb, 0).
+ * nz_ac = nz_aa + 1, 2 <= nz_aa <= 1000. ux_bar, uy_bar, dHidt_dyn and mask_kin are
+ * read by YGPU_UZ_FLUX only, jac_dxx and jac_dyy by YGPU_UZ_JAC only. uz_srf_err
+ * (optional, NULL to skip) is uz_star(:,:,nz_ac) + smb on the fully ice-covered cells
+ * and 0 elsewhere (yelmo_dynamics.f90:283-290). FP64, agreeing with the reference
+ * expressions to rounding.
  */
-#define YGPU_UZ_AA   1
-#define YGPU_UZ_FLUX 4
+#define YGPU_UZ_AA    1
+#define YGPU_UZ_NODES 2
+#define YGPU_UZ_JAC   3
+#define YGPU_UZ_FLUX  4
 typedef struct ygpu_uz3d {
     int nx, ny, nz_aa, nz_ac;
     double dx, dy;
@@ -354,10 +367,48 @@ typedef struct ygpu_uz3d {
     const int* mask_kin;
     /* outputs */
     double *uz, *uz_star, *uz_srf_err;
+    /* YGPU_UZ_JAC: jvel%dxx, jvel%dyy (nx,ny,nz_aa) */
+    const double *jac_dxx, *jac_dyy;
 } ygpu_uz3d;
 
 int ygpu_calc_uz_3D(const ygpu_uz3d* f, int boundaries, int method);
 int ygpu_calc_uz_3D_device(void* stream, const ygpu_uz3d* f, int boundaries, int method);
+
+/*
+ * Strain-rate tensor of calc_ydyn: calc_strain_rate_tensor_jac_quad3D
+ * (src/physics/deformation.f90:963-1183, called at src/yelmo_dynamics.f90:299-300)
+ * from the velocity Jacobian (the outputs of ygpu_calc_jacobian_vel_3D). On the
+ * fully ice-covered cells, per layer: dxx, dyy, dxy = (dxy + dyx)/2, dxz = (dxz +
+ * dzx)/2, dyz = (dyz + dzy)/2 at the cell centre by the 3D quadrature of
+ * ygpu_calc_uz_3D's note (acx fields with the active x faces, acy fields with the
+ * active y faces, dzx and dzy on the two ac levels bounding the layer); the
+ * effective strain rate de = sqrt(dxx^2 + dyy^2 + dxx dyy + dxy^2 + dxz^2 + dyz^2),
+ * capped at de_max; the divergence div = dxx + dyy; the shear fraction
+ * sqrt(dxz^2 + dyz^2)/de (1 where de = 0, 0 on floating cells, clipped to [0,1]).
+ * Zero elsewhere. Then the vertical trapezoid integrals of the eight fields over
+ * zeta_aa (calc_vertical_integrated_2D, yelmo_tools.f90:1064-1122) and the two
+ * eigenvalues of the averaged horizontal tensor, larger first, or 0 when they are
+ * not real and distinct (calc_2D_eigen_values, deformation.f90:1542-1595).
+ * jvel: dxx, dxy, dxz, dyx, dyy, dyz (nx,ny,nz_aa), dzx, dzy (nx,ny,nz_ac). The 2D
+ * outputs may be NULL (skipped). 2 <= nz_aa <= 1000, nz_ac = nz_aa + 1. FP64.
+ */
+typedef struct ygpu_strain3d {
+    int nx, ny, nz_aa, nz_ac;
+    double dx, dy;
+    double de_max;              /* [a-1] cap of the effective strain rate (ymat de_max) */
+    /* inputs */
+    const double *dxx, *dxy, *dxz, *dyx, *dyy, *dyz, *dzx, *dzy;
+    const double *H_ice, *f_ice, *f_grnd, *zeta_aa, *zeta_ac;
+    /* outputs, (nx,ny,nz_aa): strn%dxx ... strn%f_shear */
+    double *s_dxx, *s_dyy, *s_dxy, *s_dxz, *s_dyz, *s_de, *s_div, *s_f_shear;
+    /* outputs, (nx,ny): strn2D%dxx ... strn2D%f_shear, eps_eig_1, eps_eig_2 */
+    double *a_dxx, *a_dyy, *a_dxy, *a_dxz, *a_dyz, *a_de, *a_div, *a_f_shear, *eps_eig_1, *eps_eig_2;
+} ygpu_strain3d;
+
+/* host arrays (staged through the calling thread's default context) */
+int ygpu_calc_strain_rate_tensor(const ygpu_strain3d* s, int boundaries);
+/* device arrays, on `stream` (a cudaStream_t; NULL: the default stream); asynchronous */
+int ygpu_calc_strain_rate_tensor_device(void* stream, const ygpu_strain3d* s, int boundaries);
 
 /* host arrays (staged through the calling thread's default context) */
 int ygpu_calc_jacobian_vel_3D(const ygpu_jvel* jvel, int boundaries, int terms);

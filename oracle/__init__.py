@@ -16,22 +16,48 @@ from yelmo_gb300 import abi
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
-_lib = None
+FAST_LIB_PATH = os.path.join(HERE, "_build", "liboracle_fast.so")
+_libs = {}
+_use_fast = False
 
 
 def build(force: bool = False) -> str:
-    """Compile liboracle.so with the Makefile beside this file."""
-    if force or not os.path.exists(LIB_PATH) or \
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "yelmo_oracle.c")):
+    """Compile liboracle.so (the checker) and liboracle_fast.so (the timed CPU
+    baseline) with the Makefile beside this file."""
+    src = os.path.getmtime(os.path.join(HERE, "yelmo_oracle.c"))
+    if force or any(not os.path.exists(p) or os.path.getmtime(p) < src for p in (LIB_PATH, FAST_LIB_PATH)):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB_PATH
 
 
+def timing_flags() -> str:
+    """Compiler flags of the timed build (liboracle_fast.so) on this host."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "flags"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
+class timing_build:
+    """Context manager: the oracle calls inside it run liboracle_fast.so (-O3,
+    tuned for the host CPU, FMA contraction), the build the CPU baseline times;
+    outside it they run the checker build."""
+
+    def __enter__(self):
+        global _use_fast
+        self._prev = _use_fast
+        _use_fast = True
+        return self
+
+    def __exit__(self, *exc):
+        global _use_fast
+        _use_fast = self._prev
+        return False
+
+
 def lib():
-    global _lib
-    if _lib is None:
+    path = FAST_LIB_PATH if _use_fast else LIB_PATH
+    if path not in _libs:
         build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(path)
         abi.declare_velocity(L.orc_calc_velocity_ssa, abi.SSA_ARGS)
         abi.declare_velocity(L.orc_calc_velocity_diva, abi.DIVA_ARGS)
         abi.declare_velocity(L.orc_calc_velocity_diva_hook, abi.DIVA_ARGS)
@@ -54,8 +80,9 @@ def lib():
         L.orc_calc_gradient_column_ac.argtypes = [dp] * 5 + [ip, C.c_int, C.c_int, C.c_int]
         L.orc_calc_jacobian_vel_3D.argtypes = [C.POINTER(abi.JVel), C.c_int, C.c_int]
         L.orc_calc_uz_3D.argtypes = [C.POINTER(abi.Uz3D), C.c_int, C.c_int]
-        _lib = L
-    return _lib
+        L.orc_calc_strain_rate_tensor.argtypes = [C.POINTER(abi.Strain3D), C.c_int]
+        _libs[path] = L
+    return _libs[path]
 
 
 def set_threads(n: int):
@@ -190,6 +217,15 @@ def calc_uz_3D(arrays: dict, dx: float, dy: float, boundaries: str, method: int 
     if st != 0:
         raise RuntimeError(f"orc_calc_uz_3D failed ({st})")
     return arrays
+
+def calc_strain_rate_tensor(arrays: dict, dx: float, dy: float, boundaries: str, de_max: float = 0.5) -> dict:
+    """orc_calc_strain_rate_tensor on the arrays of yelmo_gb300.gpu.strain_arrays (filled in place)."""
+    S = abi.strain3d(arrays, dx, dy, de_max)
+    st = lib().orc_calc_strain_rate_tensor(C.byref(S), abi.BOUNDARY_CODES[boundaries])
+    if st != 0:
+        raise RuntimeError(f"orc_calc_strain_rate_tensor failed ({st})")
+    return arrays
+
 
 def linear_solve(ptr_, idx, val, b, x, method, precond, maxiter, tol, initx_zeros=False):
     it = C.c_int(0)

@@ -2813,17 +2813,348 @@ static void uz_flux(const ygpu_uz3d* U, int bc) {
     free(dzeta);
 }
 
+
+/* ------------------------------------------------------------------------ */
+/* 3D Gaussian quadrature (fesm-utils gq3D, restated as gq2D above; unpinned) */
+/* ------------------------------------------------------------------------ */
+/* Node q = (qx, qy, qz) in bits 0, 1, 2 (0: -, 1: +) at (sx*g, sy*g, sz*g),
+   g = 1/sqrt(3); corner c likewise; trilinear weight of corner c at node q =
+   prod over the axes of (1 + s_q*s_c*g)/2. The corners are the 8 corners of the
+   cell-layer box: horizontally as gq2D's (SW, SE, NE, NW), vertically the lower
+   and upper face of the layer. The dz arguments of the reference's gq3D calls do
+   not enter the mapping. */
+static double GQ3W[8][8];
+static int gq3_ready = 0;
+
+static void gq3_init(void) {
+    if (gq3_ready) return;
+    double g = 1.0 / sqrt(3.0);
+    for (int q = 0; q < 8; q++)
+        for (int c = 0; c < 8; c++) {
+            double w = 1.0;
+            for (int a = 0; a < 3; a++) {
+                double sq = ((q >> a) & 1) ? 1.0 : -1.0, sc = ((c >> a) & 1) ? 1.0 : -1.0;
+                w = w * ((1.0 + sq * sc * g) * 0.5);
+            }
+            GQ3W[q][c] = w;
+        }
+    gq3_ready = 1;
+}
+
+/* horizontal corner h (0 SW, 1 SE, 2 NE, 3 NW) and level l (0 lower, 1 upper) ->
+   corner index c with bits (x, y, z) */
+static inline int gq3_corner(int h, int l) {
+    static const int hx[4] = {0, 1, 1, 0}, hy[4] = {0, 0, 1, 1};
+    return hx[h] | (hy[h] << 1) | (l << 2);
+}
+
+static inline void gq3_corners_to_nodes(const double c[8], double v[8]) {
+    for (int q = 0; q < 8; q++) {
+        double s = 0.0;
+        for (int k = 0; k < 8; k++) s = s + GQ3W[q][k] * c[k];
+        v[q] = s;
+    }
+}
+
+/* sum(v*wt)/wt_tot with the equal Gauss-Legendre weights */
+static inline double gq3_mean(const double v[8]) {
+    double s = 0.0;
+    for (int q = 0; q < 8; q++) s = s + v[q];
+    return s / 8.0;
+}
+
+/* gq3D_to_nodes_acx on layer k (0-based) with the layers km1, kp1 below and above
+   (clamped by the caller): a lower corner is the mean of the two acx faces beside
+   it on layers km1 and k (active faces only), an upper corner on layers k and kp1 */
+static void gq3_nodes_acx(const double* var, const unsigned char* act, int i, int j, int k, int km1, int kp1,
+                          int im1, int jm1, int jp1, int nx, size_t n2, double v[8]) {
+    double c[8];
+    const int ic[4] = {im1, i, i, im1};
+    const int ja[4] = {jm1, jm1, j, j};
+    const int jb[4] = {j, j, jp1, jp1};
+    const int lay[2][2] = {{km1, k}, {k, kp1}};
+    for (int h = 0; h < 4; h++)
+        for (int l = 0; l < 2; l++) {
+            const double* p0 = var + (size_t)lay[l][0] * n2;
+            const double* p1 = var + (size_t)lay[l][1] * n2;
+            const size_t a = ID2(ic[h], ja[h]), b = ID2(ic[h], jb[h]);
+            double m0 = mean2_act(p0[a], p0[b], act[a], act[b]);
+            double m1 = mean2_act(p1[a], p1[b], act[a], act[b]);
+            c[gq3_corner(h, l)] = 0.5 * (m0 + m1);
+        }
+    gq3_corners_to_nodes(c, v);
+}
+
+/* gq3D_to_nodes_acy: as acx with the two acy faces left and right of a corner */
+static void gq3_nodes_acy(const double* var, const unsigned char* act, int i, int j, int k, int km1, int kp1,
+                          int im1, int ip1, int jm1, int nx, size_t n2, double v[8]) {
+    double c[8];
+    const int ia[4] = {im1, i, i, im1};
+    const int ib[4] = {i, ip1, ip1, i};
+    const int jc[4] = {jm1, jm1, j, j};
+    const int lay[2][2] = {{km1, k}, {k, kp1}};
+    for (int h = 0; h < 4; h++)
+        for (int l = 0; l < 2; l++) {
+            const double* p0 = var + (size_t)lay[l][0] * n2;
+            const double* p1 = var + (size_t)lay[l][1] * n2;
+            const size_t a = ID2(ia[h], jc[h]), b = ID2(ib[h], jc[h]);
+            double m0 = mean2_act(p0[a], p0[b], act[a], act[b]);
+            double m1 = mean2_act(p1[a], p1[b], act[a], act[b]);
+            c[gq3_corner(h, l)] = 0.5 * (m0 + m1);
+        }
+    gq3_corners_to_nodes(c, v);
+}
+
+/* gq3D_to_nodes_acz: a field on the vertical faces (ac levels) and the horizontal
+   cell centres; the lower corners are the means of the four cells around each
+   corner on ac level klo, the upper ones on level khi */
+static void gq3_nodes_acz(const double* var, int i, int j, int klo, int khi, int im1, int ip1, int jm1, int jp1,
+                          int nx, size_t n2, double v[8]) {
+    double c[8];
+    const int ii[4][4] = {{im1, i, im1, i}, {i, ip1, i, ip1}, {i, ip1, i, ip1}, {im1, i, im1, i}};
+    const int jj[4][4] = {{jm1, jm1, j, j}, {jm1, jm1, j, j}, {j, j, jp1, jp1}, {j, j, jp1, jp1}};
+    const int lev[2] = {klo, khi};
+    for (int h = 0; h < 4; h++)
+        for (int l = 0; l < 2; l++) {
+            const double* p = var + (size_t)lev[l] * n2;
+            double s = p[ID2(ii[h][0], jj[h][0])] + p[ID2(ii[h][1], jj[h][1])];
+            s = s + p[ID2(ii[h][2], jj[h][2])];
+            s = s + p[ID2(ii[h][3], jj[h][3])];
+            c[gq3_corner(h, l)] = 0.25 * s;
+        }
+    gq3_corners_to_nodes(c, v);
+}
+
+/* the 2D quadrature value of an acx / acy field at cell (i, j) */
+static inline double gq_acx_value(const double* var, const unsigned char* act, int i, int j, int im1, int jm1,
+                                  int jp1, int nx) {
+    double v[4];
+    gq_nodes_acx(var, act, i, j, im1, jm1, jp1, nx, v);
+    return gq_mean(v);
+}
+static inline double gq_acy_value(const double* var, const unsigned char* act, int i, int j, int im1, int ip1,
+                                  int jm1, int nx) {
+    double v[4];
+    gq_nodes_acy(var, act, i, j, im1, ip1, jm1, nx, v);
+    return gq_mean(v);
+}
+
+/* calc_uz_3D (uz_method 2), velocity_general.f90:346-681, and calc_uz_3D_jac
+   (uz_method 3), :41-344 (0-based: ac level kc, aa layer ka) */
+static void uz_quad(const ygpu_uz3d* U, int bc, int jac) {
+    const int nx = U->nx, ny = U->ny, nza = U->nz_aa, nzc = U->nz_ac;
+    const size_t n2 = (size_t)nx * ny;
+    const double *za = U->zeta_aa, *zc = U->zeta_ac, *ux = U->ux, *uy = U->uy;
+    const double f_bmb = U->use_bmb ? 1.0 : 0.0;
+    gq_init();
+    gq3_init();
+    unsigned char* ax = malloc(n2);
+    unsigned char* ay = malloc(n2);
+    active_faces(ax, ay, U->f_ice, bc, nx, ny);
+    double *dudx = NULL, *dvdy = NULL;
+    if (!jac) {
+        /* the per-layer horizontal strain rates (:453-458), no sigma correction */
+        dudx = malloc(n2 * (size_t)nza * sizeof(double));
+        dvdy = malloc(n2 * (size_t)nza * sizeof(double));
+        double* dudy = malloc(n2 * sizeof(double));
+        double* dvdx = malloc(n2 * sizeof(double));
+        for (int k = 0; k < nza; k++)
+            strain_rate_2D(dudx + (size_t)k * n2, dudy, dvdx, dvdy + (size_t)k * n2, ux + (size_t)k * n2,
+                           uy + (size_t)k * n2, U->f_ice, ax, ay, U->dx, U->dy, bc, nx, ny);
+        free(dudy);
+        free(dvdx);
+    }
+#pragma omp parallel for collapse(2)
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            int im1, ip1, jm1, jp1;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            const size_t c = ID2(i, j);
+            const double dzsdt_now = U->dzsdt[c], dzbdt_now = U->dzbdt[c];
+            if (U->f_ice[c] == 1.0) {
+                const double H_now = U->H_ice[c], H_inv = 1.0 / H_now;
+                const double dzbdx_aa = gq_acx_value(U->dzbdx, ax, i, j, im1, jm1, jp1, nx);
+                const double dzbdy_aa = gq_acy_value(U->dzbdy, ay, i, j, im1, ip1, jm1, nx);
+                const double dzsdx_aa = gq_acx_value(U->dzsdx, ax, i, j, im1, jm1, jp1, nx);
+                const double dzsdy_aa = gq_acy_value(U->dzsdy, ay, i, j, im1, ip1, jm1, nx);
+                double ux_aa = gq_acx_value(ux, ax, i, j, im1, jm1, jp1, nx);
+                double uy_aa = gq_acy_value(uy, ay, i, j, im1, ip1, jm1, nx);
+                const double uz_grid = 0.0;
+                /* basal value, Greve and Blatter (2009) Eq. 5.31 */
+                U->uz[c] = flush_tiny(dzbdt_now + uz_grid + f_bmb * U->bmb[c] + ux_aa * dzbdx_aa + uy_aa * dzbdy_aa);
+                for (int kc = 1; kc < nzc; kc++) {
+                    double dudx_aa, dvdy_aa;
+                    if (jac) {
+                        /* :218-233: layer kmid below the level, its neighbours clamped */
+                        const int kmid = kc - 1;
+                        const int km1 = kmid > 0 ? kmid - 1 : 0, kp1 = kmid < nza - 1 ? kmid + 1 : nza - 1;
+                        double v[8];
+                        gq3_nodes_acx(U->jac_dxx, ax, i, j, kmid, km1, kp1, im1, jm1, jp1, nx, n2, v);
+                        dudx_aa = gq3_mean(v);
+                        gq3_nodes_acy(U->jac_dyy, ay, i, j, kmid, km1, kp1, im1, ip1, jm1, nx, n2, v);
+                        dvdy_aa = gq3_mean(v);
+                    } else {
+                        /* :535-579 */
+                        const double zeta_now = za[kc - 1];
+                        const double c_x = -H_inv * ((1.0 - zeta_now) * dzbdx_aa + zeta_now * dzsdx_aa);
+                        const double c_y = -H_inv * ((1.0 - zeta_now) * dzbdy_aa + zeta_now * dzsdy_aa);
+                        int kup, kdn;
+                        if (kc == 1) { kup = 1; kdn = 0; }
+                        else if (kc == nzc - 1) { kup = kc - 1; kdn = kc - 2; }
+                        else { kup = kc; kdn = kc - 2; }
+                        double vu[4], vd[4], dn[4];
+                        gq_nodes_acx(ux + (size_t)kup * n2, ax, i, j, im1, jm1, jp1, nx, vu);
+                        gq_nodes_acx(ux + (size_t)kdn * n2, ax, i, j, im1, jm1, jp1, nx, vd);
+                        for (int q = 0; q < 4; q++) dn[q] = (vu[q] - vd[q]) / (za[kup] - za[kdn]);
+                        const double dudz_aa = gq_mean(dn);
+                        gq_nodes_acy(uy + (size_t)kup * n2, ay, i, j, im1, ip1, jm1, nx, vu);
+                        gq_nodes_acy(uy + (size_t)kdn * n2, ay, i, j, im1, ip1, jm1, nx, vd);
+                        for (int q = 0; q < 4; q++) dn[q] = (vu[q] - vd[q]) / (za[kup] - za[kdn]);
+                        const double dvdz_aa = gq_mean(dn);
+                        dudx_aa = gq_acx_value(dudx + (size_t)(kc - 1) * n2, ax, i, j, im1, jm1, jp1, nx) +
+                                  c_x * dudz_aa;
+                        dvdy_aa = gq_acy_value(dvdy + (size_t)(kc - 1) * n2, ay, i, j, im1, ip1, jm1, nx) +
+                                  c_y * dvdz_aa;
+                    }
+                    /* Greve and Blatter (2009) Eq. 5.95 */
+                    const double u = U->uz[(size_t)(kc - 1) * n2 + c] - H_now * (zc[kc] - zc[kc - 1]) * (dudx_aa + dvdy_aa);
+                    U->uz[(size_t)kc * n2 + c] = flush_tiny(u);
+                }
+                /* uz_star, Greve and Blatter (2009) Eq. 5.148 (no 1/H) */
+                for (int kc = 0; kc < nzc; kc++) {
+                    int kup, kdn;
+                    if (kc == 0) { kup = 0; kdn = 0; }
+                    else if (kc == nzc - 1) { kup = kc - 1; kdn = kc - 1; }
+                    else { kup = kc; kdn = kc - 1; }
+                    double vu[4], vd[4], vn[4];
+                    gq_nodes_acx(ux + (size_t)kup * n2, ax, i, j, im1, jm1, jp1, nx, vu);
+                    gq_nodes_acx(ux + (size_t)kdn * n2, ax, i, j, im1, jm1, jp1, nx, vd);
+                    for (int q = 0; q < 4; q++) vn[q] = 0.5 * (vu[q] + vd[q]);
+                    ux_aa = gq_mean(vn);
+                    gq_nodes_acy(uy + (size_t)kup * n2, ay, i, j, im1, ip1, jm1, nx, vu);
+                    gq_nodes_acy(uy + (size_t)kdn * n2, ay, i, j, im1, ip1, jm1, nx, vd);
+                    for (int q = 0; q < 4; q++) vn[q] = 0.5 * (vu[q] + vd[q]);
+                    uy_aa = gq_mean(vn);
+                    const double z = zc[kc];
+                    const double c_x = -((1.0 - z) * dzbdx_aa + z * dzsdx_aa);
+                    const double c_y = -((1.0 - z) * dzbdy_aa + z * dzsdy_aa);
+                    const double c_t = -((1.0 - z) * dzbdt_now + z * dzsdt_now);
+                    const size_t o = (size_t)kc * n2 + c;
+                    double us;
+                    if (jac) us = ux_aa * c_x + uy_aa * c_y + U->uz[o] * 1.0 + c_t;
+                    else us = U->uz[o] + ux_aa * c_x + uy_aa * c_y + c_t;
+                    U->uz_star[o] = flush_tiny(us);
+                }
+            } else {
+                for (int kc = 0; kc < nzc; kc++) {
+                    const double u = flush_tiny(dzbdt_now - fmax(U->smb[c], 0.0));
+                    U->uz[(size_t)kc * n2 + c] = u;
+                    U->uz_star[(size_t)kc * n2 + c] = u;
+                }
+            }
+        }
+    free(ax);
+    free(ay);
+    free(dudx);
+    free(dvdy);
+}
+
 int orc_calc_uz_3D(const ygpu_uz3d* U, int bc, int method) {
     if (!U || U->nx < 2 || U->ny < 2 || U->nz_aa < 2 || U->nz_aa > 1000 || U->nz_ac != U->nz_aa + 1)
         return YGPU_ERR_BAD_ARG;
+    if (method == YGPU_UZ_JAC && (!U->jac_dxx || !U->jac_dyy)) return YGPU_ERR_BAD_ARG;
     if (method == YGPU_UZ_AA) uz_aa(U, bc);
     else if (method == YGPU_UZ_FLUX) uz_flux(U, bc);
+    else if (method == YGPU_UZ_NODES) uz_quad(U, bc, 0);
+    else if (method == YGPU_UZ_JAC) uz_quad(U, bc, 1);
     else return YGPU_ERR_BAD_ARG;
     if (U->uz_srf_err) {
         const size_t n2 = (size_t)U->nx * U->ny, top = (size_t)(U->nz_ac - 1) * n2;
         for (size_t c = 0; c < n2; c++)
             U->uz_srf_err[c] = (U->f_ice[c] == 1.0) ? U->uz_star[top + c] + U->smb[c] : 0.0;
     }
+    return YGPU_OK;
+}
+
+/* ======================================================================== */
+/* Strain-rate tensor (calc_ydyn, yelmo_dynamics.f90:299-300)              */
+/* ======================================================================== */
+
+/* calc_2D_eigen_values, deformation.f90:1542-1595 */
+static void eigen_2D(double* e1, double* e2, double txx, double tyy, double txy) {
+    const double a = 1.0, b = -(txx + tyy), c = txx * tyy - txy * txy;
+    if (b * b - 4.0 * a * c > 0.0) {
+        const double root = sqrt(b * b - 4.0 * a * c);
+        const double l1 = (-b + root) / (2.0 * a), l2 = (-b - root) / (2.0 * a);
+        if (l1 > l2) { *e1 = l1; *e2 = l2; }
+        else { *e1 = l2; *e2 = l1; }
+    } else {
+        *e1 = 0.0;
+        *e2 = 0.0;
+    }
+}
+
+/* calc_strain_rate_tensor_jac_quad3D, deformation.f90:963-1183 (0-based layer k) */
+int orc_calc_strain_rate_tensor(const ygpu_strain3d* S, int bc) {
+    if (!S || S->nx < 2 || S->ny < 2 || S->nz_aa < 2 || S->nz_aa > 1000 || S->nz_ac != S->nz_aa + 1)
+        return YGPU_ERR_BAD_ARG;
+    const int nx = S->nx, ny = S->ny, nza = S->nz_aa;
+    const size_t n2 = (size_t)nx * ny, n3 = n2 * (size_t)nza;
+    gq3_init();
+    unsigned char* ax = malloc(n2);
+    unsigned char* ay = malloc(n2);
+    active_faces(ax, ay, S->f_ice, bc, nx, ny);
+    double* out3[8] = {S->s_dxx, S->s_dyy, S->s_dxy, S->s_dxz, S->s_dyz, S->s_de, S->s_div, S->s_f_shear};
+    for (int q = 0; q < 8; q++) memset(out3[q], 0, n3 * sizeof(double));
+#pragma omp parallel for collapse(2) schedule(dynamic, 64)
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const size_t c = ID2(i, j);
+            if (!(S->f_ice[c] == 1.0)) continue;
+            int im1, ip1, jm1, jp1;
+            nbr(i, j, nx, ny, bc, &im1, &ip1, &jm1, &jp1);
+            for (int k = 0; k < nza; k++) {
+                const int km1 = k > 0 ? k - 1 : 0, kp1 = k < nza - 1 ? k + 1 : nza - 1;
+                double dn[8], an[8], bn[8];
+                const size_t o = (size_t)k * n2 + c;
+                gq3_nodes_acx(S->dxx, ax, i, j, k, km1, kp1, im1, jm1, jp1, nx, n2, dn);
+                const double dxx = gq3_mean(dn);
+                gq3_nodes_acx(S->dxy, ax, i, j, k, km1, kp1, im1, jm1, jp1, nx, n2, an);
+                gq3_nodes_acy(S->dyx, ay, i, j, k, km1, kp1, im1, ip1, jm1, nx, n2, bn);
+                for (int q = 0; q < 8; q++) dn[q] = 0.5 * (an[q] + bn[q]);
+                const double dxy = gq3_mean(dn);
+                /* dzx on the ac levels k (below) and k+1 (above) of layer k */
+                gq3_nodes_acx(S->dxz, ax, i, j, k, km1, kp1, im1, jm1, jp1, nx, n2, an);
+                gq3_nodes_acz(S->dzx, i, j, k, k + 1, im1, ip1, jm1, jp1, nx, n2, bn);
+                for (int q = 0; q < 8; q++) dn[q] = 0.5 * (an[q] + bn[q]);
+                const double dxz = gq3_mean(dn);
+                gq3_nodes_acy(S->dyz, ay, i, j, k, km1, kp1, im1, ip1, jm1, nx, n2, an);
+                gq3_nodes_acz(S->dzy, i, j, k, k + 1, im1, ip1, jm1, jp1, nx, n2, bn);
+                for (int q = 0; q < 8; q++) dn[q] = 0.5 * (an[q] + bn[q]);
+                const double dyz = gq3_mean(dn);
+                gq3_nodes_acy(S->dyy, ay, i, j, k, km1, kp1, im1, ip1, jm1, nx, n2, dn);
+                const double dyy = gq3_mean(dn);
+                double de = sqrt(dxx * dxx + dyy * dyy + dxx * dyy + dxy * dxy + dxz * dxz + dyz * dyz);
+                if (de > S->de_max) de = S->de_max;
+                double fs;
+                if (de > 0.0) fs = sqrt(dxz * dxz + dyz * dyz) / de;
+                else fs = 1.0;
+                if (S->f_grnd[c] == 0.0) fs = 0.0;
+                fs = fmin(fmax(fs, 0.0), 1.0);
+                S->s_dxx[o] = dxx; S->s_dyy[o] = dyy; S->s_dxy[o] = dxy; S->s_dxz[o] = dxz;
+                S->s_dyz[o] = dyz; S->s_de[o] = de; S->s_div[o] = dxx + dyy; S->s_f_shear[o] = fs;
+            }
+        }
+    /* vertical averages (calc_vertical_integrated_2D) and the eigenvalues */
+    double* out2[8] = {S->a_dxx, S->a_dyy, S->a_dxy, S->a_dxz, S->a_dyz, S->a_de, S->a_div, S->a_f_shear};
+    for (int q = 0; q < 8; q++) {
+        if (!out2[q]) continue;
+        for (size_t c = 0; c < n2; c++) out2[q][c] = trapz_pt(out3[q] + c, S->zeta_aa, nza, n2);
+    }
+    if (S->eps_eig_1 && S->eps_eig_2 && S->a_dxx && S->a_dyy && S->a_dxy)
+        for (size_t c = 0; c < n2; c++) eigen_2D(&S->eps_eig_1[c], &S->eps_eig_2[c], S->a_dxx[c], S->a_dyy[c], S->a_dxy[c]);
+    free(ax);
+    free(ay);
     return YGPU_OK;
 }
 

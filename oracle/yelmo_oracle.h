@@ -12,9 +12,11 @@
  *     (Hestenes-Stiefel), BiCGSTAB (van der Vorst 1992), MINRES (Paige-Saunders
  *     1975), Jacobi and ILU(0) (Saad, Iterative Methods, 10.3), with LIS's
  *     relative-residual stopping rule ||b-Ax||_2 / ||b||_2 < tol;
- *   - fesm-utils gaussian_quadrature (gq2D_*): 2x2 Gauss-Legendre nodes at
- *     +-1/sqrt(3) of the cell, node values bilinear from corner means (masked
- *     by the `act` faces/cells when given), equal weights.
+ *   - fesm-utils gaussian_quadrature (gq2D_*, gq3D_*): 2x2 (2x2x2)
+ *     Gauss-Legendre nodes at +-1/sqrt(3) of the cell (cell-layer box), node
+ *     values bilinear (trilinear) from corner means (masked by the `act`
+ *     faces/cells when given; in 3D also averaged over the two layers or ac
+ *     levels meeting at a corner), equal weights.
  * Pinning: the assembly is pinned by the reference's known-answer tests
  * (tests/test_ssa_energy*.f90), the converged solve by the reference's
  * analytic benchmarks (A2 radial shelf, tests/bench/src/shelf.jl). The
@@ -167,9 +169,12 @@ int orc_calc_gradient_column_ac(double* dvdx_c, double* dvdy_c, const double* dv
                                 const double* f_ice, const int* mask_ocn, int boundaries, int nx, int ny);
 int orc_calc_jacobian_vel_3D(const ygpu_jvel* J, int boundaries, int terms);
 
-/* Vertical velocity by uz_method (calc_uz_3D_aa, calc_uz_3D_flux,
-   velocity_general.f90:683-1116) and uz_srf_err; the arguments of ygpu_calc_uz_3D. */
+/* Vertical velocity by uz_method (calc_uz_3D_aa, calc_uz_3D, calc_uz_3D_jac,
+   calc_uz_3D_flux, velocity_general.f90:41-1116) and uz_srf_err; the arguments of
+   ygpu_calc_uz_3D. */
 int orc_calc_uz_3D(const ygpu_uz3d* U, int boundaries, int method);
+/* calc_strain_rate_tensor_jac_quad3D (deformation.f90:963-1183) */
+int orc_calc_strain_rate_tensor(const ygpu_strain3d* S, int boundaries);
 
 /* calc_advec2D(solver = "impl-lis"), solver_advection.f90:20-145: the CSR system of
    linear_solver_matrix_advection_csr_2D (:171-487) solved with this oracle's BiCGSTAB

@@ -147,14 +147,15 @@ def jvel(arrays: dict, dx: float, dy: float) -> JVel:
 UZ_INPUTS = ("ux", "uy", "H_ice", "f_ice", "smb", "bmb", "dzbdt", "dzsdt", "dzsdx", "dzsdy", "dzbdx", "dzbdy",
              "zeta_aa", "zeta_ac", "ux_bar", "uy_bar", "dHidt_dyn", "mask_kin")
 UZ_OUTPUTS = ("uz", "uz_star", "uz_srf_err")
-UZ_AA, UZ_FLUX = 1, 4
+UZ_JAC_INPUTS = ("jac_dxx", "jac_dyy")
+UZ_AA, UZ_NODES, UZ_JAC, UZ_FLUX = 1, 2, 3, 4
 
 
 class Uz3D(C.Structure):
     """ygpu_uz3d: arrays of the vertical velocity."""
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz_aa", C.c_int), ("nz_ac", C.c_int),
                 ("dx", C.c_double), ("dy", C.c_double), ("use_bmb", C.c_int)] + \
-        [(n, C.c_void_p) for n in UZ_INPUTS + UZ_OUTPUTS]
+        [(n, C.c_void_p) for n in UZ_INPUTS + UZ_OUTPUTS + UZ_JAC_INPUTS]
 
 
 def uz3d(arrays: dict, dx: float, dy: float, use_bmb: bool = True) -> Uz3D:
@@ -163,17 +164,59 @@ def uz3d(arrays: dict, dx: float, dy: float, use_bmb: bool = True) -> Uz3D:
     nza, nzc = arrays["zeta_aa"].shape[0], arrays["zeta_ac"].shape[0]
     U = Uz3D()
     U.nx, U.ny, U.nz_aa, U.nz_ac, U.dx, U.dy, U.use_bmb = nx, ny, nza, nzc, dx, dy, int(bool(use_bmb))
-    for n in UZ_INPUTS + UZ_OUTPUTS:
+    for n in UZ_INPUTS + UZ_OUTPUTS + UZ_JAC_INPUTS:
         a = arrays.get(n)
         if a is None:
             continue
         want = {"zeta_aa": (nza,), "zeta_ac": (nzc,), "ux": (nx, ny, nza), "uy": (nx, ny, nza),
-                "uz": (nx, ny, nzc), "uz_star": (nx, ny, nzc)}.get(n, (nx, ny))
+                "uz": (nx, ny, nzc), "uz_star": (nx, ny, nzc), "jac_dxx": (nx, ny, nza),
+                "jac_dyy": (nx, ny, nza)}.get(n, (nx, ny))
         if a.shape != want:
             raise ValueError(f"{n}: shape {a.shape}, expected {want}")
         ptr(a, "i" if n == "mask_kin" else "d")
         setattr(U, n, a.ctypes.data)
     return U
+
+STRAIN_INPUTS = ("dxx", "dxy", "dxz", "dyx", "dyy", "dyz", "dzx", "dzy", "H_ice", "f_ice", "f_grnd",
+                 "zeta_aa", "zeta_ac")
+STRAIN_OUTPUTS_3D = ("s_dxx", "s_dyy", "s_dxy", "s_dxz", "s_dyz", "s_de", "s_div", "s_f_shear")
+STRAIN_OUTPUTS_2D = ("a_dxx", "a_dyy", "a_dxy", "a_dxz", "a_dyz", "a_de", "a_div", "a_f_shear", "eps_eig_1",
+                     "eps_eig_2")
+
+
+class Strain3D(C.Structure):
+    """ygpu_strain3d: arrays of the strain-rate tensor."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz_aa", C.c_int), ("nz_ac", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("de_max", C.c_double)] + \
+        [(n, C.c_void_p) for n in STRAIN_INPUTS + STRAIN_OUTPUTS_3D + STRAIN_OUTPUTS_2D]
+
+
+def strain3d(arrays: dict, dx: float, dy: float, de_max: float) -> Strain3D:
+    """A Strain3D over the numpy arrays of `arrays` (absent names stay NULL)."""
+    nx, ny = arrays["H_ice"].shape
+    nza, nzc = arrays["zeta_aa"].shape[0], arrays["zeta_ac"].shape[0]
+    S = Strain3D()
+    S.nx, S.ny, S.nz_aa, S.nz_ac, S.dx, S.dy, S.de_max = nx, ny, nza, nzc, dx, dy, de_max
+    for n in STRAIN_INPUTS + STRAIN_OUTPUTS_3D + STRAIN_OUTPUTS_2D:
+        a = arrays.get(n)
+        if a is None:
+            continue
+        if n == "zeta_aa":
+            want = (nza,)
+        elif n == "zeta_ac":
+            want = (nzc,)
+        elif n in ("dzx", "dzy"):
+            want = (nx, ny, nzc)
+        elif n in STRAIN_OUTPUTS_3D or n in ("dxx", "dxy", "dxz", "dyx", "dyy", "dyz"):
+            want = (nx, ny, nza)
+        else:
+            want = (nx, ny)
+        if a.shape != want:
+            raise ValueError(f"{n}: shape {a.shape}, expected {want}")
+        ptr(a, "d")
+        setattr(S, n, a.ctypes.data)
+    return S
+
 
 class Fields(C.Structure):
     """ygpu_fields: device pointers of one instance."""

@@ -24,6 +24,7 @@ UNITS = {
     "ygpu_inputs.cu": ["-fmad=false"],
     "ygpu_noalloc.cu": [],
     "ygpu_serve.cu": [],
+    "ygpu_post.cu": [],
 }
 
 

@@ -1391,8 +1391,12 @@ static int uz3d_check(const ygpu_uz3d* U, int bc, int method) {
         ygpu_set_error("bad arguments (nz_ac = nz_aa + 1, 2 <= nz_aa <= 1000)");
         return YGPU_ERR_BAD_ARG;
     }
-    if (method != YGPU_UZ_AA && method != YGPU_UZ_FLUX) {
-        ygpu_set_error("uz_method %d: only 1 (uz_aa) and 4 (uz_flux) are built; 2 and 3 need gq2D/gq3D", method);
+    if (method < YGPU_UZ_AA || method > YGPU_UZ_FLUX) {
+        ygpu_set_error("uz_method %d: 1 (uz_aa), 2 (uz_nodes), 3 (uz_jac) or 4 (uz_flux)", method);
+        return YGPU_ERR_BAD_ARG;
+    }
+    if (method == YGPU_UZ_JAC && any_null({U->jac_dxx, U->jac_dyy})) {
+        ygpu_set_error("uz_jac needs the Jacobian's jac_dxx and jac_dyy");
         return YGPU_ERR_BAD_ARG;
     }
     if (any_null({U->ux, U->uy, U->H_ice, U->f_ice, U->smb, U->bmb, U->dzbdt, U->dzsdt, U->dzsdx, U->dzsdy,
@@ -1440,12 +1444,74 @@ extern "C" int ygpu_calc_uz_3D(const ygpu_uz3d* H, int boundaries, int method) {
         in(H->ux_bar, (const void**)&D.ux_bar, b2); in(H->uy_bar, (const void**)&D.uy_bar, b2);
         in(H->dHidt_dyn, (const void**)&D.dHidt_dyn, b2); in(H->mask_kin, (const void**)&D.mask_kin, n * 4);
     }
+    if (method == YGPU_UZ_JAC) {
+        in(H->jac_dxx, (const void**)&D.jac_dxx, ba); in(H->jac_dyy, (const void**)&D.jac_dyy, ba);
+    }
     out(H->uz, &D.uz, bc3); out(H->uz_star, &D.uz_star, bc3);
     if (H->uz_srf_err) out(H->uz_srf_err, &D.uz_srf_err, b2);
     if ((st = S.upload(c))) return st;
     for (auto& m : map) *m.second = S.args[m.first].dev;
     if ((st = ygpu_uz3d_device(c->stream, D, boundaries, method))) return st;
     return S.download(c);
+}
+
+static int strain3d_check(const ygpu_strain3d* S, int bc) {
+    if (!S || S->nx < 2 || S->ny < 2 || !(S->dx > 0.0) || !(S->dy > 0.0) || bc < 0 || bc > 6 ||
+        S->nz_aa < 2 || S->nz_aa > 1000 || S->nz_ac != S->nz_aa + 1 || (size_t)S->nx * S->ny > (size_t)(1 << 28) ||
+        !(S->de_max >= 0.0)) {
+        ygpu_set_error("bad arguments (nz_ac = nz_aa + 1, 2 <= nz_aa <= 1000, de_max >= 0)");
+        return YGPU_ERR_BAD_ARG;
+    }
+    if (any_null({S->dxx, S->dxy, S->dxz, S->dyx, S->dyy, S->dyz, S->dzx, S->dzy, S->H_ice, S->f_ice, S->f_grnd,
+                  S->zeta_aa, S->zeta_ac, S->s_dxx, S->s_dyy, S->s_dxy, S->s_dxz, S->s_dyz, S->s_de, S->s_div,
+                  S->s_f_shear})) {
+        ygpu_set_error("a required strain-rate array is NULL");
+        return YGPU_ERR_BAD_ARG;
+    }
+    return YGPU_OK;
+}
+
+extern "C" int ygpu_calc_strain_rate_tensor_device(void* stream, const ygpu_strain3d* S, int boundaries) {
+    int st = strain3d_check(S, boundaries);
+    if (st) return st;
+    return ygpu_strain3d_device((cudaStream_t)stream, *S, boundaries);
+}
+
+extern "C" int ygpu_calc_strain_rate_tensor(const ygpu_strain3d* H, int boundaries) {
+    int st = strain3d_check(H, boundaries);
+    if (st) return st;
+    ygpu_ctx* c = default_ctx();
+    if (!c) return YGPU_ERR_CUDA;
+    const size_t n = (size_t)H->nx * H->ny, b2 = n * 8, ba = b2 * (size_t)H->nz_aa, bc3 = b2 * (size_t)H->nz_ac;
+    Staging Sg;
+    ygpu_strain3d D = *H;
+    std::vector<std::pair<size_t, const void**>> map;
+    auto in = [&](const void* src, const void** dst, size_t bytes) {
+        map.push_back({Sg.add((void*)src, bytes, 1, 0), dst});
+    };
+    auto out = [&](double* src, double** dst, size_t bytes) {
+        if (src) map.push_back({Sg.add((void*)src, bytes, 0, 1), (const void**)dst});
+    };
+    const double* const* f3[] = {&H->dxx, &H->dxy, &H->dxz, &H->dyx, &H->dyy, &H->dyz};
+    const double** d3[] = {&D.dxx, &D.dxy, &D.dxz, &D.dyx, &D.dyy, &D.dyz};
+    for (int q = 0; q < 6; q++) in(*f3[q], (const void**)d3[q], ba);
+    in(H->dzx, (const void**)&D.dzx, bc3); in(H->dzy, (const void**)&D.dzy, bc3);
+    in(H->H_ice, (const void**)&D.H_ice, b2); in(H->f_ice, (const void**)&D.f_ice, b2);
+    in(H->f_grnd, (const void**)&D.f_grnd, b2);
+    in(H->zeta_aa, (const void**)&D.zeta_aa, (size_t)H->nz_aa * 8);
+    in(H->zeta_ac, (const void**)&D.zeta_ac, (size_t)H->nz_ac * 8);
+    double* const o3h[] = {H->s_dxx, H->s_dyy, H->s_dxy, H->s_dxz, H->s_dyz, H->s_de, H->s_div, H->s_f_shear};
+    double** o3d[] = {&D.s_dxx, &D.s_dyy, &D.s_dxy, &D.s_dxz, &D.s_dyz, &D.s_de, &D.s_div, &D.s_f_shear};
+    for (int q = 0; q < 8; q++) out(o3h[q], o3d[q], ba);
+    double* const o2h[] = {H->a_dxx, H->a_dyy, H->a_dxy, H->a_dxz, H->a_dyz, H->a_de, H->a_div, H->a_f_shear,
+                           H->eps_eig_1, H->eps_eig_2};
+    double** o2d[] = {&D.a_dxx, &D.a_dyy, &D.a_dxy, &D.a_dxz, &D.a_dyz, &D.a_de, &D.a_div, &D.a_f_shear,
+                      &D.eps_eig_1, &D.eps_eig_2};
+    for (int q = 0; q < 10; q++) out(o2h[q], o2d[q], b2);
+    if ((st = Sg.upload(c))) return st;
+    for (auto& m : map) *m.second = Sg.args[m.first].dev;
+    if ((st = ygpu_strain3d_device(c->stream, D, boundaries))) return st;
+    return Sg.download(c);
 }
 
 extern "C" int ygpu_calc_advec2D_impl_lis(double* dvdt, const double* var, const double* ux, const double* uy,

@@ -110,6 +110,9 @@ int ygpu_gradient_column_device(cudaStream_t s, double* gx_c, double* gy_c, cons
                                 const double* f_ice, const int* mask_ocn, int bc, int nx, int ny);
 int ygpu_jacobian_device(cudaStream_t s, const ygpu_jvel& J, int bc, int terms);
 int ygpu_uz3d_device(cudaStream_t s, const ygpu_uz3d& U, int bc, int method);
+// ygpu_post.cu: uz_method 2 and 3, the strain-rate tensor
+int ygpu_uz3d_quad_device(cudaStream_t s, const ygpu_uz3d& U, int bc, int method);
+int ygpu_strain3d_device(cudaStream_t s, const ygpu_strain3d& S, int bc);
 int ygpu_ssa_masks_device(cudaStream_t s, int* mx, int* my, const int* mf, const double* f_ice, const double* f_grnd,
                           int lat, int bc, int nx, int ny);
 

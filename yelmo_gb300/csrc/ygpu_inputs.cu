@@ -858,6 +858,7 @@ __global__ void __launch_bounds__(256) k_uz3d(ygpu_uz3d U, int bc, int method) {
 }
 
 int ygpu_uz3d_device(cudaStream_t s, const ygpu_uz3d& U, int bc, int method) {
+    if (method == YGPU_UZ_NODES || method == YGPU_UZ_JAC) return ygpu_uz3d_quad_device(s, U, bc, method);
     const size_t smem = 3 * sizeof(double) * (size_t)U.nz_ac;
     k_uz3d<<<grid_for(U.nx * U.ny), 256, smem, s>>>(U, bc, method);
     cudaError_t e = cudaGetLastError();

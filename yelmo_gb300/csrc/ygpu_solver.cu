@@ -2393,6 +2393,9 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         if (!(ok = team_allreduce(T, &rr, 1))) return YGPU_ERR_TIMEOUT;
         relres = sqrt(rr) / bnrm;
         if (relres <= P.lin_tol) { status = YGPU_OK; break; }
+        // a non-finite residual (non-finite coefficients or right-hand side) ends the
+        // solve as the FP64 Krylov methods do, before a correction scaled by it
+        if (!isfinite(relres)) { status = YGPU_BREAKDOWN; break; }
         if (total >= P.lin_maxiter) { status = YGPU_MAXITER; break; }
         // inner FP32 solve of A d = r, d0 = 0, scaled by ||r||
         const double nr = sqrt(rr), sc = 1.0 / nr;

@@ -42,6 +42,7 @@ EXPORTS = [
     "ygpu_calc_dyn_diagnostics_device", "ygpu_calc_advec2D_impl_lis", "ygpu_advec2D_impl_lis_device",
     "ygpu_calc_gradient_column_ac", "ygpu_calc_gradient_column_ac_device", "ygpu_calc_jacobian_vel_3D",
     "ygpu_calc_jacobian_vel_3D_device", "ygpu_calc_uz_3D", "ygpu_calc_uz_3D_device", "ygpu_lin_method_run",
+    "ygpu_calc_strain_rate_tensor", "ygpu_calc_strain_rate_tensor_device",
 ]
 
 
@@ -116,6 +117,8 @@ def lib(build_if_missing: bool = True):
     L.ygpu_step_timing_get.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_longlong)]
     L.ygpu_lin_method_run.argtypes = [C.POINTER(abi.DynPar), C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.ygpu_lin_method_run.restype = None
+    L.ygpu_calc_strain_rate_tensor.argtypes = [C.POINTER(abi.Strain3D), C.c_int]
+    L.ygpu_calc_strain_rate_tensor_device.argtypes = [C.c_void_p, C.POINTER(abi.Strain3D), C.c_int]
     _lib = L
     return L
 
@@ -296,11 +299,36 @@ def uz_arrays(inputs: dict, srf_err: bool = True) -> dict:
 
 def calc_uz_3D(arrays: dict, dx: float, dy: float, boundaries: str, method: int = abi.UZ_AA,
                use_bmb: bool = True) -> dict:
-    """Vertical velocity on the GPU (ygpu_calc_uz_3D, uz_method 1 or 4); the
-    output arrays of `arrays` (see uz_arrays) are filled in place."""
+    """Vertical velocity on the GPU (ygpu_calc_uz_3D, uz_method 1 to 4; method 3
+    reads jac_dxx / jac_dyy); the output arrays of `arrays` (see uz_arrays) are
+    filled in place."""
     U = abi.uz3d(arrays, dx, dy, use_bmb)
     _check(lib().ygpu_calc_uz_3D(C.byref(U), abi.BOUNDARY_CODES[boundaries], int(method)))
     return arrays
+
+def strain_arrays(jac: dict, inputs: dict, want_2d: bool = True) -> dict:
+    """The strain-rate tensor's inputs (the Jacobian's dxx ... dzy from `jac`, the
+    geometry from `inputs`) with zeroed outputs."""
+    nx, ny = inputs["H_ice"].shape
+    nza = inputs["zeta_aa"].shape[0]
+    out = {k: jac[k] for k in ("dxx", "dxy", "dxz", "dyx", "dyy", "dyz", "dzx", "dzy")}
+    for k in ("H_ice", "f_ice", "f_grnd", "zeta_aa", "zeta_ac"):
+        out[k] = inputs[k]
+    for k in abi.STRAIN_OUTPUTS_3D:
+        out[k] = np.zeros((nx, ny, nza), order="F")
+    if want_2d:
+        for k in abi.STRAIN_OUTPUTS_2D:
+            out[k] = np.zeros((nx, ny), order="F")
+    return out
+
+
+def calc_strain_rate_tensor(arrays: dict, dx: float, dy: float, boundaries: str, de_max: float = 0.5) -> dict:
+    """Strain-rate tensor on the GPU (ygpu_calc_strain_rate_tensor) on the arrays of
+    strain_arrays (outputs filled in place)."""
+    S = abi.strain3d(arrays, dx, dy, de_max)
+    _check(lib().ygpu_calc_strain_rate_tensor(C.byref(S), abi.BOUNDARY_CODES[boundaries]))
+    return arrays
+
 
 def calc_dyn_inputs(inst) -> dict:
     d = inst.input_buffers()
