@@ -236,7 +236,7 @@ class Fields(C.Structure):
 class Tuning(C.Structure):
     """ygpu_tuning."""
     _fields_ = [("check_every", C.c_int), ("use_graphs", C.c_int), ("unknowns_per_cta", C.c_int),
-                ("max_active_unknowns", C.c_ulonglong), ("spin_log2", C.c_int)]
+                ("max_active_unknowns", C.c_ulonglong), ("spin_log2", C.c_int), ("cluster_ctas", C.c_int)]
 
 
 class ServerCfg(C.Structure):

@@ -179,6 +179,7 @@ struct ygpu_ctx {
     int unknowns_per_cta = 0;       // team size: unknowns per CTA (0: 2 x block)
     size_t max_active_unknowns = 1500000;   // batches beyond this run as a queue (continuous batching)
     int spin_log2 = 0;              // team waits give up after 2^spin_log2 polls (0: the default 2^22)
+    int cluster_ctas = 0;           // Krylov cluster teams: 0 chosen, k CTAs, -1 off
     int* h_flags = nullptr;         // pinned: finished count, abort flag
     int* d_misc = nullptr;          // [0] queue, [1] abort, [2..3] csr out
     double* d_miscd = nullptr;
@@ -211,14 +212,16 @@ extern "C" void ygpu_tuning_defaults(ygpu_tuning* t) {
     t->unknowns_per_cta = 2 * YG_BLOCK;
     t->max_active_unknowns = 1500000;
     t->spin_log2 = 0;
+    t->cluster_ctas = 0;
 }
 
 extern "C" int ygpu_ctx_set_tuning(ygpu_ctx* c, const ygpu_tuning* t) {
     if (!c || !t) { ygpu_set_error("NULL argument"); return YGPU_ERR_BAD_ARG; }
     if (t->check_every < 1 || t->check_every > 64 || t->unknowns_per_cta < 32 || t->unknowns_per_cta > (1 << 20) ||
-        t->spin_log2 < 0 || t->spin_log2 > 22) {
+        t->spin_log2 < 0 || t->spin_log2 > 22 || t->cluster_ctas < -1 || t->cluster_ctas == 1 || t->cluster_ctas > 16) {
         ygpu_set_error("tuning out of range: check_every %d (1..64), unknowns_per_cta %d (32..2^20), spin_log2 %d "
-                       "(0..22)", t->check_every, t->unknowns_per_cta, t->spin_log2);
+                       "(0..22), cluster_ctas %d (-1, 0, 2..16)", t->check_every, t->unknowns_per_cta, t->spin_log2,
+                       t->cluster_ctas);
         return YGPU_ERR_BAD_ARG;
     }
     c->check_every = t->check_every;
@@ -226,6 +229,7 @@ extern "C" int ygpu_ctx_set_tuning(ygpu_ctx* c, const ygpu_tuning* t) {
     c->unknowns_per_cta = t->unknowns_per_cta;
     c->max_active_unknowns = t->max_active_unknowns;
     c->spin_log2 = t->spin_log2;
+    c->cluster_ctas = t->cluster_ctas;
     ygpu_graph_cache_clear(&c->graph);
     return YGPU_OK;
 }
@@ -571,7 +575,8 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     CK(cudaEventRecord(c->e0, c->stream));
     st = ygpu_launch_solver(c->device, c->stream, c->d_insts, n, *par, c->d_ctl, n_ctl, team_ctas, c->d_misc,
                             c->d_misc + 1, mapped ? c->d_map : nullptr, map_grid, c->use_graphs ? &c->graph : nullptr,
-                            c->h_flags, c->check_every, hooked ? &hr : nullptr, c->spin_log2);
+                            c->h_flags, c->check_every, hooked ? &hr : nullptr, c->spin_log2, c->cluster_ctas,
+                            max_nu);
     if (st) return st;
     CK(cudaEventRecord(c->e1, c->stream));
     c->h_out.resize(n);

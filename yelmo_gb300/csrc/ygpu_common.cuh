@@ -4,6 +4,7 @@
 // fused, deterministic all-reduce.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -183,6 +184,9 @@ struct Team {
     double sync_ns;                // time CTA 0 / thread 0 spent in team all-reduces
     unsigned gen;                  // thread 0: count target of the last team barrier
     unsigned spin_lim;             // thread 0: polls after which a wait gives up
+    bool cl;                       // the team is one thread-block cluster: barriers are the
+                                   // hardware cluster barrier, all-reduces go through
+                                   // distributed shared memory (no global control block)
 };
 
 YG_DEV unsigned ld_acquire_u32(const unsigned int* p) {
@@ -216,6 +220,12 @@ YG_DEV void red_release_add_u32(unsigned int* p, unsigned v) {
 // arrival; the closing __syncthreads orders the CTA's later reads after thread
 // 0's acquire. Counts wrap: the comparison is on the signed difference.
 YG_DEV bool team_barrier(Team& T) {
+    if (T.cl) {
+        // barrier.cluster arrive (release) / wait (acquire): every thread of the
+        // cluster's CTAs; orders the CTAs' global and shared memory accesses
+        cooperative_groups::this_cluster().sync();
+        return true;
+    }
     __syncthreads();
     __shared__ int s_ok;
     if (threadIdx.x == 0) {
@@ -259,12 +269,41 @@ template <typename V>
 YG_DEV bool team_allreduce_impl(Team& T, const V* in, double* out, int nv) {
     __shared__ double s_red[32][YG_RED_MAX];
     __shared__ double s_tot[YG_RED_MAX];
+    // cluster teams: per-CTA totals in this CTA's shared memory, double-buffered
+    // by parity (a CTA rewrites a buffer only after the next cluster barrier, which
+    // every CTA passes after its reads of that buffer)
+    __shared__ double s_cl[2][YG_RED_MAX];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int k = 0; k < nv; k++) {
         V w = warp_sum<V>(in[k]);
         if (lane == 0) s_red[wid][k] = (double)w;
     }
     __syncthreads();
+    if (T.cl) {
+        if (wid == 0) {
+            for (int k = 0; k < nv; k++) {
+                double w = (lane < nw) ? s_red[lane][k] : 0.0;
+                w = warp_sum<double>(w);
+                if (lane == 0) s_cl[T.parity][k] = w;
+            }
+        }
+        cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+        cl.sync();
+        if (wid == 0) {
+            // every CTA sums the CTA totals in the same order: identical results
+            for (int k = 0; k < nv; k++) {
+                double w = 0.0;
+                for (int c = lane; c < T.ncta; c += 32) w += *cl.map_shared_rank(&s_cl[T.parity][k], c);
+                w = warp_sum<double>(w);
+                if (lane == 0) s_tot[k] = w;
+            }
+        }
+        T.parity ^= 1;
+        __syncthreads();
+        for (int k = 0; k < nv; k++) out[k] = s_tot[k];
+        __syncthreads();
+        return true;
+    }
     if (wid == 0) {
         for (int k = 0; k < nv; k++) {
             double w = (lane < nw) ? s_red[lane][k] : 0.0;

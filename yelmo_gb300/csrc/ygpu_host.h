@@ -29,7 +29,15 @@ struct StepShape {
     int kgrid, ktc;                // Krylov step: CTAs, CTAs per team
     const int* map = nullptr;      // device team map of the heavy steps (NULL: uniform teams)
     const int* kmap = nullptr;     // device team map of the Krylov step
+    int kcl = 0;                   // > 0: the Krylov teams are thread-block clusters of kcl CTAs
+                                   // (kgrid = clusters x kcl), see ygpu_krylov_cluster_plan
 };
+// Cluster size and count for the Krylov step of n_inst instances of at most
+// max_nu unknowns: the largest cluster size (at most 16 CTAs, at least one CTA
+// per 1024 unknowns of the largest instance) with one resident cluster per
+// instance. req > 0 asks for that size, req < 0 for none. Returns the size
+// (0: no cluster plan fits, use the global teams) and the cluster count.
+int ygpu_krylov_cluster_plan(int device, int n_inst, size_t max_nu, int req, int* n_clusters);
 int ygpu_init_constants(int device);
 void ygpu_count_launches(unsigned long long n);
 void ygpu_step_timing_flush();
@@ -87,7 +95,7 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
                        TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort,
                        const int* d_map = nullptr, int map_grid = 0, GraphCache* gc = nullptr,
                        int* h_flags = nullptr, int check_every = 4, const NeffRun* hook = nullptr,
-                       int spin_log2 = 0);
+                       int spin_log2 = 0, int cluster_req = 0, size_t max_nu = 0);
 int ygpu_sm_count(int device);
 size_t ygpu_teamctl_bytes();
 size_t ygpu_inst_bytes();

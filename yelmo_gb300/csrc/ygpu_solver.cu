@@ -2898,6 +2898,7 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
     T.sync_ns = 0.0;
     T.gen = (threadIdx.x == 0) ? ld_acquire_u32(&T.ctl->base) : 0u;
     T.spin_lim = (threadIdx.x == 0) ? team_spin_limit(T.ctl) : 0u;
+    T.cl = false;
     for (int q = team; q < n_inst; q += n_teams) {
         if (threadIdx.x == 0) {
             sI = insts[q];
@@ -2940,6 +2941,57 @@ __global__ void __launch_bounds__(YG_KBLOCK, 1) ygpu_k_krylov(const Inst* insts,
                                                               TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
     run_step<YG_STEP_KRYLOV>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
+// The Krylov step with every team one thread-block cluster (cluster size =
+// team size, at most 16 CTAs): the team barrier is the hardware cluster barrier
+// and the all-reduce reads the other CTAs' totals from their shared memory, with
+// no global control block or polling. Cluster c takes instances c, c + n_clusters,
+// ... The skip decision is the same in every CTA of a cluster: the instance's
+// done flag (not written during this step) and the abort flag as CTA 0 of the
+// cluster reads it once. Every barrier of a cluster team completes (its CTAs run
+// the same control flow on identical all-reduced values), so no wait here needs
+// a spin limit.
+__global__ void __launch_bounds__(YG_KBLOCK, 1) ygpu_k_krylov_cl(const Inst* insts, int n_inst, ygpu_dyn_par P,
+                                                                 TeamCtl* ctls, int tc, int* ab, int* dc,
+                                                                 const int* map) {
+    namespace cgx = cooperative_groups;
+    cgx::cluster_group cl = cgx::this_cluster();
+    __shared__ Inst sI;
+    __shared__ int s_flags[2];     // [0] this CTA's abort read (rank 0's is used), [1] skip
+    Team T;
+    T.ncta = (int)cl.num_blocks();
+    T.cta = (int)cl.block_rank();
+    const int team = blockIdx.x / T.ncta, n_teams = gridDim.x / T.ncta;
+    T.tid = T.cta * blockDim.x + threadIdx.x;
+    T.nthr = T.ncta * blockDim.x;
+    T.ctl = ctls;                  // not used by cluster teams
+    T.parity = 0;
+    T.abort_all = ab;
+    T.sync_ns = 0.0;
+    T.gen = 0u;
+    T.spin_lim = YG_SPIN_LIMIT;
+    T.cl = true;
+    if (threadIdx.x == 0) s_flags[0] = ld_acquire_s32(ab);
+    cl.sync();
+    const int aborted = *cl.map_shared_rank(&s_flags[0], 0);
+    for (int q = team; q < n_inst; q += n_teams) {
+        if (threadIdx.x == 0) {
+            sI = insts[q];
+            s_flags[1] = sI.out->done || aborted;
+        }
+        __syncthreads();
+        if (!s_flags[1]) {
+            step_krylov(sI, P, T, dc);
+            if (T.cta == 0 && threadIdx.x == 0) sI.out->phase_ns[8] += T.sync_ns;
+            T.sync_ns = 0.0;
+        }
+        // no CTA starts the next instance (or leaves) while another may still read
+        // its shared memory
+        cl.sync();
+    }
+    // every CTA has read CTA 0's abort flag before any of them leaves
+    cl.sync();
+}
+
 // the post step (epilogue of a Picard iteration) runs 512-thread CTAs: twice the warps
 // per SM of 256 threads, for a pass bound by load latency
 #define YG_POBLOCK 512
@@ -2978,6 +3030,7 @@ __global__ void __launch_bounds__(YG_BLOCK) ygpu_csr_kernel(CsrJob J, TeamCtl* c
     T.sync_ns = 0.0;
     T.gen = 0u;
     T.spin_lim = YG_SPIN_LIMIT;
+    T.cl = false;
     const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
     // Jacobi diagonal and ||b||
     double bn = 0.0;
@@ -3166,6 +3219,7 @@ __global__ void __launch_bounds__(YG_BLOCK) ygpu_adv_kernel(AdvJob J, TeamCtl* c
     T.sync_ns = 0.0;
     T.gen = 0u;
     T.spin_lim = YG_SPIN_LIMIT;
+    T.cl = false;
     const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
     const int nx = J.nx, ny = J.ny, n = nx * ny;
     int k[4];
@@ -3493,6 +3547,76 @@ int ygpu_launch_step(int step, cudaStream_t s, const StepShape& sh, const Inst* 
     return st;
 }
 
+// The Krylov step on cluster teams: an ordinary launch with a cluster dimension
+// (the CTAs of a cluster are co-scheduled by the hardware; clusters do not wait
+// on one another, so no cooperative launch is needed)
+static int launch_cluster_krylov(cudaStream_t s, const StepShape& sh, const Inst* d_insts, int n_inst,
+                                 const ygpu_dyn_par& P, TeamCtl* ctls, int* d_done, int* d_abort) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)sh.kcl;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)sh.kgrid);
+    cfg.blockDim = dim3(YG_KBLOCK);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    const int tc = sh.kcl;
+    const int* map = nullptr;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, ygpu_k_krylov_cl, d_insts, n_inst, P, ctls, tc, d_abort, d_done, map);
+    if (e != cudaSuccess) {
+        ygpu_set_error("cluster launch of the Krylov step failed: %s", cudaGetErrorString(e));
+        return YGPU_ERR_CUDA;
+    }
+    return YGPU_OK;
+}
+
+int ygpu_krylov_cluster_plan(int device, int n_inst, size_t max_nu, int req, int* n_clusters) {
+    *n_clusters = 0;
+    if (req < 0 || n_inst < 1 || device < 0 || device >= 64) return 0;
+    static std::mutex mu;
+    static int maxc[64][17];       // resident clusters per size (-1: not resident / not queried)
+    static bool init[64];
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!init[device]) {
+            cudaFuncSetAttribute((const void*)ygpu_k_krylov_cl, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+            for (int cs = 1; cs <= 16; cs++) {
+                cudaLaunchConfig_t cfg = {};
+                cudaLaunchAttribute at[1];
+                at[0].id = cudaLaunchAttributeClusterDimension;
+                at[0].val.clusterDim.x = (unsigned)cs;
+                at[0].val.clusterDim.y = 1;
+                at[0].val.clusterDim.z = 1;
+                cfg.gridDim = dim3((unsigned)cs);
+                cfg.blockDim = dim3(YG_KBLOCK);
+                cfg.attrs = at;
+                cfg.numAttrs = 1;
+                int n = 0;
+                if (cudaOccupancyMaxActiveClusters(&n, (const void*)ygpu_k_krylov_cl, &cfg) != cudaSuccess) n = -1;
+                maxc[device][cs] = n;
+            }
+            cudaGetLastError();
+            init[device] = true;
+        }
+    }
+    int cap = (int)((max_nu + 1023) / 1024);
+    if (cap > 16) cap = 16;
+    if (cap < 2) cap = 2;
+    for (int cs = (req > 0 ? (req > 16 ? 16 : req) : cap); cs >= 2; cs--) {
+        const int m = maxc[device][cs];
+        if (m >= n_inst || (req > 0 && m >= 1)) {
+            *n_clusters = (m < n_inst) ? m : n_inst;
+            return cs;
+        }
+        if (req > 0) break;
+    }
+    return 0;
+}
+
 static int launch_step_raw(int step, cudaStream_t s, const StepShape& sh, const Inst* d_insts, int n_inst,
                            const ygpu_dyn_par& P, TeamCtl* ctls, int* d_done, int* d_abort) {
     switch (step) {
@@ -3505,6 +3629,7 @@ static int launch_step_raw(int step, cudaStream_t s, const StepShape& sh, const 
             return coop((const void*)ygpu_k_pre64, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas,
                         d_abort, d_done, sh.map);
         case YG_STEP_KRYLOV:
+            if (sh.kcl > 0) return launch_cluster_krylov(s, sh, d_insts, n_inst, P, ctls, d_done, d_abort);
             return coop((const void*)ygpu_k_krylov, sh.kgrid, YG_KBLOCK, s, d_insts, n_inst, P, ctls, sh.ktc, d_abort, d_done, sh.kmap);
         case YG_STEP_POST:
             return coop((const void*)ygpu_k_post, sh.grid, YG_POBLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
@@ -3583,7 +3708,7 @@ static bool capture_chunk(cudaStream_t stream, const StepShape& sh, const Inst* 
 int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int n_inst, const ygpu_dyn_par& P,
                        TeamCtl* d_ctls, int n_teams, int team_ctas, int* d_done, int* d_abort, const int* d_map,
                        int map_grid, GraphCache* gc, int* h_flags, int check_every, const NeffRun* hook,
-                       int spin_log2) {
+                       int spin_log2, int cluster_req, size_t max_nu) {
     // d_done: count of finished instances; d_abort: launch-wide abort flag.
     // With a team map (one team per instance) n_teams is the number of control
     // blocks to clear (n_inst) and map_grid the CTAs of the plan.
@@ -3600,6 +3725,17 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
     if (d_map) st = ygpu_step_shape_mapped(device, map_grid, d_map, &sh);
     else st = ygpu_step_shape(device, n_teams, team_ctas, &sh);
     if (st) return st;
+    // Krylov teams as thread-block clusters when every instance gets one resident cluster
+    if (max_nu > 0) {
+        int ncl = 0;
+        const int cs = ygpu_krylov_cluster_plan(device, n_inst, max_nu, cluster_req, &ncl);
+        if (cs > 0 && ncl > 0) {
+            sh.kcl = cs;
+            sh.kgrid = cs * ncl;
+            sh.ktc = cs;
+            sh.kmap = nullptr;
+        }
+    }
     if ((st = ygpu_launch_step(YG_STEP_SETUP, stream, sh, d_insts, n_inst, P, d_ctls, d_done, d_abort))) return st;
     // Picard iterations: one pre / Krylov / post launch each; the host reads the
     // count of finished instances every `check` iterations. With a graph cache

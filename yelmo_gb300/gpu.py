@@ -444,13 +444,16 @@ class DeviceSolver:
         return out
 
     def set_tuning(self, check_every: int = 4, use_graphs: bool = True, unknowns_per_cta: int = 512,
-                   max_active_unknowns: int = 1_500_000, spin_log2: int = 0):
+                   max_active_unknowns: int = 1_500_000, spin_log2: int = 0, cluster_ctas: int = 0):
         """ygpu_ctx_set_tuning: host-check interval, chunk graphs, team size, queue threshold;
-        spin_log2 > 0 lowers the team waits' spin budget to 2^spin_log2 polls (tests)."""
-        t = abi.Tuning(check_every, 1 if use_graphs else 0, unknowns_per_cta, max_active_unknowns, spin_log2)
+        spin_log2 > 0 lowers the team waits' spin budget to 2^spin_log2 polls (tests);
+        cluster_ctas: Krylov teams as thread-block clusters (0 chosen, 2..16, -1 off)."""
+        t = abi.Tuning(check_every, 1 if use_graphs else 0, unknowns_per_cta, max_active_unknowns, spin_log2,
+                       cluster_ctas)
         _check(self.L.ygpu_ctx_set_tuning(self.ctx, C.byref(t)))
         self.tuning = {"check_every": check_every, "use_graphs": bool(use_graphs),
-                       "unknowns_per_cta": unknowns_per_cta, "max_active_unknowns": max_active_unknowns}
+                       "unknowns_per_cta": unknowns_per_cta, "max_active_unknowns": max_active_unknowns,
+                       "cluster_ctas": cluster_ctas}
 
     def solve_batch(self, kind: int, par: YdynParams, fields: list) -> list:
         n = len(fields)
