@@ -172,8 +172,17 @@ struct TeamCtl {
     int abort;
     int inst;                      // instance the team works on (work queue)
     unsigned char spin_log2;       // 0: waits give up after YG_SPIN_LIMIT polls; k: after 2^k
-    double slots[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
+    union {                        // per-CTA totals of the all-reduces, by parity
+        double slots[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
+        float fslots[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
+    };
 };
+template <typename V>
+YG_DEV V* team_slot(TeamCtl* c, int parity, int cta, int k);
+template <>
+YG_DEV double* team_slot<double>(TeamCtl* c, int parity, int cta, int k) { return &c->slots[parity][cta][k]; }
+template <>
+YG_DEV float* team_slot<float>(TeamCtl* c, int parity, int cta, int k) { return &c->fslots[parity][cta][k]; }
 
 struct Team {
     int cta, ncta;                 // rank of this CTA in the team, CTAs in the team
@@ -181,7 +190,8 @@ struct Team {
     int parity;                    // reduction slot buffer in use
     TeamCtl* ctl;
     int* abort_all;                // whole-launch abort flag (timeout anywhere)
-    double sync_ns;                // time CTA 0 / thread 0 spent in team all-reduces
+    unsigned long long sync_ns;    // time thread 0 of the CTA spent in team all-reduces (ns; an
+                                   // integer, so that the count adds nothing to the FP64 pipe)
     unsigned gen;                  // thread 0: count target of the last team barrier
     unsigned spin_lim;             // thread 0: polls after which a wait gives up
     bool cl;                       // the team is one thread-block cluster: barriers are the
@@ -262,28 +272,29 @@ YG_DEV V warp_sum(V v) {
 
 // All-reduce (sum) of nv <= YG_RED_MAX values over the team, deterministic
 // for a fixed launch shape. Every thread passes its partials; every thread
-// gets the totals. Also acts as a team barrier. The warp-level sums run in the
-// partials' type V (FP32 partials of the mixed inner solve stay off the FP64
-// pipe); the CTA and team levels sum in FP64.
+// gets the totals. Also acts as a team barrier. Every level (warp, CTA, team)
+// sums in the partials' type V: the FP32 partials of the mixed inner solves
+// never touch the FP64 pipe, whose dependent-add latency on this part is about
+// fourteen times FP32's and which would otherwise dominate the all-reduce.
 template <typename V>
-YG_DEV bool team_allreduce_impl(Team& T, const V* in, double* out, int nv) {
-    __shared__ double s_red[32][YG_RED_MAX];
-    __shared__ double s_tot[YG_RED_MAX];
+YG_DEV bool team_allreduce_impl(Team& T, const V* in, V* out, int nv) {
+    __shared__ V s_red[32][YG_RED_MAX];
+    __shared__ V s_tot[YG_RED_MAX];
     // cluster teams: per-CTA totals in this CTA's shared memory, double-buffered
     // by parity (a CTA rewrites a buffer only after the next cluster barrier, which
     // every CTA passes after its reads of that buffer)
-    __shared__ double s_cl[2][YG_RED_MAX];
+    __shared__ V s_cl[2][YG_RED_MAX];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     for (int k = 0; k < nv; k++) {
         V w = warp_sum<V>(in[k]);
-        if (lane == 0) s_red[wid][k] = (double)w;
+        if (lane == 0) s_red[wid][k] = w;
     }
     __syncthreads();
     if (T.cl) {
         if (wid == 0) {
             for (int k = 0; k < nv; k++) {
-                double w = (lane < nw) ? s_red[lane][k] : 0.0;
-                w = warp_sum<double>(w);
+                V w = (lane < nw) ? s_red[lane][k] : V(0);
+                w = warp_sum<V>(w);
                 if (lane == 0) s_cl[T.parity][k] = w;
             }
         }
@@ -292,9 +303,9 @@ YG_DEV bool team_allreduce_impl(Team& T, const V* in, double* out, int nv) {
         if (wid == 0) {
             // every CTA sums the CTA totals in the same order: identical results
             for (int k = 0; k < nv; k++) {
-                double w = 0.0;
+                V w = V(0);
                 for (int c = lane; c < T.ncta; c += 32) w += *cl.map_shared_rank(&s_cl[T.parity][k], c);
-                w = warp_sum<double>(w);
+                w = warp_sum<V>(w);
                 if (lane == 0) s_tot[k] = w;
             }
         }
@@ -306,10 +317,10 @@ YG_DEV bool team_allreduce_impl(Team& T, const V* in, double* out, int nv) {
     }
     if (wid == 0) {
         for (int k = 0; k < nv; k++) {
-            double w = (lane < nw) ? s_red[lane][k] : 0.0;
-            w = warp_sum<double>(w);
+            V w = (lane < nw) ? s_red[lane][k] : V(0);
+            w = warp_sum<V>(w);
             if (lane == 0) {
-                if (T.ncta > 1) T.ctl->slots[T.parity][T.cta][k] = w;
+                if (T.ncta > 1) *team_slot<V>(T.ctl, T.parity, T.cta, k) = w;
                 else s_tot[k] = w;
             }
         }
@@ -318,9 +329,9 @@ YG_DEV bool team_allreduce_impl(Team& T, const V* in, double* out, int nv) {
         if (!team_barrier(T)) return false;
         if (wid == 0) {
             for (int k = 0; k < nv; k++) {
-                double w = 0.0;
-                for (int c = lane; c < T.ncta; c += 32) w += __ldcg(&T.ctl->slots[T.parity][c][k]);
-                w = warp_sum<double>(w);
+                V w = V(0);
+                for (int c = lane; c < T.ncta; c += 32) w += __ldcg(team_slot<V>(T.ctl, T.parity, c, k));
+                w = warp_sum<V>(w);
                 if (lane == 0) s_tot[k] = w;
             }
         }
@@ -332,10 +343,10 @@ YG_DEV bool team_allreduce_impl(Team& T, const V* in, double* out, int nv) {
     return true;
 }
 template <typename V>
-YG_DEV bool team_allreduce_w(Team& T, const V* in, double* out, int nv) {
-    unsigned long long t0 = global_ns();
+YG_DEV bool team_allreduce_w(Team& T, const V* in, V* out, int nv) {
+    const unsigned long long t0 = (threadIdx.x == 0) ? global_ns() : 0ull;
     bool ok = team_allreduce_impl<V>(T, in, out, nv);
-    T.sync_ns += (double)(global_ns() - t0);
+    if (threadIdx.x == 0) T.sync_ns += global_ns() - t0;
     return ok;
 }
 YG_DEV bool team_allreduce(Team& T, double* vals, int nv) { return team_allreduce_w<double>(T, vals, vals, nv); }

@@ -1647,7 +1647,9 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
     // Scalar recurrences run on one thread per CTA and are broadcast through
     // shared memory: FP64 division and square root are slow on this part, and
     // every thread of the team would otherwise repeat them.
-    __shared__ double s_ab[3];     // alpha, beta, relres
+    // The all-reduced sums and the scalars are in T: an FP32 inner solve keeps
+    // its whole iteration off the FP64 pipe (relres leaves as FP64 on exit only).
+    __shared__ T s_ab[3];          // alpha, beta, relres
     __shared__ int s_flag;         // 0 continue, 1 converged, 2 breakdown
     const bool lead = (threadIdx.x == 0);
     using W = T;                   // precision of the scalar recurrences
@@ -1698,39 +1700,38 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             a1 += wk * uk;
             a2 += rk * rk;
         }
-        double red[3];
+        T red[3];
         {
             const T part[3] = {a0, a1, a2};
             if (!(ok = team_allreduce_w<T>(Tm, part, red, 3))) return YGPU_ERR_TIMEOUT;
         }
         // lead thread: gam_old / alpha_old of the recurrence
-        double gam_old = 1.0, alpha_old = 1.0;
+        W gam_old = W(1), alpha_old = W(1);
         if (lead) {
-            const double rel = sqrt(red[2]) / bnrm;
+            const W rel = sqrt(red[2]) / (W)bnrm;
             s_ab[2] = rel;
-            if (rel <= tol) s_flag = 1;
+            if (rel <= (W)tol) s_flag = 1;
             else {
-                const double gam = red[0], del = red[1];
-                const double alpha = gam / del;
-                if (!isfinite(alpha) || del == 0.0) s_flag = 2;
+                const W gam = red[0], del = red[1];
+                const W alpha = gam / del;
+                if (!isfinite(alpha) || del == W(0)) s_flag = 2;
                 else {
                     s_flag = 0;
                     s_ab[0] = alpha;
-                    s_ab[1] = 0.0;
+                    s_ab[1] = W(0);
                     gam_old = gam;
                     alpha_old = alpha;
                 }
             }
         }
         __syncthreads();
-        relres = s_ab[2];
-        if (s_flag == 1) { iters = it; return YGPU_OK; }
-        if (s_flag == 2) { iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
+        if (s_flag == 1) { relres = (double)s_ab[2]; iters = it; return YGPU_OK; }
+        if (s_flag == 2) { relres = (double)s_ab[2]; iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
         T* mc = m0;
         T* mn = m1;
         bool recheck = false;
         while (it < maxiter) {
-            const T a = (T)s_ab[0], bt = (T)s_ab[1];
+            const T a = s_ab[0], bt = s_ab[1];
             a0 = a1 = a2 = T(0);
             // one row's loads (operator row, nine vectors, preconditioner)
             struct RowIn { T n, m, z, q, s, p, x, r, u, w, mi; };
@@ -1789,14 +1790,14 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             if (lead) {
                 // FP32 inner solves: the recurrence scalars in FP32 (its division
                 // and square root are far faster than FP64's on this part)
-                const W rel = sqrt((W)red[2]) / (W)bnrm;
+                const W rel = sqrt(red[2]) / (W)bnrm;
                 s_ab[2] = rel;
                 if (!isfinite(rel)) s_flag = 2;
                 else if (rel <= (W)tol) s_flag = 1;
                 else {
-                    const W gam = (W)red[0], del = (W)red[1];
-                    const W beta = gam / (W)gam_old;
-                    const W alpha = gam / (del - beta * gam / (W)alpha_old);
+                    const W gam = red[0], del = red[1];
+                    const W beta = gam / gam_old;
+                    const W alpha = gam / (del - beta * gam / alpha_old);
                     if (!isfinite(alpha) || !isfinite(beta) || del == W(0)) s_flag = 3;
                     else {
                         s_flag = 0;
@@ -1811,7 +1812,7 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             // s_flag / s_ab are rewritten only after the next all-reduce's first
             // __syncthreads, so every thread has read them by then
             const int flag = s_flag;
-            relres = s_ab[2];
+            if (flag != 0) relres = (double)s_ab[2];
             if (flag == 2) { iters = it; return YGPU_BREAKDOWN; }
             if (flag == 1) { recheck = true; break; }
             if (flag == 3) {
@@ -1821,15 +1822,20 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             }
         }
         iters = it;
+        relres = (double)s_ab[2];
         if (!recheck) return YGPU_MAXITER;
-        // true residual check
-        double tr = 0.0;
+        // true residual check (in T, as the recurrence)
+        T tr = T(0);
         for (int k = Tm.tid; k < nu; k += Tm.nthr) {
-            const double rk = (double)b[k] - (double)A.row(k, x);
+            const T rk = b[k] - A.row(k, x);
             tr += rk * rk;
         }
-        if (!(ok = team_allreduce(Tm, &tr, 1))) return YGPU_ERR_TIMEOUT;
-        relres = sqrt(tr) / bnrm;
+        {
+            T trs;
+            if (!(ok = team_allreduce_w<T>(Tm, &tr, &trs, 1))) return YGPU_ERR_TIMEOUT;
+            tr = trs;
+        }
+        relres = (double)(sqrt(tr) / (W)bnrm);
         if (relres <= tol) return YGPU_OK;
         if (it >= maxiter) return YGPU_MAXITER;
     }
@@ -1848,7 +1854,8 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
                                             T* __restrict__ rt, T* __restrict__ p, T* v, T* __restrict__ s, T* t,
                                             T* ph, T* sh, int maxiter, double tol, double bnrm, bool precond,
                                             int& iters, double& relres, bool& ok) {
-    __shared__ double s_sc[4];     // alpha, omega, beta, relres
+    // sums and scalars in T (an FP32 inner solve stays off the FP64 pipe)
+    __shared__ T s_sc[4];          // alpha, omega, beta, relres
     __shared__ int s_flag;         // 0 continue, 1 converged, 2 breakdown
     const bool lead = (threadIdx.x == 0);
     using W = T;                   // precision of the scalar recurrences (FP32 in the inner solves)
@@ -1865,31 +1872,31 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
         sh[u] = T(0);
         a0 += ru * ru;
     }
-    double red[2] = {0.0, 0.0};
+    T red[1];
     if (!(ok = team_allreduce_w<T>(Tm, &a0, red, 1))) return YGPU_ERR_TIMEOUT;
     // rows of this thread in the iterations (its own cache slots)
     const RowItems R = make_row_items(Tm, op_acell(A), A.n2(), nu);
     // lead-thread state of the recurrence
-    double rho = red[0], rho_old = 1.0, alpha = 1.0, omega = 1.0;     // (rt, r) with rt = r
+    W rho = red[0], rho_old = W(1), alpha = W(1), omega = W(1);     // (rt, r) with rt = r
     if (lead) {
-        s_sc[3] = sqrt(red[0]) / bnrm;
-        s_flag = (s_sc[3] <= tol) ? 1 : 0;
+        s_sc[3] = sqrt(red[0]) / (W)bnrm;
+        s_flag = (s_sc[3] <= (W)tol) ? 1 : 0;
     }
     __syncthreads();
-    relres = s_sc[3];
+    relres = (double)s_sc[3];
     if (s_flag == 1) return YGPU_OK;
     for (int it = 1; it <= maxiter; it++) {
         iters = it;
         __syncthreads();           // every thread has read the previous s_flag / s_sc[3]
         if (lead) {
-            s_flag = (rho == 0.0 || !isfinite(rho)) ? 2 : 0;
-            s_sc[2] = (it == 1) ? 0.0 : (double)(((W)rho / (W)rho_old) * ((W)alpha / (W)omega));
+            s_flag = (rho == W(0) || !isfinite(rho)) ? 2 : 0;
+            s_sc[2] = (it == 1) ? W(0) : (rho / rho_old) * (alpha / omega);
             s_sc[1] = omega;
         }
         __syncthreads();
-        if (s_flag == 2) return YGPU_BREAKDOWN;
+        if (s_flag == 2) { relres = (double)s_sc[3]; return YGPU_BREAKDOWN; }
         {
-            const T beta = (T)s_sc[2], om = (T)s_sc[1];
+            const T beta = s_sc[2], om = s_sc[1];
             int q = 0;
             for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
                 const int u = R.row(e, q);
@@ -1908,19 +1915,19 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
                 tvp += rt[u] * v[u];
             }
         }
-        double tv = 0.0;
+        T tv = T(0);
         if (!(ok = team_allreduce_w<T>(Tm, &tvp, &tv, 1))) return YGPU_ERR_TIMEOUT;
         if (lead) {
-            if (tv == 0.0 || !isfinite(tv)) s_flag = 2;
+            if (tv == T(0) || !isfinite(tv)) s_flag = 2;
             else {
-                alpha = (double)((W)rho / (W)tv);
+                alpha = rho / tv;
                 s_sc[0] = alpha;
                 s_flag = 0;
             }
         }
         __syncthreads();
-        if (s_flag == 2) return YGPU_BREAKDOWN;
-        const T al = (T)s_sc[0];
+        if (s_flag == 2) { relres = (double)s_sc[3]; return YGPU_BREAKDOWN; }
+        const T al = s_sc[0];
         T ssp = T(0);
         {
             int q = 0;
@@ -1947,24 +1954,24 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
                 ts1 += tu * tu;
             }
         }
-        double ts[3];
+        T ts[3];
         {
             const T part[3] = {ts0, ts1, ssp};
             if (!(ok = team_allreduce_w<T>(Tm, part, ts, 3))) return YGPU_ERR_TIMEOUT;
         }
         if (lead) {
-            s_sc[3] = (double)(sqrt((W)ts[2]) / (W)bnrm);
-            if (s_sc[3] <= tol) s_flag = 1;
-            else if (ts[1] == 0.0 || !isfinite(ts[1])) s_flag = 2;
+            s_sc[3] = sqrt(ts[2]) / (W)bnrm;
+            if (s_sc[3] <= (W)tol) s_flag = 1;
+            else if (ts[1] == T(0) || !isfinite(ts[1])) s_flag = 2;
             else {
-                omega = (double)((W)ts[0] / (W)ts[1]);
+                omega = ts[0] / ts[1];
                 s_sc[1] = omega;
                 s_flag = 0;
             }
         }
         __syncthreads();
         if (s_flag == 1) {
-            relres = s_sc[3];
+            relres = (double)s_sc[3];
             int q = 0;
             for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
                 const int u = R.row(e, q);
@@ -1973,8 +1980,8 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
             if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
             return YGPU_OK;
         }
-        if (s_flag == 2) return YGPU_BREAKDOWN;
-        const T om = (T)s_sc[1];
+        if (s_flag == 2) { relres = (double)s_sc[3]; return YGPU_BREAKDOWN; }
+        const T om = s_sc[1];
         T rr0 = T(0), rr1 = T(0);
         {
             int q = 0;
@@ -1987,22 +1994,23 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const
                 rr1 += rt[u] * ru;
             }
         }
-        double rr[2];
+        T rr[2];
         {
             const T part[2] = {rr0, rr1};
             if (!(ok = team_allreduce_w<T>(Tm, part, rr, 2))) return YGPU_ERR_TIMEOUT;
         }
         if (lead) {
-            s_sc[3] = (double)(sqrt((W)rr[0]) / (W)bnrm);
-            s_flag = (s_sc[3] <= tol) ? 1 : ((omega == 0.0) ? 2 : 0);
+            s_sc[3] = sqrt(rr[0]) / (W)bnrm;
+            s_flag = (s_sc[3] <= (W)tol) ? 1 : ((omega == W(0)) ? 2 : 0);
             rho_old = rho;
             rho = rr[1];
         }
         __syncthreads();
-        relres = s_sc[3];
+        if (s_flag != 0) relres = (double)s_sc[3];
         if (s_flag == 1) return YGPU_OK;
-        if (s_flag == 2) return YGPU_BREAKDOWN;
+        if (s_flag == 2) { relres = (double)s_sc[3]; return YGPU_BREAKDOWN; }
     }
+    relres = (double)s_sc[3];
     return YGPU_MAXITER;
 }
 
@@ -2196,7 +2204,7 @@ __device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op
                                                 T* __restrict__ u, T* __restrict__ w, T* m0, T* m1, T* __restrict__ z,
                                                 T* __restrict__ q, T* __restrict__ s, T* __restrict__ p, int maxiter,
                                                 double tol, double bnrm, int& iters, double& relres, bool& ok) {
-    __shared__ double s_ab[3];
+    __shared__ T s_ab[3];          // alpha, beta, relres (in T, as in krylov_pcg_pipe)
     __shared__ int s_flag;
     const bool lead = (threadIdx.x == 0);
     using W = T;                   // precision of the scalar recurrences
@@ -2229,38 +2237,37 @@ __device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op
                 a2 += rk * rk;
             }
         }
-        double red[3];
+        T red[3];
         {
             const T part[3] = {a0, a1, a2};
             if (!(ok = team_allreduce_w<T>(Tm, part, red, 3))) return YGPU_ERR_TIMEOUT;
         }
-        double gam_old = 1.0, alpha_old = 1.0;
+        W gam_old = W(1), alpha_old = W(1);
         if (lead) {
-            const double rel = sqrt(red[2]) / bnrm;
+            const W rel = sqrt(red[2]) / (W)bnrm;
             s_ab[2] = rel;
-            if (rel <= tol) s_flag = 1;
+            if (rel <= (W)tol) s_flag = 1;
             else {
-                const double gam = red[0], del = red[1];
-                const double alpha = gam / del;
-                if (!isfinite(alpha) || del == 0.0) s_flag = 2;
+                const W gam = red[0], del = red[1];
+                const W alpha = gam / del;
+                if (!isfinite(alpha) || del == W(0)) s_flag = 2;
                 else {
                     s_flag = 0;
                     s_ab[0] = alpha;
-                    s_ab[1] = 0.0;
+                    s_ab[1] = W(0);
                     gam_old = gam;
                     alpha_old = alpha;
                 }
             }
         }
         __syncthreads();
-        relres = s_ab[2];
-        if (s_flag == 1) { iters = it; return YGPU_OK; }
-        if (s_flag == 2) { iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
+        if (s_flag == 1) { relres = (double)s_ab[2]; iters = it; return YGPU_OK; }
+        if (s_flag == 2) { relres = (double)s_ab[2]; iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
         T* mc = m0;
         T* mn = m1;
         bool recheck = false;
         while (it < maxiter) {
-            const T a = (T)s_ab[0], bt = (T)s_ab[1];
+            const T a = s_ab[0], bt = s_ab[1];
             a0 = a1 = a2 = T(0);
             for (int t = gw; t < nt; t += nw) {
                 const int k = tile_unknown(G, t, lane);
@@ -2293,14 +2300,14 @@ __device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op
             if (lead) {
                 // FP32 inner solves: the recurrence scalars in FP32 (its division
                 // and square root are far faster than FP64's on this part)
-                const W rel = sqrt((W)red[2]) / (W)bnrm;
+                const W rel = sqrt(red[2]) / (W)bnrm;
                 s_ab[2] = rel;
                 if (!isfinite(rel)) s_flag = 2;
                 else if (rel <= (W)tol) s_flag = 1;
                 else {
-                    const W gam = (W)red[0], del = (W)red[1];
-                    const W beta = gam / (W)gam_old;
-                    const W alpha = gam / (del - beta * gam / (W)alpha_old);
+                    const W gam = red[0], del = red[1];
+                    const W beta = gam / gam_old;
+                    const W alpha = gam / (del - beta * gam / alpha_old);
                     if (!isfinite(alpha) || !isfinite(beta) || del == W(0)) s_flag = 3;
                     else {
                         s_flag = 0;
@@ -2313,7 +2320,7 @@ __device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op
             }
             __syncthreads();
             const int flag = s_flag;
-            relres = s_ab[2];
+            if (flag != 0) relres = (double)s_ab[2];
             if (flag == 2) { iters = it; return YGPU_BREAKDOWN; }
             if (flag == 1) { recheck = true; break; }
             if (flag == 3) {
@@ -2322,14 +2329,19 @@ __device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op
             }
         }
         iters = it;
+        relres = (double)s_ab[2];
         if (!recheck) return YGPU_MAXITER;
-        double tr = 0.0;
+        T tr = T(0);
         for (int k = Tm.tid; k < G.nu; k += Tm.nthr) {
-            const double rk = (double)b[k] - (double)A.row(k, x);
+            const T rk = b[k] - A.row(k, x);
             tr += rk * rk;
         }
-        if (!(ok = team_allreduce(Tm, &tr, 1))) return YGPU_ERR_TIMEOUT;
-        relres = sqrt(tr) / bnrm;
+        {
+            T trs;
+            if (!(ok = team_allreduce_w<T>(Tm, &tr, &trs, 1))) return YGPU_ERR_TIMEOUT;
+            tr = trs;
+        }
+        relres = (double)(sqrt(tr) / (W)bnrm);
         if (relres <= tol) return YGPU_OK;
         if (it >= maxiter) return YGPU_MAXITER;
     }
@@ -2719,7 +2731,7 @@ __device__ __noinline__ void step_krylov(const Inst& I, const ygpu_dyn_par& P, T
     const bool lead = (T.cta == 0 && threadIdx.x == 0);
     PhaseClock clk;
     clk.start();
-    const double s0 = T.sync_ns;
+    const unsigned long long s0 = T.sync_ns;
     const double bn2 = out->bn2;
     int it = 0, outer = 0, st;
     double rr = 0.0;
@@ -2734,7 +2746,7 @@ __device__ __noinline__ void step_krylov(const Inst& I, const ygpu_dyn_par& P, T
     if (ok) ok = team_barrier(T);
     if (lead) {
         out->phase_ns[5] += clk.lap();
-        out->phase_ns[9] += T.sync_ns - s0;
+        out->phase_ns[9] += (double)(T.sync_ns - s0);
         out->lin_it = it;
         out->lin_st = st;
         out->lin_outer = outer;
@@ -2895,7 +2907,7 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
     T.ctl = ctls + team;
     T.parity = 0;
     T.abort_all = abort_all;
-    T.sync_ns = 0.0;
+    T.sync_ns = 0ull;
     T.gen = (threadIdx.x == 0) ? ld_acquire_u32(&T.ctl->base) : 0u;
     T.spin_lim = (threadIdx.x == 0) ? team_spin_limit(T.ctl) : 0u;
     T.cl = false;
@@ -2912,7 +2924,7 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
             else if (STEP == YG_STEP_KRYLOV) step_krylov(sI, P, T, done_count);
             else step_post(sI, P, T, done_count, STEP == YG_STEP_FINAL);
             if (T.cta == 0 && threadIdx.x == 0) sI.out->phase_ns[8] += T.sync_ns;
-            T.sync_ns = 0.0;
+            T.sync_ns = 0ull;
         }
         __syncthreads();
     }
@@ -2966,7 +2978,7 @@ __global__ void __launch_bounds__(YG_KBLOCK, 1) ygpu_k_krylov_cl(const Inst* ins
     T.ctl = ctls;                  // not used by cluster teams
     T.parity = 0;
     T.abort_all = ab;
-    T.sync_ns = 0.0;
+    T.sync_ns = 0ull;
     T.gen = 0u;
     T.spin_lim = YG_SPIN_LIMIT;
     T.cl = true;
@@ -2982,7 +2994,7 @@ __global__ void __launch_bounds__(YG_KBLOCK, 1) ygpu_k_krylov_cl(const Inst* ins
         if (!s_flags[1]) {
             step_krylov(sI, P, T, dc);
             if (T.cta == 0 && threadIdx.x == 0) sI.out->phase_ns[8] += T.sync_ns;
-            T.sync_ns = 0.0;
+            T.sync_ns = 0ull;
         }
         // no CTA starts the next instance (or leaves) while another may still read
         // its shared memory
@@ -3027,7 +3039,7 @@ __global__ void __launch_bounds__(YG_BLOCK) ygpu_csr_kernel(CsrJob J, TeamCtl* c
     T.ctl = ctl;
     T.parity = 0;
     T.abort_all = abort_all;
-    T.sync_ns = 0.0;
+    T.sync_ns = 0ull;
     T.gen = 0u;
     T.spin_lim = YG_SPIN_LIMIT;
     T.cl = false;
@@ -3216,7 +3228,7 @@ __global__ void __launch_bounds__(YG_BLOCK) ygpu_adv_kernel(AdvJob J, TeamCtl* c
     T.ctl = ctl;
     T.parity = 0;
     T.abort_all = abort_all;
-    T.sync_ns = 0.0;
+    T.sync_ns = 0ull;
     T.gen = 0u;
     T.spin_lim = YG_SPIN_LIMIT;
     T.cl = false;
