@@ -333,7 +333,7 @@ size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block) {
     b += 6 * al(nu * 4);                 // ukind, emap, mem(3), rpart
     b += al((n2 + 1) * 4);               // active cell list
     b += al(n2);                         // cell flags
-    if (mixed) b += 4 * al(n2 * 4) + 13 * al(nu * 4);
+    if (mixed) b += 4 * al(n2 * 4) + 13 * al(nu * 4) + al(8 * nu * 4);   // + CG row records
     if (block) b += al(tile_blocks(nx, ny) * 1024 * 4);
     return b;
 }
@@ -363,7 +363,9 @@ void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool m
         I.fdinv = Fv(nu); I.fx = Fv(nu); I.fr = Fv(nu); I.fp = Fv(nu); I.fq = Fv(nu); I.fz = Fv(nu);
         I.frt = Fv(nu); I.fv = Fv(nu); I.fs = Fv(nu); I.ft = Fv(nu); I.fph = Fv(nu); I.fsh = Fv(nu);
         I.fm2 = Fv(nu);
+        I.fst = (float4*)Fv(8 * nu);
     } else {
+        I.fst = nullptr;
         I.fN = I.fNab = I.fdrag_x = I.fdrag_y = I.fdinv = nullptr;
         I.fx = I.fr = I.fp = I.fq = I.fz = I.frt = I.fv = I.fs = I.ft = I.fph = I.fsh = I.fm2 = nullptr;
     }

@@ -151,6 +151,7 @@ struct Inst {
     float *fN, *fNab, *fdrag_x, *fdrag_y, *fdinv;
     float* fminv;                  // mixed, block preconditioner: inverse of each 4x4-cell tile block (32x32)
     float *fx, *fr, *fp, *fq, *fz, *frt, *fv, *fs, *ft, *fph, *fsh, *fm2;
+    float4* fst;                   // mixed CG: per unknown the records (z, q, s, p), (x, r, u, w)
     InstOut* out;
     int visc_final_in_alt;         // set by the kernel: final visc is in visc_alt
 };
@@ -166,13 +167,14 @@ struct Inst {
 // grows by the team's CTA count at each barrier. `base` holds count at the
 // start of a launch (CTA 0 stores it at the end of the previous launch, after
 // its last arrival; every CTA reads it before its first).
-struct TeamCtl {
+struct __align__(16) TeamCtl {
     unsigned int count;
     unsigned int base;
     int abort;
     int inst;                      // instance the team works on (work queue)
     unsigned char spin_log2;       // 0: waits give up after YG_SPIN_LIMIT polls; k: after 2^k
-    union {                        // per-CTA totals of the all-reduces, by parity
+    union __align__(16) {          // per-CTA totals of the all-reduces, by parity; the
+                                   // YG_RED_MAX totals of a CTA are one 16/32-byte record
         double slots[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
         float fslots[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
     };
@@ -183,6 +185,16 @@ template <>
 YG_DEV double* team_slot<double>(TeamCtl* c, int parity, int cta, int k) { return &c->slots[parity][cta][k]; }
 template <>
 YG_DEV float* team_slot<float>(TeamCtl* c, int parity, int cta, int k) { return &c->fslots[parity][cta][k]; }
+// One CTA's record of YG_RED_MAX totals in a single round trip (L2, bypassing L1)
+YG_DEV void team_slot_load(TeamCtl* c, int parity, int cta, float v[YG_RED_MAX]) {
+    const float4 r = __ldcg(reinterpret_cast<const float4*>(&c->fslots[parity][cta][0]));
+    v[0] = r.x; v[1] = r.y; v[2] = r.z; v[3] = r.w;
+}
+YG_DEV void team_slot_load(TeamCtl* c, int parity, int cta, double v[YG_RED_MAX]) {
+    const double2* p = reinterpret_cast<const double2*>(&c->slots[parity][cta][0]);
+    const double2 r0 = __ldcg(p), r1 = __ldcg(p + 1);
+    v[0] = r0.x; v[1] = r0.y; v[2] = r1.x; v[3] = r1.y;
+}
 
 struct Team {
     int cta, ncta;                 // rank of this CTA in the team, CTAs in the team
@@ -285,61 +297,103 @@ YG_DEV bool team_allreduce_impl(Team& T, const V* in, V* out, int nv) {
     // every CTA passes after its reads of that buffer)
     __shared__ V s_cl[2][YG_RED_MAX];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int k = 0; k < nv; k++) {
-        V w = warp_sum<V>(in[k]);
-        if (lane == 0) s_red[wid][k] = w;
-    }
+    // the nv sums are reduced side by side (independent shuffle chains)
+    V w[YG_RED_MAX];
+#pragma unroll
+    for (int k = 0; k < YG_RED_MAX; k++) w[k] = (k < nv) ? in[k] : V(0);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int k = 0; k < YG_RED_MAX; k++) w[k] += __shfl_xor_sync(0xffffffffu, w[k], o);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < YG_RED_MAX; k++) s_red[wid][k] = w[k];
     __syncthreads();
+    // warp 0: the CTA's totals (all YG_RED_MAX slots, unused ones 0)
+    auto cta_totals = [&](V t[YG_RED_MAX]) {
+#pragma unroll
+        for (int k = 0; k < YG_RED_MAX; k++) t[k] = (lane < nw) ? s_red[lane][k] : V(0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int k = 0; k < YG_RED_MAX; k++) t[k] += __shfl_xor_sync(0xffffffffu, t[k], o);
+    };
     if (T.cl) {
         if (wid == 0) {
-            for (int k = 0; k < nv; k++) {
-                V w = (lane < nw) ? s_red[lane][k] : V(0);
-                w = warp_sum<V>(w);
-                if (lane == 0) s_cl[T.parity][k] = w;
-            }
+            V t[YG_RED_MAX];
+            cta_totals(t);
+            if (lane == 0)
+#pragma unroll
+                for (int k = 0; k < YG_RED_MAX; k++) s_cl[T.parity][k] = t[k];
         }
         cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
         cl.sync();
         if (wid == 0) {
             // every CTA sums the CTA totals in the same order: identical results
-            for (int k = 0; k < nv; k++) {
-                V w = V(0);
-                for (int c = lane; c < T.ncta; c += 32) w += *cl.map_shared_rank(&s_cl[T.parity][k], c);
-                w = warp_sum<V>(w);
-                if (lane == 0) s_tot[k] = w;
+            V a[YG_RED_MAX];
+#pragma unroll
+            for (int k = 0; k < YG_RED_MAX; k++) a[k] = V(0);
+            for (int c = lane; c < T.ncta; c += 32) {
+                const V* r = cl.map_shared_rank(&s_cl[T.parity][0], c);
+#pragma unroll
+                for (int k = 0; k < YG_RED_MAX; k++) a[k] += r[k];
             }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int k = 0; k < YG_RED_MAX; k++) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+            if (lane == 0)
+#pragma unroll
+                for (int k = 0; k < YG_RED_MAX; k++) s_tot[k] = a[k];
         }
         T.parity ^= 1;
         __syncthreads();
         for (int k = 0; k < nv; k++) out[k] = s_tot[k];
-        __syncthreads();
+        // no closing barrier: s_tot and s_red are next written after the next
+        // call's first __syncthreads, which every thread passes after these reads
         return true;
     }
     if (wid == 0) {
-        for (int k = 0; k < nv; k++) {
-            V w = (lane < nw) ? s_red[lane][k] : V(0);
-            w = warp_sum<V>(w);
-            if (lane == 0) {
-                if (T.ncta > 1) *team_slot<V>(T.ctl, T.parity, T.cta, k) = w;
-                else s_tot[k] = w;
+        V t[YG_RED_MAX];
+        cta_totals(t);
+        if (lane == 0) {
+            if (T.ncta > 1) {
+                V* r = team_slot<V>(T.ctl, T.parity, T.cta, 0);
+#pragma unroll
+                for (int k = 0; k < YG_RED_MAX; k++) r[k] = t[k];
+            } else {
+#pragma unroll
+                for (int k = 0; k < YG_RED_MAX; k++) s_tot[k] = t[k];
             }
         }
     }
     if (T.ncta > 1) {
         if (!team_barrier(T)) return false;
         if (wid == 0) {
-            for (int k = 0; k < nv; k++) {
-                V w = V(0);
-                for (int c = lane; c < T.ncta; c += 32) w += __ldcg(team_slot<V>(T.ctl, T.parity, c, k));
-                w = warp_sum<V>(w);
-                if (lane == 0) s_tot[k] = w;
+            // one record (all the sums of a CTA) per load: a single L2 round trip
+            // for teams of up to 32 CTAs
+            V a[YG_RED_MAX];
+#pragma unroll
+            for (int k = 0; k < YG_RED_MAX; k++) a[k] = V(0);
+            for (int c = lane; c < T.ncta; c += 32) {
+                V r[YG_RED_MAX];
+                team_slot_load(T.ctl, T.parity, c, r);
+#pragma unroll
+                for (int k = 0; k < YG_RED_MAX; k++) a[k] += r[k];
             }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int k = 0; k < YG_RED_MAX; k++) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+            if (lane == 0)
+#pragma unroll
+                for (int k = 0; k < YG_RED_MAX; k++) s_tot[k] = a[k];
         }
         T.parity ^= 1;
     }
     __syncthreads();
     for (int k = 0; k < nv; k++) out[k] = s_tot[k];
-    __syncthreads();
+    // no closing barrier (see the cluster branch)
     return true;
 }
 template <typename V>

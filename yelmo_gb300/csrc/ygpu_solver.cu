@@ -223,60 +223,76 @@ YG_DEV void nodes_aa(const Geo& G, const Nb& n, F val, A act, bool use_act, doub
 // Phase: horizontal strain rates at the faces of every cell
 // (calc_strain_rate_horizontal_2D, deformation.f90:1393-1507)
 // ---------------------------------------------------------------------------
-YG_DEV double deriv_active(double vm, double v0, double vp, bool am, bool ap, double h) {
-    if (am && ap) return (vp - vm) / (2.0 * h);
-    if (ap) return (vp - v0) / h;
-    if (am) return (v0 - vm) / h;
-    return 0.0;
+// Quotient of an FP64 difference by a grid step: FP64 results divide as the
+// reference does; FP32 results (the mixed mode) scale the FP64 difference by
+// the FP32 reciprocal, with no FP64 division (a long chain on this part's FP64
+// pipe, which runs at about 1/64 of the FP32 rate)
+template <typename SD>
+YG_DEV SD quot_h(double num, double h, float inv_h) {
+    if constexpr (sizeof(SD) == sizeof(float)) return (float)num * inv_h;
+    else return num / h;
+}
+template <typename SD>
+YG_DEV SD deriv_active(double vm, double v0, double vp, bool am, bool ap, double h, float inv_h, float inv_2h) {
+    if (am && ap) return quot_h<SD>(vp - vm, 2.0 * h, inv_2h);
+    if (ap) return quot_h<SD>(vp - v0, h, inv_h);
+    if (am) return quot_h<SD>(v0 - vm, h, inv_h);
+    return SD(0);
 }
 
 template <typename SD>
-__device__ __noinline__ void phase_strain(const Inst& I, const Geo& G, Team& T, const double* ux, const double* uy, SD* sdudx,
+__device__ __noinline__ void phase_strain(const Inst& I, const Geo& Gr, Team& T, const double* ux, const double* uy, SD* sdudx,
                                           SD* sdudy, SD* sdvdx, SD* sdvdy) {
+    const Geo G = Gr;
+    const int tid = T.tid, nthr = T.nthr;
     const unsigned char* fl = I.cflag;
     const double dx = G.dx, dy = G.dy;
-    for (int c = T.tid; c < G.n2; c += T.nthr) {
+    const float ix = (float)(1.0 / dx), iy = (float)(1.0 / dy), i2x = (float)(1.0 / (2.0 * dx)),
+                i2y = (float)(1.0 / (2.0 * dy));
+    for (int c = tid; c < G.n2; c += nthr) {
         Nb n = make_nb(G, c);
         const int i = n.i, j = n.j;
-        double dudx = (ux[CI(n.ip1, j)] - ux[CI(n.im1, j)]) / (2.0 * dx);
-        double dudy = deriv_active(ux[CI(i, n.jm1)], ux[c], ux[CI(i, n.jp1)], act_x(G, fl, i, n.jm1), act_x(G, fl, i, n.jp1), dy);
-        double dvdx = deriv_active(uy[CI(n.im1, j)], uy[c], uy[CI(n.ip1, j)], act_y(G, fl, n.im1, j), act_y(G, fl, n.ip1, j), dx);
-        double dvdy = (uy[CI(i, n.jp1)] - uy[CI(i, n.jm1)]) / (2.0 * dy);
+        SD dudx = quot_h<SD>(ux[CI(n.ip1, j)] - ux[CI(n.im1, j)], 2.0 * dx, i2x);
+        SD dudy = deriv_active<SD>(ux[CI(i, n.jm1)], ux[c], ux[CI(i, n.jp1)], act_x(G, fl, i, n.jm1), act_x(G, fl, i, n.jp1),
+                                   dy, iy, i2y);
+        SD dvdx = deriv_active<SD>(uy[CI(n.im1, j)], uy[c], uy[CI(n.ip1, j)], act_y(G, fl, n.im1, j), act_y(G, fl, n.ip1, j),
+                                   dx, ix, i2x);
+        SD dvdy = quot_h<SD>(uy[CI(i, n.jp1)] - uy[CI(i, n.jm1)], 2.0 * dy, i2y);
         int d1, d2, d3;
         if ((fl[c] & CF_ICE) && !(fl[CI(n.ip1, j)] & CF_ICE)) {
             int im2;
             nbr_bc(n.im1, j, G.nx, G.ny, G.bc, im2, d1, d2, d3);
             if ((fl[CI(n.im1, j)] & CF_ICE) && im2 != n.im1)
-                dudx = (1.0 * ux[CI(im2, j)] - 4.0 * ux[CI(n.im1, j)] + 3.0 * ux[c]) / (2.0 * dx);
+                dudx = quot_h<SD>(1.0 * ux[CI(im2, j)] - 4.0 * ux[CI(n.im1, j)] + 3.0 * ux[c], 2.0 * dx, i2x);
             else
-                dudx = (ux[c] - ux[CI(n.im1, j)]) / dx;
+                dudx = quot_h<SD>(ux[c] - ux[CI(n.im1, j)], dx, ix);
         } else if (!(fl[c] & CF_ICE) && (fl[CI(n.ip1, j)] & CF_ICE)) {
             int ip2;
             nbr_bc(n.ip1, j, G.nx, G.ny, G.bc, d1, ip2, d2, d3);
             if (ip2 != n.ip1 && (fl[CI(ip2, j)] & CF_ICE))
-                dudx = -(1.0 * ux[CI(ip2, j)] - 4.0 * ux[CI(n.ip1, j)] + 3.0 * ux[c]) / (2.0 * dx);
+                dudx = quot_h<SD>(-(1.0 * ux[CI(ip2, j)] - 4.0 * ux[CI(n.ip1, j)] + 3.0 * ux[c]), 2.0 * dx, i2x);
             else
-                dudx = (ux[CI(n.ip1, j)] - ux[c]) / dx;
+                dudx = quot_h<SD>(ux[CI(n.ip1, j)] - ux[c], dx, ix);
         }
         if ((fl[c] & CF_ICE) && !(fl[CI(i, n.jp1)] & CF_ICE)) {
             int jm2;
             nbr_bc(i, n.jm1, G.nx, G.ny, G.bc, d1, d2, jm2, d3);
             if ((fl[CI(i, n.jm1)] & CF_ICE) && jm2 != n.jm1)
-                dvdy = (1.0 * uy[CI(i, jm2)] - 4.0 * uy[CI(i, n.jm1)] + 3.0 * uy[c]) / (2.0 * dy);
+                dvdy = quot_h<SD>(1.0 * uy[CI(i, jm2)] - 4.0 * uy[CI(i, n.jm1)] + 3.0 * uy[c], 2.0 * dy, i2y);
             else
-                dvdy = (uy[c] - uy[CI(i, n.jm1)]) / dy;
+                dvdy = quot_h<SD>(uy[c] - uy[CI(i, n.jm1)], dy, iy);
         } else if (!(fl[c] & CF_ICE) && (fl[CI(i, n.jp1)] & CF_ICE)) {
             int jp2;
             nbr_bc(i, n.jp1, G.nx, G.ny, G.bc, d1, d2, d3, jp2);
             if (jp2 != n.jp1 && (fl[CI(i, jp2)] & CF_ICE))
-                dvdy = -(1.0 * uy[CI(i, jp2)] - 4.0 * uy[CI(i, n.jp1)] + 3.0 * uy[c]) / (2.0 * dy);
+                dvdy = quot_h<SD>(-(1.0 * uy[CI(i, jp2)] - 4.0 * uy[CI(i, n.jp1)] + 3.0 * uy[c]), 2.0 * dy, i2y);
             else
-                dvdy = (uy[CI(i, n.jp1)] - uy[c]) / dy;
+                dvdy = quot_h<SD>(uy[CI(i, n.jp1)] - uy[c], dy, iy);
         }
-        sdudx[c] = (SD)dudx;
-        sdudy[c] = (SD)dudy;
-        sdvdx[c] = (SD)dvdx;
-        sdvdy[c] = (SD)dvdy;
+        sdudx[c] = dudx;
+        sdudy[c] = dudy;
+        sdvdx[c] = dvdx;
+        sdvdy[c] = dvdy;
     }
 }
 
@@ -434,12 +450,43 @@ YG_DEV float* shear_f32(const Inst& I, int axis) {
 // R = float (mixed mode): FP32 arithmetic into the FP32 copies that the column
 // pass reads; the caller's FP64 duxdz / duydz are those floats widened, written
 // once by the final passes rather than every iteration
+// Per-layer factors of the vertical passes: 1 - zeta(k) and zeta(k) - zeta(k-1).
+// FP32 passes read them from a table in shared memory, filled once per call
+// (every thread of the CTA constructs it), instead of forming them in FP64 for
+// every cell and layer; FP64 passes form them as the reference does.
+#define YG_ZTAB 128
+template <typename R>
+struct ZTab {
+    const double* zeta;
+    bool tab;
+    float* s_o;
+    float* s_d;
+    YG_DEV ZTab(const double* z, int nz) : zeta(z) {
+        __shared__ float so[YG_ZTAB], sd[YG_ZTAB];
+        s_o = so;
+        s_d = sd;
+        tab = (sizeof(R) == sizeof(float)) && nz <= YG_ZTAB;
+        if (tab) {
+            __syncthreads();       // a previous call's readers are done
+            for (int k = threadIdx.x; k < nz; k += blockDim.x) {
+                so[k] = (float)(1.0 - z[k]);
+                sd[k] = (k > 0) ? (float)(z[k] - z[k - 1]) : 0.0f;
+            }
+            __syncthreads();
+        }
+    }
+    YG_DEV R omz(int k) const { return tab ? (R)s_o[k] : (R)(1.0 - zeta[k]); }
+    YG_DEV R dz(int k) const { return tab ? (R)s_d[k] : (R)(zeta[k] - zeta[k - 1]); }
+};
+
 template <typename R, typename VS>
-__device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, const VS* vcur) {
+__device__ __noinline__ void phase_shear(const Inst& I, const Geo& Gr, Team& T, const VS* vcur) {
+    const Geo G = Gr;
     const int nz = G.nz, n2 = G.n2;
     const double* f = I.f_ice;
     float* sx32 = shear_f32(I, 0);
     float* sy32 = shear_f32(I, 1);
+    const ZTab<R> zt(I.zeta, nz);
     for (int c = T.tid; c < n2; c += T.nthr) {
         Nb n = make_nb(G, c);
         const int cx = CI(n.ip1, n.j), cy = CI(n.i, n.jp1);
@@ -447,7 +494,7 @@ __device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, c
         const double fc = f[c], fx = f[cx], fy = f[cy];
         for (int k = 0; k < nz; k++) {
             const size_t o = (size_t)k * n2;
-            const R omz = (R)(1.0 - I.zeta[k]);
+            const R omz = zt.omz(k);
             const R vc = (R)vcur[o + c];
             R va = stag_margin<R>(vc, (R)vcur[o + cx], fc, fx);
             const R gx = (va != R(0)) ? (tx / va) * omz : R(0);
@@ -472,10 +519,11 @@ __device__ __noinline__ void phase_shear(const Inst& I, const Geo& G, Team& T, c
 // working copy of the mixed mode); log(visc) is kept in R. vcur (the caller's
 // FP64 viscosity) is read only when no log is carried yet (first iteration).
 template <typename R, typename VD, typename SR = double>
-__device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T,
+__device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, const Geo& Gr, Team& T,
                                           const double* vcur, VD* vnew, const SR* sdudx,
                                           const SR* sdudy, const SR* sdvdx, const SR* sdvdy, bool relax,
                                           bool diva, bool first_copy, bool have_log, bool visc_only = false) {
+    const Geo G = Gr;
     const int nz = G.nz, n2 = G.n2;
     const R p1 = (R)((1.0 - I.n_glen) / (2.0 * I.n_glen));
     const bool glen3 = (I.n_glen == 3.0);
@@ -487,6 +535,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
     // A^(-1/n) at the nodes and log(visc): FP32 storage in the mixed mode
     const R* attp_r = (const R*)I.attp;
     R* lv = (R*)I.lvis;
+    const ZTab<R> zt(zeta, nz);
     for (int c = T.tid; c < n2; c += T.nthr) {
         Nb n = make_nb(G, c);
         if (first_copy) {
@@ -599,10 +648,10 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
             vnew[ck] = (VD)vr;
             // trapezoid integrals (integrate_trapezoid1D_pt, yelmo_tools.f90:1092-1122),
             // in the viscosity arithmetic R
-            const R omz = (R)(1.0 - zeta[k]);
+            const R omz = zt.omz(k);
             const R g = (Hr / vr) * (omz * omz);
             if (k > 0) {
-                const R dzt = (R)(zeta[k] - zeta[k - 1]);
+                const R dzt = zt.dz(k);
                 vint = vint + R(0.5) * (vr + vprev) * dzt;
                 f2 = f2 + R(0.5) * (g + gprev) * dzt;
             }
@@ -702,14 +751,20 @@ YG_DEV void lim_face(double& k, double& r, double u, double uc, int mask, double
     r = (k - b) * u;
 }
 
-__device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, bool diva) {
+// R: arithmetic of the effective friction, the operator drag and N_ab: FP64 in
+// the FP64 solve; FP32 in the mixed one, whose FP64 outer residual then uses
+// the FP32-rounded coefficients (the same values as its FP32 inner operator)
+template <typename R>
+__device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, const Geo& Gr, Team& T, bool diva) {
+    const Geo G = Gr;
+    const int tid = T.tid, nthr = T.nthr;
     const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
     const bool drag = (P.ssa_vel_lim_method == YGPU_VEL_LIM_DRAG);
     const bool limit = (P.beta_method != -1 && P.beta_gl_stag != -1);
     const double s0 = 0.8 * P.ssa_vel_max;
     const double inv_du = 1.0 / (P.ssa_vel_max - s0);
     const int nx = G.nx, ny = G.ny;
-    for (int c = T.tid; c < G.n2; c += T.nthr) {
+    for (int c = tid; c < G.n2; c += nthr) {
         Nb n = make_nb(G, c);
         const int i = n.i, j = n.j;
         // staggered F2 (stagger_F_integral, velocity_diva.f90:871-910)
@@ -746,25 +801,26 @@ __device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, c
         I.beta_x[c] = bx;
         I.beta_y[c] = by;
         // friction used by the matrix
-        double mx_b = bx, my_b = by;
+        R mx_b = (R)bx, my_b = (R)by;
         if (diva) {
             // calc_beta_eff, velocity_diva.f90:912-958
+            const R f2x = (R)F2x, f2y = (R)F2y, f2 = (R)I.F2[c], be = (R)I.beta[c];
             if (P.no_slip) {
-                mx_b = (F2x > 0.0) ? 1.0 / F2x : 0.0;
-                my_b = (F2y > 0.0) ? 1.0 / F2y : 0.0;
-                I.beta_eff[c] = (I.F2[c] > 0.0) ? 1.0 / I.F2[c] : 0.0;
+                mx_b = (f2x > R(0)) ? R(1) / f2x : R(0);
+                my_b = (f2y > R(0)) ? R(1) / f2y : R(0);
+                I.beta_eff[c] = (double)((f2 > R(0)) ? R(1) / f2 : R(0));
             } else {
-                mx_b = bx / (1.0 + bx * F2x);
-                my_b = by / (1.0 + by * F2y);
-                I.beta_eff[c] = I.beta[c] / (1.0 + I.beta[c] * I.F2[c]);
+                mx_b = mx_b / (R(1) + mx_b * f2x);
+                my_b = my_b / (R(1) + my_b * f2y);
+                I.beta_eff[c] = (double)(be / (R(1) + be * f2));
             }
         }
         // set_beta_min_grounded, basal_dragging.f90:706-780
         const int mx = I.mask_x[c], my = I.mask_y[c];
-        if (mx == 1 && mx_b == 0.0) mx_b = P.beta_min;
-        if (my == 1 && my_b == 0.0) my_b = P.beta_min;
-        I.bm_x[c] = mx_b;
-        I.bm_y[c] = my_b;
+        if (mx == 1 && mx_b == R(0)) mx_b = (R)P.beta_min;
+        if (my == 1 && my_b == R(0)) my_b = (R)P.beta_min;
+        I.bm_x[c] = (double)mx_b;
+        I.bm_y[c] = (double)my_b;
         // speed-limit drag around the iterate
         double kx = 0.0, ky = 0.0, rx = 0.0, ry = 0.0;
         if (drag) {
@@ -777,28 +833,30 @@ __device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, c
         }
         I.lk_x[c] = kx; I.lk_y[c] = ky; I.lr_x[c] = rx; I.lr_y[c] = ry;
         // operator drag coefficients: w*(beta + k) (* dx*dy for the energy form)
-        double wx, wy;
+        R wx, wy, dgx, dgy;
         if (energy) {
-            wx = (mx == 3 || mx == 4) ? 0.5 : 1.0;
-            wy = (my == 3 || my == 4) ? 0.5 : 1.0;
-            I.drag_x[c] = wx * (mx_b + kx) * G.dxdy;
-            I.drag_y[c] = wy * (my_b + ky) * G.dxdy;
+            wx = (mx == 3 || mx == 4) ? R(0.5) : R(1);
+            wy = (my == 3 || my == 4) ? R(0.5) : R(1);
+            dgx = wx * (mx_b + (R)kx) * (R)G.dxdy;
+            dgy = wy * (my_b + (R)ky) * (R)G.dxdy;
         } else {
-            wx = (mx == 4) ? 0.5 : 1.0;
-            wy = (my == 4) ? 0.5 : 1.0;
-            I.drag_x[c] = wx * mx_b + wx * kx;
-            I.drag_y[c] = wy * my_b + wy * ky;
+            wx = (mx == 4) ? R(0.5) : R(1);
+            wy = (my == 4) ? R(0.5) : R(1);
+            dgx = wx * mx_b + wx * (R)kx;
+            dgy = wy * my_b + wy * (R)ky;
         }
+        I.drag_x[c] = (double)dgx;
+        I.drag_y[c] = (double)dgy;
         if (I.fdrag_x) {               // mixed mode: FP32 copies of the inner solves
-            I.fdrag_x[c] = (float)I.drag_x[c];
-            I.fdrag_y[c] = (float)I.drag_y[c];
+            I.fdrag_x[c] = (float)dgx;
+            I.fdrag_y[c] = (float)dgy;
         }
         // stagger_visc_aa_ab, solver_ssa_ac.f90:1000-1067
         {
             const int cc[4] = {c, CI(n.ip1, j), CI(i, n.jp1), CI(n.ip1, n.jp1)};
             int nice = 0;
             bool anyocn = false;
-            double v[4];
+            R v[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const unsigned fq = I.cflag[cc[q]];
@@ -806,10 +864,17 @@ __device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, c
                 bool ocn = (fq & CF_OCN) != 0;
                 nice += ice;
                 anyocn = anyocn || ocn;
-                v[q] = ice ? I.visc_int[cc[q]] : 0.0;
+                v[q] = ice ? (R)I.visc_int[cc[q]] : R(0);
             }
-            I.Nab[c] = (anyocn || nice == 0) ? 0.0 : ((v[0] + v[1]) + (v[2] + v[3])) / (double)nice;
-            if (I.fNab) I.fNab[c] = (float)I.Nab[c];
+            // the mean: a division only for three iced corners (halving and
+            // quartering are exact multiplications)
+            const R sum = (v[0] + v[1]) + (v[2] + v[3]);
+            R nab;
+            if (anyocn || nice == 0) nab = R(0);
+            else if (nice == 3) nab = sum / R(3);
+            else nab = sum * ((nice == 4) ? R(0.25) : (nice == 2) ? R(0.5) : R(1));
+            I.Nab[c] = (double)nab;
+            if (I.fNab) I.fNab[c] = (float)nab;
         }
     }
 }
@@ -1163,6 +1228,22 @@ struct StencilOp {
     YG_DEV T row(int u, const T* v) const { return operator_row<T, CT>(*I, *G, K, energy, N, Nab, dgx, dgy, v, u); }
     YG_DEV int nx() const { return G->nx; }
     YG_DEV int n2() const { return G->n2; }
+    // kind of row u in the Krylov loops of the energy form: 0 interior stencil,
+    // 1 identity (Dirichlet or tied: every Krylov vector is 0 there), 2 general
+    YG_DEV unsigned row_kind(int u) const {
+        if (!energy) return 2u;
+        if (I->rpart[u] == 1) return 0u;
+        return (I->ukind[u] != DOF_FREE) ? 1u : 2u;
+    }
+    // row u outside the interior stencil
+    YG_DEV T general(int u, const T* v) const {
+        if (!energy) return residual_row<T, CT>(*I, *G, K, N, Nab, dgx, dgy, v, u, nullptr);
+        return energy_row_general<T, CT>(*I, *G, K, N, Nab, dgx, dgy, v, u);
+    }
+    // both rows of cell c = (i, j) on the interior stencil (energy form)
+    YG_DEV void cell_fast(int c, int i, int j, const T* v, T& y0, T& y1) const {
+        energy_cell_fast<T, CT>(*G, K, N, Nab, dgx, dgy, v, c, i, j, y0, y1);
+    }
     // both rows of cell c = (i, j): ux row c and uy row n2 + c
     YG_DEV void cell(int c, int i, int j, const T* v, T& y0, T& y1) const {
         const int n2 = G->n2;
@@ -1567,8 +1648,14 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
         if (ident) x0 = b;
         I.b[u] = b;
         I.x[u] = x0;
-        I.dinv[u] = (d != 0.0) ? 1.0 / d : 1.0;
-        if (I.fdinv) I.fdinv[u] = (float)I.dinv[u];
+        // the Jacobi diagonal: FP64 for the FP64 solvers; the mixed mode's FP32
+        // inner solves take an FP32 reciprocal (no FP64 division)
+        if (I.fdinv) {
+            const float df = (float)d;
+            I.fdinv[u] = (df != 0.0f) ? 1.0f / df : 1.0f;
+        } else {
+            I.dinv[u] = (d != 0.0) ? 1.0 / d : 1.0;
+        }
         bn2 += b * b;
     }
     bnorm2 = bn2;
@@ -1836,6 +1923,237 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const
             tr = trs;
         }
         relres = (double)(sqrt(tr) / (W)bnrm);
+        if (relres <= tol) return YGPU_OK;
+        if (it >= maxiter) return YGPU_MAXITER;
+    }
+    return YGPU_MAXITER;
+}
+
+// Pipelined preconditioned CG of the FP32 inner solves (energy form), the
+// same recurrence as krylov_pcg_pipe laid out for this part's memory system:
+//  - the eight recurrence vectors of an unknown are one 32-byte record of two
+//    float4, (z, q, s, p) and (x, r, u, w): a row's state moves in two vector
+//    loads and two vector stores;
+//  - each thread's active cells are cached in shared memory packed with their
+//    grid position and row kinds (i | j << 14 | kind(ux) << 28 | kind(uy) << 30),
+//    so an iteration reads no cell list or row kind and divides nothing;
+//  - a cell's state loads are issued before its stencil loads, which do not
+//    depend on them: one memory round trip per cell;
+//  - identity rows (Dirichlet or tied) are skipped: all their vectors stay 0.
+// Only the operator input m (read at neighbouring cells) and the plain x, r, u
+// of the restarts and of the true-residual check live in plain arrays; x goes
+// back to its plain array whenever the recurrence stops. Needs nx, ny < 2^14.
+YG_DEV unsigned cell_pack(int i, int j, unsigned k0, unsigned k1) {
+    return (unsigned)i | ((unsigned)j << 14) | (k0 << 28) | (k1 << 30);
+}
+template <typename Op>
+__device__ __noinline__ int krylov_pcg_cells(Team& Tm, int nu, const Op& A, const float* __restrict__ dinv,
+                                             float* __restrict__ x, const float* __restrict__ b,
+                                             float* __restrict__ r, float* __restrict__ u, float* m0, float* m1,
+                                             float4* __restrict__ st, int maxiter, double tol, double bnrm,
+                                             bool precond, int& iters, double& relres, bool& ok) {
+    __shared__ float s_ab[3];      // alpha, beta, relres
+    __shared__ int s_flag;         // 0 continue, 1 converged, 2 breakdown, 3 next coefficients broke down
+    const bool lead = (threadIdx.x == 0);
+    ok = true;
+    iters = 0;
+    auto Mi = [&](int k) -> float { return precond ? dinv[k] : 1.0f; };
+    // everything the iterations read besides the vectors is copied to registers
+    // here: the team, the grid and the operator live in local memory, and reads
+    // of them inside the loop would be repeated after every store (the stores
+    // could alias them) and would miss the L1, which each team barrier's
+    // acquire invalidates
+    const int tid = Tm.tid, nthr = Tm.nthr;
+    const Geo Gv = *A.G;
+    const OpK<float> Kv = A.K;
+    const float* __restrict__ cN = A.N;
+    const float* __restrict__ cNab = A.Nab;
+    const float* __restrict__ cdgx = A.dgx;
+    const float* __restrict__ cdgy = A.dgy;
+    const int n2 = Gv.n2, nx = Gv.nx;
+    const int nact = A.acell ? min(max(A.acell[n2], 0), n2) : n2;
+    auto pack = [&](int t) -> unsigned {
+        const int c = A.acell ? A.acell[t] : t;
+        const int j = c / nx, i = c - j * nx;
+        return cell_pack(i, j, A.row_kind(c), A.row_kind(n2 + c));
+    };
+    int* s_item = g_item_cache;
+    const int cache = (blockDim.x <= YG_ITEM_BLOCK) ? YG_ITEM_CACHE : 0;
+    {
+        int q = 0;
+        for (int t = tid; t < nact && q < cache; t += nthr, q++) s_item[q * blockDim.x + threadIdx.x] = (int)pack(t);
+    }
+    // x of the active rows back to the plain array, then a team barrier (the
+    // true-residual check and the caller read x at every row)
+    auto flush_x = [&]() -> bool {
+        int q = 0;
+        for (int t = tid; t < nact; t += nthr, q++) {
+            const unsigned pk = (q < cache) ? (unsigned)s_item[q * blockDim.x + threadIdx.x] : pack(t);
+            const int c = (int)(pk & 0x3fffu) + nx * (int)((pk >> 14) & 0x3fffu);
+            if (((pk >> 28) & 3u) != 1u) x[c] = st[2 * c + 1].x;
+            if ((pk >> 30) != 1u) x[n2 + c] = st[2 * (n2 + c) + 1].x;
+        }
+        return team_barrier(Tm);
+    };
+    int it = 0;
+    for (int restart = 0; restart < 8; restart++) {
+        // r = b - A x, u = M r (every row)
+        for (int k = Tm.tid; k < nu; k += Tm.nthr) {
+            const float rk = b[k] - A.row(k, x);
+            r[k] = rk;
+            u[k] = Mi(k) * rk;
+        }
+        if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
+        // w = A u, m = M w, the row records, partial dots
+        float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
+        for (int k = Tm.tid; k < nu; k += Tm.nthr) {
+            const float wk = A.row(k, u);
+            m0[k] = Mi(k) * wk;
+            m1[k] = 0.0f;
+            const float rk = r[k], uk = u[k];
+            st[2 * k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            st[2 * k + 1] = make_float4(x[k], rk, uk, wk);
+            a0 += rk * uk;
+            a1 += wk * uk;
+            a2 += rk * rk;
+        }
+        float red[3];
+        {
+            const float part[3] = {a0, a1, a2};
+            if (!(ok = team_allreduce_w<float>(Tm, part, red, 3))) return YGPU_ERR_TIMEOUT;
+        }
+        float gam_old = 1.0f, alpha_old = 1.0f;
+        if (lead) {
+            const float rel = sqrtf(red[2]) / (float)bnrm;
+            s_ab[2] = rel;
+            if (rel <= (float)tol) s_flag = 1;
+            else {
+                const float gam = red[0], del = red[1];
+                const float alpha = gam / del;
+                if (!isfinite(alpha) || del == 0.0f) s_flag = 2;
+                else {
+                    s_flag = 0;
+                    s_ab[0] = alpha;
+                    s_ab[1] = 0.0f;
+                    gam_old = gam;
+                    alpha_old = alpha;
+                }
+            }
+        }
+        __syncthreads();
+        if (s_flag == 1) { relres = (double)s_ab[2]; iters = it; return YGPU_OK; }
+        if (s_flag == 2) { relres = (double)s_ab[2]; iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
+        float* mc = m0;
+        float* mn = m1;
+        bool recheck = false;
+        int exit_st = YGPU_MAXITER;
+        while (it < maxiter) {
+            const float a = s_ab[0], bt = s_ab[1];
+            a0 = a1 = a2 = 0.0f;
+            // one row's update from its records, operator value nk and m, M
+            auto update = [&](int k, float4& A0, float4& A1, float nk, float mk, float mi) {
+                // A0 = (z, q, s, p), A1 = (x, r, u, w)
+                const float zk = nk + bt * A0.x;
+                const float qk = mk + bt * A0.y;
+                const float sk = A1.w + bt * A0.z;
+                const float pk = A1.z + bt * A0.w;
+                const float xk = A1.x + a * pk;
+                const float rk = A1.y - a * sk;
+                const float uk = A1.z - a * qk;
+                const float wk = A1.w - a * zk;
+                st[2 * k] = make_float4(zk, qk, sk, pk);
+                st[2 * k + 1] = make_float4(xk, rk, uk, wk);
+                mn[k] = mi * wk;
+                a0 += rk * uk;
+                a1 += wk * uk;
+                a2 += rk * rk;
+            };
+            const float* __restrict__ mcr = mc;
+            int q = 0;
+            for (int t = tid; t < nact; t += nthr, q++) {
+                const unsigned pk = (q < cache) ? (unsigned)s_item[q * blockDim.x + threadIdx.x] : pack(t);
+                const int i = (int)(pk & 0x3fffu), j = (int)((pk >> 14) & 0x3fffu);
+                const unsigned k0 = (pk >> 28) & 3u, k1 = pk >> 30;
+                const int c = i + nx * j, c1 = n2 + c;
+                if (k0 != 0u && k1 != 0u) continue;      // no interior-stencil row
+                float4 A0 = make_float4(0.f, 0.f, 0.f, 0.f), A1 = A0, B0 = A0, B1 = A0;
+                float m0v = 0.0f, m1v = 0.0f, i0 = 0.0f, i1 = 0.0f;
+                if (k0 == 0u) { A0 = st[2 * c]; A1 = st[2 * c + 1]; m0v = mcr[c]; i0 = Mi(c); }
+                if (k1 == 0u) { B0 = st[2 * c1]; B1 = st[2 * c1 + 1]; m1v = mcr[c1]; i1 = Mi(c1); }
+                float y0, y1;
+                energy_cell_fast<float, float>(Gv, Kv, cN, cNab, cdgx, cdgy, mcr, c, i, j, y0, y1);
+                if (k0 == 0u) update(c, A0, A1, y0, m0v, i0);
+                if (k1 == 0u) update(c1, B0, B1, y1, m1v, i1);
+            }
+            // rows outside the interior stencil in a second pass: the calls stay
+            // out of the main loop (whose live registers they would spill)
+            q = 0;
+            for (int t = tid; t < nact; t += nthr, q++) {
+                const unsigned pk = (q < cache) ? (unsigned)s_item[q * blockDim.x + threadIdx.x] : pack(t);
+                const unsigned k0 = (pk >> 28) & 3u, k1 = pk >> 30;
+                if (k0 != 2u && k1 != 2u) continue;
+                const int c = (int)(pk & 0x3fffu) + nx * (int)((pk >> 14) & 0x3fffu);
+#pragma unroll 1
+                for (int h = 0; h < 2; h++) {
+                    if (((h == 0) ? k0 : k1) != 2u) continue;
+                    const int k = c + h * n2;
+                    float4 R0 = st[2 * k], R1 = st[2 * k + 1];
+                    const float mk = mcr[k], mi = Mi(k);
+                    update(k, R0, R1, A.general(k, mc), mk, mi);
+                }
+            }
+            it++;
+            {
+                const float part[3] = {a0, a1, a2};
+                if (!(ok = team_allreduce_w<float>(Tm, part, red, 3))) return YGPU_ERR_TIMEOUT;
+            }
+            { float* tt = mc; mc = mn; mn = tt; }
+            if (lead) {
+                const float rel = sqrtf(red[2]) / (float)bnrm;
+                s_ab[2] = rel;
+                if (!isfinite(rel)) s_flag = 2;
+                else if (rel <= (float)tol) s_flag = 1;
+                else {
+                    const float gam = red[0], del = red[1];
+                    const float beta = gam / gam_old;
+                    const float alpha = gam / (del - beta * gam / alpha_old);
+                    if (!isfinite(alpha) || !isfinite(beta) || del == 0.0f) s_flag = 3;
+                    else {
+                        s_flag = 0;
+                        s_ab[0] = alpha;
+                        s_ab[1] = beta;
+                        gam_old = gam;
+                        alpha_old = alpha;
+                    }
+                }
+            }
+            __syncthreads();
+            // s_flag / s_ab are rewritten only after the next all-reduce's first
+            // __syncthreads, so every thread has read them by then
+            const int flag = s_flag;
+            if (flag == 2) { exit_st = YGPU_BREAKDOWN; break; }
+            if (flag == 1) { recheck = true; break; }
+            if (flag == 3) {
+                if (it < maxiter) exit_st = YGPU_BREAKDOWN;
+                break;
+            }
+        }
+        relres = (double)s_ab[2];
+        iters = it;
+        if (!(ok = flush_x())) return YGPU_ERR_TIMEOUT;
+        if (!recheck) return exit_st;
+        // true residual check
+        float tr = 0.0f;
+        for (int k = Tm.tid; k < nu; k += Tm.nthr) {
+            const float rk = b[k] - A.row(k, x);
+            tr += rk * rk;
+        }
+        {
+            float trs;
+            if (!(ok = team_allreduce_w<float>(Tm, &tr, &trs, 1))) return YGPU_ERR_TIMEOUT;
+            tr = trs;
+        }
+        relres = (double)(sqrtf(tr) / (float)bnrm);
         if (relres <= tol) return YGPU_OK;
         if (it >= maxiter) return YGPU_MAXITER;
     }
@@ -2423,6 +2741,9 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         if (use_cg && block)
             st = krylov_pcg_pipe_blk<float>(T, G, A32, I.fminv, I.fx, I.fr, I.frt, I.fv, I.ft, I.fph, I.fm2, I.fz,
                                             I.fq, I.fs, I.fp, inner_max, inner_tol, 1.0, it, rel_in, ok);
+        else if (use_cg && I.fst && G.nx <= (1 << 14) && G.ny <= (1 << 14))
+            st = krylov_pcg_cells(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.frt, I.fv, I.fph, I.fm2, I.fst, inner_max,
+                                  inner_tol, 1.0, pre, it, rel_in, ok);
         else if (use_cg)
             st = krylov_pcg_pipe<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.frt, I.fv, I.ft, I.fph, I.fm2, I.fz,
                                         I.fq, I.fs, I.fp, inner_max, inner_tol, 1.0, pre, it, rel_in, ok);
@@ -2686,7 +3007,8 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
         phase_column<double, double>(I, P, G, T, vcur, vnew, sdudx, sdudy, sdvdx, sdvdy, relax, diva, true, iter > 1);
     if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
     t2 = clk.lap();
-    phase_faces(I, P, G, T, diva);
+    if (mixed) phase_faces<float>(I, P, G, T, diva);
+    else phase_faces<double>(I, P, G, T, diva);
     if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
     t3 = clk.lap();
     phase_system(I, P, G, T, bn2);
