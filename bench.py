@@ -666,11 +666,15 @@ def main():
             steps_timing = gpu.step_timing_get()
             gpu.step_timing(False)
         vel = "ux_bar" if kind == abi.KIND_DIVA else "ux_b"
+        vel_y = "uy_bar" if kind == abi.KIND_DIVA else "uy_b"
         u_batch = [d[vel].cpu().numpy().reshape((i.nx, i.ny), order="F") for d, i in zip(devs, insts)]
+        v_batch = [d[vel_y].cpu().numpy().reshape((i.nx, i.ny), order="F") for d, i in zip(devs, insts)]
+        # the batch's first instance, every checked output (flat, Fortran order)
+        batch0 = {k: devs[0][k].cpu().numpy() for k in (vel, vel_y, "visc_eff", "beta_acx", "taub_acx")}
         tot_ms = max_over_ranks(sum(step_ms), dist, f"cuda:{local}")
         res[prec] = {"lat": lat, "st1": st1, "step_ms": step_ms, "tot_ms": tot_ms, "sts": sts,
-                     "u_single": u_single, "u_batch": u_batch, "all_sts": all_sts, "launches": launches,
-                     "steps_timing": steps_timing}
+                     "u_single": u_single, "u_batch": u_batch, "v_batch": v_batch, "batch0": batch0,
+                     "all_sts": all_sts, "launches": launches, "steps_timing": steps_timing}
 
     # e2e: the batched C-ABI entry on host buffers (the whole batch per step, the
     # host-device copies inside the timed region), and the single-solve drop-in
@@ -711,12 +715,18 @@ def main():
     K = len(mixed["step_ms"])
     value = replica_throughput(world, batch, K, mixed["tot_ms"])
     value64 = replica_throughput(world, batch, K, fp64["tot_ms"])
-    # error of the mixed batch against the FP64 batch, per instance
-    err_mixed_vs_fp64 = max(rel_l2(a, b) for a, b in zip(mixed["u_batch"], fp64["u_batch"]))
+    # error of the mixed batch against the FP64 batch: every instance, both velocity components
+    err_mixed_vs_fp64 = max(max(rel_l2(a, b) for a, b in zip(mixed["u_batch"], fp64["u_batch"])),
+                            max(rel_l2(a, b) for a, b in zip(mixed["v_batch"], fp64["v_batch"])))
     err_vs_oracle = None
     if tight is not None:
+        # against the oracle converged to 1e-10: the single solve's x velocity and
+        # every checked output of the batch's first instance, both precisions
         vel = "ux_bar" if kind == abi.KIND_DIVA else "ux_b"
         err_vs_oracle = {"mixed": rel_l2(mixed["u_single"], tight[vel]), "fp64": rel_l2(fp64["u_single"], tight[vel])}
+        for prec in ("mixed", "fp64"):
+            err_vs_oracle[prec + "_batch_instance0"] = {
+                k: rel_l2(v, np.ravel(tight[k], order="F")) for k, v in res[prec]["batch0"].items() if k in tight}
     # roofline of the dominant kernel (the Krylov step) over the timed batched
     # steps: algorithmic bytes of its launches / their CUDA-event time
     cg = insts[0].par.lis_opt.split("-i ")[1].split()[0] in ("cg", "minres")

@@ -516,11 +516,11 @@ typedef struct ygpu_tuning {
     int spin_log2;              /* for tests of the timeout path: a wait of a team of CTAs
                                    gives up after 2^spin_log2 polls (1..22) instead of 2^22
                                    (0, the default), and the solve returns YGPU_ERR_TIMEOUT */
-    int cluster_ctas;           /* Krylov step on thread-block clusters (one team = one
-                                   cluster, barriers and all-reduces in the cluster):
-                                   0 (default) when every instance of the solve gets its own
-                                   resident cluster, with the largest such size up to 16;
-                                   2..16 asks for that size; -1 keeps global teams        */
+    int cluster_ctas;           /* 2..16: the Krylov step on thread-block clusters of this
+                                   many CTAs (one team = one cluster, the barrier and the
+                                   all-reduce inside the cluster); 0 (default) or -1: teams
+                                   of CTAs with a global-memory barrier, which measured
+                                   faster on the marine DIVA workloads                     */
 } ygpu_tuning;
 void ygpu_tuning_defaults(ygpu_tuning* t);
 int  ygpu_ctx_set_tuning(ygpu_ctx* ctx, const ygpu_tuning* t);

@@ -91,3 +91,27 @@ def test_tuning_rejects_out_of_range():
             solver.set_tuning(unknowns_per_cta=1)
     finally:
         solver.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cluster_teams_equal_global_teams(precision):
+    """The Krylov step on thread-block clusters (cluster barrier, all-reduce in
+    distributed shared memory; opt-in through ygpu_tuning.cluster_ctas) gives the
+    solution of the default global-memory teams."""
+    torch = pytest.importorskip("torch")
+    insts = _instances(5)
+    par = insts[0].par.with_(precision=precision)
+    out = {}
+    for cl in (0, 4):
+        solver = gpu.DeviceSolver(0)
+        try:
+            solver.set_tuning(unknowns_per_cta=512, cluster_ctas=cl)
+            devs, fields = zip(*[_device(inst) for inst in insts])
+            torch.cuda.synchronize()
+            sts = solver.solve_batch(abi.KIND_SSA, par, list(fields))
+            assert all(st["status"] == 0 for st in sts), [st["status"] for st in sts]
+            out[cl] = [d["ux_b"].cpu().numpy() for d in devs]
+        finally:
+            solver.close()
+    for a, b in zip(out[0], out[4]):
+        assert rel_l2(b, a) <= 1e-6

@@ -179,7 +179,7 @@ struct ygpu_ctx {
     int unknowns_per_cta = 0;       // team size: unknowns per CTA (0: 2 x block)
     size_t max_active_unknowns = 1500000;   // batches beyond this run as a queue (continuous batching)
     int spin_log2 = 0;              // team waits give up after 2^spin_log2 polls (0: the default 2^22)
-    int cluster_ctas = 0;           // Krylov cluster teams: 0 chosen, k CTAs, -1 off
+    int cluster_ctas = 0;           // Krylov cluster teams of this many CTAs (2..16; else off)
     int* h_flags = nullptr;         // pinned: finished count, abort flag
     int* d_misc = nullptr;          // [0] queue, [1] abort, [2..3] csr out
     double* d_miscd = nullptr;

@@ -160,6 +160,7 @@ struct Inst {
 // Team of CTAs: barrier and fused all-reduce (bounded waits)
 // ---------------------------------------------------------------------------
 #define YG_MAX_TEAM_CTAS 1024
+#define YG_REC_MAX_CTAS 16         // teams up to this size poll the FP32 all-reduce records
 #define YG_RED_MAX 4
 
 // Team barrier: every CTA adds 1 to `count` with a release reduction and
@@ -172,12 +173,18 @@ struct __align__(16) TeamCtl {
     unsigned int base;
     int abort;
     int inst;                      // instance the team works on (work queue)
+    unsigned int abase;            // generation of the last FP32 all-reduce of a launch (CTA 0
+                                   // stores it at the end, every CTA reads it at the start)
     unsigned char spin_log2;       // 0: waits give up after YG_SPIN_LIMIT polls; k: after 2^k
     union __align__(16) {          // per-CTA totals of the all-reduces, by parity; the
                                    // YG_RED_MAX totals of a CTA are one 16/32-byte record
         double slots[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
         float fslots[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
     };
+    // FP32 all-reduce records: per CTA YG_RED_MAX words (generation << 32 | FP32
+    // bits), by parity; a word is read and written whole, so a reader that sees
+    // the current generation in every word of a record has that CTA's totals
+    unsigned long long rec[2][YG_MAX_TEAM_CTAS][YG_RED_MAX];
 };
 template <typename V>
 YG_DEV V* team_slot(TeamCtl* c, int parity, int cta, int k);
@@ -205,10 +212,22 @@ struct Team {
     unsigned long long sync_ns;    // time thread 0 of the CTA spent in team all-reduces (ns; an
                                    // integer, so that the count adds nothing to the FP64 pipe)
     unsigned gen;                  // thread 0: count target of the last team barrier
+    unsigned agen;                 // every thread: generation of the last FP32 all-reduce
     unsigned spin_lim;             // thread 0: polls after which a wait gives up
     bool cl;                       // the team is one thread-block cluster: barriers are the
                                    // hardware cluster barrier, all-reduces go through
                                    // distributed shared memory (no global control block)
+};
+
+// A register copy of the team for the body of a noinline solver. The caller's
+// Team lives in its stack frame (local memory); the team barriers and
+// all-reduces read and update its fields on every call from every thread, so
+// the loops work on this copy, which is written back when the function returns.
+struct TeamLocal {
+    Team& ref;
+    Team t;
+    YG_DEV explicit TeamLocal(Team& r) : ref(r), t(r) {}
+    YG_DEV ~TeamLocal() { ref = t; }
 };
 
 YG_DEV unsigned ld_acquire_u32(const unsigned int* p) {
@@ -352,6 +371,85 @@ YG_DEV bool team_allreduce_impl(Team& T, const V* in, V* out, int nv) {
         // no closing barrier: s_tot and s_red are next written after the next
         // call's first __syncthreads, which every thread passes after these reads
         return true;
+    }
+    if constexpr (sizeof(V) == sizeof(float)) {
+        if (T.ncta > 1 && T.ncta <= YG_REC_MAX_CTAS) {
+            // FP32 sums of a small global team: each CTA publishes its totals as words
+            // carrying the all-reduce's generation (release pattern: fence, then
+            // relaxed stores); warp 0 of every CTA polls the records themselves
+            // until every word shows the generation (acquire pattern: relaxed
+            // loads, then a fence). One L2 round trip after the last CTA's
+            // record lands, where a counter barrier followed by reads of the
+            // totals takes three. Larger teams use the counter barrier: with
+            // every CTA polling every record, the few L2 lines holding them
+            // become the bottleneck.
+            __shared__ int s_rok;
+            const unsigned g = ++T.agen;
+            if (wid == 0) {
+                V t[YG_RED_MAX];
+                cta_totals(t);
+                if (lane == 0) {
+                    unsigned long long w[YG_RED_MAX];
+#pragma unroll
+                    for (int k = 0; k < YG_RED_MAX; k++)
+                        w[k] = ((unsigned long long)g << 32) | (unsigned long long)__float_as_uint((float)t[k]);
+                    unsigned long long* r = &T.ctl->rec[T.parity][T.cta][0];
+                    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+                    asm volatile("st.relaxed.gpu.global.v2.b64 [%0], {%1, %2};" ::"l"(r), "l"(w[0]), "l"(w[1]) : "memory");
+                    asm volatile("st.relaxed.gpu.global.v2.b64 [%0], {%1, %2};" ::"l"(r + 2), "l"(w[2]), "l"(w[3]) : "memory");
+                }
+                V a[YG_RED_MAX];
+#pragma unroll
+                for (int k = 0; k < YG_RED_MAX; k++) a[k] = V(0);
+                int ok = 1;
+                unsigned n = 0;
+                for (int c0 = 0; c0 < T.ncta && ok; c0 += 32) {
+                    const int c = c0 + lane;
+                    bool have = (c >= T.ncta);
+                    unsigned long long w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+                    const unsigned long long* r = &T.ctl->rec[T.parity][c < T.ncta ? c : 0][0];
+                    while (true) {
+                        if (!have) {
+                            asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];" : "=l"(w0), "=l"(w1) : "l"(r) : "memory");
+                            asm volatile("ld.relaxed.gpu.global.v2.b64 {%0, %1}, [%2];" : "=l"(w2), "=l"(w3) : "l"(r + 2) : "memory");
+                            have = (unsigned)(w0 >> 32) == g && (unsigned)(w1 >> 32) == g && (unsigned)(w2 >> 32) == g &&
+                                   (unsigned)(w3 >> 32) == g;
+                        }
+                        if (__all_sync(0xffffffffu, have)) break;
+                        ++n;
+                        if ((n & 1023u) == 0u || n >= T.spin_lim) {
+                            int ab = ld_acquire_s32(T.abort_all);
+                            if (!ab && n >= T.spin_lim && lane == 0) {
+                                atomicExch(T.abort_all, 1);
+                                atomicExch(&T.ctl->abort, 1);
+                            }
+                            ab = __shfl_sync(0xffffffffu, ab, 0);
+                            if (ab || n >= T.spin_lim) { ok = 0; break; }
+                        }
+                    }
+                    if (ok && c < T.ncta) {
+                        a[0] += __uint_as_float((unsigned)w0);
+                        a[1] += __uint_as_float((unsigned)w1);
+                        a[2] += __uint_as_float((unsigned)w2);
+                        a[3] += __uint_as_float((unsigned)w3);
+                    }
+                }
+                asm volatile("fence.acq_rel.gpu;" ::: "memory");
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                    for (int k = 0; k < YG_RED_MAX; k++) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+                if (lane == 0) {
+#pragma unroll
+                    for (int k = 0; k < YG_RED_MAX; k++) s_tot[k] = a[k];
+                    s_rok = ok;
+                }
+            }
+            T.parity ^= 1;
+            __syncthreads();
+            for (int k = 0; k < nv; k++) out[k] = s_tot[k];
+            return s_rok != 0;
+        }
     }
     if (wid == 0) {
         V t[YG_RED_MAX];

@@ -32,11 +32,10 @@ struct StepShape {
     int kcl = 0;                   // > 0: the Krylov teams are thread-block clusters of kcl CTAs
                                    // (kgrid = clusters x kcl), see ygpu_krylov_cluster_plan
 };
-// Cluster size and count for the Krylov step of n_inst instances of at most
-// max_nu unknowns: the largest cluster size (at most 16 CTAs, at least one CTA
-// per 1024 unknowns of the largest instance) with one resident cluster per
-// instance. req > 0 asks for that size, req < 0 for none. Returns the size
-// (0: no cluster plan fits, use the global teams) and the cluster count.
+// Cluster size and count for the Krylov step of n_inst instances: req CTAs per
+// cluster (2..16; anything else: no clusters), one instance per resident cluster
+// or the instances round-robin over the resident clusters. Returns the size (0:
+// use the global teams) and the cluster count.
 int ygpu_krylov_cluster_plan(int device, int n_inst, size_t max_nu, int req, int* n_clusters);
 int ygpu_init_constants(int device);
 void ygpu_count_launches(unsigned long long n);

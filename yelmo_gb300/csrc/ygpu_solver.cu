@@ -1666,8 +1666,10 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
 // ---------------------------------------------------------------------------
 // CG with Jacobi (x updated in place). Returns LIS status; iters/relres out.
 template <typename T, typename Op, typename CT>
-__device__ __noinline__ int krylov_cg(Team& Tm, int nu, const Op& A, const CT* dinv, T* x, const T* b, T* r, T* p, T* q, T* z,
+__device__ __noinline__ int krylov_cg(Team& Tm_, int nu, const Op& A, const CT* dinv, T* x, const T* b, T* r, T* p, T* q, T* z,
                      int maxiter, double tol, double bnrm, bool precond, int& iters, double& relres, bool& ok) {
+    TeamLocal tl_(Tm_);
+    Team& Tm = tl_.t;
     ok = true;
     iters = 0;
     // r = b - A x
@@ -1725,12 +1727,14 @@ __device__ __noinline__ int krylov_cg(Team& Tm, int nu, const Op& A, const CT* d
 // the true residual.
 
 template <typename T, typename Op, typename CT>
-__device__ __noinline__ int krylov_pcg_pipe(Team& Tm, int nu, const Op& A, const CT* __restrict__ dinv,
+__device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, const CT* __restrict__ dinv,
                                             T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
                                             T* __restrict__ u, T* __restrict__ w, T* m0, T* m1, T* __restrict__ z,
                                             T* __restrict__ q, T* __restrict__ s, T* __restrict__ p, int maxiter,
                                             double tol, double bnrm, bool precond, int& iters, double& relres,
                                             bool& ok) {
+    TeamLocal tl_(Tm_);
+    Team& Tm = tl_.t;
     // Scalar recurrences run on one thread per CTA and are broadcast through
     // shared memory: FP64 division and square root are slow on this part, and
     // every thread of the team would otherwise repeat them.
@@ -1947,11 +1951,13 @@ YG_DEV unsigned cell_pack(int i, int j, unsigned k0, unsigned k1) {
     return (unsigned)i | ((unsigned)j << 14) | (k0 << 28) | (k1 << 30);
 }
 template <typename Op>
-__device__ __noinline__ int krylov_pcg_cells(Team& Tm, int nu, const Op& A, const float* __restrict__ dinv,
+__device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, const float* __restrict__ dinv,
                                              float* __restrict__ x, const float* __restrict__ b,
                                              float* __restrict__ r, float* __restrict__ u, float* m0, float* m1,
                                              float4* __restrict__ st, int maxiter, double tol, double bnrm,
                                              bool precond, int& iters, double& relres, bool& ok) {
+    TeamLocal tl_(Tm_);
+    Team& Tm = tl_.t;
     __shared__ float s_ab[3];      // alpha, beta, relres
     __shared__ int s_flag;         // 0 continue, 1 converged, 2 breakdown, 3 next coefficients broke down
     const bool lead = (threadIdx.x == 0);
@@ -2167,11 +2173,13 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm, int nu, const Op& A, cons
 // and p are zero there, and p_hat and s_hat (the operator inputs, read at
 // neighbouring columns) are cleared on every row at the start.
 template <typename T, typename Op, typename CT>
-__device__ __noinline__ int krylov_bicgstab(Team& Tm, int nu, const Op& A, const CT* __restrict__ dinv,
+__device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, const CT* __restrict__ dinv,
                                             T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
                                             T* __restrict__ rt, T* __restrict__ p, T* v, T* __restrict__ s, T* t,
                                             T* ph, T* sh, int maxiter, double tol, double bnrm, bool precond,
                                             int& iters, double& relres, bool& ok) {
+    TeamLocal tl_(Tm_);
+    Team& Tm = tl_.t;
     // sums and scalars in T (an FP32 inner solve stays off the FP64 pipe)
     __shared__ T s_sc[4];          // alpha, omega, beta, relres
     __shared__ int s_flag;         // 0 continue, 1 converged, 2 breakdown
@@ -2517,11 +2525,13 @@ YG_DEV T block_apply_lane(const MT* M, T w, int lane) {
 // preconditioner is applied to a tile's freshly computed vector through warp
 // shuffles in the same pass.
 template <typename T, typename Op>
-__device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm, const Geo& G, const Op& A, const float* __restrict__ minv,
+__device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm_, const Geo& G, const Op& A, const float* __restrict__ minv,
                                                 T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
                                                 T* __restrict__ u, T* __restrict__ w, T* m0, T* m1, T* __restrict__ z,
                                                 T* __restrict__ q, T* __restrict__ s, T* __restrict__ p, int maxiter,
                                                 double tol, double bnrm, int& iters, double& relres, bool& ok) {
+    TeamLocal tl_(Tm_);
+    Team& Tm = tl_.t;
     __shared__ T s_ab[3];          // alpha, beta, relres (in T, as in krylov_pcg_pipe)
     __shared__ int s_flag;
     const bool lead = (threadIdx.x == 0);
@@ -3231,7 +3241,8 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
     T.abort_all = abort_all;
     T.sync_ns = 0ull;
     T.gen = (threadIdx.x == 0) ? ld_acquire_u32(&T.ctl->base) : 0u;
-    T.spin_lim = (threadIdx.x == 0) ? team_spin_limit(T.ctl) : 0u;
+    T.agen = ld_acquire_u32(&T.ctl->abase);
+    T.spin_lim = team_spin_limit(T.ctl);
     T.cl = false;
     for (int q = team; q < n_inst; q += n_teams) {
         if (threadIdx.x == 0) {
@@ -3250,7 +3261,10 @@ YG_DEV void run_step(const Inst* insts, int n_inst, const ygpu_dyn_par& P, TeamC
         }
         __syncthreads();
     }
-    if (T.cta == 0 && threadIdx.x == 0) T.ctl->base = T.gen;
+    if (T.cta == 0 && threadIdx.x == 0) {
+        T.ctl->base = T.gen;
+        T.ctl->abase = T.agen;
+    }
 }
 
 #define YG_KBLOCK 512
@@ -3302,6 +3316,7 @@ __global__ void __launch_bounds__(YG_KBLOCK, 1) ygpu_k_krylov_cl(const Inst* ins
     T.abort_all = ab;
     T.sync_ns = 0ull;
     T.gen = 0u;
+    T.agen = 0u;
     T.spin_lim = YG_SPIN_LIMIT;
     T.cl = true;
     if (threadIdx.x == 0) s_flags[0] = ld_acquire_s32(ab);
@@ -3363,6 +3378,7 @@ __global__ void __launch_bounds__(YG_BLOCK) ygpu_csr_kernel(CsrJob J, TeamCtl* c
     T.abort_all = abort_all;
     T.sync_ns = 0ull;
     T.gen = 0u;
+    T.agen = 0u;
     T.spin_lim = YG_SPIN_LIMIT;
     T.cl = false;
     const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
@@ -3552,6 +3568,7 @@ __global__ void __launch_bounds__(YG_BLOCK) ygpu_adv_kernel(AdvJob J, TeamCtl* c
     T.abort_all = abort_all;
     T.sync_ns = 0ull;
     T.gen = 0u;
+    T.agen = 0u;
     T.spin_lim = YG_SPIN_LIMIT;
     T.cl = false;
     const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
@@ -3910,7 +3927,7 @@ static int launch_cluster_krylov(cudaStream_t s, const StepShape& sh, const Inst
 
 int ygpu_krylov_cluster_plan(int device, int n_inst, size_t max_nu, int req, int* n_clusters) {
     *n_clusters = 0;
-    if (req < 0 || n_inst < 1 || device < 0 || device >= 64) return 0;
+    if (req < 2 || n_inst < 1 || device < 0 || device >= 64) return 0;
     static std::mutex mu;
     static int maxc[64][17];       // resident clusters per size (-1: not resident / not queried)
     static bool init[64];
@@ -3937,18 +3954,12 @@ int ygpu_krylov_cluster_plan(int device, int n_inst, size_t max_nu, int req, int
             init[device] = true;
         }
     }
-    int cap = (int)((max_nu + 1023) / 1024);
-    if (cap > 16) cap = 16;
-    if (cap < 2) cap = 2;
-    for (int cs = (req > 0 ? (req > 16 ? 16 : req) : cap); cs >= 2; cs--) {
-        const int m = maxc[device][cs];
-        if (m >= n_inst || (req > 0 && m >= 1)) {
-            *n_clusters = (m < n_inst) ? m : n_inst;
-            return cs;
-        }
-        if (req > 0) break;
-    }
-    return 0;
+    (void)max_nu;
+    const int cs = req > 16 ? 16 : req;
+    const int m = maxc[device][cs];
+    if (m < 1) return 0;
+    *n_clusters = (m < n_inst) ? m : n_inst;
+    return cs;
 }
 
 static int launch_step_raw(int step, cudaStream_t s, const StepShape& sh, const Inst* d_insts, int n_inst,

@@ -447,7 +447,7 @@ class DeviceSolver:
                    max_active_unknowns: int = 1_500_000, spin_log2: int = 0, cluster_ctas: int = 0):
         """ygpu_ctx_set_tuning: host-check interval, chunk graphs, team size, queue threshold;
         spin_log2 > 0 lowers the team waits' spin budget to 2^spin_log2 polls (tests);
-        cluster_ctas: Krylov teams as thread-block clusters (0 chosen, 2..16, -1 off)."""
+        cluster_ctas: Krylov teams as thread-block clusters of 2..16 CTAs (0 or -1: global teams)."""
         t = abi.Tuning(check_every, 1 if use_graphs else 0, unknowns_per_cta, max_active_unknowns, spin_log2,
                        cluster_ctas)
         _check(self.L.ygpu_ctx_set_tuning(self.ctx, C.byref(t)))
