@@ -62,6 +62,10 @@ def make_instances(workload: str, batch: int):
         raise SystemExit(f"unknown workload {workload}")
     for inst in insts:
         inst.par = inst.par.with_(**BENCH_TOL)
+        if workload == "dome_ssa":
+            # the plain SSA solve keeps its configured preconditioner: BiCGSTAB with ILU(0)
+            inst.par = inst.par.with_(ssa_lis_opt_residual="-i bicgstab -p ilu -maxiter 5000 -tol 1.0e-9 "
+                                                           "-initx_zeros false")
         if workload == "continent_diva":
             # power-law friction with q = 1/3 settles into a Picard 2-cycle at the
             # beta_min floor, so this workload runs the namelist's own Picard

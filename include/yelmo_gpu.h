@@ -68,8 +68,11 @@ extern "C" {
 #define YGPU_LIN_MINRES       2
 #define YGPU_PRE_NONE         0
 #define YGPU_PRE_JACOBI       1
-#define YGPU_PRE_ILU0         2   /* requested "-p ilu"; what runs for it on the GPU is reported
-                                     in ygpu_stats.lin_precond_run                            */
+#define YGPU_PRE_ILU0         2   /* "-p ilu". With BiCGSTAB on the residual form the GPU runs
+                                     ILU(0) of the operator in a six-colour ordering (cell
+                                     colour (i - j) mod 3, then the component), which needs
+                                     periodic directions in multiples of 3 cells (else Jacobi);
+                                     the other forms run what ygpu_stats.lin_precond_run says  */
 #define YGPU_PRE_TILE_BLOCK   3   /* run only (never parsed): block Jacobi with the exact inverse
                                      of each 4x4-cell tile block (32 unknowns, inverted in FP32),
                                      what "-p ilu" runs for CG on the energy form             */
@@ -145,7 +148,8 @@ typedef struct ygpu_stats {
 } ygpu_stats;
 
 /* The Krylov method and preconditioner the GPU runs for a parameter set (the
-   values ygpu_stats.lin_solver_run / lin_precond_run report). */
+   values ygpu_stats.lin_solver_run / lin_precond_run report; a solve on a
+   periodic grid that the ILU(0) colouring does not fit reports Jacobi). */
 void ygpu_lin_method_run(const ygpu_dyn_par* par, int* lin_solver_run, int* lin_precond_run);
 
 /* ---- parameter helpers -------------------------------------------------- */

@@ -94,6 +94,7 @@ def test_struct_builders_reject_misshaped_arrays():
     ("energy", "-i cg -p ilu", (abi.LIN_CG, abi.PRE_TILE_BLOCK)),
     ("energy", "-i minres -p jacobi", (abi.LIN_CG, abi.PRE_JACOBI)),
     ("energy", "-i bicgstab -p ilu", (abi.LIN_BICGSTAB, abi.PRE_JACOBI)),
+    ("residual", "-i bicgstab -p ilu", (abi.LIN_BICGSTAB, abi.PRE_ILU0)),
     ("residual", "-i minres -p jacobi", (abi.LIN_BICGSTAB, abi.PRE_JACOBI)),
     ("residual", "-i cg -p none", (abi.LIN_BICGSTAB, abi.PRE_NONE)),
 ])

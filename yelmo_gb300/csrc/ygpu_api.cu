@@ -291,16 +291,26 @@ bool ygpu_neff_hook_is_set() { return t_hook != nullptr; }
 
 // The method and preconditioner linear_solve (ygpu_solver.cu) runs for a
 // parameter set: CG on the energy form unless BiCGSTAB is asked for, BiCGSTAB
-// on the residual form; "-p ilu" is the tile block preconditioner with CG on
-// the energy form and Jacobi otherwise.
-extern "C" void ygpu_lin_method_run(const ygpu_dyn_par* p, int* solver, int* precond) {
+// on the residual form; "-p ilu" is ILU(0) (six-colour ordering) with BiCGSTAB
+// on the residual form, the tile block preconditioner with CG on the energy
+// form, and Jacobi with BiCGSTAB on the energy form. nx, ny > 0: the grid of the
+// solve, whose periodic directions the ILU(0) colouring needs in multiples of 3
+// (Jacobi otherwise).
+void ygpu_lin_method_run_grid(const ygpu_dyn_par* p, int nx, int ny, int* solver, int* precond) {
     if (!p) return;
     const bool energy = (p->ssa_solver == YGPU_SSA_ENERGY);
     const bool cg = energy && p->lin_solver != YGPU_LIN_BICGSTAB;
     int pc = p->lin_precond;
-    if (pc == YGPU_PRE_ILU0) pc = cg ? YGPU_PRE_TILE_BLOCK : YGPU_PRE_JACOBI;
+    if (pc == YGPU_PRE_ILU0) {
+        if (cg) pc = YGPU_PRE_TILE_BLOCK;
+        else if (energy) pc = YGPU_PRE_JACOBI;
+        else if (nx > 0 && ny > 0 && !ygpu_ilu_colourable(nx, ny, p->boundaries)) pc = YGPU_PRE_JACOBI;
+    }
     if (solver) *solver = cg ? YGPU_LIN_CG : YGPU_LIN_BICGSTAB;
     if (precond) *precond = pc;
+}
+extern "C" void ygpu_lin_method_run(const ygpu_dyn_par* p, int* solver, int* precond) {
+    ygpu_lin_method_run_grid(p, 0, 0, solver, precond);
 }
 
 // default context of the calling thread (host-pointer entry points)
@@ -324,7 +334,7 @@ static size_t al(size_t b) { return ygpu_align256(b); }
 
 static size_t tile_blocks(int nx, int ny) { return (size_t)((nx + 3) / 4) * ((ny + 3) / 4); }
 
-size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block) {
+size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block, bool ilu) {
     size_t n2 = (size_t)nx * ny, nu = 2 * n2, n3 = n2 * nz;
     size_t b = al(n3 * 8);               // visc_alt
     b += al(4 * n3 * 8) + al(n3 * 8);    // attp, lvis
@@ -335,10 +345,11 @@ size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block) {
     b += al(n2);                         // cell flags
     if (mixed) b += 4 * al(n2 * 4) + 13 * al(nu * 4) + al(8 * nu * 4);   // + CG row records
     if (block) b += al(tile_blocks(nx, ny) * 1024 * 4);
+    if (ilu) b += al(YG_ILU_W * nu * 4) + al(YG_ILU_W * nu * (mixed ? 4 : 8)) + al(nu * (mixed ? 4 : 8));
     return b;
 }
 
-void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed, bool block) {
+void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed, bool block, bool ilu) {
     size_t n2 = (size_t)nx * ny, nu = 2 * n2, n3 = n2 * nz;
     char* p = base;
     auto D = [&](size_t n) { double* r = (double*)p; p += al(n * 8); return r; };
@@ -370,6 +381,16 @@ void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool m
         I.fx = I.fr = I.fp = I.fq = I.fz = I.frt = I.fv = I.fs = I.ft = I.fph = I.fsh = I.fm2 = nullptr;
     }
     I.fminv = block ? Fv(tile_blocks(nx, ny) * 1024) : nullptr;
+    I.icol = ilu ? Iv(YG_ILU_W * nu) : nullptr;
+    I.ilu = I.ipiv = nullptr;
+    I.filu = I.fipiv = nullptr;
+    if (ilu && mixed) {
+        I.filu = Fv(YG_ILU_W * nu);
+        I.fipiv = Fv(nu);
+    } else if (ilu) {
+        I.ilu = D(YG_ILU_W * nu);
+        I.ipiv = D(nu);
+    }
 }
 
 int ygpu_fields_check(int kind, const ygpu_fields* f) {
@@ -499,7 +520,8 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     size_t total = 0, max_nu = 0;
     for (int k = 0; k < n; k++) {
         off[k] = total;
-        total += al(ygpu_inst_scratch_bytes(inst[k].nx, inst[k].ny, inst[k].nz, mixed, ygpu_wants_block(*par)));
+        total += al(ygpu_inst_scratch_bytes(inst[k].nx, inst[k].ny, inst[k].nz, mixed, ygpu_wants_block(*par),
+                                              ygpu_wants_ilu(*par)));
         max_nu = std::max(max_nu, (size_t)2 * inst[k].nx * inst[k].ny);
     }
     if ((st = grow(&c->arena, &c->arena_cap, total))) return st;
@@ -548,7 +570,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
         Inst& I = c->h_insts[q];
         ygpu_fill_inst(I, kind, &inst[k]);
         ygpu_inst_scratch_carve(I, c->arena + off[k], inst[k].nx, inst[k].ny, inst[k].nz, mixed,
-                                ygpu_wants_block(*par));
+                                ygpu_wants_block(*par), ygpu_wants_ilu(*par));
         I.out = c->d_out + k;      // outputs stay in caller order
     }
     CK(cudaMemcpyAsync(c->d_insts, c->h_insts.data(), sizeof(Inst) * (size_t)n, cudaMemcpyHostToDevice, c->stream));
@@ -602,7 +624,7 @@ static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
             S.ssa_resid = o.resid;
             S.lin_resid = o.lin_resid;
             S.outer_iter = o.outer_iter; S.active_cells = o.n_active;
-            ygpu_lin_method_run(par, &S.lin_solver_run, &S.lin_precond_run);
+            ygpu_lin_method_run_grid(par, inst[k].nx, inst[k].ny, &S.lin_solver_run, &S.lin_precond_run);
             S.status = s_k;
             S.device_ms = ms;
             for (int q = 0; q < 10; q++) S.phase_ms[q] = o.phase_ns[q] * 1e-6;
@@ -629,6 +651,7 @@ static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
                        ygpu_stats* stats) {
     const bool mixed = (par->precision == YGPU_PREC_MIXED);
     const bool block = ygpu_wants_block(*par);
+    const bool ilu = ygpu_wants_ilu(*par);
     const size_t U = c->max_active_unknowns;
     std::vector<int> order(n);
     for (int k = 0; k < n; k++) order[k] = k;
@@ -639,7 +662,7 @@ static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
     // slots: enough for the smallest instances to fill U, each sized for the largest
     size_t nu_min = nu_of(order[n - 1]), slot_bytes = 0;
     for (int k = 0; k < n; k++)
-        slot_bytes = std::max(slot_bytes, al(ygpu_inst_scratch_bytes(inst[k].nx, inst[k].ny, inst[k].nz, mixed, block)));
+        slot_bytes = std::max(slot_bytes, al(ygpu_inst_scratch_bytes(inst[k].nx, inst[k].ny, inst[k].nz, mixed, block, ilu)));
     int n_slots = (int)std::min<size_t>((size_t)n, std::max<size_t>(1, U / std::max<size_t>(nu_min, 1) + 1));
     n_slots = std::min(n_slots, c->max_ctas > 0 ? c->max_ctas : 1);
     int st;
@@ -719,7 +742,7 @@ static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
             Inst I;
             ygpu_fill_inst(I, kind, &inst[k]);
             ygpu_inst_scratch_carve(I, c->arena + slot_bytes * (size_t)s, inst[k].nx, inst[k].ny, inst[k].nz, mixed,
-                                    block);
+                                    block, ilu);
             I.out = d_out + k;
             h_new.push_back(I);
             adm.push_back(k);
@@ -745,7 +768,7 @@ static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
                 Inst I;
                 ygpu_fill_inst(I, kind, &inst[k]);
                 ygpu_inst_scratch_carve(I, c->arena + slot_bytes * (size_t)slot_of[k], inst[k].nx, inst[k].ny,
-                                        inst[k].nz, mixed, block);
+                                        inst[k].nz, mixed, block, ilu);
                 I.out = d_out + k;
                 h_active.push_back(I);
             }
@@ -783,7 +806,7 @@ static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
                 Inst I;
                 ygpu_fill_inst(I, kind, &inst[k]);
                 ygpu_inst_scratch_carve(I, c->arena + slot_bytes * (size_t)slot_of[k], inst[k].nx, inst[k].ny,
-                                        inst[k].nz, mixed, block);
+                                        inst[k].nz, mixed, block, ilu);
                 I.out = d_out + k;
                 h_active.push_back(I);
             }
@@ -810,7 +833,7 @@ static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
             S.ssa_resid = o.resid;
             S.lin_resid = o.lin_resid;
             S.outer_iter = o.outer_iter; S.active_cells = o.n_active;
-            ygpu_lin_method_run(par, &S.lin_solver_run, &S.lin_precond_run);
+            ygpu_lin_method_run_grid(par, inst[k].nx, inst[k].ny, &S.lin_solver_run, &S.lin_precond_run);
             S.status = s_k;
             S.device_ms = ms;
             for (int q = 0; q < 10; q++) S.phase_ms[q] = o.phase_ns[q] * 1e-6;

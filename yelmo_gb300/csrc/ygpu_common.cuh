@@ -152,9 +152,18 @@ struct Inst {
     float* fminv;                  // mixed, block preconditioner: inverse of each 4x4-cell tile block (32x32)
     float *fx, *fr, *fp, *fq, *fz, *frt, *fv, *fs, *ft, *fph, *fsh, *fm2;
     float4* fst;                   // mixed CG: per unknown the records (z, q, s, p), (x, r, u, w)
+    // -p ilu on the residual form: ILU(0) factors in a six-colour ordering, per
+    // unknown YG_ILU_W slots of packed columns (column | colour group << 28, -1
+    // unused), the factor values in slot order and the inverse pivot; FP64 for
+    // the FP64 solve, FP32 for the mixed inner solves
+    int* icol;
+    double *ilu, *ipiv;
+    float *filu, *fipiv;
     InstOut* out;
     int visc_final_in_alt;         // set by the kernel: final visc is in visc_alt
 };
+
+#define YG_ILU_W 9                 // slots of an ILU(0) row of the residual form
 
 // ---------------------------------------------------------------------------
 // Team of CTAs: barrier and fused all-reduce (bounded waits)

@@ -131,10 +131,25 @@ bool ygpu_neff_hook_is_set();
 int ygpu_fields_check(int kind, const ygpu_fields* f);
 void ygpu_fill_inst(Inst& I, int kind, const ygpu_fields* f);
 // block: scratch for the tile-block preconditioner (mixed mode, -p ilu)
-size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block = false);
-void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed, bool block = false);
+// ilu: scratch for the ILU(0) factors of the residual form (-p ilu)
+size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block = false, bool ilu = false);
+void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool mixed, bool block = false,
+                             bool ilu = false);
 inline bool ygpu_wants_block(const ygpu_dyn_par& p) {
     return p.lin_precond == YGPU_PRE_ILU0 && p.ssa_solver == YGPU_SSA_ENERGY && p.lin_solver != YGPU_LIN_BICGSTAB;
+}
+// lin_solver_run / lin_precond_run of a solve on an nx x ny grid (0: unknown)
+void ygpu_lin_method_run_grid(const ygpu_dyn_par* p, int nx, int ny, int* solver, int* precond);
+inline bool ygpu_wants_ilu(const ygpu_dyn_par& p) {
+    return p.lin_precond == YGPU_PRE_ILU0 && p.ssa_solver != YGPU_SSA_ENERGY;
+}
+// the six-colour ordering of the ILU(0) leaves no two coupled unknowns in one
+// colour unless a periodic direction has a length that is not a multiple of 3
+inline bool ygpu_ilu_colourable(int nx, int ny, int bc) {
+    const bool px = (bc == YGPU_BND_PERIODIC || bc == YGPU_BND_PERIODIC_X);
+    const bool py = (bc == YGPU_BND_PERIODIC || bc == YGPU_BND_PERIODIC_Y || bc == YGPU_BND_MISMIP3D ||
+                     bc == YGPU_BND_TROUGH);
+    return !(px && nx % 3 != 0) && !(py && ny % 3 != 0);
 }
 size_t ygpu_align256(size_t b);
 int ygpu_single_team_ctas(int max_ctas, size_t nu, int unknowns_per_cta = 0);

@@ -117,7 +117,8 @@ extern "C" int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, cons
     const size_t off_ctl = ygpu_align256(off_out + sizeof(InstOut));
     const size_t off_misc = ygpu_align256(off_ctl + ygpu_teamctl_bytes());
     const size_t off_arena = ygpu_align256(off_misc + 2 * sizeof(int));
-    const size_t need = off_arena + ygpu_inst_scratch_bytes(f->nx, f->ny, f->nz, mixed, ygpu_wants_block(*par));
+    const size_t need = off_arena + ygpu_inst_scratch_bytes(f->nx, f->ny, f->nz, mixed, ygpu_wants_block(*par),
+                                                            ygpu_wants_ilu(*par));
     if (need > (size_t)YGPU_NOALLOC_SCRATCH_BYTES) {
         ygpu_set_error("instance %dx%dx%d needs %zu bytes of scratch, more than the %zu of the "
                        "allocation-free entry point (use ygpu_solve_device)",
@@ -127,7 +128,8 @@ extern "C" int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, cons
     char* base = S->base;
     Inst h;
     ygpu_fill_inst(h, kind, f);
-    ygpu_inst_scratch_carve(h, base + off_arena, f->nx, f->ny, f->nz, mixed, ygpu_wants_block(*par));
+    ygpu_inst_scratch_carve(h, base + off_arena, f->nx, f->ny, f->nz, mixed, ygpu_wants_block(*par),
+                            ygpu_wants_ilu(*par));
     InstOut* d_out = (InstOut*)(base + off_out);
     h.out = d_out;
     Inst* d_inst = (Inst*)(base + off_inst);
@@ -161,7 +163,7 @@ extern "C" int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, cons
         stats->ssa_resid = o.resid;
         stats->lin_resid = o.lin_resid;
         stats->outer_iter = o.outer_iter; stats->active_cells = o.n_active;
-        ygpu_lin_method_run(par, &stats->lin_solver_run, &stats->lin_precond_run);
+        ygpu_lin_method_run_grid(par, f->nx, f->ny, &stats->lin_solver_run, &stats->lin_precond_run);
         stats->status = status;
         for (int q = 0; q < 10; q++) stats->phase_ms[q] = o.phase_ns[q] * 1e-6;
     }

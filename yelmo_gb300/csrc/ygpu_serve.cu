@@ -109,6 +109,7 @@ struct ygpu_server {
     int max_slots = 1;
     bool mixed = false;
     bool block = false;            // tile-block preconditioner scratch
+    bool ilu = false;              // ILU(0) factor scratch (residual form, -p ilu)
     size_t max_active_nu = 0;      // admission: unknowns of the active solves
     size_t active_nu = 0;
     size_t held = 0;               // device bytes held
@@ -188,7 +189,7 @@ static std::vector<Admit> admit_locked(ygpu_server* S) {
     std::vector<Admit> got;
     const size_t need_max = [&] {
         size_t m = 0;
-        for (const Member& M : S->members) m = std::max(m, ygpu_inst_scratch_bytes(M.nx, M.ny, M.nz, S->mixed, S->block));
+        for (const Member& M : S->members) m = std::max(m, ygpu_inst_scratch_bytes(M.nx, M.ny, M.nz, S->mixed, S->block, S->ilu));
         return m;
     }();
     for (auto it = S->waiting.begin(); it != S->waiting.end();) {
@@ -198,7 +199,7 @@ static std::vector<Admit> admit_locked(ygpu_server* S) {
         const size_t nu = (size_t)2 * M.nx * M.ny;
         const bool idle = S->active.empty() && got.empty();
         if (!idle && S->active_nu + nu > S->max_active_nu) break;     // FIFO: wait for retirements
-        const size_t need = ygpu_inst_scratch_bytes(M.nx, M.ny, M.nz, S->mixed, S->block);
+        const size_t need = ygpu_inst_scratch_bytes(M.nx, M.ny, M.nz, S->mixed, S->block, S->ilu);
         int s = -1;
         for (int k = 0; k < (int)S->slots.size(); k++)
             if (S->slots[k].req < 0 && S->slots[k].bytes >= need) { s = k; break; }
@@ -233,7 +234,7 @@ static std::vector<Admit> admit_locked(ygpu_server* S) {
         R.t_admit = now_s();
         R.step = M.steps++;
         ygpu_fill_inst(sl.inst, S->cfg.kind, &M.f);
-        ygpu_inst_scratch_carve(sl.inst, sl.scratch, M.nx, M.ny, M.nz, S->mixed, S->block);
+        ygpu_inst_scratch_carve(sl.inst, sl.scratch, M.nx, M.ny, M.nz, S->mixed, S->block, S->ilu);
         sl.inst.out = S->d_out + s;
         const unsigned long long key = smix_host(R.seed) ^
                                        smix_host(0x5851F42D4C957F2Dull * ((unsigned long long)R.member + 1)) ^
@@ -361,7 +362,8 @@ static void retire_locked(ygpu_server* S) {
         St.ssa_resid = o.resid;
         St.lin_resid = o.lin_resid;
         St.outer_iter = o.outer_iter; St.active_cells = o.n_active;
-        ygpu_lin_method_run(&S->cfg.par, &St.lin_solver_run, &St.lin_precond_run);
+        ygpu_lin_method_run_grid(&S->cfg.par, S->members[R.member].nx, S->members[R.member].ny, &St.lin_solver_run,
+                                 &St.lin_precond_run);
         St.status = R.status;
         St.device_ms = (R.t_done - R.t_admit) * 1e3;
         for (int q = 0; q < 10; q++) St.phase_ms[q] = o.phase_ns[q] * 1e-6;
@@ -426,6 +428,7 @@ extern "C" ygpu_server* ygpu_server_create(const ygpu_server_cfg* cfg) {
     S->cfg = *cfg;
     S->mixed = (cfg->par.precision == YGPU_PREC_MIXED);
     S->block = ygpu_wants_block(cfg->par);
+    S->ilu = ygpu_wants_ilu(cfg->par);
     S->max_ctas = ygpu_solver_max_ctas(cfg->device);
     if (S->max_ctas < 1 || ygpu_init_constants(cfg->device)) {
         ygpu_set_error("solver kernels cannot be resident on device %d", cfg->device);
@@ -525,7 +528,7 @@ extern "C" int ygpu_server_add_member(ygpu_server* S, const ygpu_fields* h, int*
         if (!q) { ygpu_set_error("a member input (H_ice, z_bed, z_sl, c_bed, f_slide, ATT, zeta_aa) is NULL"); return YGPU_ERR_BAD_ARG; }
     const int kind = S->cfg.kind;
     const size_t bytes = member_bytes(kind, h->nx, h->ny, h->nz);
-    const size_t scratch = ygpu_inst_scratch_bytes(h->nx, h->ny, h->nz, S->mixed, S->block);
+    const size_t scratch = ygpu_inst_scratch_bytes(h->nx, h->ny, h->nz, S->mixed, S->block, S->ilu);
     std::lock_guard<std::mutex> lk(S->mu);
     if (!S->fatal.empty()) { ygpu_set_error("server stopped: %s", S->fatal.c_str()); return YGPU_ERR_CUDA; }
     // the member and, if no slot exists yet, one slot for it must fit the budget

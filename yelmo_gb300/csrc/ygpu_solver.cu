@@ -243,8 +243,9 @@ YG_DEV SD deriv_active(double vm, double v0, double vp, bool am, bool ap, double
 template <typename SD>
 __device__ __noinline__ void phase_strain(const Inst& I, const Geo& Gr, Team& T, const double* ux, const double* uy, SD* sdudx,
                                           SD* sdudy, SD* sdvdx, SD* sdvdy) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const Geo G = Gr;
-    const int tid = T.tid, nthr = T.nthr;
+    const int tid = t_tid, nthr = t_nthr;
     const unsigned char* fl = I.cflag;
     const double dx = G.dx, dy = G.dy;
     const float ix = (float)(1.0 / dx), iy = (float)(1.0 / dy), i2x = (float)(1.0 / (2.0 * dx)),
@@ -407,12 +408,13 @@ YG_DEV double beta_aa(const Inst& I, const ygpu_dyn_par& P, const Geo& G, int i,
 // In the mixed mode the powers are stored as FP32 (attp read as float*); the
 // upper half of the array then holds the FP32 shear copies (shear_f32).
 __device__ __noinline__ void phase_att_powers(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const int nz = G.nz, n2 = G.n2;
     const double p2 = -1.0 / I.n_glen;
     const bool glen3 = (I.n_glen == 3.0);
     const bool f32 = (P.precision == YGPU_PREC_MIXED);
     float* af = (float*)I.attp;
-    for (int c = T.tid; c < n2; c += T.nthr) {
+    for (int c = t_tid; c < n2; c += t_nthr) {
         Nb n = make_nb(G, c);
         for (int k = 0; k < nz; k++) {
             if (P.visc_method == 1) {
@@ -481,13 +483,14 @@ struct ZTab {
 
 template <typename R, typename VS>
 __device__ __noinline__ void phase_shear(const Inst& I, const Geo& Gr, Team& T, const VS* vcur) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const Geo G = Gr;
     const int nz = G.nz, n2 = G.n2;
     const double* f = I.f_ice;
     float* sx32 = shear_f32(I, 0);
     float* sy32 = shear_f32(I, 1);
     const ZTab<R> zt(I.zeta, nz);
-    for (int c = T.tid; c < n2; c += T.nthr) {
+    for (int c = t_tid; c < n2; c += t_nthr) {
         Nb n = make_nb(G, c);
         const int cx = CI(n.ip1, n.j), cy = CI(n.i, n.jp1);
         const R tx = (R)I.taub_x[c], ty = (R)I.taub_y[c];
@@ -523,6 +526,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                                           const double* vcur, VD* vnew, const SR* sdudx,
                                           const SR* sdudy, const SR* sdvdx, const SR* sdvdy, bool relax,
                                           bool diva, bool first_copy, bool have_log, bool visc_only = false) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const Geo G = Gr;
     const int nz = G.nz, n2 = G.n2;
     const R p1 = (R)((1.0 - I.n_glen) / (2.0 * I.n_glen));
@@ -533,10 +537,16 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
     const double* f = I.f_ice;
     const int vm = P.visc_method;
     // A^(-1/n) at the nodes and log(visc): FP32 storage in the mixed mode
-    const R* attp_r = (const R*)I.attp;
-    R* lv = (R*)I.lvis;
+    // restrict-qualified: the loads of the next layer may move above this
+    // layer's stores (the layers of a column are otherwise walked one memory
+    // round trip at a time)
+    const R* __restrict__ attp_r = (const R*)I.attp;
+    R* __restrict__ lv = (R*)I.lvis;
+    VD* __restrict__ vn = vnew;
+    const R* __restrict__ shx_r = (sizeof(R) == sizeof(float)) ? (const R*)shear_f32(I, 0) : (const R*)I.duxdz;
+    const R* __restrict__ shy_r = (sizeof(R) == sizeof(float)) ? (const R*)shear_f32(I, 1) : (const R*)I.duydz;
     const ZTab<R> zt(zeta, nz);
-    for (int c = T.tid; c < n2; c += T.nthr) {
+    for (int c = t_tid; c < n2; c += t_nthr) {
         Nb n = make_nb(G, c);
         if (first_copy) {
             I.ux_nm1[c] = I.u_x[c];
@@ -582,6 +592,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
         }
         R vint = R(0), f2 = R(0), vprev = R(0), gprev = R(0);
         const R Hr = (R)Hc;
+#pragma unroll 2
         for (int k = 0; k < nz; k++) {
             const size_t ck = (size_t)k * n2 + c;
             R v;
@@ -593,10 +604,8 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                 R dudzn[4], dvdzn[4], vn[4];
                 if (diva) {
                     // FP64 mode: the FP64 shear; mixed mode: its FP32 copy
-                    const R* dz = (sizeof(R) == sizeof(float)) ? (const R*)shear_f32(I, 0) : (const R*)I.duxdz;
-                    const R* dzy = (sizeof(R) == sizeof(float)) ? (const R*)shear_f32(I, 1) : (const R*)I.duydz;
-                    dz += (size_t)k * n2;
-                    dzy += (size_t)k * n2;
+                    const R* __restrict__ dz = shx_r + (size_t)k * n2;
+                    const R* __restrict__ dzy = shy_r + (size_t)k * n2;
                     nodes_acx(G, n, [&](int a, int b) { return dz[CI(a, b)]; }, ax, dudzn);
                     nodes_acy(G, n, [&](int a, int b) { return dzy[CI(a, b)]; }, ay, dvdzn);
                 }
@@ -645,7 +654,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                 vr = v;
                 if (!visc_only) lv[ck] = log(vr);
             }
-            vnew[ck] = (VD)vr;
+            vn[ck] = (VD)vr;
             // trapezoid integrals (integrate_trapezoid1D_pt, yelmo_tools.f90:1092-1122),
             // in the viscosity arithmetic R
             const R omz = zt.omz(k);
@@ -756,8 +765,9 @@ YG_DEV void lim_face(double& k, double& r, double u, double uc, int mask, double
 // the FP32-rounded coefficients (the same values as its FP32 inner operator)
 template <typename R>
 __device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, const Geo& Gr, Team& T, bool diva) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const Geo G = Gr;
-    const int tid = T.tid, nthr = T.nthr;
+    const int tid = t_tid, nthr = t_nthr;
     const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
     const bool drag = (P.ssa_vel_lim_method == YGPU_VEL_LIM_DRAG);
     const bool limit = (P.beta_method != -1 && P.beta_gl_stag != -1);
@@ -1171,6 +1181,221 @@ YG_DEV T residual_row(const Inst& I, const Geo& G, const OpK<T>& K, const CT* N,
 #undef NB
 }
 
+// ---------------------------------------------------------------------------
+// ILU(0) of the residual form (-p ilu with BiCGSTAB, solver_linear.F90:246-395
+// hands "-p ilu" to LIS). The factorization is ILU(0) (Saad, Iterative Methods,
+// 10.3: no fill outside the pattern of A) of A in a six-colour ordering: cell
+// colour (i - j) mod 3 and then the component, ux before uy. No two coupled
+// unknowns share a colour group (neighbours differ in cell colour; the two
+// components of a cell are in different groups), so the rows of a group factor
+// and solve independently and a team barrier separates the groups: 6 barriers
+// for the factorization, 6 + 6 for an application. Rows are YG_ILU_W slots in
+// a fixed stencil layout; a slot's column carries its group in bits 28..30.
+// ---------------------------------------------------------------------------
+// the colouring needs the periodic directions in multiples of 3 (Jacobi otherwise)
+YG_DEV bool ilu_colourable(const Geo& G) {
+    bool px, py;
+    periodic_dirs(G.bc, px, py);
+    return !(px && G.nx % 3 != 0) && !(py && G.ny % 3 != 0);
+}
+YG_DEV int ilu_group(int nx, int n2, int u) {
+    const int pl = (u >= n2) ? 1 : 0;
+    const int c = u - pl * n2;
+    const int i = c % nx, j = c / nx;
+    return 2 * (((i - j) % 3 + 3) % 3) + pl;
+}
+// The coefficients of residual_row (same formulas) for row u: col[s] = -1 for
+// unused slots. Slots: 0 the diagonal, then the row's stencil in the order of
+// residual_row.
+template <typename T, typename CT>
+YG_DEV void residual_row_coefs(const Inst& I, const Geo& G, const OpK<T>& K, const CT* N, const CT* Nab,
+                               const CT* dgx, const CT* dgy, int u, int col[YG_ILU_W], T val[YG_ILU_W]) {
+#pragma unroll
+    for (int s = 0; s < YG_ILU_W; s++) { col[s] = -1; val[s] = T(0); }
+    col[0] = u;
+    const int rk = I.ukind[u];
+    if (rk == RROW_ID) { val[0] = T(1); return; }
+    if (rk == RROW_FREESLIP) {
+        val[0] = T(1);
+        col[1] = I.rpart[u];
+        val[1] = T(-1);
+        return;
+    }
+    const int nx = G.nx, ny = G.ny, n2 = G.n2;
+    const int pl = (u >= n2) ? 1 : 0;
+    const int c = u - pl * n2;
+    const int i = c % nx, j = c / nx;
+    const int im1 = (i == 0) ? nx - 1 : i - 1, ip1 = (i == nx - 1) ? 0 : i + 1;
+    const int jm1 = (j == 0) ? ny - 1 : j - 1, jp1 = (j == ny - 1) ? 0 : j + 1;
+    const T inv_dx = K.inv_dx, inv_dy = K.inv_dy;
+    const T inv_dxdx = K.inv_dxdx, inv_dydy = K.inv_dydy, inv_dxdy = K.inv_dxdy;
+    auto X = [&](int a, int b) { return a + nx * b; };
+    auto Y = [&](int a, int b) { return n2 + a + nx * b; };
+    auto NN = [&](int a, int b) { return (T)N[a + nx * b]; };
+    auto NB = [&](int a, int b) { return (T)Nab[a + nx * b]; };
+    if (rk == RROW_FRONT) {
+        if (pl == 0) {
+            if (I.f_ice[c] == 1.0 && I.f_ice[ip1 + nx * j] < 1.0) {
+                const T Nn = NN(i, j);
+                val[0] = T(4) * inv_dx * Nn;
+                col[1] = X(im1, j); val[1] = -T(4) * inv_dx * Nn;
+                col[2] = Y(i, jm1); val[2] = -T(2) * inv_dy * Nn;
+                col[3] = Y(i, j); val[3] = T(2) * inv_dy * Nn;
+            } else {
+                const T Nn = NN(ip1, j);
+                val[0] = -T(4) * inv_dx * Nn;
+                col[1] = Y(ip1, jm1); val[1] = -T(2) * inv_dy * Nn;
+                col[2] = X(ip1, j); val[2] = T(4) * inv_dx * Nn;
+                col[3] = Y(ip1, j); val[3] = T(2) * inv_dy * Nn;
+            }
+        } else {
+            if (I.f_ice[c] == 1.0 && I.f_ice[i + nx * jp1] < 1.0) {
+                const T Nn = NN(i, j);
+                val[0] = T(4) * inv_dy * Nn;
+                col[1] = X(im1, j); val[1] = -T(2) * inv_dx * Nn;
+                col[2] = Y(i, jm1); val[2] = -T(4) * inv_dy * Nn;
+                col[3] = X(i, j); val[3] = T(2) * inv_dx * Nn;
+            } else {
+                const T Nn = NN(i, jp1);
+                val[0] = -T(4) * inv_dy * Nn;
+                col[1] = X(im1, jp1); val[1] = -T(2) * inv_dx * Nn;
+                col[2] = X(i, jp1); val[2] = T(2) * inv_dx * Nn;
+                col[3] = Y(i, jp1); val[3] = T(4) * inv_dy * Nn;
+            }
+        }
+    } else if (pl == 0) {
+        val[0] = -T(4) * inv_dxdx * (NN(ip1, j) + NN(i, j)) - T(1) * inv_dydy * (NB(i, j) + NB(i, jm1)) - (T)dgx[c];
+        col[1] = X(ip1, j); val[1] = T(4) * inv_dxdx * NN(ip1, j);
+        col[2] = X(im1, j); val[2] = T(4) * inv_dxdx * NN(i, j);
+        col[3] = X(i, jp1); val[3] = T(1) * inv_dydy * NB(i, j);
+        col[4] = X(i, jm1); val[4] = T(1) * inv_dydy * NB(i, jm1);
+        col[5] = Y(i, j); val[5] = -T(2) * inv_dxdy * NN(i, j) - T(1) * inv_dxdy * NB(i, j);
+        col[6] = Y(ip1, j); val[6] = T(2) * inv_dxdy * NN(ip1, j) + T(1) * inv_dxdy * NB(i, j);
+        col[7] = Y(ip1, jm1); val[7] = -T(2) * inv_dxdy * NN(ip1, j) - T(1) * inv_dxdy * NB(i, jm1);
+        col[8] = Y(i, jm1); val[8] = T(2) * inv_dxdy * NN(i, j) + T(1) * inv_dxdy * NB(i, jm1);
+    } else {
+        val[0] = -T(4) * inv_dydy * (NN(i, jp1) + NN(i, j)) - T(1) * inv_dxdx * (NB(i, j) + NB(im1, j)) - (T)dgy[c];
+        col[1] = Y(i, jp1); val[1] = T(4) * inv_dydy * NN(i, jp1);
+        col[2] = Y(i, jm1); val[2] = T(4) * inv_dydy * NN(i, j);
+        col[3] = Y(ip1, j); val[3] = T(1) * inv_dxdx * NB(i, j);
+        col[4] = Y(im1, j); val[4] = T(1) * inv_dxdx * NB(im1, j);
+        col[5] = X(i, j); val[5] = -T(2) * inv_dxdy * NN(i, j) - T(1) * inv_dxdy * NB(i, j);
+        col[6] = X(i, jp1); val[6] = T(2) * inv_dxdy * NN(i, jp1) + T(1) * inv_dxdy * NB(i, j);
+        col[7] = X(im1, jp1); val[7] = -T(2) * inv_dxdy * NN(i, jp1) - T(1) * inv_dxdy * NB(im1, j);
+        col[8] = X(im1, j); val[8] = T(2) * inv_dxdy * NN(i, j) + T(1) * inv_dxdy * NB(im1, j);
+    }
+    // repeated columns (grids of side 2 or less) merge into their first slot
+#pragma unroll
+    for (int s = 1; s < YG_ILU_W; s++) {
+        if (col[s] < 0) continue;
+        for (int t = 0; t < s; t++)
+            if (col[t] == col[s]) { val[t] += val[s]; col[s] = -1; val[s] = T(0); break; }
+    }
+}
+
+// ILU(0) factors of A (coefficients N, Nab, dgx, dgy) into lu / pivinv / icol.
+// Returns false if the team is aborting.
+template <typename T, typename CT>
+__device__ __noinline__ bool ilu_factor(const Inst& I, const Geo& G, Team& T_, const CT* N, const CT* Nab,
+                                        const CT* dgx, const CT* dgy, T* lu, T* pivinv) {
+    const OpK<T> K = make_opk<T>(G);
+    const int nx = G.nx, n2 = G.n2, nu = G.nu;
+    const int tid = T_.tid, nthr = T_.nthr;
+    int* icol = I.icol;
+    for (int g = 0; g < 6; g++) {
+        for (int u = tid; u < nu; u += nthr) {
+            if (ilu_group(nx, n2, u) != g) continue;
+            int col[YG_ILU_W];
+            T a[YG_ILU_W];
+            residual_row_coefs<T, CT>(I, G, K, N, Nab, dgx, dgy, u, col, a);
+            int grp[YG_ILU_W];
+#pragma unroll
+            for (int s = 0; s < YG_ILU_W; s++) grp[s] = (col[s] >= 0) ? ilu_group(nx, n2, col[s]) : -1;
+            const T d0 = a[0];
+            // IKJ elimination against the factored rows of the earlier groups, in group order
+            for (int gk = 0; gk < g; gk++) {
+                for (int s = 1; s < YG_ILU_W; s++) {
+                    if (grp[s] != gk) continue;
+                    const int k = col[s];
+                    const T l = a[s] * pivinv[k];
+                    a[s] = l;
+                    const int* ck = icol + (size_t)k * YG_ILU_W;
+                    const T* vk = lu + (size_t)k * YG_ILU_W;
+                    for (int t = 1; t < YG_ILU_W; t++) {
+                        const int pc = ck[t];
+                        if (pc < 0 || (pc >> 28) <= gk) continue;      // the U part of row k
+                        const int cj = pc & 0x0fffffff;
+                        const T ukj = vk[t];
+                        for (int s2 = 0; s2 < YG_ILU_W; s2++)
+                            if (col[s2] == cj) { a[s2] -= l * ukj; break; }
+                    }
+                }
+            }
+            // a pivot that cancels is replaced by the row's own diagonal (as the oracle)
+            T piv = a[0];
+            if (fabs((double)piv) <= 1e-14 * fabs((double)d0)) piv = d0;
+            if (piv == T(0)) piv = T(1);
+            a[0] = piv;
+            int* cu = icol + (size_t)u * YG_ILU_W;
+            T* vu = lu + (size_t)u * YG_ILU_W;
+#pragma unroll
+            for (int s = 0; s < YG_ILU_W; s++) {
+                cu[s] = (col[s] >= 0) ? (col[s] | (grp[s] << 28)) : -1;
+                vu[s] = a[s];
+            }
+            pivinv[u] = T(1) / piv;
+        }
+        if (!team_barrier(T_)) return false;
+    }
+    return true;
+}
+
+// z = (LU)^-1 r over every row: forward substitution by group, then backward.
+// z may not alias r. Ends with a team barrier (z is read at neighbouring rows next).
+template <typename T>
+YG_DEV bool ilu_apply(Team& T_, int nx, int n2, int nu, const int* __restrict__ icol, const T* __restrict__ lu,
+                      const T* __restrict__ pivinv, const T* r, T* z) {
+    const int tid = T_.tid, nthr = T_.nthr;
+    for (int g = 0; g < 6; g++) {
+        for (int u = tid; u < nu; u += nthr) {
+            if (ilu_group(nx, n2, u) != g) continue;
+            const int* cu = icol + (size_t)u * YG_ILU_W;
+            const T* vu = lu + (size_t)u * YG_ILU_W;
+            T s = r[u];
+#pragma unroll
+            for (int t = 1; t < YG_ILU_W; t++) {
+                const int pc = cu[t];
+                if (pc >= 0 && (pc >> 28) < g) s -= vu[t] * z[pc & 0x0fffffff];
+            }
+            z[u] = s;
+        }
+        if (!team_barrier(T_)) return false;
+    }
+    for (int g = 5; g >= 0; g--) {
+        for (int u = tid; u < nu; u += nthr) {
+            if (ilu_group(nx, n2, u) != g) continue;
+            const int* cu = icol + (size_t)u * YG_ILU_W;
+            const T* vu = lu + (size_t)u * YG_ILU_W;
+            T s = z[u];
+#pragma unroll
+            for (int t = 1; t < YG_ILU_W; t++) {
+                const int pc = cu[t];
+                if (pc >= 0 && (pc >> 28) > g) s -= vu[t] * z[pc & 0x0fffffff];
+            }
+            z[u] = s * pivinv[u];
+        }
+        if (!team_barrier(T_)) return false;
+    }
+    return true;
+}
+template <typename T>
+struct IluM {
+    int nx, n2;
+    const int* icol;
+    const T* lu;
+    const T* pivinv;
+};
+
 template <typename T, typename CT>
 YG_DEV T operator_row(const Inst& I, const Geo& G, const OpK<T>& K, bool energy, const CT* N, const CT* Nab,
                       const CT* dgx, const CT* dgy, const T* v, int u) {
@@ -1387,11 +1612,12 @@ __device__ __noinline__ bool build_active_cells(const Inst& I, const Geo& G, Tea
 }
 
 __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
     const int nx = G.nx, ny = G.ny, n2 = G.n2;
     const unsigned bb = G.bb;
     // pass 1: kind and partner
-    for (int u = T.tid; u < G.nu; u += T.nthr) {
+    for (int u = t_tid; u < G.nu; u += t_nthr) {
         const int pl = (u >= n2) ? 1 : 0, c = u - pl * n2, i = c % nx, j = c / nx;
         const int mask = pl ? I.mask_y[c] : I.mask_x[c];
         const double uval = pl ? I.u_y[c] : I.u_x[c];
@@ -1458,7 +1684,7 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
     if (!team_barrier(T)) return false;
     // pass 2: resolve tied chains to their free root (depth <= 8)
     double bad = 0.0;
-    for (int u = T.tid; u < G.nu; u += T.nthr) {
+    for (int u = t_tid; u < G.nu; u += t_nthr) {
         int m = u, depth = 0;
         while (I.ukind[m] == DOF_TIED) {
             m = I.rpart[m];
@@ -1469,7 +1695,7 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
     if (!team_allreduce(T, &bad, 1)) return false;
     if (bad > 0.0) return false;
     // pass 3: a tied unknown whose root is Dirichlet is Dirichlet (value of the root)
-    for (int u = T.tid; u < G.nu; u += T.nthr) {
+    for (int u = t_tid; u < G.nu; u += t_nthr) {
         int k = I.ukind[u];
         if (k == DOF_TIED) {
             int r = I.emap[u];
@@ -1480,7 +1706,7 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
         }
     }
     if (!team_barrier(T)) return false;
-    for (int u = T.tid; u < G.nu; u += T.nthr) {
+    for (int u = t_tid; u < G.nu; u += t_nthr) {
         if (I.rpart[u] == -2) {
             I.ukind[u] = DOF_DIR;
             I.rpart[u] = -1;
@@ -1488,7 +1714,7 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
     }
     if (!team_barrier(T)) return false;
     // pass 4: column map (free: self, tied: root, Dirichlet: -1) and member lists
-    for (int u = T.tid; u < G.nu; u += T.nthr) {
+    for (int u = t_tid; u < G.nu; u += t_nthr) {
         int k = I.ukind[u];
         int r = I.emap[u];
         if (k == DOF_DIR) I.emap[u] = -1;
@@ -1497,7 +1723,7 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
         (void)r;
     }
     if (!team_barrier(T)) return false;
-    for (int u = T.tid; u < G.nu; u += T.nthr) {
+    for (int u = t_tid; u < G.nu; u += t_nthr) {
         int* mem = I.mem + 3 * u;
         mem[0] = mem[1] = mem[2] = -1;
         if (I.ukind[u] != DOF_FREE) continue;
@@ -1515,7 +1741,7 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
     if (!team_barrier(T)) return false;
     // pass 5: interior fast-path flag (rpart = 1): a free row without members
     // whose four elements exist and hold only free, self-mapped unknowns
-    for (int u = T.tid; u < G.nu; u += T.nthr) {
+    for (int u = t_tid; u < G.nu; u += t_nthr) {
         int fast = 0;
         if (I.ukind[u] == DOF_FREE && I.mem[3 * u] < 0) {
             const int pl = (u >= n2) ? 1 : 0, c = u - pl * n2, i = c % nx, j = c / nx;
@@ -1555,13 +1781,14 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
 // Phase: linear system -- rhs, start vector, Jacobi diagonal (FP64)
 // ---------------------------------------------------------------------------
 __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, double& bnorm2) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
     const bool drag = (P.ssa_vel_lim_method == YGPU_VEL_LIM_DRAG);
     const int n2 = G.n2, nx = G.nx, ny = G.ny;
     const double* N = I.visc_int;
     const OpK<double> K64 = make_opk<double>(G);
     double bn2 = 0.0;
-    for (int u = T.tid; u < G.nu; u += T.nthr) {
+    for (int u = t_tid; u < G.nu; u += t_nthr) {
         const int pl = (u >= n2) ? 1 : 0, c = u - pl * n2;
         const double uval = pl ? I.u_y[c] : I.u_x[c];
         double b, x0, d = 1.0;
@@ -2177,7 +2404,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
                                             T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
                                             T* __restrict__ rt, T* __restrict__ p, T* v, T* __restrict__ s, T* t,
                                             T* ph, T* sh, int maxiter, double tol, double bnrm, bool precond,
-                                            int& iters, double& relres, bool& ok) {
+                                            int& iters, double& relres, bool& ok, const IluM<T>* M = nullptr) {
     TeamLocal tl_(Tm_);
     Team& Tm = tl_.t;
     // sums and scalars in T (an FP32 inner solve stays off the FP64 pipe)
@@ -2196,6 +2423,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
         p[u] = T(0);
         ph[u] = T(0);
         sh[u] = T(0);
+        s[u] = T(0);       // the ILU(0) solves read s on every row, the loops write active rows only
         a0 += ru * ru;
     }
     T red[1];
@@ -2228,10 +2456,12 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
                 const int u = R.row(e, q);
                 T pu = (it == 1) ? r[u] : r[u] + beta * (p[u] - om * v[u]);
                 p[u] = pu;
-                ph[u] = precond ? (T)dinv[u] * pu : pu;
+                if (!M) ph[u] = precond ? (T)dinv[u] * pu : pu;
             }
         }
         if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
+        // ILU(0): p_hat = M^-1 p over every row (barriers inside)
+        if (M && !(ok = ilu_apply<T>(Tm, M->nx, M->n2, nu, M->icol, M->lu, M->pivinv, p, ph))) return YGPU_ERR_TIMEOUT;
         A.apply(Tm, ph, v, R);
         T tvp = T(0);
         {
@@ -2261,7 +2491,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
                 const int u = R.row(e, q);
                 T su = r[u] - al * v[u];
                 s[u] = su;
-                sh[u] = precond ? (T)dinv[u] * su : su;
+                if (!M) sh[u] = precond ? (T)dinv[u] * su : su;
                 ssp += su * su;
             }
         }
@@ -2269,6 +2499,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
         // early-convergence test on s, which saves an all-reduce per iteration
         // (the last iteration's t is then unused)
         if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
+        if (M && !(ok = ilu_apply<T>(Tm, M->nx, M->n2, nu, M->icol, M->lu, M->pivinv, s, sh))) return YGPU_ERR_TIMEOUT;
         A.apply(Tm, sh, t, R);
         T ts0 = T(0), ts1 = T(0);
         {
@@ -2681,6 +2912,7 @@ __device__ __noinline__ int krylov_pcg_pipe_blk(Team& Tm_, const Geo& G, const O
 // ---------------------------------------------------------------------------
 __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, double bnrm, int& iters,
                         double& relres, int& outer, bool& ok) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
     const bool pre = (P.lin_precond != YGPU_PRE_NONE);
     // MINRES requests run CG on the symmetric energy system, BiCGSTAB on the residual one
@@ -2697,6 +2929,11 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         if (use_cg)
             return krylov_pcg_pipe<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.rt, I.v, I.ph, I.m2, I.z, I.q, I.s,
                                            I.p, P.lin_maxiter, P.lin_tol, bnrm, pre, iters, relres, ok);
+        if (!energy && I.icol && I.ilu && ilu_colourable(G)) {
+            const IluM<double> M{G.nx, G.n2, I.icol, I.ilu, I.ipiv};
+            return krylov_bicgstab<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.rt, I.p, I.v, I.s, I.t, I.ph, I.sh,
+                                           P.lin_maxiter, P.lin_tol, bnrm, pre, iters, relres, ok, &M);
+        }
         return krylov_bicgstab<double>(T, G.nu, A64, I.dinv, I.x, I.b, I.r, I.rt, I.p, I.v, I.s, I.t, I.ph, I.sh,
                                        P.lin_maxiter, P.lin_tol, bnrm, pre, iters, relres, ok);
     }
@@ -2716,7 +2953,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
     // The outer passes visit the rows of the active cells only (identity rows
     // hold x = b, a zero residual and a zero correction, cleared here once).
     const RowItems R = make_row_items(T, I.acell, G.n2, G.nu, false);
-    for (int u = T.tid; u < G.nu; u += T.nthr) {
+    for (int u = t_tid; u < G.nu; u += t_nthr) {
         I.fr[u] = 0.0f;
         I.fx[u] = 0.0f;
     }
@@ -2724,7 +2961,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         // r64 = b - A64 x (FP64 residual of the outer iterate)
         A64.apply(T, I.x, I.q, R);
         double rr = 0.0;
-        for (int e = T.tid; e < R.nitem; e += T.nthr) {
+        for (int e = t_tid; e < R.nitem; e += t_nthr) {
             const int u = R.lookup(e);
             double ru = I.b[u] - I.q[u];
             I.r[u] = ru;
@@ -2739,7 +2976,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         if (total >= P.lin_maxiter) { status = YGPU_MAXITER; break; }
         // inner FP32 solve of A d = r, d0 = 0, scaled by ||r||
         const double nr = sqrt(rr), sc = 1.0 / nr;
-        for (int e = T.tid; e < R.nitem; e += T.nthr) {
+        for (int e = t_tid; e < R.nitem; e += t_nthr) {
             const int u = R.lookup(e);
             I.fr[u] = (float)(I.r[u] * sc);
             I.fx[u] = 0.0f;
@@ -2757,14 +2994,17 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         else if (use_cg)
             st = krylov_pcg_pipe<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.frt, I.fv, I.ft, I.fph, I.fm2, I.fz,
                                         I.fq, I.fs, I.fp, inner_max, inner_tol, 1.0, pre, it, rel_in, ok);
-        else
+        else {
+            const IluM<float> M{G.nx, G.n2, I.icol, I.filu, I.fipiv};
+            const bool ilu = !energy && I.icol && I.filu && ilu_colourable(G);
             st = krylov_bicgstab<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.fz, I.frt, I.fp, I.fv, I.fs, I.ft, I.fph,
-                                        I.fsh, inner_max, inner_tol, 1.0, pre, it, rel_in, ok);
+                                        I.fsh, inner_max, inner_tol, 1.0, pre, it, rel_in, ok, ilu ? &M : nullptr);
+        }
         if (!ok) return YGPU_ERR_TIMEOUT;
         total += it;
         outer++;
         // x += d (FP64 accumulation)
-        for (int e = T.tid; e < R.nitem; e += T.nthr) {
+        for (int e = t_tid; e < R.nitem; e += t_nthr) {
             const int u = R.lookup(e);
             I.x[u] = I.x[u] + (double)I.fx[u] * nr;
         }
@@ -2779,11 +3019,12 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
 // Phase: epilogue of one Picard iteration
 // ---------------------------------------------------------------------------
 __device__ __noinline__ void phase_epilogue(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, bool diva, double red[4]) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
     const double lim = P.ssa_vel_max, rel = P.ssa_iter_rel;
     const double vel_tol = 1e-5;
     double r1 = 0.0, r2 = 0.0, nchk = 0.0, nbad = 0.0;
-    for (int c = T.tid; c < G.n2; c += T.nthr) {
+    for (int c = t_tid; c < G.n2; c += t_nthr) {
         double uv[2];
 #pragma unroll
         for (int pl = 0; pl < 2; pl++) {
@@ -2848,12 +3089,13 @@ __device__ __noinline__ void phase_epilogue(const Inst& I, const ygpu_dyn_par& P
 // Final passes after the Picard loop
 // ---------------------------------------------------------------------------
 __device__ __noinline__ double count_lim_part(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const bool drag = (P.ssa_vel_lim_method == YGPU_VEL_LIM_DRAG);
     const double s0 = 0.8 * P.ssa_vel_max, umax = P.ssa_vel_max;
     const double* ux = I.u_x;
     const double* uy = I.u_y;
     double n = 0.0;
-    for (int c = T.tid; c < G.n2; c += T.nthr) {
+    for (int c = t_tid; c < G.n2; c += t_nthr) {
         Nb b = make_nb(G, c);
         const int i = b.i, j = b.j;
         if (I.mask_x[c] >= 1) {
@@ -2875,10 +3117,11 @@ __device__ __noinline__ double count_lim_part(const Inst& I, const ygpu_dyn_par&
 // DIVA: final vertical shear (from the state at the start of the last
 // iteration) and the 3D velocity (calc_vel_horizontal_3D, velocity_diva.f90:431-508)
 __device__ __noinline__ void phase_diva_final(const Inst& I, const Geo& G, Team& T, const double* vlast_cur, const double* vfinal) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const int n2 = G.n2, nz = G.nz;
     const double* f = I.f_ice;
     const double* zeta = I.zeta;
-    for (int c = T.tid; c < n2; c += T.nthr) {
+    for (int c = t_tid; c < n2; c += t_nthr) {
         Nb n = make_nb(G, c);
         const int cx = CI(n.ip1, n.j), cy = CI(n.i, n.jp1);
         double F1c = 0.0, F1x = 0.0, F1y = 0.0;
@@ -2929,13 +3172,14 @@ struct PhaseClock {
 };
 
 __device__ __noinline__ void step_setup(const Inst& I, const ygpu_dyn_par& P, Team& T, int* done_count) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const bool diva = (I.kind == YGPU_KIND_DIVA);
     const Geo G = make_geo(I, P);
     InstOut* out = I.out;
     const bool lead = (T.cta == 0 && threadIdx.x == 0);
     PhaseClock clk;
     clk.start();
-    for (int c = T.tid; c < G.n2; c += T.nthr) {
+    for (int c = t_tid; c < G.n2; c += t_nthr) {
         I.err_x[c] = 1.0;
         I.err_y[c] = 1.0;
         I.cflag[c] = cell_flags(G, I, c);
@@ -3029,6 +3273,13 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
         block_setup<float, double>(I, G, T, Ab, I.fminv);
         if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
     }
+    if (I.icol && P.ssa_solver != YGPU_SSA_ENERGY && ilu_colourable(G)) {
+        // -p ilu on the residual form: the ILU(0) factors of this iteration's operator
+        const bool okf = mixed ? ilu_factor<float, float>(I, G, T, I.fN, I.fNab, I.fdrag_x, I.fdrag_y, I.filu, I.fipiv)
+                               : ilu_factor<double, double>(I, G, T, I.visc_int, I.Nab, I.drag_x, I.drag_y, I.ilu,
+                                                            I.ipiv);
+        if (!okf) { status = YGPU_ERR_TIMEOUT; goto out_; }
+    }
     if (mixed) {
         // the FP32 copies of the operator coefficients and the Jacobi diagonal
         // were written by the phases that produce them; the tile-block
@@ -3058,6 +3309,7 @@ out_:
 }
 
 __device__ __noinline__ void step_krylov(const Inst& I, const ygpu_dyn_par& P, Team& T, int* done_count) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const Geo G = make_geo(I, P);
     InstOut* out = I.out;
     const bool lead = (T.cta == 0 && threadIdx.x == 0);
@@ -3070,7 +3322,7 @@ __device__ __noinline__ void step_krylov(const Inst& I, const ygpu_dyn_par& P, T
     bool ok = true;
     if (bn2 == 0.0) {
         // homogeneous system: x = 0 (solver_linear.F90:162-174)
-        for (int u = T.tid; u < G.nu; u += T.nthr) I.x[u] = 0.0;
+        for (int u = t_tid; u < G.nu; u += t_nthr) I.x[u] = 0.0;
         st = YGPU_OK;
     } else {
         st = linear_solve(I, P, G, T, sqrt(bn2), it, rr, outer, ok);
@@ -3094,18 +3346,19 @@ __device__ __noinline__ void step_krylov(const Inst& I, const ygpu_dyn_par& P, T
 // passes after the Picard loop (also for ssa_iter_max = 0)
 __device__ __noinline__ bool final_passes(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, bool diva,
                                           int in_alt, bool looped) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     if (P.precision == YGPU_PREC_MIXED) {
         // the final FP32 viscosity goes to the caller's FP64 array first; the
         // passes below then read it there
         if (looped) {
             const size_t n3 = (size_t)G.n2 * G.nz;
             const float* vf = (const float*)I.visc_alt + (in_alt ? n3 : 0);
-            for (size_t k = T.tid; k < n3; k += T.nthr) I.visc[k] = (double)vf[k];
+            for (size_t k = t_tid; k < n3; k += t_nthr) I.visc[k] = (double)vf[k];
             if (diva) {
                 // the shear of the last iteration, kept in FP32 by the loop
                 const float* sx = shear_f32(I, 0);
                 const float* sy = shear_f32(I, 1);
-                for (size_t k = T.tid; k < n3; k += T.nthr) {
+                for (size_t k = t_tid; k < n3; k += t_nthr) {
                     I.duxdz[k] = (double)sx[k];
                     I.duydz[k] = (double)sy[k];
                 }
@@ -3126,7 +3379,7 @@ __device__ __noinline__ bool final_passes(const Inst& I, const ygpu_dyn_par& P, 
     if (diva) {
         phase_diva_final(I, G, T, vlast, vcur);
     } else {
-        for (int c = T.tid; c < G.n2; c += T.nthr) {
+        for (int c = t_tid; c < G.n2; c += t_nthr) {
             // calc_basal_stress, velocity_ssa.f90:588-617
             double tx = I.bm_x[c] * I.u_x[c], ty = I.bm_y[c] * I.u_y[c];
             I.taub_x[c] = (fabs(tx) < 1e-5) ? 0.0 : tx;
@@ -3148,7 +3401,7 @@ __device__ __noinline__ bool final_passes(const Inst& I, const ygpu_dyn_par& P, 
     }
     // the caller's visc_eff must hold the final viscosity
     if (in_alt) {
-        for (size_t k = T.tid; k < (size_t)G.n2 * G.nz; k += T.nthr) I.visc[k] = I.visc_alt[k];
+        for (size_t k = t_tid; k < (size_t)G.n2 * G.nz; k += t_nthr) I.visc[k] = I.visc_alt[k];
     }
     if (T.cta == 0 && threadIdx.x == 0) I.out->lim_n = (int)nlim;
     return team_barrier(T);
