@@ -537,9 +537,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
     const double* f = I.f_ice;
     const int vm = P.visc_method;
     // A^(-1/n) at the nodes and log(visc): FP32 storage in the mixed mode
-    // restrict-qualified: the loads of the next layer may move above this
-    // layer's stores (the layers of a column are otherwise walked one memory
-    // round trip at a time)
+    // restrict-qualified: the layer's loads do not wait for the previous layer's stores
     const R* __restrict__ attp_r = (const R*)I.attp;
     R* __restrict__ lv = (R*)I.lvis;
     VD* __restrict__ vn = vnew;
@@ -592,7 +590,6 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
         }
         R vint = R(0), f2 = R(0), vprev = R(0), gprev = R(0);
         const R Hr = (R)Hc;
-#pragma unroll 2
         for (int k = 0; k < nz; k++) {
             const size_t ck = (size_t)k * n2 + c;
             R v;
@@ -1188,9 +1185,11 @@ YG_DEV T residual_row(const Inst& I, const Geo& G, const OpK<T>& K, const CT* N,
 // colour (i - j) mod 3 and then the component, ux before uy. No two coupled
 // unknowns share a colour group (neighbours differ in cell colour; the two
 // components of a cell are in different groups), so the rows of a group factor
-// and solve independently and a team barrier separates the groups: 6 barriers
-// for the factorization, 6 + 6 for an application. Rows are YG_ILU_W slots in
-// a fixed stencil layout; a slot's column carries its group in bits 28..30.
+// and solve independently; a thread takes both rows of a cell, whose only
+// coupling inside their colour is to each other, so a team barrier separates the
+// three cell colours: 3 barriers for the factorization, 3 + 3 for an
+// application. Rows are YG_ILU_W slots in a fixed stencil layout; a slot's
+// column carries its group in bits 28..30.
 // ---------------------------------------------------------------------------
 // the colouring needs the periodic directions in multiples of 3 (Jacobi otherwise)
 YG_DEV bool ilu_colourable(const Geo& G) {
@@ -1294,95 +1293,113 @@ YG_DEV void residual_row_coefs(const Inst& I, const Geo& G, const OpK<T>& K, con
 }
 
 // ILU(0) factors of A (coefficients N, Nab, dgx, dgy) into lu / pivinv / icol.
-// Returns false if the team is aborting.
+// Colour by colour (a team barrier after each); a thread factors both rows of a
+// cell, ux (group 2 gc) then uy (group 2 gc + 1): the only column of a row in
+// its own colour is the other component of the same cell, which the same
+// thread has just factored. Returns false if the team is aborting.
 template <typename T, typename CT>
 __device__ __noinline__ bool ilu_factor(const Inst& I, const Geo& G, Team& T_, const CT* N, const CT* Nab,
                                         const CT* dgx, const CT* dgy, T* lu, T* pivinv) {
     const OpK<T> K = make_opk<T>(G);
-    const int nx = G.nx, n2 = G.n2, nu = G.nu;
+    const int nx = G.nx, n2 = G.n2;
     const int tid = T_.tid, nthr = T_.nthr;
     int* icol = I.icol;
-    for (int g = 0; g < 6; g++) {
-        for (int u = tid; u < nu; u += nthr) {
-            if (ilu_group(nx, n2, u) != g) continue;
-            int col[YG_ILU_W];
-            T a[YG_ILU_W];
-            residual_row_coefs<T, CT>(I, G, K, N, Nab, dgx, dgy, u, col, a);
-            int grp[YG_ILU_W];
+    for (int gc = 0; gc < 3; gc++) {
+        for (int c = tid; c < n2; c += nthr) {
+            if (ilu_group(nx, n2, c) != 2 * gc) continue;
+#pragma unroll 1
+            for (int h = 0; h < 2; h++) {
+                const int u = c + h * n2;
+                const int g = 2 * gc + h;
+                int col[YG_ILU_W];
+                T a[YG_ILU_W];
+                residual_row_coefs<T, CT>(I, G, K, N, Nab, dgx, dgy, u, col, a);
+                int grp[YG_ILU_W];
 #pragma unroll
-            for (int s = 0; s < YG_ILU_W; s++) grp[s] = (col[s] >= 0) ? ilu_group(nx, n2, col[s]) : -1;
-            const T d0 = a[0];
-            // IKJ elimination against the factored rows of the earlier groups, in group order
-            for (int gk = 0; gk < g; gk++) {
-                for (int s = 1; s < YG_ILU_W; s++) {
-                    if (grp[s] != gk) continue;
-                    const int k = col[s];
-                    const T l = a[s] * pivinv[k];
-                    a[s] = l;
-                    const int* ck = icol + (size_t)k * YG_ILU_W;
-                    const T* vk = lu + (size_t)k * YG_ILU_W;
-                    for (int t = 1; t < YG_ILU_W; t++) {
-                        const int pc = ck[t];
-                        if (pc < 0 || (pc >> 28) <= gk) continue;      // the U part of row k
-                        const int cj = pc & 0x0fffffff;
-                        const T ukj = vk[t];
-                        for (int s2 = 0; s2 < YG_ILU_W; s2++)
-                            if (col[s2] == cj) { a[s2] -= l * ukj; break; }
+                for (int q = 0; q < YG_ILU_W; q++) grp[q] = (col[q] >= 0) ? ilu_group(nx, n2, col[q]) : -1;
+                const T d0 = a[0];
+                // IKJ elimination against the factored rows before this one, in group order
+                for (int gk = 0; gk < g; gk++) {
+                    for (int q = 1; q < YG_ILU_W; q++) {
+                        if (grp[q] != gk) continue;
+                        const int k = col[q];
+                        const T l = a[q] * pivinv[k];
+                        a[q] = l;
+                        const int* ck = icol + (size_t)k * YG_ILU_W;
+                        const T* vk = lu + (size_t)k * YG_ILU_W;
+                        for (int t = 1; t < YG_ILU_W; t++) {
+                            const int pc = ck[t];
+                            if (pc < 0 || (pc >> 28) <= gk) continue;      // the U part of row k
+                            const int cj = pc & 0x0fffffff;
+                            const T ukj = vk[t];
+                            for (int q2 = 0; q2 < YG_ILU_W; q2++)
+                                if (col[q2] == cj) { a[q2] -= l * ukj; break; }
+                        }
                     }
                 }
-            }
-            // a pivot that cancels is replaced by the row's own diagonal (as the oracle)
-            T piv = a[0];
-            if (fabs((double)piv) <= 1e-14 * fabs((double)d0)) piv = d0;
-            if (piv == T(0)) piv = T(1);
-            a[0] = piv;
-            int* cu = icol + (size_t)u * YG_ILU_W;
-            T* vu = lu + (size_t)u * YG_ILU_W;
+                // a pivot that cancels is replaced by the row's own diagonal (as the oracle)
+                T piv = a[0];
+                if (fabs((double)piv) <= 1e-14 * fabs((double)d0)) piv = d0;
+                if (piv == T(0)) piv = T(1);
+                a[0] = piv;
+                int* cu = icol + (size_t)u * YG_ILU_W;
+                T* vu = lu + (size_t)u * YG_ILU_W;
 #pragma unroll
-            for (int s = 0; s < YG_ILU_W; s++) {
-                cu[s] = (col[s] >= 0) ? (col[s] | (grp[s] << 28)) : -1;
-                vu[s] = a[s];
+                for (int q = 0; q < YG_ILU_W; q++) {
+                    cu[q] = (col[q] >= 0) ? (col[q] | (grp[q] << 28)) : -1;
+                    vu[q] = a[q];
+                }
+                pivinv[u] = T(1) / piv;
             }
-            pivinv[u] = T(1) / piv;
         }
         if (!team_barrier(T_)) return false;
     }
     return true;
 }
 
-// z = (LU)^-1 r over every row: forward substitution by group, then backward.
-// z may not alias r. Ends with a team barrier (z is read at neighbouring rows next).
+// z = (LU)^-1 r over every row: forward substitution colour by colour (ux row,
+// then uy row of each cell), then backward (uy row, then ux row). z may not
+// alias r. Ends with a team barrier (z is read at neighbouring rows next).
 template <typename T>
 YG_DEV bool ilu_apply(Team& T_, int nx, int n2, int nu, const int* __restrict__ icol, const T* __restrict__ lu,
                       const T* __restrict__ pivinv, const T* r, T* z) {
+    (void)nu;
     const int tid = T_.tid, nthr = T_.nthr;
-    for (int g = 0; g < 6; g++) {
-        for (int u = tid; u < nu; u += nthr) {
-            if (ilu_group(nx, n2, u) != g) continue;
-            const int* cu = icol + (size_t)u * YG_ILU_W;
-            const T* vu = lu + (size_t)u * YG_ILU_W;
-            T s = r[u];
+    for (int gc = 0; gc < 3; gc++) {
+        for (int c = tid; c < n2; c += nthr) {
+            if (ilu_group(nx, n2, c) != 2 * gc) continue;
 #pragma unroll
-            for (int t = 1; t < YG_ILU_W; t++) {
-                const int pc = cu[t];
-                if (pc >= 0 && (pc >> 28) < g) s -= vu[t] * z[pc & 0x0fffffff];
+            for (int h = 0; h < 2; h++) {
+                const int u = c + h * n2, g = 2 * gc + h;
+                const int* cu = icol + (size_t)u * YG_ILU_W;
+                const T* vu = lu + (size_t)u * YG_ILU_W;
+                T s = r[u];
+#pragma unroll
+                for (int t = 1; t < YG_ILU_W; t++) {
+                    const int pc = cu[t];
+                    if (pc >= 0 && (pc >> 28) < g) s -= vu[t] * z[pc & 0x0fffffff];
+                }
+                z[u] = s;
             }
-            z[u] = s;
         }
         if (!team_barrier(T_)) return false;
     }
-    for (int g = 5; g >= 0; g--) {
-        for (int u = tid; u < nu; u += nthr) {
-            if (ilu_group(nx, n2, u) != g) continue;
-            const int* cu = icol + (size_t)u * YG_ILU_W;
-            const T* vu = lu + (size_t)u * YG_ILU_W;
-            T s = z[u];
+    for (int gc = 2; gc >= 0; gc--) {
+        for (int c = tid; c < n2; c += nthr) {
+            if (ilu_group(nx, n2, c) != 2 * gc) continue;
 #pragma unroll
-            for (int t = 1; t < YG_ILU_W; t++) {
-                const int pc = cu[t];
-                if (pc >= 0 && (pc >> 28) > g) s -= vu[t] * z[pc & 0x0fffffff];
+            for (int h = 1; h >= 0; h--) {
+                const int u = c + h * n2, g = 2 * gc + h;
+                const int* cu = icol + (size_t)u * YG_ILU_W;
+                const T* vu = lu + (size_t)u * YG_ILU_W;
+                T s = z[u];
+#pragma unroll
+                for (int t = 1; t < YG_ILU_W; t++) {
+                    const int pc = cu[t];
+                    if (pc >= 0 && (pc >> 28) > g) s -= vu[t] * z[pc & 0x0fffffff];
+                }
+                z[u] = s * pivinv[u];
             }
-            z[u] = s * pivinv[u];
         }
         if (!team_barrier(T_)) return false;
     }
@@ -1410,12 +1427,15 @@ YG_DEV T operator_row(const Inst& I, const Geo& G, const OpK<T>& K, bool energy,
 // one buffer for all the solvers of a kernel.
 __shared__ int g_item_cache[YG_ITEM_CACHE * YG_ITEM_BLOCK];
 
-// Rows a thread owns in the BiCGSTAB loops: items t = tid, tid + nthr, ... of
-// the team, row t without an active-cell list, else the listed cells' ux rows
-// then their uy rows.
+// Rows a thread owns in the BiCGSTAB loops: item t is row t without an
+// active-cell list, else the listed cells' ux rows then their uy rows. Each CTA
+// of the team takes one contiguous chunk of the items (every SM gets rows, and
+// neighbouring threads take neighbouring rows); a thread's items are t0, t0 +
+// ts, ... below t1.
 struct RowItems {
     const int* ac;
     int n2, nact, nitem, cache;
+    int t0, t1, ts;
     YG_DEV int lookup(int t) const {
         if (!ac) return t;
         return (t < nact) ? ac[t] : n2 + ac[t - nact];
@@ -1433,8 +1453,13 @@ YG_DEV RowItems make_row_items(const Team& Tm, const int* ac, int n2, int nu, bo
     R.nact = ac ? min(max(ac[n2], 0), n2) : n2;
     R.nitem = ac ? 2 * R.nact : nu;
     R.cache = (use_cache && blockDim.x <= YG_ITEM_BLOCK) ? YG_ITEM_CACHE : 0;
+    const int chunk = (R.nitem + Tm.ncta - 1) / Tm.ncta;
+    const int beg = min(Tm.cta * chunk, R.nitem);
+    R.t0 = beg + (int)threadIdx.x;
+    R.t1 = min(beg + chunk, R.nitem);
+    R.ts = (int)blockDim.x;
     int q = 0;
-    for (int t = Tm.tid; t < R.nitem && q < R.cache; t += Tm.nthr, q++)
+    for (int t = R.t0; t < R.t1 && q < R.cache; t += R.ts, q++)
         g_item_cache[q * blockDim.x + threadIdx.x] = R.lookup(t);
     return R;
 }
@@ -1487,16 +1512,16 @@ struct StencilOp {
     YG_DEV void apply(Team& Tm, const T* v, T* y, const RowItems& R) const {
         if (sizeof(T) != sizeof(float)) {
             int q = 0;
-            for (int t = Tm.tid; t < R.nitem; t += Tm.nthr, q++) {
+            for (int t = R.t0; t < R.t1; t += R.ts, q++) {
                 const int k = R.row(t, q);
                 y[k] = row(k, v);
             }
             return;
         }
         int q0 = 0;
-        for (int t0 = Tm.tid; t0 < R.nitem; t0 += 2 * Tm.nthr, q0 += 2) {
-            const int t1 = t0 + Tm.nthr;
-            const bool h1 = t1 < R.nitem;
+        for (int t0 = R.t0; t0 < R.t1; t0 += 2 * R.ts, q0 += 2) {
+            const int t1 = t0 + R.ts;
+            const bool h1 = t1 < R.t1;
             const int k0 = R.row(t0, q0);
             const int k1 = h1 ? R.row(t1, q0 + 1) : k0;
             const T y0 = row(k0, v);
@@ -1535,7 +1560,7 @@ struct CsrOp {
     YG_DEV int n2() const { return n; }
     YG_DEV void apply(Team& Tm, const double* v, double* y, const RowItems& R) const {
         int q = 0;
-        for (int t = Tm.tid; t < R.nitem; t += Tm.nthr, q++) {
+        for (int t = R.t0; t < R.t1; t += R.ts, q++) {
             const int k = R.row(t, q);
             y[k] = row(k, v);
         }
@@ -2212,15 +2237,20 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
     };
     int* s_item = g_item_cache;
     const int cache = (blockDim.x <= YG_ITEM_BLOCK) ? YG_ITEM_CACHE : 0;
+    // each CTA takes one contiguous chunk of the active-cell list (every SM of the
+    // team gets cells, and neighbouring threads take neighbouring cells)
+    const int chunk = (nact + Tm.ncta - 1) / Tm.ncta;
+    const int t_beg = min(Tm.cta * chunk, nact), t_end = min(t_beg + chunk, nact);
+    const int t0 = t_beg + (int)threadIdx.x, tstep = (int)blockDim.x;
     {
         int q = 0;
-        for (int t = tid; t < nact && q < cache; t += nthr, q++) s_item[q * blockDim.x + threadIdx.x] = (int)pack(t);
+        for (int t = t0; t < t_end && q < cache; t += tstep, q++) s_item[q * blockDim.x + threadIdx.x] = (int)pack(t);
     }
     // x of the active rows back to the plain array, then a team barrier (the
     // true-residual check and the caller read x at every row)
     auto flush_x = [&]() -> bool {
         int q = 0;
-        for (int t = tid; t < nact; t += nthr, q++) {
+        for (int t = t0; t < t_end; t += tstep, q++) {
             const unsigned pk = (q < cache) ? (unsigned)s_item[q * blockDim.x + threadIdx.x] : pack(t);
             const int c = (int)(pk & 0x3fffu) + nx * (int)((pk >> 14) & 0x3fffu);
             if (((pk >> 28) & 3u) != 1u) x[c] = st[2 * c + 1].x;
@@ -2303,7 +2333,7 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
             };
             const float* __restrict__ mcr = mc;
             int q = 0;
-            for (int t = tid; t < nact; t += nthr, q++) {
+            for (int t = t0; t < t_end; t += tstep, q++) {
                 const unsigned pk = (q < cache) ? (unsigned)s_item[q * blockDim.x + threadIdx.x] : pack(t);
                 const int i = (int)(pk & 0x3fffu), j = (int)((pk >> 14) & 0x3fffu);
                 const unsigned k0 = (pk >> 28) & 3u, k1 = pk >> 30;
@@ -2321,7 +2351,7 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
             // rows outside the interior stencil in a second pass: the calls stay
             // out of the main loop (whose live registers they would spill)
             q = 0;
-            for (int t = tid; t < nact; t += nthr, q++) {
+            for (int t = t0; t < t_end; t += tstep, q++) {
                 const unsigned pk = (q < cache) ? (unsigned)s_item[q * blockDim.x + threadIdx.x] : pack(t);
                 const unsigned k0 = (pk >> 28) & 3u, k1 = pk >> 30;
                 if (k0 != 2u && k1 != 2u) continue;
@@ -2452,7 +2482,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
         {
             const T beta = s_sc[2], om = s_sc[1];
             int q = 0;
-            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+            for (int e = R.t0; e < R.t1; e += R.ts, q++) {
                 const int u = R.row(e, q);
                 T pu = (it == 1) ? r[u] : r[u] + beta * (p[u] - om * v[u]);
                 p[u] = pu;
@@ -2466,7 +2496,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
         T tvp = T(0);
         {
             int q = 0;
-            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+            for (int e = R.t0; e < R.t1; e += R.ts, q++) {
                 const int u = R.row(e, q);
                 tvp += rt[u] * v[u];
             }
@@ -2487,7 +2517,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
         T ssp = T(0);
         {
             int q = 0;
-            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+            for (int e = R.t0; e < R.t1; e += R.ts, q++) {
                 const int u = R.row(e, q);
                 T su = r[u] - al * v[u];
                 s[u] = su;
@@ -2504,7 +2534,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
         T ts0 = T(0), ts1 = T(0);
         {
             int q = 0;
-            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+            for (int e = R.t0; e < R.t1; e += R.ts, q++) {
                 const int u = R.row(e, q);
                 const T tu = t[u];
                 ts0 += tu * s[u];
@@ -2530,7 +2560,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
         if (s_flag == 1) {
             relres = (double)s_sc[3];
             int q = 0;
-            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+            for (int e = R.t0; e < R.t1; e += R.ts, q++) {
                 const int u = R.row(e, q);
                 x[u] = x[u] + al * ph[u];
             }
@@ -2542,7 +2572,7 @@ __device__ __noinline__ int krylov_bicgstab(Team& Tm_, int nu, const Op& A, cons
         T rr0 = T(0), rr1 = T(0);
         {
             int q = 0;
-            for (int e = Tm.tid; e < R.nitem; e += Tm.nthr, q++) {
+            for (int e = R.t0; e < R.t1; e += R.ts, q++) {
                 const int u = R.row(e, q);
                 x[u] = x[u] + al * ph[u] + om * sh[u];
                 T ru = s[u] - om * t[u];
@@ -2961,7 +2991,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         // r64 = b - A64 x (FP64 residual of the outer iterate)
         A64.apply(T, I.x, I.q, R);
         double rr = 0.0;
-        for (int e = t_tid; e < R.nitem; e += t_nthr) {
+        for (int e = R.t0; e < R.t1; e += R.ts) {
             const int u = R.lookup(e);
             double ru = I.b[u] - I.q[u];
             I.r[u] = ru;
@@ -2976,7 +3006,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         if (total >= P.lin_maxiter) { status = YGPU_MAXITER; break; }
         // inner FP32 solve of A d = r, d0 = 0, scaled by ||r||
         const double nr = sqrt(rr), sc = 1.0 / nr;
-        for (int e = t_tid; e < R.nitem; e += t_nthr) {
+        for (int e = R.t0; e < R.t1; e += R.ts) {
             const int u = R.lookup(e);
             I.fr[u] = (float)(I.r[u] * sc);
             I.fx[u] = 0.0f;
@@ -3004,7 +3034,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         total += it;
         outer++;
         // x += d (FP64 accumulation)
-        for (int e = t_tid; e < R.nitem; e += t_nthr) {
+        for (int e = R.t0; e < R.t1; e += R.ts) {
             const int u = R.lookup(e);
             I.x[u] = I.x[u] + (double)I.fx[u] * nr;
         }
@@ -3803,7 +3833,7 @@ struct Adv5Op {
     }
     YG_DEV void apply(Team& Tm, const double* v, double* y, const RowItems& R) const {
         int q = 0;
-        for (int t = Tm.tid; t < R.nitem; t += Tm.nthr, q++) {
+        for (int t = R.t0; t < R.t1; t += R.ts, q++) {
             const int k = R.row(t, q);
             y[k] = row(k, v);
         }
