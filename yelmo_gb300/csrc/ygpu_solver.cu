@@ -2014,9 +2014,13 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, cons
     };
     int* s_item = g_item_cache;
     const int cache = (blockDim.x <= YG_ITEM_BLOCK) ? YG_ITEM_CACHE : 0;
+    // each CTA takes one contiguous chunk of the work items
+    const int chunk = (nitem + Tm.ncta - 1) / Tm.ncta;
+    const int t_beg = min(Tm.cta * chunk, nitem), t_end = min(t_beg + chunk, nitem);
+    const int t0 = t_beg + (int)threadIdx.x, tstep = (int)blockDim.x;
     {
         int q = 0;
-        for (int t = Tm.tid; t < nitem && q < cache; t += Tm.nthr, q++) s_item[q * blockDim.x + threadIdx.x] = item(t);
+        for (int t = t0; t < t_end && q < cache; t += tstep, q++) s_item[q * blockDim.x + threadIdx.x] = item(t);
     }
     int it = 0;
     for (int restart = 0; restart < 8; restart++) {
@@ -2109,7 +2113,7 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, cons
             // With an active-cell list the cells whose two rows are identity are
             // skipped: all their vectors are zero (m1 included) and x = b there.
             int q = 0;
-            for (int t = Tm.tid; t < nitem; t += Tm.nthr, q++) {
+            for (int t = t0; t < t_end; t += tstep, q++) {
                 const int k = (q < cache) ? s_item[q * blockDim.x + threadIdx.x] : item(t);
                 if (by_cell) {
                     const int j = k / A.nx(), i = k - j * A.nx();
