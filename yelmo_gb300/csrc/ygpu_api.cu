@@ -18,6 +18,7 @@
 #include <queue>
 #include <thread>
 #include <utility>
+#include <numeric>
 #include <vector>
 
 #include "ygpu_common.cuh"
@@ -722,13 +723,18 @@ static int solve_queue(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, co
                 return YGPU_ERR_CUDA;
             // the host vector must outlive the copy
             if (cudaStreamSynchronize(c->stream) != cudaSuccess) return YGPU_ERR_CUDA;
-            if (ygpu_step_shape_mapped(c->device, grid, c->d_map, sh) == YGPU_OK) return YGPU_OK;
+            if (ygpu_step_shape_mapped(c->device, grid, c->d_map, sh) == YGPU_OK) {
+                ygpu_step_shape_wide(sh, std::accumulate(nus.begin(), nus.end(), (size_t)0));
+                return YGPU_OK;
+            }
         }
         size_t mx = 0;
         for (size_t v : nus) mx = std::max(mx, v);
         int nt, tc;
         ygpu_choose_teams(c->max_ctas, (int)ids.size(), mx, &nt, &tc, c->unknowns_per_cta);
-        return ygpu_step_shape(c->device, nt, tc, sh);
+        const int r = ygpu_step_shape(c->device, nt, tc, sh);
+        if (r == YGPU_OK) ygpu_step_shape_wide(sh, std::accumulate(nus.begin(), nus.end(), (size_t)0));
+        return r;
     };
     while (next < n || !active.empty()) {
         // admit

@@ -31,7 +31,13 @@ struct StepShape {
     const int* kmap = nullptr;     // device team map of the Krylov step
     int kcl = 0;                   // > 0: the Krylov teams are thread-block clusters of kcl CTAs
                                    // (kgrid = clusters x kcl), see ygpu_krylov_cluster_plan
+    int wide_pre = 0;              // mixed pre step on the wide kernel (ygpu_step_shape_wide)
 };
+// The mixed pre step runs on 1024-thread CTAs (64 registers) when its CTAs hold
+// more than two cells per thread of the 512-thread kernel: twice the warps per SM
+// for the latency-bound passes; fewer cells leave the extra threads idle and the
+// register cap costs more than it saves. total_unknowns: of all the instances.
+void ygpu_step_shape_wide(StepShape* sh, size_t total_unknowns);
 // Cluster size and count for the Krylov step of n_inst instances: req CTAs per
 // cluster (2..16; anything else: no clusters), one instance per resident cluster
 // or the instances round-robin over the resident clusters. Returns the size (0:

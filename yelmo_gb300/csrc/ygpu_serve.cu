@@ -20,6 +20,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <numeric>
 #include <vector>
 
 #include "ygpu_common.cuh"
@@ -256,13 +257,18 @@ static int plan_shape(ygpu_server* S, int n, const std::vector<size_t>& nu, int*
         memcpy(h_map, map.data(), sizeof(int) * map.size());
         if (cudaMemcpyAsync(d_map, h_map, sizeof(int) * map.size(), cudaMemcpyHostToDevice, S->stream) != cudaSuccess)
             return YGPU_ERR_CUDA;
-        if (ygpu_step_shape_mapped(S->cfg.device, grid, d_map, sh) == YGPU_OK) return YGPU_OK;
+        if (ygpu_step_shape_mapped(S->cfg.device, grid, d_map, sh) == YGPU_OK) {
+            ygpu_step_shape_wide(sh, std::accumulate(nu.begin(), nu.end(), (size_t)0));
+            return YGPU_OK;
+        }
     }
     size_t max_nu = 0;
     for (size_t v : nu) max_nu = std::max(max_nu, v);
     int n_teams, team_ctas;
     ygpu_choose_teams(S->max_ctas, n, max_nu, &n_teams, &team_ctas);
-    return ygpu_step_shape(S->cfg.device, n_teams, team_ctas, sh);
+    const int r = ygpu_step_shape(S->cfg.device, n_teams, team_ctas, sh);
+    if (r == YGPU_OK) ygpu_step_shape_wide(sh, std::accumulate(nu.begin(), nu.end(), (size_t)0));
+    return r;
 }
 
 static int prepare_admitted(ygpu_server* S, const std::vector<Admit>& got) {

@@ -3567,6 +3567,13 @@ __global__ void __launch_bounds__(YG_PBLOCK, 1) ygpu_k_pre(const Inst* insts, in
                                                           TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
     run_step<YG_STEP_PRE>(insts, n_inst, P, ctls, tc, ab, dc, map);
 }
+// the same pre step on 1024-thread CTAs (64 registers), for batches whose CTAs
+// hold many cells (StepShape::wide_pre)
+#define YG_PBLOCK_W 1024
+__global__ void __launch_bounds__(YG_PBLOCK_W, 1) ygpu_k_pre_w(const Inst* insts, int n_inst, ygpu_dyn_par P,
+                                                          TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
+    run_step<YG_STEP_PRE>(insts, n_inst, P, ctls, tc, ab, dc, map);
+}
 // FP64 solves: the FP64 column pass needs the full register file (256 threads)
 __global__ void __launch_bounds__(YG_BLOCK, 1) ygpu_k_pre64(const Inst* insts, int n_inst, ygpu_dyn_par P,
                                                           TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
@@ -4057,6 +4064,10 @@ int ygpu_step_shape_mapped(int device, int grid, const int* d_map, StepShape* sh
     return YGPU_OK;
 }
 
+void ygpu_step_shape_wide(StepShape* sh, size_t total_unknowns) {
+    sh->wide_pre = (sh->grid > 0 && total_unknowns / 2 > (size_t)sh->grid * 2 * YG_PBLOCK) ? 1 : 0;
+}
+
 int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh) {
     sh->map = nullptr;
     sh->kmap = nullptr;
@@ -4255,6 +4266,9 @@ static int launch_step_raw(int step, cudaStream_t s, const StepShape& sh, const 
         case YG_STEP_SETUP:
             return coop((const void*)ygpu_k_setup, sh.grid, YG_BLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
         case YG_STEP_PRE:
+            if (P.precision == YGPU_PREC_MIXED && sh.wide_pre)
+                return coop((const void*)ygpu_k_pre_w, sh.grid, YG_PBLOCK_W, s, d_insts, n_inst, P, ctls, sh.team_ctas,
+                            d_abort, d_done, sh.map);
             if (P.precision == YGPU_PREC_MIXED)
                 return coop((const void*)ygpu_k_pre, sh.grid, YG_PBLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas,
                             d_abort, d_done, sh.map);
@@ -4357,6 +4371,7 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
     if (d_map) st = ygpu_step_shape_mapped(device, map_grid, d_map, &sh);
     else st = ygpu_step_shape(device, n_teams, team_ctas, &sh);
     if (st) return st;
+    ygpu_step_shape_wide(&sh, (size_t)n_inst * max_nu);
     // Krylov teams as thread-block clusters when every instance gets one resident cluster
     if (max_nu > 0) {
         int ncl = 0;
@@ -4479,7 +4494,8 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
 
 // Largest per-thread local memory (stack) of the step kernels, in bytes.
 size_t ygpu_solver_stack_bytes() {
-    const void* k[] = {(const void*)ygpu_k_setup, (const void*)ygpu_k_pre, (const void*)ygpu_k_pre64,
+    const void* k[] = {(const void*)ygpu_k_setup, (const void*)ygpu_k_pre, (const void*)ygpu_k_pre_w,
+                       (const void*)ygpu_k_pre64,
                        (const void*)ygpu_k_krylov, (const void*)ygpu_k_post, (const void*)ygpu_k_final};
     size_t m = 0;
     for (const void* f : k) {
@@ -4494,6 +4510,9 @@ int ygpu_solver_max_ctas(int device) {
     int nsm = 0, bps = 0, b2 = 0, b3 = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ygpu_k_pre, YG_PBLOCK, 0);
+    int bw = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bw, ygpu_k_pre_w, YG_PBLOCK_W, 0);
+    if (bw < bps) bps = bw;
     int b4 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b4, ygpu_k_pre64, YG_BLOCK, 0);
     if (b4 < bps) bps = b4;
