@@ -219,6 +219,24 @@ YG_DEV void nodes_aa(const Geo& G, const Nb& n, F val, A act, bool use_act, doub
     gq_nodes(c, v);
 }
 
+// e^(-1/3) for e > 0, the Glen n = 3 viscosity factor. FP32: the library's
+// rcbrtf. FP64: an FP32 seed refined by two Newton steps for y^-3 = e,
+// y <- y (4 - e y^3) / 3, which square the seed's relative error (about 1e-7)
+// each time, down to FP64 rounding, with a dozen FP64 operations on this part's
+// slow FP64 pipe.
+template <typename R>
+YG_DEV R rcbrt_visc(R e);
+template <>
+YG_DEV float rcbrt_visc<float>(float e) { return rcbrtf(e); }
+template <>
+YG_DEV double rcbrt_visc<double>(double e) {
+    double y = (double)rcbrtf((float)e);
+    const double third = 1.0 / 3.0;
+    y = y * (4.0 - e * (y * y * y)) * third;
+    y = y * (4.0 - e * (y * y * y)) * third;
+    return y;
+}
+
 // ---------------------------------------------------------------------------
 // Phase: horizontal strain rates at the faces of every cell
 // (calc_strain_rate_horizontal_2D, deformation.f90:1393-1507)
@@ -617,7 +635,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                         e = e + R(0.25) * (dvdzn[q] * dvdzn[q]);
                     }
                     e = e + eps0sq;
-                    R ep = glen3 ? rcbrt(e) : pow(e, p1);
+                    R ep = glen3 ? rcbrt_visc<R>(e) : pow(e, p1);
                     vn[q] = R(0.5) * ep * attp_r[((size_t)q * nz + k) * n2 + c];
                 }
                 v = (((vn[0] + vn[1]) + vn[2]) + vn[3]) / R(4);
@@ -637,7 +655,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                     e = e + R(0.25) * (dzyv * dzyv);
                 }
                 e = e + eps0sq;
-                R ep = glen3 ? rcbrt(e) : pow(e, p1);
+                R ep = glen3 ? rcbrt_visc<R>(e) : pow(e, p1);
                 v = R(0.5) * ep * attp_r[ck];
             }
             R vr;
@@ -2212,8 +2230,8 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
                                              float* __restrict__ r, float* __restrict__ u, float* m0, float* m1,
                                              float4* __restrict__ st, int maxiter, double tol, double bnrm,
                                              bool precond, int& iters, double& relres, bool& ok) {
-    TeamLocal tl_(Tm_);
-    Team& Tm = tl_.t;
+    // no register copy of the team here: the cell loop needs the registers
+    Team& Tm = Tm_;
     __shared__ float s_ab[3];      // alpha, beta, relres
     __shared__ int s_flag;         // 0 continue, 1 converged, 2 breakdown, 3 next coefficients broke down
     const bool lead = (threadIdx.x == 0);
