@@ -32,6 +32,8 @@ struct StepShape {
     int kcl = 0;                   // > 0: the Krylov teams are thread-block clusters of kcl CTAs
                                    // (kgrid = clusters x kcl), see ygpu_krylov_cluster_plan
     int wide_pre = 0;              // mixed pre step on the wide kernel (ygpu_step_shape_wide)
+    int kslots = 0;                // mixed Krylov step: cells per thread whose CG records stay in
+                                   // shared memory (ygpu_step_shape_wide sets it)
 };
 // The mixed pre step runs on 1024-thread CTAs (64 registers) when its CTAs hold
 // more than two cells per thread of the 512-thread kernel: twice the warps per SM

@@ -2221,6 +2221,21 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, cons
 // Only the operator input m (read at neighbouring cells) and the plain x, r, u
 // of the restarts and of the true-residual check live in plain arrays; x goes
 // back to its plain array whenever the recurrence stops. Needs nx, ny < 2^14.
+// Shared-memory row records of the FP32 cell CG: a thread's first S cells keep
+// their four float4 records (two per row) in dynamic shared memory for the whole
+// recurrence; slot (q, f) of a thread at (q * 4 + f) * blockDim.x + threadIdx.x
+// (consecutive threads on consecutive 16-byte words). S follows from the dynamic
+// shared memory of the launch (none: every record in global memory).
+#define YG_KREC_MAX 4
+extern __shared__ float4 g_krec[];
+YG_DEV int krec_slots() {
+    unsigned dsm;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dsm));
+    const int n = (int)(dsm / (4u * sizeof(float4) * blockDim.x));
+    return n < YG_KREC_MAX ? n : YG_KREC_MAX;
+}
+YG_DEV float4& krec(int q, int f) { return g_krec[(q * 4 + f) * blockDim.x + threadIdx.x]; }
+
 YG_DEV unsigned cell_pack(int i, int j, unsigned k0, unsigned k1) {
     return (unsigned)i | ((unsigned)j << 14) | (k0 << 28) | (k1 << 30);
 }
@@ -2264,6 +2279,7 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
     const int chunk = (nact + Tm.ncta - 1) / Tm.ncta;
     const int t_beg = min(Tm.cta * chunk, nact), t_end = min(t_beg + chunk, nact);
     const int t0 = t_beg + (int)threadIdx.x, tstep = (int)blockDim.x;
+    const int S = min(krec_slots(), cache);     // cells whose records stay in shared memory
     {
         int q = 0;
         for (int t = t0; t < t_end && q < cache; t += tstep, q++) s_item[q * blockDim.x + threadIdx.x] = (int)pack(t);
@@ -2275,8 +2291,8 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
         for (int t = t0; t < t_end; t += tstep, q++) {
             const unsigned pk = (q < cache) ? (unsigned)s_item[q * blockDim.x + threadIdx.x] : pack(t);
             const int c = (int)(pk & 0x3fffu) + nx * (int)((pk >> 14) & 0x3fffu);
-            if (((pk >> 28) & 3u) != 1u) x[c] = st[2 * c + 1].x;
-            if ((pk >> 30) != 1u) x[n2 + c] = st[2 * (n2 + c) + 1].x;
+            if (((pk >> 28) & 3u) != 1u) x[c] = (q < S) ? krec(q, 1).x : st[2 * c + 1].x;
+            if ((pk >> 30) != 1u) x[n2 + c] = (q < S) ? krec(q, 3).x : st[2 * (n2 + c) + 1].x;
         }
         return team_barrier(Tm);
     };
@@ -2328,6 +2344,17 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
         __syncthreads();
         if (s_flag == 1) { relres = (double)s_ab[2]; iters = it; return YGPU_OK; }
         if (s_flag == 2) { relres = (double)s_ab[2]; iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
+        // the first S cells' records into shared memory (their rows' records were
+        // written above by the row-strided pass, before the all-reduce)
+        {
+            int q = 0;
+            for (int t = t0; t < t_end && q < S; t += tstep, q++) {
+                const unsigned pk = (unsigned)s_item[q * blockDim.x + threadIdx.x];
+                const int c = (int)(pk & 0x3fffu) + nx * (int)((pk >> 14) & 0x3fffu);
+                krec(q, 0) = st[2 * c]; krec(q, 1) = st[2 * c + 1];
+                krec(q, 2) = st[2 * (n2 + c)]; krec(q, 3) = st[2 * (n2 + c) + 1];
+            }
+        }
         float* mc = m0;
         float* mn = m1;
         bool recheck = false;
@@ -2336,7 +2363,7 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
             const float a = s_ab[0], bt = s_ab[1];
             a0 = a1 = a2 = 0.0f;
             // one row's update from its records, operator value nk and m, M
-            auto update = [&](int k, float4& A0, float4& A1, float nk, float mk, float mi) {
+            auto update = [&](int k, float4& A0, float4& A1, float nk, float mk, float mi, float4* R0, float4* R1) {
                 // A0 = (z, q, s, p), A1 = (x, r, u, w)
                 const float zk = nk + bt * A0.x;
                 const float qk = mk + bt * A0.y;
@@ -2346,8 +2373,8 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
                 const float rk = A1.y - a * sk;
                 const float uk = A1.z - a * qk;
                 const float wk = A1.w - a * zk;
-                st[2 * k] = make_float4(zk, qk, sk, pk);
-                st[2 * k + 1] = make_float4(xk, rk, uk, wk);
+                *R0 = make_float4(zk, qk, sk, pk);
+                *R1 = make_float4(xk, rk, uk, wk);
                 mn[k] = mi * wk;
                 a0 += rk * uk;
                 a1 += wk * uk;
@@ -2363,12 +2390,17 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
                 if (k0 != 0u && k1 != 0u) continue;      // no interior-stencil row
                 float4 A0 = make_float4(0.f, 0.f, 0.f, 0.f), A1 = A0, B0 = A0, B1 = A0;
                 float m0v = 0.0f, m1v = 0.0f, i0 = 0.0f, i1 = 0.0f;
-                if (k0 == 0u) { A0 = st[2 * c]; A1 = st[2 * c + 1]; m0v = mcr[c]; i0 = Mi(c); }
-                if (k1 == 0u) { B0 = st[2 * c1]; B1 = st[2 * c1 + 1]; m1v = mcr[c1]; i1 = Mi(c1); }
+                const bool sh = q < S;
+                float4* ra0 = sh ? &krec(q, 0) : &st[2 * c];
+                float4* ra1 = sh ? &krec(q, 1) : &st[2 * c + 1];
+                float4* rb0 = sh ? &krec(q, 2) : &st[2 * c1];
+                float4* rb1 = sh ? &krec(q, 3) : &st[2 * c1 + 1];
+                if (k0 == 0u) { A0 = *ra0; A1 = *ra1; m0v = mcr[c]; i0 = Mi(c); }
+                if (k1 == 0u) { B0 = *rb0; B1 = *rb1; m1v = mcr[c1]; i1 = Mi(c1); }
                 float y0, y1;
                 energy_cell_fast<float, float>(Gv, Kv, cN, cNab, cdgx, cdgy, mcr, c, i, j, y0, y1);
-                if (k0 == 0u) update(c, A0, A1, y0, m0v, i0);
-                if (k1 == 0u) update(c1, B0, B1, y1, m1v, i1);
+                if (k0 == 0u) update(c, A0, A1, y0, m0v, i0, ra0, ra1);
+                if (k1 == 0u) update(c1, B0, B1, y1, m1v, i1, rb0, rb1);
             }
             // rows outside the interior stencil in a second pass: the calls stay
             // out of the main loop (whose live registers they would spill)
@@ -2382,9 +2414,11 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
                 for (int h = 0; h < 2; h++) {
                     if (((h == 0) ? k0 : k1) != 2u) continue;
                     const int k = c + h * n2;
-                    float4 R0 = st[2 * k], R1 = st[2 * k + 1];
+                    float4* p0 = (q < S) ? &krec(q, 2 * h) : &st[2 * k];
+                    float4* p1 = (q < S) ? &krec(q, 2 * h + 1) : &st[2 * k + 1];
+                    float4 R0 = *p0, R1 = *p1;
                     const float mk = mcr[k], mi = Mi(k);
-                    update(k, R0, R1, A.general(k, mc), mk, mi);
+                    update(k, R0, R1, A.general(k, mc), mk, mi, p0, p1);
                 }
             }
             it++;
@@ -4023,19 +4057,22 @@ int ygpu_csr_max_ctas(int device) {
 // ---------------------------------------------------------------------------
 static bool g_gqw_set[64] = {false};
 
-static int max_ctas_of(const void* kern, int block) {
+// dynamic shared memory of the FP32 cell CG's record slots
+static size_t krec_bytes(int slots) { return (size_t)slots * 4 * sizeof(float4) * YG_KBLOCK; }
+
+static int max_ctas_of(const void* kern, int block, size_t smem = 0) {
     int dev = 0, nsm = 0, bps = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, block, smem);
     return nsm * bps;
 }
 
 static int coop(const void* kern, int grid, int block, cudaStream_t s, const Inst* insts, int n_inst,
-                const ygpu_dyn_par& P, TeamCtl* ctls, int tc, int* ab, int* dc, const int* map) {
+                const ygpu_dyn_par& P, TeamCtl* ctls, int tc, int* ab, int* dc, const int* map, size_t smem = 0) {
     void* args[] = {(void*)&insts, (void*)&n_inst, (void*)&P, (void*)&ctls, (void*)&tc, (void*)&ab, (void*)&dc,
                     (void*)&map};
-    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), args, 0, s);
+    cudaError_t e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(block), args, smem, s);
     if (e != cudaSuccess) {
         ygpu_set_error("cooperative launch of a solver step failed: %s", cudaGetErrorString(e));
         return YGPU_ERR_CUDA;
@@ -4046,6 +4083,11 @@ static int coop(const void* kern, int grid, int block, cudaStream_t s, const Ins
 int ygpu_init_constants(int device) {
     if (device < 0 || device >= 64) return YGPU_OK;
     if (g_gqw_set[device]) return YGPU_OK;
+    if (cudaFuncSetAttribute((const void*)ygpu_k_krylov, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)krec_bytes(YG_KREC_MAX)) != cudaSuccess) {
+        ygpu_set_error("Krylov step: %zu bytes of dynamic shared memory refused", krec_bytes(YG_KREC_MAX));
+        return YGPU_ERR_CUDA;
+    }
     double w[4][4];
     const int sx[4] = {-1, 1, 1, -1}, sy[4] = {-1, -1, 1, 1};
     const double g = 1.0 / sqrt(3.0);
@@ -4071,7 +4113,7 @@ int ygpu_step_shape_mapped(int device, int grid, const int* d_map, StepShape* sh
     // must use a uniform shape
     static int kmax_dev[64];
     const int dslot = (device >= 0 && device < 64) ? device : 0;
-    if (kmax_dev[dslot] == 0) kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK);
+    if (kmax_dev[dslot] == 0) kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK, krec_bytes(YG_KREC_MAX));
     if (kmax_dev[dslot] < grid) return YGPU_ERR_BAD_ARG;
     sh->grid = grid;
     sh->team_ctas = 1;
@@ -4084,6 +4126,11 @@ int ygpu_step_shape_mapped(int device, int grid, const int* d_map, StepShape* sh
 
 void ygpu_step_shape_wide(StepShape* sh, size_t total_unknowns) {
     sh->wide_pre = (sh->grid > 0 && total_unknowns / 2 > (size_t)sh->grid * 2 * YG_PBLOCK) ? 1 : 0;
+    // shared-memory record slots of the FP32 cell CG: the cells per thread of the
+    // Krylov step, rounded up, at most YG_KREC_MAX
+    size_t per = 0;
+    if (sh->kgrid > 0) per = (total_unknowns / 2 + (size_t)sh->kgrid * YG_KBLOCK - 1) / ((size_t)sh->kgrid * YG_KBLOCK);
+    sh->kslots = (int)(per < YG_KREC_MAX ? per : YG_KREC_MAX);
 }
 
 int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh) {
@@ -4093,7 +4140,7 @@ int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh) {
     // teams (each CTA twice the threads), fewer teams if fewer CTAs are resident
     static int kmax_dev[64];
     const int dslot = (device >= 0 && device < 64) ? device : 0;
-    if (kmax_dev[dslot] == 0) kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK);
+    if (kmax_dev[dslot] == 0) kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK, krec_bytes(YG_KREC_MAX));
     const int kmax = kmax_dev[dslot];
     if (kmax < 1) {
         ygpu_set_error("Krylov kernel cannot be resident on device %d", device);
@@ -4294,7 +4341,8 @@ static int launch_step_raw(int step, cudaStream_t s, const StepShape& sh, const 
                         d_abort, d_done, sh.map);
         case YG_STEP_KRYLOV:
             if (sh.kcl > 0) return launch_cluster_krylov(s, sh, d_insts, n_inst, P, ctls, d_done, d_abort);
-            return coop((const void*)ygpu_k_krylov, sh.kgrid, YG_KBLOCK, s, d_insts, n_inst, P, ctls, sh.ktc, d_abort, d_done, sh.kmap);
+            return coop((const void*)ygpu_k_krylov, sh.kgrid, YG_KBLOCK, s, d_insts, n_inst, P, ctls, sh.ktc, d_abort, d_done,
+                        sh.kmap, P.precision == YGPU_PREC_MIXED ? krec_bytes(sh.kslots) : 0);
         case YG_STEP_POST:
             return coop((const void*)ygpu_k_post, sh.grid, YG_POBLOCK, s, d_insts, n_inst, P, ctls, sh.team_ctas, d_abort, d_done, sh.map);
         case YG_STEP_FINAL:
