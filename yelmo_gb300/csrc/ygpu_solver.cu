@@ -144,6 +144,9 @@ YG_DEV Nb make_nb(const Geo& G, int c) {
 #define CF_ACTX 2u     // x face active: f_ice == 1 on either side (acx ice mask)
 #define CF_ACTY 4u     // y face active
 #define CF_OCN 8u      // ice-free and z_bed < z_sl
+#define CF_PART 16u    // f_ice < 1
+#define CF_G0 32u      // f_grnd == 0
+#define CF_GPOS 64u    // f_grnd > 0
 YG_DEV unsigned char cell_flags(const Geo& G, const Inst& I, int c) {
     const Nb n = make_nb(G, c);
     const bool ice = (I.f_ice[c] == 1.0);
@@ -151,6 +154,9 @@ YG_DEV unsigned char cell_flags(const Geo& G, const Inst& I, int c) {
     if (ice || I.f_ice[CI(n.ip1, n.j)] == 1.0) fl |= CF_ACTX;
     if (ice || I.f_ice[CI(n.i, n.jp1)] == 1.0) fl |= CF_ACTY;
     if (!ice && I.z_bed[c] < I.z_sl[c]) fl |= CF_OCN;
+    if (I.f_ice[c] < 1.0) fl |= CF_PART;
+    if (I.f_grnd[c] == 0.0) fl |= CF_G0;
+    if (I.f_grnd[c] > 0.0) fl |= CF_GPOS;
     return (unsigned char)fl;
 }
 YG_DEV bool act_x(const Geo& G, const unsigned char* fl, int i, int j) { return (fl[CI(i, j)] & CF_ACTX) != 0; }
@@ -722,18 +728,22 @@ YG_DEV double stagger_beta_face(const Inst& I, const ygpu_dyn_par& P, const Geo&
     int im1, ip1, jm1, jp1;
     nbr_bc(i, j, G.nx, G.ny, G.bc, im1, ip1, jm1, jp1);
     const int c = CI(i, j), cn = xdir ? CI(ip1, j) : CI(i, jp1);
-    const double* fi = I.f_ice;
-    const double* fg = I.f_grnd;
+    // the f_ice and f_grnd tests from the cell flags (the same compares, made
+    // once by the setup step)
+    const unsigned fc = I.cflag[c], fn = I.cflag[cn];
+    const bool ice_c = (fc & CF_ICE) != 0, ice_n = (fn & CF_ICE) != 0;
+    const bool part_c = (fc & CF_PART) != 0, part_n = (fn & CF_PART) != 0;
+    const bool g0_c = (fc & CF_G0) != 0, g0_n = (fn & CF_G0) != 0;
     const double* be = I.beta;
     double b;
-    if (fg[c] == 0.0 && fg[cn] == 0.0) b = 0.0;
-    else if (fi[c] == 1.0 && fi[cn] < 1.0) b = be[c];
-    else if (fi[c] < 1.0 && fi[cn] == 1.0) b = be[cn];
+    if (g0_c && g0_n) b = 0.0;
+    else if (ice_c && part_n) b = be[c];
+    else if (part_c && ice_n) b = be[cn];
     else b = 0.5 * (be[c] + be[cn]);
     const int gs = P.beta_gl_stag;
-    if (gs >= 1 && gs <= 4 && fi[c] == 1.0 && fi[cn] == 1.0) {
-        const bool gl_r = (fg[c] > 0.0 && fg[cn] == 0.0);
-        const bool gl_l = (fg[c] == 0.0 && fg[cn] > 0.0);
+    if (gs >= 1 && gs <= 4 && ice_c && ice_n) {
+        const bool gl_r = ((fc & CF_GPOS) != 0) && g0_n;
+        const bool gl_l = g0_c && ((fn & CF_GPOS) != 0);
         if (gs == 1) {
             if (gl_r) b = be[c]; else if (gl_l) b = be[cn];
         } else if (gs == 2) {
@@ -759,12 +769,17 @@ YG_DEV double stagger_beta_face(const Inst& I, const ygpu_dyn_par& P, const Geo&
     return b;
 }
 
-YG_DEV void lim_face(double& k, double& r, double u, double uc, int mask, double s0, double inv_du, double tau_c) {
+// s0sq_lo: a bound below s0^2 (s0^2 (1 - 2^-40), rounded), so that a speed
+// square under it has sqrt(.) <= s0 and skips the FP64 square root
+YG_DEV void lim_face(double& k, double& r, double u, double uc, int mask, double s0, double s0sq_lo, double inv_du,
+                     double tau_c) {
     // calc_vel_lim_drag / lim_drag_face, solver_ssa_ac.f90:1095-1199
     k = 0.0;
     r = 0.0;
     if (mask < 1) return;
-    double s = sqrt(u * u + uc * uc);
+    const double a = u * u + uc * uc;
+    if (a <= s0sq_lo) return;
+    double s = sqrt(a);
     if (s <= s0) return;
     double x = (s - s0) * inv_du;
     double tau = tau_c * x * x;
@@ -787,6 +802,7 @@ __device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, c
     const bool drag = (P.ssa_vel_lim_method == YGPU_VEL_LIM_DRAG);
     const bool limit = (P.beta_method != -1 && P.beta_gl_stag != -1);
     const double s0 = 0.8 * P.ssa_vel_max;
+    const double s0sq_lo = (s0 * s0) * (1.0 - 0x1p-40);
     const double inv_du = 1.0 / (P.ssa_vel_max - s0);
     const int nx = G.nx, ny = G.ny;
     for (int c = tid; c < G.n2; c += nthr) {
@@ -852,11 +868,13 @@ __device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, c
             const double* ux = I.u_x;
             const double* uy = I.u_y;
             double uc = 0.25 * (uy[c] + uy[CI(n.ip1, j)] + uy[CI(i, n.jm1)] + uy[CI(n.ip1, n.jm1)]);
-            lim_face(kx, rx, ux[c], uc, mx, s0, inv_du, P.ssa_vel_lim_tau);
+            lim_face(kx, rx, ux[c], uc, mx, s0, s0sq_lo, inv_du, P.ssa_vel_lim_tau);
             uc = 0.25 * (ux[c] + ux[CI(n.im1, j)] + ux[CI(i, n.jp1)] + ux[CI(n.im1, n.jp1)]);
-            lim_face(ky, ry, uy[c], uc, my, s0, inv_du, P.ssa_vel_lim_tau);
+            lim_face(ky, ry, uy[c], uc, my, s0, s0sq_lo, inv_du, P.ssa_vel_lim_tau);
         }
-        I.lk_x[c] = kx; I.lk_y[c] = ky; I.lr_x[c] = rx; I.lr_y[c] = ry;
+        // the drag's right-hand-side terms (read by the system phase only with the
+        // drag on); kx, ky enter the operator coefficients below
+        if (drag) { I.lr_x[c] = rx; I.lr_y[c] = ry; }
         // operator drag coefficients: w*(beta + k) (* dx*dy for the energy form)
         R wx, wy, dgx, dgy;
         if (energy) {
@@ -2218,9 +2236,12 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, cons
 //  - a cell's state loads are issued before its stencil loads, which do not
 //    depend on them: one memory round trip per cell;
 //  - identity rows (Dirichlet or tied) are skipped: all their vectors stay 0.
-// Only the operator input m (read at neighbouring cells) and the plain x, r, u
-// of the restarts and of the true-residual check live in plain arrays; x goes
-// back to its plain array whenever the recurrence stops. Needs nx, ny < 2^14.
+// It is the inner solve of the mixed defect correction: A d = r64 * rs from
+// d = 0, and x64 += d * xs when the recurrence stops, with no true-residual
+// check or restart (the caller's next FP64 residual checks every correction).
+// r64 must be zero outside the non-identity rows of the active cells. Only the
+// operator input m and the first pass's u (both read at neighbouring cells) live
+// in plain arrays. Needs nx, ny < 2^14.
 // Shared-memory row records of the FP32 cell CG: a thread's first S cells keep
 // their four float4 records (two per row) in dynamic shared memory for the whole
 // recurrence; slot (q, f) of a thread at (q * 4 + f) * blockDim.x + threadIdx.x
@@ -2241,10 +2262,10 @@ YG_DEV unsigned cell_pack(int i, int j, unsigned k0, unsigned k1) {
 }
 template <typename Op>
 __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, const float* __restrict__ dinv,
-                                             float* __restrict__ x, const float* __restrict__ b,
-                                             float* __restrict__ r, float* __restrict__ u, float* m0, float* m1,
-                                             float4* __restrict__ st, int maxiter, double tol, double bnrm,
-                                             bool precond, int& iters, double& relres, bool& ok) {
+                                             double* __restrict__ x64, double xs, const double* __restrict__ r64,
+                                             double rs, float* __restrict__ u, float* m0, float* m1,
+                                             float4* __restrict__ st, int maxiter, double tol, bool precond,
+                                             int& iters, double& relres, bool& ok) {
     // no register copy of the team here: the cell loop needs the registers
     Team& Tm = Tm_;
     __shared__ float s_ab[3];      // alpha, beta, relres
@@ -2284,39 +2305,67 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
         int q = 0;
         for (int t = t0; t < t_end && q < cache; t += tstep, q++) s_item[q * blockDim.x + threadIdx.x] = (int)pack(t);
     }
-    // x of the active rows back to the plain array, then a team barrier (the
-    // true-residual check and the caller read x at every row)
+    // x64 += d * xs on the non-identity rows of the thread's cells (FP64
+    // accumulation), then a team barrier (the caller reads x64 at every row)
     auto flush_x = [&]() -> bool {
         int q = 0;
         for (int t = t0; t < t_end; t += tstep, q++) {
             const unsigned pk = (q < cache) ? (unsigned)s_item[q * blockDim.x + threadIdx.x] : pack(t);
             const int c = (int)(pk & 0x3fffu) + nx * (int)((pk >> 14) & 0x3fffu);
-            if (((pk >> 28) & 3u) != 1u) x[c] = (q < S) ? krec(q, 1).x : st[2 * c + 1].x;
-            if ((pk >> 30) != 1u) x[n2 + c] = (q < S) ? krec(q, 3).x : st[2 * (n2 + c) + 1].x;
+            if (((pk >> 28) & 3u) != 1u) {
+                const float d = (q < S) ? krec(q, 1).x : st[2 * c + 1].x;
+                x64[c] = x64[c] + (double)d * xs;
+            }
+            if ((pk >> 30) != 1u) {
+                const float d = (q < S) ? krec(q, 3).x : st[2 * (n2 + c) + 1].x;
+                x64[n2 + c] = x64[n2 + c] + (double)d * xs;
+            }
         }
         return team_barrier(Tm);
     };
     int it = 0;
-    for (int restart = 0; restart < 8; restart++) {
-        // r = b - A x, u = M r (every row)
-        for (int k = Tm.tid; k < nu; k += Tm.nthr) {
-            const float rk = b[k] - A.row(k, x);
-            r[k] = rk;
-            u[k] = Mi(k) * rk;
+    {
+        // u = M r with r = r64 * rs (d = 0: r is the right-hand side), m = 0, on
+        // every row (identity rows keep u = m = 0)
+        for (int k = tid; k < nu; k += nthr) {
+            u[k] = Mi(k) * (float)(r64[k] * rs);
+            m0[k] = 0.0f;
+            m1[k] = 0.0f;
         }
         if (!(ok = team_barrier(Tm))) return YGPU_ERR_TIMEOUT;
-        // w = A u, m = M w, the row records, partial dots
+        // w = A u on the non-identity rows of the thread's cells, m = M w, the
+        // row records (the first S cells' in shared memory), partial dots
         float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f;
-        for (int k = Tm.tid; k < nu; k += Tm.nthr) {
-            const float wk = A.row(k, u);
+        auto init = [&](int k, float wk, float4* R0, float4* R1) {
+            const float rk = (float)(r64[k] * rs), uk = u[k];
             m0[k] = Mi(k) * wk;
-            m1[k] = 0.0f;
-            const float rk = r[k], uk = u[k];
-            st[2 * k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            st[2 * k + 1] = make_float4(x[k], rk, uk, wk);
+            *R0 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            *R1 = make_float4(0.0f, rk, uk, wk);
             a0 += rk * uk;
             a1 += wk * uk;
             a2 += rk * rk;
+        };
+        {
+            int q = 0;
+            for (int t = t0; t < t_end; t += tstep, q++) {
+                const unsigned pk = (q < cache) ? (unsigned)s_item[q * blockDim.x + threadIdx.x] : pack(t);
+                const int i = (int)(pk & 0x3fffu), j = (int)((pk >> 14) & 0x3fffu);
+                const unsigned k0 = (pk >> 28) & 3u, k1 = pk >> 30;
+                const int c = i + nx * j, c1 = n2 + c;
+                const bool sh = q < S;
+                if (k0 == 0u || k1 == 0u) {
+                    float y0, y1;
+                    energy_cell_fast<float, float>(Gv, Kv, cN, cNab, cdgx, cdgy, u, c, i, j, y0, y1);
+                    if (k0 == 0u) init(c, y0, sh ? &krec(q, 0) : &st[2 * c], sh ? &krec(q, 1) : &st[2 * c + 1]);
+                    if (k1 == 0u) init(c1, y1, sh ? &krec(q, 2) : &st[2 * c1], sh ? &krec(q, 3) : &st[2 * c1 + 1]);
+                }
+#pragma unroll 1
+                for (int h = 0; h < 2; h++) {
+                    if (((h == 0) ? k0 : k1) != 2u) continue;
+                    const int k = c + h * n2;
+                    init(k, A.general(k, u), sh ? &krec(q, 2 * h) : &st[2 * k], sh ? &krec(q, 2 * h + 1) : &st[2 * k + 1]);
+                }
+            }
         }
         float red[3];
         {
@@ -2325,7 +2374,7 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
         }
         float gam_old = 1.0f, alpha_old = 1.0f;
         if (lead) {
-            const float rel = sqrtf(red[2]) / (float)bnrm;
+            const float rel = sqrtf(red[2]);     // the right-hand side has unit norm
             s_ab[2] = rel;
             if (rel <= (float)tol) s_flag = 1;
             else {
@@ -2344,20 +2393,9 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
         __syncthreads();
         if (s_flag == 1) { relres = (double)s_ab[2]; iters = it; return YGPU_OK; }
         if (s_flag == 2) { relres = (double)s_ab[2]; iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
-        // the first S cells' records into shared memory (their rows' records were
-        // written above by the row-strided pass, before the all-reduce)
-        {
-            int q = 0;
-            for (int t = t0; t < t_end && q < S; t += tstep, q++) {
-                const unsigned pk = (unsigned)s_item[q * blockDim.x + threadIdx.x];
-                const int c = (int)(pk & 0x3fffu) + nx * (int)((pk >> 14) & 0x3fffu);
-                krec(q, 0) = st[2 * c]; krec(q, 1) = st[2 * c + 1];
-                krec(q, 2) = st[2 * (n2 + c)]; krec(q, 3) = st[2 * (n2 + c) + 1];
-            }
-        }
         float* mc = m0;
         float* mn = m1;
-        bool recheck = false;
+        bool converged = false;
         int exit_st = YGPU_MAXITER;
         while (it < maxiter) {
             const float a = s_ab[0], bt = s_ab[1];
@@ -2428,7 +2466,7 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
             }
             { float* tt = mc; mc = mn; mn = tt; }
             if (lead) {
-                const float rel = sqrtf(red[2]) / (float)bnrm;
+                const float rel = sqrtf(red[2]);
                 s_ab[2] = rel;
                 if (!isfinite(rel)) s_flag = 2;
                 else if (rel <= (float)tol) s_flag = 1;
@@ -2451,7 +2489,7 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
             // __syncthreads, so every thread has read them by then
             const int flag = s_flag;
             if (flag == 2) { exit_st = YGPU_BREAKDOWN; break; }
-            if (flag == 1) { recheck = true; break; }
+            if (flag == 1) { converged = true; break; }
             if (flag == 3) {
                 if (it < maxiter) exit_st = YGPU_BREAKDOWN;
                 break;
@@ -2460,23 +2498,8 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
         relres = (double)s_ab[2];
         iters = it;
         if (!(ok = flush_x())) return YGPU_ERR_TIMEOUT;
-        if (!recheck) return exit_st;
-        // true residual check
-        float tr = 0.0f;
-        for (int k = Tm.tid; k < nu; k += Tm.nthr) {
-            const float rk = b[k] - A.row(k, x);
-            tr += rk * rk;
-        }
-        {
-            float trs;
-            if (!(ok = team_allreduce_w<float>(Tm, &tr, &trs, 1))) return YGPU_ERR_TIMEOUT;
-            tr = trs;
-        }
-        relres = (double)(sqrtf(tr) / (float)bnrm);
-        if (relres <= tol) return YGPU_OK;
-        if (it >= maxiter) return YGPU_MAXITER;
+        return converged ? YGPU_OK : exit_st;
     }
-    return YGPU_MAXITER;
 }
 
 // BiCGSTAB with Jacobi (van der Vorst 1992, as in the oracle). The scalar
@@ -3039,6 +3062,10 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
     // The outer passes visit the rows of the active cells only (identity rows
     // hold x = b, a zero residual and a zero correction, cleared here once).
     const RowItems R = make_row_items(T, I.acell, G.n2, G.nu, false);
+    // the FP32 cell CG reads the FP64 residual on every row (zero outside the
+    // active rows since the setup step) and adds its correction to x itself;
+    // the other inner solvers take FP32 copies
+    const bool cells = use_cg && !block && I.fst && G.nx <= (1 << 14) && G.ny <= (1 << 14);
     for (int u = t_tid; u < G.nu; u += t_nthr) {
         I.fr[u] = 0.0f;
         I.fx[u] = 0.0f;
@@ -3062,21 +3089,27 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         if (total >= P.lin_maxiter) { status = YGPU_MAXITER; break; }
         // inner FP32 solve of A d = r, d0 = 0, scaled by ||r||
         const double nr = sqrt(rr), sc = 1.0 / nr;
+        int it = 0;
+        double rel_in = 0.0;
+        int st;
+        if (cells) {
+            st = krylov_pcg_cells(T, G.nu, A32, I.fdinv, I.x, nr, I.r, sc, I.fv, I.fph, I.fm2, I.fst, inner_max,
+                                  inner_tol, pre, it, rel_in, ok);
+            if (!ok) return YGPU_ERR_TIMEOUT;
+            total += it;
+            outer++;
+            if (st == YGPU_BREAKDOWN && it <= 1) { status = YGPU_BREAKDOWN; break; }
+            continue;
+        }
         for (int e = R.t0; e < R.t1; e += R.ts) {
             const int u = R.lookup(e);
             I.fr[u] = (float)(I.r[u] * sc);
             I.fx[u] = 0.0f;
         }
         if (!(ok = team_barrier(T))) return YGPU_ERR_TIMEOUT;
-        int it = 0;
-        double rel_in = 0.0;
-        int st;
         if (use_cg && block)
             st = krylov_pcg_pipe_blk<float>(T, G, A32, I.fminv, I.fx, I.fr, I.frt, I.fv, I.ft, I.fph, I.fm2, I.fz,
                                             I.fq, I.fs, I.fp, inner_max, inner_tol, 1.0, it, rel_in, ok);
-        else if (use_cg && I.fst && G.nx <= (1 << 14) && G.ny <= (1 << 14))
-            st = krylov_pcg_cells(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.frt, I.fv, I.fph, I.fm2, I.fst, inner_max,
-                                  inner_tol, 1.0, pre, it, rel_in, ok);
         else if (use_cg)
             st = krylov_pcg_pipe<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.frt, I.fv, I.ft, I.fph, I.fm2, I.fz,
                                         I.fq, I.fs, I.fp, inner_max, inner_tol, 1.0, pre, it, rel_in, ok);
@@ -3104,12 +3137,26 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
 // ---------------------------------------------------------------------------
 // Phase: epilogue of one Picard iteration
 // ---------------------------------------------------------------------------
+// Magnitude tests of a double on the integer pipe: the magnitude bits order
+// like the absolute value, with inf above every finite bound and NaN above inf.
+// b is a positive finite bound.
+YG_DEV unsigned long long dmag(double v) { return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull; }
+YG_DEV unsigned long long dbits(double b) { return (unsigned long long)__double_as_longlong(b); }
+// fabs(v) < b (false for NaN)
+YG_DEV bool abs_lt(double v, double b) { return dmag(v) < dbits(b); }
+// fabs(v) > b (false for NaN)
+YG_DEV bool abs_gt(double v, double b) { const unsigned long long m = dmag(v); return m > dbits(b) && m <= 0x7ff0000000000000ull; }
+YG_DEV bool finite_d(double v) { return dmag(v) < 0x7ff0000000000000ull; }
+
 __device__ __noinline__ void phase_epilogue(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, bool diva, double red[4]) {
     const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
     const double lim = P.ssa_vel_max, rel = P.ssa_iter_rel;
     const double vel_tol = 1e-5;
-    double r1 = 0.0, r2 = 0.0, nchk = 0.0, nbad = 0.0;
+    // the tests and counts on the integer pipe (GB300's FP64 pipe is slow): the
+    // FP64 work left is the relaxation, the norm sums and the basal terms
+    double r1 = 0.0, r2 = 0.0;
+    int nchk = 0, nbad = 0;
     for (int c = t_tid; c < G.n2; c += t_nthr) {
         double uv[2];
 #pragma unroll
@@ -3122,38 +3169,34 @@ __device__ __noinline__ void phase_epilogue(const Inst& I, const ygpu_dyn_par& P
             }
             double val = I.x[src];
             // linear_solver_save_velocity: underflow flush
-            if (fabs(val) < TOL_UNDERFLOW) val = 0.0;
+            if (abs_lt(val, TOL_UNDERFLOW)) val = 0.0;
             // ssa_vel_clip (NaN passes through)
-            if (val > lim) val = lim;
-            if (val < -lim) val = -lim;
+            if (abs_gt(val, lim)) val = copysign(lim, val);
             // picard_relax_vel
             const double up = pl ? I.uy_nm1[c] : I.ux_nm1[c];
             val = up + rel * (val - up);
             uv[pl] = val;
             // picard_calc_convergence_l2 contributions
             const int mask = pl ? I.mask_y[c] : I.mask_x[c];
-            if (fabs(val) > vel_tol && mask > 0) {
-                nchk += 1.0;
+            if (abs_gt(val, vel_tol) && mask > 0) {
+                nchk++;
                 double t = val - up;
-                if (fabs(t) < TOL_UNDERFLOW) t = 0.0;
+                if (abs_lt(t, TOL_UNDERFLOW)) t = 0.0;
                 r1 += t * t;
                 t = up;
-                if (fabs(t) < TOL_UNDERFLOW) t = 0.0;
+                if (abs_lt(t, TOL_UNDERFLOW)) t = 0.0;
                 r2 += t * t;
             }
-            if (mask > 0 && !isfinite(val)) nbad += 1.0;
-            // picard_calc_convergence_l1rel_matrix
-            double err = (fabs(val) > 1e-2) ? 2.0 * fabs(val - up) / fabs(val + up + 1e-5) : 0.0;
-            if (pl) I.err_y[c] = err; else I.err_x[c] = err;
+            if (mask > 0 && !finite_d(val)) nbad++;
         }
         I.u_x[c] = uv[0];
         I.u_y[c] = uv[1];
         if (diva) {
             // calc_basal_stress (velocity_diva.f90:1011-1050) and calc_vel_basal (:960-1009)
             double tx = I.bm_x[c] * uv[0];
-            if (fabs(tx) < TOL_UNDERFLOW) tx = 0.0;
+            if (abs_lt(tx, TOL_UNDERFLOW)) tx = 0.0;
             double ty = I.bm_y[c] * uv[1];
-            if (fabs(ty) < TOL_UNDERFLOW) ty = 0.0;
+            if (abs_lt(ty, TOL_UNDERFLOW)) ty = 0.0;
             I.taub_x[c] = tx;
             I.taub_y[c] = ty;
             if (P.no_slip) {
@@ -3167,8 +3210,23 @@ __device__ __noinline__ void phase_epilogue(const Inst& I, const ygpu_dyn_par& P
     }
     red[0] = r1;
     red[1] = r2;
-    red[2] = nchk;
-    red[3] = nbad;
+    red[2] = (double)nchk;
+    red[3] = (double)nbad;
+}
+
+// picard_calc_convergence_l1rel_matrix of the last iteration (an output only):
+// from the relaxed velocity and the previous iterate, once the loop finishes
+__device__ __noinline__ void phase_err(const Inst& I, const Geo& G, Team& T) {
+    const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
+    for (int c = t_tid; c < G.n2; c += t_nthr) {
+#pragma unroll
+        for (int pl = 0; pl < 2; pl++) {
+            const double val = pl ? I.u_y[c] : I.u_x[c];
+            const double up = pl ? I.uy_nm1[c] : I.ux_nm1[c];
+            const double err = (fabs(val) > 1e-2) ? 2.0 * fabs(val - up) / fabs(val + up + 1e-5) : 0.0;
+            if (pl) I.err_y[c] = err; else I.err_x[c] = err;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -3269,6 +3327,12 @@ __device__ __noinline__ void step_setup(const Inst& I, const ygpu_dyn_par& P, Te
         I.err_x[c] = 1.0;
         I.err_y[c] = 1.0;
         I.cflag[c] = cell_flags(G, I, c);
+        // the mixed defect correction writes its FP64 residual on the active
+        // rows only; the FP32 cell CG reads it on every row
+        if (P.precision == YGPU_PREC_MIXED) {
+            I.r[c] = 0.0;
+            I.r[G.n2 + c] = 0.0;
+        }
         if (!diva) {
             // set_inactive_margins (velocity_general.f90:1687-1750), SSA only
             Nb n = make_nb(G, c);
@@ -3521,6 +3585,8 @@ __device__ __noinline__ void step_post(const Inst& I, const ygpu_dyn_par& P, Tea
         }
     }
     const double t6 = clk.lap();
+    // the last iteration's relative change (nothing on the device reads it)
+    if (finish && out->iter_now > 0) phase_err(I, G, T);
     if (finish && status == YGPU_OK) {
         if (!final_passes(I, P, G, T, diva, out->in_alt, out->iter_now > 0)) status = YGPU_ERR_TIMEOUT;
     }
