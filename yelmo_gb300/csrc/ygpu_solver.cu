@@ -538,6 +538,26 @@ __device__ __noinline__ void phase_shear(const Inst& I, const Geo& Gr, Team& T, 
     }
 }
 
+// The layer-independent part of the strain-rate invariant at the four
+// quadrature nodes of cell n: the horizontal terms, summed in the reference's
+// order (the layer loops add the shear terms and eps_0^2)
+template <typename R, typename SR>
+YG_DEV void node_strain_invariant(const Geo& G, const Nb& n, const SR* sdudx, const SR* sdudy, const SR* sdvdx,
+                                  const SR* sdvdy, const bool* ax, const bool* ay, R eb[4]) {
+    R dudxn[4], dudyn[4], dvdxn[4], dvdyn[4];
+    nodes_acx(G, n, [&](int a, int b) { return sdudx[CI(a, b)]; }, ax, dudxn);
+    nodes_acx(G, n, [&](int a, int b) { return sdudy[CI(a, b)]; }, ax, dudyn);
+    nodes_acy(G, n, [&](int a, int b) { return sdvdx[CI(a, b)]; }, ay, dvdxn);
+    nodes_acy(G, n, [&](int a, int b) { return sdvdy[CI(a, b)]; }, ay, dvdyn);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const R sh = dudyn[q] + dvdxn[q];
+        R e = dudxn[q] * dudxn[q] + dvdyn[q] * dvdyn[q];
+        e = e + dudxn[q] * dvdyn[q];
+        eb[q] = e + R(0.25) * (sh * sh);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Phase: column pass -- viscosity, relaxation, depth integrals, beta (aa)
 // R is the arithmetic of the viscosity (double: FP64 solve; float: mixed)
@@ -580,8 +600,9 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
         }
         const bool ice = (I.cflag[c] & CF_ICE) != 0;
         const double Hc = I.H[c];
-        // quadrature-node horizontal strain rates (independent of k)
-        R dudxn[4], dudyn[4], dvdxn[4], dvdyn[4];
+        // quadrature nodes: the layer-independent part of the strain-rate invariant
+        // (the horizontal terms, summed in the reference's order)
+        R eb[4];
         bool ax[6], ay[6];
         R e_aa = R(0);
         if (ice && vm == 1) {
@@ -590,10 +611,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
             ax[3] = act_x(G, fl, n.i, n.jm1); ax[4] = act_x(G, fl, n.i, n.j); ax[5] = act_x(G, fl, n.i, n.jp1);
             ay[0] = act_y(G, fl, n.im1, n.jm1); ay[1] = act_y(G, fl, n.i, n.jm1); ay[2] = act_y(G, fl, n.ip1, n.jm1);
             ay[3] = act_y(G, fl, n.im1, n.j); ay[4] = act_y(G, fl, n.i, n.j); ay[5] = act_y(G, fl, n.ip1, n.j);
-            nodes_acx(G, n, [&](int a, int b) { return sdudx[CI(a, b)]; }, ax, dudxn);
-            nodes_acx(G, n, [&](int a, int b) { return sdudy[CI(a, b)]; }, ax, dudyn);
-            nodes_acy(G, n, [&](int a, int b) { return sdvdx[CI(a, b)]; }, ay, dvdxn);
-            nodes_acy(G, n, [&](int a, int b) { return sdvdy[CI(a, b)]; }, ay, dvdyn);
+            node_strain_invariant<R>(G, n, sdudx, sdudy, sdvdx, sdvdy, ax, ay, eb);
         } else if (ice && vm == 2) {
             const double* ux = I.u_x;
             const double* uy = I.u_y;
@@ -632,10 +650,7 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
                 }
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    R sh = dudyn[q] + dvdxn[q];
-                    R e = dudxn[q] * dudxn[q] + dvdyn[q] * dvdyn[q];
-                    e = e + dudxn[q] * dvdyn[q];
-                    e = e + R(0.25) * (sh * sh);
+                    R e = eb[q];
                     if (diva) {
                         e = e + R(0.25) * (dudzn[q] * dudzn[q]);
                         e = e + R(0.25) * (dvdzn[q] * dvdzn[q]);
@@ -4125,6 +4140,20 @@ static bool g_gqw_set[64] = {false};
 
 // dynamic shared memory of the FP32 cell CG's record slots
 static size_t krec_bytes(int slots) { return (size_t)slots * 4 * sizeof(float4) * YG_KBLOCK; }
+// the Krylov kernel's dynamic shared memory limit, once per device (occupancy
+// queries with the record slots need it set)
+static bool set_smem_limits(int device) {
+    static bool done[64] = {false};
+    const int d = (device >= 0 && device < 64) ? device : 0;
+    if (done[d]) return true;
+    if (cudaFuncSetAttribute((const void*)ygpu_k_krylov, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)krec_bytes(YG_KREC_MAX)) != cudaSuccess) {
+        ygpu_set_error("step kernels: dynamic shared memory limits refused");
+        return false;
+    }
+    done[d] = true;
+    return true;
+}
 
 static int max_ctas_of(const void* kern, int block, size_t smem = 0) {
     int dev = 0, nsm = 0, bps = 0;
@@ -4149,11 +4178,7 @@ static int coop(const void* kern, int grid, int block, cudaStream_t s, const Ins
 int ygpu_init_constants(int device) {
     if (device < 0 || device >= 64) return YGPU_OK;
     if (g_gqw_set[device]) return YGPU_OK;
-    if (cudaFuncSetAttribute((const void*)ygpu_k_krylov, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)krec_bytes(YG_KREC_MAX)) != cudaSuccess) {
-        ygpu_set_error("Krylov step: %zu bytes of dynamic shared memory refused", krec_bytes(YG_KREC_MAX));
-        return YGPU_ERR_CUDA;
-    }
+    if (!set_smem_limits(device)) return YGPU_ERR_CUDA;
     double w[4][4];
     const int sx[4] = {-1, 1, 1, -1}, sy[4] = {-1, -1, 1, 1};
     const double g = 1.0 / sqrt(3.0);
@@ -4179,7 +4204,8 @@ int ygpu_step_shape_mapped(int device, int grid, const int* d_map, StepShape* sh
     // must use a uniform shape
     static int kmax_dev[64];
     const int dslot = (device >= 0 && device < 64) ? device : 0;
-    if (kmax_dev[dslot] == 0) kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK, krec_bytes(YG_KREC_MAX));
+    if (kmax_dev[dslot] == 0 && set_smem_limits(device))
+        kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK, krec_bytes(YG_KREC_MAX));
     if (kmax_dev[dslot] < grid) return YGPU_ERR_BAD_ARG;
     sh->grid = grid;
     sh->team_ctas = 1;
@@ -4206,7 +4232,8 @@ int ygpu_step_shape(int device, int n_teams, int team_ctas, StepShape* sh) {
     // teams (each CTA twice the threads), fewer teams if fewer CTAs are resident
     static int kmax_dev[64];
     const int dslot = (device >= 0 && device < 64) ? device : 0;
-    if (kmax_dev[dslot] == 0) kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK, krec_bytes(YG_KREC_MAX));
+    if (kmax_dev[dslot] == 0 && set_smem_limits(device))
+        kmax_dev[dslot] = max_ctas_of((const void*)ygpu_k_krylov, YG_KBLOCK, krec_bytes(YG_KREC_MAX));
     const int kmax = kmax_dev[dslot];
     if (kmax < 1) {
         ygpu_set_error("Krylov kernel cannot be resident on device %d", device);
