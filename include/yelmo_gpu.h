@@ -567,9 +567,11 @@ int ygpu_solve_batch_host(int kind, const ygpu_dyn_par* par, int n_inst, const y
  * GPU that loads the library until the process exits. Instances whose scratch
  * does not fit are rejected with YGPU_ERR_BAD_ARG (a 161x161x10 FP64 solve needs
  * about 24 MB). The first call on a device looks up the array's device address
- * and checks that the kernels' stack (about 1 KB per thread) fits the context's
- * stack limit, which it does not raise; make that first call before any stream
- * capture. All calls share the array and it keeps the last call's contents:
+ * and checks that the kernels' stack (up to about 1.3 KB per thread) fits the
+ * context's stack limit, which it does not raise. The call reads the count of finished
+ * solves back and synchronises its stream, so it cannot be recorded into a CUDA
+ * graph: on a stream that is being captured it returns YGPU_ERR_BAD_ARG and
+ * enqueues nothing. All calls share the array and it keeps the last call's contents:
  * calls that overlap on the GPU race, so serialise them. A neff hook is not run
  * here: with one set on the calling thread a DIVA solve returns YGPU_ERR_BAD_ARG.
  * stream is a cudaStream_t (NULL: the legacy default stream); the call returns

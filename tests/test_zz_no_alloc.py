@@ -15,6 +15,7 @@ here leaves every other test already run.
 import os
 import subprocess
 import sys
+import warnings
 
 import numpy as np
 import pytest
@@ -100,6 +101,38 @@ def test_noalloc_refuses_a_neff_hook():
     finally:
         L.ygpu_set_neff_hook(abi.NEFF_HOOK(), None)
     st, _ = _solve(lambda fl: gpu.solve_device_noalloc(abi.KIND_DIVA, inst.par, fl), inst, f0)
+    assert st["status"] == 0
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """The entry point synchronises its stream, which a capture forbids: on a
+    stream being captured it is refused before anything is enqueued, the capture
+    stays valid, and the same call on a plain stream afterwards solves."""
+    pytest.importorskip("torch")
+    import torch
+    inst = _instance()
+    f0 = gpu.prepare(inst)
+    dev = gpu.to_device(f0)
+    fields = gpu.make_fields(dev, inst.nx, inst.ny, inst.nz, inst.dx, inst.dx, inst.n_glen)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    err = None
+    with torch.cuda.stream(s):
+        g.capture_begin()
+        try:
+            gpu.solve_device_noalloc(abi.KIND_DIVA, inst.par, fields, stream=s.cuda_stream)
+        except gpu.YgpuError as e:
+            err = e
+        finally:
+            # the graph is empty (nothing was enqueued), which torch reports
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore")
+                g.capture_end()
+    assert err is not None and err.status == abi.ERR_BAD_ARG and "captured" in str(err)
+    torch.cuda.synchronize()
+    st = gpu.solve_device_noalloc(abi.KIND_DIVA, inst.par, fields, stream=s.cuda_stream)
+    torch.cuda.synchronize()
     assert st["status"] == 0
 
 

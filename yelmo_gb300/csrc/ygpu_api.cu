@@ -246,8 +246,8 @@ extern "C" ygpu_ctx* ygpu_ctx_create(int device) {
         delete c;
         return nullptr;
     }
-    // the step kernels' non-inlined phases take up to about 1 KB of stack per thread
-    // (ptxas' cumulative stack size), at the default limit: give them 4 KB
+    // the step kernels' non-inlined phases take up to about 1.3 KB of stack per
+    // thread (ptxas' cumulative stack size), above the default limit: give them 4 KB
     size_t stack = 0;
     cudaDeviceGetLimit(&stack, cudaLimitStackSize);
     if (stack < 4096) cudaDeviceSetLimit(cudaLimitStackSize, 4096);

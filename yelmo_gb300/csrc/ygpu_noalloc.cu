@@ -100,6 +100,18 @@ extern "C" int ygpu_solve_device_noalloc(int kind, const ygpu_dyn_par* par, cons
                        "(use ygpu_solve_device or ygpu_calc_velocity_diva, or clear the hook)");
         return YGPU_ERR_BAD_ARG;
     }
+    // the call reads the count of finished solves back and synchronises its
+    // stream, which a stream capture forbids: refuse before enqueueing anything
+    {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        const cudaError_t ce = cudaStreamIsCapturing((cudaStream_t)stream, &cs);
+        if (ce != cudaSuccess) cudaGetLastError();
+        if (ce != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+            ygpu_set_error("the stream is being captured: the allocation-free entry point synchronises its "
+                           "stream and cannot be recorded into a CUDA graph");
+            return YGPU_ERR_BAD_ARG;
+        }
+    }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) {

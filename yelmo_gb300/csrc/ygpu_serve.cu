@@ -425,8 +425,8 @@ extern "C" ygpu_server* ygpu_server_create(const ygpu_server_cfg* cfg) {
     if (cfg->kind != YGPU_KIND_SSA && cfg->kind != YGPU_KIND_DIVA) { ygpu_set_error("bad solver kind %d", cfg->kind); return nullptr; }
     if (cfg->dH_sigma < 0.0) { ygpu_set_error("dH_sigma must be >= 0"); return nullptr; }
     if (cudaSetDevice(cfg->device) != cudaSuccess) { ygpu_set_error("cannot use device %d", cfg->device); return nullptr; }
-    // the step kernels' non-inlined phases take up to about 1 KB of stack per thread
-    // (ptxas' cumulative stack size), at the default limit: give them 4 KB
+    // the step kernels' non-inlined phases take up to about 1.3 KB of stack per
+    // thread (ptxas' cumulative stack size), above the default limit: give them 4 KB
     size_t stack = 0;
     cudaDeviceGetLimit(&stack, cudaLimitStackSize);
     if (stack < 4096) cudaDeviceSetLimit(cudaLimitStackSize, 4096);

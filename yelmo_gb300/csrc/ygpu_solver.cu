@@ -159,6 +159,14 @@ YG_DEV unsigned char cell_flags(const Geo& G, const Inst& I, int c) {
     if (I.f_grnd[c] > 0.0) fl |= CF_GPOS;
     return (unsigned char)fl;
 }
+// calc_staggered_margin (velocity_diva.f90:1052-1082) with the f_ice tests read
+// from the cell flags of the two cells (the same compares, made by the setup step)
+template <typename T>
+YG_DEV T stag_margin_fl(T v0, T v1, unsigned f0, unsigned f1) {
+    if ((f0 & CF_ICE) && (f1 & CF_PART)) return v0;
+    if ((f0 & CF_PART) && (f1 & CF_ICE)) return v1;
+    return T(0.5) * (v0 + v1);
+}
 YG_DEV bool act_x(const Geo& G, const unsigned char* fl, int i, int j) { return (fl[CI(i, j)] & CF_ACTX) != 0; }
 YG_DEV bool act_y(const Geo& G, const unsigned char* fl, int i, int j) { return (fl[CI(i, j)] & CF_ACTY) != 0; }
 
@@ -241,6 +249,13 @@ YG_DEV double rcbrt_visc<double>(double e) {
     y = y * (4.0 - e * (y * y * y)) * third;
     y = y * (4.0 - e * (y * y * y)) * third;
     return y;
+}
+// a^(-1/3) for any a: the seeded Newton form where a is a normal FP32 number
+// (where the seed is), the library's FP64 rcbrt elsewhere (0, inf, NaN, tiny)
+YG_DEV double rcbrt_any(double a) {
+    const float af = (float)a;
+    if (af >= 1.17549435e-38f && af <= 3.4e38f) return rcbrt_visc<double>(a);
+    return rcbrt(a);
 }
 
 // ---------------------------------------------------------------------------
@@ -447,14 +462,14 @@ __device__ __noinline__ void phase_att_powers(const Inst& I, const ygpu_dyn_par&
                 nodes_aa(G, n, att, [](int, int) { return true; }, false, attn);
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    const double v = glen3 ? rcbrt(attn[q]) : pow(attn[q], p2);
+                    const double v = glen3 ? rcbrt_any(attn[q]) : pow(attn[q], p2);
                     const size_t o = ((size_t)q * nz + k) * n2 + c;
                     if (f32) af[o] = (float)v;
                     else I.attp[o] = v;
                 }
             } else {
                 const double a = I.ATT[(size_t)k * n2 + c];
-                const double v = glen3 ? rcbrt(a) : pow(a, p2);
+                const double v = glen3 ? rcbrt_any(a) : pow(a, p2);
                 if (f32) af[(size_t)k * n2 + c] = (float)v;
                 else I.attp[(size_t)k * n2 + c] = v;
             }
@@ -510,7 +525,6 @@ __device__ __noinline__ void phase_shear(const Inst& I, const Geo& Gr, Team& T, 
     const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const Geo G = Gr;
     const int nz = G.nz, n2 = G.n2;
-    const double* f = I.f_ice;
     float* sx32 = shear_f32(I, 0);
     float* sy32 = shear_f32(I, 1);
     const ZTab<R> zt(I.zeta, nz);
@@ -518,14 +532,14 @@ __device__ __noinline__ void phase_shear(const Inst& I, const Geo& Gr, Team& T, 
         Nb n = make_nb(G, c);
         const int cx = CI(n.ip1, n.j), cy = CI(n.i, n.jp1);
         const R tx = (R)I.taub_x[c], ty = (R)I.taub_y[c];
-        const double fc = f[c], fx = f[cx], fy = f[cy];
+        const unsigned fc = I.cflag[c], fx = I.cflag[cx], fy = I.cflag[cy];
         for (int k = 0; k < nz; k++) {
             const size_t o = (size_t)k * n2;
             const R omz = zt.omz(k);
             const R vc = (R)vcur[o + c];
-            R va = stag_margin<R>(vc, (R)vcur[o + cx], fc, fx);
+            R va = stag_margin_fl<R>(vc, (R)vcur[o + cx], fc, fx);
             const R gx = (va != R(0)) ? (tx / va) * omz : R(0);
-            va = stag_margin<R>(vc, (R)vcur[o + cy], fc, fy);
+            va = stag_margin_fl<R>(vc, (R)vcur[o + cy], fc, fy);
             const R gy = (va != R(0)) ? (ty / va) * omz : R(0);
             if (sizeof(R) == sizeof(float)) {
                 sx32[o + c] = (float)gx;
@@ -826,8 +840,9 @@ __device__ __noinline__ void phase_faces(const Inst& I, const ygpu_dyn_par& P, c
         // staggered F2 (stagger_F_integral, velocity_diva.f90:871-910)
         double F2x = 0.0, F2y = 0.0;
         if (diva) {
-            F2x = stag_margin(I.F2[c], I.F2[CI(n.ip1, j)], I.f_ice[c], I.f_ice[CI(n.ip1, j)]);
-            F2y = stag_margin(I.F2[c], I.F2[CI(i, n.jp1)], I.f_ice[c], I.f_ice[CI(i, n.jp1)]);
+            const unsigned fc = I.cflag[c];
+            F2x = stag_margin_fl(I.F2[c], I.F2[CI(n.ip1, j)], fc, (unsigned)I.cflag[CI(n.ip1, j)]);
+            F2y = stag_margin_fl(I.F2[c], I.F2[CI(i, n.jp1)], fc, (unsigned)I.cflag[CI(i, n.jp1)]);
             I.F2x[c] = F2x;
             I.F2y[c] = F2y;
         }
