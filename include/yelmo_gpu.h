@@ -71,8 +71,9 @@ extern "C" {
 #define YGPU_PRE_ILU0         2   /* "-p ilu". With BiCGSTAB on the residual form the GPU runs
                                      ILU(0) of the operator in a six-colour ordering (cell
                                      colour (i - j) mod 3, then the component), which needs
-                                     periodic directions in multiples of 3 cells (else Jacobi);
-                                     the other forms run what ygpu_stats.lin_precond_run says  */
+                                     periodic directions in multiples of 3 cells (else Jacobi),
+                                     with FP64 factors and BiCGSTAB in both precisions; the
+                                     other forms run what ygpu_stats.lin_precond_run says      */
 #define YGPU_PRE_TILE_BLOCK   3   /* run only (never parsed): block Jacobi with the exact inverse
                                      of each 4x4-cell tile block (32 unknowns, inverted in FP32),
                                      what "-p ilu" runs for CG on the energy form             */

@@ -346,7 +346,7 @@ size_t ygpu_inst_scratch_bytes(int nx, int ny, int nz, bool mixed, bool block, b
     b += al(n2);                         // cell flags
     if (mixed) b += 4 * al(n2 * 4) + 13 * al(nu * 4) + al(8 * nu * 4);   // + CG row records
     if (block) b += al(tile_blocks(nx, ny) * 1024 * 4);
-    if (ilu) b += al(YG_ILU_W * nu * 4) + al(YG_ILU_W * nu * (mixed ? 4 : 8)) + al(nu * (mixed ? 4 : 8));
+    if (ilu) b += al(YG_ILU_W * nu * 4) + al(YG_ILU_W * nu * 8) + al(nu * 8);   // FP64 factors in both modes
     return b;
 }
 
@@ -385,10 +385,8 @@ void ygpu_inst_scratch_carve(Inst& I, char* base, int nx, int ny, int nz, bool m
     I.icol = ilu ? Iv(YG_ILU_W * nu) : nullptr;
     I.ilu = I.ipiv = nullptr;
     I.filu = I.fipiv = nullptr;
-    if (ilu && mixed) {
-        I.filu = Fv(YG_ILU_W * nu);
-        I.fipiv = Fv(nu);
-    } else if (ilu) {
+    if (ilu) {
+        // -p ilu runs on the residual form, whose BiCGSTAB is FP64 in both modes
         I.ilu = D(YG_ILU_W * nu);
         I.ipiv = D(nu);
     }

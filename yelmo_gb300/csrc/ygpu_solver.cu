@@ -592,7 +592,6 @@ __device__ __noinline__ void phase_column(const Inst& I, const ygpu_dyn_par& P, 
     const R eps0sq = (R)(P.eps_0 * P.eps_0);
     const R rel = (R)P.ssa_iter_rel;
     const double* zeta = I.zeta;
-    const double* f = I.f_ice;
     const int vm = P.visc_method;
     // A^(-1/n) at the nodes and log(visc): FP32 storage in the mixed mode
     // restrict-qualified: the layer's loads do not wait for the previous layer's stores
@@ -1269,6 +1268,32 @@ YG_DEV int ilu_group(int nx, int n2, int u) {
     const int i = c % nx, j = c / nx;
     return 2 * (((i - j) % 3 + 3) % 3) + pl;
 }
+// The cells of colour gc, (i - j) mod 3 == gc, for a team of nthr threads.
+// With fewer threads than cells (batches), slot t = j * m + k holds cell
+// (i0(j) + 3 k, j), i0(j) = (j + gc) mod 3, m = ceil(nx / 3): no slot of another
+// colour, so every lane of a warp works. With a thread per cell (small single
+// solves) slot t is cell t, and the cells of other colours are skipped: their
+// lanes idle, but the colour's rows spread over three times as many warps,
+// which hides the FP64 latency of a row's elimination better (measured).
+// Returns -1 for a slot without a cell of colour gc.
+struct IluColour {
+    int nx, n2, m, slots;
+    bool compact;
+    YG_DEV IluColour(int nx_, int n2_, int nthr) : nx(nx_), n2(n2_) {
+        m = (nx + 2) / 3;
+        compact = nthr < n2;
+        slots = compact ? (n2 / nx) * m : n2;
+    }
+    YG_DEV int cell(int gc, int t) const {
+        if (!compact) {
+            const int j = t / nx, i = t - j * nx;
+            return (((i - j) % 3 + 3) % 3 == gc) ? t : -1;
+        }
+        const int j = t / m;
+        const int i = (j + gc) % 3 + 3 * (t - j * m);
+        return (i < nx) ? i + nx * j : -1;
+    }
+};
 // The coefficients of residual_row (same formulas) for row u: col[s] = -1 for
 // unused slots. Slots: 0 the diagonal, then the row's stencil in the order of
 // residual_row.
@@ -1370,9 +1395,11 @@ __device__ __noinline__ bool ilu_factor(const Inst& I, const Geo& G, Team& T_, c
     const int nx = G.nx, n2 = G.n2;
     const int tid = T_.tid, nthr = T_.nthr;
     int* icol = I.icol;
+    const IluColour cl(nx, n2, nthr);
     for (int gc = 0; gc < 3; gc++) {
-        for (int c = tid; c < n2; c += nthr) {
-            if (ilu_group(nx, n2, c) != 2 * gc) continue;
+        for (int t = tid; t < cl.slots; t += nthr) {
+            const int c = cl.cell(gc, t);
+            if (c < 0) continue;
 #pragma unroll 1
             for (int h = 0; h < 2; h++) {
                 const int u = c + h * n2;
@@ -1431,9 +1458,11 @@ YG_DEV bool ilu_apply(Team& T_, int nx, int n2, int nu, const int* __restrict__ 
                       const T* __restrict__ pivinv, const T* r, T* z) {
     (void)nu;
     const int tid = T_.tid, nthr = T_.nthr;
+    const IluColour cl(nx, n2, nthr);
     for (int gc = 0; gc < 3; gc++) {
-        for (int c = tid; c < n2; c += nthr) {
-            if (ilu_group(nx, n2, c) != 2 * gc) continue;
+        for (int t = tid; t < cl.slots; t += nthr) {
+            const int c = cl.cell(gc, t);
+            if (c < 0) continue;
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 const int u = c + h * n2, g = 2 * gc + h;
@@ -1451,8 +1480,9 @@ YG_DEV bool ilu_apply(Team& T_, int nx, int n2, int nu, const int* __restrict__ 
         if (!team_barrier(T_)) return false;
     }
     for (int gc = 2; gc >= 0; gc--) {
-        for (int c = tid; c < n2; c += nthr) {
-            if (ilu_group(nx, n2, c) != 2 * gc) continue;
+        for (int t = tid; t < cl.slots; t += nthr) {
+            const int c = cl.cell(gc, t);
+            if (c < 0) continue;
 #pragma unroll
             for (int h = 1; h >= 0; h--) {
                 const int u = c + h * n2, g = 2 * gc + h;
@@ -1871,6 +1901,13 @@ __device__ __noinline__ bool phase_classify(const Inst& I, const ygpu_dyn_par& P
 // ---------------------------------------------------------------------------
 // Phase: linear system -- rhs, start vector, Jacobi diagonal (FP64)
 // ---------------------------------------------------------------------------
+// -p ilu on the residual form: BiCGSTAB with the ILU(0) factors, in FP64 in both
+// precisions. Warm-started from the last Picard iterate it needs a few
+// iterations per linear solve, where the mixed mode's FP32 inner solves would
+// only add defect-correction steps (the FP32 coefficients stay as they are).
+YG_DEV bool krylov_fp64_ilu(const Inst& I, const ygpu_dyn_par& P, const Geo& G) {
+    return P.ssa_solver != YGPU_SSA_ENERGY && P.lin_precond == YGPU_PRE_ILU0 && I.icol && I.ilu && ilu_colourable(G);
+}
 __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, const Geo& G, Team& T, double& bnorm2) {
     const int t_tid = T.tid, t_nthr = T.nthr;   // registers: the Team lives in the stack frame
     const bool energy = (P.ssa_solver == YGPU_SSA_ENERGY);
@@ -1878,6 +1915,7 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
     const int n2 = G.n2, nx = G.nx, ny = G.ny;
     const double* N = I.visc_int;
     const OpK<double> K64 = make_opk<double>(G);
+    const bool ilu64 = krylov_fp64_ilu(I, P, G);     // the FP64 BiCGSTAB of -p ilu reads the FP64 diagonal too
     double bn2 = 0.0;
     for (int u = t_tid; u < G.nu; u += t_nthr) {
         const int pl = (u >= n2) ? 1 : 0, c = u - pl * n2;
@@ -1971,9 +2009,8 @@ __device__ __noinline__ void phase_system(const Inst& I, const ygpu_dyn_par& P, 
         if (I.fdinv) {
             const float df = (float)d;
             I.fdinv[u] = (df != 0.0f) ? 1.0f / df : 1.0f;
-        } else {
-            I.dinv[u] = (d != 0.0) ? 1.0 / d : 1.0;
         }
+        if (!I.fdinv || ilu64) I.dinv[u] = (d != 0.0) ? 1.0 / d : 1.0;
         bn2 += b * b;
     }
     bnorm2 = bn2;
@@ -3059,7 +3096,7 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
     outer = 0;
     const StencilOp<double, double> A64{&I, &G, energy, I.visc_int, I.Nab, I.drag_x, I.drag_y, make_opk<double>(G),
                                         I.acell};
-    if (P.precision != YGPU_PREC_MIXED) {
+    if (P.precision != YGPU_PREC_MIXED || krylov_fp64_ilu(I, P, G)) {
         // -p ilu on the energy form: the FP32 tile inverses (built by the pre step)
         // precondition the FP64 CG
         if (use_cg && energy && P.lin_precond == YGPU_PRE_ILU0 && I.fminv)
@@ -3143,12 +3180,9 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         else if (use_cg)
             st = krylov_pcg_pipe<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.frt, I.fv, I.ft, I.fph, I.fm2, I.fz,
                                         I.fq, I.fs, I.fp, inner_max, inner_tol, 1.0, pre, it, rel_in, ok);
-        else {
-            const IluM<float> M{G.nx, G.n2, I.icol, I.filu, I.fipiv};
-            const bool ilu = !energy && I.icol && I.filu && ilu_colourable(G);
+        else
             st = krylov_bicgstab<float>(T, G.nu, A32, I.fdinv, I.fx, I.fr, I.fz, I.frt, I.fp, I.fv, I.fs, I.ft, I.fph,
-                                        I.fsh, inner_max, inner_tol, 1.0, pre, it, rel_in, ok, ilu ? &M : nullptr);
-        }
+                                        I.fsh, inner_max, inner_tol, 1.0, pre, it, rel_in, ok);
         if (!ok) return YGPU_ERR_TIMEOUT;
         total += it;
         outer++;
@@ -3454,10 +3488,9 @@ __device__ __noinline__ void step_pre(const Inst& I, const ygpu_dyn_par& P, Team
         if (!team_barrier(T)) { status = YGPU_ERR_TIMEOUT; goto out_; }
     }
     if (I.icol && P.ssa_solver != YGPU_SSA_ENERGY && ilu_colourable(G)) {
-        // -p ilu on the residual form: the ILU(0) factors of this iteration's operator
-        const bool okf = mixed ? ilu_factor<float, float>(I, G, T, I.fN, I.fNab, I.fdrag_x, I.fdrag_y, I.filu, I.fipiv)
-                               : ilu_factor<double, double>(I, G, T, I.visc_int, I.Nab, I.drag_x, I.drag_y, I.ilu,
-                                                            I.ipiv);
+        // -p ilu on the residual form: the FP64 ILU(0) factors of this iteration's
+        // operator (the mixed mode's coefficients are its FP32 values widened)
+        const bool okf = ilu_factor<double, double>(I, G, T, I.visc_int, I.Nab, I.drag_x, I.drag_y, I.ilu, I.ipiv);
         if (!okf) { status = YGPU_ERR_TIMEOUT; goto out_; }
     }
     if (mixed) {
