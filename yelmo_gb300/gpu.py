@@ -500,7 +500,7 @@ def host_io_bytes(kind: int, nx: int, ny: int, nz: int):
 
 
 def algorithmic_bytes(stats: dict, kind: int, nx: int, ny: int, nz: int, mixed: bool, energy: bool = True,
-                      cg: bool = True, by_step: bool = False):
+                      cg: bool = True, by_step: bool = False, krylov64: bool = False, minimal: bool = False):
     """Algorithmic HBM bytes of one solve: every distinct array read once and
     written once per kernel pass, per cell (w = 8 B FP64, 4 B FP32):
 
@@ -519,6 +519,13 @@ def algorithmic_bytes(stats: dict, kind: int, nx: int, ny: int, nz: int, mixed: 
       Picard iteration;
     - post step, per Picard iteration: epilogue 16w+8.
 
+    krylov64: the mixed mode's Krylov step runs in FP64 (BiCGSTAB with ILU(0) on
+    the residual form). minimal: the Krylov bytes of the least-traffic form of the
+    same method instead, per active cell and iteration: plain PCG 23w (per row the
+    operator input, the coefficients' share and the output, x, r and p read and
+    written, the preconditioner read and z written), BiCGSTAB 36w (two operator
+    applies and the eight vector updates, each vector read or written once).
+
     Returns the total, or {step: bytes} with by_step."""
     n2 = nx * ny
     w = 8
@@ -527,8 +534,11 @@ def algorithmic_bytes(stats: dict, kind: int, nx: int, ny: int, nz: int, mixed: 
     col = (3 * nz + (14 if kind == abi.KIND_DIVA else 10)) * w
     pre = 7 * w + col + (20 * w + 8) + (16 * w + 8)
     post = 16 * w + 8
-    wk = 4 if mixed else 8
-    it_bytes = (42 * wk + 8) if cg else (62 * wk + 16)
+    wk = 4 if (mixed and not krylov64) else 8
+    if minimal:
+        it_bytes = (23 * wk) if cg else (36 * wk)
+    else:
+        it_bytes = (42 * wk + 8) if cg else (62 * wk + 16)
     n_act = stats.get("active_cells") or n2
     krylov = float(n_act) * lin * it_bytes
     if mixed:
