@@ -2081,6 +2081,23 @@ __device__ __noinline__ int krylov_cg(Team& Tm_, int nu, const Op& A, const CT* 
 // the tolerance; if the true residual is above it, the recursion restarts from
 // the true residual.
 
+// 1/b for the recurrence scalars of the Krylov methods. FP32: the division.
+// FP64: the FP32 reciprocal refined by two Newton steps, y <- y + y (1 - b y),
+// each squaring the relative error (about 1e-7 from the seed), to within a few
+// ulp in about six dependent operations where the IEEE division takes a longer
+// chain on this part's FP64 pipe; the division where b is outside FP32's
+// normal range.
+YG_DEV float scalar_rcp(float b) { return 1.0f / b; }
+YG_DEV double scalar_rcp(double b) {
+    const float bf = fabsf((float)b);
+    if (!(bf >= 1.17549435e-38f && bf <= 3.4e38f)) return 1.0 / b;
+    double y = (double)__frcp_rn((float)b);
+    double e = fma(-b, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-b, y, 1.0);
+    return fma(y, e, y);
+}
+
 template <typename T, typename Op, typename CT>
 __device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, const CT* __restrict__ dinv,
                                             T* __restrict__ x, const T* __restrict__ b, T* __restrict__ r,
@@ -2155,28 +2172,34 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, cons
             const T part[3] = {a0, a1, a2};
             if (!(ok = team_allreduce_w<T>(Tm, part, red, 3))) return YGPU_ERR_TIMEOUT;
         }
-        // lead thread: gam_old / alpha_old of the recurrence
-        W gam_old = W(1), alpha_old = W(1);
+        // lead thread: the reciprocals of gam and alpha carried by the recurrence
+        // (alpha = gam / t with t = del - beta gam / alpha_old, so 1 / alpha =
+        // t / gam); s_ab[2] holds ||r||^2, compared with (tol ||b||)^2
+        W inv_gam_old = W(1), inv_alpha_old = W(1);
+        const W tol2 = ((W)tol * (W)bnrm) * ((W)tol * (W)bnrm);
+        auto rel_of = [&](W rr) -> double { return (double)(sqrt(rr) / (W)bnrm); };
         if (lead) {
-            const W rel = sqrt(red[2]) / (W)bnrm;
-            s_ab[2] = rel;
-            if (rel <= (W)tol) s_flag = 1;
+            const W rr = red[2];
+            s_ab[2] = rr;
+            // a non-finite norm (an Inf or NaN right-hand side) breaks down below
+            if (isfinite(rr) && rr <= tol2) s_flag = 1;
             else {
                 const W gam = red[0], del = red[1];
-                const W alpha = gam / del;
+                const W inv_gam = scalar_rcp(gam);
+                const W alpha = gam * scalar_rcp(del);
                 if (!isfinite(alpha) || del == W(0)) s_flag = 2;
                 else {
                     s_flag = 0;
                     s_ab[0] = alpha;
                     s_ab[1] = W(0);
-                    gam_old = gam;
-                    alpha_old = alpha;
+                    inv_gam_old = inv_gam;
+                    inv_alpha_old = del * inv_gam;
                 }
             }
         }
         __syncthreads();
-        if (s_flag == 1) { relres = (double)s_ab[2]; iters = it; return YGPU_OK; }
-        if (s_flag == 2) { relres = (double)s_ab[2]; iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
+        if (s_flag == 1) { relres = rel_of(s_ab[2]); iters = it; return YGPU_OK; }
+        if (s_flag == 2) { relres = rel_of(s_ab[2]); iters = it; return (it < maxiter) ? YGPU_BREAKDOWN : YGPU_MAXITER; }
         T* mc = m0;
         T* mn = m1;
         bool recheck = false;
@@ -2239,22 +2262,25 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, cons
             { T* t = mc; mc = mn; mn = t; }
             if (lead) {
                 // FP32 inner solves: the recurrence scalars in FP32 (its division
-                // and square root are far faster than FP64's on this part)
-                const W rel = sqrt(red[2]) / (W)bnrm;
-                s_ab[2] = rel;
-                if (!isfinite(rel)) s_flag = 2;
-                else if (rel <= (W)tol) s_flag = 1;
+                // and square root are far faster than FP64's on this part); FP64:
+                // two independent reciprocals, no division or square root
+                const W rr = red[2];
+                s_ab[2] = rr;
+                if (!isfinite(rr)) s_flag = 2;
+                else if (rr <= tol2) s_flag = 1;
                 else {
                     const W gam = red[0], del = red[1];
-                    const W beta = gam / gam_old;
-                    const W alpha = gam / (del - beta * gam / alpha_old);
+                    const W inv_gam = scalar_rcp(gam);
+                    const W beta = gam * inv_gam_old;
+                    const W t = del - beta * gam * inv_alpha_old;
+                    const W alpha = gam * scalar_rcp(t);
                     if (!isfinite(alpha) || !isfinite(beta) || del == W(0)) s_flag = 3;
                     else {
                         s_flag = 0;
                         s_ab[0] = alpha;
                         s_ab[1] = beta;
-                        gam_old = gam;
-                        alpha_old = alpha;
+                        inv_gam_old = inv_gam;
+                        inv_alpha_old = t * inv_gam;
                     }
                 }
             }
@@ -2262,7 +2288,7 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, cons
             // s_flag / s_ab are rewritten only after the next all-reduce's first
             // __syncthreads, so every thread has read them by then
             const int flag = s_flag;
-            if (flag != 0) relres = (double)s_ab[2];
+            if (flag != 0) relres = rel_of(s_ab[2]);
             if (flag == 2) { iters = it; return YGPU_BREAKDOWN; }
             if (flag == 1) { recheck = true; break; }
             if (flag == 3) {
@@ -2272,7 +2298,7 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, cons
             }
         }
         iters = it;
-        relres = (double)s_ab[2];
+        relres = rel_of(s_ab[2]);
         if (!recheck) return YGPU_MAXITER;
         // true residual check (in T, as the recurrence)
         T tr = T(0);
