@@ -453,7 +453,7 @@ def run_reference(args, insts, rank, world):
 
 def cpu_baseline_leg(inst, budget_s=20.0):
     """Oracle timed on the host cores (bounded sample), and its tightly converged
-    solution, the checker of the GPU results."""
+    solution, against which the GPU results are compared."""
     import oracle
     cores = os.cpu_count() or 1
     flags = oracle.timing_flags()

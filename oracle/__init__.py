@@ -22,7 +22,7 @@ _use_fast = False
 
 
 def build(force: bool = False) -> str:
-    """Compile liboracle.so (the checker) and liboracle_fast.so (the timed CPU
+    """Compile liboracle.so (the oracle the tests compare with) and liboracle_fast.so (the timed CPU
     baseline) with the Makefile beside this file."""
     src = os.path.getmtime(os.path.join(HERE, "yelmo_oracle.c"))
     if force or any(not os.path.exists(p) or os.path.getmtime(p) < src for p in (LIB_PATH, FAST_LIB_PATH)):
@@ -39,7 +39,7 @@ def timing_flags() -> str:
 class timing_build:
     """Context manager: the oracle calls inside it run liboracle_fast.so (-O3,
     tuned for the host CPU, FMA contraction), the build the CPU baseline times;
-    outside it they run the checker build."""
+    outside it they run the reference build (liboracle.so)."""
 
     def __enter__(self):
         global _use_fast

@@ -1,7 +1,7 @@
 /*
  * yelmo_oracle.c -- CPU FP64 restatement of Yelmo's SSA/DIVA velocity solve.
  *
- * TEST INFRASTRUCTURE ONLY (the checker): used by tests/, the smoke check of
+ * TEST INFRASTRUCTURE ONLY (the oracle): used by tests/, the smoke check of
  * __graft_entry__.py and the CPU-baseline leg of bench.py. The GPU library
  * never links or calls this file. See yelmo_oracle.h for provenance and pinning.
  *

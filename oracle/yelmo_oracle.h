@@ -1,7 +1,7 @@
 /*
  * yelmo_oracle.h -- CPU FP64 restatement of Yelmo's SSA/DIVA velocity solve.
  *
- * TEST INFRASTRUCTURE ONLY. This is the checker of the GPU solver: only the
+ * TEST INFRASTRUCTURE ONLY. This is the oracle of the GPU solver: only the
  * tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it. The
  * product (libyelmo_gpu.so) never links or calls it.
  *
