@@ -165,6 +165,9 @@ struct ygpu_ctx {
     size_t fbuf_cap = 0;
     char* hbuf = nullptr;           // pinned host mirror of fbuf
     size_t hbuf_cap = 0;
+    char* dpieces = nullptr;        // copy list of the direct host<->device copies
+    size_t dpieces_cap = 0;
+    int pageable = -1;              // the device reads and writes pageable host memory (-1: not asked yet)
     Inst* d_insts = nullptr;
     int insts_cap = 0;
     InstOut* d_out = nullptr;
@@ -264,6 +267,7 @@ extern "C" void ygpu_ctx_destroy(ygpu_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->arena);
     cudaFree(c->fbuf);
+    if (c->dpieces) cudaFree(c->dpieces);
     if (c->hbuf) cudaFreeHost(c->hbuf);
     cudaFree(c->d_insts);
     cudaFree(c->d_out);
@@ -913,16 +917,77 @@ static void copy_segments(const std::vector<Seg>& segs) {
     for (auto& t : th) t.join();
 }
 
-// Host staging of the host-pointer entries. The arrays are packed into one
-// pinned host buffer, in the order in-only, in/out, out-only, then device-only
-// scratch, mirrored by the device buffer: the inputs go up in one copy and the
-// results come back in one.
+// A copy list entry of the direct host<->device copies: one piece of at most
+// YG_PIECE bytes of one array.
+struct CopyPiece {
+    const char* src;
+    char* dst;
+    unsigned long long n;
+};
+#define YG_PIECE (256u << 10)
+// One CTA per piece (grid-stride over the list): 16-byte words where both
+// addresses are 16-byte aligned, else 4-byte words (every array here holds
+// 4- or 8-byte elements), then the tail bytes.
+__global__ void __launch_bounds__(512) k_copy_pieces(const CopyPiece* __restrict__ list, int n) {
+    for (int b = blockIdx.x; b < n; b += gridDim.x) {
+        const CopyPiece q = list[b];
+        unsigned long long done = 0;
+        if ((((unsigned long long)q.src | (unsigned long long)q.dst) & 15ull) == 0) {
+            const unsigned long long w = q.n / 16;
+            const uint4* s = (const uint4*)q.src;
+            uint4* d = (uint4*)q.dst;
+            for (unsigned long long i = threadIdx.x; i < w; i += blockDim.x) d[i] = s[i];
+            done = w * 16;
+        } else if ((((unsigned long long)q.src | (unsigned long long)q.dst) & 3ull) == 0) {
+            const unsigned long long w = q.n / 4;
+            const unsigned* s = (const unsigned*)q.src;
+            unsigned* d = (unsigned*)q.dst;
+            for (unsigned long long i = threadIdx.x; i < w; i += blockDim.x) d[i] = s[i];
+            done = w * 4;
+        }
+        for (unsigned long long i = done + threadIdx.x; i < q.n; i += blockDim.x) q.dst[i] = q.src[i];
+    }
+}
+
+// Host staging of the host-pointer entries. The device buffer holds the arrays in
+// the order in-only, in/out, out-only, then device-only scratch. Where the device
+// reads and writes pageable host memory itself (cudaDevAttrPageableMemoryAccess,
+// the coherent host-device link of Grace-based parts), one kernel gathers the
+// inputs from the caller's arrays and one scatters the results back: no host copy
+// at all. Elsewhere the arrays are packed into a pinned mirror: the inputs go up
+// in one copy and the results come back in one.
 struct Staging {
     std::vector<HostArg> args;
     size_t up = 0, down = 0, dend = 0, tot = 0;   // [0, up) goes up, [down, dend) comes back; scratch after
+    bool direct = false;
     size_t add(void* h, size_t bytes, bool in, bool out) {
         args.push_back({h, bytes, in, out, nullptr, 0});
         return args.size() - 1;
+    }
+    // the pieces of the arrays of one direction, copied by one kernel on the stream
+    int copy_direct(ygpu_ctx* c, bool to_device) {
+        std::vector<CopyPiece> list;
+        for (auto& a : args) {
+            if (to_device ? !a.in : !a.out) continue;
+            char* dev = c->fbuf + a.off;
+            char* host = (char*)a.host;
+            for (size_t o = 0; o < a.bytes; o += YG_PIECE) {
+                const size_t n = std::min((size_t)YG_PIECE, a.bytes - o);
+                list.push_back(to_device ? CopyPiece{host + o, dev + o, n} : CopyPiece{dev + o, host + o, n});
+            }
+        }
+        if (list.empty()) return YGPU_OK;
+        const size_t lb = list.size() * sizeof(CopyPiece);
+        int st = grow(&c->dpieces, &c->dpieces_cap, lb);
+        if (st) return st;
+        // the list goes up from pageable memory: the call returns once it is staged
+        CK(cudaMemcpyAsync(c->dpieces, list.data(), lb, cudaMemcpyHostToDevice, c->stream));
+        const int grid = std::min((int)list.size(), 4 * std::max(c->sms, 1));
+        k_copy_pieces<<<grid, 512, 0, c->stream>>>((const CopyPiece*)c->dpieces, (int)list.size());
+        CK(cudaGetLastError());
+        // the next call may rewrite the list: it waits for this copy first
+        CK(cudaStreamSynchronize(c->stream));
+        return YGPU_OK;
     }
     int upload(ygpu_ctx* c) {
         size_t off = 0;
@@ -940,6 +1005,17 @@ struct Staging {
         tot = off;
         int st = grow(&c->fbuf, &c->fbuf_cap, tot);
         if (st) return st;
+        if (c->pageable < 0) {
+            int v = 0;
+            c->pageable = (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, c->device) == cudaSuccess && v == 1)
+                              ? 1 : 0;
+            cudaGetLastError();
+        }
+        direct = (c->pageable == 1);
+        if (direct) {
+            for (auto& a : args) a.dev = c->fbuf + a.off;
+            return copy_direct(c, true);
+        }
         if (c->hbuf_cap < dend) {          // the pinned mirror leaves the scratch out
             if (c->hbuf) cudaFreeHost(c->hbuf);
             c->hbuf = nullptr;
@@ -962,6 +1038,7 @@ struct Staging {
         return YGPU_OK;
     }
     int download(ygpu_ctx* c) {
+        if (direct) return copy_direct(c, false);
         if (dend > down) CK(cudaMemcpyAsync(c->hbuf + down, c->fbuf + down, dend - down, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         std::vector<Seg> segs;
