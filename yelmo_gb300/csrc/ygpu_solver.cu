@@ -2332,8 +2332,6 @@ __device__ __noinline__ int krylov_pcg_pipe(Team& Tm_, int nu, const Op& A, cons
 // It is the inner solve of the mixed defect correction: A d = r64 * rs from
 // d = 0, and x64 += d * xs when the recurrence stops, with no true-residual
 // check or restart (the caller's next FP64 residual checks every correction).
-// It runs to tol; a tol below tol_std is a bid to finish the linear solve in
-// this step, abandoned after as many iterations again as tol_std took.
 // r64 must be zero outside the non-identity rows of the active cells. Only the
 // operator input m and the first pass's u (both read at neighbouring cells) live
 // in plain arrays. Needs nx, ny < 2^14.
@@ -2359,8 +2357,8 @@ template <typename Op>
 __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, const float* __restrict__ dinv,
                                              double* __restrict__ x64, double xs, const double* __restrict__ r64,
                                              double rs, float* __restrict__ u, float* m0, float* m1,
-                                             float4* __restrict__ st, int maxiter, double tol, double tol_std,
-                                             bool precond, int& iters, double& relres, bool& ok) {
+                                             float4* __restrict__ st, int maxiter, double tol, bool precond,
+                                             int& iters, double& relres, bool& ok) {
     // no register copy of the team here: the cell loop needs the registers
     Team& Tm = Tm_;
     __shared__ float s_ab[3];      // alpha, beta, relres
@@ -2468,7 +2466,6 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
             if (!(ok = team_allreduce_w<float>(Tm, part, red, 3))) return YGPU_ERR_TIMEOUT;
         }
         float gam_old = 1.0f, alpha_old = 1.0f;
-        int it_std = -1;                         // lead thread: the iteration that met tol_std
         if (lead) {
             const float rel = sqrtf(red[2]);     // the right-hand side has unit norm
             s_ab[2] = rel;
@@ -2564,13 +2561,8 @@ __device__ __noinline__ int krylov_pcg_cells(Team& Tm_, int nu, const Op& A, con
             if (lead) {
                 const float rel = sqrtf(red[2]);
                 s_ab[2] = rel;
-                if (it_std < 0 && rel <= (float)tol_std) it_std = it;
                 if (!isfinite(rel)) s_flag = 2;
                 else if (rel <= (float)tol) s_flag = 1;
-                // past the standard tolerance, the run towards a tighter target gets
-                // as many iterations again (at least 8): where FP32 cannot get there,
-                // the correction so far goes to the FP64 residual
-                else if (it_std >= 0 && it - it_std > max(it_std, 8)) s_flag = 1;
                 else {
                     const float gam = red[0], del = red[1];
                     const float beta = gam / gam_old;
@@ -3194,14 +3186,8 @@ __device__ __noinline__ int linear_solve(const Inst& I, const ygpu_dyn_par& P, c
         double rel_in = 0.0;
         int st;
         if (cells) {
-            // the reduction that would meet the outer tolerance in this step, when it
-            // is within reach of FP32 (one inner solve and a check instead of two
-            // inner solves and a check per linear solve)
-            double tol_o = inner_tol;
-            const double want = 0.5 * P.lin_tol * bnrm / nr;
-            if (want < tol_o) tol_o = (want > 1e-5) ? want : 1e-5;
             st = krylov_pcg_cells(T, G.nu, A32, I.fdinv, I.x, nr, I.r, sc, I.fv, I.fph, I.fm2, I.fst, inner_max,
-                                  tol_o, inner_tol, pre, it, rel_in, ok);
+                                  inner_tol, pre, it, rel_in, ok);
             if (!ok) return YGPU_ERR_TIMEOUT;
             total += it;
             outer++;
