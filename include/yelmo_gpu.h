@@ -247,6 +247,26 @@ int ygpu_calc_dyn_inputs(const double* H_ice, const double* z_bed, const double*
                          int boundaries, int nx, int ny);
 
 /*
+ * ygpu_calc_dyn_inputs_bg -- ygpu_calc_dyn_inputs with a uniform background
+ * slope (ytopo slope_bg_x, slope_bg_y; yelmo_topography.f90:1373-1374) that
+ * z_srf does not contain: it is added to dzsdx and dzsdy before the grad_lim
+ * limit (calc_gradient_acx/acy, yelmo_tools.f90:401,470) and so enters the
+ * driving stress. The inclined-plane domains (ISMIP-HOM, tests/yelmo_ismiphom.f90:
+ * 102-106) carry their mean slope this way on a periodic grid.
+ * ygpu_calc_dyn_inputs is this call with both slopes 0.
+ */
+int ygpu_calc_dyn_inputs_bg(const double* H_ice, const double* z_bed, const double* z_sl,
+                            double* f_ice, double* H_grnd, double* z_srf,
+                            double* f_grnd, double* f_grnd_acx, double* f_grnd_acy,
+                            int* mask_frnt, double* dzsdx, double* dzsdy,
+                            double* taud_acx, double* taud_acy,
+                            double* taul_int_acx, double* taul_int_acy,
+                            double dx, double grad_lim, double taud_lim,
+                            double rho_ice, double rho_sw, double g,
+                            double slope_bg_x, double slope_bg_y,
+                            int boundaries, int nx, int ny);
+
+/*
  * Post-solve diagnostics of calc_ydyn (src/yelmo_dynamics.f90:304-336 and the
  * DIVA depth averages of :642-644), on the GPU. All arrays are (nx,ny) or
  * (nx,ny,nz) column-major like the solver fields; f_ice is f_ice_dyn.

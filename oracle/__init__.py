@@ -63,6 +63,7 @@ def lib():
         abi.declare_velocity(L.orc_calc_velocity_diva_hook, abi.DIVA_ARGS)
         L.orc_calc_velocity_diva_hook.argtypes = L.orc_calc_velocity_diva_hook.argtypes + [abi.NEFF_HOOK, C.c_void_p]
         abi.declare_inputs(L.orc_calc_dyn_inputs)
+        abi.declare_inputs(L.orc_calc_dyn_inputs_bg, bg=True)
         abi.declare_masks(L.orc_set_ssa_masks)
         dp, ip = C.POINTER(C.c_double), C.POINTER(C.c_int)
         L.orc_assemble_csr.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int] + \
@@ -93,8 +94,10 @@ def calc_dyn_inputs(inst) -> dict:
     """Oracle restatement of the fields calc_ydyn builds before the solve."""
     d = inst.input_buffers()
     p = inst.par
-    st = abi.call_inputs(lib().orc_calc_dyn_inputs, d, inst.dx, p.grad_lim, p.taud_lim,
-                         p.rho_ice, p.rho_sw, p.g, abi.BOUNDARY_CODES[p.boundaries])
+    bg = tuple(getattr(inst, "slope_bg", (0.0, 0.0)))
+    fn = lib().orc_calc_dyn_inputs if bg == (0.0, 0.0) else lib().orc_calc_dyn_inputs_bg
+    st = abi.call_inputs(fn, d, inst.dx, p.grad_lim, p.taud_lim, p.rho_ice, p.rho_sw, p.g,
+                         abi.BOUNDARY_CODES[p.boundaries], None if bg == (0.0, 0.0) else bg)
     assert st == 0
     return d
 

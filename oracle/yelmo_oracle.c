@@ -1779,6 +1779,15 @@ int orc_calc_dyn_inputs(const double* H_ice, const double* z_bed, const double* 
                         double* dzsdx, double* dzsdy, double* tdx, double* tdy, double* tlx, double* tly,
                         double dx, double grad_lim, double taud_lim, double rho_ice, double rho_sw, double g,
                         int bc, int nx, int ny) {
+    return orc_calc_dyn_inputs_bg(H_ice, z_bed, z_sl, f_ice, H_grnd, z_srf, f_grnd, fgx, fgy, mf, dzsdx, dzsdy, tdx,
+                                  tdy, tlx, tly, dx, grad_lim, taud_lim, rho_ice, rho_sw, g, 0.0, 0.0, bc, nx, ny);
+}
+
+int orc_calc_dyn_inputs_bg(const double* H_ice, const double* z_bed, const double* z_sl, double* f_ice,
+                           double* H_grnd, double* z_srf, double* f_grnd, double* fgx, double* fgy, int* mf,
+                           double* dzsdx, double* dzsdy, double* tdx, double* tdy, double* tlx, double* tly,
+                           double dx, double grad_lim, double taud_lim, double rho_ice, double rho_sw, double g,
+                           double slope_bg_x, double slope_bg_y, int bc, int nx, int ny) {
     size_t n2 = (size_t)nx * ny;
     double rsi = rho_sw / rho_ice, ris = rho_ice / rho_sw, rhog = rho_ice * g;
     for (size_t c = 0; c < n2; c++) {
@@ -1852,6 +1861,9 @@ int orc_calc_dyn_inputs(const double* H_ice, const double* z_bed, const double* 
             dzsdy[ID2(i, ny - 1)] = dzsdy[ID2(i, ny - 2)];
         }
     for (size_t c = 0; c < n2; c++) {
+        /* the background slope, then the limit (yelmo_tools.f90:400-404) */
+        dzsdx[c] = dzsdx[c] + slope_bg_x;
+        dzsdy[c] = dzsdy[c] + slope_bg_y;
         if (dzsdx[c] < -grad_lim) dzsdx[c] = -grad_lim; else if (dzsdx[c] > grad_lim) dzsdx[c] = grad_lim;
         if (dzsdy[c] < -grad_lim) dzsdy[c] = -grad_lim; else if (dzsdy[c] > grad_lim) dzsdy[c] = grad_lim;
     }

@@ -145,6 +145,17 @@ int orc_calc_dyn_inputs(const double* H_ice, const double* z_bed, const double* 
                         double* taul_int_acx, double* taul_int_acy,
                         double dx, double grad_lim, double taud_lim,
                         double rho_ice, double rho_sw, double g, int bc, int nx, int ny);
+/* the same with the uniform background slope added to dzsdx, dzsdy before the
+   limit (calc_gradient_acx/acy slope_bg, yelmo_tools.f90:401,470) */
+int orc_calc_dyn_inputs_bg(const double* H_ice, const double* z_bed, const double* z_sl,
+                           double* f_ice, double* H_grnd, double* z_srf,
+                           double* f_grnd, double* f_grnd_acx, double* f_grnd_acy,
+                           int* mask_frnt, double* dzsdx, double* dzsdy,
+                           double* taud_acx, double* taud_acy,
+                           double* taul_int_acx, double* taul_int_acy,
+                           double dx, double grad_lim, double taud_lim,
+                           double rho_ice, double rho_sw, double g,
+                           double slope_bg_x, double slope_bg_y, int bc, int nx, int ny);
 
 /* sigma grid, calc_zeta (yelmo_grid.f90:41): scale 0 linear, 1 exp, 2 exp-inv, 3 tanh */
 void orc_calc_zeta(int nz, int scale, double zeta_exp, double* zeta_aa);

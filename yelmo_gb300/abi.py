@@ -305,8 +305,9 @@ def declare_velocity(fn, args):
     fn.restype = C.c_int
 
 
-def declare_inputs(fn):
-    fn.argtypes = [_ctype(t) for _, t in INPUT_ARGS] + [C.c_double] * 6 + [C.c_int] * 3
+def declare_inputs(fn, bg: bool = False):
+    """ygpu_calc_dyn_inputs (bg: ygpu_calc_dyn_inputs_bg, two background slopes more)."""
+    fn.argtypes = [_ctype(t) for _, t in INPUT_ARGS] + [C.c_double] * (8 if bg else 6) + [C.c_int] * 3
     fn.restype = C.c_int
 
 
@@ -361,9 +362,11 @@ def call_velocity(fn, args, fields: dict, dx, dy, n_glen, par: DynPar, extra=())
     return out
 
 
-def call_inputs(fn, fields: dict, dx, grad_lim, taud_lim, rho_ice, rho_sw, g, bc):
+def call_inputs(fn, fields: dict, dx, grad_lim, taud_lim, rho_ice, rho_sw, g, bc, slope_bg=None):
+    """Call ygpu_calc_dyn_inputs, or the _bg entry with slope_bg = (slope_bg_x, slope_bg_y)."""
     nx, ny = fields["H_ice"].shape
     cargs = [ptr(fields[n], t) for n, t in INPUT_ARGS]
+    bg = () if slope_bg is None else (C.c_double(slope_bg[0]), C.c_double(slope_bg[1]))
     return int(fn(*cargs, C.c_double(dx), C.c_double(grad_lim), C.c_double(taud_lim),
-                  C.c_double(rho_ice), C.c_double(rho_sw), C.c_double(g),
+                  C.c_double(rho_ice), C.c_double(rho_sw), C.c_double(g), *bg,
                   C.c_int(bc), C.c_int(nx), C.c_int(ny)))

@@ -120,6 +120,8 @@ class Instance:
     f_slide: np.ndarray
     n_glen: float = 3.0
     extra: dict = field(default_factory=dict)
+    # uniform background slope (ytopo slope_bg_x, slope_bg_y) not contained in z_bed
+    slope_bg: tuple = (0.0, 0.0)
 
     @property
     def nx(self):
@@ -347,6 +349,46 @@ def schoof_slab(dx_km: float = 2.0, lx: float = 100e3, ly: float = 80e3, alpha: 
                     _F(np.zeros((nx, ny))), _F(np.full((nx, ny, nz), A)), calc_zeta(nz),
                     _F(np.zeros((nx, ny))), _F(c_bed), _F(np.ones((nx, ny))))
     inst.extra = {"y": y, "u": u, "taud": par.rho_ice * par.g * H0 * alpha, "W": W}
+    return inst
+
+
+ISMIPHOM_A = 2.140373e-7       # [Pa-1 a-1] rate factor of experiment F (n = 1)
+
+
+def ismiphom_f(exp: int = 1, dx_km: float = 2.5, L_km: float = 100.0, nz: int = 10,
+               alpha_deg: float = 3.0, bump: float = 100.0, sigma: float = 10e3) -> Instance:
+    """ISMIP-HOM experiment F (tests/yelmo_ismiphom.f90:59-77,149-186, par/yelmo_ISMIPHOM.nml):
+    a slab of mean thickness 1000 m on a mean slope alpha over a Gaussian bed bump,
+    periodic square domain of side L centred on the bump (x0 = -L/2, dx = L/40), DIVA
+    with linear rheology (n = 1, A = 2.140373e-7 Pa-1 a-1), zero mass balance.
+    exp 1 (F1): no slip (solver "diva-noslip"); exp 2 (F2): slip ratio 1, imposed
+    beta = 1/(A H0) on the aa-nodes (beta_method -1). The inclined plane is the
+    background slope slope_bg_x = -tan(alpha); z_srf starts at 0 and z_bed holds the
+    periodic part, z_bed = -1000 + bump exp(-(x^2+y^2)/sigma^2). z_sl = -10000 keeps
+    every cell grounded. bump = 0 gives the unperturbed slab, whose surface speed is
+    A rho g tan(alpha) H0^2 (F1) and twice that (F2)."""
+    if exp not in (1, 2):
+        raise ValueError("exp is 1 (F1, no slip) or 2 (F2, slip ratio 1)")
+    dx = dx_km * 1e3
+    n = int(round(L_km / dx_km))
+    x = -0.5 * L_km * 1e3 + dx * np.arange(n)
+    r2 = x[:, None] ** 2 + x[None, :] ** 2
+    z_bed = -1000.0 + bump * np.exp(-r2 / sigma ** 2)
+    H = 0.0 - z_bed
+    H0 = 1000.0
+    beta = np.full((n, n), 1000.0 if exp == 1 else 1.0 / (ISMIPHOM_A * H0))
+    par = YdynParams(solver="diva-noslip" if exp == 1 else "diva", visc_method=1, beta_method=-1,
+                     beta_gl_scale=0, beta_gl_stag=1, beta_gl_f=1.0, beta_min=0.0, eps_0=1e-6,
+                     ssa_solver="energy", ssa_lat_bc="marine", ssa_vel_max=10000.0, ssa_iter_max=100,
+                     ssa_iter_rel=0.7, ssa_iter_conv=1e-5, taud_lim=1e6, grad_lim=0.5,
+                     boundaries="periodic", rho_ice=910.0, rho_sw=1028.0, g=9.81)
+    inst = Instance(f"ismiphom_f{exp}", par, dx, _F(H), _F(z_bed), _F(np.full((n, n), -10000.0)),
+                    _F(np.full((n, n, nz), ISMIPHOM_A)), calc_zeta(nz, "linear"), _F(beta),
+                    _F(np.zeros((n, n))), _F(np.ones((n, n))), n_glen=1.0,
+                    slope_bg=(-np.tan(np.deg2rad(alpha_deg)), 0.0))
+    tau = par.rho_ice * par.g * H0 * np.tan(np.deg2rad(alpha_deg))
+    u_def = ISMIPHOM_A * tau * H0          # n = 1: 2A/(n+1) tau^n H0
+    inst.extra = {"x": x, "exp": exp, "u_s_slab": u_def if exp == 1 else 2.0 * u_def}
     return inst
 
 

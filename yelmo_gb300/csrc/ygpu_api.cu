@@ -1297,7 +1297,20 @@ extern "C" int ygpu_calc_dyn_inputs(const double* H_ice, const double* z_bed, co
                                     double* taud_acx, double* taud_acy, double* taul_int_acx, double* taul_int_acy,
                                     double dx, double grad_lim, double taud_lim, double rho_ice, double rho_sw,
                                     double g, int boundaries, int nx, int ny) {
-    if (nx < 3 || ny < 3 || !(dx > 0.0) || boundaries < 0 || boundaries > 6 ||
+    return ygpu_calc_dyn_inputs_bg(H_ice, z_bed, z_sl, f_ice, H_grnd, z_srf, f_grnd, f_grnd_acx, f_grnd_acy, mask_frnt,
+                                   dzsdx, dzsdy, taud_acx, taud_acy, taul_int_acx, taul_int_acy, dx, grad_lim,
+                                   taud_lim, rho_ice, rho_sw, g, 0.0, 0.0, boundaries, nx, ny);
+}
+
+extern "C" int ygpu_calc_dyn_inputs_bg(const double* H_ice, const double* z_bed, const double* z_sl, double* f_ice,
+                                       double* H_grnd, double* z_srf, double* f_grnd, double* f_grnd_acx,
+                                       double* f_grnd_acy, int* mask_frnt, double* dzsdx, double* dzsdy,
+                                       double* taud_acx, double* taud_acy, double* taul_int_acx,
+                                       double* taul_int_acy, double dx, double grad_lim, double taud_lim,
+                                       double rho_ice, double rho_sw, double g, double slope_bg_x,
+                                       double slope_bg_y, int boundaries, int nx, int ny) {
+    if (nx < 3 || ny < 3 || !(dx > 0.0) || boundaries < 0 || boundaries > 6 || !isfinite(slope_bg_x) ||
+        !isfinite(slope_bg_y) ||
         any_null({H_ice, z_bed, z_sl, f_ice, H_grnd, z_srf, f_grnd, f_grnd_acx, f_grnd_acy, mask_frnt, dzsdx, dzsdy,
                   taud_acx, taud_acy, taul_int_acx, taul_int_acy})) {
         ygpu_set_error("bad arguments");
@@ -1318,7 +1331,8 @@ extern "C" int ygpu_calc_dyn_inputs(const double* H_ice, const double* z_bed, co
     auto d = [&](size_t k) { return (double*)S.args[k].dev; };
     st = ygpu_dyn_inputs_device(c->stream, d(a_H), d(a_zb), d(a_zl), d(a_fi), d(a_hg), d(a_zs), d(a_fg), d(a_fx),
                                 d(a_fy), (int*)S.args[a_mf].dev, d(a_dx), d(a_dy), d(a_tx), d(a_ty), d(a_lx), d(a_ly),
-                                dx, grad_lim, taud_lim, rho_ice, rho_sw, g, boundaries, nx, ny);
+                                dx, grad_lim, taud_lim, rho_ice, rho_sw, g, boundaries, nx, ny, slope_bg_x,
+                                slope_bg_y);
     if (st) return st;
     return S.download(c);
 }

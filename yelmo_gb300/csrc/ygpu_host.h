@@ -119,7 +119,7 @@ int ygpu_dyn_inputs_device(cudaStream_t s, const double* H, const double* zb, co
                            double* H_grnd, double* z_srf, double* f_grnd, double* fgx, double* fgy, int* mf,
                            double* dzsdx, double* dzsdy, double* tdx, double* tdy, double* tlx, double* tly,
                            double dx, double grad_lim, double taud_lim, double rho_ice, double rho_sw, double g,
-                           int bc, int nx, int ny);
+                           int bc, int nx, int ny, double slope_bg_x = 0.0, double slope_bg_y = 0.0);
 int ygpu_dyn_diagnostics_device(cudaStream_t s, const ygpu_dyn_diag& D, int bc);
 int ygpu_gradient_column_device(cudaStream_t s, double* gx_c, double* gy_c, const double* gx, const double* gy,
                                 const double* f_ice, const int* mask_ocn, int bc, int nx, int ny);

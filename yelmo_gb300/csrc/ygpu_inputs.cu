@@ -27,9 +27,11 @@ __global__ void k_inputs_pointwise(int n2, const double* H, const double* zb, co
 }
 
 // grounded fraction of the faces (calc_f_grnd_subgrid_linear) and the
-// surface gradient (calc_gradient_acx/acy, zero_outside=.FALSE.)
+// surface gradient (calc_gradient_acx/acy, zero_outside=.FALSE.) with the
+// uniform background slope (sbx, sby) added before the limit (yelmo_tools.f90:401)
 __global__ void k_inputs_faces(int nx, int ny, int bc, const double* H_grnd, const double* z_srf, double* fgx,
-                               double* fgy, double* dzsdx, double* dzsdy, double dx, double grad_lim) {
+                               double* fgy, double* dzsdx, double* dzsdy, double dx, double grad_lim, double sbx,
+                               double sby) {
     int n2 = nx * ny;
     bool px, py;
     periodic_dirs(bc, px, py);
@@ -61,6 +63,7 @@ __global__ void k_inputs_faces(int nx, int ny, int bc, const double* H_grnd, con
             int im1, ip1, jm1, jp1;
             nbr_bc(gi, j, nx, ny, bc, im1, ip1, jm1, jp1);
             double d = (z_srf[ip1 + nx * j] - z_srf[gi + nx * j]) / dx;
+            d = d + sbx;
             if (d < -grad_lim) d = -grad_lim; else if (d > grad_lim) d = grad_lim;   // minmax
             dzsdx[c] = d;
         }
@@ -72,6 +75,7 @@ __global__ void k_inputs_faces(int nx, int ny, int bc, const double* H_grnd, con
             int im1, ip1, jm1, jp1;
             nbr_bc(i, gj, nx, ny, bc, im1, ip1, jm1, jp1);
             double d = (z_srf[i + nx * jp1] - z_srf[i + nx * gj]) / dx;
+            d = d + sby;
             if (d < -grad_lim) d = -grad_lim; else if (d > grad_lim) d = grad_lim;
             dzsdy[c] = d;
         }
@@ -210,11 +214,12 @@ int ygpu_dyn_inputs_device(cudaStream_t s, const double* H, const double* zb, co
                            double* H_grnd, double* z_srf, double* f_grnd, double* fgx, double* fgy, int* mf,
                            double* dzsdx, double* dzsdy, double* tdx, double* tdy, double* tlx, double* tly,
                            double dx, double grad_lim, double taud_lim, double rho_ice, double rho_sw, double g,
-                           int bc, int nx, int ny) {
+                           int bc, int nx, int ny, double slope_bg_x, double slope_bg_y) {
     int n2 = nx * ny, gb = grid_for(n2);
     k_inputs_pointwise<<<gb, 256, 0, s>>>(n2, H, zb, zsl, f_ice, H_grnd, z_srf, f_grnd, rho_sw / rho_ice,
                                           rho_ice / rho_sw);
-    k_inputs_faces<<<gb, 256, 0, s>>>(nx, ny, bc, H_grnd, z_srf, fgx, fgy, dzsdx, dzsdy, dx, grad_lim);
+    k_inputs_faces<<<gb, 256, 0, s>>>(nx, ny, bc, H_grnd, z_srf, fgx, fgy, dzsdx, dzsdy, dx, grad_lim,
+                                           slope_bg_x, slope_bg_y);
     k_ice_front<<<gb, 256, 0, s>>>(nx, ny, bc, f_ice, f_grnd, zb, zsl, mf);
     k_stresses<<<gb, 256, 0, s>>>(nx, ny, bc, H, f_ice, dzsdx, dzsdy, z_srf, zsl, mf, tdx, tdy, tlx, tly, rho_ice,
                                   rho_sw, g, taud_lim);

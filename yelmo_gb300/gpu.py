@@ -33,6 +33,7 @@ _lib = None
 EXPORTS = [
     "ygpu_dyn_par_defaults", "ygpu_parse_lis_opt", "ygpu_boundary_code", "ygpu_last_error", "ygpu_version",
     "ygpu_calc_velocity_ssa", "ygpu_calc_velocity_diva", "ygpu_set_ssa_masks", "ygpu_calc_dyn_inputs",
+    "ygpu_calc_dyn_inputs_bg",
     "ygpu_linear_solver_matrix_solve", "ygpu_ctx_create", "ygpu_ctx_destroy", "ygpu_ctx_stream",
     "ygpu_solve_device", "ygpu_solve_batch_device", "ygpu_solve_device_noalloc",
     "ygpu_server_create", "ygpu_server_destroy", "ygpu_server_add_member", "ygpu_server_submit",
@@ -66,6 +67,7 @@ def lib(build_if_missing: bool = True):
     abi.declare_velocity(L.ygpu_calc_velocity_ssa, abi.SSA_ARGS)
     abi.declare_velocity(L.ygpu_calc_velocity_diva, abi.DIVA_ARGS)
     abi.declare_inputs(L.ygpu_calc_dyn_inputs)
+    abi.declare_inputs(L.ygpu_calc_dyn_inputs_bg, bg=True)
     abi.declare_masks(L.ygpu_set_ssa_masks)
     L.ygpu_last_error.restype = C.c_char_p
     L.ygpu_version.restype = C.c_char_p
@@ -333,8 +335,10 @@ def calc_strain_rate_tensor(arrays: dict, dx: float, dy: float, boundaries: str,
 def calc_dyn_inputs(inst) -> dict:
     d = inst.input_buffers()
     p = inst.par
-    _check(abi.call_inputs(lib().ygpu_calc_dyn_inputs, d, inst.dx, p.grad_lim, p.taud_lim, p.rho_ice,
-                           p.rho_sw, p.g, abi.BOUNDARY_CODES[p.boundaries]))
+    bg = tuple(getattr(inst, "slope_bg", (0.0, 0.0)))
+    fn = lib().ygpu_calc_dyn_inputs if bg == (0.0, 0.0) else lib().ygpu_calc_dyn_inputs_bg
+    _check(abi.call_inputs(fn, d, inst.dx, p.grad_lim, p.taud_lim, p.rho_ice, p.rho_sw, p.g,
+                           abi.BOUNDARY_CODES[p.boundaries], None if bg == (0.0, 0.0) else bg))
     return d
 
 
