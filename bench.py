@@ -633,15 +633,22 @@ def main():
     for prec in ("fp64", "mixed"):
         par = insts[0].par.with_(precision=prec)
         # launch tuning by measurement (untimed): the batch, and the single solve
+        # (and, mixed, the inner tolerance by full solves)
         tb = autotune(solver, kind, par, fields, lambda: reset(range(batch)))
         t1 = None if ensemble else autotune(solver1, kind, par, fields[:1], lambda: reset([0]))
         tuned[prec] = {"batch": tb["tuning"], "single": t1["tuning"] if t1 else None}
+        if tb["inner_tol"] is not None:
+            tuned[prec]["inner_tol"] = {"batch": tb["inner_tol"], "single": t1["inner_tol"] if t1 else None,
+                                        "batch_ms": tb["inner_tol_ms"]}
+        par1 = par.with_(inner_tol=t1["inner_tol"]) if t1 and t1["inner_tol"] else par
+        if tb["inner_tol"]:
+            par = par.with_(inner_tol=tb["inner_tol"])
         # single-solve latency (instance 0)
         lat, st1 = [], None
         n_single = 0 if ensemble else args.warmup + args.steps
         for s in range(n_single):
             reset([0])
-            st1 = solver1.solve(kind, par, fields[0])
+            st1 = solver1.solve(kind, par1, fields[0])
             if s >= args.warmup:
                 lat.append(st1["device_ms"])
         u_single = None if ensemble else devs[0]["ux_bar" if kind == abi.KIND_DIVA else "ux_b"].cpu().numpy().reshape(
@@ -683,6 +690,11 @@ def main():
     # e2e: the batched C-ABI entry on host buffers (the whole batch per step, the
     # host-device copies inside the timed region), and the single-solve drop-in
     par_m = insts[0].par.with_(precision="mixed")
+    if tuned["mixed"].get("inner_tol"):
+        par_m = par_m.with_(inner_tol=tuned["mixed"]["inner_tol"]["batch"])
+    par_m1 = par_m
+    if tuned["mixed"].get("inner_tol") and tuned["mixed"]["inner_tol"]["single"]:
+        par_m1 = par_m.with_(inner_tol=tuned["mixed"]["inner_tol"]["single"])
     n_e2e = args.warmup + max(3, args.steps)
     e2e_times, e2e1_times = [], []
     barrier()
@@ -699,7 +711,7 @@ def main():
         for s in range(n_e2e):
             f = _copy(hosts[0])
             t = time.perf_counter()
-            gpu.calc_velocity(f, insts[0].dx, insts[0].n_glen, par_m)
+            gpu.calc_velocity(f, insts[0].dx, insts[0].n_glen, par_m1)
             dt = time.perf_counter() - t
             if s >= args.warmup:
                 e2e1_times.append(dt)

@@ -115,3 +115,40 @@ def test_cluster_teams_equal_global_teams(precision):
             solver.close()
     for a, b in zip(out[0], out[4]):
         assert rel_l2(b, a) <= 1e-6
+
+
+def test_autotune_picks_launch_shape_and_inner_tolerance():
+    """The autotuner's trials leave the fields as reset() restores them; in mixed
+    precision it picks the inner tolerance from its candidates, and a solve with that
+    choice still meets the parity bar against the FP64 solve."""
+    torch = pytest.importorskip("torch")
+    from yelmo_gb300.autotune import autotune
+    insts = _instances(4)
+    devs, fields = zip(*[_device(inst) for inst in insts])
+    pristine = [{k: d[k].clone() for k in gpu.STATE_NAMES} for d in devs]
+
+    def reset():
+        for d, p in zip(devs, pristine):
+            for k in gpu.STATE_NAMES:
+                d[k].copy_(p[k])
+
+    solver = gpu.DeviceSolver(0)
+    try:
+        par64 = insts[0].par.with_(precision="fp64")
+        reset()
+        assert all(st["status"] == 0 for st in solver.solve_batch(abi.KIND_SSA, par64, list(fields)))
+        ref = [d["ux_b"].cpu().numpy() for d in devs]
+        par = insts[0].par.with_(precision="mixed")
+        grid = {"unknowns_per_cta": (512, 1024), "check_every": (4,), "use_graphs": (True,)}
+        out = autotune(solver, abi.KIND_SSA, par, list(fields), reset, iters=4, grid=grid)
+        assert out["tuning"]["unknowns_per_cta"] in (512, 1024)
+        assert out["inner_tol"] in (5e-4, 1e-3, 2e-3)
+        assert set(out["inner_tol_ms"]) == {"0.0005", "0.001", "0.002"}
+        for d, p in zip(devs, pristine):          # left reset
+            assert torch.equal(d["ux_b"], p["ux_b"])
+        sts = solver.solve_batch(abi.KIND_SSA, par.with_(inner_tol=out["inner_tol"]), list(fields))
+        for k, (d, st) in enumerate(zip(devs, sts)):
+            assert st["status"] == 0, (k, st)
+            assert rel_l2(d["ux_b"].cpu().numpy(), ref[k]) <= 1e-6
+    finally:
+        solver.close()

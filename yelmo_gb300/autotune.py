@@ -1,7 +1,11 @@
 """Launch autotuner: picks a context's tuning (team size, host-check interval,
 chunk graphs, lockstep batch or queue) for a workload by timing a fixed number
 of Picard iterations of its batched solve under each candidate (and, for the
-batch-or-queue choice, full solves).
+batch-or-queue choice, full solves). In mixed precision it also picks the inner
+FP32 solve's tolerance (``inner_tol`` of the parameters) from ``inner_tols`` by
+full solves: the outer FP64 defect correction reaches the requested linear
+tolerance whatever the inner one, so the choice trades inner iterations against
+outer steps and changes the time, not the answer's tolerance.
 
     best = autotune(solver, kind, par, fields, reset)
 
@@ -22,8 +26,11 @@ DEFAULT_GRID = {
 }
 
 
+DEFAULT_INNER_TOLS = (5e-4, 1e-3, 2e-3)
+
+
 def autotune(solver, kind: int, par, fields: list, reset, iters: int = 8, grid: dict | None = None,
-             reps: int = 1) -> dict:
+             reps: int = 1, inner_tols=DEFAULT_INNER_TOLS) -> dict:
     import torch
     grid = grid or DEFAULT_GRID
     trial_par = par.with_(ssa_iter_max=iters, ssa_iter_conv=0.0)
@@ -75,5 +82,24 @@ def autotune(solver, kind: int, par, fields: list, reset, iters: int = 8, grid: 
         full.sort(key=lambda r: r[0])
         best = full[0][1]
     solver.set_tuning(**best)
+    # the inner tolerance of the mixed mode, by full solves at the chosen tuning
+    inner = None
+    if par.precision == "mixed" and inner_tols:
+        timed = []
+        for tol in inner_tols:
+            p = par.with_(inner_tol=tol)
+            t = float("inf")
+            for _ in range(reps + 1):
+                reset()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                solver.solve_batch(kind, p, fields)
+                torch.cuda.synchronize()
+                t = min(t, time.perf_counter() - t0)
+            timed.append((t, tol))
+        timed.sort(key=lambda r: r[0])
+        inner = {"inner_tol": timed[0][1], "ms": {f"{tol:g}": t * 1e3 for t, tol in timed}}
+    reset()
     return {"tuning": best, "trial_ms": best_t * 1e3, "iters": iters,
-            "candidates": [{"ms": r[0] * 1e3, **r[1]} for r in results]}
+            "candidates": [{"ms": r[0] * 1e3, **r[1]} for r in results],
+            "inner_tol": inner["inner_tol"] if inner else None, "inner_tol_ms": inner["ms"] if inner else None}
