@@ -359,6 +359,31 @@ def vertical_velocity_leg(device: str, steps: int, warmup: int) -> dict:
     out["kernels"] = 1
     return out
 
+def ismiphom_leg(years: float = 200.0) -> dict:
+    """ISMIP-HOM F2 (40 x 40, dx 2.5 km, slip ratio 1, linear solves to 1e-8) for
+    `years` 1-year steps of the thickness time loop (yelmo_gb300.prognostic) through
+    the host drop-in calls on the GPU, and the same steps on the oracle as its CPU
+    baseline and checker (4 threads: on 1600 cells more threads only add OpenMP
+    overhead): wall time per step and the largest z_srf difference after the last
+    step, relative to the surface relief."""
+    import oracle
+    from tests.golden.make_ismiphom_f_golden import OracleBackend, case
+    from yelmo_gb300 import prognostic
+    prognostic.run(case(2, "tight"), 1.0, 5.0)          # warm-up (library load, first launches)
+    t0 = time.perf_counter()
+    g = prognostic.run(case(2, "tight"), 1.0, years)
+    t_gpu = time.perf_counter() - t0
+    oracle.set_threads(4)
+    t0 = time.perf_counter()
+    o = prognostic.run(case(2, "tight"), 1.0, years, backend=OracleBackend())
+    t_cpu = time.perf_counter() - t0
+    err = float(np.max(np.abs(g["z_srf"] - o["z_srf"])) / np.max(np.abs(o["z_srf"])))
+    return {"workload": f"ISMIP-HOM F2 40x40, {int(years)} one-year steps (advection, inputs, DIVA solve)",
+            "gpu_ms_per_step": 1e3 * t_gpu / g["steps"], "oracle_ms_per_step": 1e3 * t_cpu / o["steps"],
+            "oracle_threads": 4, "zs_rel_diff_gpu_vs_oracle": err,
+            "picard_iters": int(g["history"]["picard"].sum())}
+
+
 def advection_leg(device: str, steps: int, warmup: int) -> dict:
     """Time calc_advec2D(impl-lis) on the device (ygpu_advec2D_impl_lis_device)
     on a 801 x 801 grid resident in HBM: seeded thickness, velocities and source,
@@ -717,6 +742,7 @@ def main():
                 e2e1_times.append(dt)
     diag = diagnostics_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
     adv = advection_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
+    ismip = ismiphom_leg() if (rank == 0 and not args.no_cpu) else None
     jac = jacobian_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
     uzl = vertical_velocity_leg(f"cuda:{local}", max(3, args.steps), args.warmup) if rank == 0 else None
     i0 = insts[0]
@@ -817,6 +843,7 @@ def main():
         "clocks": clocks,
         "diagnostics": (dict(diag, frac=diag["achieved_gbs"] / peak) if diag else None),
         "advection": (dict(adv, frac=adv["achieved_gbs"] / peak) if adv else None),
+        "ismiphom_f": ismip,
         "jacobian": (dict(jac, frac=jac["achieved_gbs"] / peak) if jac else None),
         "vertical_velocity": ({k: (dict(v, frac=v["achieved_gbs"] / peak) if isinstance(v, dict) else v)
                                for k, v in uzl.items()} if uzl else None),
