@@ -659,6 +659,11 @@ typedef struct ygpu_server_info {
 #define YGPU_SRV_H     3        /* H_ice                                         */
 #define YGPU_SRV_UXB   4        /* ux_b                                          */
 #define YGPU_SRV_UYB   5
+#define YGPU_SRV_TAUBX 6        /* taub_acx                                      */
+#define YGPU_SRV_TAUBY 7        /* taub_acy                                      */
+#define YGPU_SRV_BETA  8        /* beta (aa-nodes)                               */
+#define YGPU_SRV_BETAX 9        /* beta_acx                                      */
+#define YGPU_SRV_BETAY 10       /* beta_acy                                      */
 
 /* NULL on error (ygpu_last_error). Starts the serving thread. */
 ygpu_server* ygpu_server_create(const ygpu_server_cfg* cfg);
@@ -681,6 +686,20 @@ int ygpu_server_wait(ygpu_server* srv, int request_id, double timeout_s, ygpu_st
                      double* latency_ms);
 /* Copies a member field to a host buffer; YGPU_ERR_BUSY while it is solving. */
 int ygpu_server_fetch(ygpu_server* srv, int member, int field, double* host);
+/*
+ * Checkpoint and restart of a member. Its evolving state is the thickness and
+ * the warm start of its next solve: YGPU_SRV_H, _UX, _UY, _UXB, _UYB, _VISC,
+ * _TAUBX, _TAUBY, _BETA, _BETAX, _BETAY (fetched while it is idle), plus the
+ * count of its requests admitted so far. Registering those arrays with the
+ * member's fixed inputs (z_bed, z_sl, c_bed, f_slide, ATT, zeta_aa) through
+ * ygpu_server_add_member, under the same member id (members added in the same
+ * order: the id keys the thickness perturbations), and setting the count with
+ * ygpu_server_set_member_steps resumes it: its next request solves the state
+ * the uninterrupted server's would. The step count can only be set while the
+ * member is idle with no request of it waiting (else YGPU_ERR_BUSY).
+ */
+int ygpu_server_member_steps(ygpu_server* srv, int member, unsigned long long* steps);
+int ygpu_server_set_member_steps(ygpu_server* srv, int member, unsigned long long steps);
 int ygpu_server_get_info(ygpu_server* srv, ygpu_server_info* info);
 
 /* ======================================================================== */

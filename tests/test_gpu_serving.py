@@ -112,3 +112,48 @@ def test_admission_by_hbm_budget():
             srv.add_member(member_state(big), big.dx)
         assert e.value.status == abi.ERR_ADMISSION
         assert srv.info()["bytes_held"] <= 64e6
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("mixed", 1e-6)])
+def test_member_resumes_from_checkpoint(precision, tol, tmp_path):
+    """Checkpoint every member after two steps, write the restart file, restore the
+    members into a new server and run the last two steps there: thickness equal, the
+    velocities and viscosity those of the uninterrupted server."""
+    insts = _members(3, precision)
+    seeds = [[11, 12, 13, 14], [21, 22, 23, 24], [31, 32, 33, 34]]
+
+    def run(srv, ids, steps):
+        for k in steps:
+            rids = [srv.submit(m, seeds[i][k]) for i, m in enumerate(ids)]
+            for r in rids:
+                status, stats, _ = srv.wait(r, timeout=120.0)
+                assert status == 0, stats
+
+    def final(srv, ids):
+        return [{k: srv.fetch(m, k) for k in ("H_ice", "ux", "uy", "visc_eff")} for m in ids]
+
+    srv, ids = _server(insts)
+    with srv:
+        run(srv, ids, (0, 1))
+        cks = [srv.checkpoint(m) for m in ids]
+        assert [int(ck["steps"]) for ck in cks] == [2, 2, 2]
+        run(srv, ids, (2, 3))
+        ref = final(srv, ids)
+    path = tmp_path / "restart.npz"
+    np.savez(path, **{f"m{i}_{k}": v for i, ck in enumerate(cks) for k, v in ck.items()})
+    z = np.load(path)
+    cks = [{k: z[f"m{i}_{k}"] for k in cks[0]} for i in range(len(insts))]
+    with Server(insts[0].par, dH_sigma=5.0) as srv2:
+        ids2 = [srv2.restore(member_state(inst), ck, inst.dx) for inst, ck in zip(insts, cks)]
+        assert ids2 == ids and [srv2.steps(m) for m in ids2] == [2, 2, 2]
+        run(srv2, ids2, (2, 3))
+        got = final(srv2, ids2)
+        # a member with a request waiting cannot have its step count set
+        rid = srv2.submit(ids2[0], 99)
+        st = srv2.L.ygpu_server_set_member_steps(srv2.srv, ids2[0], 0)
+        assert st in (0, abi.ERR_BUSY)
+        assert srv2.wait(rid, timeout=120.0)[0] == 0
+    for a, b in zip(got, ref):
+        assert np.array_equal(a["H_ice"], b["H_ice"])
+        for k in ("ux", "uy", "visc_eff"):
+            assert rel_l2(a[k], b[k]) <= tol, k

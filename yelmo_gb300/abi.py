@@ -258,6 +258,7 @@ class ServerInfo(C.Structure):
 
 
 SRV_UX, SRV_UY, SRV_VISC, SRV_H, SRV_UXB, SRV_UYB = 0, 1, 2, 3, 4, 5
+SRV_TAUBX, SRV_TAUBY, SRV_BETA, SRV_BETAX, SRV_BETAY = 6, 7, 8, 9, 10
 
 
 # Argument names of calc_velocity_ssa (velocity_ssa.f90:60) and

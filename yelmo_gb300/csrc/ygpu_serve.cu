@@ -680,6 +680,11 @@ extern "C" int ygpu_server_fetch(ygpu_server* S, int member, int field, double* 
         case YGPU_SRV_H: src = M.H; break;
         case YGPU_SRV_UXB: src = M.f.ux_b; break;
         case YGPU_SRV_UYB: src = M.f.uy_b; break;
+        case YGPU_SRV_TAUBX: src = M.f.taub_acx; break;
+        case YGPU_SRV_TAUBY: src = M.f.taub_acy; break;
+        case YGPU_SRV_BETA: src = M.f.beta; break;
+        case YGPU_SRV_BETAX: src = M.f.beta_acx; break;
+        case YGPU_SRV_BETAY: src = M.f.beta_acy; break;
         default: ygpu_set_error("bad field code %d", field); return YGPU_ERR_BAD_ARG;
     }
     cudaSetDevice(S->cfg.device);
@@ -687,6 +692,26 @@ extern "C" int ygpu_server_fetch(ygpu_server* S, int member, int field, double* 
         ygpu_set_error("fetch failed: %s", cudaGetErrorString(cudaGetLastError()));
         return YGPU_ERR_CUDA;
     }
+    return YGPU_OK;
+}
+
+extern "C" int ygpu_server_member_steps(ygpu_server* S, int member, unsigned long long* steps) {
+    if (!S || !steps) { ygpu_set_error("NULL argument"); return YGPU_ERR_BAD_ARG; }
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (member < 0 || member >= (int)S->members.size()) { ygpu_set_error("bad member %d", member); return YGPU_ERR_BAD_ARG; }
+    *steps = S->members[member].steps;
+    return YGPU_OK;
+}
+
+extern "C" int ygpu_server_set_member_steps(ygpu_server* S, int member, unsigned long long steps) {
+    if (!S) { ygpu_set_error("NULL argument"); return YGPU_ERR_BAD_ARG; }
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (member < 0 || member >= (int)S->members.size()) { ygpu_set_error("bad member %d", member); return YGPU_ERR_BAD_ARG; }
+    Member& M = S->members[member];
+    bool waiting = M.busy;
+    for (int id : S->waiting) waiting = waiting || (S->requests[id].member == member);
+    if (waiting) { ygpu_set_error("member %d has a request waiting or solving", member); return YGPU_ERR_BUSY; }
+    M.steps = steps;
     return YGPU_OK;
 }
 

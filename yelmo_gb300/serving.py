@@ -15,7 +15,11 @@ from .gpu import YgpuError, last_error, lib
 from .params import YdynParams
 
 FIELDS = {"ux": abi.SRV_UX, "uy": abi.SRV_UY, "visc_eff": abi.SRV_VISC, "H_ice": abi.SRV_H,
-          "ux_b": abi.SRV_UXB, "uy_b": abi.SRV_UYB}
+          "ux_b": abi.SRV_UXB, "uy_b": abi.SRV_UYB, "taub_acx": abi.SRV_TAUBX, "taub_acy": abi.SRV_TAUBY,
+          "beta": abi.SRV_BETA, "beta_acx": abi.SRV_BETAX, "beta_acy": abi.SRV_BETAY}
+# the member fields a checkpoint holds (with the step count)
+CHECKPOINT_FIELDS = ("H_ice", "ux", "uy", "ux_b", "uy_b", "visc_eff", "taub_acx", "taub_acy",
+                     "beta", "beta_acx", "beta_acy")
 
 
 class Server:
@@ -99,11 +103,46 @@ class Server:
     def fetch(self, member: int, field: str) -> np.ndarray:
         nx, ny, nz = self.shapes[member]
         shape = (nx, ny, nz) if field == "visc_eff" else (nx, ny)
+        if field not in FIELDS:
+            raise ValueError(f"unknown member field {field!r}")
         out = np.zeros(shape, order="F")
         st = self.L.ygpu_server_fetch(self.srv, member, FIELDS[field], out.ctypes.data_as(C.POINTER(C.c_double)))
         if st != 0:
             raise YgpuError(st, last_error())
         return out
+
+    def steps(self, member: int) -> int:
+        """Requests of the member admitted so far (the index of its next step)."""
+        n = C.c_ulonglong(0)
+        st = self.L.ygpu_server_member_steps(self.srv, member, C.byref(n))
+        if st != 0:
+            raise YgpuError(st, last_error())
+        return int(n.value)
+
+    def checkpoint(self, member: int) -> dict:
+        """The member's evolving state (an idle member): CHECKPOINT_FIELDS and its
+        step count. With the member's fixed inputs it is everything restore() needs;
+        np.savez of the dict is a restart file."""
+        ck = {k: self.fetch(member, k) for k in CHECKPOINT_FIELDS}
+        ck["steps"] = np.int64(self.steps(member))
+        return ck
+
+    def restore(self, fixed: dict, ck: dict, dx: float, n_glen: float = 3.0) -> int:
+        """Register a member from a checkpoint and its fixed inputs (z_bed, z_sl,
+        c_bed, f_slide, ATT, zeta_aa); members restored in their original order keep
+        their ids, so their next requests solve what the uninterrupted server would."""
+        kind_diva = self.par.kind == abi.KIND_DIVA
+        state = {k: fixed[k] for k in ("z_bed", "z_sl", "c_bed", "f_slide", "ATT", "zeta_aa")}
+        for k in CHECKPOINT_FIELDS:
+            if k in ("ux", "uy"):
+                state[(k + "_bar") if kind_diva else (k + "_b")] = ck[k]
+            else:
+                state[k] = ck[k]
+        m = self.add_member(state, dx, n_glen)
+        st = self.L.ygpu_server_set_member_steps(self.srv, m, C.c_ulonglong(int(ck["steps"])))
+        if st != 0:
+            raise YgpuError(st, last_error())
+        return m
 
     def info(self) -> dict:
         i = abi.ServerInfo()
