@@ -70,7 +70,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
-        run([cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+        run([cc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-ldl"])
     return LIB
 
 

@@ -511,6 +511,7 @@ bool ygpu_plan_teams(int max_ctas, int n, const size_t* nu, std::vector<int>& ma
 
 static int solve_batch(ygpu_ctx* c, int kind, const ygpu_dyn_par* par, int n, const ygpu_fields* inst,
                        ygpu_stats* stats, double* host_cbed = nullptr) {
+    YgRange range("ygpu solve_batch");
     int st = ygpu_check_par(par);
     if (st) return st;
     if (kind != YGPU_KIND_SSA && kind != YGPU_KIND_DIVA) { ygpu_set_error("bad solver kind %d", kind); return YGPU_ERR_BAD_ARG; }
@@ -990,6 +991,7 @@ struct Staging {
         return YGPU_OK;
     }
     int upload(ygpu_ctx* c) {
+        YgRange range("ygpu stage in");
         size_t off = 0;
         for (int cls = 0; cls < 4; cls++) {
             if (cls == 1) down = off;
@@ -1038,6 +1040,7 @@ struct Staging {
         return YGPU_OK;
     }
     int download(ygpu_ctx* c) {
+        YgRange range("ygpu stage out");
         if (direct) return copy_direct(c, false);
         if (dend > down) CK(cudaMemcpyAsync(c->hbuf + down, c->fbuf + down, dend - down, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));

@@ -3,8 +3,19 @@
 #include <vector>
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/yelmo_gpu.h"
+
+// An NVTX range over a C++ scope: the solve, a batch, a chunk of Picard
+// iterations, the host staging copies, a serving tick. NVTX3 is header-only and
+// does nothing unless a profiler or an NVTX injection library is attached.
+struct YgRange {
+    explicit YgRange(const char* name) { nvtxRangePushA(name); }
+    ~YgRange() { nvtxRangePop(); }
+    YgRange(const YgRange&) = delete;
+    YgRange& operator=(const YgRange&) = delete;
+};
 
 #ifndef YG_BLOCK
 #define YG_BLOCK 256

@@ -309,6 +309,7 @@ static int prepare_admitted(ygpu_server* S, const std::vector<Admit>& got) {
 }
 
 static int run_tick(ygpu_server* S) {
+    YgRange range("ygpu serve tick");
     const ygpu_dyn_par& P = S->cfg.par;
     const int n = (int)S->active.size();
     if (S->active_dirty) {

@@ -4591,6 +4591,7 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
     // d_done: count of finished instances; d_abort: launch-wide abort flag.
     // With a team map (one team per instance) n_teams is the number of control
     // blocks to clear (n_inst) and map_grid the CTAs of the plan.
+    YgRange range("ygpu solve");
     int st;
     if ((st = ygpu_init_constants(device))) return st;
     if (cudaMemsetAsync(d_done, 0, sizeof(int), stream) != cudaSuccess) return YGPU_ERR_CUDA;
@@ -4689,6 +4690,7 @@ int ygpu_launch_solver(int device, cudaStream_t stream, const Inst* d_insts, int
     if (use_graph && gc->valid) {
         // whole chunks as graph replays
         while (it + check <= P.ssa_iter_max) {
+            YgRange chunk("ygpu picard chunk");
             if (cudaGraphLaunch(gc->exec, stream) != cudaSuccess || cudaStreamSynchronize(stream) != cudaSuccess) {
                 ygpu_set_error("solver graph failed: %s", cudaGetErrorString(cudaGetLastError()));
                 return YGPU_ERR_CUDA;
