@@ -456,6 +456,22 @@ int ygpu_calc_advec2D_impl_lis(double* dvdt, const double* var, const double* ux
                                double dx, double dy, double dt, int boundaries, int nx, int ny,
                                int* lin_iter, int* lin_status);
 struct ygpu_ctx;
+/*
+ * ygpu_calc_dyn_inputs_bg and ygpu_set_ssa_masks on DEVICE arrays, enqueued on
+ * ctx's stream without synchronising (same arguments after ctx). A time loop
+ * that keeps every field on the device chains them with
+ * ygpu_advec2D_impl_lis_device and ygpu_solve_device on the same stream.
+ */
+int ygpu_calc_dyn_inputs_bg_device(struct ygpu_ctx* ctx, const double* H_ice, const double* z_bed,
+                                   const double* z_sl, double* f_ice, double* H_grnd, double* z_srf,
+                                   double* f_grnd, double* f_grnd_acx, double* f_grnd_acy, int* mask_frnt,
+                                   double* dzsdx, double* dzsdy, double* taud_acx, double* taud_acy,
+                                   double* taul_int_acx, double* taul_int_acy, double dx, double grad_lim,
+                                   double taud_lim, double rho_ice, double rho_sw, double g,
+                                   double slope_bg_x, double slope_bg_y, int boundaries, int nx, int ny);
+int ygpu_set_ssa_masks_device(struct ygpu_ctx* ctx, int* ssa_mask_acx, int* ssa_mask_acy, const int* mask_frnt,
+                              const double* f_ice, const double* f_grnd, int lateral_bc, int boundaries,
+                              int nx, int ny);
 /* the same on device arrays, on ctx's stream (scratch from its arena); synchronises */
 int ygpu_advec2D_impl_lis_device(struct ygpu_ctx* ctx, double* dvdt, const double* var, const double* ux,
                                  const double* uy, const double* var_dot, const int* mask_ice,

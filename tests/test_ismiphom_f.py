@@ -140,3 +140,19 @@ def test_steady_state_namelist_solver(exp):
     r = prognostic.run(case(exp, "nml"), DT, T_END)
     assert _zs_err(r["z_srf"], g[f"f{exp}_nml_zs"]) < 0.02
     assert _us_err(r["us_aa"], g[f"f{exp}_nml_us"]) < 0.01
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("exp", [1, 2])
+def test_device_resident_loop_matches_oracle(exp, precision):
+    """The same 2000 years with every field on the GPU (run_device: the device entry
+    points on one stream) against the oracle's run."""
+    g = np.load(FIXTURE)
+    inst = case(exp, "tight")
+    inst.par = inst.par.with_(precision=precision)
+    r = prognostic.run_device(inst, DT, T_END)
+    assert r["steps"] == int(T_END / DT)
+    assert _zs_err(r["z_srf"], g[f"f{exp}_tight_zs"]) < 1e-6
+    assert _us_err(r["us_aa"], g[f"f{exp}_tight_us"]) < 1e-6
+    assert r["history"]["dhdt_max"][-1] < 1e-4

@@ -1340,6 +1340,39 @@ extern "C" int ygpu_calc_dyn_inputs_bg(const double* H_ice, const double* z_bed,
     return S.download(c);
 }
 
+extern "C" int ygpu_calc_dyn_inputs_bg_device(ygpu_ctx* c, const double* H_ice, const double* z_bed,
+                                              const double* z_sl, double* f_ice, double* H_grnd, double* z_srf,
+                                              double* f_grnd, double* f_grnd_acx, double* f_grnd_acy, int* mask_frnt,
+                                              double* dzsdx, double* dzsdy, double* taud_acx, double* taud_acy,
+                                              double* taul_int_acx, double* taul_int_acy, double dx, double grad_lim,
+                                              double taud_lim, double rho_ice, double rho_sw, double g,
+                                              double slope_bg_x, double slope_bg_y, int boundaries, int nx, int ny) {
+    if (!c || nx < 3 || ny < 3 || !(dx > 0.0) || boundaries < 0 || boundaries > 6 || !isfinite(slope_bg_x) ||
+        !isfinite(slope_bg_y) ||
+        any_null({H_ice, z_bed, z_sl, f_ice, H_grnd, z_srf, f_grnd, f_grnd_acx, f_grnd_acy, mask_frnt, dzsdx, dzsdy,
+                  taud_acx, taud_acy, taul_int_acx, taul_int_acy})) {
+        ygpu_set_error("bad arguments");
+        return YGPU_ERR_BAD_ARG;
+    }
+    CK(cudaSetDevice(c->device));
+    return ygpu_dyn_inputs_device(c->stream, H_ice, z_bed, z_sl, f_ice, H_grnd, z_srf, f_grnd, f_grnd_acx, f_grnd_acy,
+                                  mask_frnt, dzsdx, dzsdy, taud_acx, taud_acy, taul_int_acx, taul_int_acy, dx,
+                                  grad_lim, taud_lim, rho_ice, rho_sw, g, boundaries, nx, ny, slope_bg_x, slope_bg_y);
+}
+
+extern "C" int ygpu_set_ssa_masks_device(ygpu_ctx* c, int* ssa_mask_acx, int* ssa_mask_acy, const int* mask_frnt,
+                                         const double* f_ice, const double* f_grnd, int lateral_bc, int boundaries,
+                                         int nx, int ny) {
+    if (!c || nx < 2 || ny < 2 || lateral_bc < 0 || lateral_bc > 3 || boundaries < 0 || boundaries > 6 ||
+        any_null({ssa_mask_acx, ssa_mask_acy, mask_frnt, f_ice, f_grnd})) {
+        ygpu_set_error("bad arguments");
+        return YGPU_ERR_BAD_ARG;
+    }
+    CK(cudaSetDevice(c->device));
+    return ygpu_ssa_masks_device(c->stream, ssa_mask_acx, ssa_mask_acy, mask_frnt, f_ice, f_grnd, lateral_bc,
+                                 boundaries, nx, ny);
+}
+
 static int dyn_diag_check(const ygpu_dyn_diag* D, int bc) {
     if (!D || D->nx < 2 || D->ny < 2 || !(D->dx > 0.0) || !(D->dy > 0.0) || bc < 0 || bc > 6) {
         ygpu_set_error("bad arguments");

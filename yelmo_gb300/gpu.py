@@ -38,7 +38,8 @@ EXPORTS = [
     "ygpu_solve_device", "ygpu_solve_batch_device", "ygpu_solve_device_noalloc",
     "ygpu_server_create", "ygpu_server_destroy", "ygpu_server_add_member", "ygpu_server_submit",
     "ygpu_server_poll", "ygpu_server_wait", "ygpu_server_fetch", "ygpu_server_get_info",
-    "ygpu_server_member_steps", "ygpu_server_set_member_steps", "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get", "ygpu_tuning_defaults",
+    "ygpu_server_member_steps", "ygpu_server_set_member_steps", "ygpu_calc_dyn_inputs_bg_device",
+    "ygpu_set_ssa_masks_device", "ygpu_kernel_launches", "ygpu_step_timing", "ygpu_step_timing_get", "ygpu_tuning_defaults",
     "ygpu_ctx_set_tuning", "ygpu_set_neff_hook", "ygpu_solve_batch_host", "ygpu_calc_dyn_diagnostics",
     "ygpu_calc_dyn_diagnostics_device", "ygpu_calc_advec2D_impl_lis", "ygpu_advec2D_impl_lis_device",
     "ygpu_calc_gradient_column_ac", "ygpu_calc_gradient_column_ac_device", "ygpu_calc_jacobian_vel_3D",
@@ -110,6 +111,9 @@ def lib(build_if_missing: bool = True):
     L.ygpu_server_wait.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(abi.Stats), dp]
     L.ygpu_server_fetch.argtypes = [C.c_void_p, C.c_int, C.c_int, dp]
     L.ygpu_server_get_info.argtypes = [C.c_void_p, C.POINTER(abi.ServerInfo)]
+    L.ygpu_calc_dyn_inputs_bg_device.argtypes = [C.c_void_p] + [C.c_void_p] * 16 + [C.c_double] * 8 + \
+        [C.c_int] * 3
+    L.ygpu_set_ssa_masks_device.argtypes = [C.c_void_p] * 6 + [C.c_int] * 4
     L.ygpu_server_member_steps.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_ulonglong)]
     L.ygpu_server_set_member_steps.argtypes = [C.c_void_p, C.c_int, C.c_ulonglong]
     L.ygpu_kernel_launches.restype = C.c_ulonglong

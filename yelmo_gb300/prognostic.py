@@ -26,7 +26,10 @@ choice shows.
 
 The calls go through a backend: the GPU library by default (``GpuBackend``).
 Any object with the same four methods can stand in for it (a test passes the
-oracle's functions to compare the two loops step by step).
+oracle's functions to compare the two loops step by step). ``run_device`` is the
+same loop with every field resident on the GPU: the device entry points of the
+library on one context stream, and the thickness update as a torch operation
+on that stream; only max |dH/dt| and the statuses come back to the host.
 """
 from __future__ import annotations
 
@@ -120,3 +123,80 @@ def run(inst, dt: float, t_end: float, backend=None, dhdt_tol: float = 0.0, on_s
             "ux_bar": f["ux_bar"].copy(order="F"), "uy_bar": f["uy_bar"].copy(order="F"),
             "ux_s": ux_s, "uy_s": uy_s, "us_aa": surface_speed_aa(ux_s, uy_s), "fields": f,
             "history": {kk: np.asarray(v) for kk, v in hist.items()}}
+
+
+def run_device(inst, dt: float, t_end: float, device: int = 0, dhdt_tol: float = 0.0) -> dict:
+    """``run`` with the fields on the GPU (device tensors, no host staging per step):
+    ygpu_advec2D_impl_lis_device, the thickness update, ygpu_calc_dyn_inputs_bg_device,
+    ygpu_set_ssa_masks_device and ygpu_solve_device on one context's stream. Returns
+    what ``run`` returns, without the solve's field dict ("fields")."""
+    import ctypes as C
+
+    import torch
+
+    from . import abi
+    p = inst.par
+    nx, ny, nz = inst.nx, inst.ny, inst.nz
+    dev_name = f"cuda:{device}"
+    st = dataclasses.replace(inst, H_ice=np.array(inst.H_ice, dtype=np.float64, order="F", copy=True))
+    d = gpu.to_device(gpu.prepare(st), dev_name)
+    z2 = lambda: torch.zeros(nx * ny, dtype=torch.float64, device=dev_name)
+    dzsdx, dzsdy, dvdt, smb = z2(), z2(), z2(), z2()
+    mask_ice = torch.full((nx * ny,), 2, dtype=torch.int32, device=dev_name)       # MASK_ICE_DYNAMIC
+    solver = gpu.DeviceSolver(device)
+    L = solver.L
+    ptr = lambda k: C.c_void_p(d[k].data_ptr())
+    try:
+        stream = torch.cuda.ExternalStream(L.ygpu_ctx_stream(solver.ctx), device=dev_name)
+        fields = gpu.make_fields(d, nx, ny, nz, st.dx, st.dx, st.n_glen)
+        bc = abi.BOUNDARY_CODES[p.boundaries]
+        latbc = abi.LATBC_CODES[p.ssa_lat_bc]
+        sbx, sby = (float(v) for v in st.slope_bg)
+        torch.cuda.synchronize(dev_name)
+        solver.solve(p.kind, p, fields)
+        n_steps = int(np.ceil(t_end / dt - 1e-9))
+        hist = {"dhdt_max": [], "picard": [], "adv_iter": []}
+        it, ls = C.c_int(0), C.c_int(0)
+        t, k = 0.0, 0
+        for k in range(1, n_steps + 1):
+            gpu._check(L.ygpu_advec2D_impl_lis_device(
+                solver.ctx, C.c_void_p(dvdt.data_ptr()), ptr("H_ice"), ptr("ux_bar"), ptr("uy_bar"),
+                C.c_void_p(smb.data_ptr()), C.c_void_p(mask_ice.data_ptr()), ptr("H_ice"), st.dx, st.dx, dt,
+                abi.ADV_BOUNDARY_CODES[p.boundaries], nx, ny, C.byref(it), C.byref(ls)))
+            if ls.value != 0:
+                raise RuntimeError(f"advection linear solve failed at step {k} (status {ls.value})")
+            with torch.cuda.stream(stream):
+                d["H_ice"].add_(dvdt, alpha=dt)
+                m = dvdt.abs().max()
+            gpu._check(L.ygpu_calc_dyn_inputs_bg_device(
+                solver.ctx, ptr("H_ice"), ptr("z_bed"), ptr("z_sl"), ptr("f_ice"), ptr("H_grnd"), ptr("z_srf"),
+                ptr("f_grnd"), ptr("f_grnd_acx"), ptr("f_grnd_acy"), ptr("mask_frnt"),
+                C.c_void_p(dzsdx.data_ptr()), C.c_void_p(dzsdy.data_ptr()), ptr("taud_acx"), ptr("taud_acy"),
+                ptr("taul_int_acx"), ptr("taul_int_acy"), st.dx, p.grad_lim, p.taud_lim, p.rho_ice, p.rho_sw,
+                p.g, sbx, sby, bc, nx, ny))
+            gpu._check(L.ygpu_set_ssa_masks_device(solver.ctx, ptr("ssa_mask_acx"), ptr("ssa_mask_acy"),
+                                                   ptr("mask_frnt"), ptr("f_ice"), ptr("f_grnd"), latbc, bc,
+                                                   nx, ny))
+            out = solver.solve(p.kind, p, fields)
+            if out["status"] != 0:
+                raise RuntimeError(f"velocity solve failed at step {k} (status {out['status']})")
+            t = k * dt
+            mv = float(m.item())
+            hist["dhdt_max"].append(mv)
+            hist["picard"].append(out["ssa_iter_now"])
+            hist["adv_iter"].append(it.value)
+            if not np.isfinite(mv):
+                raise RuntimeError(f"thickness diverged at step {k} (t = {t} a): reduce dt")
+            if dhdt_tol > 0.0 and mv < dhdt_tol:
+                break
+        torch.cuda.synchronize(dev_name)
+        host = lambda key, shape: d[key].cpu().numpy().reshape(shape, order="F")
+        ux = host("ux", (nx, ny, nz))
+        uy = host("uy", (nx, ny, nz))
+        ux_s, uy_s = np.asfortranarray(ux[:, :, -1]), np.asfortranarray(uy[:, :, -1])
+        return {"t": t, "steps": k, "H_ice": host("H_ice", (nx, ny)), "z_srf": host("z_srf", (nx, ny)),
+                "ux_bar": host("ux_bar", (nx, ny)), "uy_bar": host("uy_bar", (nx, ny)), "ux_s": ux_s,
+                "uy_s": uy_s, "us_aa": surface_speed_aa(ux_s, uy_s),
+                "history": {kk: np.asarray(v) for kk, v in hist.items()}}
+    finally:
+        solver.close()
