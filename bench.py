@@ -364,8 +364,8 @@ def ismiphom_leg(years: float = 200.0) -> dict:
     `years` 1-year steps of the thickness time loop (yelmo_gb300.prognostic) through
     the host drop-in calls on the GPU, the same loop with the fields resident on the
     GPU (run_device), and the same steps on the oracle as its CPU
-    baseline and checker (4 threads: on 1600 cells more threads only add OpenMP
-    overhead): wall time per step and the largest z_srf difference after the last
+    baseline and the values the GPU is compared with (4 threads: on 1600 cells more
+    threads only add OpenMP overhead): wall time per step and the largest z_srf difference after the last
     step, relative to the surface relief."""
     import oracle
     from tests.golden.make_ismiphom_f_golden import OracleBackend, case

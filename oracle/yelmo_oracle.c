@@ -1842,7 +1842,7 @@ int orc_calc_dyn_inputs_bg(const double* H_ice, const double* z_bed, const doubl
                         mf[nb[q]] = (z_bed[nb[q]] < z_sl[nb[q]]) ? MASK_FRNT_ICE_FREE : MASK_FRNT_ICE_FREE_LAND;
             }
         }
-    /* calc_gradient_acx/acy (zero_outside = .FALSE., no background slope) */
+    /* calc_gradient_acx/acy (zero_outside = .FALSE.; the background slope is added below) */
     for (int j = 0; j < ny; j++)
         for (int i = 0; i < nx; i++) {
             int im1, ip1, jm1, jp1;
