@@ -106,3 +106,28 @@ def test_method_run_is_reported(solver, opt, want):
     s, pc = C.c_int(-1), C.c_int(-1)
     L.ygpu_lin_method_run(C.byref(p), C.byref(s), C.byref(pc))
     assert (s.value, pc.value) == want
+
+
+def test_new_entries_refuse_bad_arguments_before_any_device_call():
+    """Argument checks of the background-slope prologue, its device form, the
+    device masks and the member step count run on the host and refuse without
+    touching CUDA."""
+    import numpy as np
+    L = gpu.lib()
+    n = 8
+    arrs = [np.zeros((n, n), order="F") for _ in range(16)]
+    arrs[9] = np.zeros((n, n), dtype=np.int32, order="F")          # mask_frnt
+    ptrs = [a.ctypes.data_as(C.POINTER(C.c_int if a.dtype == np.int32 else C.c_double)) for a in arrs]
+    # a non-finite slope
+    assert L.ygpu_calc_dyn_inputs_bg(*ptrs, 1e3, 0.5, 2e5, 910.0, 1028.0, 9.81, float("nan"), 0.0,
+                                     0, n, n) == abi.ERR_BAD_ARG
+    # a grid below 3 x 3
+    assert L.ygpu_calc_dyn_inputs_bg(*ptrs, 1e3, 0.5, 2e5, 910.0, 1028.0, 9.81, 0.0, 0.0, 0, 2, n) == abi.ERR_BAD_ARG
+    vp = [C.c_void_p(a.ctypes.data) for a in arrs]
+    # the device forms need a context
+    assert L.ygpu_calc_dyn_inputs_bg_device(None, *vp, 1e3, 0.5, 2e5, 910.0, 1028.0, 9.81, 0.0, 0.0,
+                                            0, n, n) == abi.ERR_BAD_ARG
+    assert L.ygpu_set_ssa_masks_device(None, vp[0], vp[1], vp[9], vp[2], vp[3], 2, 0, n, n) == abi.ERR_BAD_ARG
+    steps = C.c_ulonglong(0)
+    assert L.ygpu_server_member_steps(None, 0, C.byref(steps)) == abi.ERR_BAD_ARG
+    assert L.ygpu_server_set_member_steps(None, 0, 3) == abi.ERR_BAD_ARG
