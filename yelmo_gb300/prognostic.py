@@ -125,11 +125,13 @@ def run(inst, dt: float, t_end: float, backend=None, dhdt_tol: float = 0.0, on_s
             "history": {kk: np.asarray(v) for kk, v in hist.items()}}
 
 
-def run_device(inst, dt: float, t_end: float, device: int = 0, dhdt_tol: float = 0.0) -> dict:
+def run_device(inst, dt: float, t_end: float, device: int = 0, dhdt_tol: float = 0.0,
+               tuning: dict | None = None) -> dict:
     """``run`` with the fields on the GPU (device tensors, no host staging per step):
     ygpu_advec2D_impl_lis_device, the thickness update, ygpu_calc_dyn_inputs_bg_device,
     ygpu_set_ssa_masks_device and ygpu_solve_device on one context's stream. Returns
-    what ``run`` returns, without the solve's field dict ("fields")."""
+    what ``run`` returns, without the solve's field dict ("fields"). tuning: keyword
+    arguments of DeviceSolver.set_tuning for the context (None: its defaults)."""
     import ctypes as C
 
     import torch
@@ -144,6 +146,8 @@ def run_device(inst, dt: float, t_end: float, device: int = 0, dhdt_tol: float =
     dzsdx, dzsdy, dvdt, smb = z2(), z2(), z2(), z2()
     mask_ice = torch.full((nx * ny,), 2, dtype=torch.int32, device=dev_name)       # MASK_ICE_DYNAMIC
     solver = gpu.DeviceSolver(device)
+    if tuning:
+        solver.set_tuning(**tuning)
     L = solver.L
     ptr = lambda k: C.c_void_p(d[k].data_ptr())
     try:
