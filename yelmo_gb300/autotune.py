@@ -26,7 +26,7 @@ DEFAULT_GRID = {
 }
 
 
-DEFAULT_INNER_TOLS = (5e-4, 1e-3, 2e-3)
+DEFAULT_INNER_TOLS = (5e-4, 1e-3, 2e-3, 4e-3)
 
 
 def autotune(solver, kind: int, par, fields: list, reset, iters: int = 8, grid: dict | None = None,
