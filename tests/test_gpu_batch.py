@@ -122,7 +122,7 @@ def test_autotune_picks_launch_shape_and_inner_tolerance():
     precision it picks the inner tolerance from its candidates, and a solve with that
     choice still meets the parity bar against the FP64 solve."""
     torch = pytest.importorskip("torch")
-    from yelmo_gb300.autotune import autotune
+    from yelmo_gb300.autotune import DEFAULT_INNER_TOLS, autotune
     insts = _instances(4)
     devs, fields = zip(*[_device(inst) for inst in insts])
     pristine = [{k: d[k].clone() for k in gpu.STATE_NAMES} for d in devs]
@@ -142,8 +142,8 @@ def test_autotune_picks_launch_shape_and_inner_tolerance():
         grid = {"unknowns_per_cta": (512, 1024), "check_every": (4,), "use_graphs": (True,)}
         out = autotune(solver, abi.KIND_SSA, par, list(fields), reset, iters=4, grid=grid)
         assert out["tuning"]["unknowns_per_cta"] in (512, 1024)
-        assert out["inner_tol"] in (5e-4, 1e-3, 2e-3)
-        assert set(out["inner_tol_ms"]) == {"0.0005", "0.001", "0.002"}
+        assert out["inner_tol"] in DEFAULT_INNER_TOLS
+        assert set(out["inner_tol_ms"]) == {f"{t:g}" for t in DEFAULT_INNER_TOLS}
         for d, p in zip(devs, pristine):          # left reset
             assert torch.equal(d["ux_b"], p["ux_b"])
         sts = solver.solve_batch(abi.KIND_SSA, par.with_(inner_tol=out["inner_tol"]), list(fields))
